@@ -1,0 +1,90 @@
+"""Extract the reference's golden values for the two-site path into a fixture.
+
+Reads the reference test sources as text (nothing is compiled or run) and
+writes ``reference_goldens.json`` next to this script:
+
+* golden ground-state energies and tolerances of the two-site VMPS tests
+  (``tests/test_algorithm/test_two_site_update_finite_vmps.cc``) and the
+  FiniteDMRG tests (``tests/test_algorithm/test_finite_dmrg.cc``) for the models
+  the oracle builds (Ising, Heisenberg 1D/2D, Hubbard 2x2);
+* the MATLAB known answers of ``TridiagExpme1Solver``
+  (``tests/test_algorithm/test_lanczos_expmv_solver.cc:70-109``);
+* the TDVP free-fermion ground-state energy
+  (``tests/test_algorithm/test_two_site_finite_tdvp.cc``).
+
+Usage: python tests/golden/extract_reference_goldens.py [reference_root]
+"""
+import json
+import os
+import re
+import sys
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def read(rel):
+    with open(os.path.join(REF, rel)) as f:
+        return f.read()
+
+
+def case_energies(src, case):
+    """Energies passed to RunTest*Case inside TEST_F(..., case)."""
+    m = re.search(r"TEST_F\(\s*\w+\s*,\s*%s\s*\)(.*?)(?=\nTEST_F|\Z)" % case, src, re.S)
+    body = m.group(1)
+    out = []
+    for mm in re.finditer(r"RunTest\w*Case\((.*?)\);", body, re.S):
+        args = [a.strip() for a in mm.group(1).split(",")]
+        out.append((args[-2], args[-1]))
+    return out
+
+
+def num(s):
+    s = s.replace(" ", "")
+    if s == "-0.25*(N-1)":
+        return -0.25 * 5
+    return float(s)
+
+
+def main():
+    vmps = read("tests/test_algorithm/test_two_site_update_finite_vmps.cc")
+    dmrg = read("tests/test_algorithm/test_finite_dmrg.cc")
+    expmv = read("tests/test_algorithm/test_lanczos_expmv_solver.cc")
+    tdvp = read("tests/test_algorithm/test_two_site_finite_tdvp.cc")
+    goldens = {"source": "text of the reference test files (see script)", "vmps": {}, "dmrg": {}}
+    for case in ("1DIsing", "1DHeisenberg", "2DHeisenberg"):
+        e = case_energies(vmps, case)
+        goldens["vmps"][case] = {"energy": num(e[0][0]), "tol": float(e[0][1])}
+    e = case_energies(vmps, "2Dcase")
+    goldens["vmps"]["Hubbard2x2"] = {"energy": num(e[0][0]), "tol": float(e[0][1])}
+    for case in ("1DIsing", "1DHeisenberg", "2DHeisenberg"):
+        try:
+            e = case_energies(dmrg, case)
+            goldens["dmrg"][case] = {"energy": num(e[0][0]), "tol": float(e[0][1])}
+        except Exception:  # noqa: BLE001 - case absent in this file
+            pass
+    # TridiagExpme1Solver known answers
+    cplx = re.compile(r"QLTEN_Complex\(\s*([-0-9.eE]+)\s*,\s*([-0-9.eE]+)\s*\)")
+    m1 = re.search(r"matrix2x2_example1\s*=\s*SymmetricTriDiagonalMatrix\(2,\s*\{([^}]*)\},\s*\{([^}]*)\}\)", expmv)
+    d1 = re.search(r"delta1\s*=\s*([-0-9.]+)", expmv)
+    r1 = re.search(r"res_example1\[2\]\s*=\s*\{(.*?)\};", expmv, re.S)
+    m2 = re.search(r"matrix5x5_example2\s*=\s*SymmetricTriDiagonalMatrix\(\s*5,\s*\{([^}]*)\},\s*\{([^}]*)\}\)", expmv, re.S)
+    d2 = re.search(r"delta2\s*=\s*([-0-9.]+)", expmv)
+    r2 = re.search(r"res_example2\[5\]\s*\{(.*?)\};", expmv, re.S)
+    fl = lambda s: [float(x) for x in s.split(",")]
+    goldens["expme1"] = [
+        {"a": fl(m1.group(1)), "b": fl(m1.group(2)), "delta": float(d1.group(1)),
+         "res": [[float(x), float(y)] for x, y in cplx.findall(r1.group(1))]},
+        {"a": fl(m2.group(1)), "b": fl(m2.group(2)), "delta": float(d2.group(1)),
+         "res": [[float(x), float(y)] for x, y in cplx.findall(r2.group(1))]},
+    ]
+    gs = re.search(r"(-3\.49395920743493\d*)", tdvp)
+    if gs:
+        goldens["tdvp_free_fermion_gs"] = float(gs.group(1))
+    with open(os.path.join(HERE, "reference_goldens.json"), "w") as f:
+        json.dump(goldens, f, indent=1)
+    print(json.dumps(goldens, indent=1))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,143 @@
+"""Pin the CPU oracle against the reference's own golden values.
+
+Golden numbers come from ``tests/golden/reference_goldens.json`` (extracted
+from the reference test sources by ``tests/golden/extract_reference_goldens.py``).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import blocksparse as bs
+from oracle import krylov, vmps
+from ultradmrg_gb300 import models as M
+from ultradmrg_gb300.tensor_data import IN, OUT, BlockTensorData, Index
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                   "reference_goldens.json")))
+
+
+def _run(mpo, pb, labels, params):
+    mps = M.direct_product_mps([pb] * len(labels), labels)
+    return vmps.two_site_finite_vmps(mps, mpo, params)
+
+
+def test_vmps_ising_golden():
+    g = GOLD["vmps"]["1DIsing"]
+    mpo, pb = M.ising_chain_mpo(6)
+    e = _run(mpo, pb, [i % 2 for i in range(6)],
+             vmps.FiniteVMPSSweepParams(4, 1, 10, 1e-5, krylov.LanczosParams(1e-7)))
+    assert abs(e - g["energy"]) < g["tol"]
+
+
+def test_vmps_heisenberg_golden():
+    g = GOLD["vmps"]["1DHeisenberg"]
+    mpo, pb = M.heisenberg_chain_mpo(6)
+    e = _run(mpo, pb, [i % 2 for i in range(6)],
+             vmps.FiniteVMPSSweepParams(4, 8, 8, 1e-9, krylov.LanczosParams(1e-7)))
+    assert abs(e - g["energy"]) < g["tol"]
+
+
+def test_vmps_heisenberg2d_golden():
+    g = GOLD["vmps"]["2DHeisenberg"]
+    pairs = [(0, 1), (0, 2), (1, 3), (2, 3), (2, 4), (3, 5), (4, 5)]
+    mpo, pb = M.heisenberg_chain_mpo(6, pairs=pairs)
+    e = _run(mpo, pb, [i % 2 for i in range(6)],
+             vmps.FiniteVMPSSweepParams(4, 8, 8, 1e-9, krylov.LanczosParams(1e-7)))
+    assert abs(e - g["energy"]) < g["tol"]
+
+
+def test_vmps_hubbard2x2_golden():
+    g = GOLD["vmps"]["Hubbard2x2"]
+    mpo, pb = M.hubbard_2x2_test_mpo()
+    e = _run(mpo, pb, [1 if i % 2 == 0 else 2 for i in range(4)],
+             vmps.FiniteVMPSSweepParams(10, 16, 16, 1e-9, krylov.LanczosParams(1e-8, 20)))
+    assert abs(e - g["energy"]) < g["tol"]
+
+
+@pytest.mark.parametrize("case", [0, 1])
+def test_tridiag_expme1_known_answers(case):
+    c = GOLD["expme1"][case]
+    n = len(c["a"])
+    res = krylov.tridiag_expme1_solver(c["a"], c["b"], n, c["delta"])
+    ref = np.array([complex(x, y) for x, y in c["res"]])
+    assert krylov.distance(res, ref) < 1e-13
+
+
+def _random_single_sector_eff_ham(D=20, d=2, dh=2, seed=0, dtype=np.float64):
+    """Random Hermitian L, W, R on one-sector indexes, the layout of
+    ``tests/test_algorithm/test_lanczos_solver.cc:114-150``."""
+    rng = np.random.default_rng(seed)
+    q0 = (0,)
+    iD = lambda dr: Index.make([(q0, D)], dr)
+    id_ = lambda dr: Index.make([(q0, d)], dr)
+    iv = lambda dr: Index.make([(q0, dh)], dr)
+
+    def sym(n):
+        a = rng.random((n, n))
+        if dtype == np.complex128:
+            a = a + 1j * rng.random((n, n))
+        return a + a.conj().T
+
+    blk = sym(D)
+    L = BlockTensorData([iD(IN), iv(OUT), iD(OUT)], {}, dtype)
+    R = BlockTensorData([iD(OUT), iv(IN), iD(IN)], {}, dtype)
+    Lb = np.zeros((D, dh, D), dtype)
+    Rb = np.zeros((D, dh, D), dtype)
+    for k in range(dh):
+        Lb[:, k, :] = blk
+        Rb[:, k, :] = blk.T
+    L.blocks[(0, 0, 0)] = Lb
+    R.blocks[(0, 0, 0)] = Rb
+    site = sym(d)
+    Wb = np.zeros((dh, d, d, dh), dtype)
+    for k in range(dh):
+        Wb[k, :, :, k] = site
+    W = BlockTensorData([iv(IN), id_(IN), id_(OUT), iv(OUT)], {(0, 0, 0, 0): Wb}, dtype)
+    psi = BlockTensorData([iD(IN), id_(OUT), id_(OUT), iD(OUT)],
+                          {(0, 0, 0, 0): rng.standard_normal((D, d, d, D)).astype(dtype)},
+                          dtype)
+    return [L, W, W.copy(), R], psi
+
+
+def dense_eff_ham(eff_ham):
+    """Dense matrix of H_eff (rows: output (a,s1,s2,b), cols: input)."""
+    L, W1, W2, R = [t.to_dense() for t in eff_ham]
+    H = np.einsum('xwa,wsty,yuvz,bzc->xtvbasuc', L, W1, W2, R)
+    n = H.shape[0] * H.shape[1] * H.shape[2] * H.shape[3]
+    return H.reshape(n, n)
+
+
+@pytest.mark.parametrize("dtype,params", [(np.float64, (1e-9, 200)),
+                                          (np.float64, (1e-16, 20)),
+                                          (np.complex128, (1e-9, 200))])
+def test_lanczos_vs_dense_ed(dtype, params):
+    """Cases of ``tests/test_algorithm/test_lanczos_solver.cc:145-207``: tolerance
+    stop and max-iteration stop (real), tolerance stop (complex)."""
+    eff_ham, psi = _random_single_sector_eff_ham(dtype=dtype)
+    H = dense_eff_ham(eff_ham)
+    assert np.allclose(H, H.conj().T)
+    w = np.linalg.eigvalsh(H)
+    res = krylov.lanczos_solver(eff_ham, psi, krylov.eff_ham_mul_two_site_state,
+                                krylov.LanczosParams(*params))
+    assert abs(res.gs_eng - w[0]) < 1e-8
+
+
+def test_matvec_matches_dense():
+    eff_ham, psi = _random_single_sector_eff_ham(D=6, seed=3)
+    H = dense_eff_ham(eff_ham)
+    out = krylov.eff_ham_mul_two_site_state(eff_ham, psi)
+    ref = H @ psi.to_dense().ravel()
+    assert np.allclose(out.to_dense().ravel(), ref, atol=1e-12)
+
+
+def test_svd_truncation_rule():
+    sv = [np.array([0.9, 0.3, 0.1]), np.array([0.3, 0.05])]
+    kept, D, err = bs.select_kept(sv, 1e-2, 1, 10)
+    # weights .81 .09 .09 .01 .0025 ; keep until discarded <= 1e-2 of total
+    tot = 0.81 + 0.09 + 0.09 + 0.01 + 0.0025
+    assert D == 4 and kept == [3, 1]
+    assert abs(err - 0.0025 / tot) < 1e-15
+    kept, D, _ = bs.select_kept(sv, 1e-2, 1, 2)
+    assert D == 2 and kept == [2, 0]  # tie 0.3/0.3 broken by sector order

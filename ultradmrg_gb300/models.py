@@ -1,0 +1,489 @@
+"""Host-side model builders: local Hilbert spaces, operators, MPOs, product MPS.
+
+These make the inputs of the two-site update (MPO tensors and initial MPS);
+they run once per job on the host and are not part of the GPU hot path.
+
+MPO construction is a finite-state machine over "channels" of each virtual
+bond, with prefix sharing: terms that have applied the same operators on the
+same sites so far (and carry the same pending string operator) share one
+channel.  Channel 0 of every bulk bond is "nothing applied yet" and the last
+channel of a bond is "term completed".  The resulting tensors follow the
+reference's MPO conventions:
+
+* ``W(lvb IN, pb_in IN, pb_out OUT, rvb OUT)`` and an operator ``O`` given
+  as ``O[in, out]`` is written to ``W[l, in, out, r]``
+  (``one_dim_tn/mpo/mpogen/mpogen_impl.h:445-545``);
+* a right-bond channel carries ``qn(lvb channel) - Div(O)``
+  (``mpogen_impl.h:373-381``) so every MPO tensor is divergence free;
+* terms with a zero coefficient are skipped (``mpogen_impl.h:92-101``);
+* ``AddTerm(coef, op1, s1, op2, s2, inst)`` puts ``inst`` on every site strictly
+  between ``s1`` and ``s2`` (Jordan-Wigner strings,
+  ``benchmark/ultradmrg_hubbard2d.cpp:149-181``).
+
+The generator in the reference additionally compresses the channel graph; this
+one does prefix sharing only, so its bond dimension can differ from the
+reference's for the same Hamiltonian (the operator it represents is the same).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from .tensor_data import IN, OUT, BlockTensorData, Index, qn_sub
+
+# ---------------------------------------------------------------------------
+# Local Hilbert spaces and operators.  Operators are dense d x d matrices
+# indexed [in, out], i.e. O[i, o] = <o|O|i>, the element layout of
+# QLTensor({pb_in, pb_out}) in the reference tests.
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class Operator:
+    name: str
+    mat: np.ndarray  # [in, out]
+
+    def __mul__(self, s):
+        return Operator(f"{s}*{self.name}", self.mat * s)
+
+    __rmul__ = __mul__
+
+
+def _op(name, d, entries, dtype=np.float64):
+    m = np.zeros((d, d), dtype=dtype)
+    for (i, o), v in entries.items():
+        m[i, o] = v
+    return Operator(name, m)
+
+
+def spin_half_site(dtype=np.float64):
+    """S=1/2 with U(1) Sz in units of 1/2: basis [up (+1), down (-1)].
+
+    Operator tables follow ``tests/test_algorithm/test_two_site_update_finite_vmps.cc:64-110``
+    (``sp`` sets element {0,1}, ``sm`` element {1,0}).
+    """
+    pb_out = Index.make([((1,), 1), ((-1,), 1)], OUT)
+    ops = {
+        "id": _op("id", 2, {(0, 0): 1, (1, 1): 1}, dtype),
+        "sz": _op("sz", 2, {(0, 0): 0.5, (1, 1): -0.5}, dtype),
+        "sp": _op("sp", 2, {(0, 1): 1}, dtype),
+        "sm": _op("sm", 2, {(1, 0): 1}, dtype),
+    }
+    return pb_out, ops
+
+
+def hubbard_site_nsz(dtype=np.float64):
+    """Hubbard site with U(1)xU(1) (N, Sz): basis [(2,0), (1,1), (1,-1), (0,0)].
+
+    Operator tables (hard-core bosons times the on-site parity F) are those of
+    ``benchmark/ultradmrg_hubbard2d.cpp:17-121``.
+    """
+    pb_out = Index.make([((2, 0), 1), ((1, 1), 1), ((1, -1), 1), ((0, 0), 1)], OUT)
+    e = lambda name, t: _op(name, 4, t, dtype)
+    ops = {
+        "id": e("id", {(0, 0): 1, (1, 1): 1, (2, 2): 1, (3, 3): 1}),
+        "f": e("f", {(0, 0): 1, (1, 1): -1, (2, 2): -1, (3, 3): 1}),
+        "sz": e("sz", {(1, 1): 0.5, (2, 2): -0.5}),
+        "sp": e("sp", {(1, 2): 1.0}),
+        "sm": e("sm", {(2, 1): 1.0}),
+        "bupc": e("bupc", {(0, 2): 1, (1, 3): 1}),
+        "bdnc": e("bdnc", {(0, 1): 1, (2, 3): 1}),
+        "bupa": e("bupa", {(2, 0): 1, (3, 1): 1}),
+        "bdna": e("bdna", {(1, 0): 1, (3, 2): 1}),
+        "bupcF": e("bupcF", {(0, 2): -1, (1, 3): 1}),
+        "Fbdnc": e("Fbdnc", {(0, 1): 1, (2, 3): -1}),
+        "bupaF": e("bupaF", {(2, 0): 1, (3, 1): -1}),
+        "Fbdna": e("Fbdna", {(1, 0): -1, (3, 2): 1}),
+        "Uterm": e("Uterm", {(0, 0): 1}),
+        "nf": e("nf", {(0, 0): 2, (1, 1): 1, (2, 2): 1}),
+    }
+    return pb_out, ops
+
+
+def hubbard_site_nupndn(dtype=np.float64):
+    """Hubbard site with U(1)xU(1) (Nup, Ndn): basis [(0,0), (1,0), (0,1), (1,1)].
+
+    Operator tables of ``tests/test_algorithm/test_two_site_update_finite_vmps.cc:759-843``.
+    """
+    pb_out = Index.make([((0, 0), 1), ((1, 0), 1), ((0, 1), 1), ((1, 1), 1)], OUT)
+    e = lambda name, t: _op(name, 4, t, dtype)
+    ops = {
+        "id": e("id", {(0, 0): 1, (1, 1): 1, (2, 2): 1, (3, 3): 1}),
+        "f": e("f", {(0, 0): 1, (1, 1): -1, (2, 2): -1, (3, 3): 1}),
+        "nupdn": e("nupdn", {(3, 3): 1}),
+        "adagupf": e("adagupf", {(1, 0): 1, (3, 2): -1}),
+        "aup": e("aup", {(0, 1): 1, (2, 3): 1}),
+        "adagdn": e("adagdn", {(2, 0): 1, (3, 1): 1}),
+        "fadn": e("fadn", {(0, 2): 1, (1, 3): -1}),
+        "naupf": e("naupf", {(0, 1): 1, (2, 3): -1}),
+        "adagup": e("adagup", {(1, 0): 1, (3, 2): 1}),
+        "nadn": e("nadn", {(0, 2): -1, (1, 3): -1}),
+        "fadagdn": e("fadagdn", {(2, 0): -1, (3, 1): 1}),
+    }
+    return pb_out, ops
+
+
+def op_div(op: Operator, pb_out: Index):
+    """Div of an operator tensor {pb_in, pb_out}: qn(out) - qn(in)."""
+    nz = np.argwhere(op.mat != 0)
+    if len(nz) == 0:
+        return None
+    divs = set()
+    for i, o in nz:
+        si, _ = pb_out.sector_of(int(i))
+        so, _ = pb_out.sector_of(int(o))
+        divs.add(qn_sub(pb_out.qns[so], pb_out.qns[si]))
+    if len(divs) != 1:
+        raise ValueError(f"operator {op.name} does not conserve the quantum numbers")
+    return divs.pop()
+
+
+# ---------------------------------------------------------------------------
+# MPO generator
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class _Term:
+    coef: float
+    sites: List[int]
+    ops: List[Operator]
+    insts: List[Optional[Operator]]  # string operator after ops[k] (len = len(ops)-1)
+
+
+class MPOGenerator:
+    """Sum-of-products Hamiltonian -> MPO tensors (host side).
+
+    Mirrors the ``AddTerm`` surface of ``one_dim_tn/mpo/mpogen/mpogen.h:38-127``.
+    """
+
+    def __init__(self, sites: Sequence[Index], ops_id: Sequence[Operator], dtype=np.float64):
+        self.sites = list(sites)
+        self.N = len(self.sites)
+        self.ids = list(ops_id)
+        self.dtype = dtype
+        self.terms: List[_Term] = []
+        self.zero = tuple(0 for _ in range(self.sites[0].nq))
+
+    def add_term(self, coef, ops: Sequence[Operator], sites: Sequence[int],
+                 insts: Optional[Sequence[Optional[Operator]]] = None):
+        if coef == 0:
+            return
+        order = np.argsort(sites, kind="stable")
+        sites = [int(sites[i]) for i in order]
+        ops = [ops[i] for i in order]
+        if len(set(sites)) != len(sites):
+            raise ValueError("one operator per site per term")
+        if insts is None:
+            insts = [None] * (len(ops) - 1)
+        elif not isinstance(insts, (list, tuple)):
+            insts = [insts] * (len(ops) - 1)
+        self.terms.append(_Term(coef, sites, list(ops), list(insts)))
+
+    def add_two_site(self, coef, op1, s1, op2, s2, inst=None):
+        """``AddTerm(coef, op1, s1, op2, s2, inst)`` of the reference."""
+        if s1 > s2:
+            raise ValueError("s1 must precede s2")
+        self.add_term(coef, [op1, op2], [s1, s2], [inst])
+
+    def gen(self) -> List[BlockTensorData]:
+        N = self.N
+        # channel keys per bond b (between site b and b+1): key -> channel id
+        # key = ("ready",) | ("done",) | (prefix, inst_name)
+        bond_keys: List[Dict] = [dict() for _ in range(N - 1)]
+        bond_qn: List[List] = [[] for _ in range(N - 1)]
+
+        def key_of(term: _Term, b: int):
+            k = max(i for i, s in enumerate(term.sites) if s <= b)
+            prefix = tuple((term.sites[i], term.ops[i].name) for i in range(k + 1))
+            gap_empty = term.sites[k + 1] == b + 1
+            inst = term.insts[k]
+            return prefix, (None if inst is None else inst.name), gap_empty, k
+
+        def qn_after(term: _Term, k: int):
+            q = self.zero
+            for i in range(k + 1):
+                q = qn_sub(q, op_div(term.ops[i], self.sites[term.sites[i]]))
+            return q
+
+        for b in range(N - 1):
+            bond_keys[b][("ready",)] = 0
+            bond_qn[b].append(self.zero)
+        # pass 1: channels of terms whose pending gap is non-empty; pass 2 reuses
+        # a channel with the same prefix for terms whose next operator is adjacent
+        for pass_no in (1, 2):
+            for term in self.terms:
+                if len(term.sites) < 2:
+                    continue
+                for b in range(term.sites[0], term.sites[-1]):
+                    prefix, inst, gap_empty, k = key_of(term, b)
+                    if gap_empty != (pass_no == 2):
+                        continue
+                    keys = bond_keys[b]
+                    if (prefix, inst) in keys:
+                        continue
+                    if gap_empty:
+                        hit = [kk for kk in keys if kk[0] == prefix]
+                        if hit:
+                            continue
+                    keys[(prefix, inst)] = len(bond_qn[b])
+                    bond_qn[b].append(qn_after(term, k))
+        for b in range(N - 1):
+            bond_keys[b][("done",)] = len(bond_qn[b])
+            bond_qn[b].append(self.zero)
+
+        def chan(term, b):
+            prefix, inst, gap_empty, k = key_of(term, b)
+            keys = bond_keys[b]
+            if (prefix, inst) in keys:
+                return keys[(prefix, inst)]
+            for kk, v in keys.items():
+                if kk[0] == prefix:
+                    return v
+            raise KeyError("channel missing")
+
+        # per-site operator matrix entries: (l_chan, r_chan) -> accumulated op
+        entries: List[Dict[Tuple[int, int], np.ndarray]] = [dict() for _ in range(N)]
+
+        def add(site, l, r, mat):
+            e = entries[site]
+            if (l, r) in e:
+                e[(l, r)] = e[(l, r)] + mat
+            else:
+                e[(l, r)] = mat.astype(self.dtype).copy()
+
+        ready_l = lambda i: 0
+        done_r = lambda i: 0 if i == N - 1 else bond_keys[i][("done",)]
+        ready_r = lambda i: 0
+        done_l = lambda i: 0 if i == 0 else bond_keys[i - 1][("done",)]
+
+        for i in range(N):
+            idm = self.ids[i].mat
+            if i < N - 1 and i > 0:
+                add(i, ready_l(i), ready_r(i), idm)
+                add(i, done_l(i), done_r(i), idm)
+            elif i == 0 and N > 1:
+                add(i, 0, ready_r(i), idm)
+            elif i == N - 1 and N > 1:
+                add(i, done_l(i), 0, idm)
+        for term in self.terms:
+            if len(term.sites) == 1:
+                s = term.sites[0]
+                l = 0 if s == 0 else ready_l(s)
+                r = done_r(s)
+                add(s, l, r, term.coef * term.ops[0].mat)
+                continue
+            first, last = term.sites[0], term.sites[-1]
+            for s in range(first, last + 1):
+                l = 0 if s == first else chan(term, s - 1)
+                r = done_r(s) if s == last else chan(term, s)
+                if s in term.sites:
+                    k = term.sites.index(s)
+                    mat = term.ops[k].mat
+                    if s == last:
+                        mat = term.coef * mat
+                else:
+                    k = max(j for j, t in enumerate(term.sites) if t < s)
+                    inst = term.insts[k]
+                    mat = self.ids[s].mat if inst is None else inst.mat
+                # an identical (l, r, mat) entry from another term is the same
+                # shared channel transition; only add transitions once
+                key = (l, r)
+                e = entries[s]
+                if s != last and key in e:
+                    continue
+                add(s, l, r, mat)
+
+        # bond indexes: group channels by QN (ascending), keep creation order
+        bond_perm, bond_index = [], []
+        for b in range(N - 1):
+            qns = bond_qn[b]
+            uniq = sorted(set(qns))
+            order = []
+            sectors = []
+            for q in uniq:
+                members = [c for c in range(len(qns)) if qns[c] == q]
+                order.extend(members)
+                sectors.append((q, len(members)))
+            pos = {c: p for p, c in enumerate(order)}
+            bond_perm.append(pos)
+            bond_index.append(Index.make(sectors, OUT))
+        triv = Index.make([(self.zero, 1)], OUT)
+        mpo = []
+        for i in range(N):
+            lvb = (triv if i == 0 else bond_index[i - 1]).inverse()
+            rvb = triv if i == N - 1 else bond_index[i]
+            pb_out = self.sites[i]
+            W = BlockTensorData([lvb, pb_out.inverse(), pb_out, rvb], {}, self.dtype)
+            for (l, r), mat in entries[i].items():
+                lc = l if i == 0 else bond_perm[i - 1][l]
+                rc = r if i == N - 1 else bond_perm[i][r]
+                for a, o in np.argwhere(mat != 0):
+                    W.set_elem((lc, int(a), int(o), rc), mat[a, o])
+            mpo.append(W)
+        return mpo
+
+
+# ---------------------------------------------------------------------------
+# Hamiltonians used by the tests and the benchmark
+# ---------------------------------------------------------------------------
+
+
+def heisenberg_chain_mpo(N, J=1.0, dtype=np.float64, pairs=None):
+    pb, ops = spin_half_site(dtype)
+    g = MPOGenerator([pb] * N, [ops["id"]] * N, dtype)
+    if pairs is None:
+        pairs = [(i, i + 1) for i in range(N - 1)]
+    for (i, j) in pairs:
+        i, j = min(i, j), max(i, j)
+        g.add_two_site(J, ops["sz"], i, ops["sz"], j)
+        g.add_two_site(0.5 * J, ops["sp"], i, ops["sm"], j)
+        g.add_two_site(0.5 * J, ops["sm"], i, ops["sp"], j)
+    return g.gen(), pb
+
+
+def ising_chain_mpo(N, dtype=np.float64):
+    pb, ops = spin_half_site(dtype)
+    g = MPOGenerator([pb] * N, [ops["id"]] * N, dtype)
+    for i in range(N - 1):
+        g.add_two_site(1.0, ops["sz"], i, ops["sz"], i + 1)
+    return g.gen(), pb
+
+
+def heisenberg_ladder_pairs(Lx, Ly=2):
+    """Nearest-neighbour bonds of an Lx x Ly open ladder, site = x*Ly + y."""
+    pairs = []
+    for x in range(Lx):
+        for y in range(Ly):
+            s = x * Ly + y
+            if y + 1 < Ly:
+                pairs.append((s, s + 1))
+            if x + 1 < Lx:
+                pairs.append((s, s + Ly))
+    return pairs
+
+
+def hubbard_cylinder_mpo(Lx, Ly, t=1.0, U=8.0, t2=0.0, dtype=np.float64):
+    """Hubbard cylinder (open x, periodic y) with the site map and hopping terms
+    of ``benchmark/ultradmrg_hubbard2d.cpp:138-202`` (site = x*Ly + y)."""
+    pb, o = hubbard_site_nsz(dtype)
+    N = Lx * Ly
+    g = MPOGenerator([pb] * N, [o["id"]] * N, dtype)
+    f = o["f"]
+
+    def hop(tt, s1, s2, inst):
+        g.add_two_site(-tt, o["bupcF"], s1, o["bupa"], s2, inst)
+        g.add_two_site(-tt, o["bdnc"], s1, o["Fbdna"], s2, inst)
+        g.add_two_site(tt, o["bupaF"], s1, o["bupc"], s2, inst)
+        g.add_two_site(tt, o["bdna"], s1, o["Fbdnc"], s2, inst)
+
+    for i in range(N):
+        g.add_term(U, [o["Uterm"]], [i])
+    for i in range(N - Ly):
+        hop(t, i, i + Ly, f)
+    for i in range(N):
+        y = i % Ly
+        if y < Ly - 1:
+            hop(t, i, i + 1, None)
+        elif Ly > 2:
+            hop(t, i - Ly + 1, i, f)
+    if t2 != 0.0:
+        for i in range(N - Ly):
+            y, x = i % Ly, i // Ly
+            for T in ((y + 1) % Ly + (x + 1) * Ly, (y + Ly - 1) % Ly + (x + 1) * Ly):
+                hop(t2, min(i, T), max(i, T), f)
+    return g.gen(), pb
+
+
+def hubbard_cylinder_holes(N, n_holes_per=8):
+    """Initial product state labels of ``benchmark/ultradmrg_hubbard2d.cpp:206-225``
+    (one hole every N/8 sites, alternating up/down elsewhere): basis labels
+    0=(2,0), 1=(1,1), 2=(1,-1), 3=(0,0)."""
+    per = N // n_holes_per
+    labs, sz = [], 0
+    for i in range(N):
+        if i % per == per - 1:
+            labs.append(3)
+        else:
+            labs.append(sz % 2 + 1)
+            sz += 1
+    return labs
+
+
+def hubbard_2x2_test_mpo(dtype=np.float64, t0=1.0, t1=0.5, U=2.0, Nx=2, Ny=2):
+    """Hubbard model of ``test_two_site_update_finite_vmps.cc:848-905``."""
+    pb, o = hubbard_site_nupndn(dtype)
+    N = Nx * Ny
+    g = MPOGenerator([pb] * N, [o["id"]] * N, dtype)
+    f = o["f"]
+    idx = lambda i, j: i * Ny + j
+
+    def hop(tt, s0, s1):
+        g.add_two_site(1, -tt * o["adagupf"], s0, o["aup"], s1, f)
+        g.add_two_site(1, -tt * o["adagdn"], s0, o["fadn"], s1, f)
+        g.add_two_site(1, o["naupf"], s0, -tt * o["adagup"], s1, f)
+        g.add_two_site(1, o["nadn"], s0, -tt * o["fadagdn"], s1, f)
+
+    for i in range(Nx):
+        for j in range(Ny):
+            s0 = idx(i, j)
+            g.add_term(U, [o["nupdn"]], [s0])
+            if i != Nx - 1:
+                hop(t0, s0, idx(i + 1, j))
+            if j != Ny - 1:
+                hop(t0, s0, idx(i, j + 1))
+            if j != Ny - 1:
+                if i != 0:
+                    a, b = sorted((s0, idx(i - 1, j + 1)))
+                    hop(t1, a, b)
+                if i != Nx - 1:
+                    a, b = sorted((s0, idx(i + 1, j + 1)))
+                    hop(t1, a, b)
+    return g.gen(), pb
+
+
+# ---------------------------------------------------------------------------
+# MPS initialisation
+# ---------------------------------------------------------------------------
+
+
+def direct_product_mps(sites: Sequence[Index], labels: Sequence[int], dtype=np.float64):
+    """Product-state MPS with the bond conventions of ``DirectStateInitMps``
+    (``one_dim_tn/mps/finite_mps/finite_mps_init.h:213-266``): tensors
+    (lvb IN, pb OUT, rvb OUT); site 0 carries the total divergence and
+    ``qn(rvb_i) = qn(lvb_i) - qn(pb_i)``.  The reference then calls
+    ``Centralize(0)``, which leaves a product state's tensors as they are
+    up to signs; this builder returns them unchanged (centre at site 0).
+    """
+    N = len(sites)
+    qn_of = lambda i: sites[i].qns[sites[i].sector_of(labels[i])[0]]
+    zero = tuple(0 for _ in range(sites[0].nq))
+    div = zero
+    for i in range(N):
+        div = tuple(a + b for a, b in zip(div, qn_of(i)))
+    mps = []
+    lvb = Index.make([(zero, 1)], IN)
+    rq = qn_sub(div, qn_of(0))
+    for i in range(N):
+        if i == 0:
+            lvb = Index.make([(zero, 1)], IN)
+            rvb = Index.make([(rq, 1)], OUT)
+        else:
+            lvb = rvb.inverse()
+            if i == N - 1:
+                rvb = Index.make([(zero, 1)], OUT)
+            else:
+                rvb = Index.make([(qn_sub(lvb.qns[0], qn_of(i)), 1)], OUT)
+        A = BlockTensorData([lvb, sites[i], rvb], {}, dtype)
+        A.set_elem((0, labels[i], 0), 1.0)
+        mps.append(A)
+    return mps
+
+
+def random_sz0_labels(N, seed):
+    """Random half-up / half-down spin labels (total Sz=0) from numpy's PCG64."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    labs = np.array([0] * (N // 2) + [1] * (N - N // 2))
+    return [int(v) for v in rng.permutation(labs)]
