@@ -1,0 +1,157 @@
+/*
+ * C ABI of the GB300-native two-site DMRG/TDVP local update.
+ *
+ * Every entry point returns 0 on success or a nonzero status code; the
+ * message of the last failure on the calling thread is udmrg_last_error().
+ * Tensors live on the device of their context; host data crosses the
+ * boundary only through udmrg_tensor_upload / udmrg_tensor_download as the
+ * packed block data (blocks in lexicographic order of their sector-id
+ * tuples, each block row-major; complex data interleaved re, im).
+ *
+ * The block-sparse model is the QLTensor model of QuantumLiquids/TensorToolkit
+ * used by qlmps: an index is a list of quantum-number sectors (qn, dim) plus a
+ * direction (OUT = +1, IN = -1); a block exists only if
+ * sum_i dir_i * qn_i == divergence.
+ */
+#ifndef ULTRADMRG_GB300_H
+#define ULTRADMRG_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct udmrg_ctx udmrg_ctx;
+typedef struct udmrg_tensor udmrg_tensor;
+typedef struct udmrg_matvec_plan udmrg_matvec_plan;
+
+enum { UDMRG_F64 = 0, UDMRG_C128 = 1 };
+enum { UDMRG_SVD_FULL = 0, UDMRG_SVD_SPLIT_LEFT = 1, UDMRG_SVD_SPLIT_RIGHT = 2 };
+
+/* LanczosParams (include/qlmps/algorithm/lanczos_params.h:27-46). */
+typedef struct {
+  double error;           /* absolute energy change that stops the iteration */
+  int64_t max_iterations; /* maximal Krylov dimension */
+} udmrg_lanczos_params;
+
+/* LanczosRes (include/qlmps/algorithm/vmps/lanczos_vmps_solver_impl.h:98-103).
+ * gs_vec is a new tensor owned by the caller. */
+typedef struct {
+  int64_t iters;
+  double gs_eng;
+  udmrg_tensor *gs_vec;
+  double matvec_seconds; /* device time of the matvecs (CUDA events) */
+  int64_t matvecs;
+} udmrg_lanczos_res;
+
+/* FiniteVMPSSweepParams without the noise and path fields
+ * (include/qlmps/algorithm/finite_vmps_sweep_params.h:31-107). */
+typedef struct {
+  int64_t sweeps;
+  int64_t Dmin;
+  int64_t Dmax;
+  double trunc_err;
+  udmrg_lanczos_params lancz_params;
+} udmrg_sweep_params;
+
+/* One line of the per-site log printed by TwoSiteFiniteVMPSUpdate
+ * (two_site_update_finite_vmps_impl.h:362-371). */
+typedef struct {
+  int64_t site;
+  double e0, trunc_err;
+  int64_t D, iters;
+  double ee, lancz_sec, svd_sec, env_sec, tot_sec, matvec_flops;
+} udmrg_site_log;
+
+const char *udmrg_last_error(void);
+
+/* ---- context -------------------------------------------------------- */
+int udmrg_ctx_create(int device, udmrg_ctx **out);
+int udmrg_ctx_destroy(udmrg_ctx *ctx);
+int udmrg_ctx_sync(udmrg_ctx *ctx);
+/* Number of device kernels this library launched through ctx so far. */
+int udmrg_ctx_launches(udmrg_ctx *ctx, uint64_t *out);
+
+/* ---- tensors (QLTensor storage model) -------------------------------- */
+/* nsec[rank]: sectors per index; qns[sum(nsec)*nq]; dims[sum(nsec)];
+ * dirs[rank] (+1 OUT / -1 IN); keys[nblocks*rank] sector ids of the blocks
+ * (any order; stored sorted).  Data is uninitialised until uploaded. */
+int udmrg_tensor_create(udmrg_ctx *ctx, int dtype, int nq, int rank, const int32_t *nsec,
+                        const int32_t *qns, const int64_t *dims, const int32_t *dirs,
+                        int64_t nblocks, const int32_t *keys, udmrg_tensor **out);
+int udmrg_tensor_destroy(udmrg_tensor *t);
+int udmrg_tensor_info(const udmrg_tensor *t, int *dtype, int *nq, int *rank, int64_t *nblocks,
+                      int64_t *size);
+/* Index of one axis.  Call with qns == dims == NULL to read *nsec first. */
+int udmrg_tensor_index(const udmrg_tensor *t, int axis, int32_t *nsec, int32_t *qns,
+                       int64_t *dims, int32_t *dir);
+int udmrg_tensor_keys(const udmrg_tensor *t, int32_t *keys);
+int udmrg_tensor_upload(udmrg_tensor *t, const double *host);
+int udmrg_tensor_download(const udmrg_tensor *t, double *host);
+/* Device address of the packed data (for device-resident callers). */
+int udmrg_tensor_device_ptr(const udmrg_tensor *t, double **dptr);
+
+/* ---- block-sparse operations ---------------------------------------- */
+/* Contract(A, B, {axes_a, axes_b}, C): output = A's free axes then B's. */
+int udmrg_contract(udmrg_ctx *ctx, const udmrg_tensor *a, const udmrg_tensor *b, int n,
+                   const int32_t *axes_a, const int32_t *axes_b, udmrg_tensor **out);
+/* Contract<T, Q, a_tail, b_head>(A, B, a_start, b_start, n, C): cyclic axes. */
+int udmrg_contract_cyclic(udmrg_ctx *ctx, const udmrg_tensor *a, const udmrg_tensor *b,
+                          int a_start, int b_start, int n, udmrg_tensor **out);
+int udmrg_dag(udmrg_ctx *ctx, const udmrg_tensor *a, udmrg_tensor **out);
+
+/* ---- the hot path ---------------------------------------------------- */
+/* eff_ham_mul_two_site_state (lanczos_vmps_solver_impl.h:260-289):
+ * eff_ham = {L, W_l, W_r, R}; returns a new tensor H_eff * state. */
+int udmrg_eff_ham_mul_two_site_state(udmrg_ctx *ctx, udmrg_tensor *const *eff_ham,
+                                     const udmrg_tensor *state, udmrg_tensor **out);
+/* LanczosSolver with eff_ham_mul_two_site_state
+ * (lanczos_vmps_solver_impl.h:114-248). init_state is not modified. */
+int udmrg_lanczos_solver(udmrg_ctx *ctx, udmrg_tensor *const *eff_ham,
+                         const udmrg_tensor *init_state, const udmrg_lanczos_params *params,
+                         udmrg_lanczos_res *res);
+/* LanczosExpmvSolver (algorithm/tdvp/lanczos_expmv_solver_impl.h:70-184):
+ * exp(-i step H_eff) state for complex tensors; iters returned. */
+int udmrg_lanczos_expmv_solver(udmrg_ctx *ctx, udmrg_tensor *const *eff_ham,
+                               const udmrg_tensor *init_state, double step,
+                               const udmrg_lanczos_params *params, int64_t *iters,
+                               udmrg_tensor **out);
+/* UpdateSiteLenvs / UpdateSiteRenvs (algorithm/vmps/vmps_init.h:343-373). */
+int udmrg_update_site_lenvs(udmrg_ctx *ctx, const udmrg_tensor *lenv, const udmrg_tensor *mps_ten,
+                            const udmrg_tensor *mpo_ten, udmrg_tensor **out);
+int udmrg_update_site_renvs(udmrg_ctx *ctx, const udmrg_tensor *renv, const udmrg_tensor *mps_ten,
+                            const udmrg_tensor *mpo_ten, udmrg_tensor **out);
+/* SVD(T, ldims, ldiv, trunc_err, Dmin, Dmax, &u, &s, &vt, &err, &D)
+ * (call site two_site_update_finite_vmps_impl.h:302-307).  mode selects the
+ * plain factors (FULL) or the fused MPS splits of :320-334 (SPLIT_LEFT:
+ * vt := s*vt; SPLIT_RIGHT: u := u*s). ldiv has nq entries. */
+int udmrg_svd(udmrg_ctx *ctx, const udmrg_tensor *t, int ldims, const int32_t *ldiv,
+              double trunc_err, int64_t Dmin, int64_t Dmax, int mode, udmrg_tensor **u,
+              udmrg_tensor **s, udmrg_tensor **vt, double *actual_trunc_err, int64_t *D);
+/* TwoSiteFiniteVMPS (two_site_update_finite_vmps_impl.h:95-494), device
+ * resident.  mps[N] is read and replaced by the updated tensors (the old
+ * handles are destroyed); mpo[N] is borrowed.  log may be NULL. */
+int udmrg_two_site_finite_vmps(udmrg_ctx *ctx, int64_t N, udmrg_tensor **mps,
+                               udmrg_tensor *const *mpo, const udmrg_sweep_params *params,
+                               double *e0, udmrg_site_log *log, int64_t log_cap,
+                               int64_t *log_len);
+
+/* ---- reusable matvec plan (repeated H_eff * psi on device buffers) -------- */
+/* The plan fixes {L, W_l, W_r, R} and the block structure closed under the
+ * matvec that contains psi_struct's blocks (the Krylov structure). */
+int udmrg_matvec_plan_create(udmrg_ctx *ctx, udmrg_tensor *const *eff_ham,
+                             const udmrg_tensor *psi_struct, udmrg_matvec_plan **out);
+int udmrg_matvec_plan_info(const udmrg_matvec_plan *p, double *flops, int64_t *psi_size,
+                           int64_t *workspace_bytes);
+/* Tensor with the plan's Krylov structure holding `src` (zero elsewhere). */
+int udmrg_matvec_plan_embed(udmrg_matvec_plan *p, const udmrg_tensor *src, udmrg_tensor **out);
+/* out = H_eff * in on device buffers laid out in the Krylov structure. */
+int udmrg_matvec_plan_apply(udmrg_matvec_plan *p, const double *d_in, double *d_out);
+int udmrg_matvec_plan_destroy(udmrg_matvec_plan *p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ULTRADMRG_GB300_H */

@@ -1,0 +1,113 @@
+"""ctypes binding of ``include/ultradmrg_gb300.h`` (the C ABI).
+
+The library is the in-tree ``libudmrg_gb300.so``; there is no fallback: if it
+is missing or does not load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libudmrg_gb300.so")
+
+c_double_p = C.POINTER(C.c_double)
+c_int32_p = C.POINTER(C.c_int32)
+c_int64_p = C.POINTER(C.c_int64)
+c_void_pp = C.POINTER(C.c_void_p)
+
+
+class LanczosParams(C.Structure):
+    _fields_ = [("error", C.c_double), ("max_iterations", C.c_int64)]
+
+
+class LanczosRes(C.Structure):
+    _fields_ = [("iters", C.c_int64), ("gs_eng", C.c_double), ("gs_vec", C.c_void_p),
+                ("matvec_seconds", C.c_double), ("matvecs", C.c_int64)]
+
+
+class SweepParams(C.Structure):
+    _fields_ = [("sweeps", C.c_int64), ("Dmin", C.c_int64), ("Dmax", C.c_int64),
+                ("trunc_err", C.c_double), ("lancz_params", LanczosParams)]
+
+
+class SiteLog(C.Structure):
+    _fields_ = [("site", C.c_int64), ("e0", C.c_double), ("trunc_err", C.c_double),
+                ("D", C.c_int64), ("iters", C.c_int64), ("ee", C.c_double),
+                ("lancz_sec", C.c_double), ("svd_sec", C.c_double), ("env_sec", C.c_double),
+                ("tot_sec", C.c_double), ("matvec_flops", C.c_double)]
+
+
+# name -> argtypes (all return int status)
+SIGNATURES = {
+    "udmrg_ctx_create": [C.c_int, c_void_pp],
+    "udmrg_ctx_destroy": [C.c_void_p],
+    "udmrg_ctx_sync": [C.c_void_p],
+    "udmrg_ctx_launches": [C.c_void_p, C.POINTER(C.c_uint64)],
+    "udmrg_tensor_create": [C.c_void_p, C.c_int, C.c_int, C.c_int, c_int32_p, c_int32_p,
+                            c_int64_p, c_int32_p, C.c_int64, c_int32_p, c_void_pp],
+    "udmrg_tensor_destroy": [C.c_void_p],
+    "udmrg_tensor_info": [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                          C.POINTER(C.c_int), c_int64_p, c_int64_p],
+    "udmrg_tensor_index": [C.c_void_p, C.c_int, c_int32_p, c_int32_p, c_int64_p, c_int32_p],
+    "udmrg_tensor_keys": [C.c_void_p, c_int32_p],
+    "udmrg_tensor_upload": [C.c_void_p, c_double_p],
+    "udmrg_tensor_download": [C.c_void_p, c_double_p],
+    "udmrg_tensor_device_ptr": [C.c_void_p, C.POINTER(c_double_p)],
+    "udmrg_contract": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, c_int32_p, c_int32_p,
+                       c_void_pp],
+    "udmrg_contract_cyclic": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                              c_void_pp],
+    "udmrg_dag": [C.c_void_p, C.c_void_p, c_void_pp],
+    "udmrg_eff_ham_mul_two_site_state": [C.c_void_p, c_void_pp, C.c_void_p, c_void_pp],
+    "udmrg_lanczos_solver": [C.c_void_p, c_void_pp, C.c_void_p, C.POINTER(LanczosParams),
+                             C.POINTER(LanczosRes)],
+    "udmrg_lanczos_expmv_solver": [C.c_void_p, c_void_pp, C.c_void_p, C.c_double,
+                                   C.POINTER(LanczosParams), c_int64_p, c_void_pp],
+    "udmrg_update_site_lenvs": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, c_void_pp],
+    "udmrg_update_site_renvs": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, c_void_pp],
+    "udmrg_svd": [C.c_void_p, C.c_void_p, C.c_int, c_int32_p, C.c_double, C.c_int64, C.c_int64,
+                  C.c_int, c_void_pp, c_void_pp, c_void_pp, c_double_p, c_int64_p],
+    "udmrg_two_site_finite_vmps": [C.c_void_p, C.c_int64, c_void_pp, c_void_pp,
+                                   C.POINTER(SweepParams), c_double_p, C.POINTER(SiteLog),
+                                   C.c_int64, c_int64_p],
+    "udmrg_matvec_plan_create": [C.c_void_p, c_void_pp, C.c_void_p, c_void_pp],
+    "udmrg_matvec_plan_info": [C.c_void_p, c_double_p, c_int64_p, c_int64_p],
+    "udmrg_matvec_plan_embed": [C.c_void_p, C.c_void_p, c_void_pp],
+    "udmrg_matvec_plan_apply": [C.c_void_p, c_double_p, c_double_p],
+    "udmrg_matvec_plan_destroy": [C.c_void_p],
+}
+
+_lib = None
+
+
+class UdmrgError(RuntimeError):
+    pass
+
+
+def lib():
+    """Load the library (once) and declare every entry point."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise UdmrgError(f"{LIB_PATH} is missing: build it with ultradmrg_gb300.build.build()")
+    L = C.CDLL(LIB_PATH)
+    for name, args in SIGNATURES.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.udmrg_last_error.argtypes = []
+    L.udmrg_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def check(status: int, what: str = ""):
+    if status != 0:
+        msg = lib().udmrg_last_error().decode(errors="replace")
+        raise UdmrgError(f"{what} failed (status {status}): {msg}")
+
+
+def call(name: str, *args):
+    check(getattr(lib(), name)(*args), name)

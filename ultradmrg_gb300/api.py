@@ -1,0 +1,321 @@
+"""Python mirror of the qlmps-facing API, over the C ABI.
+
+Names and argument meaning follow the reference's entry points for the
+two-site path (``LanczosSolver``, ``eff_ham_mul_two_site_state``,
+``UpdateSiteLenvs/Renvs``, ``SVD``, ``TwoSiteFiniteVMPS``); the numerics run
+in ``libudmrg_gb300.so`` on the GPU.  Host data are
+:class:`~ultradmrg_gb300.tensor_data.BlockTensorData` objects.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import call
+from .tensor_data import BlockTensorData, Index, from_packed
+
+F64, C128 = 0, 1
+
+
+class Context:
+    """One GPU, one stream (``udmrg_ctx``)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        call("udmrg_ctx_create", device, C.byref(h))
+        self.h = h
+
+    def sync(self):
+        call("udmrg_ctx_sync", self.h)
+
+    def launches(self) -> int:
+        v = C.c_uint64()
+        call("udmrg_ctx_launches", self.h, C.byref(v))
+        return int(v.value)
+
+    def close(self):
+        if self.h:
+            call("udmrg_ctx_destroy", self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+
+
+def _i32(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(_lib.c_int32_p)
+
+
+def _i64(a):
+    a = np.ascontiguousarray(a, dtype=np.int64)
+    return a, a.ctypes.data_as(_lib.c_int64_p)
+
+
+class DeviceTensor:
+    """Block-sparse tensor resident on the GPU (``udmrg_tensor``)."""
+
+    def __init__(self, ctx: Context, handle: C.c_void_p):
+        self.ctx = ctx
+        self.h = handle
+
+    @staticmethod
+    def from_data(ctx: Context, t: BlockTensorData, dtype=None) -> "DeviceTensor":
+        dtype = np.dtype(dtype or t.dtype)
+        cplx = dtype == np.complex128
+        nq = t.nq
+        nsec, qns, dims, dirs = [], [], [], []
+        for ind in t.indexes:
+            nsec.append(ind.nsec)
+            for q, d in zip(ind.qns, ind.dims):
+                qns.extend(q)
+                dims.append(d)
+            dirs.append(ind.dir)
+        keys = t.sorted_keys()
+        a_nsec, p_nsec = _i32(nsec)
+        a_qns, p_qns = _i32(qns if qns else [0])
+        a_dims, p_dims = _i64(dims if dims else [1])
+        a_dirs, p_dirs = _i32(dirs)
+        a_keys, p_keys = _i32(np.array(keys, dtype=np.int32).ravel() if keys else [0])
+        h = C.c_void_p()
+        call("udmrg_tensor_create", ctx.h, C128 if cplx else F64, nq, t.rank, p_nsec, p_qns,
+             p_dims, p_dirs, len(keys), p_keys, C.byref(h))
+        dt = DeviceTensor(ctx, h)
+        data = t.packed().astype(np.complex128 if cplx else np.float64)
+        dt.upload_packed(data)
+        return dt
+
+    # --- metadata ---------------------------------------------------------
+    def info(self):
+        dt, nq, r = C.c_int(), C.c_int(), C.c_int()
+        nb, sz = C.c_int64(), C.c_int64()
+        call("udmrg_tensor_info", self.h, C.byref(dt), C.byref(nq), C.byref(r), C.byref(nb),
+             C.byref(sz))
+        return dict(dtype=dt.value, nq=nq.value, rank=r.value, nblocks=nb.value, size=sz.value)
+
+    @property
+    def is_complex(self):
+        return self.info()["dtype"] == C128
+
+    def indexes(self) -> List[Index]:
+        inf = self.info()
+        out = []
+        for ax in range(inf["rank"]):
+            ns, dr = C.c_int32(), C.c_int32()
+            call("udmrg_tensor_index", self.h, ax, C.byref(ns), None, None, C.byref(dr))
+            qns = np.zeros(max(ns.value * inf["nq"], 1), np.int32)
+            dims = np.zeros(max(ns.value, 1), np.int64)
+            call("udmrg_tensor_index", self.h, ax, None, qns.ctypes.data_as(_lib.c_int32_p),
+                 dims.ctypes.data_as(_lib.c_int64_p), None)
+            q = qns[:ns.value * inf["nq"]].reshape(ns.value, inf["nq"])
+            out.append(Index(tuple(tuple(int(v) for v in row) for row in q),
+                             tuple(int(d) for d in dims[:ns.value]), int(dr.value)))
+        return out
+
+    def keys(self):
+        inf = self.info()
+        k = np.zeros(max(inf["nblocks"] * inf["rank"], 1), np.int32)
+        call("udmrg_tensor_keys", self.h, k.ctypes.data_as(_lib.c_int32_p))
+        return [tuple(int(v) for v in row) for row in
+                k[:inf["nblocks"] * inf["rank"]].reshape(inf["nblocks"], inf["rank"])]
+
+    def upload_packed(self, data: np.ndarray):
+        buf = np.ascontiguousarray(data)
+        if buf.dtype == np.complex128:
+            buf = buf.view(np.float64)
+        call("udmrg_tensor_upload", self.h, buf.ctypes.data_as(_lib.c_double_p))
+
+    def download_packed(self) -> np.ndarray:
+        inf = self.info()
+        n = inf["size"] * (2 if inf["dtype"] == C128 else 1)
+        buf = np.zeros(max(n, 1), np.float64)
+        call("udmrg_tensor_download", self.h, buf.ctypes.data_as(_lib.c_double_p))
+        buf = buf[:n]
+        return buf.view(np.complex128) if inf["dtype"] == C128 else buf
+
+    def to_data(self) -> BlockTensorData:
+        dtype = np.complex128 if self.is_complex else np.float64
+        return from_packed(self.indexes(), self.keys(), self.download_packed(), dtype)
+
+    def device_ptr(self) -> int:
+        p = _lib.c_double_p()
+        call("udmrg_tensor_device_ptr", self.h, C.byref(p))
+        return C.cast(p, C.c_void_p).value or 0
+
+    def close(self):
+        if self.h:
+            call("udmrg_tensor_destroy", self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+def _handles(ts: Sequence[DeviceTensor]):
+    arr = (C.c_void_p * len(ts))(*[t.h.value if isinstance(t.h, C.c_void_p) else t.h for t in ts])
+    return arr
+
+
+def _new(ctx, h):
+    return DeviceTensor(ctx, h)
+
+
+# --- block-sparse operations ---------------------------------------------------
+
+def contract(ctx, a: DeviceTensor, b: DeviceTensor, axes_a, axes_b) -> DeviceTensor:
+    xa, pa = _i32(axes_a)
+    xb, pb = _i32(axes_b)
+    h = C.c_void_p()
+    call("udmrg_contract", ctx.h, a.h, b.h, len(axes_a), pa, pb, C.byref(h))
+    return _new(ctx, h)
+
+
+def contract_cyclic(ctx, a, b, a_start, b_start, n) -> DeviceTensor:
+    h = C.c_void_p()
+    call("udmrg_contract_cyclic", ctx.h, a.h, b.h, a_start, b_start, n, C.byref(h))
+    return _new(ctx, h)
+
+
+def dag(ctx, a) -> DeviceTensor:
+    h = C.c_void_p()
+    call("udmrg_dag", ctx.h, a.h, C.byref(h))
+    return _new(ctx, h)
+
+
+# --- hot path ------------------------------------------------------------------
+
+def eff_ham_mul_two_site_state(ctx, eff_ham: Sequence[DeviceTensor], state: DeviceTensor):
+    h = C.c_void_p()
+    call("udmrg_eff_ham_mul_two_site_state", ctx.h, _handles(eff_ham), state.h, C.byref(h))
+    return _new(ctx, h)
+
+
+@dataclass
+class LanczosResult:
+    iters: int
+    gs_eng: float
+    gs_vec: DeviceTensor
+    matvec_seconds: float
+    matvecs: int
+
+
+def lanczos_solver(ctx, eff_ham, init_state, error=1e-7, max_iterations=200) -> LanczosResult:
+    p = _lib.LanczosParams(error, max_iterations)
+    r = _lib.LanczosRes()
+    call("udmrg_lanczos_solver", ctx.h, _handles(eff_ham), init_state.h, C.byref(p), C.byref(r))
+    return LanczosResult(int(r.iters), float(r.gs_eng), _new(ctx, C.c_void_p(r.gs_vec)),
+                         float(r.matvec_seconds), int(r.matvecs))
+
+
+def lanczos_expmv_solver(ctx, eff_ham, init_state, step, error=1e-10, max_iterations=20):
+    p = _lib.LanczosParams(error, max_iterations)
+    it = C.c_int64()
+    h = C.c_void_p()
+    call("udmrg_lanczos_expmv_solver", ctx.h, _handles(eff_ham), init_state.h, step, C.byref(p),
+         C.byref(it), C.byref(h))
+    return int(it.value), _new(ctx, h)
+
+
+def update_site_lenvs(ctx, lenv, mps_ten, mpo_ten) -> DeviceTensor:
+    h = C.c_void_p()
+    call("udmrg_update_site_lenvs", ctx.h, lenv.h, mps_ten.h, mpo_ten.h, C.byref(h))
+    return _new(ctx, h)
+
+
+def update_site_renvs(ctx, renv, mps_ten, mpo_ten) -> DeviceTensor:
+    h = C.c_void_p()
+    call("udmrg_update_site_renvs", ctx.h, renv.h, mps_ten.h, mpo_ten.h, C.byref(h))
+    return _new(ctx, h)
+
+
+SVD_FULL, SVD_SPLIT_LEFT, SVD_SPLIT_RIGHT = 0, 1, 2
+
+
+def svd(ctx, t, ldims, ldiv, trunc_err, Dmin, Dmax, mode=SVD_FULL):
+    xd, pd = _i32(list(ldiv))
+    u, s, vt = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    err, D = C.c_double(), C.c_int64()
+    call("udmrg_svd", ctx.h, t.h, ldims, pd, trunc_err, Dmin, Dmax, mode, C.byref(u), C.byref(s),
+         C.byref(vt), C.byref(err), C.byref(D))
+    return _new(ctx, u), _new(ctx, s), _new(ctx, vt), float(err.value), int(D.value)
+
+
+@dataclass
+class FiniteVMPSSweepParams:
+    """``FiniteVMPSSweepParams`` (sweeps, Dmin, Dmax, trunc_err, Lanczos params)."""
+
+    sweeps: int
+    Dmin: int
+    Dmax: int
+    trunc_err: float
+    lanczos_error: float = 1e-7
+    lanczos_max_iterations: int = 200
+
+
+def two_site_finite_vmps(ctx, mps: List[DeviceTensor], mpo: List[DeviceTensor],
+                         params: FiniteVMPSSweepParams):
+    """``TwoSiteFiniteVMPS``: updates ``mps`` in place, returns (e0, per-site log)."""
+    N = len(mps)
+    sp = _lib.SweepParams(params.sweeps, params.Dmin, params.Dmax, params.trunc_err,
+                          _lib.LanczosParams(params.lanczos_error, params.lanczos_max_iterations))
+    cap = 2 * N * max(params.sweeps, 1)
+    log = (_lib.SiteLog * cap)()
+    e0 = C.c_double()
+    nlog = C.c_int64()
+    call("udmrg_two_site_finite_vmps", ctx.h, N, _handles(mps), _handles(mpo), C.byref(sp),
+         C.byref(e0), log, cap, C.byref(nlog))
+    rows = []
+    for i in range(min(cap, nlog.value)):
+        L = log[i]
+        rows.append(dict(site=L.site, e0=L.e0, trunc_err=L.trunc_err, D=L.D, iters=L.iters,
+                         ee=L.ee, lancz_sec=L.lancz_sec, svd_sec=L.svd_sec, env_sec=L.env_sec,
+                         tot_sec=L.tot_sec, matvec_flops=L.matvec_flops))
+    return float(e0.value), rows
+
+
+class MatvecPlan:
+    """Reusable H_eff * psi on device buffers (``udmrg_matvec_plan``)."""
+
+    def __init__(self, ctx, eff_ham, psi_struct):
+        self.ctx = ctx
+        h = C.c_void_p()
+        call("udmrg_matvec_plan_create", ctx.h, _handles(eff_ham), psi_struct.h, C.byref(h))
+        self.h = h
+
+    def info(self):
+        f, n, w = C.c_double(), C.c_int64(), C.c_int64()
+        call("udmrg_matvec_plan_info", self.h, C.byref(f), C.byref(n), C.byref(w))
+        return dict(flops=f.value, psi_size=n.value, workspace_bytes=w.value)
+
+    def embed(self, t: DeviceTensor) -> DeviceTensor:
+        h = C.c_void_p()
+        call("udmrg_matvec_plan_embed", self.h, t.h, C.byref(h))
+        return _new(self.ctx, h)
+
+    def apply_ptr(self, d_in: int, d_out: int):
+        call("udmrg_matvec_plan_apply", self.h, C.cast(C.c_void_p(d_in), _lib.c_double_p),
+             C.cast(C.c_void_p(d_out), _lib.c_double_p))
+
+    def apply(self, x: DeviceTensor, y: DeviceTensor):
+        self.apply_ptr(x.device_ptr(), y.device_ptr())
+
+    def close(self):
+        if self.h:
+            call("udmrg_matvec_plan_destroy", self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass

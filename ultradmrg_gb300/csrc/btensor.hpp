@@ -1,0 +1,121 @@
+// Block-sparse tensor runtime: host metadata, device data.
+//
+// Storage model (the QLTensor model of QuantumLiquids/TensorToolkit as used
+// by qlmps): an Index is an ordered list of QN sectors (qn, dim) plus a
+// direction (OUT = +1, IN = -1).  A tensor holds dense blocks keyed by one
+// sector id per index; a block may exist only if sum_i dir_i * qn_i == div.
+// Blocks are kept sorted lexicographically by their sector-id tuples and
+// packed back to back in one device buffer, each block row-major over the
+// tensor's axes.
+#pragma once
+
+#include <memory>
+#include <unordered_map>
+
+#include "common.hpp"
+
+namespace udmrg {
+
+struct Index {
+  std::vector<QN> qns;
+  std::vector<int64_t> dims;
+  int dir = 1;  // +1 OUT, -1 IN
+  int nsec() const { return (int)qns.size(); }
+  int64_t dim() const {
+    int64_t s = 0;
+    for (auto d : dims) s += d;
+    return s;
+  }
+  Index inverse() const {
+    Index r = *this;
+    r.dir = -dir;
+    return r;
+  }
+  bool same_space(const Index &o) const { return qns == o.qns && dims == o.dims; }
+  bool operator==(const Index &o) const { return same_space(o) && dir == o.dir; }
+  int find(const QN &q) const {
+    for (int i = 0; i < nsec(); ++i)
+      if (qns[i] == q) return i;
+    return -1;
+  }
+};
+
+// Device context: one GPU, one stream, stream-ordered allocations.
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  // pinned host scratch for small device->host reads
+  double *pinned = nullptr;
+  size_t pinned_cap = 0;
+  // counts of kernels launched by this library through this context
+  uint64_t launches = 0;
+
+  explicit Ctx(int dev);
+  ~Ctx();
+  void *alloc(size_t bytes);
+  void free(void *p);
+  void sync();
+  double *host_scratch(size_t ndoubles);
+};
+
+struct KeyHash {
+  size_t operator()(const std::vector<int32_t> &k) const {
+    uint64_t h = 1469598103934665603ull;
+    for (auto v : k) {
+      h ^= (uint64_t)(uint32_t)v;
+      h *= 1099511628211ull;
+    }
+    return (size_t)h;
+  }
+};
+
+struct BTensor {
+  Ctx *ctx = nullptr;
+  DType dtype = kF64;
+  int nq = 1;
+  std::vector<Index> idx;
+  std::vector<int32_t> keys;  // nblocks * rank, sorted lexicographically
+  std::vector<int64_t> offs;  // element offset of each block (nblocks + 1)
+  double *data = nullptr;     // device buffer, offs.back() elements
+  bool owns = true;
+
+  BTensor() = default;
+  BTensor(const BTensor &) = delete;
+  BTensor &operator=(const BTensor &) = delete;
+  ~BTensor();
+
+  int rank() const { return (int)idx.size(); }
+  int64_t nblocks() const { return rank() ? (int64_t)keys.size() / rank() : 0; }
+  int64_t size() const { return offs.empty() ? 0 : offs.back(); }
+  const int32_t *key(int64_t b) const { return keys.data() + b * rank(); }
+  int64_t block_elems(int64_t b) const { return offs[b + 1] - offs[b]; }
+  int64_t dim_of(int64_t b, int axis) const { return idx[axis].dims[key(b)[axis]]; }
+  QN block_div(const int32_t *k) const;
+  QN div() const;  // divergence of the first block (all blocks agree)
+
+  // block lookup by sector-id tuple (built on demand)
+  int64_t find(const std::vector<int32_t> &k) const;
+  void build_lookup() const;
+
+  // Set the block list (must be sorted and unique), compute offsets.
+  void set_blocks(std::vector<int32_t> sorted_keys);
+  void alloc_data();   // allocate (uninitialised) device data for size()
+  void zero_data();    // memset device data to 0 (stream ordered)
+  size_t bytes() const { return (size_t)size() * elem_doubles(dtype) * sizeof(double); }
+
+  // structure copy without data
+  std::unique_ptr<BTensor> clone_struct() const;
+  std::unique_ptr<BTensor> clone() const;  // with data (device copy)
+
+ private:
+  mutable std::unordered_map<std::vector<int32_t>, int64_t, KeyHash> lookup_;
+  mutable bool lookup_built_ = false;
+};
+
+using TensorPtr = std::unique_ptr<BTensor>;
+
+// Sort + deduplicate a flat key list (rank-sized tuples).
+std::vector<int32_t> sort_keys(const std::vector<int32_t> &flat, int rank);
+
+}  // namespace udmrg

@@ -1,0 +1,387 @@
+// extern "C" boundary: plain pointers and sizes, status codes, no exceptions.
+#include <cstring>
+
+#include "../../include/ultradmrg_gb300.h"
+#include "dmrg.hpp"
+
+using namespace udmrg;
+
+struct udmrg_ctx {
+  Ctx ctx;
+  explicit udmrg_ctx(int dev) : ctx(dev) {}
+};
+struct udmrg_tensor {
+  TensorPtr t;
+};
+struct udmrg_matvec_plan {
+  Ctx *ctx;
+  std::unique_ptr<MatvecPlan> plan;
+  TensorPtr promoted[4];  // complex copies of real operators, when needed
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+template <typename F>
+int guarded(F &&f) {
+  try {
+    f();
+    return kOk;
+  } catch (const Error &e) {
+    g_err = e.what();
+    return e.code;
+  } catch (const std::exception &e) {
+    g_err = e.what();
+    return kErrInternal;
+  } catch (...) {
+    g_err = "unknown error";
+    return kErrInternal;
+  }
+}
+
+udmrg_tensor *wrap(TensorPtr t) {
+  auto *h = new udmrg_tensor;
+  h->t = std::move(t);
+  return h;
+}
+
+const BTensor &T(const udmrg_tensor *h) {
+  UDMRG_REQUIRE(h && h->t, "null tensor handle");
+  return *h->t;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *udmrg_last_error(void) { return g_err.c_str(); }
+
+int udmrg_ctx_create(int device, udmrg_ctx **out) {
+  return guarded([&] {
+    UDMRG_REQUIRE(out, "null output");
+    *out = new udmrg_ctx(device);
+  });
+}
+
+int udmrg_ctx_destroy(udmrg_ctx *c) {
+  return guarded([&] { delete c; });
+}
+
+int udmrg_ctx_sync(udmrg_ctx *c) {
+  return guarded([&] { c->ctx.sync(); });
+}
+
+int udmrg_ctx_launches(udmrg_ctx *c, uint64_t *out) {
+  return guarded([&] { *out = c->ctx.launches; });
+}
+
+int udmrg_tensor_create(udmrg_ctx *c, int dtype, int nq, int rank, const int32_t *nsec,
+                        const int32_t *qns, const int64_t *dims, const int32_t *dirs,
+                        int64_t nblocks, const int32_t *keys, udmrg_tensor **out) {
+  return guarded([&] {
+    UDMRG_REQUIRE(c && out, "null argument");
+    UDMRG_REQUIRE(dtype == kF64 || dtype == kC128, "dtype must be UDMRG_F64 or UDMRG_C128");
+    UDMRG_REQUIRE(nq >= 1 && nq <= kMaxQ, "nq out of range");
+    UDMRG_REQUIRE(rank >= 1, "rank must be positive");
+    auto t = std::make_unique<BTensor>();
+    t->ctx = &c->ctx;
+    t->dtype = (DType)dtype;
+    t->nq = nq;
+    int64_t s = 0;
+    for (int i = 0; i < rank; ++i) {
+      Index ix;
+      ix.dir = dirs[i];
+      UDMRG_REQUIRE(ix.dir == 1 || ix.dir == -1, "direction must be +1 (OUT) or -1 (IN)");
+      for (int j = 0; j < nsec[i]; ++j, ++s) {
+        QN q;
+        for (int k = 0; k < nq; ++k) q.v[k] = qns[s * nq + k];
+        ix.qns.push_back(q);
+        UDMRG_REQUIRE(dims[s] > 0, "sector dimensions must be positive");
+        ix.dims.push_back(dims[s]);
+      }
+      t->idx.push_back(std::move(ix));
+    }
+    std::vector<int32_t> flat(keys, keys + nblocks * rank);
+    auto sorted = sort_keys(flat, rank);
+    UDMRG_REQUIRE((int64_t)sorted.size() == nblocks * rank, "duplicate block keys");
+    t->set_blocks(std::move(sorted));
+    if (t->nblocks() > 0) {
+      const QN d = t->div();
+      for (int64_t b = 1; b < t->nblocks(); ++b)
+        UDMRG_REQUIRE(t->block_div(t->key(b)) == d, "blocks with different divergences");
+    }
+    t->alloc_data();
+    *out = wrap(std::move(t));
+  });
+}
+
+int udmrg_tensor_destroy(udmrg_tensor *t) {
+  return guarded([&] { delete t; });
+}
+
+int udmrg_tensor_info(const udmrg_tensor *h, int *dtype, int *nq, int *rank, int64_t *nblocks,
+                      int64_t *size) {
+  return guarded([&] {
+    const BTensor &t = T(h);
+    if (dtype) *dtype = t.dtype;
+    if (nq) *nq = t.nq;
+    if (rank) *rank = t.rank();
+    if (nblocks) *nblocks = t.nblocks();
+    if (size) *size = t.size();
+  });
+}
+
+int udmrg_tensor_index(const udmrg_tensor *h, int axis, int32_t *nsec, int32_t *qns,
+                       int64_t *dims, int32_t *dir) {
+  return guarded([&] {
+    const BTensor &t = T(h);
+    UDMRG_REQUIRE(axis >= 0 && axis < t.rank(), "axis out of range");
+    const Index &ix = t.idx[axis];
+    if (nsec) *nsec = ix.nsec();
+    if (dir) *dir = ix.dir;
+    for (int j = 0; j < ix.nsec(); ++j) {
+      if (qns)
+        for (int k = 0; k < t.nq; ++k) qns[j * t.nq + k] = ix.qns[j].v[k];
+      if (dims) dims[j] = ix.dims[j];
+    }
+  });
+}
+
+int udmrg_tensor_keys(const udmrg_tensor *h, int32_t *keys) {
+  return guarded([&] {
+    const BTensor &t = T(h);
+    std::memcpy(keys, t.keys.data(), t.keys.size() * sizeof(int32_t));
+  });
+}
+
+int udmrg_tensor_upload(udmrg_tensor *h, const double *host) {
+  return guarded([&] {
+    BTensor &t = *h->t;
+    if (t.size())
+      UDMRG_CHECK_CUDA(
+          cudaMemcpyAsync(t.data, host, t.bytes(), cudaMemcpyHostToDevice, t.ctx->stream));
+    t.ctx->sync();
+  });
+}
+
+int udmrg_tensor_download(const udmrg_tensor *h, double *host) {
+  return guarded([&] {
+    const BTensor &t = T(h);
+    if (t.size())
+      UDMRG_CHECK_CUDA(
+          cudaMemcpyAsync(host, t.data, t.bytes(), cudaMemcpyDeviceToHost, t.ctx->stream));
+    t.ctx->sync();
+  });
+}
+
+int udmrg_tensor_device_ptr(const udmrg_tensor *h, double **dptr) {
+  return guarded([&] { *dptr = T(h).data; });
+}
+
+int udmrg_contract(udmrg_ctx *c, const udmrg_tensor *a, const udmrg_tensor *b, int n,
+                   const int32_t *axes_a, const int32_t *axes_b, udmrg_tensor **out) {
+  return guarded([&] {
+    std::vector<int> ca(axes_a, axes_a + n), cb(axes_b, axes_b + n);
+    *out = wrap(contract_axes(c->ctx, T(a), T(b), ca, cb));
+  });
+}
+
+int udmrg_contract_cyclic(udmrg_ctx *c, const udmrg_tensor *a, const udmrg_tensor *b,
+                          int a_start, int b_start, int n, udmrg_tensor **out) {
+  return guarded([&] { *out = wrap(contract_cyclic(c->ctx, T(a), T(b), a_start, b_start, n)); });
+}
+
+int udmrg_dag(udmrg_ctx *c, const udmrg_tensor *a, udmrg_tensor **out) {
+  return guarded([&] { *out = wrap(dag(c->ctx, T(a))); });
+}
+
+namespace {
+
+// Operators with the element type of the state (real ones promoted).
+struct EffHam {
+  const BTensor *op[4];
+  TensorPtr keep[4];
+};
+
+void prepare_eff_ham(Ctx &ctx, udmrg_tensor *const *eff_ham, DType dt, EffHam &e) {
+  for (int i = 0; i < 4; ++i) {
+    const BTensor &t = T(eff_ham[i]);
+    if (t.dtype == dt) {
+      e.op[i] = &t;
+    } else {
+      UDMRG_REQUIRE(dt == kC128, "real state with complex operators is not supported");
+      e.keep[i] = to_complex(ctx, t);
+      e.op[i] = e.keep[i].get();
+    }
+  }
+}
+
+}  // namespace
+
+int udmrg_eff_ham_mul_two_site_state(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
+                                     const udmrg_tensor *state, udmrg_tensor **out) {
+  return guarded([&] {
+    Ctx &ctx = c->ctx;
+    const BTensor &psi = T(state);
+    EffHam e;
+    prepare_eff_ham(ctx, eff_ham, psi.dtype, e);
+    auto mv = plan_matvec2(ctx, *e.op[0], *e.op[1], *e.op[2], *e.op[3], psi);
+    auto in = embed(ctx, psi, *mv->sstruct);
+    auto res = mv->sstruct->clone_struct();
+    res->alloc_data();
+    mv->apply(in->data, res->data);
+    ctx.sync();
+    *out = wrap(std::move(res));
+  });
+}
+
+int udmrg_lanczos_solver(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
+                         const udmrg_tensor *init_state, const udmrg_lanczos_params *params,
+                         udmrg_lanczos_res *res) {
+  return guarded([&] {
+    Ctx &ctx = c->ctx;
+    const BTensor &psi = T(init_state);
+    EffHam e;
+    prepare_eff_ham(ctx, eff_ham, psi.dtype, e);
+    auto mv = plan_matvec2(ctx, *e.op[0], *e.op[1], *e.op[2], *e.op[3], psi);
+    LanczosParams p{params->error, params->max_iterations};
+    auto r = lanczos_gs(ctx, *mv, psi, p);
+    res->iters = r.iters;
+    res->gs_eng = r.gs_eng;
+    res->matvec_seconds = r.matvec_seconds;
+    res->matvecs = r.matvecs;
+    res->gs_vec = wrap(std::move(r.gs_vec));
+  });
+}
+
+int udmrg_lanczos_expmv_solver(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
+                               const udmrg_tensor *init_state, double step,
+                               const udmrg_lanczos_params *params, int64_t *iters,
+                               udmrg_tensor **out) {
+  return guarded([&] {
+    Ctx &ctx = c->ctx;
+    TensorPtr promoted;
+    const BTensor *psi = &T(init_state);
+    if (psi->dtype != kC128) {
+      promoted = to_complex(ctx, *psi);
+      psi = promoted.get();
+    }
+    EffHam e;
+    prepare_eff_ham(ctx, eff_ham, kC128, e);
+    auto mv = plan_matvec2(ctx, *e.op[0], *e.op[1], *e.op[2], *e.op[3], *psi);
+    LanczosParams p{params->error, params->max_iterations};
+    auto r = lanczos_expmv(ctx, *mv, *psi, step, p);
+    if (iters) *iters = r.iters;
+    *out = wrap(std::move(r.expmv));
+  });
+}
+
+int udmrg_update_site_lenvs(udmrg_ctx *c, const udmrg_tensor *lenv, const udmrg_tensor *mps_ten,
+                            const udmrg_tensor *mpo_ten, udmrg_tensor **out) {
+  return guarded([&] {
+    *out = wrap(update_site_lenv(c->ctx, T(lenv), T(mps_ten), T(mpo_ten)));
+  });
+}
+
+int udmrg_update_site_renvs(udmrg_ctx *c, const udmrg_tensor *renv, const udmrg_tensor *mps_ten,
+                            const udmrg_tensor *mpo_ten, udmrg_tensor **out) {
+  return guarded([&] {
+    *out = wrap(update_site_renv(c->ctx, T(renv), T(mps_ten), T(mpo_ten)));
+  });
+}
+
+int udmrg_svd(udmrg_ctx *c, const udmrg_tensor *t, int ldims, const int32_t *ldiv,
+              double trunc_err, int64_t Dmin, int64_t Dmax, int mode, udmrg_tensor **u,
+              udmrg_tensor **s, udmrg_tensor **vt, double *actual_trunc_err, int64_t *D) {
+  return guarded([&] {
+    const BTensor &x = T(t);
+    QN q;
+    for (int k = 0; k < x.nq; ++k) q.v[k] = ldiv[k];
+    UDMRG_REQUIRE(mode >= 0 && mode <= 2, "bad SVD mode");
+    auto r = svd_trunc(c->ctx, x, ldims, q, trunc_err, Dmin, Dmax, mode);
+    *u = wrap(std::move(r.u));
+    *s = wrap(std::move(r.s));
+    *vt = wrap(std::move(r.vt));
+    if (actual_trunc_err) *actual_trunc_err = r.trunc_err;
+    if (D) *D = r.D;
+  });
+}
+
+int udmrg_two_site_finite_vmps(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
+                               udmrg_tensor *const *mpo, const udmrg_sweep_params *params,
+                               double *e0, udmrg_site_log *log, int64_t log_cap,
+                               int64_t *log_len) {
+  return guarded([&] {
+    std::vector<TensorPtr> m(N);
+    for (int64_t i = 0; i < N; ++i) m[i] = T(mps[i]).clone();
+    std::vector<const BTensor *> w(N);
+    for (int64_t i = 0; i < N; ++i) w[i] = &T(mpo[i]);
+    SweepParams p;
+    p.sweeps = params->sweeps;
+    p.Dmin = params->Dmin;
+    p.Dmax = params->Dmax;
+    p.trunc_err = params->trunc_err;
+    p.lancz = {params->lancz_params.error, params->lancz_params.max_iterations};
+    std::vector<SiteLog> lg;
+    const double e = two_site_finite_vmps(c->ctx, m, w, p, &lg);
+    c->ctx.sync();
+    for (int64_t i = 0; i < N; ++i) mps[i]->t = std::move(m[i]);
+    if (e0) *e0 = e;
+    if (log_len) *log_len = (int64_t)lg.size();
+    if (log)
+      for (int64_t i = 0; i < std::min<int64_t>(log_cap, (int64_t)lg.size()); ++i) {
+        const SiteLog &s = lg[i];
+        log[i] = {s.site, s.e0, s.trunc_err, s.D, s.iters, s.ee,
+                  s.lancz_sec, s.svd_sec, s.env_sec, s.tot_sec, s.matvec_flops};
+      }
+  });
+}
+
+int udmrg_matvec_plan_create(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
+                             const udmrg_tensor *psi_struct, udmrg_matvec_plan **out) {
+  return guarded([&] {
+    Ctx &ctx = c->ctx;
+    const BTensor &psi = T(psi_struct);
+    auto p = new udmrg_matvec_plan;
+    p->ctx = &ctx;
+    const BTensor *op[4];
+    for (int i = 0; i < 4; ++i) {
+      const BTensor &t = T(eff_ham[i]);
+      if (t.dtype == psi.dtype) {
+        op[i] = &t;
+      } else {
+        p->promoted[i] = to_complex(ctx, t);
+        op[i] = p->promoted[i].get();
+      }
+    }
+    p->plan = plan_matvec2(ctx, *op[0], *op[1], *op[2], *op[3], psi);
+    *out = p;
+  });
+}
+
+int udmrg_matvec_plan_info(const udmrg_matvec_plan *p, double *flops, int64_t *psi_size,
+                           int64_t *workspace_bytes) {
+  return guarded([&] {
+    const MatvecPlan &m = *p->plan;
+    if (flops) *flops = m.flops;
+    if (psi_size) *psi_size = m.sstruct->size();
+    if (workspace_bytes)
+      *workspace_bytes = (m.p1->out->size() + m.p2->out->size() + m.p3->out->size()) *
+                         elem_doubles(m.sstruct->dtype) * (int64_t)sizeof(double);
+  });
+}
+
+int udmrg_matvec_plan_embed(udmrg_matvec_plan *p, const udmrg_tensor *src, udmrg_tensor **out) {
+  return guarded([&] { *out = wrap(embed(*p->ctx, T(src), *p->plan->sstruct)); });
+}
+
+int udmrg_matvec_plan_apply(udmrg_matvec_plan *p, const double *d_in, double *d_out) {
+  return guarded([&] { p->plan->apply(d_in, d_out); });
+}
+
+int udmrg_matvec_plan_destroy(udmrg_matvec_plan *p) {
+  return guarded([&] { delete p; });
+}
+
+}  // extern "C"

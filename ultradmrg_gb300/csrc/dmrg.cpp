@@ -1,0 +1,579 @@
+#include "dmrg.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+
+namespace udmrg {
+
+TensorPtr contract_axes(Ctx &ctx, const BTensor &A, const BTensor &B, const std::vector<int> &ca,
+                        const std::vector<int> &cb) {
+  auto p = plan_contract_axes(A, B, ca, cb);
+  return run_contract(ctx, *p, A, B);
+}
+
+TensorPtr contract_cyclic(Ctx &ctx, const BTensor &A, const BTensor &B, int a_start, int b_start,
+                          int n) {
+  auto p = plan_contract_cyclic(A, B, a_start, b_start, n);
+  return run_contract(ctx, *p, A, B);
+}
+
+TensorPtr dag(Ctx &ctx, const BTensor &A) {
+  auto t = A.clone();
+  for (auto &i : t->idx) i.dir = -i.dir;
+  if (t->dtype == kC128) conj_inplace(ctx, t->data, t->size());
+  return t;
+}
+
+TensorPtr to_complex(Ctx &ctx, const BTensor &A) {
+  auto t = A.clone_struct();
+  t->dtype = kC128;
+  t->alloc_data();
+  if (A.dtype == kC128) {
+    if (A.size())
+      UDMRG_CHECK_CUDA(cudaMemcpyAsync(t->data, A.data, A.bytes(), cudaMemcpyDeviceToDevice,
+                                       ctx.stream));
+  } else {
+    real_to_complex(ctx, A.data, t->data, A.size());
+  }
+  return t;
+}
+
+TensorPtr struct_union(const BTensor &a, const BTensor &b) {
+  UDMRG_REQUIRE(a.rank() == b.rank(), "union: rank mismatch");
+  for (int i = 0; i < a.rank(); ++i) UDMRG_REQUIRE(a.idx[i] == b.idx[i], "union: index mismatch");
+  std::vector<int32_t> flat = a.keys;
+  flat.insert(flat.end(), b.keys.begin(), b.keys.end());
+  auto t = a.clone_struct();
+  t->set_blocks(sort_keys(flat, a.rank()));
+  return t;
+}
+
+TensorPtr embed(Ctx &ctx, const BTensor &src, const BTensor &dst_struct) {
+  auto t = dst_struct.clone_struct();
+  t->dtype = src.dtype;
+  t->alloc_data();
+  t->zero_data();
+  const int es = elem_doubles(src.dtype);
+  for (int64_t b = 0; b < src.nblocks(); ++b) {
+    const int64_t d = t->find(std::vector<int32_t>(src.key(b), src.key(b) + src.rank()));
+    UDMRG_REQUIRE(d >= 0, "embed: block absent from destination structure");
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(t->data + t->offs[d] * es, src.data + src.offs[b] * es,
+                                     src.block_elems(b) * es * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, ctx.stream));
+  }
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// Matvec plan
+// ---------------------------------------------------------------------------
+
+MatvecPlan::~MatvecPlan() {
+  if (!ctx) return;
+  ctx->free(t1);
+  ctx->free(t2);
+  ctx->free(t3);
+}
+
+std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTensor &W1,
+                                         const BTensor &W2, const BTensor &R,
+                                         const BTensor &psi0) {
+  UDMRG_REQUIRE(psi0.rank() == 4 && L.rank() == 3 && R.rank() == 3 && W1.rank() == 4 &&
+                    W2.rank() == 4,
+                "matvec: expects L(3), W1(4), W2(4), R(3), psi(4)");
+  auto mv = std::make_unique<MatvecPlan>();
+  mv->ctx = &ctx;
+  mv->L = &L;
+  mv->W1 = &W1;
+  mv->W2 = &W2;
+  mv->R = &R;
+  TensorPtr S = psi0.clone_struct();
+  std::vector<int> ca, cb, fa, fb;
+  for (int it = 0; it < 16; ++it) {
+    mv->p1 = plan_contract_axes(L, *S, {2}, {0});
+    mv->p2 = plan_contract_cyclic(*mv->p1->out, W1, 1, 0, 2);
+    mv->p3 = plan_contract_cyclic(*mv->p2->out, W2, 4, 0, 2);
+    cyclic_axes(5, 3, 4, 1, 2, ca, cb, fa, fb);
+    auto p4 = plan_contract(*mv->p3->out, R, ca, cb, fa, fb);
+    auto U = struct_union(*S, *p4->out);
+    const bool closed = U->keys == S->keys;
+    S = std::move(U);
+    if (closed) break;
+    UDMRG_REQUIRE(it < 15, "matvec: Krylov block structure did not close");
+  }
+  mv->p4 = plan_contract_into(*mv->p3->out, R, ca, cb, fa, fb, *S, &mv->missing);
+  mv->sstruct = std::move(S);
+  const int es = elem_doubles(psi0.dtype);
+  mv->t1 = (double *)ctx.alloc(std::max<int64_t>(mv->p1->out->size(), 1) * es * sizeof(double));
+  mv->t2 = (double *)ctx.alloc(std::max<int64_t>(mv->p2->out->size(), 1) * es * sizeof(double));
+  mv->t3 = (double *)ctx.alloc(std::max<int64_t>(mv->p3->out->size(), 1) * es * sizeof(double));
+  mv->flops = mv->p1->gemm.flops + mv->p2->gemm.flops + mv->p3->gemm.flops + mv->p4->gemm.flops;
+  return mv;
+}
+
+void MatvecPlan::apply(const double *in, double *out) {
+  const DType dt = sstruct->dtype;
+  const int es = elem_doubles(dt);
+  run_gemm(*ctx, p1->gemm, dt, L->data, in, t1, 1.0, 0.0);
+  run_gemm(*ctx, p2->gemm, dt, t1, W1->data, t2, 1.0, 0.0);
+  run_gemm(*ctx, p3->gemm, dt, t2, W2->data, t3, 1.0, 0.0);
+  for (int64_t b : missing)
+    UDMRG_CHECK_CUDA(cudaMemsetAsync(out + sstruct->offs[b] * es, 0,
+                                     sstruct->block_elems(b) * es * sizeof(double), ctx->stream));
+  run_gemm(*ctx, p4->gemm, dt, t3, R->data, out, 1.0, 0.0);
+}
+
+// ---------------------------------------------------------------------------
+// Tridiagonal eigenproblems (host, FP64).  Implicit QL iteration with
+// Wilkinson-type shifts on a symmetric tridiagonal matrix (the method of
+// Bowdler, Martin, Reinsch and Wilkinson, Numer. Math. 11 (1968) 293).
+// ---------------------------------------------------------------------------
+
+void tridiag_eig(const std::vector<double> &a, const std::vector<double> &b, int64_t n,
+                 std::vector<double> &w, std::vector<double> &z) {
+  std::vector<double> d(a.begin(), a.begin() + n), e(n, 0.0);
+  for (int64_t i = 0; i + 1 < n; ++i) e[i] = b[i];
+  z.assign(n * n, 0.0);
+  for (int64_t i = 0; i < n; ++i) z[i * n + i] = 1.0;
+  const double eps = 2.220446049250313e-16;
+  for (int64_t l = 0; l < n; ++l) {
+    int iter = 0;
+    while (true) {
+      int64_t m = l;
+      for (; m + 1 < n; ++m) {
+        const double dd = std::fabs(d[m]) + std::fabs(d[m + 1]);
+        if (std::fabs(e[m]) <= eps * dd) break;
+      }
+      if (m == l) break;
+      if (++iter > 200) throw Error(kErrNumerics, "tridiagonal eigensolver did not converge");
+      // shift from the leading 2x2 block
+      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+      double r = std::hypot(g, 1.0);
+      g = d[m] - d[l] + e[l] / (g + (g >= 0 ? std::fabs(r) : -std::fabs(r)));
+      double s = 1.0, c = 1.0, p = 0.0;
+      bool deflated = false;
+      for (int64_t i = m - 1; i >= l; --i) {
+        double f = s * e[i], bb = c * e[i];
+        r = std::hypot(f, g);
+        e[i + 1] = r;
+        if (r == 0.0) {  // underflow: split the matrix here
+          d[i + 1] -= p;
+          e[m] = 0.0;
+          deflated = true;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = d[i + 1] - p;
+        r = (d[i] - g) * s + 2.0 * c * bb;
+        p = s * r;
+        d[i + 1] = g + p;
+        g = c * r - bb;
+        for (int64_t k = 0; k < n; ++k) {  // accumulate the rotation into z
+          const double zk1 = z[k * n + i + 1];
+          z[k * n + i + 1] = s * z[k * n + i] + c * zk1;
+          z[k * n + i] = c * z[k * n + i] - s * zk1;
+        }
+      }
+      if (deflated) continue;
+      d[l] -= p;
+      e[l] = g;
+      e[m] = 0.0;
+    }
+  }
+  // ascending order
+  std::vector<int64_t> ord(n);
+  for (int64_t i = 0; i < n; ++i) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int64_t x, int64_t y) { return d[x] < d[y]; });
+  w.resize(n);
+  std::vector<double> zs(n * n);
+  for (int64_t j = 0; j < n; ++j) {
+    w[j] = d[ord[j]];
+    for (int64_t k = 0; k < n; ++k) zs[k * n + j] = z[k * n + ord[j]];
+  }
+  z.swap(zs);
+}
+
+double tridiag_lowest(const std::vector<double> &a, const std::vector<double> &b, int64_t n,
+                      std::vector<double> *vec) {
+  std::vector<double> w, z;
+  tridiag_eig(a, b, n, w, z);
+  if (vec) {
+    vec->resize(n);
+    for (int64_t k = 0; k < n; ++k) (*vec)[k] = z[k * n];
+  }
+  return w[0];
+}
+
+std::vector<double> tridiag_expme1(const std::vector<double> &a, const std::vector<double> &b,
+                                   int64_t n, double dt) {
+  std::vector<double> w, z;
+  tridiag_eig(a, b, n, w, z);
+  std::vector<double> out(2 * n, 0.0);
+  for (int64_t j = 0; j < n; ++j) {
+    const double ph = -dt * w[j];
+    const double cr = std::cos(ph) * z[j], ci = std::sin(ph) * z[j];  // e^{-i dt w_j} z[0][j]
+    for (int64_t i = 0; i < n; ++i) {
+      out[2 * i] += z[i * n + j] * cr;
+      out[2 * i + 1] += z[i * n + j] * ci;
+    }
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+// Lanczos
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct EventTimer {
+  cudaEvent_t a, b;
+  EventTimer() {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+  }
+  ~EventTimer() {
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+};
+
+struct Bases {
+  Ctx &ctx;
+  std::vector<double *> v;
+  explicit Bases(Ctx &c) : ctx(c) {}
+  ~Bases() {
+    for (auto p : v) ctx.free(p);
+  }
+};
+
+}  // namespace
+
+LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
+                         const LanczosParams &p) {
+  const BTensor &S = *mv.sstruct;
+  const bool cplx = S.dtype == kC128;
+  const int es = elem_doubles(S.dtype);
+  const int64_t n = S.size();
+  const int64_t nd = n * es;
+  const size_t vbytes = std::max<int64_t>(nd, 1) * sizeof(double);
+  // eff_ham_eff_dim: element count of the initial state
+  const int64_t eff_dim = init_state.size();
+  const int64_t maxit = p.max_iterations;
+  VecWork w(ctx);
+  Bases bases(ctx);
+  std::vector<double> a(maxit, 0.0), b(maxit, 0.0), N(maxit, 0.0);
+  LanczosResult res;
+  EventTimer ev;
+  float ms = 0;
+  auto matvec = [&](const double *in) {
+    double *out = (double *)ctx.alloc(vbytes);
+    cudaEventRecord(ev.a, ctx.stream);
+    mv.apply(in, out);
+    cudaEventRecord(ev.b, ctx.stream);
+    UDMRG_CHECK_CUDA(cudaEventSynchronize(ev.b));
+    cudaEventElapsedTime(&ms, ev.a, ev.b);
+    res.matvec_seconds += ms * 1e-3;
+    res.matvecs++;
+    return out;
+  };
+  auto finish = [&](int64_t m, const std::vector<double> &vec) {
+    auto gs = S.clone_struct();
+    gs->alloc_data();
+    std::vector<const double *> vs(bases.v.begin(), bases.v.begin() + m);
+    std::vector<double> coef;
+    for (int64_t i = 0; i < m; ++i) {
+      coef.push_back(vec[i]);
+      if (cplx) coef.push_back(0.0);
+    }
+    if (cplx) {
+      lincomb(w, gs->data, vs, coef, n, true);
+    } else {
+      lincomb(w, gs->data, vs, coef, n, false);
+    }
+    return gs;
+  };
+  // bases[0] = init / |init| (QuasiNormalize)
+  {
+    auto v0 = embed(ctx, init_state, S);
+    double *d0 = (double *)ctx.alloc(vbytes);
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(d0, v0->data, nd * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     ctx.stream));
+    const double nrm = std::sqrt(norm2(w, d0, nd));
+    if (nrm != 0.0) scale(ctx, d0, nd, 1.0 / nrm);
+    bases.v.push_back(d0);
+  }
+  double *last = matvec(bases.v[0]);
+  a[0] = dot(w, bases.v[0], last, n, cplx).real();
+  N[0] = 0.0;
+  int64_t m = 0;
+  double energy0 = a[0];
+  double *hres = ctx.host_scratch(4);
+  while (true) {
+    m += 1;
+    double *gamma = last;
+    lanczos_update_async(w, gamma, bases.v[m - 1], m == 1 ? nullptr : bases.v[m - 2], a[m - 1],
+                         m == 1 ? 0.0 : std::sqrt(N[m - 1]), nd, w.result);
+    UDMRG_CHECK_CUDA(
+        cudaMemcpyAsync(hres, w.result, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.sync();
+    const double norm_gamma = std::sqrt(hres[0]);
+    if (norm_gamma == 0.0) {
+      ctx.free(gamma);
+      if (m == 1) {
+        res.iters = m;
+        res.gs_eng = energy0;
+        res.gs_vec = finish(1, {1.0});
+        return res;
+      }
+      std::vector<double> vec;
+      tridiag_lowest(a, b, m, &vec);
+      res.iters = m;
+      res.gs_eng = energy0;
+      res.gs_vec = finish(m, vec);
+      return res;
+    }
+    scale(ctx, gamma, nd, 1.0 / norm_gamma);
+    N[m] = norm_gamma * norm_gamma;
+    b[m - 1] = norm_gamma;
+    bases.v.push_back(gamma);
+    last = matvec(bases.v[m]);
+    a[m] = dot(w, bases.v[m], last, n, cplx).real();
+    const double e_new = tridiag_lowest(a, b, m + 1, nullptr);
+    if ((energy0 - e_new) < p.error || m == eff_dim || m == maxit - 1) {
+      std::vector<double> vec;
+      tridiag_lowest(a, b, m + 1, &vec);
+      ctx.free(last);
+      res.iters = m + 1;
+      res.gs_eng = e_new;
+      res.gs_vec = finish(m + 1, vec);
+      return res;
+    }
+    energy0 = e_new;
+  }
+}
+
+ExpmvResult lanczos_expmv(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state, double step,
+                          const LanczosParams &p) {
+  const BTensor &S = *mv.sstruct;
+  UDMRG_REQUIRE(S.dtype == kC128, "expmv: complex state required");
+  const int64_t n = S.size();
+  const int64_t nd = 2 * n;
+  const size_t vbytes = std::max<int64_t>(nd, 1) * sizeof(double);
+  const int64_t eff_dim = init_state.size();
+  const int64_t maxit = p.max_iterations;
+  VecWork w(ctx);
+  Bases bases(ctx);
+  std::vector<double> a(maxit, 0.0), b(maxit, 0.0);
+  ExpmvResult res;
+  auto combine = [&](int64_t m, const std::vector<double> &coef_il) {
+    auto out = S.clone_struct();
+    out->alloc_data();
+    std::vector<const double *> vs(bases.v.begin(), bases.v.begin() + m);
+    lincomb(w, out->data, vs, coef_il, n, true);
+    return out;
+  };
+  double initial_norm;
+  {
+    auto v0 = embed(ctx, init_state, S);
+    double *d0 = (double *)ctx.alloc(vbytes);
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(d0, v0->data, nd * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     ctx.stream));
+    initial_norm = std::sqrt(norm2(w, d0, nd));
+    if (initial_norm != 0.0) scale(ctx, d0, nd, 1.0 / initial_norm);
+    bases.v.push_back(d0);
+  }
+  auto matvec = [&](const double *in) {
+    double *out = (double *)ctx.alloc(vbytes);
+    mv.apply(in, out);
+    return out;
+  };
+  double *last = matvec(bases.v[0]);
+  a[0] = dot(w, bases.v[0], last, n, true).real();
+  int64_t m = 0;
+  std::vector<double> last_coef(2 * maxit, 0.0);
+  double *hres = ctx.host_scratch(4);
+  while (true) {
+    m += 1;
+    double *gamma = last;
+    lanczos_update_async(w, gamma, bases.v[m - 1], m == 1 ? nullptr : bases.v[m - 2], a[m - 1],
+                         m == 1 ? 0.0 : b[m - 2], nd, w.result);
+    UDMRG_CHECK_CUDA(
+        cudaMemcpyAsync(hres, w.result, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.sync();
+    const double norm_gamma = std::sqrt(hres[0]);
+    if (norm_gamma == 0.0) {
+      ctx.free(gamma);
+      res.iters = m;
+      if (m == 1) {
+        const double ph = -step * a[0];
+        res.expmv = combine(1, {initial_norm * std::cos(ph), initial_norm * std::sin(ph)});
+      } else {
+        auto c = tridiag_expme1(a, b, m, step);
+        for (auto &x : c) x *= initial_norm;
+        res.expmv = combine(m, c);
+      }
+      return res;
+    }
+    scale(ctx, gamma, nd, 1.0 / norm_gamma);
+    b[m - 1] = norm_gamma;
+    bases.v.push_back(gamma);
+    last = matvec(bases.v[m]);
+    a[m] = dot(w, bases.v[m], last, n, true).real();
+    auto coef = tridiag_expme1(a, b, m + 1, step);
+    double dist = 0;
+    for (int64_t i = 0; i < m + 1; ++i) {
+      const double dr = coef[2 * i] - last_coef[2 * i], di = coef[2 * i + 1] - last_coef[2 * i + 1];
+      dist += dr * dr + di * di;
+    }
+    dist = std::sqrt(dist);
+    if (dist < p.error || m == eff_dim || m == maxit - 1) {
+      ctx.free(last);
+      for (auto &x : coef) x *= initial_norm;
+      res.iters = m + 1;
+      res.expmv = combine(m + 1, coef);
+      return res;
+    }
+    std::fill(last_coef.begin(), last_coef.end(), 0.0);
+    std::copy(coef.begin(), coef.end(), last_coef.begin());
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Environments
+// ---------------------------------------------------------------------------
+
+TensorPtr update_site_lenv(Ctx &ctx, const BTensor &lenv, const BTensor &A, const BTensor &W) {
+  auto Ad = dag(ctx, A);
+  auto t = contract_cyclic(ctx, lenv, A, 2, 0, 1);
+  auto t2 = contract_cyclic(ctx, *t, W, 1, 0, 2);
+  t.reset();
+  return contract_cyclic(ctx, *Ad, *t2, 0, 1, 2);
+}
+
+TensorPtr update_site_renv(Ctx &ctx, const BTensor &renv, const BTensor &A, const BTensor &W) {
+  auto Ad = dag(ctx, A);
+  auto t = contract_cyclic(ctx, *Ad, renv, 2, 0, 1);
+  auto t2 = contract_cyclic(ctx, *t, W, 1, 2, 2);
+  t.reset();
+  return contract_cyclic(ctx, *t2, A, 3, 1, 2);
+}
+
+static TensorPtr trivial_env(Ctx &ctx, const Index &i0, const Index &iw, DType dt) {
+  auto t = std::make_unique<BTensor>();
+  t->ctx = &ctx;
+  t->dtype = dt;
+  t->idx = {i0, iw, i0.inverse()};
+  UDMRG_REQUIRE(i0.nsec() == 1 && i0.dims[0] == 1 && iw.nsec() == 1 && iw.dims[0] == 1,
+                "trivial env: boundary indexes must be one-dimensional");
+  t->set_blocks({0, 0, 0});
+  t->alloc_data();
+  double one[2] = {1.0, 0.0};
+  UDMRG_CHECK_CUDA(cudaMemcpyAsync(t->data, one, elem_doubles(dt) * sizeof(double),
+                                   cudaMemcpyHostToDevice, ctx.stream));
+  ctx.sync();
+  return t;
+}
+
+TensorPtr trivial_renv(Ctx &ctx, const BTensor &mps_last, const BTensor &mpo_last) {
+  auto t = trivial_env(ctx, mps_last.idx[2], mpo_last.idx[3].inverse(), mps_last.dtype);
+  t->nq = mps_last.nq;
+  return t;
+}
+
+TensorPtr trivial_lenv(Ctx &ctx, const BTensor &mps_first, const BTensor &mpo_first) {
+  auto t = trivial_env(ctx, mps_first.idx[0], mpo_first.idx[0].inverse(), mps_first.dtype);
+  t->nq = mps_first.nq;
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// Sweeps
+// ---------------------------------------------------------------------------
+
+static double now() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+static double two_site_update(Ctx &ctx, std::vector<TensorPtr> &mps,
+                              std::vector<TensorPtr> &lenvs, std::vector<TensorPtr> &renvs,
+                              const std::vector<const BTensor *> &mpo, const SweepParams &p,
+                              char dir, int64_t target, std::vector<SiteLog> *log) {
+  const int64_t N = (int64_t)mps.size();
+  int64_t l, r, lenv_len, renv_len;
+  if (dir == 'r') {
+    l = target;
+    r = target + 1;
+    lenv_len = target;
+    renv_len = N - (target + 2);
+  } else {
+    l = target - 1;
+    r = target;
+    lenv_len = target - 1;
+    renv_len = N - target - 1;
+  }
+  const double t0 = now();
+  auto init_state = contract_axes(ctx, *mps[l], *mps[r], {2}, {0});
+  auto mv = plan_matvec2(ctx, *lenvs[lenv_len], *mpo[l], *mpo[r], *renvs[renv_len], *init_state);
+  auto lres = lanczos_gs(ctx, *mv, *init_state, p.lancz);
+  const double t1 = now();
+  const double mvflops = mv->flops;
+  mv.reset();
+  init_state.reset();
+  const QN ldiv = mps[l]->div();
+  auto sres = svd_trunc(ctx, *lres.gs_vec, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax,
+                        dir == 'r' ? kSvdSplitLeft : kSvdSplitRight);
+  lres.gs_vec.reset();
+  mps[l] = std::move(sres.u);
+  mps[r] = std::move(sres.vt);
+  ctx.sync();
+  const double t2 = now();
+  if (dir == 'r')
+    lenvs[lenv_len + 1] = update_site_lenv(ctx, *lenvs[lenv_len], *mps[target], *mpo[target]);
+  else
+    renvs[renv_len + 1] = update_site_renv(ctx, *renvs[renv_len], *mps[target], *mpo[target]);
+  ctx.sync();
+  const double t3 = now();
+  if (log)
+    log->push_back({target, lres.gs_eng, sres.trunc_err, sres.D, lres.iters, sres.ee, t1 - t0,
+                    t2 - t1, t3 - t2, t3 - t0, mvflops});
+  return lres.gs_eng;
+}
+
+double two_site_finite_vmps(Ctx &ctx, std::vector<TensorPtr> &mps,
+                            const std::vector<const BTensor *> &mpo, const SweepParams &p,
+                            std::vector<SiteLog> *log) {
+  const int64_t N = (int64_t)mps.size();
+  UDMRG_REQUIRE(N >= 3 && (int64_t)mpo.size() == N, "vmps: MPS and MPO sizes differ or N < 3");
+  // mixed element types: promote real MPO / MPS to complex
+  bool cplx = false;
+  for (auto &t : mps) cplx |= t->dtype == kC128;
+  for (auto *t : mpo) cplx |= t->dtype == kC128;
+  std::vector<TensorPtr> mpo_c;
+  std::vector<const BTensor *> W = mpo;
+  if (cplx) {
+    for (auto &t : mps)
+      if (t->dtype != kC128) t = to_complex(ctx, *t);
+    for (int64_t i = 0; i < N; ++i)
+      if (mpo[i]->dtype != kC128) {
+        mpo_c.push_back(to_complex(ctx, *mpo[i]));
+        W[i] = mpo_c.back().get();
+      }
+  }
+  std::vector<TensorPtr> lenvs(N), renvs(N);
+  renvs[0] = trivial_renv(ctx, *mps[N - 1], *W[N - 1]);
+  for (int64_t i = 1; i <= N - 2; ++i)
+    renvs[i] = update_site_renv(ctx, *renvs[i - 1], *mps[N - i], *W[N - i]);
+  lenvs[0] = trivial_lenv(ctx, *mps[0], *W[0]);
+  double e0 = 0;
+  for (int64_t s = 0; s < p.sweeps; ++s) {
+    for (int64_t i = 0; i < N - 2; ++i) e0 = two_site_update(ctx, mps, lenvs, renvs, W, p, 'r', i, log);
+    for (int64_t i = N - 1; i > 1; --i) e0 = two_site_update(ctx, mps, lenvs, renvs, W, p, 'l', i, log);
+  }
+  return e0;
+}
+
+}  // namespace udmrg

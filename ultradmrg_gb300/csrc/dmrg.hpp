@@ -1,0 +1,105 @@
+// Two-site update: matvec plan, Lanczos solvers, environment updates, sweeps.
+#pragma once
+
+#include "svd.hpp"
+
+namespace udmrg {
+
+// Block-sparse ops built on plan + run.
+TensorPtr contract_axes(Ctx &ctx, const BTensor &A, const BTensor &B, const std::vector<int> &ca,
+                        const std::vector<int> &cb);
+TensorPtr contract_cyclic(Ctx &ctx, const BTensor &A, const BTensor &B, int a_start, int b_start,
+                          int n);
+TensorPtr dag(Ctx &ctx, const BTensor &A);
+TensorPtr to_complex(Ctx &ctx, const BTensor &A);
+// Same data laid out in the (superset) structure `dst` (missing blocks zero).
+TensorPtr embed(Ctx &ctx, const BTensor &src, const BTensor &dst_struct);
+// Union of two block structures over identical indexes (structure only).
+TensorPtr struct_union(const BTensor &a, const BTensor &b);
+
+// H_eff * psi for fixed (L, W1, W2, R), with psi and the result in one
+// "Krylov structure": the smallest block set containing psi0's blocks that is
+// closed under the matvec.  Reference: eff_ham_mul_two_site_state,
+// algorithm/vmps/lanczos_vmps_solver_impl.h:260-289 (same four contractions).
+struct MatvecPlan {
+  Ctx *ctx = nullptr;
+  const BTensor *L = nullptr, *W1 = nullptr, *W2 = nullptr, *R = nullptr;
+  TensorPtr sstruct;  // the Krylov structure (no data)
+  std::unique_ptr<ContractPlan> p1, p2, p3, p4;
+  std::vector<int64_t> missing;  // blocks of sstruct the matvec does not write
+  double *t1 = nullptr, *t2 = nullptr, *t3 = nullptr;
+  double flops = 0;  // algorithmic flops of one matvec
+  ~MatvecPlan();
+  void apply(const double *in, double *out);  // device buffers in sstruct layout
+};
+
+std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTensor &W1,
+                                         const BTensor &W2, const BTensor &R,
+                                         const BTensor &psi0);
+
+struct LanczosParams {
+  double error = 1e-7;
+  int64_t max_iterations = 200;
+};
+
+struct LanczosResult {
+  int64_t iters = 0;
+  double gs_eng = 0;
+  TensorPtr gs_vec;
+  double matvec_seconds = 0;  // device time spent in matvecs (CUDA events)
+  int64_t matvecs = 0;
+};
+
+// Ground state by Lanczos (lanczos_vmps_solver_impl.h:114-248): three-term
+// recurrence without reorthogonalisation, all bases kept on the device,
+// FP64 tridiagonal eigenproblem on the host.
+LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
+                         const LanczosParams &p);
+
+// exp(-i dt H_eff) psi (lanczos_expmv_solver_impl.h:70-184).
+struct ExpmvResult {
+  int64_t iters = 0;
+  TensorPtr expmv;
+};
+ExpmvResult lanczos_expmv(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state, double step,
+                          const LanczosParams &p);
+
+// Host tridiagonal eigen-solver (implicit QL with shifts).  Returns the lowest
+// eigenvalue; if vec != nullptr, the matching normalised eigenvector.
+double tridiag_lowest(const std::vector<double> &a, const std::vector<double> &b, int64_t n,
+                      std::vector<double> *vec);
+// All eigenpairs (ascending); z is row-major n x n with eigenvectors as columns.
+void tridiag_eig(const std::vector<double> &a, const std::vector<double> &b, int64_t n,
+                 std::vector<double> &w, std::vector<double> &z);
+// exp(-i dt T) e1 for tridiagonal T (interleaved complex output).
+std::vector<double> tridiag_expme1(const std::vector<double> &a, const std::vector<double> &b,
+                                   int64_t n, double dt);
+
+// Environment updates (algorithm/vmps/vmps_init.h:343-373).
+TensorPtr update_site_lenv(Ctx &ctx, const BTensor &lenv, const BTensor &A, const BTensor &W);
+TensorPtr update_site_renv(Ctx &ctx, const BTensor &renv, const BTensor &A, const BTensor &W);
+TensorPtr trivial_renv(Ctx &ctx, const BTensor &mps_last, const BTensor &mpo_last);
+TensorPtr trivial_lenv(Ctx &ctx, const BTensor &mps_first, const BTensor &mpo_first);
+
+struct SweepParams {
+  int64_t sweeps = 1;
+  int64_t Dmin = 1, Dmax = 1;
+  double trunc_err = 0;
+  LanczosParams lancz;
+};
+
+struct SiteLog {
+  int64_t site;
+  double e0, trunc_err;
+  int64_t D, iters;
+  double ee, lancz_sec, svd_sec, env_sec, tot_sec;
+  double matvec_flops;
+};
+
+// TwoSiteFiniteVMPS (two_site_update_finite_vmps_impl.h:95-494), device
+// resident: mps tensors are replaced in place; returns the last energy.
+double two_site_finite_vmps(Ctx &ctx, std::vector<TensorPtr> &mps,
+                            const std::vector<const BTensor *> &mpo, const SweepParams &p,
+                            std::vector<SiteLog> *log);
+
+}  // namespace udmrg

@@ -482,6 +482,113 @@ def direct_product_mps(sites: Sequence[Index], labels: Sequence[int], dtype=np.f
     return mps
 
 
+def _qn_sum_counts(sites: Sequence[Index]):
+    """counts[b][q] = number of product states of sites[0..b] with QN sum q."""
+    out = []
+    cur = {tuple(0 for _ in range(sites[0].nq)): 1.0}
+    for ind in sites:
+        nxt = {}
+        for q, c in cur.items():
+            for sq, d in zip(ind.qns, ind.dims):
+                k = tuple(a + b for a, b in zip(q, sq))
+                nxt[k] = nxt.get(k, 0.0) + c * d
+        out.append(nxt)
+        cur = nxt
+    return out
+
+
+def bond_sectors(sites: Sequence[Index], div, D: int, sigma: float = 2.5):
+    """Bond QN sectors of an MPS with total QN ``div`` and bond dimension <= D.
+
+    Bond b (right of site b) carries r = div - sum_{i<=b} q_i (the convention of
+    ``DirectStateInitMps``).  A sector's weight is a Gaussian of width ``sigma``
+    (in QN units) around the mean filling of the right block, the shape of the
+    Schmidt-spectrum weight of a converged ground state; the dimensions are the
+    weights scaled to fit D, never above c (the smaller of the numbers of left
+    and right product states with that QN) and at least 1 for kept sectors.
+    """
+    N = len(sites)
+    left = _qn_sum_counts(sites)
+    right = _qn_sum_counts(list(reversed(sites)))
+    bonds = []
+    for b in range(N - 1):
+        cl, cr = left[b], right[N - 2 - b]
+        sec = {}
+        for ql, c in cl.items():
+            r = qn_sub(div, ql)
+            if r in cr:
+                sec[r] = min(c, cr[r])
+        qs = sorted(sec)
+        cnt = np.array([sec[q] for q in qs], dtype=float)
+        if cnt.sum() <= D:
+            dims = cnt
+        else:
+            mean = np.array(div, dtype=float) * (N - 1 - b) / N
+            d2 = np.array([np.sum((np.array(q, dtype=float) - mean) ** 2) for q in qs])
+            w = np.exp(-d2 / (2.0 * sigma ** 2))
+            keep_min = w > 1e-3 * w.max()
+            w = np.where(keep_min, w, 0.0)
+            order = np.argsort(-w, kind="stable")
+            keep = np.zeros(len(qs), bool)
+            keep[order[:D]] = True
+            keep &= w > 0
+            dims = np.zeros(len(qs))
+            budget = D
+            # water-filling: sectors capped by their count, the rest share the budget
+            active = keep.copy()
+            while True:
+                share = budget / w[active].sum()
+                cand = np.where(active, np.floor(w * share), 0)
+                capped = active & (cand >= cnt)
+                if not capped.any():
+                    dims[active] = np.maximum(1, cand[active])
+                    break
+                dims[capped] = cnt[capped]
+                budget -= cnt[capped].sum()
+                active &= ~capped
+            while dims.sum() > D:
+                dims[np.argmax(dims)] -= 1
+        bonds.append([(q, int(d)) for q, d in zip(qs, dims) if d > 0])
+    return bonds
+
+
+def random_mps(sites: Sequence[Index], div, D: int, seed: int = 0, dtype=np.float64,
+               sigma: float = 2.5):
+    """Random MPS with the block structure of ``bond_sectors`` (site 0 carries the
+    divergence); each tensor is scaled to squared norm min(D_l*d, D_r)."""
+    rng = np.random.default_rng(seed)
+    N = len(sites)
+    bonds = bond_sectors(sites, div, D, sigma)
+    zero = tuple(0 for _ in range(sites[0].nq))
+    mps = []
+    for i in range(N):
+        lvb = Index.make([(zero, 1)], IN) if i == 0 else Index.make(bonds[i - 1], OUT).inverse()
+        rvb = Index.make([(zero, 1)], OUT) if i == N - 1 else Index.make(bonds[i], OUT)
+        A = BlockTensorData([lvb, sites[i], rvb], {}, dtype)
+        target = div if i == 0 else zero
+        rpos = {q: s for s, q in enumerate(rvb.qns)}
+        for li, lq in enumerate(lvb.qns):
+            for pi, pq in enumerate(sites[i].qns):
+                # Div = -lq + pq + rq = target
+                rq = tuple(t + a - b for t, a, b in zip(target, lq, pq))
+                ri = rpos.get(rq)
+                if ri is None:
+                    continue
+                shp = (lvb.dims[li], sites[i].dims[pi], rvb.dims[ri])
+                blk = rng.standard_normal(shp)
+                if dtype == np.complex128:
+                    blk = blk + 1j * rng.standard_normal(shp)
+                A.blocks[(li, pi, ri)] = blk.astype(dtype)
+        nrm2 = sum(np.vdot(b, b).real for b in A.blocks.values())
+        want = min(lvb.dim * sites[i].dim, rvb.dim)
+        if nrm2 > 0:
+            s = np.sqrt(want / nrm2)
+            for k in A.blocks:
+                A.blocks[k] = A.blocks[k] * s
+        mps.append(A)
+    return mps
+
+
 def random_sz0_labels(N, seed):
     """Random half-up / half-down spin labels (total Sz=0) from numpy's PCG64."""
     rng = np.random.Generator(np.random.PCG64(seed))
