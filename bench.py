@@ -1,0 +1,363 @@
+#!/usr/bin/env python
+"""Benchmark of the two-site DMRG hot path: H_eff * psi (L.W.W.R.psi) over
+U(1)xU(1) block-sparse tensors, the matvec inside Lanczos.
+
+One step = one matvec at the centre bond of the workload (default: Hubbard
+4x16 cylinder, 1/8 doping, D=2000; synthetic seeded inputs, see
+``ultradmrg_gb300/workloads.py``).  ``value`` is matvec TFLOP/s with the
+inputs resident in HBM (device time, CUDA events on the library's stream,
+L2 flushed before every step); ``e2e`` is the same metric through the C ABI
+with host buffers (pinned host -> device copy of psi, matvec, device -> host
+copy of the result, every step).  FLOPs are algorithmic: sum of 2*M*N*K over
+the block-pair GEMMs of the schedule.
+
+``--impl reference`` times the CPU FP64 oracle (numpy + OpenBLAS, all host
+threads) on the same workload; the reference's own C++ path cannot be built
+here (its tensor library is not vendored).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "two-site matvec TFLOP/s (H_eff*psi, U(1)xU(1) block-sparse, FP64)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="hubbard4x16_D2000")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0,
+                    help="seconds of CPU work for the cpu_baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+# ---------------------------------------------------------------------------
+# CPU side (oracle) -- the cpu_baseline leg and the reference arm
+# ---------------------------------------------------------------------------
+
+def cpu_problem(w):
+    """Host inputs of the workload built with the oracle's environment updates."""
+    from oracle import blocksparse as bs
+    from oracle import vmps as ovmps
+    from ultradmrg_gb300.workloads import build_host
+
+    mpo, mps = build_host(w)
+    l = w.centre
+    N = w.N
+    L = ovmps.trivial_lenv(mps[0], mpo[0])
+    for i in range(l):
+        L = ovmps.update_site_lenvs(L, mps[i], mpo[i])
+        L = bs.scale(L, 1.0 / max(bs.norm(L), 1e-300))
+    R = ovmps.trivial_renv(mps[N - 1], mpo[N - 1])
+    for i in range(N - 1, l + 1, -1):
+        R = ovmps.update_site_renvs(R, mps[i], mpo[i])
+        R = bs.scale(R, 1.0 / max(bs.norm(R), 1e-300))
+    psi = bs.contract(mps[l], mps[l + 1], [2], [0])
+    return [L, mpo[l], mpo[l + 1], R], psi
+
+
+def cpu_matvec_sample(eff, psi, budget_s):
+    """Time the oracle matvec; if one full matvec exceeds the budget, time it on
+    a subset of the left environment's bra sectors (a proportional sample)."""
+    from oracle import blocksparse as bs
+    from oracle import krylov
+
+    L = eff[0]
+    bra = sorted({k[0] for k in L.blocks})
+    frac = 1.0
+    for _ in range(6):
+        keep = set(bra[::max(1, int(round(1 / frac)))]) if frac < 1 else set(bra)
+        Ls = bs.T(list(L.indexes), {k: v for k, v in L.blocks.items() if k[0] in keep}, L.dtype)
+        bs.FLOPS[0] = 0.0
+        t0 = time.perf_counter()
+        krylov.eff_ham_mul_two_site_state([Ls] + list(eff[1:]), psi)
+        dt = time.perf_counter() - t0
+        if dt <= budget_s or frac < 0.02:
+            return bs.FLOPS[0], dt, len(keep), len(bra)
+        frac = frac * max(0.05, budget_s / dt * 0.8)
+    return bs.FLOPS[0], dt, len(keep), len(bra)
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count()
+
+
+def run_reference(args):
+    from ultradmrg_gb300.workloads import WORKLOADS
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import blocksparse as bs
+    from oracle import krylov
+
+    w = WORKLOADS[args.workload]
+    eff, psi = cpu_problem(w)
+    # size each step so that warm-up + steps stay within about two minutes
+    per_step = max(2.0, min(args.cpu_budget, 120.0 / max(1, args.steps + args.warmup)))
+    flops, dt, kept, nbra = cpu_matvec_sample(eff, psi, per_step)
+    L = eff[0]
+    bra = sorted({k[0] for k in L.blocks})
+    keep = set(bra[::max(1, int(round(nbra / max(kept, 1))))])
+    Ls = bs.T(list(L.indexes), {k: v for k, v in L.blocks.items() if k[0] in keep}, L.dtype)
+    times = []
+    for i in range(args.warmup + args.steps):
+        bs.FLOPS[0] = 0.0
+        t0 = time.perf_counter()
+        krylov.eff_ham_mul_two_site_state([Ls] + list(eff[1:]), psi)
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            times.append(t1 - t0)
+            flops = bs.FLOPS[0]
+    kept = len(keep)
+    tot = sum(times)
+    val = flops * len(times) / tot / 1e12
+    sample = (f"oracle matvec (numpy/OpenBLAS FP64) on {kept}/{nbra} bra sectors of the "
+              f"left environment of {w.name}")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "TFLOP/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random MPS, sector model)",
+        "config": {"workload": w.name, "D": w.D, "sites": w.N, "bond": w.centre,
+                   "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": cpu_threads(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args):
+    import numpy as np
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("gloo")
+    from ultradmrg_gb300 import api, build
+    from ultradmrg_gb300.workloads import WORKLOADS, build_host
+
+    if rank == 0 or ws == 1:
+        build.build()
+    if ws > 1:
+        tdist.barrier()
+    w = WORKLOADS[args.workload]
+    ctx = api.Context(local)
+    mpo, mps = build_host(w)
+    l = w.centre
+    L, R = api.build_envs(ctx, mpo, mps, l)
+    A1 = api.DeviceTensor.from_data(ctx, mps[l])
+    A2 = api.DeviceTensor.from_data(ctx, mps[l + 1])
+    psi = api.contract(ctx, A1, A2, [2], [0])
+    W1 = api.DeviceTensor.from_data(ctx, mpo[l])
+    W2 = api.DeviceTensor.from_data(ctx, mpo[l + 1])
+    t0 = time.perf_counter()
+    plan = api.MatvecPlan(ctx, [L, W1, W2, R], psi)
+    plan_s = time.perf_counter() - t0
+    info = plan.info()
+    x = plan.embed(psi)
+    y = plan.embed(psi)
+    xp, yp = x.device_ptr(), y.device_ptr()
+    flops = info["flops"]
+    nbytes = info["psi_size"] * 8
+
+    def step():
+        plan.apply_ptr(xp, yp)
+
+    for _ in range(args.warmup):
+        ctx.flush_l2()
+        step()
+    ctx.sync()
+    if ws > 1:
+        tdist.barrier()
+    l0 = ctx.launches()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for i in range(args.steps):
+            ctx.flush_l2()
+            ctx.event(2 * i)
+            step()
+            ctx.event(2 * i + 1)
+        ctx.sync()
+        wall = time.perf_counter() - wall0
+    launches = ctx.launches() - l0
+    dev_ms = sum(ctx.elapsed_ms(2 * i, 2 * i + 1) for i in range(args.steps))
+    t_step = dev_ms / 1e3 / args.steps
+    if ws > 1:
+        import torch
+        tt = torch.tensor([t_step], dtype=torch.float64)
+        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+        t_step = float(tt.item())
+    value = ws * flops / t_step / 1e12
+
+    # e2e through the C ABI with host buffers
+    try:
+        import torch
+        hx = torch.empty(info["psi_size"], dtype=torch.float64, pin_memory=True)
+        hy = torch.empty(info["psi_size"], dtype=torch.float64, pin_memory=True)
+        hxp, hyp = hx.data_ptr(), hy.data_ptr()
+    except Exception:  # noqa: BLE001 - pinned memory unavailable
+        hx = np.zeros(info["psi_size"])
+        hy = np.zeros(info["psi_size"])
+        hxp, hyp = hx.ctypes.data, hy.ctypes.data
+    import ctypes
+    from ultradmrg_gb300 import _lib
+    x.download_packed()  # warm the path
+    for _ in range(2):
+        _lib.call("udmrg_tensor_upload", x.h, ctypes.cast(hxp, _lib.c_double_p))
+        step()
+        _lib.call("udmrg_tensor_download", y.h, ctypes.cast(hyp, _lib.c_double_p))
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        _lib.call("udmrg_tensor_upload", x.h, ctypes.cast(hxp, _lib.c_double_p))
+        step()
+        _lib.call("udmrg_tensor_download", y.h, ctypes.cast(hyp, _lib.c_double_p))
+    e2e_t = (time.perf_counter() - e0) / args.steps
+    if ws > 1:
+        tt = torch.tensor([e2e_t], dtype=torch.float64)
+        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+        e2e_t = float(tt.item())
+    e2e_val = ws * flops / e2e_t / 1e12
+
+    fp64_peak = ctx.fp64_peak_tflops()
+    peaks = measured_peaks()
+    line = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded random MPS with a Gaussian QN-sector model; environments "
+                "by device environment updates)",
+        "config": {"workload": w.name, "D": w.D, "sites": w.N, "bond": l,
+                   "psi_elements": info["psi_size"], "mpo_bond_dim": mpo[l].indexes[3].dim,
+                   "parallelism": "replicas only" if ws > 1 else "single GPU",
+                   "l2": "flushed (512 MB write) before every timed step",
+                   "plan_seconds": plan_s},
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_val, "unit": "TFLOP/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes},
+        "roofline": {"bound": "fp64", "pipe": "FP64 FMA (grouped block GEMM)",
+                     "achieved": flops / t_step / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": flops / t_step / 1e12 / fp64_peak, "traffic": None,
+                     "peak_source": "measured in this run by the library's DFMA probe "
+                                    "(MEASURED_PEAKS.json has no FP64 entry)",
+                     "hbm_peak_gbs_measured": peaks.get("hbm_gbs")},
+        "clocks": clk.summary(),
+        "wall_seconds_timed": wall,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        eff, hpsi = cpu_problem(w)
+        cf, ct, kept, nbra = cpu_matvec_sample(eff, hpsi, args.cpu_budget)
+        line["cpu_baseline"] = {
+            "value": cf / ct / 1e12, "unit": "TFLOP/s", "cores": cpu_threads(), "kind": "port",
+            "sample": f"one oracle matvec (numpy/OpenBLAS FP64) over {kept}/{nbra} bra sectors "
+                      f"of the left environment, {ct:.1f} s"}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        tdist.barrier()
+        tdist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

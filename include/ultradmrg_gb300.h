@@ -91,6 +91,10 @@ int udmrg_tensor_upload(udmrg_tensor *t, const double *host);
 int udmrg_tensor_download(const udmrg_tensor *t, double *host);
 /* Device address of the packed data (for device-resident callers). */
 int udmrg_tensor_device_ptr(const udmrg_tensor *t, double **dptr);
+/* 2-norm of the data, and in-place scaling by a real factor
+ * (the Normalize()/QuasiNormalize() building blocks of qlten). */
+int udmrg_tensor_norm(udmrg_ctx *ctx, const udmrg_tensor *t, double *norm);
+int udmrg_tensor_scale(udmrg_ctx *ctx, udmrg_tensor *t, double alpha);
 
 /* ---- block-sparse operations ---------------------------------------- */
 /* Contract(A, B, {axes_a, axes_b}, C): output = A's free axes then B's. */
@@ -149,6 +153,17 @@ int udmrg_matvec_plan_embed(udmrg_matvec_plan *p, const udmrg_tensor *src, udmrg
 /* out = H_eff * in on device buffers laid out in the Krylov structure. */
 int udmrg_matvec_plan_apply(udmrg_matvec_plan *p, const double *d_in, double *d_out);
 int udmrg_matvec_plan_destroy(udmrg_matvec_plan *p);
+
+/* ---- measurement ---------------------------------------------------- */
+/* FP64 FMA throughput of the device (TFLOP/s), measured by a DFMA-bound
+ * kernel; the roofline denominator of the plain FP64 block GEMMs. */
+int udmrg_probe_fp64_tflops(udmrg_ctx *ctx, double *tflops);
+/* CUDA events on the context's stream (slot in [0, 1024)), elapsed ms
+ * between two recorded slots, and an L2 flush (a write of `bytes` bytes to
+ * a scratch buffer, stream ordered) for cold-cache timing. */
+int udmrg_ctx_event_record(udmrg_ctx *ctx, int slot);
+int udmrg_ctx_event_elapsed(udmrg_ctx *ctx, int slot_a, int slot_b, float *ms);
+int udmrg_ctx_flush_l2(udmrg_ctx *ctx, int64_t bytes);
 
 #ifdef __cplusplus
 }

@@ -30,6 +30,10 @@ from ultradmrg_gb300.tensor_data import BlockTensorData, Index
 
 T = BlockTensorData
 
+# algorithmic flop counter of block contractions: 2*M*N*K per block pair
+# (x4 for complex data), the same count the device schedule reports
+FLOPS = [0.0]
+
 
 def zeros_like_struct(t: T) -> T:
     return T(list(t.indexes), {k: np.zeros_like(v) for k, v in t.blocks.items()}, t.dtype)
@@ -56,11 +60,15 @@ def contract(a: T, b: T, axes_a: Sequence[int], axes_b: Sequence[int],
     for kb in b.sorted_keys():
         bgroups.setdefault(tuple(kb[i] for i in axes_b), []).append(kb)
     out: Dict[Tuple[int, ...], np.ndarray] = {}
+    cplx = 4.0 if np.dtype(dtype).kind == 'c' else 1.0
     for ka in a.sorted_keys():
         ck = tuple(ka[i] for i in axes_a)
         for kb in bgroups.get(ck, []):
             key = tuple(ka[i] for i in free_a) + tuple(kb[i] for i in free_b)
-            prod = np.tensordot(a.blocks[ka], b.blocks[kb], axes=(axes_a, axes_b))
+            blk_a, blk_b = a.blocks[ka], b.blocks[kb]
+            kdim = int(np.prod([blk_a.shape[i] for i in axes_a])) if axes_a else 1
+            FLOPS[0] += 2.0 * cplx * (blk_a.size // max(kdim, 1)) * (blk_b.size // max(kdim, 1)) * kdim
+            prod = np.tensordot(blk_a, blk_b, axes=(axes_a, axes_b))
             if key in out:
                 out[key] += prod
             else:

@@ -54,6 +54,8 @@ SIGNATURES = {
     "udmrg_tensor_upload": [C.c_void_p, c_double_p],
     "udmrg_tensor_download": [C.c_void_p, c_double_p],
     "udmrg_tensor_device_ptr": [C.c_void_p, C.POINTER(c_double_p)],
+    "udmrg_tensor_norm": [C.c_void_p, C.c_void_p, c_double_p],
+    "udmrg_tensor_scale": [C.c_void_p, C.c_void_p, C.c_double],
     "udmrg_contract": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, c_int32_p, c_int32_p,
                        c_void_pp],
     "udmrg_contract_cyclic": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
@@ -76,6 +78,10 @@ SIGNATURES = {
     "udmrg_matvec_plan_embed": [C.c_void_p, C.c_void_p, c_void_pp],
     "udmrg_matvec_plan_apply": [C.c_void_p, c_double_p, c_double_p],
     "udmrg_matvec_plan_destroy": [C.c_void_p],
+    "udmrg_probe_fp64_tflops": [C.c_void_p, c_double_p],
+    "udmrg_ctx_event_record": [C.c_void_p, C.c_int],
+    "udmrg_ctx_event_elapsed": [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)],
+    "udmrg_ctx_flush_l2": [C.c_void_p, C.c_int64],
 }
 
 _lib = None

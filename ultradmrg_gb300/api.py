@@ -37,6 +37,22 @@ class Context:
         call("udmrg_ctx_launches", self.h, C.byref(v))
         return int(v.value)
 
+    def event(self, slot: int):
+        call("udmrg_ctx_event_record", self.h, slot)
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        v = C.c_float()
+        call("udmrg_ctx_event_elapsed", self.h, a, b, C.byref(v))
+        return float(v.value)
+
+    def flush_l2(self, nbytes: int = 512 << 20):
+        call("udmrg_ctx_flush_l2", self.h, int(nbytes))
+
+    def fp64_peak_tflops(self) -> float:
+        v = C.c_double()
+        call("udmrg_probe_fp64_tflops", self.h, C.byref(v))
+        return float(v.value)
+
     def close(self):
         if self.h:
             call("udmrg_ctx_destroy", self.h)
@@ -143,6 +159,15 @@ class DeviceTensor:
     def to_data(self) -> BlockTensorData:
         dtype = np.complex128 if self.is_complex else np.float64
         return from_packed(self.indexes(), self.keys(), self.download_packed(), dtype)
+
+    def norm(self) -> float:
+        v = C.c_double()
+        call("udmrg_tensor_norm", self.ctx.h, self.h, C.byref(v))
+        return float(v.value)
+
+    def scale_(self, alpha: float) -> "DeviceTensor":
+        call("udmrg_tensor_scale", self.ctx.h, self.h, float(alpha))
+        return self
 
     def device_ptr(self) -> int:
         p = _lib.c_double_p()
@@ -281,6 +306,43 @@ def two_site_finite_vmps(ctx, mps: List[DeviceTensor], mpo: List[DeviceTensor],
                          ee=L.ee, lancz_sec=L.lancz_sec, svd_sec=L.svd_sec, env_sec=L.env_sec,
                          tot_sec=L.tot_sec, matvec_flops=L.matvec_flops))
     return float(e0.value), rows
+
+
+def trivial_env_data(mps_ten: BlockTensorData, mpo_ten: BlockTensorData, side: str):
+    """The 1x1x1 boundary environment of ``InitEnvs``
+    (``two_site_update_finite_vmps_impl.h:157-186``): (mps bond, inverse MPO
+    bond, inverse mps bond) with element 1."""
+    if side == "l":
+        i0, iw = mps_ten.indexes[0], mpo_ten.indexes[0].inverse()
+    else:
+        i0, iw = mps_ten.indexes[2], mpo_ten.indexes[3].inverse()
+    t = BlockTensorData([i0, iw, i0.inverse()], {}, np.result_type(mps_ten.dtype, mpo_ten.dtype))
+    t.set_elem((0, 0, 0), 1.0)
+    return t
+
+
+def build_envs(ctx, mpo: Sequence[BlockTensorData], mps: Sequence[BlockTensorData], l: int,
+               normalize: bool = True):
+    """Left environment of sites [0, l) and right environment of sites (l+1, N)
+    by device environment updates (each one normalised when ``normalize``)."""
+    N = len(mps)
+    L = DeviceTensor.from_data(ctx, trivial_env_data(mps[0], mpo[0], "l"))
+    for i in range(l):
+        nxt = update_site_lenvs(ctx, L, DeviceTensor.from_data(ctx, mps[i]),
+                                DeviceTensor.from_data(ctx, mpo[i]))
+        L.close()
+        L = nxt
+        if normalize:
+            L.scale_(1.0 / max(L.norm(), 1e-300))
+    R = DeviceTensor.from_data(ctx, trivial_env_data(mps[N - 1], mpo[N - 1], "r"))
+    for i in range(N - 1, l + 1, -1):
+        nxt = update_site_renvs(ctx, R, DeviceTensor.from_data(ctx, mps[i]),
+                                DeviceTensor.from_data(ctx, mpo[i]))
+        R.close()
+        R = nxt
+        if normalize:
+            R.scale_(1.0 / max(R.norm(), 1e-300))
+    return L, R
 
 
 class MatvecPlan:

@@ -1,4 +1,5 @@
 // extern "C" boundary: plain pointers and sizes, status codes, no exceptions.
+#include <cmath>
 #include <cstring>
 
 #include "../../include/ultradmrg_gb300.h"
@@ -6,9 +7,21 @@
 
 using namespace udmrg;
 
+namespace udmrg {
+double probe_fp64_tflops(Ctx &ctx);
+}
+
 struct udmrg_ctx {
   Ctx ctx;
+  std::vector<cudaEvent_t> events;
+  void *flush_buf = nullptr;
+  int64_t flush_bytes = 0;
   explicit udmrg_ctx(int dev) : ctx(dev) {}
+  ~udmrg_ctx() {
+    for (auto e : events)
+      if (e) cudaEventDestroy(e);
+    if (flush_buf) ctx.free(flush_buf);
+  }
 };
 struct udmrg_tensor {
   TensorPtr t;
@@ -177,6 +190,22 @@ int udmrg_tensor_download(const udmrg_tensor *h, double *host) {
 
 int udmrg_tensor_device_ptr(const udmrg_tensor *h, double **dptr) {
   return guarded([&] { *dptr = T(h).data; });
+}
+
+int udmrg_tensor_norm(udmrg_ctx *c, const udmrg_tensor *h, double *norm) {
+  return guarded([&] {
+    const BTensor &t = T(h);
+    VecWork w(c->ctx);
+    *norm = std::sqrt(norm2(w, t.data, t.size() * elem_doubles(t.dtype)));
+  });
+}
+
+int udmrg_tensor_scale(udmrg_ctx *c, udmrg_tensor *h, double alpha) {
+  return guarded([&] {
+    BTensor &t = *h->t;
+    scale(c->ctx, t.data, t.size() * elem_doubles(t.dtype), alpha);
+    c->ctx.sync();
+  });
 }
 
 int udmrg_contract(udmrg_ctx *c, const udmrg_tensor *a, const udmrg_tensor *b, int n,
@@ -378,6 +407,41 @@ int udmrg_matvec_plan_embed(udmrg_matvec_plan *p, const udmrg_tensor *src, udmrg
 
 int udmrg_matvec_plan_apply(udmrg_matvec_plan *p, const double *d_in, double *d_out) {
   return guarded([&] { p->plan->apply(d_in, d_out); });
+}
+
+int udmrg_probe_fp64_tflops(udmrg_ctx *c, double *tflops) {
+  return guarded([&] { *tflops = probe_fp64_tflops(c->ctx); });
+}
+
+int udmrg_ctx_event_record(udmrg_ctx *c, int slot) {
+  return guarded([&] {
+    UDMRG_REQUIRE(slot >= 0 && slot < 1024, "event slot out of range");
+    if ((int)c->events.size() <= slot) c->events.resize(slot + 1, nullptr);
+    if (!c->events[slot]) UDMRG_CHECK_CUDA(cudaEventCreate(&c->events[slot]));
+    UDMRG_CHECK_CUDA(cudaEventRecord(c->events[slot], c->ctx.stream));
+  });
+}
+
+int udmrg_ctx_event_elapsed(udmrg_ctx *c, int a, int b, float *ms) {
+  return guarded([&] {
+    UDMRG_REQUIRE(a >= 0 && b >= 0 && a < (int)c->events.size() && b < (int)c->events.size() &&
+                      c->events[a] && c->events[b],
+                  "event slot not recorded");
+    UDMRG_CHECK_CUDA(cudaEventSynchronize(c->events[b]));
+    UDMRG_CHECK_CUDA(cudaEventElapsedTime(ms, c->events[a], c->events[b]));
+  });
+}
+
+int udmrg_ctx_flush_l2(udmrg_ctx *c, int64_t bytes) {
+  return guarded([&] {
+    UDMRG_REQUIRE(bytes > 0, "flush size must be positive");
+    if (c->flush_bytes < bytes) {
+      if (c->flush_buf) c->ctx.free(c->flush_buf);
+      c->flush_buf = c->ctx.alloc(bytes);
+      c->flush_bytes = bytes;
+    }
+    UDMRG_CHECK_CUDA(cudaMemsetAsync(c->flush_buf, c->flush_bytes & 0xff, bytes, c->ctx.stream));
+  });
 }
 
 int udmrg_matvec_plan_destroy(udmrg_matvec_plan *p) {
