@@ -165,6 +165,20 @@ int udmrg_ctx_event_record(udmrg_ctx *ctx, int slot);
 int udmrg_ctx_event_elapsed(udmrg_ctx *ctx, int slot_a, int slot_b, float *ms);
 int udmrg_ctx_flush_l2(udmrg_ctx *ctx, int64_t bytes);
 
+/* ---- allocation-free entry point ---------------------------------------- */
+/* No counterpart in the reference.  2-norm of n_doubles device doubles at
+ * d_x, written to the device double *d_norm, stream ordered on `stream` (a
+ * cudaStream_t; NULL is the legacy default stream) on the current device.
+ * For callers that cannot allocate device memory when they need it (inside
+ * their own stream capture, under another allocator, in loops that must not
+ * touch an allocator): it calls no cudaMalloc/cudaFree or allocating routine;
+ * its scratch is a fixed 32 KB device array held by every GPU that loads the
+ * library until exit.  At most 16,777,216 doubles per call (status 1 above
+ * that).  The first call on a device sets up the scratch address, so make it
+ * before any stream capture.  Calls that overlap on the GPU race on the
+ * shared scratch. */
+int udmrg_norm_noalloc(const double *d_x, int64_t n_doubles, double *d_norm, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -66,6 +66,14 @@ const BTensor &T(const udmrg_tensor *h) {
 
 }  // namespace
 
+namespace udmrg {
+// Error reporting for entry points defined in other translation units.
+const char *set_last_error_noalloc(const char *msg) {
+  g_err = msg;
+  return g_err.c_str();
+}
+}  // namespace udmrg
+
 extern "C" {
 
 const char *udmrg_last_error(void) { return g_err.c_str(); }
