@@ -162,6 +162,11 @@ int udmrg_probe_fp64_tflops(udmrg_ctx *ctx, double *tflops);
  * between two recorded slots, and an L2 flush (a write of `bytes` bytes to
  * a scratch buffer, stream ordered) for cold-cache timing. */
 int udmrg_ctx_event_record(udmrg_ctx *ctx, int slot);
+/* Self-test of the tcgen05 split-BF16 GEMM: C = A * B for dense row-major
+ * host matrices A (M x K), B (K x N), C (M x N).  No counterpart in the
+ * reference (a kernel check used by the tests). */
+int udmrg_selftest_tc_gemm(udmrg_ctx *ctx, int64_t M, int64_t N, int64_t K, const double *hA,
+                           const double *hB, double *hC);
 int udmrg_ctx_event_elapsed(udmrg_ctx *ctx, int slot_a, int slot_b, float *ms);
 int udmrg_ctx_flush_l2(udmrg_ctx *ctx, int64_t bytes);
 

@@ -4,6 +4,7 @@
 
 #include "../../include/ultradmrg_gb300.h"
 #include "dmrg.hpp"
+#include "tc_gemm.hpp"
 
 using namespace udmrg;
 
@@ -419,6 +420,41 @@ int udmrg_matvec_plan_apply(udmrg_matvec_plan *p, const double *d_in, double *d_
 
 int udmrg_probe_fp64_tflops(udmrg_ctx *c, double *tflops) {
   return guarded([&] { *tflops = probe_fp64_tflops(c->ctx); });
+}
+
+int udmrg_selftest_tc_gemm(udmrg_ctx *c, int64_t M, int64_t N, int64_t K, const double *hA,
+                           const double *hB, double *hC) {
+  return guarded([&] {
+    Ctx &ctx = c->ctx;
+    UDMRG_REQUIRE(M > 0 && N > 0 && K > 0 && M * K < (1ll << 28) && K * N < (1ll << 28),
+                  "selftest: bad sizes");
+    double *dA = (double *)ctx.alloc(M * K * sizeof(double));
+    double *dB = (double *)ctx.alloc(K * N * sizeof(double));
+    double *dC = (double *)ctx.alloc(M * N * sizeof(double));
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(dA, hA, M * K * sizeof(double), cudaMemcpyHostToDevice, ctx.stream));
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(dB, hB, K * N * sizeof(double), cudaMemcpyHostToDevice, ctx.stream));
+    const int64_t abytes = tc_image_bytes(M, K, kTcBM), bbytes = tc_image_bytes(N, K, kTcBN);
+    uint8_t *ai = (uint8_t *)ctx.alloc(abytes), *bi = (uint8_t *)ctx.alloc(bbytes);
+    UDMRG_CHECK_CUDA(cudaMemsetAsync(ai, 0, abytes, ctx.stream));
+    UDMRG_CHECK_CUDA(cudaMemsetAsync(bi, 0, bbytes, ctx.stream));
+    const int32_t kc = (int32_t)((K + kTcBK - 1) / kTcBK);
+    PackOp pa{0, K, 1, 0, (int32_t)M, (int32_t)K, 0, 0, kc, kTcBM};
+    PackOp pb{0, 1, N, 0, (int32_t)N, (int32_t)K, 0, 0, kc, kTcBN};
+    run_pack(ctx, {pa}, nullptr, 1, dA, true, ai);
+    run_pack(ctx, {pb}, nullptr, 1, dB, true, bi);
+    TcPlan plan;
+    plan.ctx = &ctx;
+    std::vector<int64_t> rows(M);
+    for (int64_t m = 0; m < M; ++m) rows[m] = m * N;
+    plan.add_group(0, 0, (int32_t)M, (int32_t)N, (int32_t)K, rows);
+    plan.finalize();
+    run_tc_gemm(ctx, plan, ai, bi, dC, kTcOutF64, 1.0);
+    const int st = tc_check(ctx, plan);
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(hC, dC, M * N * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.sync();
+    for (void *p : {(void *)dA, (void *)dB, (void *)dC, (void *)ai, (void *)bi}) ctx.free(p);
+    if (st) throw Error(kErrTimeout, "tcgen05 GEMM: a bounded device wait ran out");
+  });
 }
 
 int udmrg_ctx_event_record(udmrg_ctx *c, int slot) {

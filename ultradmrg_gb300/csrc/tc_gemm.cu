@@ -1,0 +1,332 @@
+// tcgen05 split-BF16 grouped GEMM and the image packing kernel.
+#include <algorithm>
+
+#include "tc_common.cuh"
+#include "tc_gemm.hpp"
+
+namespace udmrg {
+
+namespace {
+
+constexpr int kStages = 2;
+constexpr int kThreads = 128;
+constexpr int kStageBytes = (int)(kTcUnitA + kTcUnitB);  // 72 KB
+// Headroom after the stage buffers: no descriptor read can leave the
+// allocation even if a stride field were misread.
+constexpr int kPadBytes = 32 * 1024;
+constexpr int kBarOffset = kStages * kStageBytes + kPadBytes;
+constexpr int kSmemBytes = kBarOffset + 1024;
+constexpr uint32_t kTmemCols = kTcBN;  // FP32 accumulator: BN columns x 128 lanes
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s: a wait this long means a fault
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for an mbarrier phase with a wall-clock limit; false on timeout.
+__device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t parity) {
+  if (tc::mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  while (true) {
+    if (tc::mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > kWaitNs) return false;
+  }
+}
+
+// Byte offset of element (r, k) inside one plane of a TR x 64 tile.
+__device__ __forceinline__ int canon_off(int r, int k, int tr) {
+  return (((k >> 3) * (tr >> 3) + (r >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1);
+}
+
+template <typename T>
+__device__ __forceinline__ void split3(T x, __nv_bfloat16 &h, __nv_bfloat16 &m,
+                                       __nv_bfloat16 &l);
+template <>
+__device__ __forceinline__ void split3<double>(double x, __nv_bfloat16 &h, __nv_bfloat16 &m,
+                                               __nv_bfloat16 &l) {
+  h = __double2bfloat16(x);
+  const double r1 = x - (double)__bfloat162float(h);
+  m = __double2bfloat16(r1);
+  const double r2 = r1 - (double)__bfloat162float(m);
+  l = __double2bfloat16(r2);
+}
+template <>
+__device__ __forceinline__ void split3<float>(float x, __nv_bfloat16 &h, __nv_bfloat16 &m,
+                                              __nv_bfloat16 &l) {
+  h = __float2bfloat16_rn(x);
+  const float r1 = x - __bfloat162float(h);
+  m = __float2bfloat16_rn(r1);
+  const float r2 = r1 - __bfloat162float(m);
+  l = __float2bfloat16_rn(r2);
+}
+
+template <typename T>
+__global__ void pack_kernel(const PackOp *__restrict__ ops, int nops, const T *__restrict__ src,
+                            uint8_t *__restrict__ img) {
+  for (int o = blockIdx.x; o < nops; o += gridDim.x) {
+    const PackOp op = ops[o];
+    const int64_t tot = (int64_t)op.rows * op.cols;
+    const int64_t plane = (int64_t)op.tr * kTcBK * 2;
+    for (int64_t e = threadIdx.x; e < tot; e += blockDim.x) {
+      const int r = (int)(e / op.cols), k = (int)(e - (int64_t)r * op.cols);
+      const T x = src[op.src_off + r * op.src_rs + k * op.src_cs];
+      __nv_bfloat16 h, m, l;
+      split3<T>(x, h, m, l);
+      const int rr = op.r0 + r, kk = op.k0 + k;
+      const int64_t unit = ((int64_t)(rr / op.tr) * op.kc + kk / kTcBK) * 3 * plane;
+      const int64_t off = op.img_off + unit + canon_off(rr % op.tr, kk % kTcBK, op.tr);
+      *(__nv_bfloat16 *)(img + off) = h;
+      *(__nv_bfloat16 *)(img + off + plane) = m;
+      *(__nv_bfloat16 *)(img + off + 2 * plane) = l;
+    }
+  }
+}
+
+// Plane pairs (A plane, B plane) of the six split products.
+__device__ __constant__ int kProdA[6] = {0, 0, 1, 0, 1, 2};
+__device__ __constant__ int kProdB[6] = {0, 1, 0, 2, 1, 0};
+
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_gemm_kernel(const TcTile *__restrict__ tiles, int ntiles, const TcGroup *__restrict__ groups,
+                   const uint8_t *__restrict__ aimg, const uint8_t *__restrict__ bimg,
+                   const int64_t *__restrict__ rowaddr, void *__restrict__ out, int out_kind,
+                   double alpha, int *__restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint64_t *full = (uint64_t *)(smem + kBarOffset);
+  uint64_t *empty = full + kStages;
+  uint64_t *done = empty + kStages;
+  uint64_t *fin = done + 1;
+  uint32_t *tmem_slot = (uint32_t *)(fin + 1);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(done, 1);
+    tc::mbar_init(fin, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tmem_slot, kTmemCols);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  constexpr uint32_t idesc = tc::idesc_bf16_f32(kTcBM, kTcBN);
+
+  uint32_t gchunk = 0;  // chunks issued so far by this CTA (thread 0's view)
+  uint32_t tile_iter = 0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const TcTile tile = tiles[t];
+    const TcGroup g = groups[tile.group];
+    const int nk = g.kc;
+    if (tid == 0 && !*abort_flag) {
+      const uint8_t *abase = aimg + g.a_img + (int64_t)tile.mtile * g.kc * kTcUnitA;
+      const uint8_t *bbase = bimg + g.b_img + (int64_t)tile.ntile * g.kc * kTcUnitB;
+      auto issue = [&](int c) -> bool {
+        const uint32_t G = gchunk + c, s = G % kStages;
+        if (G >= kStages && !wait_phase(&empty[s], ((G / kStages) - 1) & 1)) return false;
+        uint8_t *st = smem + s * kStageBytes;
+        tc::mbar_expect_tx(&full[s], (uint32_t)(kTcUnitA + kTcUnitB));
+        tc::bulk_g2s(st, abase + (int64_t)c * kTcUnitA, (uint32_t)kTcUnitA, &full[s]);
+        tc::bulk_g2s(st + kTcUnitA, bbase + (int64_t)c * kTcUnitB, (uint32_t)kTcUnitB, &full[s]);
+        return true;
+      };
+      bool ok = true;
+      for (int c = 0; c < min(kStages, nk) && ok; ++c) ok = issue(c);
+      for (int c = 0; c < nk && ok; ++c) {
+        const uint32_t G = gchunk + c, s = G % kStages;
+        if (!wait_phase(&full[s], (G / kStages) & 1)) {
+          ok = false;
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t sa = tc::smem_u32(smem + s * kStageBytes);
+        const uint32_t sb = sa + (uint32_t)kTcUnitA;
+        constexpr uint32_t planeA = kTcBM * kTcBK * 2, planeB = kTcBN * kTcBK * 2;
+#pragma unroll
+        for (int ks = 0; ks < kTcBK / 16; ++ks) {
+#pragma unroll
+          for (int p = 0; p < 6; ++p) {
+            // K step ks covers core-matrix columns 2ks, 2ks+1
+            const uint64_t ad = tc::make_desc(sa + kProdA[p] * planeA + ks * 2 * (kTcBM / 8) * 128,
+                                              (kTcBM / 8) * 128, 128);
+            const uint64_t bd = tc::make_desc(sb + kProdB[p] * planeB + ks * 2 * (kTcBN / 8) * 128,
+                                              (kTcBN / 8) * 128, 128);
+            tc::mma_bf16(tmem, ad, bd, idesc, (c > 0 || ks > 0 || p > 0) ? 1u : 0u);
+          }
+        }
+        tc::mma_commit(&empty[s]);
+        if (c + kStages < nk) ok = issue(c + kStages);
+      }
+      gchunk += nk;
+      tc::mma_commit(done);  // arrives once every MMA of this tile completed
+      if (!ok) {
+        atomicExch(err, 1);
+        *abort_flag = 1;
+      }
+    }
+    // epilogue: all warps drain their 32 TMEM lanes
+    const bool got = wait_phase(done, tile_iter & 1);
+    if (!got) {
+      if (lane == 0) atomicExch(err, 2);
+      *abort_flag = 1;
+    }
+    tc::fence_after_sync();
+    const int m = warp * 32 + lane;
+    const int64_t grow = (int64_t)tile.mtile * kTcBM + m;
+    const bool row_ok = grow < g.M && got && !*abort_flag;
+    const int64_t base = row_ok ? rowaddr[g.row0 + grow] : 0;
+    const int n0 = tile.ntile * kTcBN;
+#pragma unroll
+    for (int cb = 0; cb < kTcBN / 16; ++cb) {
+      uint32_t r[16];
+      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + cb * 16, r);
+      tc::tmem_wait_ld();
+      if (row_ok) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int n = n0 + cb * 16 + j;
+          if (n < g.N) {
+            const float v = nk > 0 ? __uint_as_float(r[j]) : 0.0f;
+            if (out_kind == kTcOutF64)
+              ((double *)out)[base + n] = alpha * (double)v;
+            else
+              ((float *)out)[base + n] = (float)(alpha * (double)v);
+          }
+        }
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    ++tile_iter;
+    if (*abort_flag) break;
+  }
+  // all MMAs of this CTA have completed before the accumulator is released
+  if (tid == 0) {
+    tc::mma_commit(fin);
+    if (!wait_phase(fin, 0)) atomicExch(err, 3);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+}  // namespace
+
+int64_t tc_image_bytes(int64_t rows, int64_t K, int tr) {
+  const int64_t rt = (rows + tr - 1) / tr, kc = (K + kTcBK - 1) / kTcBK;
+  return rt * kc * 3 * tr * kTcBK * 2;
+}
+
+TcPlan::~TcPlan() {
+  if (!ctx) return;
+  ctx->free(d_groups);
+  ctx->free(d_tiles);
+  ctx->free(d_rowaddr);
+  ctx->free(d_err);
+}
+
+void TcPlan::add_group(int64_t a_img, int64_t b_img, int32_t M, int32_t N, int32_t K,
+                       const std::vector<int64_t> &rows) {
+  UDMRG_REQUIRE((int64_t)rows.size() == M, "tc plan: one output row address per row");
+  if (M == 0 || N == 0) return;
+  TcGroup g{};
+  g.a_img = a_img;
+  g.b_img = b_img;
+  g.row0 = (int64_t)rowaddr.size();
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.mt = (M + kTcBM - 1) / kTcBM;
+  g.nt = (N + kTcBN - 1) / kTcBN;
+  g.kc = (K + kTcBK - 1) / kTcBK;
+  rowaddr.insert(rowaddr.end(), rows.begin(), rows.end());
+  const int32_t gid = (int32_t)groups.size();
+  groups.push_back(g);
+  for (int mt = 0; mt < g.mt; ++mt)
+    for (int nt = 0; nt < g.nt; ++nt) tiles.push_back({gid, mt, nt, 0});
+  flops += 2.0 * (double)M * (double)N * (double)K;
+}
+
+template <typename V>
+static V *upload(Ctx *ctx, const std::vector<V> &v) {
+  if (v.empty()) return nullptr;
+  V *d = (V *)ctx->alloc(v.size() * sizeof(V));
+  UDMRG_CHECK_CUDA(
+      cudaMemcpyAsync(d, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice, ctx->stream));
+  return d;
+}
+
+void TcPlan::finalize() {
+  std::stable_sort(tiles.begin(), tiles.end(), [&](const TcTile &a, const TcTile &b) {
+    return groups[a.group].kc > groups[b.group].kc;
+  });
+  d_groups = upload(ctx, groups);
+  d_tiles = upload(ctx, tiles);
+  d_rowaddr = upload(ctx, rowaddr);
+  d_err = (int *)ctx->alloc(sizeof(int));
+  UDMRG_CHECK_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
+  ctx->sync();
+}
+
+PackOp *upload_pack_ops(Ctx &ctx, const std::vector<PackOp> &ops) { return upload(&ctx, ops); }
+
+void run_pack(Ctx &ctx, const std::vector<PackOp> &ops, const PackOp *d_ops, int nops,
+              const void *src, bool src_f64, uint8_t *img) {
+  if (nops == 0) return;
+  PackOp *tmp = nullptr;
+  if (!d_ops) {
+    tmp = upload(&ctx, ops);
+    d_ops = tmp;
+  }
+  const int grid = std::min(nops, 16 * ctx.num_sms);
+  if (src_f64)
+    pack_kernel<double><<<grid, 256, 0, ctx.stream>>>(d_ops, nops, (const double *)src, img);
+  else
+    pack_kernel<float><<<grid, 256, 0, ctx.stream>>>(d_ops, nops, (const float *)src, img);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  ctx.launches++;
+  if (tmp) {
+    ctx.sync();
+    ctx.free(tmp);
+  }
+}
+
+void run_tc_gemm(Ctx &ctx, const TcPlan &plan, const uint8_t *a_img, const uint8_t *b_img,
+                 void *out, int out_kind, double alpha) {
+  const int ntiles = (int)plan.tiles.size();
+  if (ntiles == 0) return;
+  static bool attr_set = false;
+  if (!attr_set) {
+    UDMRG_CHECK_CUDA(cudaFuncSetAttribute(tc_gemm_kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          kSmemBytes));
+    attr_set = true;
+  }
+  const int grid = std::min(ntiles, ctx.num_sms);
+  tc_gemm_kernel<<<grid, kThreads, kSmemBytes, ctx.stream>>>(
+      plan.d_tiles, ntiles, plan.d_groups, a_img, b_img, plan.d_rowaddr, out, out_kind, alpha,
+      plan.d_err);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  ctx.launches++;
+}
+
+int tc_check(Ctx &ctx, const TcPlan &plan) {
+  int h = 0;
+  UDMRG_CHECK_CUDA(cudaMemcpyAsync(&h, plan.d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+  ctx.sync();
+  if (h) UDMRG_CHECK_CUDA(cudaMemsetAsync(plan.d_err, 0, sizeof(int), ctx.stream));
+  return h;
+}
+
+}  // namespace udmrg

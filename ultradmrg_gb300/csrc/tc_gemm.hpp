@@ -1,0 +1,85 @@
+// Mixed-precision grouped GEMM on the tcgen05 tensor cores (split BF16).
+//
+// Operands are stored in HBM as "tile images": the exact shared-memory
+// layout the MMA reads (no swizzle, K-major canonical layout of 8-row x
+// 16-byte core matrices), pre-split into three BF16 planes (x = hi + mid + lo,
+// each the BF16 rounding of the remainder, ~24 significant bits together).
+// A tile image unit holds TR rows x 64 K for the three planes; units are
+// ordered [row tile][K chunk].  The kernel fills shared memory with one bulk
+// asynchronous copy per unit (cp.async.bulk, completion on an mbarrier), one
+// elected thread issues the six cross products hi*hi, hi*mid, mid*hi, hi*lo,
+// mid*mid, lo*hi per 16-deep K step into an FP32 accumulator in tensor
+// memory, and all four warps drain the accumulator (tcgen05.ld) into FP32 or
+// FP64 outputs addressed through a per-row address table.
+#pragma once
+
+#include "btensor.hpp"
+
+namespace udmrg {
+
+constexpr int kTcBM = 128;  // rows of an A tile (UMMA M)
+constexpr int kTcBN = 64;   // rows of a B tile (UMMA N)
+constexpr int kTcBK = 64;   // K per chunk (four K=16 MMA steps)
+constexpr int64_t kTcUnitA = 3LL * kTcBM * kTcBK * 2;  // 48 KB
+constexpr int64_t kTcUnitB = 3LL * kTcBN * kTcBK * 2;  // 24 KB
+
+// Pack one strided sub-matrix into an image (element type of the source:
+// FP64 or FP32).  Element (r, k) of the sub-matrix is
+// src[src_off + r*src_rs + k*src_cs] and lands at image row r0 + r, column
+// k0 + k.
+struct PackOp {
+  int64_t src_off, src_rs, src_cs;
+  int64_t img_off;  // byte offset of the image
+  int32_t rows, cols;
+  int32_t r0, k0;
+  int32_t kc;  // K chunks of the image
+  int32_t tr;  // rows per tile of the image (kTcBM or kTcBN)
+};
+
+// One dense GEMM C(MxN) = alpha * A(MxK) * B(NxK)^T between two images.
+struct TcGroup {
+  int64_t a_img, b_img;  // byte offsets into the A / B image arenas
+  int64_t row0;          // first entry of this group in the row address table
+  int32_t M, N, K;
+  int32_t mt, nt, kc;
+};
+
+struct TcTile {
+  int32_t group, mtile, ntile, pad;
+};
+
+enum TcOut : int { kTcOutF32 = 0, kTcOutF64 = 1 };
+
+struct TcPlan {
+  Ctx *ctx = nullptr;
+  std::vector<TcGroup> groups;
+  std::vector<TcTile> tiles;
+  std::vector<int64_t> rowaddr;  // output element offset of each output row
+  TcGroup *d_groups = nullptr;
+  TcTile *d_tiles = nullptr;
+  int64_t *d_rowaddr = nullptr;
+  int *d_err = nullptr;
+  double flops = 0;  // algorithmic 2*M*N*K
+  TcPlan() = default;
+  TcPlan(const TcPlan &) = delete;
+  TcPlan &operator=(const TcPlan &) = delete;
+  ~TcPlan();
+  void add_group(int64_t a_img, int64_t b_img, int32_t M, int32_t N, int32_t K,
+                 const std::vector<int64_t> &rows);
+  void finalize();  // sort tiles (largest K first), upload
+};
+
+int64_t tc_image_bytes(int64_t rows, int64_t K, int tr);
+
+void run_pack(Ctx &ctx, const std::vector<PackOp> &ops, const PackOp *d_ops, int nops,
+              const void *src, bool src_f64, uint8_t *img);
+// Upload pack ops once (returns device copy; caller frees with ctx.free).
+PackOp *upload_pack_ops(Ctx &ctx, const std::vector<PackOp> &ops);
+
+void run_tc_gemm(Ctx &ctx, const TcPlan &plan, const uint8_t *a_img, const uint8_t *b_img,
+                 void *out, int out_kind, double alpha);
+// Returns and clears the device error flag of the plan (nonzero: a bounded
+// wait inside the kernel ran out).
+int tc_check(Ctx &ctx, const TcPlan &plan);
+
+}  // namespace udmrg
