@@ -28,7 +28,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-METRIC = "two-site matvec TFLOP/s (H_eff*psi, U(1)xU(1) block-sparse, FP64)"
+METRIC = ("two-site matvec TFLOP/s (H_eff*psi, U(1)xU(1) block-sparse; algorithmic FLOPs; "
+          "mixed split-BF16 tensor-core form, plain FP64 reported beside)")
 
 
 def parse():
@@ -244,18 +245,30 @@ def run_ours(args):
     psi = api.contract(ctx, A1, A2, [2], [0])
     W1 = api.DeviceTensor.from_data(ctx, mpo[l])
     W2 = api.DeviceTensor.from_data(ctx, mpo[l + 1])
+    ops = [L, W1, W2, R]
     t0 = time.perf_counter()
-    plan = api.MatvecPlan(ctx, [L, W1, W2, R], psi)
+    plan = api.MatvecPlan(ctx, ops, psi, precision=api.PREC_MIXED)
     plan_s = time.perf_counter() - t0
+    plan64 = api.MatvecPlan(ctx, ops, psi, precision=api.PREC_FP64)
     info = plan.info()
     x = plan.embed(psi)
     y = plan.embed(psi)
+    y64 = plan.embed(psi)
     xp, yp = x.device_ptr(), y.device_ptr()
     flops = info["flops"]
     nbytes = info["psi_size"] * 8
 
     def step():
         plan.apply_ptr(xp, yp)
+
+    def timed(fn, steps, slot0):
+        for i in range(steps):
+            ctx.flush_l2()
+            ctx.event(slot0 + 2 * i)
+            fn()
+            ctx.event(slot0 + 2 * i + 1)
+        ctx.sync()
+        return sum(ctx.elapsed_ms(slot0 + 2 * i, slot0 + 2 * i + 1) for i in range(steps)) / steps / 1e3
 
     for _ in range(args.warmup):
         ctx.flush_l2()
@@ -266,22 +279,31 @@ def run_ours(args):
     l0 = ctx.launches()
     with ClockSampler(local) as clk:
         wall0 = time.perf_counter()
-        for i in range(args.steps):
-            ctx.flush_l2()
-            ctx.event(2 * i)
-            step()
-            ctx.event(2 * i + 1)
-        ctx.sync()
+        t_step = timed(step, args.steps, 0)
         wall = time.perf_counter() - wall0
     launches = ctx.launches() - l0
-    dev_ms = sum(ctx.elapsed_ms(2 * i, 2 * i + 1) for i in range(args.steps))
-    t_step = dev_ms / 1e3 / args.steps
     if ws > 1:
         import torch
         tt = torch.tensor([t_step], dtype=torch.float64)
         tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
         t_step = float(tt.item())
     value = ws * flops / t_step / 1e12
+
+    # plain FP64 form on the same inputs (fewer steps: it is ~100x slower)
+    y64p = y64.device_ptr()
+    plan64.apply_ptr(xp, y64p)
+    t64 = timed(lambda: plan64.apply_ptr(xp, y64p), max(2, min(args.steps, 5)), 200)
+    ym, yd = y.download_packed(), y64.download_packed()
+    mixed_err = float(np.linalg.norm(ym - yd) / max(np.linalg.norm(yd), 1e-300))
+    # per-stage device times (dominant kernel roofline)
+    ms_mx, fl_mx = plan.stage_times(xp, yp)
+    ms_64, fl_64 = plan64.stage_times(xp, y64p)
+    # Lanczos energies of both forms from the same start vector
+    lz = {}
+    for name, prec in (("mixed", api.PREC_MIXED), ("fp64", api.PREC_FP64)):
+        r = api.lanczos_solver(ctx, ops, psi, 1e-12, 12, precision=prec)
+        lz[name] = (r.gs_eng, r.iters, r.matvec_seconds / max(r.matvecs, 1))
+        r.gs_vec.close()
 
     # e2e through the C ABI with host buffers
     try:
@@ -314,26 +336,46 @@ def run_ours(args):
 
     fp64_peak = ctx.fp64_peak_tflops()
     peaks = measured_peaks()
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    # dominant mixed-precision kernel: the larger of the two tcgen05 GEMM stages;
+    # algorithmic flops of that stage are those of the matching FP64 contraction
+    dom = 1 if ms_mx[1] >= ms_mx[3] else 3
+    alg_dom = fl_64[0] if dom == 1 else fl_64[3]
+    ach = alg_dom / (ms_mx[dom] / 1e3) / 1e12
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16x3 split products, f32 accumulate (f64 Krylov vectors)",
         "data": "synthetic (seeded random MPS with a Gaussian QN-sector model; environments "
                 "by device environment updates)",
         "config": {"workload": w.name, "D": w.D, "sites": w.N, "bond": l,
                    "psi_elements": info["psi_size"], "mpo_bond_dim": mpo[l].indexes[3].dim,
+                   "form": "mixed (tcgen05 split-BF16 block GEMMs)",
                    "parallelism": "replicas only" if ws > 1 else "single GPU",
                    "l2": "flushed (512 MB write) before every timed step",
                    "plan_seconds": plan_s},
         "gpu_launches": launches,
         "e2e": {"value": e2e_val, "unit": "TFLOP/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes},
-        "roofline": {"bound": "fp64", "pipe": "FP64 FMA (grouped block GEMM)",
-                     "achieved": flops / t_step / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": flops / t_step / 1e12 / fp64_peak, "traffic": None,
-                     "peak_source": "measured in this run by the library's DFMA probe "
-                                    "(MEASURED_PEAKS.json has no FP64 entry)",
-                     "hbm_peak_gbs_measured": peaks.get("hbm_gbs")},
+        "roofline": {"bound": "tensor", "kernel": "tc_gemm_kernel (GEMM L.psi)" if dom == 1
+                     else "tc_gemm_kernel (GEMM .R)",
+                     "achieved": ach, "peak": bf16_peak, "unit": "TFLOP/s",
+                     "frac": ach / bf16_peak, "traffic": None,
+                     "peak_source": "bf16_tflops of MEASURED_PEAKS.json (burst)",
+                     "issued_tensor_tflops": fl_mx[dom] / (ms_mx[dom] / 1e3) / 1e12,
+                     "stage_ms": {"psi_pack": ms_mx[0], "gemm_L_psi": ms_mx[1],
+                                  "mpo_step": ms_mx[2], "gemm_R": ms_mx[3]}},
+        "plain_fp64": {"value": flops / t64 / 1e12, "unit": "TFLOP/s", "ms_per_step": t64 * 1e3,
+                       "roofline": {"bound": "fp64", "peak": fp64_peak,
+                                    "frac": flops / t64 / 1e12 / fp64_peak,
+                                    "peak_source": "library DFMA probe (no FP64 entry in "
+                                                   "MEASURED_PEAKS.json)"},
+                       "stage_ms": ms_64},
+        "speedup_mixed_vs_fp64": t64 / t_step,
+        "accuracy": {"matvec_rel_err_mixed_vs_fp64": mixed_err,
+                     "lanczos12_E_mixed": lz["mixed"][0], "lanczos12_E_fp64": lz["fp64"][0],
+                     "lanczos12_rel_dE": abs(lz["mixed"][0] - lz["fp64"][0]) / abs(lz["fp64"][0])},
         "clocks": clk.summary(),
         "wall_seconds_timed": wall,
     }

@@ -29,10 +29,16 @@ typedef struct udmrg_matvec_plan udmrg_matvec_plan;
 enum { UDMRG_F64 = 0, UDMRG_C128 = 1 };
 enum { UDMRG_SVD_FULL = 0, UDMRG_SVD_SPLIT_LEFT = 1, UDMRG_SVD_SPLIT_RIGHT = 2 };
 
-/* LanczosParams (include/qlmps/algorithm/lanczos_params.h:27-46). */
+enum { UDMRG_PREC_FP64 = 0, UDMRG_PREC_MIXED = 1 };
+
+/* LanczosParams (include/qlmps/algorithm/lanczos_params.h:27-46), plus the
+ * matvec precision: UDMRG_PREC_FP64 (plain FP64 block GEMMs) or
+ * UDMRG_PREC_MIXED (split-BF16 tcgen05 GEMMs with FP32 accumulation; Krylov
+ * vectors, dot products and the tridiagonal problem stay FP64). */
 typedef struct {
   double error;           /* absolute energy change that stops the iteration */
   int64_t max_iterations; /* maximal Krylov dimension */
+  int64_t matvec_precision;
 } udmrg_lanczos_params;
 
 /* LanczosRes (include/qlmps/algorithm/vmps/lanczos_vmps_solver_impl.h:98-103).
@@ -146,6 +152,10 @@ int udmrg_two_site_finite_vmps(udmrg_ctx *ctx, int64_t N, udmrg_tensor **mps,
  * matvec that contains psi_struct's blocks (the Krylov structure). */
 int udmrg_matvec_plan_create(udmrg_ctx *ctx, udmrg_tensor *const *eff_ham,
                              const udmrg_tensor *psi_struct, udmrg_matvec_plan **out);
+/* Same with a matvec precision (UDMRG_PREC_FP64 / UDMRG_PREC_MIXED). */
+int udmrg_matvec_plan_create_ex(udmrg_ctx *ctx, udmrg_tensor *const *eff_ham,
+                                const udmrg_tensor *psi_struct, int precision,
+                                udmrg_matvec_plan **out);
 int udmrg_matvec_plan_info(const udmrg_matvec_plan *p, double *flops, int64_t *psi_size,
                            int64_t *workspace_bytes);
 /* Tensor with the plan's Krylov structure holding `src` (zero elsewhere). */
@@ -153,6 +163,13 @@ int udmrg_matvec_plan_embed(udmrg_matvec_plan *p, const udmrg_tensor *src, udmrg
 /* out = H_eff * in on device buffers laid out in the Krylov structure. */
 int udmrg_matvec_plan_apply(udmrg_matvec_plan *p, const double *d_in, double *d_out);
 int udmrg_matvec_plan_destroy(udmrg_matvec_plan *p);
+/* One matvec with CUDA events between its four stages (device ms, written to
+ * ms[4]) and the work of each stage in FLOP (flops[4]: algorithmic for the
+ * FP64 form; tensor-core work issued, six split products included, for the
+ * mixed form).  Mixed stages: psi pack, GEMM L.psi, MPO step, GEMM .R;
+ * FP64 stages: the four block contractions. */
+int udmrg_matvec_plan_stage_times(udmrg_matvec_plan *p, const double *d_in, double *d_out,
+                                  double *ms, double *flops);
 
 /* ---- measurement ---------------------------------------------------- */
 /* FP64 FMA throughput of the device (TFLOP/s), measured by a DFMA-bound

@@ -1,0 +1,111 @@
+"""Mixed-precision matvec (split-BF16 tcgen05 GEMMs, FP32 accumulation)
+against the FP64 oracle.
+
+Element-wise the mixed matvec is FP32-accurate (tolerance 2e-5 of the
+largest element); energies from Lanczos and from whole sweeps must stay
+within |dE/E| <= 1e-9 of the FP64 results, the accuracy bar of the
+mixed-precision form.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import blocksparse as bs
+from oracle import krylov, vmps as ovmps
+from systems import heisenberg_system, hubbard_system, max_block_diff, two_site_problem
+from ultradmrg_gb300 import api, models as M
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_goldens.json")))
+MIXED = api.PREC_MIXED
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from ultradmrg_gb300 import build
+    build.build()
+    c = api.Context(0)
+    yield c
+    c.close()
+
+
+def up(ctx, t):
+    return api.DeviceTensor.from_data(ctx, t)
+
+
+SYSTEMS = {
+    "heis": lambda: heisenberg_system(N=10, D=24, seed=0),
+    "hub": lambda: hubbard_system(Lx=3, Ly=2, D=40, seed=1),
+    "hub_big": lambda: hubbard_system(Lx=4, Ly=2, D=120, seed=3),
+}
+
+
+@pytest.mark.parametrize("name,l", [("heis", 4), ("heis", 0), ("heis", 8), ("hub", 2),
+                                    ("hub_big", 3)])
+def test_mixed_matvec_parity(ctx, name, l):
+    mpo, mps = SYSTEMS[name]()
+    eff, psi = two_site_problem(mpo, mps, l)
+    ref = krylov.eff_ham_mul_two_site_state(eff, psi)
+    dev = [up(ctx, t) for t in eff]
+    dpsi = up(ctx, psi)
+    plan = api.MatvecPlan(ctx, dev, dpsi, precision=MIXED)
+    x = plan.embed(dpsi)
+    y = plan.embed(dpsi)
+    plan.apply(x, y)
+    out = y.to_data()
+    assert set(ref.blocks) <= set(out.blocks)
+    d, s = max_block_diff(out, ref)
+    assert d <= 2e-5 * s, (d, s)
+
+
+@pytest.mark.parametrize("name,l", [("heis", 4), ("hub", 2), ("hub_big", 3)])
+def test_mixed_lanczos_energy(ctx, name, l):
+    mpo, mps = SYSTEMS[name]()
+    eff, psi = two_site_problem(mpo, mps, l)
+    ref = krylov.lanczos_solver(eff, psi.copy(), krylov.eff_ham_mul_two_site_state,
+                                krylov.LanczosParams(1e-12, 100))
+    res = api.lanczos_solver(ctx, [up(ctx, t) for t in eff], up(ctx, psi), 1e-12, 100,
+                             precision=MIXED)
+    rel = abs(res.gs_eng - ref.gs_eng) / abs(ref.gs_eng)
+    print(f"{name}: mixed Lanczos |dE/E| = {rel:.2e} ({res.iters} iterations)")
+    assert rel <= 1e-9
+
+
+def _gpu_vmps(ctx, mpo, pb, labels, params):
+    mps0 = M.direct_product_mps([pb] * len(labels), labels)
+    dmps = [up(ctx, t) for t in mps0]
+    dmpo = [up(ctx, t) for t in mpo]
+    return api.two_site_finite_vmps(ctx, dmps, dmpo, params)
+
+
+def test_mixed_vmps_golden_heisenberg(ctx):
+    g = GOLD["vmps"]["1DHeisenberg"]
+    mpo, pb = M.heisenberg_chain_mpo(6)
+    e0, _ = _gpu_vmps(ctx, mpo, pb, [i % 2 for i in range(6)],
+                      api.FiniteVMPSSweepParams(4, 8, 8, 1e-9, 1e-7, precision=MIXED))
+    assert abs(e0 - g["energy"]) <= 1e-9 * abs(g["energy"])
+
+
+def test_mixed_vmps_golden_hubbard2x2(ctx):
+    g = GOLD["vmps"]["Hubbard2x2"]
+    mpo, pb = M.hubbard_2x2_test_mpo()
+    e0, _ = _gpu_vmps(ctx, mpo, pb, [1 if i % 2 == 0 else 2 for i in range(4)],
+                      api.FiniteVMPSSweepParams(10, 16, 16, 1e-9, 1e-8, 20, precision=MIXED))
+    assert abs(e0 - g["energy"]) <= 1e-9 * abs(g["energy"])
+
+
+def test_mixed_vmps_heisenberg16_vs_fp64(ctx):
+    N = 16
+    mpo, pb = M.heisenberg_chain_mpo(N)
+    labels = M.random_sz0_labels(N, 0)
+    e_mixed, log_m = _gpu_vmps(ctx, mpo, pb, labels,
+                               api.FiniteVMPSSweepParams(3, 32, 32, 1e-10, 1e-10, 100,
+                                                         precision=MIXED))
+    e_fp64, log_d = _gpu_vmps(ctx, mpo, pb, labels,
+                              api.FiniteVMPSSweepParams(3, 32, 32, 1e-10, 1e-10, 100))
+    rel = abs(e_mixed - e_fp64) / abs(e_fp64)
+    print(f"L=16 D=32 sweep: |dE/E| mixed vs FP64 = {rel:.2e}")
+    assert rel <= 1e-9

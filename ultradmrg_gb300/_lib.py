@@ -18,7 +18,8 @@ c_void_pp = C.POINTER(C.c_void_p)
 
 
 class LanczosParams(C.Structure):
-    _fields_ = [("error", C.c_double), ("max_iterations", C.c_int64)]
+    _fields_ = [("error", C.c_double), ("max_iterations", C.c_int64),
+                ("matvec_precision", C.c_int64)]
 
 
 class LanczosRes(C.Structure):
@@ -74,10 +75,13 @@ SIGNATURES = {
                                    C.POINTER(SweepParams), c_double_p, C.POINTER(SiteLog),
                                    C.c_int64, c_int64_p],
     "udmrg_matvec_plan_create": [C.c_void_p, c_void_pp, C.c_void_p, c_void_pp],
+    "udmrg_matvec_plan_create_ex": [C.c_void_p, c_void_pp, C.c_void_p, C.c_int, c_void_pp],
     "udmrg_matvec_plan_info": [C.c_void_p, c_double_p, c_int64_p, c_int64_p],
     "udmrg_matvec_plan_embed": [C.c_void_p, C.c_void_p, c_void_pp],
     "udmrg_matvec_plan_apply": [C.c_void_p, c_double_p, c_double_p],
     "udmrg_matvec_plan_destroy": [C.c_void_p],
+    "udmrg_matvec_plan_stage_times": [C.c_void_p, c_double_p, c_double_p, c_double_p,
+                                      c_double_p],
     "udmrg_probe_fp64_tflops": [C.c_void_p, c_double_p],
     "udmrg_ctx_event_record": [C.c_void_p, C.c_int],
     "udmrg_ctx_event_elapsed": [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)],

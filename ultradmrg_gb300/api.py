@@ -234,8 +234,12 @@ class LanczosResult:
     matvecs: int
 
 
-def lanczos_solver(ctx, eff_ham, init_state, error=1e-7, max_iterations=200) -> LanczosResult:
-    p = _lib.LanczosParams(error, max_iterations)
+PREC_FP64, PREC_MIXED = 0, 1
+
+
+def lanczos_solver(ctx, eff_ham, init_state, error=1e-7, max_iterations=200,
+                   precision=PREC_FP64) -> LanczosResult:
+    p = _lib.LanczosParams(error, max_iterations, precision)
     r = _lib.LanczosRes()
     call("udmrg_lanczos_solver", ctx.h, _handles(eff_ham), init_state.h, C.byref(p), C.byref(r))
     return LanczosResult(int(r.iters), float(r.gs_eng), _new(ctx, C.c_void_p(r.gs_vec)),
@@ -243,7 +247,7 @@ def lanczos_solver(ctx, eff_ham, init_state, error=1e-7, max_iterations=200) -> 
 
 
 def lanczos_expmv_solver(ctx, eff_ham, init_state, step, error=1e-10, max_iterations=20):
-    p = _lib.LanczosParams(error, max_iterations)
+    p = _lib.LanczosParams(error, max_iterations, PREC_FP64)
     it = C.c_int64()
     h = C.c_void_p()
     call("udmrg_lanczos_expmv_solver", ctx.h, _handles(eff_ham), init_state.h, step, C.byref(p),
@@ -285,6 +289,7 @@ class FiniteVMPSSweepParams:
     trunc_err: float
     lanczos_error: float = 1e-7
     lanczos_max_iterations: int = 200
+    precision: int = 0  # matvec precision: 0 FP64, 1 mixed (split-BF16 tensor cores)
 
 
 def two_site_finite_vmps(ctx, mps: List[DeviceTensor], mpo: List[DeviceTensor],
@@ -292,7 +297,8 @@ def two_site_finite_vmps(ctx, mps: List[DeviceTensor], mpo: List[DeviceTensor],
     """``TwoSiteFiniteVMPS``: updates ``mps`` in place, returns (e0, per-site log)."""
     N = len(mps)
     sp = _lib.SweepParams(params.sweeps, params.Dmin, params.Dmax, params.trunc_err,
-                          _lib.LanczosParams(params.lanczos_error, params.lanczos_max_iterations))
+                          _lib.LanczosParams(params.lanczos_error, params.lanczos_max_iterations,
+                                             params.precision))
     cap = 2 * N * max(params.sweeps, 1)
     log = (_lib.SiteLog * cap)()
     e0 = C.c_double()
@@ -348,10 +354,11 @@ def build_envs(ctx, mpo: Sequence[BlockTensorData], mps: Sequence[BlockTensorDat
 class MatvecPlan:
     """Reusable H_eff * psi on device buffers (``udmrg_matvec_plan``)."""
 
-    def __init__(self, ctx, eff_ham, psi_struct):
+    def __init__(self, ctx, eff_ham, psi_struct, precision=PREC_FP64):
         self.ctx = ctx
         h = C.c_void_p()
-        call("udmrg_matvec_plan_create", ctx.h, _handles(eff_ham), psi_struct.h, C.byref(h))
+        call("udmrg_matvec_plan_create_ex", ctx.h, _handles(eff_ham), psi_struct.h, precision,
+             C.byref(h))
         self.h = h
 
     def info(self):
@@ -370,6 +377,14 @@ class MatvecPlan:
 
     def apply(self, x: DeviceTensor, y: DeviceTensor):
         self.apply_ptr(x.device_ptr(), y.device_ptr())
+
+    def stage_times(self, d_in: int, d_out: int):
+        """(ms[4], flops[4]) of one matvec, CUDA events between the stages."""
+        ms = (C.c_double * 4)()
+        fl = (C.c_double * 4)()
+        call("udmrg_matvec_plan_stage_times", self.h, C.cast(C.c_void_p(d_in), _lib.c_double_p),
+             C.cast(C.c_void_p(d_out), _lib.c_double_p), ms, fl)
+        return list(ms), list(fl)
 
     def close(self):
         if self.h:

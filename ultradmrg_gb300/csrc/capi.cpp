@@ -282,8 +282,8 @@ int udmrg_lanczos_solver(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
     const BTensor &psi = T(init_state);
     EffHam e;
     prepare_eff_ham(ctx, eff_ham, psi.dtype, e);
-    auto mv = plan_matvec2(ctx, *e.op[0], *e.op[1], *e.op[2], *e.op[3], psi);
-    LanczosParams p{params->error, params->max_iterations};
+    LanczosParams p{params->error, params->max_iterations, (int)params->matvec_precision};
+    auto mv = plan_matvec2(ctx, *e.op[0], *e.op[1], *e.op[2], *e.op[3], psi, p.precision);
     auto r = lanczos_gs(ctx, *mv, psi, p);
     res->iters = r.iters;
     res->gs_eng = r.gs_eng;
@@ -360,7 +360,8 @@ int udmrg_two_site_finite_vmps(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
     p.Dmin = params->Dmin;
     p.Dmax = params->Dmax;
     p.trunc_err = params->trunc_err;
-    p.lancz = {params->lancz_params.error, params->lancz_params.max_iterations};
+    p.lancz = {params->lancz_params.error, params->lancz_params.max_iterations,
+               (int)params->lancz_params.matvec_precision};
     std::vector<SiteLog> lg;
     const double e = two_site_finite_vmps(c->ctx, m, w, p, &lg);
     c->ctx.sync();
@@ -378,6 +379,12 @@ int udmrg_two_site_finite_vmps(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
 
 int udmrg_matvec_plan_create(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
                              const udmrg_tensor *psi_struct, udmrg_matvec_plan **out) {
+  return udmrg_matvec_plan_create_ex(c, eff_ham, psi_struct, kPrecFP64, out);
+}
+
+int udmrg_matvec_plan_create_ex(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
+                                const udmrg_tensor *psi_struct, int precision,
+                                udmrg_matvec_plan **out) {
   return guarded([&] {
     Ctx &ctx = c->ctx;
     const BTensor &psi = T(psi_struct);
@@ -393,7 +400,7 @@ int udmrg_matvec_plan_create(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
         op[i] = p->promoted[i].get();
       }
     }
-    p->plan = plan_matvec2(ctx, *op[0], *op[1], *op[2], *op[3], psi);
+    p->plan = plan_matvec2(ctx, *op[0], *op[1], *op[2], *op[3], psi, precision);
     *out = p;
   });
 }
@@ -485,6 +492,48 @@ int udmrg_ctx_flush_l2(udmrg_ctx *c, int64_t bytes) {
       c->flush_bytes = bytes;
     }
     UDMRG_CHECK_CUDA(cudaMemsetAsync(c->flush_buf, c->flush_bytes & 0xff, bytes, c->ctx.stream));
+  });
+}
+
+int udmrg_matvec_plan_stage_times(udmrg_matvec_plan *p, const double *d_in, double *d_out,
+                                  double *ms, double *flops) {
+  return guarded([&] {
+    MatvecPlan &m = *p->plan;
+    Ctx &ctx = *p->ctx;
+    float t[4] = {0, 0, 0, 0};
+    if (m.sg) {
+      m.sg->apply_timed(d_in, d_out, t);
+      flops[0] = 0;
+      flops[1] = 6.0 * m.sg->g1.flops;
+      flops[2] = 0;
+      flops[3] = 6.0 * m.sg->g3.flops;
+    } else {
+      const DType dt = m.sstruct->dtype;
+      const int es = elem_doubles(dt);
+      cudaEvent_t ev[5];
+      for (auto &e : ev) UDMRG_CHECK_CUDA(cudaEventCreate(&e));
+      cudaEventRecord(ev[0], ctx.stream);
+      run_gemm(ctx, m.p1->gemm, dt, m.L->data, d_in, m.t1, 1.0, 0.0);
+      cudaEventRecord(ev[1], ctx.stream);
+      run_gemm(ctx, m.p2->gemm, dt, m.t1, m.W1->data, m.t2, 1.0, 0.0);
+      cudaEventRecord(ev[2], ctx.stream);
+      run_gemm(ctx, m.p3->gemm, dt, m.t2, m.W2->data, m.t3, 1.0, 0.0);
+      cudaEventRecord(ev[3], ctx.stream);
+      for (int64_t b : m.missing)
+        UDMRG_CHECK_CUDA(cudaMemsetAsync(d_out + m.sstruct->offs[b] * es, 0,
+                                         m.sstruct->block_elems(b) * es * sizeof(double),
+                                         ctx.stream));
+      run_gemm(ctx, m.p4->gemm, dt, m.t3, m.R->data, d_out, 1.0, 0.0);
+      cudaEventRecord(ev[4], ctx.stream);
+      UDMRG_CHECK_CUDA(cudaEventSynchronize(ev[4]));
+      for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&t[i], ev[i], ev[i + 1]);
+      for (auto &e : ev) cudaEventDestroy(e);
+      flops[0] = m.p1->gemm.flops;
+      flops[1] = m.p2->gemm.flops;
+      flops[2] = m.p3->gemm.flops;
+      flops[3] = m.p4->gemm.flops;
+    }
+    for (int i = 0; i < 4; ++i) ms[i] = t[i];
   });
 }
 

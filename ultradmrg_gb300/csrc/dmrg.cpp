@@ -78,7 +78,7 @@ MatvecPlan::~MatvecPlan() {
 
 std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTensor &W1,
                                          const BTensor &W2, const BTensor &R,
-                                         const BTensor &psi0) {
+                                         const BTensor &psi0, int precision) {
   UDMRG_REQUIRE(psi0.rank() == 4 && L.rank() == 3 && R.rank() == 3 && W1.rank() == 4 &&
                     W2.rank() == 4,
                 "matvec: expects L(3), W1(4), W2(4), R(3), psi(4)");
@@ -104,15 +104,26 @@ std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTens
   }
   mv->p4 = plan_contract_into(*mv->p3->out, R, ca, cb, fa, fb, *S, &mv->missing);
   mv->sstruct = std::move(S);
+  mv->flops = mv->p1->gemm.flops + mv->p2->gemm.flops + mv->p3->gemm.flops + mv->p4->gemm.flops;
+  mv->precision = precision;
+  if (precision == kPrecMixed) {
+    UDMRG_REQUIRE(psi0.dtype == kF64, "mixed-precision matvec: real tensors only");
+    mv->sg = plan_sg_matvec(ctx, L, W1, W2, R, *mv->sstruct);
+    return mv;
+  }
+  UDMRG_REQUIRE(precision == kPrecFP64, "matvec: unknown precision");
   const int es = elem_doubles(psi0.dtype);
   mv->t1 = (double *)ctx.alloc(std::max<int64_t>(mv->p1->out->size(), 1) * es * sizeof(double));
   mv->t2 = (double *)ctx.alloc(std::max<int64_t>(mv->p2->out->size(), 1) * es * sizeof(double));
   mv->t3 = (double *)ctx.alloc(std::max<int64_t>(mv->p3->out->size(), 1) * es * sizeof(double));
-  mv->flops = mv->p1->gemm.flops + mv->p2->gemm.flops + mv->p3->gemm.flops + mv->p4->gemm.flops;
   return mv;
 }
 
 void MatvecPlan::apply(const double *in, double *out) {
+  if (sg) {
+    sg->apply(in, out);
+    return;
+  }
   const DType dt = sstruct->dtype;
   const int es = elem_doubles(dt);
   run_gemm(*ctx, p1->gemm, dt, L->data, in, t1, 1.0, 0.0);
@@ -280,6 +291,8 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
     return out;
   };
   auto finish = [&](int64_t m, const std::vector<double> &vec) {
+    if (mv.sg && (tc_check(ctx, mv.sg->g1) | tc_check(ctx, mv.sg->g3)))
+      throw Error(kErrTimeout, "tcgen05 GEMM: a bounded device wait ran out");
     auto gs = S.clone_struct();
     gs->alloc_data();
     std::vector<const double *> vs(bases.v.begin(), bases.v.begin() + m);
@@ -517,7 +530,8 @@ static double two_site_update(Ctx &ctx, std::vector<TensorPtr> &mps,
   }
   const double t0 = now();
   auto init_state = contract_axes(ctx, *mps[l], *mps[r], {2}, {0});
-  auto mv = plan_matvec2(ctx, *lenvs[lenv_len], *mpo[l], *mpo[r], *renvs[renv_len], *init_state);
+  auto mv = plan_matvec2(ctx, *lenvs[lenv_len], *mpo[l], *mpo[r], *renvs[renv_len], *init_state,
+                         p.lancz.precision);
   auto lres = lanczos_gs(ctx, *mv, *init_state, p.lancz);
   const double t1 = now();
   const double mvflops = mv->flops;

@@ -1,9 +1,14 @@
 // Two-site update: matvec plan, Lanczos solvers, environment updates, sweeps.
 #pragma once
 
+#include "sg_matvec.hpp"
 #include "svd.hpp"
 
 namespace udmrg {
+
+// Matvec precision: plain FP64 block GEMMs, or split-BF16 tcgen05 GEMMs with
+// FP32 accumulation (Krylov vectors, dots and the tridiagonal problem stay FP64).
+enum Precision : int { kPrecFP64 = 0, kPrecMixed = 1 };
 
 // Block-sparse ops built on plan + run.
 TensorPtr contract_axes(Ctx &ctx, const BTensor &A, const BTensor &B, const std::vector<int> &ca,
@@ -29,17 +34,20 @@ struct MatvecPlan {
   std::vector<int64_t> missing;  // blocks of sstruct the matvec does not write
   double *t1 = nullptr, *t2 = nullptr, *t3 = nullptr;
   double flops = 0;  // algorithmic flops of one matvec
+  int precision = kPrecFP64;
+  std::unique_ptr<SgMatvecPlan> sg;  // the mixed-precision form
   ~MatvecPlan();
   void apply(const double *in, double *out);  // device buffers in sstruct layout
 };
 
 std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTensor &W1,
                                          const BTensor &W2, const BTensor &R,
-                                         const BTensor &psi0);
+                                         const BTensor &psi0, int precision = kPrecFP64);
 
 struct LanczosParams {
   double error = 1e-7;
   int64_t max_iterations = 200;
+  int precision = kPrecFP64;
 };
 
 struct LanczosResult {

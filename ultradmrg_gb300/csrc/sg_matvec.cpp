@@ -1,0 +1,333 @@
+#include "sg_matvec.hpp"
+
+#include <map>
+
+namespace udmrg {
+
+SgMatvecPlan::~SgMatvecPlan() {
+  if (!ctx) return;
+  for (void *p : {(void *)l_img, (void *)psi_img, (void *)t3_img, (void *)r_img, (void *)t1,
+                  (void *)d_psi_ops, (void *)d_targets, (void *)d_sources, (void *)d_coefs})
+    ctx->free(p);
+}
+
+namespace {
+
+template <typename V>
+V *upload_vec(Ctx &ctx, const std::vector<V> &v) {
+  if (v.empty()) return nullptr;
+  V *d = (V *)ctx.alloc(v.size() * sizeof(V));
+  UDMRG_CHECK_CUDA(
+      cudaMemcpyAsync(d, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice, ctx.stream));
+  return d;
+}
+
+std::vector<double> download(Ctx &ctx, const BTensor &t) {
+  std::vector<double> h(t.size());
+  if (t.size())
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(h.data(), t.data, t.size() * sizeof(double),
+                                     cudaMemcpyDeviceToHost, ctx.stream));
+  ctx.sync();
+  return h;
+}
+
+using Key = std::vector<int32_t>;
+
+struct T1Block {
+  int64_t origin;  // element offset of (a'=0, w=0, s1=s2=0, b=0)
+  int64_t pitch;
+  int32_t dw, ds12;
+};
+
+}  // namespace
+
+std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const BTensor &W1,
+                                             const BTensor &W2, const BTensor &R,
+                                             const BTensor &S) {
+  UDMRG_REQUIRE(L.dtype == kF64 && W1.dtype == kF64 && W2.dtype == kF64 && R.dtype == kF64 &&
+                    S.dtype == kF64,
+                "mixed matvec: real FP64 tensors required");
+  auto p = std::make_unique<SgMatvecPlan>();
+  p->ctx = &ctx;
+  p->g1.ctx = &ctx;
+  p->g3.ctx = &ctx;
+  p->psi_size = S.size();
+  auto dim = [](const BTensor &t, int64_t b, int ax) { return t.idx[ax].dims[t.key(b)[ax]]; };
+
+  // ---------------- step 1 groups: one per ket sector A ----------------------
+  const int nA = L.idx[2].nsec();
+  std::vector<std::vector<int64_t>> lrows(nA), pcols(nA);
+  for (int64_t b = 0; b < L.nblocks(); ++b) lrows[L.key(b)[2]].push_back(b);
+  for (int64_t b = 0; b < S.nblocks(); ++b) pcols[S.key(b)[0]].push_back(b);
+  std::map<Key, T1Block> t1map;  // (A', W, S1, S2, B) -> location in T1
+  std::vector<PackOp> lops;
+  int64_t t1tot = 0, lbytes = 0, pbytes = 0;
+  struct G1 {
+    int A;
+    int64_t M, N, K, t1_off, l_off, p_off;
+  };
+  std::vector<G1> g1s;
+  for (int A = 0; A < nA; ++A) {
+    if (lrows[A].empty() || pcols[A].empty()) continue;
+    G1 g{A, 0, 0, L.idx[2].dims[A], t1tot, lbytes, pbytes};
+    std::vector<int64_t> rof, cof;
+    for (int64_t b : lrows[A]) {
+      rof.push_back(g.M);
+      g.M += dim(L, b, 0) * dim(L, b, 1);
+    }
+    for (int64_t b : pcols[A]) {
+      cof.push_back(g.N);
+      g.N += dim(S, b, 1) * dim(S, b, 2) * dim(S, b, 3);
+    }
+    UDMRG_REQUIRE(g.M < (1 << 30) && g.N < (1 << 30) && g.K < (1 << 30), "mixed matvec: group too large");
+    const int32_t kc = (int32_t)((g.K + kTcBK - 1) / kTcBK);
+    for (size_t i = 0; i < lrows[A].size(); ++i) {
+      const int64_t b = lrows[A][i];
+      PackOp op{};
+      op.src_off = L.offs[b];
+      op.src_rs = g.K;
+      op.src_cs = 1;
+      op.img_off = g.l_off;
+      op.rows = (int32_t)(dim(L, b, 0) * dim(L, b, 1));
+      op.cols = (int32_t)g.K;
+      op.r0 = (int32_t)rof[i];
+      op.k0 = 0;
+      op.kc = kc;
+      op.tr = kTcBM;
+      lops.push_back(op);
+    }
+    for (size_t j = 0; j < pcols[A].size(); ++j) {
+      const int64_t b = pcols[A][j];
+      const int64_t ncol = dim(S, b, 1) * dim(S, b, 2) * dim(S, b, 3);
+      PackOp op{};
+      op.src_off = S.offs[b];
+      op.src_rs = 1;
+      op.src_cs = ncol;
+      op.img_off = g.p_off;
+      op.rows = (int32_t)ncol;
+      op.cols = (int32_t)g.K;
+      op.r0 = (int32_t)cof[j];
+      op.k0 = 0;
+      op.kc = kc;
+      op.tr = kTcBN;
+      p->psi_ops.push_back(op);
+    }
+    // T1 block locations
+    for (size_t i = 0; i < lrows[A].size(); ++i) {
+      const int64_t lb = lrows[A][i];
+      for (size_t j = 0; j < pcols[A].size(); ++j) {
+        const int64_t pb = pcols[A][j];
+        Key k = {L.key(lb)[0], L.key(lb)[1], S.key(pb)[1], S.key(pb)[2], S.key(pb)[3]};
+        T1Block t;
+        t.origin = g.t1_off + rof[i] * g.N + cof[j];
+        t.pitch = g.N;
+        t.dw = (int32_t)dim(L, lb, 1);
+        t.ds12 = (int32_t)(dim(S, pb, 1) * dim(S, pb, 2));
+        t1map[k] = t;
+      }
+    }
+    t1tot += g.M * g.N;
+    lbytes += tc_image_bytes(g.M, g.K, kTcBM);
+    pbytes += tc_image_bytes(g.N, g.K, kTcBN);
+    g1s.push_back(g);
+  }
+  p->t1_size = t1tot;
+  p->l_bytes = lbytes;
+  p->psi_bytes = pbytes;
+
+  // ---------------- step 3 groups: one per bra sector B' of R -----------------
+  const int nB = R.idx[0].nsec();
+  std::vector<std::vector<int64_t>> rks(nB), orows(nB);
+  for (int64_t b = 0; b < R.nblocks(); ++b) rks[R.key(b)[0]].push_back(b);
+  for (int64_t b = 0; b < S.nblocks(); ++b) orows[S.key(b)[3]].push_back(b);
+  std::vector<PackOp> rops;
+  int64_t t3bytes = 0, rbytes = 0;
+  // host copies of the MPO tensors for the fused coefficients
+  const std::vector<double> w1h = download(ctx, W1), w2h = download(ctx, W2);
+  // W1 blocks by (s1_out); W2 blocks by (wr, s2_out, w2)
+  std::map<int32_t, std::vector<int64_t>> w1_by_s1o;
+  for (int64_t b = 0; b < W1.nblocks(); ++b) w1_by_s1o[W1.key(b)[2]].push_back(b);
+  std::map<Key, std::vector<int64_t>> w2_by;  // (wr, s2out, w2)
+  for (int64_t b = 0; b < W2.nblocks(); ++b)
+    w2_by[{W2.key(b)[0], W2.key(b)[2], W2.key(b)[3]}].push_back(b);
+  for (int Bp = 0; Bp < nB; ++Bp) {
+    if (orows[Bp].empty()) continue;
+    const int64_t dBp = R.idx[0].dims[Bp];
+    int64_t M = 0, K = 0;
+    std::vector<int64_t> rof, kof;
+    for (int64_t b : orows[Bp]) {
+      rof.push_back(M);
+      M += dim(S, b, 0) * dim(S, b, 1) * dim(S, b, 2);
+    }
+    for (int64_t b : rks[Bp]) {
+      kof.push_back(K);
+      K += dim(R, b, 1) * dim(R, b, 2);
+    }
+    UDMRG_REQUIRE(M < (1 << 30) && K < (1 << 30), "mixed matvec: group too large");
+    const int32_t kc = (int32_t)((K + kTcBK - 1) / kTcBK);
+    const int64_t t3_off = t3bytes, r_off = rbytes;
+    std::vector<int64_t> rows(M);
+    for (size_t i = 0; i < orows[Bp].size(); ++i) {
+      const int64_t b = orows[Bp][i];
+      const int64_t nr = dim(S, b, 0) * dim(S, b, 1) * dim(S, b, 2);
+      for (int64_t m = 0; m < nr; ++m) rows[rof[i] + m] = S.offs[b] + m * dBp;
+    }
+    for (size_t j = 0; j < rks[Bp].size(); ++j) {
+      const int64_t b = rks[Bp][j];
+      PackOp op{};
+      op.src_off = R.offs[b];
+      op.src_rs = dim(R, b, 1) * dim(R, b, 2);
+      op.src_cs = 1;
+      op.img_off = r_off;
+      op.rows = (int32_t)dBp;
+      op.cols = (int32_t)(dim(R, b, 1) * dim(R, b, 2));
+      op.r0 = 0;
+      op.k0 = (int32_t)kof[j];
+      op.kc = kc;
+      op.tr = kTcBN;
+      rops.push_back(op);
+    }
+    // MPO-step targets of this group
+    for (size_t i = 0; i < orows[Bp].size(); ++i) {
+      const int64_t ob = orows[Bp][i];
+      const int32_t Ap = S.key(ob)[0], S1p = S.key(ob)[1], S2p = S.key(ob)[2];
+      const int32_t da = (int32_t)dim(S, ob, 0);
+      const int32_t ds1p = (int32_t)dim(S, ob, 1), ds2p = (int32_t)dim(S, ob, 2);
+      for (size_t j = 0; j < rks[Bp].size(); ++j) {
+        const int64_t rb = rks[Bp][j];
+        const int32_t W2s = R.key(rb)[1], Bs = R.key(rb)[2];
+        const int32_t dw2 = (int32_t)dim(R, rb, 1), db = (int32_t)dim(R, rb, 2);
+        MpoTarget tg{};
+        tg.img_off = t3_off;
+        tg.row0 = (int32_t)rof[i];
+        tg.k0 = (int32_t)kof[j];
+        tg.kc = kc;
+        tg.da = da;
+        tg.db = db;
+        tg.ds12p = ds1p * ds2p;
+        tg.dw2 = dw2;
+        tg.nout = tg.ds12p * dw2;
+        tg.src0 = (int32_t)p->sources.size();
+        // sources: T1 blocks (A', W, S1, S2, B) through W1 (W,S1,S1p,Wr) W2 (Wr,S2,S2p,W2s)
+        std::map<Key, std::vector<double>> acc;  // (W, S1, S2) -> coef
+        auto it1 = w1_by_s1o.find(S1p);
+        if (it1 != w1_by_s1o.end()) {
+          for (int64_t b1 : it1->second) {
+            const int32_t Ws = W1.key(b1)[0], S1 = W1.key(b1)[1], Wr = W1.key(b1)[3];
+            for (int32_t S2 = 0; S2 < W2.idx[1].nsec(); ++S2) {
+              auto it2 = w2_by.find({Wr, S2p, W2s});
+              if (it2 == w2_by.end()) break;
+              for (int64_t b2 : it2->second) {
+                if (W2.key(b2)[1] != S2) continue;
+                Key src = {Ap, Ws, S1, S2, Bs};
+                if (!t1map.count(src)) continue;
+                const int64_t dw = W1.idx[0].dims[Ws], ds1 = W1.idx[1].dims[S1];
+                const int64_t dwr = W1.idx[3].dims[Wr], ds2 = W2.idx[1].dims[S2];
+                const int64_t nin = dw * ds1 * ds2;
+                auto &c = acc[{Ws, S1, S2}];
+                if (c.empty()) c.assign(nin * tg.nout, 0.0);
+                // W1(w, s1, s1', wr) W2(wr, s2, s2', w2), blocks row-major
+                const double *w1 = w1h.data() + W1.offs[b1];
+                const double *w2 = w2h.data() + W2.offs[b2];
+                for (int64_t w = 0; w < dw; ++w)
+                  for (int64_t s1 = 0; s1 < ds1; ++s1)
+                    for (int64_t s2 = 0; s2 < ds2; ++s2)
+                      for (int64_t s1o = 0; s1o < ds1p; ++s1o)
+                        for (int64_t s2o = 0; s2o < ds2p; ++s2o)
+                          for (int64_t w2i = 0; w2i < dw2; ++w2i) {
+                            double v = 0;
+                            for (int64_t wr = 0; wr < dwr; ++wr)
+                              v += w1[((w * ds1 + s1) * ds1p + s1o) * dwr + wr] *
+                                   w2[((wr * ds2 + s2) * ds2p + s2o) * dw2 + w2i];
+                            const int64_t ic = (w * ds1 + s1) * ds2 + s2;
+                            const int64_t oc = (s1o * ds2p + s2o) * dw2 + w2i;
+                            c[ic * tg.nout + oc] += v;
+                          }
+              }
+            }
+          }
+        }
+        for (auto &kv : acc) {
+          bool nz = false;
+          for (double v : kv.second) nz |= (v != 0.0);
+          if (!nz) continue;
+          const Key src = {Ap, kv.first[0], kv.first[1], kv.first[2], Bs};
+          const T1Block &tb = t1map.at(src);
+          MpoSource s{};
+          s.t1_off = tb.origin;
+          s.row_pitch = tb.pitch;
+          s.dw = tb.dw;
+          s.ds12 = tb.ds12;
+          s.coef_off = (int32_t)p->coefs.size();
+          for (double v : kv.second) p->coefs.push_back((float)v);
+          p->sources.push_back(s);
+        }
+        tg.nsrc = (int32_t)p->sources.size() - tg.src0;
+        UDMRG_REQUIRE(tg.nout <= 32, "mixed matvec: more than 32 MPO output channels per block");
+        if (tg.nsrc > 0) p->targets.push_back(tg);
+      }
+    }
+    p->g3.add_group(t3_off, r_off, (int32_t)M, (int32_t)dBp, (int32_t)K, rows);
+    t3bytes += tc_image_bytes(M, K, kTcBM);
+    rbytes += tc_image_bytes(dBp, K, kTcBN);
+  }
+  p->t3_bytes = t3bytes;
+  p->r_bytes = rbytes;
+
+  // ---------------- allocate, pack the fixed operands -------------------------
+  auto zalloc = [&](int64_t bytes) {
+    uint8_t *d = (uint8_t *)ctx.alloc(std::max<int64_t>(bytes, 256));
+    UDMRG_CHECK_CUDA(cudaMemsetAsync(d, 0, std::max<int64_t>(bytes, 256), ctx.stream));
+    return d;
+  };
+  p->l_img = zalloc(lbytes);
+  p->psi_img = zalloc(pbytes);
+  p->t3_img = zalloc(t3bytes);
+  p->r_img = zalloc(rbytes);
+  p->t1 = (float *)ctx.alloc(std::max<int64_t>(t1tot, 1) * sizeof(float));
+  run_pack(ctx, lops, nullptr, (int)lops.size(), L.data, true, p->l_img);
+  run_pack(ctx, rops, nullptr, (int)rops.size(), R.data, true, p->r_img);
+  p->d_psi_ops = upload_pack_ops(ctx, p->psi_ops);
+  for (auto &g : g1s) {
+    std::vector<int64_t> rows(g.M);
+    for (int64_t m = 0; m < g.M; ++m) rows[m] = g.t1_off + m * g.N;
+    p->g1.add_group(g.l_off, g.p_off, (int32_t)g.M, (int32_t)g.N, (int32_t)g.K, rows);
+  }
+  p->g1.finalize();
+  p->g3.finalize();
+  p->d_targets = upload_vec(ctx, p->targets);
+  p->d_sources = upload_vec(ctx, p->sources);
+  p->d_coefs = upload_vec(ctx, p->coefs);
+  p->mixed_flops = 6.0 * (p->g1.flops + p->g3.flops);
+  ctx.sync();
+  return p;
+}
+
+void SgMatvecPlan::apply(const double *psi_in, double *out) {
+  run_pack(*ctx, psi_ops, d_psi_ops, (int)psi_ops.size(), psi_in, true, psi_img);
+  run_tc_gemm(*ctx, g1, l_img, psi_img, t1, kTcOutF32, 1.0);
+  run_mpo_step(*ctx, *this);
+  run_tc_gemm(*ctx, g3, t3_img, r_img, out, kTcOutF64, 1.0);
+}
+
+void SgMatvecPlan::apply_timed(const double *psi_in, double *out, float ms[4]) {
+  cudaEvent_t ev[5];
+  for (auto &e : ev) UDMRG_CHECK_CUDA(cudaEventCreate(&e));
+  cudaEventRecord(ev[0], ctx->stream);
+  run_pack(*ctx, psi_ops, d_psi_ops, (int)psi_ops.size(), psi_in, true, psi_img);
+  cudaEventRecord(ev[1], ctx->stream);
+  run_tc_gemm(*ctx, g1, l_img, psi_img, t1, kTcOutF32, 1.0);
+  cudaEventRecord(ev[2], ctx->stream);
+  run_mpo_step(*ctx, *this);
+  cudaEventRecord(ev[3], ctx->stream);
+  run_tc_gemm(*ctx, g3, t3_img, r_img, out, kTcOutF64, 1.0);
+  cudaEventRecord(ev[4], ctx->stream);
+  UDMRG_CHECK_CUDA(cudaEventSynchronize(ev[4]));
+  for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
+  for (auto &e : ev) cudaEventDestroy(e);
+  int st = tc_check(*ctx, g1);
+  st |= tc_check(*ctx, g3);
+  if (st) throw Error(kErrTimeout, "tcgen05 GEMM: a bounded device wait ran out");
+}
+
+}  // namespace udmrg

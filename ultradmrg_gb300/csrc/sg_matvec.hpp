@@ -1,0 +1,80 @@
+// Mixed-precision two-site matvec on the tensor cores, regrouped by sector.
+//
+// H_eff psi = L . (W1 W2) . R . psi is computed as
+//   step 1 (tcgen05): for every ket sector A of L, one dense GEMM
+//          T1_A[(a',w) x (s1 s2 b)] = L_A[(a',w) x a] . Psi_A[a x (s1 s2 b)],
+//          where L_A stacks all L blocks (A',W,A) and Psi_A all psi blocks
+//          (A,S1,S2,B); every entry of T1_A is a T1 block entry, none padding;
+//   step 2 (CUDA cores): T3[a',s1',s2',w2,b] = sum W1 W2 T1 over (w, s1, s2)
+//          with the two MPO tensors contracted over their shared bond,
+//          written straight into split-BF16 tile images of the step-3 operand;
+//   step 3 (tcgen05): for every bra sector B' of R, one dense GEMM
+//          res_B'[(a',s1',s2') x b'] = T3_B'[(a',s1',s2') x (w2,b)] . R_B'[b' x (w2,b)]^T.
+// L_A and R_B' images are packed once per plan (the environments are fixed
+// during a Lanczos solve); psi is packed every matvec.  T1 is FP32.
+#pragma once
+
+#include "gemm.hpp"
+#include "tc_gemm.hpp"
+
+namespace udmrg {
+
+// One MPO-step target: a T3 block (a', s1', s2', w2, b) in the step-3 image.
+struct MpoTarget {
+  int64_t img_off;     // byte offset of the group's A image (step-3 arena)
+  int32_t row0;        // first image row of the block (a' = 0, s1' = s2' = 0)
+  int32_t k0;          // first image column (w2 = 0, b = 0)
+  int32_t kc;          // K chunks of the image
+  int32_t da, db;      // a' and b sector dims
+  int32_t nout;        // output channels per (a', b): ds1' * ds2' * dw2
+  int32_t ds12p;       // ds1' * ds2'
+  int32_t dw2;
+  int32_t src0, nsrc;  // source list
+};
+
+// One MPO-step source: a T1 block (a', w, s1, s2, b) in T1_A and its
+// coefficient matrix coef[(w s1 s2) x (s1' s2' w2)].
+struct MpoSource {
+  int64_t t1_off;      // element offset of entry (a'=0, w=0, s1=s2=0, b=0) in T1
+  int64_t row_pitch;   // T1 elements between consecutive (a', w) rows (N_A)
+  int32_t dw, ds12;    // w dim, ds1 * ds2
+  int32_t coef_off;    // offset into the coefficient array
+  int32_t pad;
+};
+
+struct SgMatvecPlan {
+  Ctx *ctx = nullptr;
+  int64_t psi_size = 0;
+  // images
+  uint8_t *l_img = nullptr, *psi_img = nullptr, *t3_img = nullptr, *r_img = nullptr;
+  int64_t l_bytes = 0, psi_bytes = 0, t3_bytes = 0, r_bytes = 0;
+  float *t1 = nullptr;
+  int64_t t1_size = 0;
+  // psi pack ops (device resident)
+  std::vector<PackOp> psi_ops;
+  PackOp *d_psi_ops = nullptr;
+  // GEMM plans
+  TcPlan g1, g3;
+  // MPO step
+  std::vector<MpoTarget> targets;
+  std::vector<MpoSource> sources;
+  std::vector<float> coefs;
+  MpoTarget *d_targets = nullptr;
+  MpoSource *d_sources = nullptr;
+  float *d_coefs = nullptr;
+  double mixed_flops = 0;  // tensor-core work actually issued (2MNK per group, x6 products)
+  ~SgMatvecPlan();
+  void apply(const double *psi_in, double *out);
+  // apply with CUDA events between the stages: ms[0] psi pack, ms[1] GEMM
+  // L.psi, ms[2] MPO step, ms[3] GEMM .R
+  void apply_timed(const double *psi_in, double *out, float ms[4]);
+};
+
+// L(a',w,a), W1, W2, R(b',w2,b) real FP64; S the Krylov structure of psi.
+std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const BTensor &W1,
+                                             const BTensor &W2, const BTensor &R,
+                                             const BTensor &S);
+
+void run_mpo_step(Ctx &ctx, const SgMatvecPlan &p);
+
+}  // namespace udmrg
