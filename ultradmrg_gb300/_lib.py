@@ -24,7 +24,8 @@ class LanczosParams(C.Structure):
 
 class LanczosRes(C.Structure):
     _fields_ = [("iters", C.c_int64), ("gs_eng", C.c_double), ("gs_vec", C.c_void_p),
-                ("matvec_seconds", C.c_double), ("matvecs", C.c_int64)]
+                ("matvec_seconds", C.c_double), ("matvecs", C.c_int64),
+                ("ritz_eng", C.c_double), ("fp64_matvecs", C.c_int64)]
 
 
 class SweepParams(C.Structure):

@@ -232,6 +232,8 @@ class LanczosResult:
     gs_vec: DeviceTensor
     matvec_seconds: float
     matvecs: int
+    ritz_eng: float = 0.0
+    fp64_matvecs: int = 0
 
 
 PREC_FP64, PREC_MIXED = 0, 1
@@ -243,7 +245,8 @@ def lanczos_solver(ctx, eff_ham, init_state, error=1e-7, max_iterations=200,
     r = _lib.LanczosRes()
     call("udmrg_lanczos_solver", ctx.h, _handles(eff_ham), init_state.h, C.byref(p), C.byref(r))
     return LanczosResult(int(r.iters), float(r.gs_eng), _new(ctx, C.c_void_p(r.gs_vec)),
-                         float(r.matvec_seconds), int(r.matvecs))
+                         float(r.matvec_seconds), int(r.matvecs), float(r.ritz_eng),
+                         int(r.fp64_matvecs))
 
 
 def lanczos_expmv_solver(ctx, eff_ham, init_state, step, error=1e-10, max_iterations=20):

@@ -289,6 +289,8 @@ int udmrg_lanczos_solver(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
     res->gs_eng = r.gs_eng;
     res->matvec_seconds = r.matvec_seconds;
     res->matvecs = r.matvecs;
+    res->ritz_eng = r.ritz_eng;
+    res->fp64_matvecs = r.fp64_matvecs;
     res->gs_vec = wrap(std::move(r.gs_vec));
   });
 }

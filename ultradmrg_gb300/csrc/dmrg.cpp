@@ -106,12 +106,12 @@ std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTens
   mv->sstruct = std::move(S);
   mv->flops = mv->p1->gemm.flops + mv->p2->gemm.flops + mv->p3->gemm.flops + mv->p4->gemm.flops;
   mv->precision = precision;
+  UDMRG_REQUIRE(precision == kPrecFP64 || precision == kPrecMixed, "matvec: unknown precision");
   if (precision == kPrecMixed) {
     UDMRG_REQUIRE(psi0.dtype == kF64, "mixed-precision matvec: real tensors only");
     mv->sg = plan_sg_matvec(ctx, L, W1, W2, R, *mv->sstruct);
-    return mv;
   }
-  UDMRG_REQUIRE(precision == kPrecFP64, "matvec: unknown precision");
+  // the FP64 form is kept in both modes (the mixed solver's final Rayleigh quotient)
   const int es = elem_doubles(psi0.dtype);
   mv->t1 = (double *)ctx.alloc(std::max<int64_t>(mv->p1->out->size(), 1) * es * sizeof(double));
   mv->t2 = (double *)ctx.alloc(std::max<int64_t>(mv->p2->out->size(), 1) * es * sizeof(double));
@@ -124,6 +124,10 @@ void MatvecPlan::apply(const double *in, double *out) {
     sg->apply(in, out);
     return;
   }
+  apply_fp64(in, out);
+}
+
+void MatvecPlan::apply_fp64(const double *in, double *out) {
   const DType dt = sstruct->dtype;
   const int es = elem_doubles(dt);
   run_gemm(*ctx, p1->gemm, dt, L->data, in, t1, 1.0, 0.0);
@@ -277,6 +281,7 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
   Bases bases(ctx);
   std::vector<double> a(maxit, 0.0), b(maxit, 0.0), N(maxit, 0.0);
   LanczosResult res;
+  const bool mixed = mv.sg != nullptr;
   EventTimer ev;
   float ms = 0;
   auto matvec = [&](const double *in) {
@@ -306,7 +311,41 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
     } else {
       lincomb(w, gs->data, vs, coef, n, false);
     }
+    if (mixed) {
+      // reported energy: FP64 Rayleigh quotient of the mixed-precision eigenvector
+      double *y = (double *)ctx.alloc(vbytes);
+      mv.apply_fp64(gs->data, y);
+      const double num = dot(w, gs->data, y, n, cplx).real();
+      const double den = dot(w, gs->data, gs->data, n, cplx).real();
+      ctx.free(y);
+      res.ritz_eng = res.gs_eng;
+      res.gs_eng = num / den;
+      res.fp64_matvecs = 1;
+    }
     return gs;
+  };
+  // Mixed precision: FP64 Gram-Schmidt (twice) of every new Lanczos vector
+  // against all previous ones, so rounding in the matvec cannot build up
+  // ghost Ritz values; returns |gamma|.
+  auto reorthogonalize = [&](double *gamma, int64_t m) {
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int64_t j = 0; j < m; ++j) dot_async(w, bases.v[j], gamma, n, cplx, w.result + 2 * j);
+      double *h = ctx.host_scratch(2 * m + 2);
+      UDMRG_CHECK_CUDA(cudaMemcpyAsync(h, w.result, 2 * m * sizeof(double),
+                                       cudaMemcpyDeviceToHost, ctx.stream));
+      ctx.sync();
+      std::vector<double> c(h, h + 2 * m);
+      std::vector<const double *> vs = {gamma};
+      std::vector<double> coef = {1.0};
+      if (cplx) coef.push_back(0.0);
+      for (int64_t j = 0; j < m; ++j) {
+        vs.push_back(bases.v[j]);
+        coef.push_back(-c[2 * j]);
+        if (cplx) coef.push_back(-c[2 * j + 1]);
+      }
+      lincomb(w, gamma, vs, coef, n, cplx);
+    }
+    return std::sqrt(norm2(w, gamma, nd));
   };
   // bases[0] = init / |init| (QuasiNormalize)
   {
@@ -332,7 +371,8 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
     UDMRG_CHECK_CUDA(
         cudaMemcpyAsync(hres, w.result, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
     ctx.sync();
-    const double norm_gamma = std::sqrt(hres[0]);
+    double norm_gamma = std::sqrt(hres[0]);
+    if (mixed && norm_gamma != 0.0) norm_gamma = reorthogonalize(gamma, m);
     if (norm_gamma == 0.0) {
       ctx.free(gamma);
       if (m == 1) {
@@ -355,7 +395,10 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
     last = matvec(bases.v[m]);
     a[m] = dot(w, bases.v[m], last, n, cplx).real();
     const double e_new = tridiag_lowest(a, b, m + 1, nullptr);
-    if ((energy0 - e_new) < p.error || m == eff_dim || m == maxit - 1) {
+    // mixed precision also stops once the Ritz value no longer moves above the
+    // rounding level of the split-BF16 products
+    const bool noise_floor = mixed && std::fabs(energy0 - e_new) <= 1e-12 * std::fabs(e_new);
+    if ((energy0 - e_new) < p.error || noise_floor || m == eff_dim || m == maxit - 1) {
       std::vector<double> vec;
       tridiag_lowest(a, b, m + 1, &vec);
       ctx.free(last);

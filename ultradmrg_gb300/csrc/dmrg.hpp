@@ -37,7 +37,8 @@ struct MatvecPlan {
   int precision = kPrecFP64;
   std::unique_ptr<SgMatvecPlan> sg;  // the mixed-precision form
   ~MatvecPlan();
-  void apply(const double *in, double *out);  // device buffers in sstruct layout
+  void apply(const double *in, double *out);       // device buffers in sstruct layout
+  void apply_fp64(const double *in, double *out);  // always the plain FP64 form
 };
 
 std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTensor &W1,
@@ -56,6 +57,8 @@ struct LanczosResult {
   TensorPtr gs_vec;
   double matvec_seconds = 0;  // device time spent in matvecs (CUDA events)
   int64_t matvecs = 0;
+  double ritz_eng = 0;       // mixed precision: the last Ritz value
+  int64_t fp64_matvecs = 0;  // mixed precision: FP64 matvecs (final Rayleigh quotient)
 };
 
 // Ground state by Lanczos (lanczos_vmps_solver_impl.h:114-248): three-term

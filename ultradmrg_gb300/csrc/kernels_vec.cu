@@ -150,7 +150,7 @@ int ew_grid(const Ctx &ctx, int64_t n) {
 
 VecWork::VecWork(Ctx &c) : ctx(c) {
   partial = (double *)ctx.alloc(sizeof(double) * 2 * 8 * 1024);
-  result = (double *)ctx.alloc(sizeof(double) * 64);
+  result = (double *)ctx.alloc(sizeof(double) * 2 * kMaxVecs);
   ptrs = (const double **)ctx.alloc(sizeof(double *) * kMaxVecs);
   coefs = (double *)ctx.alloc(sizeof(double) * 2 * kMaxVecs);
 }
