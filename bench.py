@@ -132,11 +132,9 @@ def cpu_problem(w):
     L = ovmps.trivial_lenv(mps[0], mpo[0])
     for i in range(l):
         L = ovmps.update_site_lenvs(L, mps[i], mpo[i])
-        L = bs.scale(L, 1.0 / max(bs.norm(L), 1e-300))
     R = ovmps.trivial_renv(mps[N - 1], mpo[N - 1])
     for i in range(N - 1, l + 1, -1):
         R = ovmps.update_site_renvs(R, mps[i], mpo[i])
-        R = bs.scale(R, 1.0 / max(bs.norm(R), 1e-300))
     psi = bs.contract(mps[l], mps[l + 1], [2], [0])
     return [L, mpo[l], mpo[l + 1], R], psi
 
@@ -239,7 +237,7 @@ def run_ours(args):
     ctx = api.Context(local)
     mpo, mps = build_host(w)
     l = w.centre
-    L, R = api.build_envs(ctx, mpo, mps, l)
+    L, R = api.build_envs(ctx, mpo, mps, l, normalize=False)
     A1 = api.DeviceTensor.from_data(ctx, mps[l])
     A2 = api.DeviceTensor.from_data(ctx, mps[l + 1])
     psi = api.contract(ctx, A1, A2, [2], [0])

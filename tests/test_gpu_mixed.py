@@ -14,7 +14,8 @@ import pytest
 
 from oracle import blocksparse as bs
 from oracle import krylov, vmps as ovmps
-from systems import heisenberg_system, hubbard_system, max_block_diff, two_site_problem
+from systems import (canonical_system, heisenberg_system, hubbard_system, max_block_diff,
+                     two_site_problem)
 from ultradmrg_gb300 import api, models as M
 
 pytestmark = pytest.mark.gpu
@@ -61,10 +62,12 @@ def test_mixed_matvec_parity(ctx, name, l):
     assert d <= 2e-5 * s, (d, s)
 
 
-@pytest.mark.parametrize("name,l", [("heis", 4), ("hub", 2), ("hub_big", 3)])
+@pytest.mark.parametrize("name,l", [("heis", 4), ("hub", 2), ("hub_big", 3), ("hub_big", 1)])
 def test_mixed_lanczos_energy(ctx, name, l):
-    mpo, mps = SYSTEMS[name]()
-    eff, psi = two_site_problem(mpo, mps, l)
+    """Mixed-canonical environments (the scale of a DMRG run): the FP64
+    Rayleigh quotient of the mixed-precision ground state vs FP64 Lanczos."""
+    mpo, mps = canonical_system(name, l, seed=5)
+    eff, psi = two_site_problem(mpo, mps, l, normalize=False)
     ref = krylov.lanczos_solver(eff, psi.copy(), krylov.eff_ham_mul_two_site_state,
                                 krylov.LanczosParams(1e-12, 100))
     res = api.lanczos_solver(ctx, [up(ctx, t) for t in eff], up(ctx, psi), 1e-12, 100,
@@ -102,10 +105,14 @@ def test_mixed_vmps_heisenberg16_vs_fp64(ctx):
     mpo, pb = M.heisenberg_chain_mpo(N)
     labels = M.random_sz0_labels(N, 0)
     e_mixed, log_m = _gpu_vmps(ctx, mpo, pb, labels,
-                               api.FiniteVMPSSweepParams(3, 32, 32, 1e-10, 1e-10, 100,
+                               api.FiniteVMPSSweepParams(6, 32, 32, 1e-10, 1e-10, 100,
                                                          precision=MIXED))
     e_fp64, log_d = _gpu_vmps(ctx, mpo, pb, labels,
-                              api.FiniteVMPSSweepParams(3, 32, 32, 1e-10, 1e-10, 100))
+                              api.FiniteVMPSSweepParams(6, 32, 32, 1e-10, 1e-10, 100))
+    per_sweep = 2 * (N - 2)
+    for s in range(6):
+        em, ed = log_m[(s + 1) * per_sweep - 1]["e0"], log_d[(s + 1) * per_sweep - 1]["e0"]
+        print(f"sweep {s + 1}: mixed {em:.12f} fp64 {ed:.12f} |dE/E| {abs(em - ed) / abs(ed):.2e}")
     rel = abs(e_mixed - e_fp64) / abs(e_fp64)
     print(f"L=16 D=32 sweep: |dE/E| mixed vs FP64 = {rel:.2e}")
     assert rel <= 1e-9

@@ -589,6 +589,54 @@ def random_mps(sites: Sequence[Index], div, D: int, seed: int = 0, dtype=np.floa
     return mps
 
 
+def random_canonical_mps(sites: Sequence[Index], div, D: int, centre: int, seed: int = 0,
+                         dtype=np.float64, sigma: float = 2.5):
+    """Random MPS in mixed-canonical form around ``centre``: sites left of it
+    are left isometries, sites right of it right isometries (per bond sector,
+    by QR of Gaussian blocks), the centre tensor is Gaussian with unit norm.
+    Environments built from it have the scale of a converged DMRG state."""
+    mps = random_mps(sites, div, D, seed=seed, dtype=dtype, sigma=sigma)
+    N = len(mps)
+
+    def orthonormalize(A: BlockTensorData, left: bool):
+        # group blocks by the sector of the open bond (right bond if left-isometry)
+        ax = 2 if left else 0
+        groups: Dict[int, List[Tuple[int, ...]]] = {}
+        for k in sorted(A.blocks):
+            groups.setdefault(k[ax], []).append(k)
+        for sec, keys in groups.items():
+            if left:
+                mats = [A.blocks[k].reshape(-1, A.blocks[k].shape[2]) for k in keys]
+                M = np.concatenate(mats, axis=0)
+            else:
+                mats = [A.blocks[k].reshape(A.blocks[k].shape[0], -1) for k in keys]
+                M = np.concatenate(mats, axis=1).T
+            q, _ = np.linalg.qr(M)
+            Q = np.zeros_like(M)
+            Q[:, :q.shape[1]] = q
+            if not left:
+                Q = Q.T
+            off = 0
+            for k, mt in zip(keys, mats):
+                if left:
+                    A.blocks[k] = Q[off:off + mt.shape[0], :].reshape(A.blocks[k].shape)
+                    off += mt.shape[0]
+                else:
+                    A.blocks[k] = Q[:, off:off + mt.shape[1]].reshape(A.blocks[k].shape)
+                    off += mt.shape[1]
+
+    for i in range(N):
+        if i < centre:
+            orthonormalize(mps[i], True)
+        elif i > centre:
+            orthonormalize(mps[i], False)
+    c = mps[centre]
+    nrm = np.sqrt(sum(np.vdot(b, b).real for b in c.blocks.values()))
+    for k in c.blocks:
+        c.blocks[k] = c.blocks[k] / nrm
+    return mps
+
+
 def random_sz0_labels(N, seed):
     """Random half-up / half-down spin labels (total Sz=0) from numpy's PCG64."""
     rng = np.random.Generator(np.random.PCG64(seed))

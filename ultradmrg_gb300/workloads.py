@@ -2,10 +2,11 @@
 
 There is no public dataset for this path; the reference benchmark builds its
 inputs deterministically (``benchmark/ultradmrg_hubbard2d.cpp``).  Here a
-workload is: the model's MPO, a seeded random MPS whose bond sectors follow a
-Gaussian Schmidt-weight model (``models.bond_sectors``), and the two-site
-problem at the centre bond (environments from the MPS by environment
-updates, normalised after each update).
+workload is: the model's MPO, a seeded random MPS in mixed-canonical form
+around the centre bond whose bond sectors follow a Gaussian Schmidt-weight
+model (``models.bond_sectors``, ``models.random_canonical_mps``), and the
+two-site problem at the centre bond (environments from the MPS by
+environment updates, at the physical scale of a DMRG run).
 """
 from __future__ import annotations
 
@@ -58,5 +59,5 @@ def build_host(w: Workload):
     else:
         mpo, pb = M.heisenberg_chain_mpo(w.N)
         div = (0,)
-    mps = M.random_mps([pb] * w.N, div, w.D, seed=w.seed, sigma=w.sigma)
+    mps = M.random_canonical_mps([pb] * w.N, div, w.D, w.centre, seed=w.seed, sigma=w.sigma)
     return mpo, mps
