@@ -1,7 +1,11 @@
-// MPO step of the mixed-precision matvec: T3 = (W1 W2) T1 on CUDA cores
-// (HBM bound: FP32 reads of T1, split-BF16 writes of the step-3 operand
-// images).  One CTA per target block; each thread owns (a', b) positions and
-// accumulates all output channels of that position in registers.
+// MPO step of the mixed-precision matvec: T3 = (W1 W2) T1 on CUDA cores,
+// grouped by (A', B) sector pair.  One CTA takes a pair and a chunk of a'
+// rows; for every 32-wide tile of the contiguous b index it stages all input
+// channels of the pair in shared memory (each T1 entry is read once), then
+// each warp produces output channels (lanes over b) as FP32 dot products with
+// the pair's coefficient matrix, split into three BF16 planes and written into
+// the step-3 tile images.  HBM bound: T1 read once (FP32), T3 written once
+// (3 x BF16).
 #include <cuda_bf16.h>
 
 #include "sg_matvec.hpp"
@@ -10,81 +14,81 @@ namespace udmrg {
 
 namespace {
 
-constexpr int kMaxOut = 32;
+constexpr int kAChunk = 8;  // a' rows per work unit (matches the planner)
+constexpr int kThreads = 256;
 
 __device__ __forceinline__ int canon(int r, int k, int tr) {
   return (((k >> 3) * (tr >> 3) + (r >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1);
 }
 
-template <int NOUT>
-__device__ void target_body(const MpoTarget &tg, const MpoSource *__restrict__ src,
-                            const float *__restrict__ coefs, const float *__restrict__ t1,
-                            uint8_t *__restrict__ img) {
+__global__ void __launch_bounds__(kThreads)
+    mpo_pair_kernel(const int32_t *__restrict__ units, int nunits,
+                    const MpoPair *__restrict__ pairs, const MpoIn *__restrict__ ins,
+                    const MpoOut *__restrict__ outs, const float *__restrict__ coefs,
+                    const float *__restrict__ t1, uint8_t *__restrict__ img) {
+  extern __shared__ float sm[];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int nwarps = kThreads / 32;
   const int64_t plane = (int64_t)kTcBM * kTcBK * 2;
-  const int npos = tg.da * tg.db;
-  for (int e = threadIdx.x; e < npos; e += blockDim.x) {
-    const int a = e / tg.db, b = e - a * tg.db;
-    float acc[NOUT];
-#pragma unroll
-    for (int o = 0; o < NOUT; ++o) acc[o] = 0.f;
-    for (int s = 0; s < tg.nsrc; ++s) {
-      const MpoSource sr = src[tg.src0 + s];
-      const float *c = coefs + sr.coef_off;
-      const int nin = sr.dw * sr.ds12;
-      for (int ic = 0; ic < nin; ++ic) {
-        const int w = ic / sr.ds12, s12 = ic - w * sr.ds12;
-        const float x =
-            t1[sr.t1_off + ((int64_t)a * sr.dw + w) * sr.row_pitch + (int64_t)s12 * tg.db + b];
-#pragma unroll
-        for (int o = 0; o < NOUT; ++o)
-          if (o < tg.nout) acc[o] = fmaf(__ldg(c + ic * tg.nout + o), x, acc[o]);
+  for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+    const MpoPair pr = pairs[units[2 * u]];
+    const int a0 = units[2 * u + 1];
+    float *C = sm;
+    float *X = sm + pr.nout * pr.nin;
+    __syncthreads();  // previous unit done with shared memory
+    for (int e = tid; e < pr.nout * pr.nin; e += kThreads) C[e] = coefs[pr.coef0 + e];
+    const int a1 = min(a0 + kAChunk, pr.da);
+    for (int a = a0; a < a1; ++a) {
+      for (int b0 = 0; b0 < pr.db; b0 += 32) {
+        __syncthreads();  // C loaded / previous tile consumed
+        for (int e = tid; e < pr.nin * 32; e += kThreads) {
+          const int i = e >> 5, b = b0 + (e & 31);
+          const MpoIn in = ins[pr.in0 + i];
+          X[e] = b < pr.db ? t1[in.base + (int64_t)a * in.astride + b] : 0.f;
+        }
+        __syncthreads();
+        const int b = b0 + lane;
+        for (int o = warp; o < pr.nout; o += nwarps) {
+          const float *c = C + o * pr.nin;
+          float acc = 0.f;
+          for (int i = 0; i < pr.nin; ++i) acc = fmaf(c[i], X[(i << 5) + lane], acc);
+          if (b < pr.db) {
+            const MpoOut ot = outs[pr.out0 + o];
+            const int row = ot.row0 + a * ot.rstride;
+            const int col = ot.col0 + b;
+            const int64_t off = ot.img_off +
+                                ((int64_t)(row / kTcBM) * ot.kc + col / kTcBK) * 3 * plane +
+                                canon(row % kTcBM, col % kTcBK, kTcBM);
+            const __nv_bfloat16 h = __float2bfloat16_rn(acc);
+            const float r1 = acc - __bfloat162float(h);
+            const __nv_bfloat16 m = __float2bfloat16_rn(r1);
+            const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
+            *(__nv_bfloat16 *)(img + off) = h;
+            *(__nv_bfloat16 *)(img + off + plane) = m;
+            *(__nv_bfloat16 *)(img + off + 2 * plane) = l;
+          }
+        }
       }
     }
-#pragma unroll
-    for (int o = 0; o < NOUT; ++o) {
-      if (o >= tg.nout) break;
-      const int row = tg.row0 + a * tg.ds12p + o / tg.dw2;
-      const int col = tg.k0 + (o % tg.dw2) * tg.db + b;
-      const int64_t off = tg.img_off +
-                          ((int64_t)(row / kTcBM) * tg.kc + col / kTcBK) * 3 * plane +
-                          canon(row % kTcBM, col % kTcBK, kTcBM);
-      const float v = acc[o];
-      const __nv_bfloat16 h = __float2bfloat16_rn(v);
-      const float r1 = v - __bfloat162float(h);
-      const __nv_bfloat16 m = __float2bfloat16_rn(r1);
-      const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
-      *(__nv_bfloat16 *)(img + off) = h;
-      *(__nv_bfloat16 *)(img + off + plane) = m;
-      *(__nv_bfloat16 *)(img + off + 2 * plane) = l;
-    }
-  }
-}
-
-__global__ void mpo_step_kernel(const MpoTarget *__restrict__ targets, int ntargets,
-                                const MpoSource *__restrict__ src,
-                                const float *__restrict__ coefs, const float *__restrict__ t1,
-                                uint8_t *__restrict__ img) {
-  for (int t = blockIdx.x; t < ntargets; t += gridDim.x) {
-    const MpoTarget tg = targets[t];
-    if (tg.nout <= 4)
-      target_body<4>(tg, src, coefs, t1, img);
-    else if (tg.nout <= 8)
-      target_body<8>(tg, src, coefs, t1, img);
-    else if (tg.nout <= 16)
-      target_body<16>(tg, src, coefs, t1, img);
-    else
-      target_body<kMaxOut>(tg, src, coefs, t1, img);
   }
 }
 
 }  // namespace
 
 void run_mpo_step(Ctx &ctx, const SgMatvecPlan &p) {
-  const int n = (int)p.targets.size();
-  if (n == 0) return;
-  const int grid = std::min(n, 32 * ctx.num_sms);
-  mpo_step_kernel<<<grid, 128, 0, ctx.stream>>>(p.d_targets, n, p.d_sources, p.d_coefs, p.t1,
-                                                p.t3_img);
+  const int nunits = (int)p.units.size() / 2;
+  if (nunits == 0) return;
+  const size_t smem = ((size_t)p.max_nout * p.max_nin + (size_t)p.max_nin * 32) * sizeof(float);
+  UDMRG_REQUIRE(smem <= 200 * 1024, "mixed matvec: MPO channel matrix of a sector pair too large");
+  static size_t attr = 0;
+  if (smem > 48 * 1024 && smem > attr) {
+    UDMRG_CHECK_CUDA(cudaFuncSetAttribute(mpo_pair_kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = smem;
+  }
+  const int grid = std::min(nunits, 16 * ctx.num_sms);
+  mpo_pair_kernel<<<grid, kThreads, smem, ctx.stream>>>(p.d_units, nunits, p.d_pairs, p.d_ins,
+                                                         p.d_outs, p.d_pcoefs, p.t1, p.t3_img);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches++;
 }

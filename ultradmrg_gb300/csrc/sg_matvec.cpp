@@ -7,7 +7,9 @@ namespace udmrg {
 SgMatvecPlan::~SgMatvecPlan() {
   if (!ctx) return;
   for (void *p : {(void *)l_img, (void *)psi_img, (void *)t3_img, (void *)r_img, (void *)t1,
-                  (void *)d_psi_ops, (void *)d_targets, (void *)d_sources, (void *)d_coefs})
+                  (void *)d_psi_ops, (void *)d_targets, (void *)d_sources, (void *)d_coefs,
+                  (void *)d_pairs, (void *)d_ins, (void *)d_outs, (void *)d_pcoefs,
+                  (void *)d_units})
     ctx->free(p);
 }
 
@@ -147,6 +149,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   // W1 blocks by (s1_out); W2 blocks by (wr, s2_out, w2)
   std::map<int32_t, std::vector<int64_t>> w1_by_s1o;
   for (int64_t b = 0; b < W1.nblocks(); ++b) w1_by_s1o[W1.key(b)[2]].push_back(b);
+  std::vector<std::pair<int32_t, int32_t>> tgt_key;  // (A', B) of every target
   std::map<Key, std::vector<int64_t>> w2_by;  // (wr, s2out, w2)
   for (int64_t b = 0; b < W2.nblocks(); ++b)
     w2_by[{W2.key(b)[0], W2.key(b)[2], W2.key(b)[3]}].push_back(b);
@@ -263,8 +266,10 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
           p->sources.push_back(s);
         }
         tg.nsrc = (int32_t)p->sources.size() - tg.src0;
-        UDMRG_REQUIRE(tg.nout <= 32, "mixed matvec: more than 32 MPO output channels per block");
-        if (tg.nsrc > 0) p->targets.push_back(tg);
+        if (tg.nsrc > 0) {
+          p->targets.push_back(tg);
+          tgt_key.push_back({Ap, Bs});
+        }
       }
     }
     p->g3.add_group(t3_off, r_off, (int32_t)M, (int32_t)dBp, (int32_t)K, rows);
@@ -295,9 +300,75 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   }
   p->g1.finalize();
   p->g3.finalize();
-  p->d_targets = upload_vec(ctx, p->targets);
-  p->d_sources = upload_vec(ctx, p->sources);
-  p->d_coefs = upload_vec(ctx, p->coefs);
+  // ---------------- MPO step regrouped by (A', B) pair ------------------------
+  {
+    std::map<std::pair<int32_t, int32_t>, std::vector<int>> by_pair;
+    for (size_t t = 0; t < p->targets.size(); ++t) by_pair[tgt_key[t]].push_back((int)t);
+    constexpr int kAChunk = 8;
+    for (auto &kv : by_pair) {
+      MpoPair pr{};
+      pr.in0 = (int32_t)p->ins.size();
+      pr.out0 = (int32_t)p->outs.size();
+      pr.coef0 = (int32_t)p->pcoefs.size();
+      const MpoTarget &t0 = p->targets[kv.second[0]];
+      pr.da = t0.da;
+      pr.db = t0.db;
+      // input channels: one per (w, s1 s2) of every distinct source block
+      std::map<int64_t, int32_t> in_first;  // T1 origin -> first channel
+      for (int t : kv.second) {
+        const MpoTarget &tg = p->targets[t];
+        for (int s = 0; s < tg.nsrc; ++s) {
+          const MpoSource &sr = p->sources[tg.src0 + s];
+          if (in_first.count(sr.t1_off)) continue;
+          in_first[sr.t1_off] = (int32_t)(p->ins.size() - pr.in0);
+          for (int w = 0; w < sr.dw; ++w)
+            for (int s12 = 0; s12 < sr.ds12; ++s12)
+              p->ins.push_back({sr.t1_off + (int64_t)w * sr.row_pitch + (int64_t)s12 * tg.db,
+                                (int64_t)sr.dw * sr.row_pitch});
+        }
+      }
+      pr.nin = (int32_t)p->ins.size() - pr.in0;
+      // output channels: one per (s1' s2', w2) of every target block
+      std::vector<int32_t> out_first;
+      for (int t : kv.second) {
+        const MpoTarget &tg = p->targets[t];
+        out_first.push_back((int32_t)(p->outs.size() - pr.out0));
+        for (int oc = 0; oc < tg.nout; ++oc)
+          p->outs.push_back({tg.img_off, tg.row0 + oc / tg.dw2, tg.ds12p,
+                             tg.k0 + (oc % tg.dw2) * tg.db, tg.kc});
+      }
+      pr.nout = (int32_t)p->outs.size() - pr.out0;
+      UDMRG_REQUIRE(pr.nin <= 256 && pr.nout <= 256,
+                    "mixed matvec: more than 256 MPO channels in one sector pair");
+      std::vector<float> C((size_t)pr.nout * pr.nin, 0.f);
+      for (size_t j = 0; j < kv.second.size(); ++j) {
+        const MpoTarget &tg = p->targets[kv.second[j]];
+        for (int s = 0; s < tg.nsrc; ++s) {
+          const MpoSource &sr = p->sources[tg.src0 + s];
+          const int i0 = in_first[sr.t1_off];
+          const int nin_s = sr.dw * sr.ds12;
+          for (int ic = 0; ic < nin_s; ++ic)
+            for (int oc = 0; oc < tg.nout; ++oc)
+              C[(size_t)(out_first[j] + oc) * pr.nin + i0 + ic] +=
+                  p->coefs[sr.coef_off + ic * tg.nout + oc];
+        }
+      }
+      p->pcoefs.insert(p->pcoefs.end(), C.begin(), C.end());
+      p->max_nin = std::max(p->max_nin, (int)pr.nin);
+      p->max_nout = std::max(p->max_nout, (int)pr.nout);
+      const int32_t pid = (int32_t)p->pairs.size();
+      for (int a = 0; a < pr.da; a += kAChunk) {
+        p->units.push_back(pid);
+        p->units.push_back(a);
+      }
+      p->pairs.push_back(pr);
+    }
+  }
+  p->d_pairs = upload_vec(ctx, p->pairs);
+  p->d_ins = upload_vec(ctx, p->ins);
+  p->d_outs = upload_vec(ctx, p->outs);
+  p->d_pcoefs = upload_vec(ctx, p->pcoefs);
+  p->d_units = upload_vec(ctx, p->units);
   p->mixed_flops = 6.0 * (p->g1.flops + p->g3.flops);
   ctx.sync();
   return p;

@@ -42,6 +42,22 @@ struct MpoSource {
   int32_t pad;
 };
 
+// The MPO step regrouped by (A', B) sector pair: every T1 entry of the pair
+// is an input channel (a' rows x b columns), every T3 entry an output
+// channel, and out[o] = sum_i coef[o][i] in[i] at each (a', b).
+struct MpoPair {
+  int32_t in0, nin, out0, nout;
+  int32_t coef0, da, db, pad;
+};
+struct MpoIn {
+  int64_t base;     // T1 element offset of (a' = 0, b = 0)
+  int64_t astride;  // T1 elements between consecutive a'
+};
+struct MpoOut {
+  int64_t img_off;  // byte offset of the step-3 A image of the target's group
+  int32_t row0, rstride, col0, kc;  // image row = row0 + a' * rstride, column = col0 + b
+};
+
 struct SgMatvecPlan {
   Ctx *ctx = nullptr;
   int64_t psi_size = 0;
@@ -62,6 +78,18 @@ struct SgMatvecPlan {
   MpoTarget *d_targets = nullptr;
   MpoSource *d_sources = nullptr;
   float *d_coefs = nullptr;
+  // pair-grouped form (the one the kernel runs)
+  std::vector<MpoPair> pairs;
+  std::vector<MpoIn> ins;
+  std::vector<MpoOut> outs;
+  std::vector<float> pcoefs;
+  std::vector<int32_t> units;  // (pair, first a') work units, flattened pairs
+  MpoPair *d_pairs = nullptr;
+  MpoIn *d_ins = nullptr;
+  MpoOut *d_outs = nullptr;
+  float *d_pcoefs = nullptr;
+  int32_t *d_units = nullptr;
+  int max_nin = 0, max_nout = 0;
   double mixed_flops = 0;  // tensor-core work actually issued (2MNK per group, x6 products)
   ~SgMatvecPlan();
   void apply(const double *psi_in, double *out);
