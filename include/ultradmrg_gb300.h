@@ -144,6 +144,17 @@ int udmrg_update_site_renvs(udmrg_ctx *ctx, const udmrg_tensor *renv, const udmr
 int udmrg_svd(udmrg_ctx *ctx, const udmrg_tensor *t, int ldims, const int32_t *ldiv,
               double trunc_err, int64_t Dmin, int64_t Dmax, int mode, udmrg_tensor **u,
               udmrg_tensor **s, udmrg_tensor **vt, double *actual_trunc_err, int64_t *D);
+/* TwoSiteFiniteVMPSUpdate (two_site_update_finite_vmps_impl.h:232-373) on one
+ * bond: lenv = left environment of sites [0, l), renv = right environment of
+ * sites (l+1, N), the two MPS tensors and MPO tensors of sites l, l+1.  dir is
+ * 'r' or 'l'.  Returns the new MPS tensors (isometry on the side of dir's
+ * origin) and the environment grown by one site (left env of [0, l] for 'r',
+ * right env of [l+1, N) for 'l').  log may be NULL. */
+int udmrg_two_site_update(udmrg_ctx *ctx, const udmrg_tensor *lenv, const udmrg_tensor *renv,
+                          const udmrg_tensor *mps_l, const udmrg_tensor *mps_r,
+                          const udmrg_tensor *mpo_l, const udmrg_tensor *mpo_r,
+                          const udmrg_sweep_params *params, char dir, udmrg_tensor **new_l,
+                          udmrg_tensor **new_r, udmrg_tensor **new_env, udmrg_site_log *log);
 /* TwoSiteFiniteVMPS (two_site_update_finite_vmps_impl.h:95-494), device
  * resident.  mps[N] is read and replaced by the updated tensors (the old
  * handles are destroyed); mpo[N] is borrowed.  log may be NULL. */

@@ -72,6 +72,9 @@ SIGNATURES = {
     "udmrg_update_site_renvs": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, c_void_pp],
     "udmrg_svd": [C.c_void_p, C.c_void_p, C.c_int, c_int32_p, C.c_double, C.c_int64, C.c_int64,
                   C.c_int, c_void_pp, c_void_pp, c_void_pp, c_double_p, c_int64_p],
+    "udmrg_two_site_update": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                              C.c_void_p, C.c_void_p, C.POINTER(SweepParams), C.c_char,
+                              c_void_pp, c_void_pp, c_void_pp, C.POINTER(SiteLog)],
     "udmrg_two_site_finite_vmps": [C.c_void_p, C.c_int64, c_void_pp, c_void_pp,
                                    C.POINTER(SweepParams), c_double_p, C.POINTER(SiteLog),
                                    C.c_int64, c_int64_p],
@@ -93,6 +96,20 @@ SIGNATURES = {
 }
 
 _lib = None
+
+# Set at interpreter exit: handle finalizers then skip their device frees (the
+# process is ending; the driver reclaims the memory), so no CUDA call runs in
+# an arbitrary finalisation order.
+SHUTDOWN = [False]
+
+
+def _at_exit():
+    SHUTDOWN[0] = True
+
+
+import atexit  # noqa: E402
+
+atexit.register(_at_exit)
 
 
 class UdmrgError(RuntimeError):

@@ -59,6 +59,8 @@ class Context:
             self.h = None
 
     def __del__(self):
+        if _lib.SHUTDOWN[0]:
+            return
         try:
             self.close()
         except Exception:  # noqa: BLE001 - interpreter shutdown
@@ -180,6 +182,8 @@ class DeviceTensor:
             self.h = None
 
     def __del__(self):
+        if _lib.SHUTDOWN[0]:
+            return
         try:
             self.close()
         except Exception:  # noqa: BLE001
@@ -354,6 +358,22 @@ def build_envs(ctx, mpo: Sequence[BlockTensorData], mps: Sequence[BlockTensorDat
     return L, R
 
 
+def two_site_update(ctx, lenv, renv, mps_l, mps_r, mpo_l, mpo_r,
+                    params: FiniteVMPSSweepParams, dir: str = "r"):
+    """``TwoSiteFiniteVMPSUpdate`` on one bond: (new_l, new_r, new_env, log)."""
+    sp = _lib.SweepParams(1, params.Dmin, params.Dmax, params.trunc_err,
+                          _lib.LanczosParams(params.lanczos_error, params.lanczos_max_iterations,
+                                             params.precision))
+    a, b, e = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    lg = _lib.SiteLog()
+    call("udmrg_two_site_update", ctx.h, lenv.h, renv.h, mps_l.h, mps_r.h, mpo_l.h, mpo_r.h,
+         C.byref(sp), dir.encode(), C.byref(a), C.byref(b), C.byref(e), C.byref(lg))
+    log = dict(e0=lg.e0, trunc_err=lg.trunc_err, D=lg.D, iters=lg.iters, ee=lg.ee,
+               lancz_sec=lg.lancz_sec, svd_sec=lg.svd_sec, env_sec=lg.env_sec,
+               tot_sec=lg.tot_sec, matvec_flops=lg.matvec_flops)
+    return _new(ctx, a), _new(ctx, b), _new(ctx, e), log
+
+
 class MatvecPlan:
     """Reusable H_eff * psi on device buffers (``udmrg_matvec_plan``)."""
 
@@ -395,6 +415,8 @@ class MatvecPlan:
             self.h = None
 
     def __del__(self):
+        if _lib.SHUTDOWN[0]:
+            return
         try:
             self.close()
         except Exception:  # noqa: BLE001

@@ -115,6 +115,22 @@ struct BTensor {
 
 using TensorPtr = std::unique_ptr<BTensor>;
 
+// Scope-bound device allocations (freed on every exit path, exceptions included).
+struct DeviceScratch {
+  Ctx &ctx;
+  std::vector<void *> ptrs;
+  explicit DeviceScratch(Ctx &c) : ctx(c) {}
+  ~DeviceScratch() {
+    for (void *p : ptrs) ctx.free(p);
+  }
+  template <typename T>
+  T *get(size_t count) {
+    void *p = ctx.alloc(std::max<size_t>(count, 1) * sizeof(T));
+    ptrs.push_back(p);
+    return (T *)p;
+  }
+};
+
 // Sort + deduplicate a flat key list (rank-sized tuples).
 std::vector<int32_t> sort_keys(const std::vector<int32_t> &flat, int rank);
 

@@ -348,6 +348,31 @@ int udmrg_svd(udmrg_ctx *c, const udmrg_tensor *t, int ldims, const int32_t *ldi
   });
 }
 
+int udmrg_two_site_update(udmrg_ctx *c, const udmrg_tensor *lenv, const udmrg_tensor *renv,
+                          const udmrg_tensor *mps_l, const udmrg_tensor *mps_r,
+                          const udmrg_tensor *mpo_l, const udmrg_tensor *mpo_r,
+                          const udmrg_sweep_params *params, char dir, udmrg_tensor **new_l,
+                          udmrg_tensor **new_r, udmrg_tensor **new_env, udmrg_site_log *log) {
+  return guarded([&] {
+    SweepParams p;
+    p.sweeps = 1;
+    p.Dmin = params->Dmin;
+    p.Dmax = params->Dmax;
+    p.trunc_err = params->trunc_err;
+    p.lancz = {params->lancz_params.error, params->lancz_params.max_iterations,
+               (int)params->lancz_params.matvec_precision};
+    SiteLog s{};
+    auto r = two_site_update_local(c->ctx, T(lenv), T(renv), T(mps_l), T(mps_r), T(mpo_l),
+                                   T(mpo_r), p, dir, &s);
+    *new_l = wrap(std::move(r.mps_l));
+    *new_r = wrap(std::move(r.mps_r));
+    *new_env = wrap(std::move(r.env));
+    if (log)
+      *log = {s.site, s.e0, s.trunc_err, s.D, s.iters, s.ee,
+              s.lancz_sec, s.svd_sec, s.env_sec, s.tot_sec, s.matvec_flops};
+  });
+}
+
 int udmrg_two_site_finite_vmps(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
                                udmrg_tensor *const *mpo, const udmrg_sweep_params *params,
                                double *e0, udmrg_site_log *log, int64_t log_cap,

@@ -571,33 +571,52 @@ static double two_site_update(Ctx &ctx, std::vector<TensorPtr> &mps,
     lenv_len = target - 1;
     renv_len = N - target - 1;
   }
+  SiteLog lg{};
+  auto res = two_site_update_local(ctx, *lenvs[lenv_len], *renvs[renv_len], *mps[l], *mps[r],
+                                   *mpo[l], *mpo[r], p, dir, &lg);
+  lg.site = target;
+  mps[l] = std::move(res.mps_l);
+  mps[r] = std::move(res.mps_r);
+  if (dir == 'r')
+    lenvs[lenv_len + 1] = std::move(res.env);
+  else
+    renvs[renv_len + 1] = std::move(res.env);
+  if (log) log->push_back(lg);
+  return lg.e0;
+}
+
+LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &renv,
+                                  const BTensor &mps_l, const BTensor &mps_r,
+                                  const BTensor &mpo_l, const BTensor &mpo_r,
+                                  const SweepParams &p, char dir, SiteLog *log) {
+  UDMRG_REQUIRE(dir == 'r' || dir == 'l', "dir must be 'r' or 'l'");
   const double t0 = now();
-  auto init_state = contract_axes(ctx, *mps[l], *mps[r], {2}, {0});
-  auto mv = plan_matvec2(ctx, *lenvs[lenv_len], *mpo[l], *mpo[r], *renvs[renv_len], *init_state,
-                         p.lancz.precision);
+  auto init_state = contract_axes(ctx, mps_l, mps_r, {2}, {0});
+  auto mv = plan_matvec2(ctx, lenv, mpo_l, mpo_r, renv, *init_state, p.lancz.precision);
   auto lres = lanczos_gs(ctx, *mv, *init_state, p.lancz);
   const double t1 = now();
   const double mvflops = mv->flops;
   mv.reset();
   init_state.reset();
-  const QN ldiv = mps[l]->div();
+  const QN ldiv = mps_l.div();
   auto sres = svd_trunc(ctx, *lres.gs_vec, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax,
                         dir == 'r' ? kSvdSplitLeft : kSvdSplitRight);
   lres.gs_vec.reset();
-  mps[l] = std::move(sres.u);
-  mps[r] = std::move(sres.vt);
+  LocalUpdate out;
+  out.mps_l = std::move(sres.u);
+  out.mps_r = std::move(sres.vt);
   ctx.sync();
   const double t2 = now();
   if (dir == 'r')
-    lenvs[lenv_len + 1] = update_site_lenv(ctx, *lenvs[lenv_len], *mps[target], *mpo[target]);
+    out.env = update_site_lenv(ctx, lenv, *out.mps_l, mpo_l);
   else
-    renvs[renv_len + 1] = update_site_renv(ctx, *renvs[renv_len], *mps[target], *mpo[target]);
+    out.env = update_site_renv(ctx, renv, *out.mps_r, mpo_r);
   ctx.sync();
   const double t3 = now();
   if (log)
-    log->push_back({target, lres.gs_eng, sres.trunc_err, sres.D, lres.iters, sres.ee, t1 - t0,
-                    t2 - t1, t3 - t2, t3 - t0, mvflops});
-  return lres.gs_eng;
+    *log = {0, lres.gs_eng, sres.trunc_err, sres.D, lres.iters, sres.ee, t1 - t0,
+            t2 - t1, t3 - t2, t3 - t0, mvflops};
+  return out;
 }
 
 double two_site_finite_vmps(Ctx &ctx, std::vector<TensorPtr> &mps,

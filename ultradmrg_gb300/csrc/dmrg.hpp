@@ -107,6 +107,17 @@ struct SiteLog {
   double matvec_flops;
 };
 
+// One local update (TwoSiteFiniteVMPSUpdate, two_site_update_finite_vmps_impl.h:232-373):
+// Lanczos on the bond (l, l+1), truncated SVD, MPS split by direction, and the
+// environment grown by one site in that direction.
+struct LocalUpdate {
+  TensorPtr mps_l, mps_r, env;
+};
+LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &renv,
+                                  const BTensor &mps_l, const BTensor &mps_r,
+                                  const BTensor &mpo_l, const BTensor &mpo_r,
+                                  const SweepParams &p, char dir, SiteLog *log);
+
 // TwoSiteFiniteVMPS (two_site_update_finite_vmps_impl.h:95-494), device
 // resident: mps tensors are replaced in place; returns the last energy.
 double two_site_finite_vmps(Ctx &ctx, std::vector<TensorPtr> &mps,

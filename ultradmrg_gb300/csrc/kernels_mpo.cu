@@ -24,8 +24,9 @@ __device__ __forceinline__ int canon(int r, int k, int tr) {
 __global__ void __launch_bounds__(kThreads)
     mpo_pair_kernel(const int32_t *__restrict__ units, int nunits,
                     const MpoPair *__restrict__ pairs, const MpoIn *__restrict__ ins,
-                    const MpoOut *__restrict__ outs, const float *__restrict__ coefs,
-                    const float *__restrict__ t1, uint8_t *__restrict__ img) {
+                    const MpoOut *__restrict__ outs, const int32_t *__restrict__ rowptr,
+                    const MpoNz *__restrict__ nz, const float *__restrict__ t1,
+                    uint8_t *__restrict__ img) {
   extern __shared__ float sm[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int nwarps = kThreads / 32;
@@ -33,10 +34,7 @@ __global__ void __launch_bounds__(kThreads)
   for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
     const MpoPair pr = pairs[units[2 * u]];
     const int a0 = units[2 * u + 1];
-    float *C = sm;
-    float *X = sm + pr.nout * pr.nin;
-    __syncthreads();  // previous unit done with shared memory
-    for (int e = tid; e < pr.nout * pr.nin; e += kThreads) C[e] = coefs[pr.coef0 + e];
+    float *X = sm;
     const int a1 = min(a0 + kAChunk, pr.da);
     for (int a = a0; a < a1; ++a) {
       for (int b0 = 0; b0 < pr.db; b0 += 32) {
@@ -49,9 +47,12 @@ __global__ void __launch_bounds__(kThreads)
         __syncthreads();
         const int b = b0 + lane;
         for (int o = warp; o < pr.nout; o += nwarps) {
-          const float *c = C + o * pr.nin;
+          const int k0 = __ldg(rowptr + pr.row0 + o), k1 = __ldg(rowptr + pr.row0 + o + 1);
           float acc = 0.f;
-          for (int i = 0; i < pr.nin; ++i) acc = fmaf(c[i], X[(i << 5) + lane], acc);
+          for (int k = k0; k < k1; ++k) {
+            const MpoNz e = nz[k];
+            acc = fmaf(e.v, X[(e.i << 5) + lane], acc);
+          }
           if (b < pr.db) {
             const MpoOut ot = outs[pr.out0 + o];
             const int row = ot.row0 + a * ot.rstride;
@@ -78,8 +79,8 @@ __global__ void __launch_bounds__(kThreads)
 void run_mpo_step(Ctx &ctx, const SgMatvecPlan &p) {
   const int nunits = (int)p.units.size() / 2;
   if (nunits == 0) return;
-  const size_t smem = ((size_t)p.max_nout * p.max_nin + (size_t)p.max_nin * 32) * sizeof(float);
-  UDMRG_REQUIRE(smem <= 200 * 1024, "mixed matvec: MPO channel matrix of a sector pair too large");
+  const size_t smem = (size_t)p.max_nin * 32 * sizeof(float);
+  UDMRG_REQUIRE(smem <= 200 * 1024, "mixed matvec: too many MPO input channels in a sector pair");
   static size_t attr = 0;
   if (smem > 48 * 1024 && smem > attr) {
     UDMRG_CHECK_CUDA(cudaFuncSetAttribute(mpo_pair_kernel,
@@ -88,7 +89,8 @@ void run_mpo_step(Ctx &ctx, const SgMatvecPlan &p) {
   }
   const int grid = std::min(nunits, 16 * ctx.num_sms);
   mpo_pair_kernel<<<grid, kThreads, smem, ctx.stream>>>(p.d_units, nunits, p.d_pairs, p.d_ins,
-                                                         p.d_outs, p.d_pcoefs, p.t1, p.t3_img);
+                                                         p.d_outs, p.d_rowptr, p.d_nz, p.t1,
+                                                         p.t3_img);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches++;
 }

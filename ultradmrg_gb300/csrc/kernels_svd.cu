@@ -89,7 +89,9 @@ __global__ void jacobi_eig_kernel(const EigJob *__restrict__ jobs, double *__res
     if (tid == 0) {
       double s = 0;
       for (int w = 0; w < (nt + 31) / 32; ++w) s += red[w];
-      done = (off_tot <= tol * tol * s) ? 1 : 0;
+      // rounding keeps the off-diagonal norm near n * eps * |G|: scale the target with n
+      const double t = tol * (double)n;
+      done = (off_tot <= t * t * s) ? 1 : 0;
     }
     __syncthreads();
     if (done) break;
@@ -222,7 +224,7 @@ int run_jacobi_eig(Ctx &ctx, const std::vector<EigJob> &jobs_in, double *G, doub
   UDMRG_CHECK_CUDA(cudaMemsetAsync(dstat, 0, sizeof(int), ctx.stream));
   UDMRG_CHECK_CUDA(cudaMemcpyAsync(d, jobs.data(), jobs.size() * sizeof(EigJob),
                                    cudaMemcpyHostToDevice, ctx.stream));
-  jacobi_eig_kernel<<<(int)jobs.size(), 512, smem, ctx.stream>>>(d, G, V, lam, W, 40, 1e-15,
+  jacobi_eig_kernel<<<(int)jobs.size(), 512, smem, ctx.stream>>>(d, G, V, lam, W, 40, 4e-16,
                                                                   dstat);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches++;

@@ -8,8 +8,8 @@ SgMatvecPlan::~SgMatvecPlan() {
   if (!ctx) return;
   for (void *p : {(void *)l_img, (void *)psi_img, (void *)t3_img, (void *)r_img, (void *)t1,
                   (void *)d_psi_ops, (void *)d_targets, (void *)d_sources, (void *)d_coefs,
-                  (void *)d_pairs, (void *)d_ins, (void *)d_outs, (void *)d_pcoefs,
-                  (void *)d_units})
+                  (void *)d_pairs, (void *)d_ins, (void *)d_outs, (void *)d_rowptr,
+                  (void *)d_nz, (void *)d_units})
     ctx->free(p);
 }
 
@@ -309,7 +309,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       MpoPair pr{};
       pr.in0 = (int32_t)p->ins.size();
       pr.out0 = (int32_t)p->outs.size();
-      pr.coef0 = (int32_t)p->pcoefs.size();
+      pr.row0 = (int32_t)p->outs.size();
       const MpoTarget &t0 = p->targets[kv.second[0]];
       pr.da = t0.da;
       pr.db = t0.db;
@@ -353,7 +353,14 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
                   p->coefs[sr.coef_off + ic * tg.nout + oc];
         }
       }
-      p->pcoefs.insert(p->pcoefs.end(), C.begin(), C.end());
+      if (p->rowptr.empty()) p->rowptr.push_back(0);
+      for (int o = 0; o < pr.nout; ++o) {
+        for (int i = 0; i < pr.nin; ++i) {
+          const float v = C[(size_t)o * pr.nin + i];
+          if (v != 0.f) p->nz.push_back({i, v});
+        }
+        p->rowptr.push_back((int32_t)p->nz.size());
+      }
       p->max_nin = std::max(p->max_nin, (int)pr.nin);
       p->max_nout = std::max(p->max_nout, (int)pr.nout);
       const int32_t pid = (int32_t)p->pairs.size();
@@ -367,7 +374,8 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   p->d_pairs = upload_vec(ctx, p->pairs);
   p->d_ins = upload_vec(ctx, p->ins);
   p->d_outs = upload_vec(ctx, p->outs);
-  p->d_pcoefs = upload_vec(ctx, p->pcoefs);
+  p->d_rowptr = upload_vec(ctx, p->rowptr);
+  p->d_nz = upload_vec(ctx, p->nz);
   p->d_units = upload_vec(ctx, p->units);
   p->mixed_flops = 6.0 * (p->g1.flops + p->g3.flops);
   ctx.sync();

@@ -47,7 +47,12 @@ struct MpoSource {
 // channel, and out[o] = sum_i coef[o][i] in[i] at each (a', b).
 struct MpoPair {
   int32_t in0, nin, out0, nout;
-  int32_t coef0, da, db, pad;
+  int32_t row0, da, db, pad;  // row0: first CSR row (output channel) of the pair
+};
+// Nonzero of the pair's coefficient matrix (CSR): input channel and value.
+struct MpoNz {
+  int32_t i;
+  float v;
 };
 struct MpoIn {
   int64_t base;     // T1 element offset of (a' = 0, b = 0)
@@ -82,12 +87,14 @@ struct SgMatvecPlan {
   std::vector<MpoPair> pairs;
   std::vector<MpoIn> ins;
   std::vector<MpoOut> outs;
-  std::vector<float> pcoefs;
+  std::vector<int32_t> rowptr;  // CSR row pointers over all output channels (+1)
+  std::vector<MpoNz> nz;
   std::vector<int32_t> units;  // (pair, first a') work units, flattened pairs
   MpoPair *d_pairs = nullptr;
   MpoIn *d_ins = nullptr;
   MpoOut *d_outs = nullptr;
-  float *d_pcoefs = nullptr;
+  int32_t *d_rowptr = nullptr;
+  MpoNz *d_nz = nullptr;
   int32_t *d_units = nullptr;
   int max_nin = 0, max_nout = 0;
   double mixed_flops = 0;  // tensor-core work actually issued (2MNK per group, x6 products)

@@ -125,7 +125,8 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
   }
   const int nsec = (int)secs.size();
   // 2. gather dense sector matrices
-  double *Mbuf = (double *)ctx.alloc(std::max<int64_t>(mtot, 1) * sizeof(double));
+  DeviceScratch scratch(ctx);
+  double *Mbuf = scratch.get<double>(std::max<int64_t>(mtot, 1));
   UDMRG_CHECK_CUDA(cudaMemsetAsync(Mbuf, 0, std::max<int64_t>(mtot, 1) * sizeof(double), ctx.stream));
   {
     std::vector<Copy2D> ops;
@@ -163,10 +164,10 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
     gtot += n * n;
     ltot += n;
   }
-  double *G = (double *)ctx.alloc(std::max<int64_t>(gtot, 1) * sizeof(double));
-  double *V = (double *)ctx.alloc(std::max<int64_t>(gtot, 1) * sizeof(double));
-  double *W = (double *)ctx.alloc(std::max<int64_t>(gtot, 1) * sizeof(double));
-  double *lam = (double *)ctx.alloc(std::max<int64_t>(ltot, 1) * sizeof(double));
+  double *G = scratch.get<double>(std::max<int64_t>(gtot, 1));
+  double *V = scratch.get<double>(std::max<int64_t>(gtot, 1));
+  double *W = scratch.get<double>(std::max<int64_t>(gtot, 1));
+  double *lam = scratch.get<double>(std::max<int64_t>(ltot, 1));
   {
     GemmPlan g;
     g.ctx = &ctx;
@@ -269,7 +270,7 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
     coffs[q] = ctot;
     ctot += kept[q] * (left ? secs[q].cols : secs[q].rows);
   }
-  double *Cbuf = (double *)ctx.alloc(std::max<int64_t>(ctot, 1) * sizeof(double));
+  double *Cbuf = scratch.get<double>(std::max<int64_t>(ctot, 1));
   {
     GemmPlan g;
     g.ctx = &ctx;
@@ -305,11 +306,10 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
       sj.push_back(j);
       for (int64_t i = 0; i < kept[q]; ++i) inv.push_back(sv[q][i] > 0 ? 1.0 / sv[q][i] : 0.0);
     }
-    double *dinv = (double *)ctx.alloc(std::max<size_t>(inv.size(), 1) * sizeof(double));
+    double *dinv = scratch.get<double>(std::max<size_t>(inv.size(), 1));
     UDMRG_CHECK_CUDA(cudaMemcpyAsync(dinv, inv.data(), inv.size() * sizeof(double),
                                      cudaMemcpyHostToDevice, ctx.stream));
     run_scale(ctx, sj, Cbuf, dinv, false);
-    ctx.free(dinv);
   }
   // scatter into u and vt
   std::vector<Copy2D> uops, vops;
@@ -363,12 +363,6 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
   }
   run_copy2d(ctx, uops, left ? V : Cbuf, u->data, false);
   run_copy2d(ctx, vops, left ? Cbuf : V, vt->data, false);
-  ctx.free(Mbuf);
-  ctx.free(G);
-  ctx.free(V);
-  ctx.free(W);
-  ctx.free(lam);
-  ctx.free(Cbuf);
   res.u = std::move(u);
   res.s = std::move(s);
   res.vt = std::move(vt);
