@@ -58,12 +58,20 @@ typedef struct {
 
 /* FiniteVMPSSweepParams without the noise and path fields
  * (include/qlmps/algorithm/finite_vmps_sweep_params.h:31-107). */
+enum { UDMRG_SVD_EXACT = 0, UDMRG_SVD_SKETCH_PREV = 1, UDMRG_SVD_SKETCH_LEARNED = 2 };
+
 typedef struct {
   int64_t sweeps;
   int64_t Dmin;
   int64_t Dmax;
   double trunc_err;
   udmrg_lanczos_params lancz_params;
+  /* truncated SVD of the local update: UDMRG_SVD_EXACT, or the sector-wise
+   * randomized SVD with sketch sizes from the bond's current sector
+   * dimensions (SKETCH_PREV) or from the learned rank predictor
+   * (SKETCH_LEARNED, see udmrg_rank_model_*); svd_oversample extra columns */
+  int64_t svd_mode;
+  int64_t svd_oversample;
 } udmrg_sweep_params;
 
 /* One line of the per-site log printed by TwoSiteFiniteVMPSUpdate
@@ -73,6 +81,8 @@ typedef struct {
   double e0, trunc_err;
   int64_t D, iters;
   double ee, lancz_sec, svd_sec, env_sec, tot_sec, matvec_flops;
+  int64_t svd_sketch_total; /* randomized SVD: sum of sketch sizes (0: exact) */
+  int64_t svd_grow_rounds;  /* randomized SVD: enlargements after a miss */
 } udmrg_site_log;
 
 const char *udmrg_last_error(void);
@@ -144,6 +154,17 @@ int udmrg_update_site_renvs(udmrg_ctx *ctx, const udmrg_tensor *renv, const udmr
 int udmrg_svd(udmrg_ctx *ctx, const udmrg_tensor *t, int ldims, const int32_t *ldiv,
               double trunc_err, int64_t Dmin, int64_t Dmax, int mode, udmrg_tensor **u,
               udmrg_tensor **s, udmrg_tensor **vt, double *actual_trunc_err, int64_t *D);
+/* Sector-wise randomized truncated SVD (same outputs as udmrg_svd).
+ * sketch_qns[nsk*nq] / sketch_sizes[nsk]: requested sketch size per bond QN
+ * (sectors not listed use their full rank, i.e. are exact); a sector whose
+ * sketch is entirely kept grows x2 and is redone (grow_rounds counts these
+ * passes).  No counterpart in the reference (its SVD is exact). */
+int udmrg_svd_randomized(udmrg_ctx *ctx, const udmrg_tensor *t, int ldims, const int32_t *ldiv,
+                         double trunc_err, int64_t Dmin, int64_t Dmax, int mode, int64_t nsk,
+                         const int32_t *sketch_qns, const int64_t *sketch_sizes,
+                         int64_t oversample, int power_iters, uint64_t seed, udmrg_tensor **u,
+                         udmrg_tensor **s, udmrg_tensor **vt, double *actual_trunc_err,
+                         int64_t *D, int64_t *grow_rounds);
 /* TwoSiteFiniteVMPSUpdate (two_site_update_finite_vmps_impl.h:232-373) on one
  * bond: lenv = left environment of sites [0, l), renv = right environment of
  * sites (l+1, N), the two MPS tensors and MPO tensors of sites l, l+1.  dir is

@@ -30,14 +30,16 @@ class LanczosRes(C.Structure):
 
 class SweepParams(C.Structure):
     _fields_ = [("sweeps", C.c_int64), ("Dmin", C.c_int64), ("Dmax", C.c_int64),
-                ("trunc_err", C.c_double), ("lancz_params", LanczosParams)]
+                ("trunc_err", C.c_double), ("lancz_params", LanczosParams),
+                ("svd_mode", C.c_int64), ("svd_oversample", C.c_int64)]
 
 
 class SiteLog(C.Structure):
     _fields_ = [("site", C.c_int64), ("e0", C.c_double), ("trunc_err", C.c_double),
                 ("D", C.c_int64), ("iters", C.c_int64), ("ee", C.c_double),
                 ("lancz_sec", C.c_double), ("svd_sec", C.c_double), ("env_sec", C.c_double),
-                ("tot_sec", C.c_double), ("matvec_flops", C.c_double)]
+                ("tot_sec", C.c_double), ("matvec_flops", C.c_double),
+                ("svd_sketch_total", C.c_int64), ("svd_grow_rounds", C.c_int64)]
 
 
 # name -> argtypes (all return int status)
@@ -72,6 +74,10 @@ SIGNATURES = {
     "udmrg_update_site_renvs": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, c_void_pp],
     "udmrg_svd": [C.c_void_p, C.c_void_p, C.c_int, c_int32_p, C.c_double, C.c_int64, C.c_int64,
                   C.c_int, c_void_pp, c_void_pp, c_void_pp, c_double_p, c_int64_p],
+    "udmrg_svd_randomized": [C.c_void_p, C.c_void_p, C.c_int, c_int32_p, C.c_double, C.c_int64,
+                             C.c_int64, C.c_int, C.c_int64, c_int32_p, c_int64_p, C.c_int64,
+                             C.c_int, C.c_uint64, c_void_pp, c_void_pp, c_void_pp, c_double_p,
+                             c_int64_p, c_int64_p],
     "udmrg_two_site_update": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                               C.c_void_p, C.c_void_p, C.POINTER(SweepParams), C.c_char,
                               c_void_pp, c_void_pp, c_void_pp, C.POINTER(SiteLog)],

@@ -286,6 +286,22 @@ def svd(ctx, t, ldims, ldiv, trunc_err, Dmin, Dmax, mode=SVD_FULL):
     return _new(ctx, u), _new(ctx, s), _new(ctx, vt), float(err.value), int(D.value)
 
 
+def svd_randomized(ctx, t, ldims, ldiv, trunc_err, Dmin, Dmax, sketch, mode=SVD_FULL,
+                   oversample=8, power_iters=2, seed=1):
+    """Sector-wise randomized SVD; ``sketch`` = [(bond QN tuple, sketch size), ...]."""
+    xd, pd = _i32(list(ldiv))
+    qns = [v for q, _ in sketch for v in q] or [0]
+    xq, pq = _i32(qns)
+    xs, ps = _i64([k for _, k in sketch] or [0])
+    u, s, vt = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    err, D, gr = C.c_double(), C.c_int64(), C.c_int64()
+    call("udmrg_svd_randomized", ctx.h, t.h, ldims, pd, trunc_err, Dmin, Dmax, mode,
+         len(sketch), pq, ps, oversample, power_iters, seed, C.byref(u), C.byref(s),
+         C.byref(vt), C.byref(err), C.byref(D), C.byref(gr))
+    return (_new(ctx, u), _new(ctx, s), _new(ctx, vt), float(err.value), int(D.value),
+            int(gr.value))
+
+
 @dataclass
 class FiniteVMPSSweepParams:
     """``FiniteVMPSSweepParams`` (sweeps, Dmin, Dmax, trunc_err, Lanczos params)."""
@@ -297,6 +313,8 @@ class FiniteVMPSSweepParams:
     lanczos_error: float = 1e-7
     lanczos_max_iterations: int = 200
     precision: int = 0  # matvec precision: 0 FP64, 1 mixed (split-BF16 tensor cores)
+    svd_mode: int = 0  # 0 exact, 1 randomized (previous sector dims), 2 randomized (learned)
+    svd_oversample: int = 8
 
 
 def two_site_finite_vmps(ctx, mps: List[DeviceTensor], mpo: List[DeviceTensor],
@@ -305,7 +323,8 @@ def two_site_finite_vmps(ctx, mps: List[DeviceTensor], mpo: List[DeviceTensor],
     N = len(mps)
     sp = _lib.SweepParams(params.sweeps, params.Dmin, params.Dmax, params.trunc_err,
                           _lib.LanczosParams(params.lanczos_error, params.lanczos_max_iterations,
-                                             params.precision))
+                                             params.precision),
+                          params.svd_mode, params.svd_oversample)
     cap = 2 * N * max(params.sweeps, 1)
     log = (_lib.SiteLog * cap)()
     e0 = C.c_double()
@@ -363,7 +382,8 @@ def two_site_update(ctx, lenv, renv, mps_l, mps_r, mpo_l, mpo_r,
     """``TwoSiteFiniteVMPSUpdate`` on one bond: (new_l, new_r, new_env, log)."""
     sp = _lib.SweepParams(1, params.Dmin, params.Dmax, params.trunc_err,
                           _lib.LanczosParams(params.lanczos_error, params.lanczos_max_iterations,
-                                             params.precision))
+                                             params.precision),
+                          params.svd_mode, params.svd_oversample)
     a, b, e = C.c_void_p(), C.c_void_p(), C.c_void_p()
     lg = _lib.SiteLog()
     call("udmrg_two_site_update", ctx.h, lenv.h, renv.h, mps_l.h, mps_r.h, mpo_l.h, mpo_r.h,

@@ -348,6 +348,36 @@ int udmrg_svd(udmrg_ctx *c, const udmrg_tensor *t, int ldims, const int32_t *ldi
   });
 }
 
+int udmrg_svd_randomized(udmrg_ctx *c, const udmrg_tensor *t, int ldims, const int32_t *ldiv,
+                         double trunc_err, int64_t Dmin, int64_t Dmax, int mode, int64_t nsk,
+                         const int32_t *sketch_qns, const int64_t *sketch_sizes,
+                         int64_t oversample, int power_iters, uint64_t seed, udmrg_tensor **u,
+                         udmrg_tensor **s, udmrg_tensor **vt, double *actual_trunc_err,
+                         int64_t *D, int64_t *grow_rounds) {
+  return guarded([&] {
+    const BTensor &x = T(t);
+    QN q;
+    for (int k = 0; k < x.nq; ++k) q.v[k] = ldiv[k];
+    UDMRG_REQUIRE(mode >= 0 && mode <= 2, "bad SVD mode");
+    SketchParams sp;
+    sp.oversample = oversample;
+    sp.power_iters = power_iters;
+    sp.seed = seed;
+    for (int64_t i = 0; i < nsk; ++i) {
+      QN qi;
+      for (int k = 0; k < x.nq; ++k) qi.v[k] = sketch_qns[i * x.nq + k];
+      sp.sketch.push_back({qi, sketch_sizes[i]});
+    }
+    auto r = svd_trunc_sketch(c->ctx, x, ldims, q, trunc_err, Dmin, Dmax, mode, sp);
+    *u = wrap(std::move(r.u));
+    *s = wrap(std::move(r.s));
+    *vt = wrap(std::move(r.vt));
+    if (actual_trunc_err) *actual_trunc_err = r.trunc_err;
+    if (D) *D = r.D;
+    if (grow_rounds) *grow_rounds = r.grow_rounds;
+  });
+}
+
 int udmrg_two_site_update(udmrg_ctx *c, const udmrg_tensor *lenv, const udmrg_tensor *renv,
                           const udmrg_tensor *mps_l, const udmrg_tensor *mps_r,
                           const udmrg_tensor *mpo_l, const udmrg_tensor *mpo_r,
@@ -361,6 +391,8 @@ int udmrg_two_site_update(udmrg_ctx *c, const udmrg_tensor *lenv, const udmrg_te
     p.trunc_err = params->trunc_err;
     p.lancz = {params->lancz_params.error, params->lancz_params.max_iterations,
                (int)params->lancz_params.matvec_precision};
+    p.svd_mode = (int)params->svd_mode;
+    p.svd_oversample = params->svd_oversample;
     SiteLog s{};
     auto r = two_site_update_local(c->ctx, T(lenv), T(renv), T(mps_l), T(mps_r), T(mpo_l),
                                    T(mpo_r), p, dir, &s);
@@ -369,7 +401,7 @@ int udmrg_two_site_update(udmrg_ctx *c, const udmrg_tensor *lenv, const udmrg_te
     *new_env = wrap(std::move(r.env));
     if (log)
       *log = {s.site, s.e0, s.trunc_err, s.D, s.iters, s.ee,
-              s.lancz_sec, s.svd_sec, s.env_sec, s.tot_sec, s.matvec_flops};
+              s.lancz_sec, s.svd_sec, s.env_sec, s.tot_sec, s.matvec_flops, s.svd_sketch_total, s.svd_grow_rounds};
   });
 }
 
@@ -389,6 +421,8 @@ int udmrg_two_site_finite_vmps(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
     p.trunc_err = params->trunc_err;
     p.lancz = {params->lancz_params.error, params->lancz_params.max_iterations,
                (int)params->lancz_params.matvec_precision};
+    p.svd_mode = (int)params->svd_mode;
+    p.svd_oversample = params->svd_oversample;
     std::vector<SiteLog> lg;
     const double e = two_site_finite_vmps(c->ctx, m, w, p, &lg);
     c->ctx.sync();
@@ -399,7 +433,7 @@ int udmrg_two_site_finite_vmps(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
       for (int64_t i = 0; i < std::min<int64_t>(log_cap, (int64_t)lg.size()); ++i) {
         const SiteLog &s = lg[i];
         log[i] = {s.site, s.e0, s.trunc_err, s.D, s.iters, s.ee,
-                  s.lancz_sec, s.svd_sec, s.env_sec, s.tot_sec, s.matvec_flops};
+                  s.lancz_sec, s.svd_sec, s.env_sec, s.tot_sec, s.matvec_flops, s.svd_sketch_total, s.svd_grow_rounds};
       }
   });
 }

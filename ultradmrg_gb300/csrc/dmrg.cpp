@@ -588,7 +588,8 @@ static double two_site_update(Ctx &ctx, std::vector<TensorPtr> &mps,
 LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &renv,
                                   const BTensor &mps_l, const BTensor &mps_r,
                                   const BTensor &mpo_l, const BTensor &mpo_r,
-                                  const SweepParams &p, char dir, SiteLog *log) {
+                                  const SweepParams &p, char dir, SiteLog *log,
+                                  const SketchHint *hint, BondSpectra *spectra) {
   UDMRG_REQUIRE(dir == 'r' || dir == 'l', "dir must be 'r' or 'l'");
   const double t0 = now();
   auto init_state = contract_axes(ctx, mps_l, mps_r, {2}, {0});
@@ -599,9 +600,28 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
   mv.reset();
   init_state.reset();
   const QN ldiv = mps_l.div();
-  auto sres = svd_trunc(ctx, *lres.gs_vec, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax,
-                        dir == 'r' ? kSvdSplitLeft : kSvdSplitRight);
+  const int split = dir == 'r' ? kSvdSplitLeft : kSvdSplitRight;
+  SvdResult sres;
+  if (p.svd_mode == kSvdExact || (p.svd_mode == kSvdSketchLearned && !hint)) {
+    sres = svd_trunc(ctx, *lres.gs_vec, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split);
+  } else {
+    SketchParams sp;
+    sp.oversample = p.svd_oversample;
+    sp.seed = 0x5EEDull + (uint64_t)mps_l.nblocks();
+    if (hint) {
+      sp.sketch = *hint;
+    } else {  // the bond's current sector dimensions (its state from the last visit)
+      const Index &bond = mps_l.idx[2];
+      for (int q = 0; q < bond.nsec(); ++q) sp.sketch.push_back({bond.qns[q], bond.dims[q]});
+    }
+    sres = svd_trunc_sketch(ctx, *lres.gs_vec, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split, sp);
+  }
   lres.gs_vec.reset();
+  if (spectra) {
+    spectra->clear();
+    for (size_t q = 0; q < sres.sector_qn.size(); ++q)
+      spectra->push_back({sres.sector_qn[q], sres.sector_svals[q]});
+  }
   LocalUpdate out;
   out.mps_l = std::move(sres.u);
   out.mps_r = std::move(sres.vt);
@@ -613,9 +633,13 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
     out.env = update_site_renv(ctx, renv, *out.mps_r, mpo_r);
   ctx.sync();
   const double t3 = now();
-  if (log)
-    *log = {0, lres.gs_eng, sres.trunc_err, sres.D, lres.iters, sres.ee, t1 - t0,
-            t2 - t1, t3 - t2, t3 - t0, mvflops};
+  {
+    int64_t sk = 0;
+    for (int64_t v : sres.sector_sketch) sk += v;
+    if (log)
+      *log = {0, lres.gs_eng, sres.trunc_err, sres.D, lres.iters, sres.ee, t1 - t0,
+              t2 - t1, t3 - t2, t3 - t0, mvflops, sk, sres.grow_rounds};
+  }
   return out;
 }
 

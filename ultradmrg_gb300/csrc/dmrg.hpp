@@ -92,11 +92,15 @@ TensorPtr update_site_renv(Ctx &ctx, const BTensor &renv, const BTensor &A, cons
 TensorPtr trivial_renv(Ctx &ctx, const BTensor &mps_last, const BTensor &mpo_last);
 TensorPtr trivial_lenv(Ctx &ctx, const BTensor &mps_first, const BTensor &mpo_first);
 
+enum SvdChoice : int { kSvdExact = 0, kSvdSketchPrev = 1, kSvdSketchLearned = 2 };
+
 struct SweepParams {
   int64_t sweeps = 1;
   int64_t Dmin = 1, Dmax = 1;
   double trunc_err = 0;
   LanczosParams lancz;
+  int svd_mode = kSvdExact;
+  int64_t svd_oversample = 8;
 };
 
 struct SiteLog {
@@ -105,7 +109,14 @@ struct SiteLog {
   int64_t D, iters;
   double ee, lancz_sec, svd_sec, env_sec, tot_sec;
   double matvec_flops;
+  int64_t svd_sketch_total;  // sum of the final sketch sizes (0: exact SVD)
+  int64_t svd_grow_rounds;   // sketch enlargements after a miss
 };
+
+// Sketch sizes of the randomized SVD per bond QN.
+using SketchHint = std::vector<std::pair<QN, int64_t>>;
+// Spectra of the last SVD at a bond: bond QN -> leading singular values.
+using BondSpectra = std::vector<std::pair<QN, std::vector<double>>>;
 
 // One local update (TwoSiteFiniteVMPSUpdate, two_site_update_finite_vmps_impl.h:232-373):
 // Lanczos on the bond (l, l+1), truncated SVD, MPS split by direction, and the
@@ -113,10 +124,14 @@ struct SiteLog {
 struct LocalUpdate {
   TensorPtr mps_l, mps_r, env;
 };
+// hint: sketch sizes for the randomized SVD (learned mode); spectra: receives
+// the leading singular values of every bond sector of this update.
 LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &renv,
                                   const BTensor &mps_l, const BTensor &mps_r,
                                   const BTensor &mpo_l, const BTensor &mpo_r,
-                                  const SweepParams &p, char dir, SiteLog *log);
+                                  const SweepParams &p, char dir, SiteLog *log,
+                                  const SketchHint *hint = nullptr,
+                                  BondSpectra *spectra = nullptr);
 
 // TwoSiteFiniteVMPS (two_site_update_finite_vmps_impl.h:95-494), device
 // resident: mps tensors are replaced in place; returns the last energy.

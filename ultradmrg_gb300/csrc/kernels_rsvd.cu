@@ -1,0 +1,109 @@
+// Kernels of the sector-wise randomized SVD: Gaussian sketch matrices from a
+// counter-based generator, and the inverse Cholesky factor of small
+// symmetric positive semi-definite Gram matrices (one CTA per sector) used by
+// Cholesky-QR orthonormalisation.
+#include "svd.hpp"
+
+namespace udmrg {
+
+namespace {
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+// Standard normal deviates by the Box-Muller transform of two uniforms.
+__global__ void fill_normal_kernel(double *__restrict__ x, int64_t n, uint64_t seed) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint64_t a = splitmix64(seed ^ (uint64_t)(2 * i)), b = splitmix64(seed + (uint64_t)(2 * i + 1));
+    const double u1 = ((double)(a >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    const double u2 = (double)(b >> 11) * (1.0 / 9007199254740992.0);
+    x[i] = sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+  }
+}
+
+// In place: S (n x n, symmetric PSD, row-major) -> R^{-1} where S = R^T R,
+// R upper triangular.  Pivots below rel_tol * max diag drop their direction
+// (row/column of R^{-1} set to zero), which handles rank-deficient sketches.
+// One CTA per job; the matrix stays in global memory (L1/L2 resident).
+__global__ void chol_inv_kernel(const EigJob *__restrict__ jobs, double *__restrict__ S_all,
+                                double *__restrict__ work_all, double rel_tol) {
+  const EigJob job = jobs[blockIdx.x];
+  const int n = job.n;
+  if (n == 0) return;
+  double *S = S_all + job.g_off;
+  double *Ri = work_all + job.g_off;  // R^{-1}
+  const int tid = threadIdx.x, nt = blockDim.x;
+  __shared__ double dmax;
+  __shared__ double piv;
+  if (tid == 0) {
+    double m = 0;
+    for (int i = 0; i < n; ++i) m = fmax(m, S[(int64_t)i * n + i]);
+    dmax = m;
+  }
+  __syncthreads();
+  // Cholesky, upper factor R stored in the upper triangle of S (row k of R)
+  for (int k = 0; k < n; ++k) {
+    if (tid == 0) {
+      const double d = S[(int64_t)k * n + k];
+      piv = (d > rel_tol * dmax && d > 0) ? sqrt(d) : 0.0;
+      S[(int64_t)k * n + k] = piv;
+    }
+    __syncthreads();
+    const double p = piv;
+    for (int j = k + 1 + tid; j < n; j += nt) S[(int64_t)k * n + j] = p > 0 ? S[(int64_t)k * n + j] / p : 0.0;
+    __syncthreads();
+    // trailing update S[i][j] -= R[k][i] R[k][j] for k < i <= j
+    const int m = n - k - 1;
+    for (int64_t e = tid; e < (int64_t)m * m; e += nt) {
+      const int i = k + 1 + (int)(e / m), j = k + 1 + (int)(e % m);
+      if (j >= i) S[(int64_t)i * n + j] -= S[(int64_t)k * n + i] * S[(int64_t)k * n + j];
+    }
+    __syncthreads();
+  }
+  // R^{-1} by back substitution, column by column (upper triangular)
+  for (int64_t e = tid; e < (int64_t)n * n; e += nt) Ri[e] = 0.0;
+  __syncthreads();
+  for (int j = tid; j < n; j += nt) {
+    // solve R x = e_j for column j of R^{-1}
+    const double djj = S[(int64_t)j * n + j];
+    if (djj == 0.0) continue;
+    Ri[(int64_t)j * n + j] = 1.0 / djj;
+    for (int i = j - 1; i >= 0; --i) {
+      const double dii = S[(int64_t)i * n + i];
+      if (dii == 0.0) continue;
+      double s = 0.0;
+      for (int k = i + 1; k <= j; ++k) s += S[(int64_t)i * n + k] * Ri[(int64_t)k * n + j];
+      Ri[(int64_t)i * n + j] = -s / dii;
+    }
+  }
+}
+
+}  // namespace
+
+void fill_normal(Ctx &ctx, double *x, int64_t n, uint64_t seed) {
+  if (n == 0) return;
+  const int grid = (int)std::min<int64_t>((n + 255) / 256, 8 * ctx.num_sms);
+  fill_normal_kernel<<<grid, 256, 0, ctx.stream>>>(x, n, seed);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  ctx.launches++;
+}
+
+void run_chol_inv(Ctx &ctx, const std::vector<EigJob> &jobs, double *S, double *Rinv,
+                  double rel_tol) {
+  if (jobs.empty()) return;
+  EigJob *d = (EigJob *)ctx.alloc(jobs.size() * sizeof(EigJob));
+  UDMRG_CHECK_CUDA(cudaMemcpyAsync(d, jobs.data(), jobs.size() * sizeof(EigJob),
+                                   cudaMemcpyHostToDevice, ctx.stream));
+  chol_inv_kernel<<<(int)jobs.size(), 256, 0, ctx.stream>>>(d, S, Rinv, rel_tol);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  ctx.launches++;
+  ctx.sync();
+  ctx.free(d);
+}
+
+}  // namespace udmrg

@@ -3,11 +3,14 @@
 // The tensor is grouped into bond sectors by the QN of the new bond
 // (qn_bond = ldiv - sum_{i<ldims} dir_i qn_i, the call convention of
 // two_site_update_finite_vmps_impl.h:302-307, where SVD gets Div(mps[l])).
-// Each sector is gathered into a dense matrix M_q.  The side that has to come
-// out as an isometry is taken from the eigen-decomposition of a Gram matrix
-// (M M^T for the left factor, M^T M for the right one; cyclic Jacobi, FP64),
-// and the other factor is the exact product with M (U^T M = S V^T or
-// M V = U S), so no division by small singular values is needed.
+// Each sector is gathered into a dense matrix M_q.  The factor that has to be
+// an isometry (U for a right move / the plain SVD, V for a left move) comes
+// from an eigen-decomposition in FP64; the other factor is the exact product
+// with M (U^T M = S V^T or M V = U S), so no division by small singular
+// values is needed.
+//   exact path:      eigenvectors of the full Gram matrix M M^T (or M^T M);
+//   randomized path: range of a Gaussian sketch refined by power iterations,
+//                    then the eigenvectors of the projected Gram matrix.
 #include "svd.hpp"
 
 #include <algorithm>
@@ -18,7 +21,7 @@ namespace udmrg {
 
 void select_kept(const std::vector<std::vector<double>> &svals, double trunc_err, int64_t Dmin,
                  int64_t Dmax, std::vector<int64_t> &kept, int64_t &D, double &err,
-                 double rtol) {
+                 double rtol, double extra_mass) {
   struct E {
     double s;
     int q;
@@ -55,6 +58,7 @@ void select_kept(const std::vector<std::vector<double>> &svals, double trunc_err
     i = j;
   }
   std::vector<double> tail(n + 1, 0.0);
+  tail[n] = extra_mass;
   for (int64_t k = n - 1; k >= 0; --k) tail[k] = tail[k + 1] + ord[k].s * ord[k].s;
   const double total = tail[0];
   const int64_t lo = std::min(Dmin, n), hi = std::min(Dmax, n);
@@ -84,26 +88,24 @@ int64_t prod_dims(const BTensor &T, const std::vector<int32_t> &k, int first) {
   return p;
 }
 
-}  // namespace
+QN row_qn(const BTensor &T, int64_t b, int ldims) {
+  QN q;
+  for (int i = 0; i < ldims; ++i) q = q + T.idx[i].qns[T.key(b)[i]].scaled(T.idx[i].dir);
+  return q;
+}
 
-SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, double trunc_err,
-                    int64_t Dmin, int64_t Dmax, int mode) {
-  UDMRG_REQUIRE(ldims > 0 && ldims < T.rank(), "svd: bad ldims");
-  UDMRG_REQUIRE(T.dtype == kF64, "svd: complex tensors are not supported by this SVD yet");
+std::vector<Sector> group_sectors(const BTensor &T, int ldims, const QN &ldiv, int64_t &mtot) {
   const int r = T.rank();
-  // 1. bond sectors
   std::map<QN, std::pair<std::map<std::vector<int32_t>, int>, std::map<std::vector<int32_t>, int>>>
       smap;
   for (int64_t b = 0; b < T.nblocks(); ++b) {
     std::vector<int32_t> lk(T.key(b), T.key(b) + ldims), rk(T.key(b) + ldims, T.key(b) + r);
-    QN qrow;
-    for (int i = 0; i < ldims; ++i) qrow = qrow + T.idx[i].qns[lk[i]].scaled(T.idx[i].dir);
-    auto &sec = smap[ldiv - qrow];
+    auto &sec = smap[ldiv - row_qn(T, b, ldims)];
     sec.first[lk] = 0;
     sec.second[rk] = 0;
   }
   std::vector<Sector> secs;
-  int64_t mtot = 0;
+  mtot = 0;
   for (auto &kv : smap) {
     Sector s;
     s.qn = kv.first;
@@ -123,85 +125,54 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
     mtot += s.rows * s.cols;
     secs.push_back(std::move(s));
   }
-  const int nsec = (int)secs.size();
-  // 2. gather dense sector matrices
-  DeviceScratch scratch(ctx);
-  double *Mbuf = scratch.get<double>(std::max<int64_t>(mtot, 1));
+  return secs;
+}
+
+void gather(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, std::vector<Sector> &secs,
+            double *Mbuf, int64_t mtot) {
+  const int r = T.rank();
   UDMRG_CHECK_CUDA(cudaMemsetAsync(Mbuf, 0, std::max<int64_t>(mtot, 1) * sizeof(double), ctx.stream));
-  {
-    std::vector<Copy2D> ops;
-    std::map<QN, int> qidx;
-    for (int q = 0; q < nsec; ++q) qidx[secs[q].qn] = q;
-    for (int64_t b = 0; b < T.nblocks(); ++b) {
-      std::vector<int32_t> lk(T.key(b), T.key(b) + ldims), rk(T.key(b) + ldims, T.key(b) + r);
-      QN qrow;
-      for (int i = 0; i < ldims; ++i) qrow = qrow + T.idx[i].qns[lk[i]].scaled(T.idx[i].dir);
-      Sector &s = secs[qidx[ldiv - qrow]];
-      const int li = (int)(std::lower_bound(s.lkeys.begin(), s.lkeys.end(), lk) - s.lkeys.begin());
-      const int ri = (int)(std::lower_bound(s.rkeys.begin(), s.rkeys.end(), rk) - s.rkeys.begin());
-      Copy2D c{};
-      c.src_off = T.offs[b];
-      c.rows = (int32_t)s.rsz[li];
-      c.cols = (int32_t)s.csz[ri];
-      c.src_ld = c.cols;
-      c.src_cs = 1;
-      c.dst_off = s.m_off + s.roff[li] * s.cols + s.coff[ri];
-      c.dst_ld = s.cols;
-      c.dst_cs = 1;
-      ops.push_back(c);
-    }
-    run_copy2d(ctx, ops, T.data, Mbuf, false);
+  std::vector<Copy2D> ops;
+  std::map<QN, int> qidx;
+  for (int q = 0; q < (int)secs.size(); ++q) qidx[secs[q].qn] = q;
+  for (int64_t b = 0; b < T.nblocks(); ++b) {
+    std::vector<int32_t> lk(T.key(b), T.key(b) + ldims), rk(T.key(b) + ldims, T.key(b) + r);
+    Sector &s = secs[qidx[ldiv - row_qn(T, b, ldims)]];
+    const int li = (int)(std::lower_bound(s.lkeys.begin(), s.lkeys.end(), lk) - s.lkeys.begin());
+    const int ri = (int)(std::lower_bound(s.rkeys.begin(), s.rkeys.end(), rk) - s.rkeys.begin());
+    Copy2D c{};
+    c.src_off = T.offs[b];
+    c.rows = (int32_t)s.rsz[li];
+    c.cols = (int32_t)s.csz[ri];
+    c.src_ld = c.cols;
+    c.src_cs = 1;
+    c.dst_off = s.m_off + s.roff[li] * s.cols + s.coff[ri];
+    c.dst_ld = s.cols;
+    c.dst_cs = 1;
+    ops.push_back(c);
   }
-  // 3. Gram matrices on the isometry side
+  run_copy2d(ctx, ops, T.data, Mbuf, false);
+}
+
+// View of M_q (left side) or M_q^T (right side) as an (xr x xc) matrix.
+struct XView {
+  int64_t off, xr, xc, sr, sc;  // element (i, j) at off + i*sr + j*sc
+};
+XView xview(const Sector &s, bool left) {
+  if (left) return {s.m_off, s.rows, s.cols, s.cols, 1};
+  return {s.m_off, s.cols, s.rows, 1, s.cols};
+}
+
+// Build u, s, vt from the isometric factor of every sector: iso(i, j) =
+// iso_buf[iso_off[q] + i*iso_ld[q] + j], i over rows (left) or columns (right)
+// of M_q, j over the kept states.
+void build_outputs(Ctx &ctx, DeviceScratch &scratch, const BTensor &T, int ldims,
+                   const std::vector<Sector> &secs, const std::vector<int64_t> &kept,
+                   const std::vector<std::vector<double>> &sv, int mode, const double *iso_buf,
+                   const std::vector<int64_t> &iso_off, const std::vector<int64_t> &iso_ld,
+                   const double *Mbuf, SvdResult &res) {
+  const int nsec = (int)secs.size();
   const bool left = (mode != kSvdSplitRight);
-  std::vector<EigJob> jobs(nsec);
-  int64_t gtot = 0, ltot = 0;
-  for (int q = 0; q < nsec; ++q) {
-    const int64_t n = left ? secs[q].rows : secs[q].cols;
-    jobs[q].g_off = gtot;
-    jobs[q].lam_off = ltot;
-    jobs[q].n = (int32_t)n;
-    gtot += n * n;
-    ltot += n;
-  }
-  double *G = scratch.get<double>(std::max<int64_t>(gtot, 1));
-  double *V = scratch.get<double>(std::max<int64_t>(gtot, 1));
-  double *W = scratch.get<double>(std::max<int64_t>(gtot, 1));
-  double *lam = scratch.get<double>(std::max<int64_t>(ltot, 1));
-  {
-    GemmPlan g;
-    g.ctx = &ctx;
-    for (int q = 0; q < nsec; ++q) {
-      const Sector &s = secs[q];
-      if (left)  // G = M M^T
-        gemm_add_simple(g, jobs[q].g_off, s.rows, s.rows, s.cols, s.m_off, s.cols, 1, s.m_off, 1,
-                        s.cols, false);
-      else  // G = M^T M
-        gemm_add_simple(g, jobs[q].g_off, s.cols, s.cols, s.rows, s.m_off, 1, s.cols, s.m_off,
-                        s.cols, 1, false);
-    }
-    gemm_finalize(g);
-    run_gemm(ctx, g, kF64, Mbuf, Mbuf, G, 1.0, 0.0);
-  }
-  const int st = run_jacobi_eig(ctx, jobs, G, V, W, lam);
-  if (st != 0) throw Error(kErrNumerics, "svd: Jacobi eigensolver did not converge");
-  // 4. selection on the host
-  std::vector<double> hlam(ltot);
-  if (ltot)
-    UDMRG_CHECK_CUDA(cudaMemcpyAsync(hlam.data(), lam, ltot * sizeof(double),
-                                     cudaMemcpyDeviceToHost, ctx.stream));
-  ctx.sync();
-  std::vector<std::vector<double>> sv(nsec);
-  for (int q = 0; q < nsec; ++q) {
-    const int64_t n = jobs[q].n;
-    const int64_t rank_max = std::min(secs[q].rows, secs[q].cols);
-    for (int64_t i = 0; i < std::min(n, rank_max); ++i)
-      sv[q].push_back(std::sqrt(std::max(hlam[jobs[q].lam_off + i], 0.0)));
-  }
-  SvdResult res;
-  std::vector<int64_t> kept;
-  select_kept(sv, trunc_err, Dmin, Dmax, kept, res.D, res.trunc_err);
-  // 5. outputs
   Index bond;
   bond.dir = 1;
   std::vector<int> bid(nsec, -1);
@@ -244,7 +215,6 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
   u->alloc_data();
   vt->alloc_data();
   s->alloc_data();
-  // s: diagonal blocks, filled on the host
   {
     std::vector<double> hs(s->size(), 0.0);
     for (int q = 0; q < nsec; ++q) {
@@ -277,19 +247,18 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
     for (int q = 0; q < nsec; ++q) {
       if (!kept[q]) continue;
       const Sector &sc = secs[q];
-      const int64_t n = jobs[q].n;
-      if (left)  // C(i, col) = sum_row V[row, i] M[row, col]
-        gemm_add_simple(g, coffs[q], kept[q], sc.cols, sc.rows, jobs[q].g_off, 1, n, sc.m_off,
+      if (left)  // C(i, col) = sum_row U[row, i] M[row, col]
+        gemm_add_simple(g, coffs[q], kept[q], sc.cols, sc.rows, iso_off[q], 1, iso_ld[q], sc.m_off,
                         sc.cols, 1, false);
       else  // C(row, i) = sum_col M[row, col] V[col, i]
         gemm_add_simple(g, coffs[q], sc.rows, kept[q], sc.cols, sc.m_off, sc.cols, 1,
-                        jobs[q].g_off, n, 1, false);
+                        iso_off[q], iso_ld[q], 1, false);
     }
     gemm_finalize(g);
     if (left)
-      run_gemm(ctx, g, kF64, V, Mbuf, Cbuf, 1.0, 0.0);
+      run_gemm(ctx, g, kF64, iso_buf, Mbuf, Cbuf, 1.0, 0.0);
     else
-      run_gemm(ctx, g, kF64, Mbuf, V, Cbuf, 1.0, 0.0);
+      run_gemm(ctx, g, kF64, Mbuf, iso_buf, Cbuf, 1.0, 0.0);
   }
   if (mode == kSvdFull) {
     // vt = S^{-1} (U^T M): scale row i of each centre block by 1/s_i (0 for s_i == 0)
@@ -311,13 +280,11 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
                                      cudaMemcpyHostToDevice, ctx.stream));
     run_scale(ctx, sj, Cbuf, dinv, false);
   }
-  // scatter into u and vt
   std::vector<Copy2D> uops, vops;
   for (int q = 0; q < nsec; ++q) {
     if (!kept[q]) continue;
     const Sector &sc = secs[q];
     const int64_t k = kept[q];
-    const int64_t n = jobs[q].n;
     for (size_t li = 0; li < sc.lkeys.size(); ++li) {
       std::vector<int32_t> key = sc.lkeys[li];
       key.push_back(bid[q]);
@@ -328,15 +295,14 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
       c.cols = (int32_t)k;
       c.dst_ld = k;
       c.dst_cs = 1;
-      if (left) {  // U rows from the eigenvectors (row-major n x n, columns sorted)
-        c.src_off = jobs[q].g_off + sc.roff[li] * n;
-        c.src_ld = n;
-        c.src_cs = 1;
+      if (left) {  // U rows from the isometric factor
+        c.src_off = iso_off[q] + sc.roff[li] * iso_ld[q];
+        c.src_ld = iso_ld[q];
       } else {  // U S = M V rows from the centre (rows x k)
         c.src_off = coffs[q] + sc.roff[li] * k;
         c.src_ld = k;
-        c.src_cs = 1;
       }
+      c.src_cs = 1;
       uops.push_back(c);
     }
     for (size_t ri = 0; ri < sc.rkeys.size(); ++ri) {
@@ -354,19 +320,279 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
         c.src_ld = sc.cols;
         c.src_cs = 1;
       } else {  // V^T(i, j) = V[coff + j, i]
-        c.src_off = jobs[q].g_off + sc.coff[ri] * n;
+        c.src_off = iso_off[q] + sc.coff[ri] * iso_ld[q];
         c.src_ld = 1;
-        c.src_cs = n;
+        c.src_cs = iso_ld[q];
       }
       vops.push_back(c);
     }
   }
-  run_copy2d(ctx, uops, left ? V : Cbuf, u->data, false);
-  run_copy2d(ctx, vops, left ? Cbuf : V, vt->data, false);
+  run_copy2d(ctx, uops, left ? iso_buf : Cbuf, u->data, false);
+  run_copy2d(ctx, vops, left ? Cbuf : iso_buf, vt->data, false);
   res.u = std::move(u);
   res.s = std::move(s);
   res.vt = std::move(vt);
+  for (int q = 0; q < nsec; ++q) {
+    res.sector_qn.push_back(secs[q].qn);
+    res.sector_rows.push_back(secs[q].rows);
+    res.sector_cols.push_back(secs[q].cols);
+    res.sector_kept.push_back(kept[q]);
+    res.sector_svals.push_back(sv[q]);
+  }
+}
+
+std::vector<double> download_vec(Ctx &ctx, const double *d, int64_t n) {
+  std::vector<double> h(n);
+  if (n)
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(h.data(), d, n * sizeof(double), cudaMemcpyDeviceToHost,
+                                     ctx.stream));
+  ctx.sync();
+  return h;
+}
+
+}  // namespace
+
+SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, double trunc_err,
+                    int64_t Dmin, int64_t Dmax, int mode) {
+  UDMRG_REQUIRE(ldims > 0 && ldims < T.rank(), "svd: bad ldims");
+  UDMRG_REQUIRE(T.dtype == kF64, "svd: complex tensors are not supported by this SVD yet");
+  int64_t mtot = 0;
+  auto secs = group_sectors(T, ldims, ldiv, mtot);
+  const int nsec = (int)secs.size();
+  DeviceScratch scratch(ctx);
+  double *Mbuf = scratch.get<double>(std::max<int64_t>(mtot, 1));
+  gather(ctx, T, ldims, ldiv, secs, Mbuf, mtot);
+  // Gram matrices on the isometry side
+  const bool left = (mode != kSvdSplitRight);
+  std::vector<EigJob> jobs(nsec);
+  int64_t gtot = 0, ltot = 0;
+  for (int q = 0; q < nsec; ++q) {
+    const int64_t n = left ? secs[q].rows : secs[q].cols;
+    jobs[q].g_off = gtot;
+    jobs[q].lam_off = ltot;
+    jobs[q].n = (int32_t)n;
+    gtot += n * n;
+    ltot += n;
+  }
+  double *G = scratch.get<double>(std::max<int64_t>(gtot, 1));
+  double *V = scratch.get<double>(std::max<int64_t>(gtot, 1));
+  double *W = scratch.get<double>(std::max<int64_t>(gtot, 1));
+  double *lam = scratch.get<double>(std::max<int64_t>(ltot, 1));
+  {
+    GemmPlan g;
+    g.ctx = &ctx;
+    for (int q = 0; q < nsec; ++q) {
+      const XView x = xview(secs[q], left);  // G = X X^T
+      gemm_add_simple(g, jobs[q].g_off, x.xr, x.xr, x.xc, x.off, x.sr, x.sc, x.off, x.sc, x.sr,
+                      false);
+    }
+    gemm_finalize(g);
+    run_gemm(ctx, g, kF64, Mbuf, Mbuf, G, 1.0, 0.0);
+  }
+  const int st = run_jacobi_eig(ctx, jobs, G, V, W, lam);
+  if (st != 0) throw Error(kErrNumerics, "svd: Jacobi eigensolver did not converge");
+  const std::vector<double> hlam = download_vec(ctx, lam, ltot);
+  std::vector<std::vector<double>> sv(nsec);
+  for (int q = 0; q < nsec; ++q) {
+    const int64_t n = jobs[q].n;
+    const int64_t rank_max = std::min(secs[q].rows, secs[q].cols);
+    for (int64_t i = 0; i < std::min(n, rank_max); ++i)
+      sv[q].push_back(std::sqrt(std::max(hlam[jobs[q].lam_off + i], 0.0)));
+  }
+  SvdResult res;
+  std::vector<int64_t> kept;
+  select_kept(sv, trunc_err, Dmin, Dmax, kept, res.D, res.trunc_err);
+  std::vector<int64_t> iso_off(nsec), iso_ld(nsec);
+  for (int q = 0; q < nsec; ++q) {
+    iso_off[q] = jobs[q].g_off;
+    iso_ld[q] = jobs[q].n;
+  }
+  build_outputs(ctx, scratch, T, ldims, secs, kept, sv, mode, V, iso_off, iso_ld, Mbuf, res);
+  res.sector_sketch.assign(nsec, 0);
   return res;
+}
+
+SvdResult svd_trunc_sketch(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv,
+                           double trunc_err, int64_t Dmin, int64_t Dmax, int mode,
+                           const SketchParams &sp) {
+  UDMRG_REQUIRE(ldims > 0 && ldims < T.rank(), "svd: bad ldims");
+  UDMRG_REQUIRE(T.dtype == kF64, "svd: complex tensors are not supported by this SVD yet");
+  int64_t mtot = 0;
+  auto secs = group_sectors(T, ldims, ldiv, mtot);
+  const int nsec = (int)secs.size();
+  const bool left = (mode != kSvdSplitRight);
+  DeviceScratch scratch(ctx);
+  double *Mbuf = scratch.get<double>(std::max<int64_t>(mtot, 1));
+  gather(ctx, T, ldims, ldiv, secs, Mbuf, mtot);
+  // exact squared Frobenius norm of every sector (the residual mass reference)
+  std::vector<double> fro(nsec, 0.0);
+  {
+    VecWork w(ctx);
+    for (int q = 0; q < nsec; ++q)
+      fro[q] = norm2(w, Mbuf + secs[q].m_off, secs[q].rows * secs[q].cols);
+  }
+  std::map<QN, int64_t> req;
+  for (auto &kv : sp.sketch) req[kv.first] = kv.second;
+  std::vector<int64_t> s(nsec);
+  for (int q = 0; q < nsec; ++q) {
+    const int64_t full = std::min(secs[q].rows, secs[q].cols);
+    auto it = req.find(secs[q].qn);
+    const int64_t want = it == req.end() ? full : it->second + sp.oversample;
+    s[q] = std::max<int64_t>(1, std::min(full, want));
+  }
+  SvdResult res;
+  for (int round = 0;; ++round) {
+    DeviceScratch rs(ctx);
+    // buffers: Y (xr x s), Z (xc x s), Omega (xc x s), S/Rinv (s x s)
+    std::vector<int64_t> yoff(nsec), zoff(nsec), soff(nsec);
+    int64_t ytot = 0, ztot = 0, stot = 0;
+    for (int q = 0; q < nsec; ++q) {
+      const XView x = xview(secs[q], left);
+      yoff[q] = ytot;
+      zoff[q] = ztot;
+      soff[q] = stot;
+      ytot += x.xr * s[q];
+      ztot += x.xc * s[q];
+      stot += s[q] * s[q];
+    }
+    double *Y = rs.get<double>(ytot), *Y2 = rs.get<double>(ytot);
+    double *Z = rs.get<double>(ztot), *Z2 = rs.get<double>(ztot);
+    double *Sg = rs.get<double>(stot), *Ri = rs.get<double>(stot);
+    double *Vv = rs.get<double>(stot), *Wk = rs.get<double>(stot);
+    double *lam = rs.get<double>(std::max<int64_t>(1, [&] {
+      int64_t t = 0;
+      for (int q = 0; q < nsec; ++q) t += s[q];
+      return t;
+    }()));
+    std::vector<EigJob> jobs(nsec);
+    {
+      int64_t lt = 0;
+      for (int q = 0; q < nsec; ++q) {
+        jobs[q].g_off = soff[q];
+        jobs[q].lam_off = lt;
+        jobs[q].n = (int32_t)s[q];
+        lt += s[q];
+      }
+    }
+    // Z <- Omega (xc x s), Y <- X Z
+    fill_normal(ctx, Z, ztot, sp.seed * 0x9E3779B97F4A7C15ull + (uint64_t)round);
+    auto mult_xz = [&](const double *zin, double *yout) {  // Y = X Z
+      GemmPlan g;
+      g.ctx = &ctx;
+      for (int q = 0; q < nsec; ++q) {
+        const XView x = xview(secs[q], left);
+        gemm_add_simple(g, yoff[q], x.xr, s[q], x.xc, x.off, x.sr, x.sc, zoff[q], s[q], 1, false);
+      }
+      gemm_finalize(g);
+      run_gemm(ctx, g, kF64, Mbuf, zin, yout, 1.0, 0.0);
+    };
+    auto mult_xty = [&](const double *yin, double *zout) {  // Z = X^T Y
+      GemmPlan g;
+      g.ctx = &ctx;
+      for (int q = 0; q < nsec; ++q) {
+        const XView x = xview(secs[q], left);
+        gemm_add_simple(g, zoff[q], x.xc, s[q], x.xr, x.off, x.sc, x.sr, yoff[q], s[q], 1, false);
+      }
+      gemm_finalize(g);
+      run_gemm(ctx, g, kF64, Mbuf, yin, zout, 1.0, 0.0);
+    };
+    // Cholesky-QR of the columns of B (rows x s per sector): out = B R^{-1}
+    auto cholqr = [&](const double *bin, double *bout, const std::vector<int64_t> &boff,
+                      bool on_y) {
+      GemmPlan g;
+      g.ctx = &ctx;
+      for (int q = 0; q < nsec; ++q) {
+        const XView x = xview(secs[q], left);
+        const int64_t rows = on_y ? x.xr : x.xc;
+        gemm_add_simple(g, soff[q], s[q], s[q], rows, boff[q], 1, s[q], boff[q], s[q], 1, false);
+      }
+      gemm_finalize(g);
+      run_gemm(ctx, g, kF64, bin, bin, Sg, 1.0, 0.0);
+      run_chol_inv(ctx, jobs, Sg, Ri, 1e-28);
+      GemmPlan h;
+      h.ctx = &ctx;
+      for (int q = 0; q < nsec; ++q) {
+        const XView x = xview(secs[q], left);
+        const int64_t rows = on_y ? x.xr : x.xc;
+        gemm_add_simple(h, boff[q], rows, s[q], s[q], boff[q], s[q], 1, soff[q], s[q], 1, false);
+      }
+      gemm_finalize(h);
+      run_gemm(ctx, h, kF64, bin, Ri, bout, 1.0, 0.0);
+    };
+    mult_xz(Z, Y);
+    for (int it = 0; it < sp.power_iters; ++it) {
+      cholqr(Y, Y2, yoff, true);
+      mult_xty(Y2, Z);
+      cholqr(Z, Z2, zoff, false);
+      mult_xz(Z2, Y);
+    }
+    cholqr(Y, Y2, yoff, true);
+    cholqr(Y2, Y, yoff, true);  // second pass: Q = Y (orthonormal to FP64 accuracy)
+    // B^T = X^T Q (xc x s) -> G = B B^T = (X^T Q)^T (X^T Q) (s x s)
+    mult_xty(Y, Z);
+    {
+      GemmPlan g;
+      g.ctx = &ctx;
+      for (int q = 0; q < nsec; ++q) {
+        const XView x = xview(secs[q], left);
+        gemm_add_simple(g, soff[q], s[q], s[q], x.xc, zoff[q], 1, s[q], zoff[q], s[q], 1, false);
+      }
+      gemm_finalize(g);
+      run_gemm(ctx, g, kF64, Z, Z, Sg, 1.0, 0.0);
+    }
+    const int st = run_jacobi_eig(ctx, jobs, Sg, Vv, Wk, lam);
+    if (st != 0) throw Error(kErrNumerics, "svd: Jacobi eigensolver did not converge");
+    // isometric factor U = Q W (xr x s), written into Y2
+    {
+      GemmPlan g;
+      g.ctx = &ctx;
+      for (int q = 0; q < nsec; ++q) {
+        const XView x = xview(secs[q], left);
+        gemm_add_simple(g, yoff[q], x.xr, s[q], s[q], yoff[q], s[q], 1, soff[q], s[q], 1, false);
+      }
+      gemm_finalize(g);
+      run_gemm(ctx, g, kF64, Y, Vv, Y2, 1.0, 0.0);
+    }
+    int64_t ltot = 0;
+    for (int q = 0; q < nsec; ++q) ltot += s[q];
+    const std::vector<double> hl = download_vec(ctx, lam, ltot);
+    std::vector<std::vector<double>> sv(nsec);
+    double resid = 0.0;
+    for (int q = 0; q < nsec; ++q) {
+      double got = 0.0;
+      for (int64_t i = 0; i < s[q]; ++i) {
+        const double l = std::max(hl[jobs[q].lam_off + i], 0.0);
+        sv[q].push_back(std::sqrt(l));
+        got += l;
+      }
+      resid += std::max(fro[q] - got, 0.0);
+    }
+    std::vector<int64_t> kept;
+    SvdResult trial;
+    select_kept(sv, trunc_err, Dmin, Dmax, kept, trial.D, trial.trunc_err, 1e-12, resid);
+    // misses: a sector whose whole sketch is kept, while it could hold more
+    bool grow = false;
+    for (int q = 0; q < nsec; ++q) {
+      const int64_t full = std::min(secs[q].rows, secs[q].cols);
+      if (kept[q] == s[q] && s[q] < full) {
+        s[q] = std::min(full, 2 * s[q] + sp.oversample);
+        grow = true;
+      }
+    }
+    if (grow && round < 8) continue;
+    std::vector<int64_t> iso_off(nsec), iso_ld(nsec);
+    for (int q = 0; q < nsec; ++q) {
+      iso_off[q] = yoff[q];
+      iso_ld[q] = s[q];
+    }
+    res.D = trial.D;
+    res.trunc_err = trial.trunc_err;
+    build_outputs(ctx, scratch, T, ldims, secs, kept, sv, mode, Y2, iso_off, iso_ld, Mbuf, res);
+    res.sector_sketch = s;
+    res.grow_rounds = round;
+    ctx.sync();
+    return res;
+  }
 }
 
 }  // namespace udmrg

@@ -40,7 +40,12 @@ void run_scale(Ctx &ctx, const std::vector<ScaleJob> &jobs, double *X, const dou
 // discarded weight sum_{discarded} s^2 / sum s^2 <= trunc_err.
 void select_kept(const std::vector<std::vector<double>> &svals, double trunc_err, int64_t Dmin,
                  int64_t Dmax, std::vector<int64_t> &kept, int64_t &D, double &err,
-                 double rtol = 1e-12);
+                 double rtol = 1e-12, double extra_mass = 0.0);
+
+void fill_normal(Ctx &ctx, double *x, int64_t n, uint64_t seed);
+// S (per job, n x n PSD) -> R^{-1} with S = R^T R (pivots below rel_tol drop)
+void run_chol_inv(Ctx &ctx, const std::vector<EigJob> &jobs, double *S, double *Rinv,
+                  double rel_tol);
 
 enum SvdMode : int {
   kSvdFull = 0,        // u, s, vt with M = u s vt
@@ -54,9 +59,33 @@ struct SvdResult {
   int64_t D = 0;
   std::vector<double> svals;  // kept singular values, bond-sector order
   double ee = 0;              // -sum s^2 log s^2 over kept values
+  // per bond sector (ascending QN): QN, matrix shape, kept count, sketch size
+  // (randomized path; 0 for the exact one) and the leading singular values
+  std::vector<QN> sector_qn;
+  std::vector<int64_t> sector_rows, sector_cols, sector_kept, sector_sketch;
+  std::vector<std::vector<double>> sector_svals;
+  int64_t grow_rounds = 0;  // randomized path: sketch enlargements after a miss
 };
 
 SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, double trunc_err,
                     int64_t Dmin, int64_t Dmax, int mode);
+
+// Sector-wise randomized truncated SVD.  For every bond sector a Gaussian
+// sketch of `sketch[q]` columns (default: full rank, i.e. exact) spans the
+// dominant subspace after `power_iters` power iterations with Cholesky-QR
+// re-orthonormalisation; the projected problem is solved exactly (FP64 Gram +
+// Jacobi).  Discarded weight counts the exact residual mass outside the
+// sketches.  A sector whose sketch is entirely kept is a miss: its sketch
+// grows (x2) and the decomposition is repeated, up to full rank, so the kept
+// set never depends on a too-small sketch.
+struct SketchParams {
+  std::vector<std::pair<QN, int64_t>> sketch;  // requested sketch size per bond QN
+  int64_t oversample = 8;
+  int power_iters = 2;
+  uint64_t seed = 1;
+};
+SvdResult svd_trunc_sketch(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv,
+                           double trunc_err, int64_t Dmin, int64_t Dmax, int mode,
+                           const SketchParams &sp);
 
 }  // namespace udmrg
