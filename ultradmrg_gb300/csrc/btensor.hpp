@@ -50,6 +50,11 @@ struct Ctx {
   size_t pinned_cap = 0;
   // counts of kernels launched by this library through this context
   uint64_t launches = 0;
+  // C-ABI lifetime: live tensor / plan handles on this context; a context
+  // whose destroy was requested is deleted when the last handle goes
+  int64_t live_handles = 0;
+  bool closing = false;
+  void *owner = nullptr;  // the C-ABI object that holds this context
 
   explicit Ctx(int dev);
   ~Ctx();

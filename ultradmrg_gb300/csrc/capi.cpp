@@ -56,8 +56,17 @@ int guarded(F &&f) {
 
 udmrg_tensor *wrap(TensorPtr t) {
   auto *h = new udmrg_tensor;
+  if (t && t->ctx) t->ctx->live_handles++;
   h->t = std::move(t);
   return h;
+}
+
+// A handle on `c` went away: delete the context if its destroy was requested
+// and this was the last handle.
+void release_ctx(Ctx *c) {
+  if (!c) return;
+  c->live_handles--;
+  if (c->closing && c->live_handles <= 0) delete (udmrg_ctx *)c->owner;
 }
 
 const BTensor &T(const udmrg_tensor *h) {
@@ -83,11 +92,17 @@ int udmrg_ctx_create(int device, udmrg_ctx **out) {
   return guarded([&] {
     UDMRG_REQUIRE(out, "null output");
     *out = new udmrg_ctx(device);
+    (*out)->ctx.owner = *out;
   });
 }
 
 int udmrg_ctx_destroy(udmrg_ctx *c) {
-  return guarded([&] { delete c; });
+  return guarded([&] {
+    if (!c) return;
+    // tensors and plans still alive keep the context until they are destroyed
+    c->ctx.closing = true;
+    if (c->ctx.live_handles <= 0) delete c;
+  });
 }
 
 int udmrg_ctx_sync(udmrg_ctx *c) {
@@ -139,7 +154,12 @@ int udmrg_tensor_create(udmrg_ctx *c, int dtype, int nq, int rank, const int32_t
 }
 
 int udmrg_tensor_destroy(udmrg_tensor *t) {
-  return guarded([&] { delete t; });
+  return guarded([&] {
+    if (!t) return;
+    Ctx *c = t->t ? t->t->ctx : nullptr;
+    delete t;
+    release_ctx(c);
+  });
 }
 
 int udmrg_tensor_info(const udmrg_tensor *h, int *dtype, int *nq, int *rank, int64_t *nblocks,
@@ -451,6 +471,7 @@ int udmrg_matvec_plan_create_ex(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
     const BTensor &psi = T(psi_struct);
     auto p = new udmrg_matvec_plan;
     p->ctx = &ctx;
+    ctx.live_handles++;
     const BTensor *op[4];
     for (int i = 0; i < 4; ++i) {
       const BTensor &t = T(eff_ham[i]);
@@ -599,7 +620,12 @@ int udmrg_matvec_plan_stage_times(udmrg_matvec_plan *p, const double *d_in, doub
 }
 
 int udmrg_matvec_plan_destroy(udmrg_matvec_plan *p) {
-  return guarded([&] { delete p; });
+  return guarded([&] {
+    if (!p) return;
+    Ctx *c = p->ctx;
+    delete p;
+    release_ctx(c);
+  });
 }
 
 }  // extern "C"
