@@ -72,6 +72,9 @@ typedef struct {
    * (SKETCH_LEARNED, see udmrg_rank_model_*); svd_oversample extra columns */
   int64_t svd_mode;
   int64_t svd_oversample;
+  /* nonzero: the exact block SVD also runs on every randomized SVD's input
+   * and judges it (svd_audit_* of the site log; its time is not counted) */
+  int64_t svd_audit;
 } udmrg_sweep_params;
 
 /* One line of the per-site log printed by TwoSiteFiniteVMPSUpdate
@@ -83,6 +86,10 @@ typedef struct {
   double ee, lancz_sec, svd_sec, env_sec, tot_sec, matvec_flops;
   int64_t svd_sketch_total; /* randomized SVD: sum of sketch sizes (0: exact) */
   int64_t svd_grow_rounds;  /* randomized SVD: enlargements after a miss */
+  /* audit (svd_audit): |truncation error - exact SVD's| (-1: not audited)
+   * and the number of kept states that differ from the exact SVD's */
+  double svd_audit_err;
+  int64_t svd_audit_kept_diff;
 } udmrg_site_log;
 
 const char *udmrg_last_error(void);
@@ -183,6 +190,48 @@ int udmrg_two_site_finite_vmps(udmrg_ctx *ctx, int64_t N, udmrg_tensor **mps,
                                udmrg_tensor *const *mpo, const udmrg_sweep_params *params,
                                double *e0, udmrg_site_log *log, int64_t log_cap,
                                int64_t *log_len);
+
+/* ---- learned rank predictor (no counterpart in the reference) --------------- */
+/* Two-layer MLP (n_in = 70 features -> 128 ReLU -> 1) predicting, for one
+ * bond sector, y = log2(1 + kept states) from the sector's spectrum at the
+ * previous visit of its bond.  Features per sample: log10 of the leading 64
+ * singular values (floor 1e-20) / 10, the two QN components relative to the
+ * bond's dominant sector / 4, log10(trunc_err) / 10, log2(1 + previous
+ * kept) / 10, log10 of the bond's smallest kept singular value at the
+ * previous visit / 10, log2(Dmax / previous bond dimension).  FP32; trained
+ * and evaluated on the device.  The handle also holds the bond history
+ * (spectra and kept counts per bond) of the chain it last swept, kept across
+ * sweep calls until udmrg_rank_model_forget. */
+typedef struct udmrg_rank_model udmrg_rank_model;
+int udmrg_rank_model_sizes(int *n_in, int *n_hidden, int *n_params);
+int udmrg_rank_model_create(udmrg_ctx *ctx, uint64_t seed, udmrg_rank_model **out);
+int udmrg_rank_model_destroy(udmrg_rank_model *m);
+int udmrg_rank_model_forget(udmrg_rank_model *m);
+/* Parameters: W1 (hidden x in, row-major) | b1 | w2 | b2, n_params floats. */
+int udmrg_rank_model_get_params(udmrg_rank_model *m, float *params);
+int udmrg_rank_model_set_params(udmrg_rank_model *m, const float *params);
+int udmrg_rank_model_predict(udmrg_rank_model *m, int64_t n, const float *x, float *y);
+/* Mean squared error over n samples and its gradient (grad may be NULL). */
+int udmrg_rank_model_loss_grad(udmrg_rank_model *m, int64_t n, const float *x, const float *t,
+                               float *loss, float *grad);
+/* Adam on shuffled minibatches; returns the loss over all samples after training. */
+int udmrg_rank_model_train(udmrg_rank_model *m, int64_t n, const float *x, const float *t,
+                           int epochs, int batch, float lr, uint64_t seed, float *final_loss);
+/* TwoSiteFiniteVMPS with learned truncation: like udmrg_two_site_finite_vmps;
+ * with params->svd_mode == UDMRG_SVD_SKETCH_LEARNED the model sizes the
+ * randomized SVD's sketches of every bond it has seen before (exact SVD on a
+ * bond's first visit; a sector whose whole sketch is kept is a miss and is
+ * regrown, up to its full dimension, until the kept set is exact);
+ * with record != 0 the training samples of every update (features of each
+ * bond sector at its previous visit, label log2(1 + kept now)) are written to
+ * samples_x (cap x n_in) and samples_y (cap), their total number to
+ * *nsamples.  model may be NULL only without learning (plain sweep). */
+int udmrg_two_site_finite_vmps_learned(udmrg_ctx *ctx, int64_t N, udmrg_tensor **mps,
+                                       udmrg_tensor *const *mpo, const udmrg_sweep_params *params,
+                                       udmrg_rank_model *model, int record, float *samples_x,
+                                       float *samples_y, int64_t cap, int64_t *nsamples,
+                                       double *e0, udmrg_site_log *log, int64_t log_cap,
+                                       int64_t *log_len);
 
 /* ---- reusable matvec plan (repeated H_eff * psi on device buffers) -------- */
 /* The plan fixes {L, W_l, W_r, R} and the block structure closed under the

@@ -12,6 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libudmrg_gb300.so")
 
 c_double_p = C.POINTER(C.c_double)
+c_float_p = C.POINTER(C.c_float)
 c_int32_p = C.POINTER(C.c_int32)
 c_int64_p = C.POINTER(C.c_int64)
 c_void_pp = C.POINTER(C.c_void_p)
@@ -31,7 +32,8 @@ class LanczosRes(C.Structure):
 class SweepParams(C.Structure):
     _fields_ = [("sweeps", C.c_int64), ("Dmin", C.c_int64), ("Dmax", C.c_int64),
                 ("trunc_err", C.c_double), ("lancz_params", LanczosParams),
-                ("svd_mode", C.c_int64), ("svd_oversample", C.c_int64)]
+                ("svd_mode", C.c_int64), ("svd_oversample", C.c_int64),
+                ("svd_audit", C.c_int64)]
 
 
 class SiteLog(C.Structure):
@@ -39,7 +41,8 @@ class SiteLog(C.Structure):
                 ("D", C.c_int64), ("iters", C.c_int64), ("ee", C.c_double),
                 ("lancz_sec", C.c_double), ("svd_sec", C.c_double), ("env_sec", C.c_double),
                 ("tot_sec", C.c_double), ("matvec_flops", C.c_double),
-                ("svd_sketch_total", C.c_int64), ("svd_grow_rounds", C.c_int64)]
+                ("svd_sketch_total", C.c_int64), ("svd_grow_rounds", C.c_int64),
+                ("svd_audit_err", C.c_double), ("svd_audit_kept_diff", C.c_int64)]
 
 
 # name -> argtypes (all return int status)
@@ -84,6 +87,22 @@ SIGNATURES = {
     "udmrg_two_site_finite_vmps": [C.c_void_p, C.c_int64, c_void_pp, c_void_pp,
                                    C.POINTER(SweepParams), c_double_p, C.POINTER(SiteLog),
                                    C.c_int64, c_int64_p],
+    "udmrg_two_site_finite_vmps_learned": [C.c_void_p, C.c_int64, c_void_pp, c_void_pp,
+                                           C.POINTER(SweepParams), C.c_void_p, C.c_int,
+                                           c_float_p, c_float_p, C.c_int64, c_int64_p,
+                                           c_double_p, C.POINTER(SiteLog), C.c_int64,
+                                           c_int64_p],
+    "udmrg_rank_model_sizes": [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)],
+    "udmrg_rank_model_create": [C.c_void_p, C.c_uint64, c_void_pp],
+    "udmrg_rank_model_destroy": [C.c_void_p],
+    "udmrg_rank_model_forget": [C.c_void_p],
+    "udmrg_rank_model_get_params": [C.c_void_p, c_float_p],
+    "udmrg_rank_model_set_params": [C.c_void_p, c_float_p],
+    "udmrg_rank_model_predict": [C.c_void_p, C.c_int64, c_float_p, c_float_p],
+    "udmrg_rank_model_loss_grad": [C.c_void_p, C.c_int64, c_float_p, c_float_p, c_float_p,
+                                   c_float_p],
+    "udmrg_rank_model_train": [C.c_void_p, C.c_int64, c_float_p, c_float_p, C.c_int, C.c_int,
+                               C.c_float, C.c_uint64, c_float_p],
     "udmrg_matvec_plan_create": [C.c_void_p, c_void_pp, C.c_void_p, c_void_pp],
     "udmrg_matvec_plan_create_ex": [C.c_void_p, c_void_pp, C.c_void_p, C.c_int, c_void_pp],
     "udmrg_matvec_plan_info": [C.c_void_p, c_double_p, c_int64_p, c_int64_p],

@@ -287,7 +287,7 @@ def svd(ctx, t, ldims, ldiv, trunc_err, Dmin, Dmax, mode=SVD_FULL):
 
 
 def svd_randomized(ctx, t, ldims, ldiv, trunc_err, Dmin, Dmax, sketch, mode=SVD_FULL,
-                   oversample=8, power_iters=2, seed=1):
+                   oversample=8, power_iters=4, seed=1):
     """Sector-wise randomized SVD; ``sketch`` = [(bond QN tuple, sketch size), ...]."""
     xd, pd = _i32(list(ldiv))
     qns = [v for q, _ in sketch for v in q] or [0]
@@ -315,29 +315,143 @@ class FiniteVMPSSweepParams:
     precision: int = 0  # matvec precision: 0 FP64, 1 mixed (split-BF16 tensor cores)
     svd_mode: int = 0  # 0 exact, 1 randomized (previous sector dims), 2 randomized (learned)
     svd_oversample: int = 8
+    svd_audit: bool = False  # exact SVD judges every randomized one (untimed)
+
+
+def _sweep_params(params: FiniteVMPSSweepParams):
+    return _lib.SweepParams(params.sweeps, params.Dmin, params.Dmax, params.trunc_err,
+                            _lib.LanczosParams(params.lanczos_error,
+                                               params.lanczos_max_iterations, params.precision),
+                            params.svd_mode, params.svd_oversample, int(params.svd_audit))
+
+
+def _log_rows(log, n):
+    rows = []
+    for i in range(n):
+        L = log[i]
+        rows.append(dict(site=L.site, e0=L.e0, trunc_err=L.trunc_err, D=L.D, iters=L.iters,
+                         ee=L.ee, lancz_sec=L.lancz_sec, svd_sec=L.svd_sec, env_sec=L.env_sec,
+                         tot_sec=L.tot_sec, matvec_flops=L.matvec_flops,
+                         svd_sketch_total=L.svd_sketch_total,
+                         svd_grow_rounds=L.svd_grow_rounds, svd_audit_err=L.svd_audit_err,
+                         svd_audit_kept_diff=L.svd_audit_kept_diff))
+    return rows
 
 
 def two_site_finite_vmps(ctx, mps: List[DeviceTensor], mpo: List[DeviceTensor],
                          params: FiniteVMPSSweepParams):
     """``TwoSiteFiniteVMPS``: updates ``mps`` in place, returns (e0, per-site log)."""
     N = len(mps)
-    sp = _lib.SweepParams(params.sweeps, params.Dmin, params.Dmax, params.trunc_err,
-                          _lib.LanczosParams(params.lanczos_error, params.lanczos_max_iterations,
-                                             params.precision),
-                          params.svd_mode, params.svd_oversample)
+    sp = _sweep_params(params)
     cap = 2 * N * max(params.sweeps, 1)
     log = (_lib.SiteLog * cap)()
     e0 = C.c_double()
     nlog = C.c_int64()
     call("udmrg_two_site_finite_vmps", ctx.h, N, _handles(mps), _handles(mpo), C.byref(sp),
          C.byref(e0), log, cap, C.byref(nlog))
-    rows = []
-    for i in range(min(cap, nlog.value)):
-        L = log[i]
-        rows.append(dict(site=L.site, e0=L.e0, trunc_err=L.trunc_err, D=L.D, iters=L.iters,
-                         ee=L.ee, lancz_sec=L.lancz_sec, svd_sec=L.svd_sec, env_sec=L.env_sec,
-                         tot_sec=L.tot_sec, matvec_flops=L.matvec_flops))
-    return float(e0.value), rows
+    return float(e0.value), _log_rows(log, min(cap, nlog.value))
+
+
+class RankModel:
+    """The learned rank predictor (``udmrg_rank_model``): a 68-128-1 ReLU MLP
+    mapping a bond sector's previous spectrum to log2(1 + kept states) there."""
+
+    def __init__(self, ctx, seed: int = 0):
+        n_in, n_hid, n_par = C.c_int(), C.c_int(), C.c_int()
+        call("udmrg_rank_model_sizes", C.byref(n_in), C.byref(n_hid), C.byref(n_par))
+        self.n_in, self.n_hidden, self.n_params = n_in.value, n_hid.value, n_par.value
+        h = C.c_void_p()
+        call("udmrg_rank_model_create", ctx.h, int(seed), C.byref(h))
+        self.ctx, self.h = ctx, h
+
+    @staticmethod
+    def _f32(a):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        return a, a.ctypes.data_as(_lib.c_float_p)
+
+    @property
+    def params(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        call("udmrg_rank_model_get_params", self.h, out.ctypes.data_as(_lib.c_float_p))
+        return out
+
+    @params.setter
+    def params(self, p):
+        p, pp = self._f32(p)
+        if p.size != self.n_params:
+            raise ValueError(f"rank model: expected {self.n_params} parameters, got {p.size}")
+        call("udmrg_rank_model_set_params", self.h, pp)
+
+    def predict(self, x) -> np.ndarray:
+        x, xp = self._f32(x)
+        n = x.shape[0]
+        y = np.empty(n, np.float32)
+        call("udmrg_rank_model_predict", self.h, n, xp, y.ctypes.data_as(_lib.c_float_p))
+        return y
+
+    def loss_grad(self, x, t):
+        x, xp = self._f32(x)
+        t, tp = self._f32(t)
+        loss = C.c_float()
+        g = np.empty(self.n_params, np.float32)
+        call("udmrg_rank_model_loss_grad", self.h, x.shape[0], xp, tp, C.byref(loss),
+             g.ctypes.data_as(_lib.c_float_p))
+        return float(loss.value), g
+
+    def train(self, x, t, epochs=200, batch=256, lr=1e-3, seed=0) -> float:
+        x, xp = self._f32(x)
+        t, tp = self._f32(t)
+        loss = C.c_float()
+        call("udmrg_rank_model_train", self.h, x.shape[0], xp, tp, int(epochs), int(batch),
+             float(lr), int(seed), C.byref(loss))
+        return float(loss.value)
+
+    def forget(self):
+        """Drop the bond history of the last chain swept with this model."""
+        call("udmrg_rank_model_forget", self.h)
+
+    def close(self):
+        if self.h:
+            call("udmrg_rank_model_destroy", self.h)
+            self.h = None
+
+    def __del__(self):
+        if _lib.SHUTDOWN[0]:
+            return
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+def two_site_finite_vmps_learned(ctx, mps: List[DeviceTensor], mpo: List[DeviceTensor],
+                                 params: FiniteVMPSSweepParams,
+                                 model: Optional[RankModel] = None, record: bool = False,
+                                 cap: int = 1 << 16):
+    """``TwoSiteFiniteVMPS`` with learned truncation.  With ``svd_mode == 2``
+    the sketch size of every bond sector comes from ``model``; with ``record``
+    the sweep also returns training samples (features, log2(1 + kept)).
+    The model keeps each bond's last spectrum across calls (a schedule of
+    sweeps with growing Dmax); ``record`` needs a model (it may be untrained).
+    Returns (e0, per-site log, x, y)."""
+    N = len(mps)
+    sp = _sweep_params(params)
+    lcap = 2 * N * max(params.sweeps, 1)
+    log = (_lib.SiteLog * lcap)()
+    e0 = C.c_double()
+    nlog = C.c_int64()
+    n_in = C.c_int()
+    call("udmrg_rank_model_sizes", C.byref(n_in), None, None)
+    xs = np.zeros((cap if record else 0, n_in.value), np.float32)
+    ys = np.zeros(cap if record else 0, np.float32)
+    ns = C.c_int64()
+    call("udmrg_two_site_finite_vmps_learned", ctx.h, N, _handles(mps), _handles(mpo),
+         C.byref(sp), model.h if model is not None else None, int(record),
+         xs.ctypes.data_as(_lib.c_float_p) if record else None,
+         ys.ctypes.data_as(_lib.c_float_p) if record else None, cap if record else 0,
+         C.byref(ns), C.byref(e0), log, lcap, C.byref(nlog))
+    n = min(ns.value, xs.shape[0])
+    return float(e0.value), _log_rows(log, min(lcap, nlog.value)), xs[:n], ys[:n]
 
 
 def trivial_env_data(mps_ten: BlockTensorData, mpo_ten: BlockTensorData, side: str):
@@ -380,17 +494,13 @@ def build_envs(ctx, mpo: Sequence[BlockTensorData], mps: Sequence[BlockTensorDat
 def two_site_update(ctx, lenv, renv, mps_l, mps_r, mpo_l, mpo_r,
                     params: FiniteVMPSSweepParams, dir: str = "r"):
     """``TwoSiteFiniteVMPSUpdate`` on one bond: (new_l, new_r, new_env, log)."""
-    sp = _lib.SweepParams(1, params.Dmin, params.Dmax, params.trunc_err,
-                          _lib.LanczosParams(params.lanczos_error, params.lanczos_max_iterations,
-                                             params.precision),
-                          params.svd_mode, params.svd_oversample)
+    sp = _sweep_params(params)
+    sp.sweeps = 1
     a, b, e = C.c_void_p(), C.c_void_p(), C.c_void_p()
     lg = _lib.SiteLog()
     call("udmrg_two_site_update", ctx.h, lenv.h, renv.h, mps_l.h, mps_r.h, mpo_l.h, mpo_r.h,
          C.byref(sp), dir.encode(), C.byref(a), C.byref(b), C.byref(e), C.byref(lg))
-    log = dict(e0=lg.e0, trunc_err=lg.trunc_err, D=lg.D, iters=lg.iters, ee=lg.ee,
-               lancz_sec=lg.lancz_sec, svd_sec=lg.svd_sec, env_sec=lg.env_sec,
-               tot_sec=lg.tot_sec, matvec_flops=lg.matvec_flops)
+    log = _log_rows([lg], 1)[0]
     return _new(ctx, a), _new(ctx, b), _new(ctx, e), log
 
 

@@ -1,6 +1,8 @@
 // extern "C" boundary: plain pointers and sizes, status codes, no exceptions.
 #include <cmath>
+#include <algorithm>
 #include <cstring>
+#include <memory>
 
 #include "../../include/ultradmrg_gb300.h"
 #include "dmrg.hpp"
@@ -398,6 +400,13 @@ int udmrg_svd_randomized(udmrg_ctx *c, const udmrg_tensor *t, int ldims, const i
   });
 }
 
+static udmrg_site_log site_log(const SiteLog &s) {
+  return {s.site,    s.e0,      s.trunc_err, s.D,           s.iters,
+          s.ee,      s.lancz_sec, s.svd_sec, s.env_sec,     s.tot_sec,
+          s.matvec_flops, s.svd_sketch_total, s.svd_grow_rounds, s.svd_audit_err,
+          s.svd_audit_kept_diff};
+}
+
 int udmrg_two_site_update(udmrg_ctx *c, const udmrg_tensor *lenv, const udmrg_tensor *renv,
                           const udmrg_tensor *mps_l, const udmrg_tensor *mps_r,
                           const udmrg_tensor *mpo_l, const udmrg_tensor *mpo_r,
@@ -413,6 +422,7 @@ int udmrg_two_site_update(udmrg_ctx *c, const udmrg_tensor *lenv, const udmrg_te
                (int)params->lancz_params.matvec_precision};
     p.svd_mode = (int)params->svd_mode;
     p.svd_oversample = params->svd_oversample;
+    p.svd_audit = params->svd_audit != 0;
     SiteLog s{};
     auto r = two_site_update_local(c->ctx, T(lenv), T(renv), T(mps_l), T(mps_r), T(mpo_l),
                                    T(mpo_r), p, dir, &s);
@@ -420,8 +430,7 @@ int udmrg_two_site_update(udmrg_ctx *c, const udmrg_tensor *lenv, const udmrg_te
     *new_r = wrap(std::move(r.mps_r));
     *new_env = wrap(std::move(r.env));
     if (log)
-      *log = {s.site, s.e0, s.trunc_err, s.D, s.iters, s.ee,
-              s.lancz_sec, s.svd_sec, s.env_sec, s.tot_sec, s.matvec_flops, s.svd_sketch_total, s.svd_grow_rounds};
+      *log = site_log(s);
   });
 }
 
@@ -429,7 +438,152 @@ int udmrg_two_site_finite_vmps(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
                                udmrg_tensor *const *mpo, const udmrg_sweep_params *params,
                                double *e0, udmrg_site_log *log, int64_t log_cap,
                                int64_t *log_len) {
+  return udmrg_two_site_finite_vmps_learned(c, N, mps, mpo, params, nullptr, 0, nullptr, nullptr,
+                                            0, nullptr, e0, log, log_cap, log_len);
+}
+
+struct udmrg_rank_model {
+  Ctx *ctx;
+  std::unique_ptr<RankModel> m;
+  LearnState hist;  // bond spectra of the chain it last swept
+};
+
+int udmrg_rank_model_sizes(int *n_in, int *n_hidden, int *n_params) {
   return guarded([&] {
+    if (n_in) *n_in = kRankIn;
+    if (n_hidden) *n_hidden = kRankHidden;
+    if (n_params) *n_params = kRankParams;
+  });
+}
+
+int udmrg_rank_model_create(udmrg_ctx *c, uint64_t seed, udmrg_rank_model **out) {
+  return guarded([&] {
+    auto *m = new udmrg_rank_model;
+    m->ctx = &c->ctx;
+    m->m = std::make_unique<RankModel>(c->ctx, seed);
+    c->ctx.live_handles++;
+    *out = m;
+  });
+}
+
+int udmrg_rank_model_forget(udmrg_rank_model *m) {
+  return guarded([&] {
+    m->hist.prev.clear();
+    m->hist.prev_kept.clear();
+  });
+}
+
+int udmrg_rank_model_destroy(udmrg_rank_model *m) {
+  return guarded([&] {
+    if (!m) return;
+    Ctx *c = m->ctx;
+    delete m;
+    release_ctx(c);
+  });
+}
+
+int udmrg_rank_model_get_params(udmrg_rank_model *m, float *params) {
+  return guarded([&] {
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(params, m->m->params, kRankParams * sizeof(float),
+                                     cudaMemcpyDeviceToHost, m->ctx->stream));
+    m->ctx->sync();
+  });
+}
+
+int udmrg_rank_model_set_params(udmrg_rank_model *m, const float *params) {
+  return guarded([&] {
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(m->m->params, params, kRankParams * sizeof(float),
+                                     cudaMemcpyHostToDevice, m->ctx->stream));
+    m->ctx->sync();
+  });
+}
+
+int udmrg_rank_model_predict(udmrg_rank_model *m, int64_t n, const float *x, float *y) {
+  return guarded([&] {
+    Ctx &ctx = *m->ctx;
+    DeviceScratch s(ctx);
+    float *dx = s.get<float>(n * kRankIn), *dy = s.get<float>(n);
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(dx, x, n * kRankIn * sizeof(float), cudaMemcpyHostToDevice,
+                                     ctx.stream));
+    m->m->predict(dx, n, dy);
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(y, dy, n * sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.sync();
+  });
+}
+
+int udmrg_rank_model_loss_grad(udmrg_rank_model *m, int64_t n, const float *x, const float *t,
+                               float *loss, float *grad) {
+  return guarded([&] {
+    Ctx &ctx = *m->ctx;
+    DeviceScratch s(ctx);
+    float *dx = s.get<float>(n * kRankIn), *dt = s.get<float>(n);
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(dx, x, n * kRankIn * sizeof(float), cudaMemcpyHostToDevice,
+                                     ctx.stream));
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(dt, t, n * sizeof(float), cudaMemcpyHostToDevice, ctx.stream));
+    const float l = m->m->loss_grad(dx, dt, n);
+    if (loss) *loss = l;
+    if (grad) {
+      UDMRG_CHECK_CUDA(cudaMemcpyAsync(grad, m->m->grad, kRankParams * sizeof(float),
+                                       cudaMemcpyDeviceToHost, ctx.stream));
+      ctx.sync();
+    }
+  });
+}
+
+int udmrg_rank_model_train(udmrg_rank_model *m, int64_t n, const float *x, const float *t,
+                           int epochs, int batch, float lr, uint64_t seed, float *final_loss) {
+  return guarded([&] {
+    UDMRG_REQUIRE(n > 0 && batch > 0 && epochs >= 0, "rank model: bad training arguments");
+    Ctx &ctx = *m->ctx;
+    DeviceScratch s(ctx);
+    float *dx = s.get<float>(n * kRankIn), *dt = s.get<float>(n);
+    float *bx = s.get<float>((int64_t)batch * kRankIn), *bt = s.get<float>(batch);
+    // shuffled copies per epoch are assembled on the host (the data set is small)
+    std::vector<int64_t> ord(n);
+    for (int64_t i = 0; i < n; ++i) ord[i] = i;
+    uint64_t st = seed * 6364136223846793005ull + 1442695040888963407ull;
+    std::vector<float> hx((size_t)batch * kRankIn), ht(batch);
+    for (int e = 0; e < epochs; ++e) {
+      for (int64_t i = n - 1; i > 0; --i) {  // Fisher-Yates with an LCG
+        st = st * 6364136223846793005ull + 1442695040888963407ull;
+        std::swap(ord[i], ord[(int64_t)((st >> 33) % (uint64_t)(i + 1))]);
+      }
+      for (int64_t b0 = 0; b0 < n; b0 += batch) {
+        const int64_t nb = std::min<int64_t>(batch, n - b0);
+        for (int64_t i = 0; i < nb; ++i) {
+          std::memcpy(hx.data() + i * kRankIn, x + ord[b0 + i] * kRankIn, kRankIn * sizeof(float));
+          ht[i] = t[ord[b0 + i]];
+        }
+        UDMRG_CHECK_CUDA(cudaMemcpyAsync(bx, hx.data(), nb * kRankIn * sizeof(float),
+                                         cudaMemcpyHostToDevice, ctx.stream));
+        UDMRG_CHECK_CUDA(cudaMemcpyAsync(bt, ht.data(), nb * sizeof(float), cudaMemcpyHostToDevice,
+                                         ctx.stream));
+        m->m->loss_grad(bx, bt, nb);
+        m->m->adam(lr);
+      }
+    }
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(dx, x, n * kRankIn * sizeof(float), cudaMemcpyHostToDevice,
+                                     ctx.stream));
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(dt, t, n * sizeof(float), cudaMemcpyHostToDevice, ctx.stream));
+    const float l = m->m->loss_grad(dx, dt, n);
+    if (final_loss) *final_loss = l;
+  });
+}
+
+int udmrg_two_site_finite_vmps_learned(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
+                                       udmrg_tensor *const *mpo, const udmrg_sweep_params *params,
+                                       udmrg_rank_model *model, int record, float *samples_x,
+                                       float *samples_y, int64_t cap, int64_t *nsamples,
+                                       double *e0, udmrg_site_log *log, int64_t log_cap,
+                                       int64_t *log_len) {
+  return guarded([&] {
+    LearnState scratch_state;
+    LearnState &learn = model ? model->hist : scratch_state;
+    learn.model = model ? model->m.get() : nullptr;
+    learn.record = record != 0;
+    learn.x.clear();
+    learn.y.clear();
+    const bool use_learn = learn.model || learn.record;
     std::vector<TensorPtr> m(N);
     for (int64_t i = 0; i < N; ++i) m[i] = T(mps[i]).clone();
     std::vector<const BTensor *> w(N);
@@ -443,17 +597,22 @@ int udmrg_two_site_finite_vmps(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
                (int)params->lancz_params.matvec_precision};
     p.svd_mode = (int)params->svd_mode;
     p.svd_oversample = params->svd_oversample;
+    p.svd_audit = params->svd_audit != 0;
     std::vector<SiteLog> lg;
-    const double e = two_site_finite_vmps(c->ctx, m, w, p, &lg);
+    const double e = two_site_finite_vmps(c->ctx, m, w, p, &lg, use_learn ? &learn : nullptr);
     c->ctx.sync();
     for (int64_t i = 0; i < N; ++i) mps[i]->t = std::move(m[i]);
+    if (nsamples) *nsamples = (int64_t)learn.y.size();
+    if (samples_x && samples_y) {
+      const int64_t ns = std::min<int64_t>(cap, (int64_t)learn.y.size());
+      std::memcpy(samples_x, learn.x.data(), ns * kRankIn * sizeof(float));
+      std::memcpy(samples_y, learn.y.data(), ns * sizeof(float));
+    }
     if (e0) *e0 = e;
     if (log_len) *log_len = (int64_t)lg.size();
     if (log)
       for (int64_t i = 0; i < std::min<int64_t>(log_cap, (int64_t)lg.size()); ++i) {
-        const SiteLog &s = lg[i];
-        log[i] = {s.site, s.e0, s.trunc_err, s.D, s.iters, s.ee,
-                  s.lancz_sec, s.svd_sec, s.env_sec, s.tot_sec, s.matvec_flops, s.svd_sketch_total, s.svd_grow_rounds};
+        log[i] = site_log(lg[i]);
       }
   });
 }

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <map>
 
 namespace udmrg {
 
@@ -557,7 +558,8 @@ static double now() {
 static double two_site_update(Ctx &ctx, std::vector<TensorPtr> &mps,
                               std::vector<TensorPtr> &lenvs, std::vector<TensorPtr> &renvs,
                               const std::vector<const BTensor *> &mpo, const SweepParams &p,
-                              char dir, int64_t target, std::vector<SiteLog> *log) {
+                              char dir, int64_t target, std::vector<SiteLog> *log,
+                              LearnState *learn) {
   const int64_t N = (int64_t)mps.size();
   int64_t l, r, lenv_len, renv_len;
   if (dir == 'r') {
@@ -572,9 +574,84 @@ static double two_site_update(Ctx &ctx, std::vector<TensorPtr> &mps,
     renv_len = N - target - 1;
   }
   SiteLog lg{};
+  // learned sketch sizes from the spectra this bond had at its previous visit
+  SketchHint hint;
+  const SketchHint *hp = nullptr;
+  BondSpectra now;
+  BondSpectra *prev = learn ? &learn->prev[l] : nullptr;
+  std::vector<float> feats;
+  std::vector<QN> fqn;
+  if (prev && !prev->empty()) {
+    // dominant sector of the previous spectrum and previous kept counts
+    QN top = (*prev)[0].first;
+    double best = -1;
+    for (auto &kv : *prev)
+      if (!kv.second.empty() && kv.second[0] > best) {
+        best = kv.second[0];
+        top = kv.first;
+      }
+    const auto &kept_prev = learn->prev_kept[l];
+    auto kept_of = [&](const QN &q) {
+      for (auto &kk : kept_prev)
+        if (kk.first == q) return kk.second;
+      return (int64_t)0;
+    };
+    // the bond's previous cutoff (smallest kept value) and dimension
+    double cut = 0.0;
+    int64_t dprev = 0;
+    for (auto &kv : *prev) {
+      const int64_t k = kept_of(kv.first);
+      dprev += k;
+      if (k > 0 && k <= (int64_t)kv.second.size())
+        cut = cut == 0.0 ? kv.second[k - 1] : std::min(cut, kv.second[k - 1]);
+    }
+    const double growth = std::log2((double)std::max<int64_t>(p.Dmax, 1) /
+                                    (double)std::max<int64_t>(dprev, 1));
+    for (auto &kv : *prev) {
+      feats.resize(feats.size() + kRankIn);
+      rank_features(kv.second, kv.first, top, p.trunc_err, kept_of(kv.first), cut, growth,
+                    feats.data() + feats.size() - kRankIn);
+      fqn.push_back(kv.first);
+    }
+    if (learn->model && p.svd_mode == kSvdSketchLearned) {
+      const int64_t n = (int64_t)fqn.size();
+      DeviceScratch s(ctx);
+      float *dx = s.get<float>(feats.size()), *dy = s.get<float>(n);
+      UDMRG_CHECK_CUDA(cudaMemcpyAsync(dx, feats.data(), feats.size() * sizeof(float),
+                                       cudaMemcpyHostToDevice, ctx.stream));
+      learn->model->predict(dx, n, dy);
+      std::vector<float> y(n);
+      UDMRG_CHECK_CUDA(
+          cudaMemcpyAsync(y.data(), dy, n * sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
+      ctx.sync();
+      for (int64_t i = 0; i < n; ++i) {
+        const double k = std::max(0.0, std::ceil(std::exp2((double)y[i]) - 1.0));
+        hint.push_back({fqn[i], (int64_t)k});
+      }
+      hp = &hint;
+    }
+  }
   auto res = two_site_update_local(ctx, *lenvs[lenv_len], *renvs[renv_len], *mps[l], *mps[r],
-                                   *mpo[l], *mpo[r], p, dir, &lg);
+                                   *mpo[l], *mpo[r], p, dir, &lg, hp, learn ? &now : nullptr);
   lg.site = target;
+  if (learn) {
+    // kept counts of this update per bond QN = the new bond index of mps[l]
+    std::vector<std::pair<QN, int64_t>> kept_now;
+    const Index &bond = res.mps_l->idx[2];
+    for (int q = 0; q < bond.nsec(); ++q) kept_now.push_back({bond.qns[q], bond.dims[q]});
+    if (learn->record) {
+      for (size_t i = 0; i < fqn.size(); ++i) {
+        int64_t k = 0;
+        for (auto &kk : kept_now)
+          if (kk.first == fqn[i]) k = kk.second;
+        learn->x.insert(learn->x.end(), feats.begin() + i * kRankIn,
+                        feats.begin() + (i + 1) * kRankIn);
+        learn->y.push_back((float)std::log2(1.0 + (double)k));
+      }
+    }
+    learn->prev[l] = std::move(now);
+    learn->prev_kept[l] = std::move(kept_now);
+  }
   mps[l] = std::move(res.mps_l);
   mps[r] = std::move(res.mps_r);
   if (dir == 'r')
@@ -602,6 +679,8 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
   const QN ldiv = mps_l.div();
   const int split = dir == 'r' ? kSvdSplitLeft : kSvdSplitRight;
   SvdResult sres;
+  double audit_err = -1.0, audit_sec = 0.0;
+  int64_t audit_diff = 0;
   if (p.svd_mode == kSvdExact || (p.svd_mode == kSvdSketchLearned && !hint)) {
     sres = svd_trunc(ctx, *lres.gs_vec, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split);
   } else {
@@ -615,6 +694,21 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
       for (int q = 0; q < bond.nsec(); ++q) sp.sketch.push_back({bond.qns[q], bond.dims[q]});
     }
     sres = svd_trunc_sketch(ctx, *lres.gs_vec, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split, sp);
+    if (p.svd_audit) {  // the exact block SVD judges the randomized one
+      const double ta = now();
+      SvdResult ex = svd_trunc(ctx, *lres.gs_vec, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split);
+      audit_err = std::fabs(ex.trunc_err - sres.trunc_err);
+      std::map<QN, int64_t> kx;
+      for (size_t q = 0; q < ex.sector_qn.size(); ++q) kx[ex.sector_qn[q]] = ex.sector_kept[q];
+      for (size_t q = 0; q < sres.sector_qn.size(); ++q) {
+        auto it = kx.find(sres.sector_qn[q]);
+        const int64_t k = it == kx.end() ? 0 : it->second;
+        audit_diff += std::llabs(k - sres.sector_kept[q]);
+        if (it != kx.end()) kx.erase(it);
+      }
+      for (auto &kv : kx) audit_diff += kv.second;
+      audit_sec = now() - ta;
+    }
   }
   lres.gs_vec.reset();
   if (spectra) {
@@ -638,14 +732,15 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
     for (int64_t v : sres.sector_sketch) sk += v;
     if (log)
       *log = {0, lres.gs_eng, sres.trunc_err, sres.D, lres.iters, sres.ee, t1 - t0,
-              t2 - t1, t3 - t2, t3 - t0, mvflops, sk, sres.grow_rounds};
+              t2 - t1 - audit_sec, t3 - t2, t3 - t0 - audit_sec, mvflops, sk, sres.grow_rounds,
+              audit_err, audit_diff};
   }
   return out;
 }
 
 double two_site_finite_vmps(Ctx &ctx, std::vector<TensorPtr> &mps,
                             const std::vector<const BTensor *> &mpo, const SweepParams &p,
-                            std::vector<SiteLog> *log) {
+                            std::vector<SiteLog> *log, LearnState *learn) {
   const int64_t N = (int64_t)mps.size();
   UDMRG_REQUIRE(N >= 3 && (int64_t)mpo.size() == N, "vmps: MPS and MPO sizes differ or N < 3");
   // mixed element types: promote real MPO / MPS to complex
@@ -669,9 +764,15 @@ double two_site_finite_vmps(Ctx &ctx, std::vector<TensorPtr> &mps,
     renvs[i] = update_site_renv(ctx, *renvs[i - 1], *mps[N - i], *W[N - i]);
   lenvs[0] = trivial_lenv(ctx, *mps[0], *W[0]);
   double e0 = 0;
+  if (learn && (int64_t)learn->prev.size() != N) {  // history is kept across calls
+    learn->prev.assign(N, {});
+    learn->prev_kept.assign(N, {});
+  }
   for (int64_t s = 0; s < p.sweeps; ++s) {
-    for (int64_t i = 0; i < N - 2; ++i) e0 = two_site_update(ctx, mps, lenvs, renvs, W, p, 'r', i, log);
-    for (int64_t i = N - 1; i > 1; --i) e0 = two_site_update(ctx, mps, lenvs, renvs, W, p, 'l', i, log);
+    for (int64_t i = 0; i < N - 2; ++i)
+      e0 = two_site_update(ctx, mps, lenvs, renvs, W, p, 'r', i, log, learn);
+    for (int64_t i = N - 1; i > 1; --i)
+      e0 = two_site_update(ctx, mps, lenvs, renvs, W, p, 'l', i, log, learn);
   }
   return e0;
 }

@@ -1,6 +1,7 @@
 // Two-site update: matvec plan, Lanczos solvers, environment updates, sweeps.
 #pragma once
 
+#include "rank_mlp.hpp"
 #include "sg_matvec.hpp"
 #include "svd.hpp"
 
@@ -101,6 +102,7 @@ struct SweepParams {
   LanczosParams lancz;
   int svd_mode = kSvdExact;
   int64_t svd_oversample = 8;
+  bool svd_audit = false;  // judge every randomized SVD by the exact one
 };
 
 struct SiteLog {
@@ -111,6 +113,8 @@ struct SiteLog {
   double matvec_flops;
   int64_t svd_sketch_total;  // sum of the final sketch sizes (0: exact SVD)
   int64_t svd_grow_rounds;   // sketch enlargements after a miss
+  double svd_audit_err;      // |trunc_err - exact SVD's| (-1: not audited)
+  int64_t svd_audit_kept_diff;  // kept states differing from the exact SVD's
 };
 
 // Sketch sizes of the randomized SVD per bond QN.
@@ -133,10 +137,24 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
                                   const SketchHint *hint = nullptr,
                                   BondSpectra *spectra = nullptr);
 
+// Learned truncation state: the rank model (used when svd_mode ==
+// kSvdSketchLearned), the spectra and kept counts of every bond at its last
+// visit (kept across sweep calls on the same chain, so a schedule of sweeps
+// with growing Dmax keeps its history), and (when record) training samples:
+// features of each bond sector from the previous visit and the label
+// log2(1 + kept now).
+struct LearnState {
+  RankModel *model = nullptr;
+  bool record = false;
+  std::vector<BondSpectra> prev;
+  std::vector<std::vector<std::pair<QN, int64_t>>> prev_kept;
+  std::vector<float> x, y;
+};
+
 // TwoSiteFiniteVMPS (two_site_update_finite_vmps_impl.h:95-494), device
 // resident: mps tensors are replaced in place; returns the last energy.
 double two_site_finite_vmps(Ctx &ctx, std::vector<TensorPtr> &mps,
                             const std::vector<const BTensor *> &mpo, const SweepParams &p,
-                            std::vector<SiteLog> *log);
+                            std::vector<SiteLog> *log, LearnState *learn = nullptr);
 
 }  // namespace udmrg

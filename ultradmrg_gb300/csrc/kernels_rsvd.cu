@@ -83,7 +83,35 @@ __global__ void chol_inv_kernel(const EigJob *__restrict__ jobs, double *__restr
   }
 }
 
+// Sum of squares of every column of row-major rows x cols matrices (one CTA
+// per matrix, consecutive threads on consecutive columns).
+__global__ void col_sumsq_kernel(const ScaleJob *__restrict__ jobs, const double *__restrict__ X,
+                                 double *__restrict__ out) {
+  const ScaleJob jb = jobs[blockIdx.x];
+  for (int j = threadIdx.x; j < jb.cols; j += blockDim.x) {
+    double acc = 0.0;
+    const double *x = X + jb.x_off + j;
+    for (int i = 0; i < jb.rows; ++i) {
+      const double v = x[(int64_t)i * jb.cols];
+      acc = fma(v, v, acc);
+    }
+    out[jb.f_off + j] = acc;
+  }
+}
+
 }  // namespace
+
+void run_col_sumsq(Ctx &ctx, const std::vector<ScaleJob> &jobs, const double *X, double *out) {
+  if (jobs.empty()) return;
+  ScaleJob *d = (ScaleJob *)ctx.alloc(jobs.size() * sizeof(ScaleJob));
+  UDMRG_CHECK_CUDA(cudaMemcpyAsync(d, jobs.data(), jobs.size() * sizeof(ScaleJob),
+                                   cudaMemcpyHostToDevice, ctx.stream));
+  col_sumsq_kernel<<<(int)jobs.size(), 128, 0, ctx.stream>>>(d, X, out);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  ctx.launches++;
+  ctx.sync();
+  ctx.free(d);
+}
 
 void fill_normal(Ctx &ctx, double *x, int64_t n, uint64_t seed) {
   if (n == 0) return;

@@ -54,12 +54,63 @@ __global__ void jacobi_eig_kernel(const EigJob *__restrict__ jobs, double *__res
   if (job.smem)
     for (int64_t e = tid; e < (int64_t)n * n; e += nt) G[e] = G_all[job.g_off + e];
   for (int64_t e = tid; e < (int64_t)n * n; e += nt) V[e] = (e / n == e % n) ? 1.0 : 0.0;
+  // scale to unit max-abs, so the stopping test below cannot underflow for a
+  // sector of tiny weight; non-finite input is reported, not iterated on
+  __shared__ double gscale;
+  __shared__ int nonfinite;
+  {
+    double mx = 0.0;
+    int bad = 0;
+    for (int64_t e = tid; e < (int64_t)n * n; e += nt) {
+      const double g = G[e];
+      bad |= !isfinite(g);
+      mx = fmax(mx, fabs(g));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+      bad |= __shfl_down_sync(0xffffffffu, bad, o);
+    }
+    if (tid == 0) nonfinite = 0;
+    __syncthreads();
+    if ((tid & 31) == 0) {
+      red[tid >> 5] = mx;
+      if (bad) atomicOr(&nonfinite, 1);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double m = 0.0;
+      for (int w = 0; w < (nt + 31) / 32; ++w) m = fmax(m, red[w]);
+      gscale = m;
+    }
+    __syncthreads();
+  }
+  if (nonfinite) {
+    if (tid == 0) atomicExch(status, 2);
+    return;
+  }
+  const double gs = gscale;
+  if (gs > 0.0 && gs != 1.0) {
+    const double inv = 1.0 / gs;
+    for (int64_t e = tid; e < (int64_t)n * n; e += nt) G[e] *= inv;
+  }
   __syncthreads();
 
   const int npad = n + (n & 1);
   const int npairs = npad / 2;
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
+    // re-symmetrise: the input Gram matrix and the parallel rotations are
+    // symmetric only up to rounding, and rotations preserve the norm of an
+    // antisymmetric part, which would otherwise floor the off-diagonal norm
+    for (int64_t e = tid; e < (int64_t)n * n; e += nt) {
+      const int i = (int)(e / n), j = (int)(e % n);
+      if (i < j) {
+        const double v = 0.5 * (G[(int64_t)i * n + j] + G[(int64_t)j * n + i]);
+        G[(int64_t)i * n + j] = v;
+        G[(int64_t)j * n + i] = v;
+      }
+    }
+    __syncthreads();
     // convergence: off-diagonal norm vs diagonal norm
     double off = 0.0, dia = 0.0;
     for (int64_t e = tid; e < (int64_t)n * n; e += nt) {
@@ -150,7 +201,7 @@ __global__ void jacobi_eig_kernel(const EigJob *__restrict__ jobs, double *__res
       __syncthreads();
     }
   }
-  if (tid == 0 && sweep >= max_sweeps) atomicExch(status, 1);
+  if (tid == 0 && sweep >= max_sweeps) atomicCAS(status, 0, 1);
   // sort eigenvalues descending (rank by counting; ties by index), permute V
   for (int i = tid; i < n; i += nt) {
     const double li = G[(int64_t)i * n + i];
@@ -159,7 +210,7 @@ __global__ void jacobi_eig_kernel(const EigJob *__restrict__ jobs, double *__res
       const double lj = G[(int64_t)j * n + j];
       if (lj > li || (lj == li && j < i)) ++rank;
     }
-    lam_all[job.lam_off + rank] = li;
+    lam_all[job.lam_off + rank] = li * gs;
     // column i of V -> column rank of the output
     for (int k = 0; k < n; ++k) V_all[job.g_off + (int64_t)k * n + rank] = V[(int64_t)k * n + i];
   }

@@ -341,6 +341,12 @@ void build_outputs(Ctx &ctx, DeviceScratch &scratch, const BTensor &T, int ldims
   }
 }
 
+// throws on a failed eigensolve (1: no convergence, 2: non-finite input)
+void check_eig_status(int st) {
+  if (st == 2) throw Error(kErrNumerics, "svd: non-finite values in the matrix to decompose");
+  if (st != 0) throw Error(kErrNumerics, "svd: Jacobi eigensolver did not converge");
+}
+
 std::vector<double> download_vec(Ctx &ctx, const double *d, int64_t n) {
   std::vector<double> h(n);
   if (n)
@@ -389,8 +395,7 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
     gemm_finalize(g);
     run_gemm(ctx, g, kF64, Mbuf, Mbuf, G, 1.0, 0.0);
   }
-  const int st = run_jacobi_eig(ctx, jobs, G, V, W, lam);
-  if (st != 0) throw Error(kErrNumerics, "svd: Jacobi eigensolver did not converge");
+  check_eig_status(run_jacobi_eig(ctx, jobs, G, V, W, lam));
   const std::vector<double> hlam = download_vec(ctx, lam, ltot);
   std::vector<std::vector<double>> sv(nsec);
   for (int q = 0; q < nsec; ++q) {
@@ -433,98 +438,112 @@ SvdResult svd_trunc_sketch(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv
   }
   std::map<QN, int64_t> req;
   for (auto &kv : sp.sketch) req[kv.first] = kv.second;
-  std::vector<int64_t> s(nsec);
+  std::vector<int64_t> s(nsec), full(nsec);
   for (int q = 0; q < nsec; ++q) {
-    const int64_t full = std::min(secs[q].rows, secs[q].cols);
+    full[q] = std::min(secs[q].rows, secs[q].cols);
     auto it = req.find(secs[q].qn);
-    const int64_t want = it == req.end() ? full : it->second + sp.oversample;
-    s[q] = std::max<int64_t>(1, std::min(full, want));
+    const int64_t want = it == req.end() ? full[q] : it->second + sp.oversample;
+    s[q] = std::max<int64_t>(1, std::min(full[q], want));
   }
-  SvdResult res;
-  for (int round = 0;; ++round) {
+  // isometric factor of sector q (xr x s_q, row-major) kept at uoff[q] across
+  // rounds; a round recomputes only the sectors that missed
+  std::vector<int64_t> uoff(nsec);
+  int64_t utot = 0;
+  for (int q = 0; q < nsec; ++q) {
+    uoff[q] = utot;
+    utot += xview(secs[q], left).xr * full[q];
+  }
+  double *Ubuf = scratch.get<double>(std::max<int64_t>(utot, 1));
+  std::vector<std::vector<double>> sv(nsec), r2(nsec);
+  std::vector<char> need(nsec, 1);
+
+  // One sketch round over the sectors `act`: Gaussian sketch, power iterations
+  // with Cholesky-QR, Rayleigh-Ritz (Gram of B = Q^T X, Jacobi), the isometric
+  // factor U = Q W into Ubuf, Ritz values into sv and residual norms
+  // ||X X^T u_i - theta_i u_i||^2 into r2.
+  auto sketch_round = [&](const std::vector<int> &act, int round) {
+    const int na = (int)act.size();
     DeviceScratch rs(ctx);
-    // buffers: Y (xr x s), Z (xc x s), Omega (xc x s), S/Rinv (s x s)
-    std::vector<int64_t> yoff(nsec), zoff(nsec), soff(nsec);
-    int64_t ytot = 0, ztot = 0, stot = 0;
-    for (int q = 0; q < nsec; ++q) {
+    std::vector<int64_t> yoff(na), zoff(na), soff(na);
+    int64_t ytot = 0, ztot = 0, stot = 0, ltot = 0;
+    std::vector<EigJob> jobs(na);
+    for (int a = 0; a < na; ++a) {
+      const int q = act[a];
       const XView x = xview(secs[q], left);
-      yoff[q] = ytot;
-      zoff[q] = ztot;
-      soff[q] = stot;
+      yoff[a] = ytot;
+      zoff[a] = ztot;
+      soff[a] = stot;
       ytot += x.xr * s[q];
       ztot += x.xc * s[q];
       stot += s[q] * s[q];
+      jobs[a].g_off = soff[a];
+      jobs[a].lam_off = ltot;
+      jobs[a].n = (int32_t)s[q];
+      ltot += s[q];
     }
     double *Y = rs.get<double>(ytot), *Y2 = rs.get<double>(ytot);
     double *Z = rs.get<double>(ztot), *Z2 = rs.get<double>(ztot);
     double *Sg = rs.get<double>(stot), *Ri = rs.get<double>(stot);
     double *Vv = rs.get<double>(stot), *Wk = rs.get<double>(stot);
-    double *lam = rs.get<double>(std::max<int64_t>(1, [&] {
-      int64_t t = 0;
-      for (int q = 0; q < nsec; ++q) t += s[q];
-      return t;
-    }()));
-    std::vector<EigJob> jobs(nsec);
-    {
-      int64_t lt = 0;
-      for (int q = 0; q < nsec; ++q) {
-        jobs[q].g_off = soff[q];
-        jobs[q].lam_off = lt;
-        jobs[q].n = (int32_t)s[q];
-        lt += s[q];
-      }
-    }
+    double *lam = rs.get<double>(std::max<int64_t>(1, ltot));
     // Z <- Omega (xc x s), Y <- X Z
     fill_normal(ctx, Z, ztot, sp.seed * 0x9E3779B97F4A7C15ull + (uint64_t)round);
-    auto mult_xz = [&](const double *zin, double *yout) {  // Y = X Z
+    auto mult_xz = [&](const double *zin, double *yout, double beta) {  // Y = X Z (+ beta Y)
       GemmPlan g;
       g.ctx = &ctx;
-      for (int q = 0; q < nsec; ++q) {
-        const XView x = xview(secs[q], left);
-        gemm_add_simple(g, yoff[q], x.xr, s[q], x.xc, x.off, x.sr, x.sc, zoff[q], s[q], 1, false);
+      for (int a = 0; a < na; ++a) {
+        const XView x = xview(secs[act[a]], left);
+        const int64_t sq = s[act[a]];
+        gemm_add_simple(g, yoff[a], x.xr, sq, x.xc, x.off, x.sr, x.sc, zoff[a], sq, 1, false);
       }
       gemm_finalize(g);
-      run_gemm(ctx, g, kF64, Mbuf, zin, yout, 1.0, 0.0);
+      run_gemm(ctx, g, kF64, Mbuf, zin, yout, 1.0, beta);
     };
     auto mult_xty = [&](const double *yin, double *zout) {  // Z = X^T Y
       GemmPlan g;
       g.ctx = &ctx;
-      for (int q = 0; q < nsec; ++q) {
-        const XView x = xview(secs[q], left);
-        gemm_add_simple(g, zoff[q], x.xc, s[q], x.xr, x.off, x.sc, x.sr, yoff[q], s[q], 1, false);
+      for (int a = 0; a < na; ++a) {
+        const XView x = xview(secs[act[a]], left);
+        const int64_t sq = s[act[a]];
+        gemm_add_simple(g, zoff[a], x.xc, sq, x.xr, x.off, x.sc, x.sr, yoff[a], sq, 1, false);
       }
       gemm_finalize(g);
       run_gemm(ctx, g, kF64, Mbuf, yin, zout, 1.0, 0.0);
+    };
+    // small per-sector products: out(rows x s) = in(rows x s) * S(s x s)
+    auto mult_small = [&](const double *in, const double *S, double *out,
+                          const std::vector<int64_t> &off, bool on_y) {
+      GemmPlan h;
+      h.ctx = &ctx;
+      for (int a = 0; a < na; ++a) {
+        const XView x = xview(secs[act[a]], left);
+        const int64_t rows = on_y ? x.xr : x.xc, sq = s[act[a]];
+        gemm_add_simple(h, off[a], rows, sq, sq, off[a], sq, 1, soff[a], sq, 1, false);
+      }
+      gemm_finalize(h);
+      run_gemm(ctx, h, kF64, in, S, out, 1.0, 0.0);
     };
     // Cholesky-QR of the columns of B (rows x s per sector): out = B R^{-1}
     auto cholqr = [&](const double *bin, double *bout, const std::vector<int64_t> &boff,
                       bool on_y) {
       GemmPlan g;
       g.ctx = &ctx;
-      for (int q = 0; q < nsec; ++q) {
-        const XView x = xview(secs[q], left);
-        const int64_t rows = on_y ? x.xr : x.xc;
-        gemm_add_simple(g, soff[q], s[q], s[q], rows, boff[q], 1, s[q], boff[q], s[q], 1, false);
+      for (int a = 0; a < na; ++a) {
+        const XView x = xview(secs[act[a]], left);
+        const int64_t rows = on_y ? x.xr : x.xc, sq = s[act[a]];
+        gemm_add_simple(g, soff[a], sq, sq, rows, boff[a], 1, sq, boff[a], sq, 1, false);
       }
       gemm_finalize(g);
       run_gemm(ctx, g, kF64, bin, bin, Sg, 1.0, 0.0);
       run_chol_inv(ctx, jobs, Sg, Ri, 1e-28);
-      GemmPlan h;
-      h.ctx = &ctx;
-      for (int q = 0; q < nsec; ++q) {
-        const XView x = xview(secs[q], left);
-        const int64_t rows = on_y ? x.xr : x.xc;
-        gemm_add_simple(h, boff[q], rows, s[q], s[q], boff[q], s[q], 1, soff[q], s[q], 1, false);
-      }
-      gemm_finalize(h);
-      run_gemm(ctx, h, kF64, bin, Ri, bout, 1.0, 0.0);
+      mult_small(bin, Ri, bout, boff, on_y);
     };
-    mult_xz(Z, Y);
+    mult_xz(Z, Y, 0.0);
     for (int it = 0; it < sp.power_iters; ++it) {
       cholqr(Y, Y2, yoff, true);
       mult_xty(Y2, Z);
       cholqr(Z, Z2, zoff, false);
-      mult_xz(Z2, Y);
+      mult_xz(Z2, Y, 0.0);
     }
     cholqr(Y, Y2, yoff, true);
     cholqr(Y2, Y, yoff, true);  // second pass: Q = Y (orthonormal to FP64 accuracy)
@@ -533,62 +552,115 @@ SvdResult svd_trunc_sketch(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv
     {
       GemmPlan g;
       g.ctx = &ctx;
-      for (int q = 0; q < nsec; ++q) {
-        const XView x = xview(secs[q], left);
-        gemm_add_simple(g, soff[q], s[q], s[q], x.xc, zoff[q], 1, s[q], zoff[q], s[q], 1, false);
+      for (int a = 0; a < na; ++a) {
+        const XView x = xview(secs[act[a]], left);
+        const int64_t sq = s[act[a]];
+        gemm_add_simple(g, soff[a], sq, sq, x.xc, zoff[a], 1, sq, zoff[a], sq, 1, false);
       }
       gemm_finalize(g);
       run_gemm(ctx, g, kF64, Z, Z, Sg, 1.0, 0.0);
     }
-    const int st = run_jacobi_eig(ctx, jobs, Sg, Vv, Wk, lam);
-    if (st != 0) throw Error(kErrNumerics, "svd: Jacobi eigensolver did not converge");
-    // isometric factor U = Q W (xr x s), written into Y2
-    {
-      GemmPlan g;
-      g.ctx = &ctx;
-      for (int q = 0; q < nsec; ++q) {
-        const XView x = xview(secs[q], left);
-        gemm_add_simple(g, yoff[q], x.xr, s[q], s[q], yoff[q], s[q], 1, soff[q], s[q], 1, false);
-      }
-      gemm_finalize(g);
-      run_gemm(ctx, g, kF64, Y, Vv, Y2, 1.0, 0.0);
+    check_eig_status(run_jacobi_eig(ctx, jobs, Sg, Vv, Wk, lam));
+    mult_small(Y, Vv, Y2, yoff, true);   // U = Q W (xr x s)
+    mult_small(Z, Vv, Z2, zoff, false);  // P = X^T U = Z W (xc x s)
+    // residuals: Y := X P - U Theta (Q in Y is no longer needed), column norms
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(Y, Y2, ytot * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     ctx.stream));
+    std::vector<ScaleJob> sj(na);
+    for (int a = 0; a < na; ++a) {
+      const XView x = xview(secs[act[a]], left);
+      sj[a] = ScaleJob{yoff[a], jobs[a].lam_off, (int32_t)x.xr, (int32_t)s[act[a]], 0, 0};
     }
-    int64_t ltot = 0;
-    for (int q = 0; q < nsec; ++q) ltot += s[q];
+    run_scale(ctx, sj, Y, lam, false);
+    mult_xz(Z2, Y, -1.0);
+    run_col_sumsq(ctx, sj, Y, Wk);  // ||r_i||^2 at lam_off (Wk holds >= ltot doubles)
+    // keep U of these sectors
+    for (int a = 0; a < na; ++a) {
+      const int q = act[a];
+      UDMRG_CHECK_CUDA(cudaMemcpyAsync(Ubuf + uoff[q], Y2 + yoff[a],
+                                       xview(secs[q], left).xr * s[q] * sizeof(double),
+                                       cudaMemcpyDeviceToDevice, ctx.stream));
+    }
+    const std::vector<double> hr = download_vec(ctx, Wk, ltot);
     const std::vector<double> hl = download_vec(ctx, lam, ltot);
-    std::vector<std::vector<double>> sv(nsec);
+    for (int a = 0; a < na; ++a) {
+      const int q = act[a];
+      sv[q].assign(s[q], 0.0);
+      r2[q].assign(s[q], 0.0);
+      for (int64_t i = 0; i < s[q]; ++i) {
+        sv[q][i] = std::sqrt(std::max(hl[jobs[a].lam_off + i], 0.0));
+        r2[q][i] = std::max(hr[jobs[a].lam_off + i], 0.0);
+      }
+    }
+  };
+
+  SvdResult res;
+  for (int round = 0;; ++round) {
+    std::vector<int> act;
+    for (int q = 0; q < nsec; ++q)
+      if (need[q]) act.push_back(q);
+    if (!act.empty()) sketch_round(act, round);
+    // selection over the Ritz values of all sectors; the weight outside them
+    // (exact norms minus Ritz values) counts as discarded
     double resid = 0.0;
     for (int q = 0; q < nsec; ++q) {
       double got = 0.0;
-      for (int64_t i = 0; i < s[q]; ++i) {
-        const double l = std::max(hl[jobs[q].lam_off + i], 0.0);
-        sv[q].push_back(std::sqrt(l));
-        got += l;
-      }
+      for (double v : sv[q]) got += v * v;
       resid += std::max(fro[q] - got, 0.0);
     }
     std::vector<int64_t> kept;
     SvdResult trial;
     select_kept(sv, trunc_err, Dmin, Dmax, kept, trial.D, trial.trunc_err, 1e-12, resid);
-    // misses: a sector whose whole sketch is kept, while it could hold more
+    // Misses: a sector whose whole sketch is kept, or whose Ritz values are
+    // not accurate enough to certify the kept set.  Error of Ritz value i:
+    // ||r_i||^2 / (theta_i - theta_last) (the gap to the unresolved part of
+    // the spectrum), and ||r_last|| for the last one.  Certified when (a) the
+    // kept values of all sectors are accurate to 1e-11 of the total weight and
+    // (b) no discarded Ritz value can reach the cutoff c (the smallest kept
+    // theta) beyond the tie tolerance of the selection rule.
+    double ftot = 0.0, tmax = 0.0, cut = -1.0;
+    for (int q = 0; q < nsec; ++q) {
+      ftot += fro[q];
+      for (int64_t i = 0; i < s[q]; ++i) {
+        const double th = sv[q][i] * sv[q][i];
+        tmax = std::max(tmax, th);
+        if (i < kept[q]) cut = cut < 0 ? th : std::min(cut, th);
+      }
+    }
+    const double tie = 2e-12 * tmax, acc_tol = 1e-11 * ftot / std::max(1, nsec);
     bool grow = false;
     for (int q = 0; q < nsec; ++q) {
-      const int64_t full = std::min(secs[q].rows, secs[q].cols);
-      if (kept[q] == s[q] && s[q] < full) {
-        s[q] = std::min(full, 2 * s[q] + sp.oversample);
+      need[q] = 0;
+      if (s[q] >= full[q]) continue;
+      bool miss = kept[q] == s[q];
+      const int64_t last = s[q] - 1;
+      const double th_last = sv[q][last] * sv[q][last];
+      auto err = [&](int64_t i) {
+        if (i == last) return std::sqrt(r2[q][i]);
+        const double gap = sv[q][i] * sv[q][i] - th_last;
+        return gap > 0 ? r2[q][i] / gap : std::sqrt(r2[q][i]);
+      };
+      double kerr = 0.0;
+      for (int64_t i = 0; i < kept[q] && !miss; ++i) kerr += err(i);
+      miss |= kerr > acc_tol;
+      for (int64_t j = kept[q]; j < s[q] && !miss && cut >= 0; ++j) {
+        const double th = sv[q][j] * sv[q][j];
+        miss |= err(j) > std::max(cut - th, tie);
+      }
+      if (miss) {
+        s[q] = std::min(full[q], 2 * s[q] + sp.oversample);
+        need[q] = 1;
         grow = true;
       }
     }
     if (grow && round < 8) continue;
-    std::vector<int64_t> iso_off(nsec), iso_ld(nsec);
-    for (int q = 0; q < nsec; ++q) {
-      iso_off[q] = yoff[q];
-      iso_ld[q] = s[q];
-    }
+    // (after the last round, sectors still marked keep the sketch they have)
+    std::vector<int64_t> iso_ld(nsec);
+    for (int q = 0; q < nsec; ++q) iso_ld[q] = (int64_t)sv[q].size();
     res.D = trial.D;
     res.trunc_err = trial.trunc_err;
-    build_outputs(ctx, scratch, T, ldims, secs, kept, sv, mode, Y2, iso_off, iso_ld, Mbuf, res);
-    res.sector_sketch = s;
+    build_outputs(ctx, scratch, T, ldims, secs, kept, sv, mode, Ubuf, uoff, iso_ld, Mbuf, res);
+    res.sector_sketch = iso_ld;
     res.grow_rounds = round;
     ctx.sync();
     return res;

@@ -43,6 +43,8 @@ void select_kept(const std::vector<std::vector<double>> &svals, double trunc_err
                  double rtol = 1e-12, double extra_mass = 0.0);
 
 void fill_normal(Ctx &ctx, double *x, int64_t n, uint64_t seed);
+// out[f_off + j] = sum_i X[x_off + i * cols + j]^2 for every job (by_row unused)
+void run_col_sumsq(Ctx &ctx, const std::vector<ScaleJob> &jobs, const double *X, double *out);
 // S (per job, n x n PSD) -> R^{-1} with S = R^T R (pivots below rel_tol drop)
 void run_chol_inv(Ctx &ctx, const std::vector<EigJob> &jobs, double *S, double *Rinv,
                   double rel_tol);
@@ -81,7 +83,7 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
 struct SketchParams {
   std::vector<std::pair<QN, int64_t>> sketch;  // requested sketch size per bond QN
   int64_t oversample = 8;
-  int power_iters = 2;
+  int power_iters = 4;
   uint64_t seed = 1;
 };
 SvdResult svd_trunc_sketch(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv,
