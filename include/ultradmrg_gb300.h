@@ -270,6 +270,13 @@ int udmrg_ctx_event_record(udmrg_ctx *ctx, int slot);
  * reference (a kernel check used by the tests). */
 int udmrg_selftest_tc_gemm(udmrg_ctx *ctx, int64_t M, int64_t N, int64_t K, const double *hA,
                            const double *hB, double *hC);
+/* Self-test of the batched symmetric eigensolver used by the SVD: for nmat
+ * row-major symmetric host matrices (sizes n[i], concatenated in mats), all
+ * eigenvalues (descending, concatenated in lam) and the leading k[i]
+ * eigenvectors (row-major n[i] x k[i], concatenated in vecs).  No counterpart
+ * in the reference (a kernel check used by the tests). */
+int udmrg_selftest_sym_eig(udmrg_ctx *ctx, int64_t nmat, const int32_t *n, const double *mats,
+                           const int32_t *k, double *lam, double *vecs);
 int udmrg_ctx_event_elapsed(udmrg_ctx *ctx, int slot_a, int slot_b, float *ms);
 int udmrg_ctx_flush_l2(udmrg_ctx *ctx, int64_t bytes);
 

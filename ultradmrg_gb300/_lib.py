@@ -116,6 +116,8 @@ SIGNATURES = {
     "udmrg_ctx_event_elapsed": [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)],
     "udmrg_ctx_flush_l2": [C.c_void_p, C.c_int64],
     "udmrg_norm_noalloc": [c_double_p, C.c_int64, c_double_p, C.c_void_p],
+    "udmrg_selftest_sym_eig": [C.c_void_p, C.c_int64, c_int32_p, c_double_p, c_int32_p,
+                               c_double_p, c_double_p],
     "udmrg_selftest_tc_gemm": [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, c_double_p,
                                c_double_p, c_double_p],
 }

@@ -6,6 +6,7 @@
 
 #include "../../include/ultradmrg_gb300.h"
 #include "dmrg.hpp"
+#include "svd.hpp"
 #include "tc_gemm.hpp"
 
 using namespace udmrg;
@@ -668,6 +669,43 @@ int udmrg_matvec_plan_apply(udmrg_matvec_plan *p, const double *d_in, double *d_
 
 int udmrg_probe_fp64_tflops(udmrg_ctx *c, double *tflops) {
   return guarded([&] { *tflops = probe_fp64_tflops(c->ctx); });
+}
+
+int udmrg_selftest_sym_eig(udmrg_ctx *c, int64_t nmat, const int32_t *n, const double *mats,
+                           const int32_t *k, double *lam, double *vecs) {
+  return guarded([&] {
+    Ctx &ctx = c->ctx;
+    std::vector<EigJob> jobs(nmat);
+    std::vector<int64_t> kk(nmat), zoff(nmat), zld(nmat);
+    int64_t gtot = 0, ltot = 0, ztot = 0;
+    for (int64_t i = 0; i < nmat; ++i) {
+      UDMRG_REQUIRE(n[i] >= 1 && k[i] >= 0 && k[i] <= n[i], "sym_eig: bad sizes");
+      jobs[i] = EigJob{gtot, ltot, n[i], 0};
+      kk[i] = k[i];
+      zoff[i] = ztot;
+      zld[i] = std::max<int64_t>(k[i], 1);
+      gtot += (int64_t)n[i] * n[i];
+      ltot += n[i];
+      ztot += (int64_t)n[i] * k[i];
+    }
+    DeviceScratch s(ctx);
+    double *G = s.get<double>(gtot), *L = s.get<double>(ltot), *Z = s.get<double>(ztot);
+    UDMRG_CHECK_CUDA(
+        cudaMemcpyAsync(G, mats, gtot * sizeof(double), cudaMemcpyHostToDevice, ctx.stream));
+    SymEigWork wk;
+    const int st = sym_eig_values(ctx, s, jobs, G, L, wk);
+    UDMRG_REQUIRE(st == 0, "sym_eig: non-finite input");
+    std::vector<double> hl(ltot);
+    UDMRG_CHECK_CUDA(
+        cudaMemcpyAsync(hl.data(), L, ltot * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.sync();
+    sym_eig_vectors(ctx, s, jobs, G, L, hl, kk, zoff, zld, Z, wk);
+    std::memcpy(lam, hl.data(), ltot * sizeof(double));
+    if (ztot > 0)
+      UDMRG_CHECK_CUDA(
+          cudaMemcpyAsync(vecs, Z, ztot * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.sync();
+  });
 }
 
 int udmrg_selftest_tc_gemm(udmrg_ctx *c, int64_t M, int64_t N, int64_t K, const double *hA,

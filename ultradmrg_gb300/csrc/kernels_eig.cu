@@ -1,0 +1,543 @@
+// Batched symmetric eigen-solver of the truncated SVD (Gram matrices of the
+// bond sectors and the Rayleigh-Ritz matrices of the randomized SVD).
+//
+// FP64 throughput per SM is low on this GPU, so the solver does as little
+// FP64 work as the problem allows:
+//   1. Householder reduction to tridiagonal form (about 2 n^3 flops, one CTA
+//      per matrix; the reflectors stay in the matrix's upper triangle);
+//   2. every eigenvalue by Sturm-sequence bisection (O(n) per step and
+//      eigenvalue, all eigenvalues of all matrices in parallel);
+//   3. only the eigenvectors the caller needs, by inverse iteration on the
+//      tridiagonal matrix (one thread per cluster of close eigenvalues;
+//      modified Gram-Schmidt inside a cluster);
+//   4. orthonormalisation by Newton-Schulz steps (grouped GEMMs, host side);
+//   5. back-transformation by the Householder reflectors (one CTA per matrix).
+// These are the textbook methods (Golub & Van Loan ch. 8; Wilkinson's
+// inverse iteration; the Sturm count of Barth, Martin & Wilkinson), written
+// for this batch layout.
+#include <cmath>
+
+#include "svd.hpp"
+
+namespace udmrg {
+
+namespace {
+
+constexpr int kTriThreads = 512;
+constexpr int kBisectThreads = 128;
+constexpr int kBackThreads = 256;
+
+__device__ double block_sum(double v, double *red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < nw; ++i) s += red[i];
+    red[32] = s;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+// Householder tridiagonalisation of the symmetric n x n matrix of each job
+// (row-major at G + g_off; the matrix is first scaled to unit max-abs, the
+// scale goes to scale[job]).  Step j reflects row/column j: v (v_0 = 1) is
+// stored in row j right of the first superdiagonal, tau in tau[lam_off + j],
+// the diagonal in d[lam_off + i] and the off-diagonal in e[lam_off + i].
+__global__ void tridiag_kernel(const EigJob *__restrict__ jobs, double *__restrict__ G_all,
+                               double *__restrict__ d_all, double *__restrict__ e_all,
+                               double *__restrict__ tau_all, double *__restrict__ scale_all,
+                               int *__restrict__ status) {
+  extern __shared__ double sm[];
+  __shared__ double red[33];
+  __shared__ int bad;
+  const EigJob job = jobs[blockIdx.x];
+  const int n = job.n;
+  if (n == 0) return;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  double *A = job.smem ? sm : G_all + job.g_off;
+  double *v = sm + (job.smem ? (int64_t)n * n : 0);
+  double *w = v + n;
+  double *d = d_all + job.lam_off, *e = e_all + job.lam_off, *tau = tau_all + job.lam_off;
+
+  if (job.smem)
+    for (int64_t x = tid; x < (int64_t)n * n; x += nt) A[x] = G_all[job.g_off + x];
+  // scale to unit max-abs; non-finite input is reported
+  double mx = 0.0;
+  int nf = 0;
+  if (tid == 0) bad = 0;
+  for (int64_t x = tid; x < (int64_t)n * n; x += nt) {
+    const double g = A[x];
+    nf |= !isfinite(g);
+    mx = fmax(mx, fabs(g));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    nf |= __shfl_down_sync(0xffffffffu, nf, o);
+  }
+  __syncthreads();
+  if (lane == 0) {
+    red[warp] = mx;
+    if (nf) atomicOr(&bad, 1);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double m = 0.0;
+    for (int i = 0; i < nwarp; ++i) m = fmax(m, red[i]);
+    red[32] = m;
+  }
+  __syncthreads();
+  if (bad) {
+    if (tid == 0) atomicExch(status, 2);
+    return;
+  }
+  const double scale = red[32];
+  if (tid == 0) scale_all[blockIdx.x] = scale;
+  // scale and symmetrise (a GEMM-made Gram matrix is symmetric only up to rounding)
+  const double inv = scale > 0.0 ? 1.0 / scale : 0.0;
+  for (int64_t x = tid; x < (int64_t)n * n; x += nt) {
+    const int r = (int)(x / n), c = (int)(x - (int64_t)r * n);
+    if (r < c) {
+      const double g = 0.5 * inv * (A[x] + A[(int64_t)c * n + r]);
+      A[x] = g;
+      A[(int64_t)c * n + r] = g;
+    } else if (r == c) {
+      A[x] *= inv;
+    }
+  }
+  __syncthreads();
+
+  for (int j = 0; j + 2 < n; ++j) {
+    const int m = n - j - 1;  // length of the reflected vector (rows j+1 .. n-1)
+    double *rowj = A + (int64_t)j * n;
+    const double alpha = rowj[j + 1];
+    double x2 = 0.0;
+    for (int c = j + 2 + tid; c < n; c += nt) x2 += rowj[c] * rowj[c];
+    x2 = block_sum(x2, red);
+    double t = 0.0, beta = alpha, vs = 0.0;
+    if (x2 > 0.0) {
+      beta = -copysign(sqrt(alpha * alpha + x2), alpha);
+      t = (beta - alpha) / beta;
+      vs = 1.0 / (alpha - beta);
+    }
+    for (int r = tid; r < m; r += nt) {
+      const double vr = r == 0 ? 1.0 : rowj[j + 1 + r] * vs;
+      v[r] = t == 0.0 ? (r == 0 ? 1.0 : 0.0) : vr;
+      if (r > 0) rowj[j + 1 + r] = v[r];
+    }
+    if (tid == 0) {
+      d[j] = rowj[j];
+      e[j] = beta;
+      tau[j] = t;
+    }
+    __syncthreads();
+    if (t == 0.0) continue;
+    // w = t * A_t v, A_t = trailing block rows/cols j+1 .. n-1 (one warp per row)
+    for (int r = warp; r < m; r += nwarp) {
+      const double *ar = A + (int64_t)(j + 1 + r) * n + (j + 1);
+      double s = 0.0;
+      for (int c = lane; c < m; c += 32) s += ar[c] * v[c];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) w[r] = t * s;
+    }
+    __syncthreads();
+    double wv = 0.0;
+    for (int r = tid; r < m; r += nt) wv += w[r] * v[r];
+    wv = block_sum(wv, red);
+    const double K = -0.5 * t * wv;
+    for (int r = tid; r < m; r += nt) w[r] += K * v[r];
+    __syncthreads();
+    // A_t -= v w^T + w v^T
+    for (int64_t x = tid; x < (int64_t)m * m; x += nt) {
+      const int r = (int)(x / m), c = (int)(x - (int64_t)r * m);
+      A[(int64_t)(j + 1 + r) * n + (j + 1 + c)] -= v[r] * w[c] + w[r] * v[c];
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    if (n >= 2) {
+      d[n - 2] = A[(int64_t)(n - 2) * n + (n - 2)];
+      e[n - 2] = A[(int64_t)(n - 2) * n + (n - 1)];
+      tau[n - 2] = 0.0;
+    }
+    d[n - 1] = A[(int64_t)(n - 1) * n + (n - 1)];
+    e[n - 1] = 0.0;
+    tau[n - 1] = 0.0;
+  }
+  __syncthreads();
+  if (job.smem)  // the reflectors live in the rows' upper parts
+    for (int64_t x = tid; x < (int64_t)n * n; x += nt) G_all[job.g_off + x] = A[x];
+}
+
+// Number of eigenvalues of the tridiagonal (d, e) below x (Sturm count).
+__device__ __forceinline__ int sturm_count(const double *d, const double *e, int n, double x,
+                                           double pivmin) {
+  int cnt = 0;
+  double q = d[0] - x;
+  if (fabs(q) < pivmin) q = -pivmin;
+  if (q < 0.0) ++cnt;
+  for (int k = 1; k < n; ++k) {
+    q = d[k] - x - e[k - 1] * e[k - 1] / q;
+    if (fabs(q) < pivmin) q = -pivmin;
+    if (q < 0.0) ++cnt;
+  }
+  return cnt;
+}
+
+// All eigenvalues by bisection; lam[lam_off + i] (descending) = scale * value.
+__global__ void bisect_kernel(const EigJob *__restrict__ jobs, const double *__restrict__ d_all,
+                              const double *__restrict__ e_all,
+                              const double *__restrict__ scale_all, double *__restrict__ lam_all) {
+  extern __shared__ double sm[];
+  const EigJob job = jobs[blockIdx.x];
+  const int n = job.n;
+  if (n == 0) return;
+  double *d = sm, *e = sm + n;
+  __shared__ double lo0, hi0, emax;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    d[i] = d_all[job.lam_off + i];
+    e[i] = i + 1 < n ? e_all[job.lam_off + i] : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // Gershgorin interval
+    double lo = d[0], hi = d[0], em = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
+      lo = fmin(lo, d[i] - r);
+      hi = fmax(hi, d[i] + r);
+      if (i + 1 < n) em = fmax(em, fabs(e[i]));
+    }
+    const double pad = 2.2e-16 * fmax(fabs(lo), fabs(hi)) * n + 1e-300;
+    lo0 = lo - pad;
+    hi0 = hi + pad;
+    emax = em;
+  }
+  __syncthreads();
+  const double pivmin = 1e-290 * fmax(1.0, emax * emax);
+  const double scale = scale_all[blockIdx.x];
+  // absolute accuracy far below the eps * |T| the reduction itself achieves
+  const double atol = 1e-18 * fmax(fabs(lo0), fabs(hi0));
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {  // i-th smallest
+    double lo = lo0, hi = hi0;
+    for (int it = 0; it < 128; ++it) {
+      const double mid = 0.5 * (lo + hi);
+      if (hi - lo <= 4.4e-16 * fmax(fabs(lo), fabs(hi)) + atol || mid <= lo || mid >= hi)
+        break;
+      if (sturm_count(d, e, n, mid, pivmin) > i)
+        hi = mid;
+      else
+        lo = mid;
+    }
+    lam_all[job.lam_off + (n - 1 - i)] = scale * 0.5 * (lo + hi);
+  }
+}
+
+__device__ __forceinline__ double start_entry(uint64_t seed, int i) {
+  uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(i + 1);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
+// Inverse iteration: one thread per cluster of eigenvalues (descending
+// positions first .. first+count-1 of job `job`), each eigenvector found with
+// an LU factorisation (partial pivoting) of T - lambda I and three solves,
+// orthogonalised against the cluster's earlier vectors (modified
+// Gram-Schmidt).  Vector of position p goes to column p of Z (row-major
+// n x ld at z_off).  Work arrays are interleaved by thread (coalesced).
+__global__ void invit_kernel(const EigCluster *__restrict__ cl, int ncl,
+                             const EigJob *__restrict__ jobs, const double *__restrict__ d_all,
+                             const double *__restrict__ e_all,
+                             const double *__restrict__ scale_all,
+                             const double *__restrict__ lam_all, double *__restrict__ Z,
+                             double *__restrict__ work, int nmax) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncl) return;
+  const EigCluster c = cl[t];
+  const EigJob job = jobs[c.job];
+  const int n = job.n;
+  const double *d = d_all + job.lam_off, *e = e_all + job.lam_off;
+  const int64_t T = ncl;
+  double *l = work + 0 * (int64_t)nmax * T, *u0 = work + 1 * (int64_t)nmax * T;
+  double *u1 = work + 2 * (int64_t)nmax * T, *u2 = work + 3 * (int64_t)nmax * T;
+  double *y = work + 4 * (int64_t)nmax * T, *pv = work + 5 * (int64_t)nmax * T;
+  auto at = [&](double *a, int i) -> double & { return a[(int64_t)i * T + t]; };
+  double tnorm = 0.0;
+  for (int i = 0; i < n; ++i)
+    tnorm = fmax(tnorm, fabs(d[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0) +
+                            (i + 1 < n ? fabs(e[i]) : 0.0));
+  const double tiny = 2.2e-16 * (tnorm > 0.0 ? tnorm : 1.0);  // zero matrix: any basis
+  const double inv_scale = scale_all[c.job] > 0.0 ? 1.0 / scale_all[c.job] : 0.0;
+  double *zc = Z + c.z_off;
+  for (int k = 0; k < c.count; ++k) {
+    const int p = c.first + k;
+    const double lam = lam_all[job.lam_off + p] * inv_scale;
+    if (n == 1) {
+      zc[p] = 1.0;
+      continue;
+    }
+    // LU of T - lam I with row interchanges: row i of U holds u0 (diagonal),
+    // u1, u2 (the two superdiagonals); l the multipliers; pv the interchanges
+    double a = d[0] - lam, b = e[0];
+    for (int i = 0; i + 1 < n; ++i) {
+      const double sub = e[i], dn = d[i + 1] - lam, sup = i + 2 < n ? e[i + 1] : 0.0;
+      if (fabs(a) >= fabs(sub)) {
+        const double piv = a != 0.0 ? a : tiny;
+        const double f = sub / piv;
+        at(u0, i) = piv;
+        at(u1, i) = b;
+        at(u2, i) = 0.0;
+        at(l, i) = f;
+        at(pv, i) = 0.0;
+        a = dn - f * b;
+        b = sup;
+      } else {
+        const double f = a / sub;
+        at(u0, i) = sub;
+        at(u1, i) = dn;
+        at(u2, i) = sup;
+        at(l, i) = f;
+        at(pv, i) = 1.0;
+        a = b - f * dn;
+        b = -f * sup;
+      }
+    }
+    at(u0, n - 1) = fabs(a) > tiny ? a : (a < 0 ? -tiny : tiny);
+    for (int i = 0; i < n; ++i) at(y, i) = start_entry(c.seed + 7919ull * (uint64_t)p, i);
+    for (int it = 0; it < 3; ++it) {
+      // forward: apply the interchanges and multipliers
+      for (int i = 0; i + 1 < n; ++i) {
+        if (at(pv, i) != 0.0) {
+          const double tmp = at(y, i);
+          at(y, i) = at(y, i + 1);
+          at(y, i + 1) = tmp - at(l, i) * at(y, i);
+        } else {
+          at(y, i + 1) -= at(l, i) * at(y, i);
+        }
+      }
+      // back substitution with U
+      for (int i = n - 1; i >= 0; --i) {
+        double s = at(y, i);
+        if (i + 1 < n) s -= at(u1, i) * at(y, i + 1);
+        if (i + 2 < n) s -= at(u2, i) * at(y, i + 2);
+        const double piv = fabs(at(u0, i)) > tiny ? at(u0, i) : (at(u0, i) < 0 ? -tiny : tiny);
+        at(y, i) = s / piv;
+      }
+      // orthogonalise against the cluster's earlier vectors, normalise
+      for (int q = c.first; q < p; ++q) {
+        double s = 0.0;
+        for (int i = 0; i < n; ++i) s += zc[(int64_t)i * c.ld + q] * at(y, i);
+        for (int i = 0; i < n; ++i) at(y, i) -= s * zc[(int64_t)i * c.ld + q];
+      }
+      double nrm = 0.0;
+      for (int i = 0; i < n; ++i) nrm += at(y, i) * at(y, i);
+      nrm = sqrt(nrm);
+      const double f = nrm > 0.0 ? 1.0 / nrm : 0.0;
+      for (int i = 0; i < n; ++i) at(y, i) *= f;
+    }
+    for (int i = 0; i < n; ++i) zc[(int64_t)i * c.ld + p] = at(y, i);
+  }
+}
+
+// Z (row-major n x k, leading dimension ld, at z_off) <- Q Z with
+// Q = H_0 H_1 ... H_{n-3}, H_j = I - tau_j v_j v_j^T acting on rows j+1 ...
+__global__ void backtransform_kernel(const EigJob *__restrict__ jobs,
+                                     const int64_t *__restrict__ zoff,
+                                     const int32_t *__restrict__ kcols,
+                                     const int64_t *__restrict__ zld,
+                                     const double *__restrict__ G_all,
+                                     const double *__restrict__ tau_all, double *__restrict__ Z) {
+  extern __shared__ double sm[];
+  const EigJob job = jobs[blockIdx.x];
+  const int n = job.n, k = kcols[blockIdx.x];
+  if (n < 3 || k == 0) return;
+  const int64_t ld = zld[blockIdx.x];
+  double *z = Z + zoff[blockIdx.x];
+  double *v = sm, *w = sm + n;  // v (n), w (k)
+  const double *A = G_all + job.g_off;
+  for (int j = n - 3; j >= 0; --j) {
+    const double t = tau_all[job.lam_off + j];
+    if (t == 0.0) continue;  // uniform across the block
+    const int m = n - j - 1;
+    for (int r = threadIdx.x; r < m; r += blockDim.x)
+      v[r] = r == 0 ? 1.0 : A[(int64_t)j * n + j + 1 + r];
+    __syncthreads();
+    for (int cc = threadIdx.x; cc < k; cc += blockDim.x) {
+      double s = 0.0;
+      for (int r = 0; r < m; ++r) s += v[r] * z[(int64_t)(j + 1 + r) * ld + cc];
+      w[cc] = t * s;
+    }
+    __syncthreads();
+    for (int64_t x = threadIdx.x; x < (int64_t)m * k; x += blockDim.x) {
+      const int r = (int)(x / k), cc = (int)(x - (int64_t)r * k);
+      z[(int64_t)(j + 1 + r) * ld + cc] -= v[r] * w[cc];
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+constexpr size_t kTriSmemBytes = 200 * 1024;
+
+int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, double *G,
+                   double *lam, SymEigWork &wk) {
+  const int nj = (int)jobs.size();
+  if (nj == 0) return 0;
+  int64_t ltot = 0;
+  int nmax = 0;
+  for (auto &j : jobs) {
+    ltot = std::max<int64_t>(ltot, j.lam_off + j.n);
+    nmax = std::max(nmax, j.n);
+  }
+  UDMRG_REQUIRE(nmax <= 4096, "eigensolver: matrix larger than 4096 is not supported");
+  wk.d = scratch.get<double>(std::max<int64_t>(ltot, 1));
+  wk.e = scratch.get<double>(std::max<int64_t>(ltot, 1));
+  wk.tau = scratch.get<double>(std::max<int64_t>(ltot, 1));
+  wk.scale = scratch.get<double>(nj);
+  size_t smem = 0;
+  for (auto &j : jobs) {
+    const size_t base = 2 * (size_t)j.n * sizeof(double);
+    const size_t full = base + (size_t)j.n * j.n * sizeof(double);
+    j.smem = full <= kTriSmemBytes ? 1 : 0;
+    smem = std::max(smem, j.smem ? full : base);
+  }
+  UDMRG_CHECK_CUDA(cudaFuncSetAttribute(tridiag_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)kTriSmemBytes));
+  wk.jobs = scratch.get<EigJob>(nj);
+  int *dstat = scratch.get<int>(1);
+  UDMRG_CHECK_CUDA(cudaMemsetAsync(dstat, 0, sizeof(int), ctx.stream));
+  UDMRG_CHECK_CUDA(cudaMemcpyAsync(wk.jobs, jobs.data(), nj * sizeof(EigJob),
+                                   cudaMemcpyHostToDevice, ctx.stream));
+  tridiag_kernel<<<nj, kTriThreads, smem, ctx.stream>>>(wk.jobs, G, wk.d, wk.e, wk.tau, wk.scale,
+                                                        dstat);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  const size_t bsmem = 2 * (size_t)nmax * sizeof(double);
+  if (bsmem > 48 * 1024)
+    UDMRG_CHECK_CUDA(cudaFuncSetAttribute(bisect_kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem));
+  bisect_kernel<<<nj, kBisectThreads, bsmem, ctx.stream>>>(
+      wk.jobs, wk.d, wk.e, wk.scale, lam);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  ctx.launches += 2;
+  int hstat = 0;
+  UDMRG_CHECK_CUDA(cudaMemcpyAsync(&hstat, dstat, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+  ctx.sync();
+  return hstat;
+}
+
+void sym_eig_vectors(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJob> &jobs,
+                     const double *G, const double *lam, const std::vector<double> &hlam,
+                     const std::vector<int64_t> &k, const std::vector<int64_t> &z_off,
+                     const std::vector<int64_t> &z_ld, double *Z, const SymEigWork &wk,
+                     uint64_t seed) {
+  const int nj = (int)jobs.size();
+  // clusters: descending neighbours closer than 1e-9 of the matrix's largest |eigenvalue|
+  std::vector<EigCluster> cl;
+  int nmax = 0;
+  for (int q = 0; q < nj; ++q) {
+    const int n = jobs[q].n;
+    nmax = std::max(nmax, n);
+    if (k[q] == 0) continue;
+    const double *h = hlam.data() + jobs[q].lam_off;
+    const double big = std::max(std::fabs(h[0]), std::fabs(h[n - 1]));
+    const double tol = 1e-9 * big;
+    int first = 0;
+    for (int p = 1; p <= k[q]; ++p) {
+      if (p == k[q] || h[p - 1] - h[p] > tol) {
+        cl.push_back(EigCluster{z_off[q], z_ld[q], seed + 1000003ull * (uint64_t)q, q, first,
+                                p - first, 0});
+        first = p;
+      }
+    }
+  }
+  if (!cl.empty()) {
+    const int ncl = (int)cl.size();
+    EigCluster *dcl = scratch.get<EigCluster>(ncl);
+    double *work = scratch.get<double>(6 * (int64_t)nmax * ncl);
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(dcl, cl.data(), ncl * sizeof(EigCluster),
+                                     cudaMemcpyHostToDevice, ctx.stream));
+    invit_kernel<<<(ncl + 63) / 64, 64, 0, ctx.stream>>>(dcl, ncl, wk.jobs, wk.d, wk.e, wk.scale,
+                                                        lam, Z, work, nmax);
+    UDMRG_CHECK_CUDA(cudaGetLastError());
+    ctx.launches++;
+  }
+  // Newton-Schulz: Z <- 1.5 Z - 0.5 Z (Z^T Z), twice (grouped GEMMs)
+  {
+    int64_t stot = 0, ztot = 0;
+    std::vector<int64_t> soff(nj), zc_off(nj);
+    for (int q = 0; q < nj; ++q) {
+      soff[q] = stot;
+      stot += k[q] * k[q];
+      zc_off[q] = ztot;
+      ztot += (int64_t)jobs[q].n * k[q];
+    }
+    if (stot > 0) {
+      DeviceScratch ns(ctx);
+      double *S = ns.get<double>(stot), *Zc = ns.get<double>(ztot);
+      GemmPlan gs, gz, gc;
+      gs.ctx = gz.ctx = gc.ctx = &ctx;
+      for (int q = 0; q < nj; ++q) {
+        if (k[q] == 0) continue;
+        const int64_t n = jobs[q].n, kk = k[q];
+        // S = Z^T Z (k x k): A = Z^T (ms 1, ks ld), B = Z (ks ld, ns 1)
+        gemm_add_simple(gs, soff[q], kk, kk, n, z_off[q], 1, z_ld[q], z_off[q], z_ld[q], 1, false);
+        // Zc = Z S (n x k, packed): accumulated as Zc = -0.5 Z S + 1.5 Zc
+        gemm_add_simple(gz, zc_off[q], n, kk, kk, z_off[q], z_ld[q], 1, soff[q], kk, 1, false);
+      }
+      gemm_finalize(gs);
+      gemm_finalize(gz);
+      std::vector<Copy2D> to_c, from_c;
+      for (int q = 0; q < nj; ++q) {
+        if (k[q] == 0) continue;
+        to_c.push_back(Copy2D{z_off[q], zc_off[q], jobs[q].n, (int32_t)k[q], z_ld[q], 1, k[q], 1});
+        from_c.push_back(
+            Copy2D{zc_off[q], z_off[q], jobs[q].n, (int32_t)k[q], k[q], 1, z_ld[q], 1});
+      }
+      for (int it = 0; it < 2; ++it) {
+        run_gemm(ctx, gs, kF64, Z, Z, S, 1.0, 0.0);
+        run_copy2d(ctx, to_c, Z, Zc, false);
+        run_gemm(ctx, gz, kF64, Z, S, Zc, -0.5, 1.5);
+        run_copy2d(ctx, from_c, Zc, Z, false);
+      }
+    }
+  }
+  // back-transformation by the reflectors
+  {
+    std::vector<int64_t> zo(nj), zl(nj);
+    std::vector<int32_t> kc(nj);
+    int kmax = 0;
+    for (int q = 0; q < nj; ++q) {
+      zo[q] = z_off[q];
+      zl[q] = z_ld[q];
+      kc[q] = (int32_t)k[q];
+      kmax = std::max<int>(kmax, (int)k[q]);
+    }
+    int64_t *dzo = scratch.get<int64_t>(nj), *dzl = scratch.get<int64_t>(nj);
+    int32_t *dkc = scratch.get<int32_t>(nj);
+    UDMRG_CHECK_CUDA(
+        cudaMemcpyAsync(dzo, zo.data(), nj * sizeof(int64_t), cudaMemcpyHostToDevice, ctx.stream));
+    UDMRG_CHECK_CUDA(
+        cudaMemcpyAsync(dzl, zl.data(), nj * sizeof(int64_t), cudaMemcpyHostToDevice, ctx.stream));
+    UDMRG_CHECK_CUDA(
+        cudaMemcpyAsync(dkc, kc.data(), nj * sizeof(int32_t), cudaMemcpyHostToDevice, ctx.stream));
+    const size_t smem = ((size_t)nmax + kmax) * sizeof(double);
+    if (smem > 48 * 1024)
+      UDMRG_CHECK_CUDA(cudaFuncSetAttribute(backtransform_kernel,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem));
+    backtransform_kernel<<<nj, kBackThreads, smem, ctx.stream>>>(wk.jobs, dzo, dkc, dzl, G, wk.tau,
+                                                                 Z);
+    UDMRG_CHECK_CUDA(cudaGetLastError());
+    ctx.launches++;
+  }
+  ctx.sync();  // host vectors above must outlive the uploads
+}
+
+}  // namespace udmrg

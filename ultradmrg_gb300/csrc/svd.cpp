@@ -381,8 +381,6 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
     ltot += n;
   }
   double *G = scratch.get<double>(std::max<int64_t>(gtot, 1));
-  double *V = scratch.get<double>(std::max<int64_t>(gtot, 1));
-  double *W = scratch.get<double>(std::max<int64_t>(gtot, 1));
   double *lam = scratch.get<double>(std::max<int64_t>(ltot, 1));
   {
     GemmPlan g;
@@ -395,7 +393,8 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
     gemm_finalize(g);
     run_gemm(ctx, g, kF64, Mbuf, Mbuf, G, 1.0, 0.0);
   }
-  check_eig_status(run_jacobi_eig(ctx, jobs, G, V, W, lam));
+  SymEigWork wk;
+  check_eig_status(sym_eig_values(ctx, scratch, jobs, G, lam, wk));
   const std::vector<double> hlam = download_vec(ctx, lam, ltot);
   std::vector<std::vector<double>> sv(nsec);
   for (int q = 0; q < nsec; ++q) {
@@ -407,12 +406,17 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
   SvdResult res;
   std::vector<int64_t> kept;
   select_kept(sv, trunc_err, Dmin, Dmax, kept, res.D, res.trunc_err);
+  // eigenvectors of the kept states only: the isometric factor (n x kept)
   std::vector<int64_t> iso_off(nsec), iso_ld(nsec);
+  int64_t ztot = 0;
   for (int q = 0; q < nsec; ++q) {
-    iso_off[q] = jobs[q].g_off;
-    iso_ld[q] = jobs[q].n;
+    iso_off[q] = ztot;
+    iso_ld[q] = std::max<int64_t>(kept[q], 1);
+    ztot += (int64_t)jobs[q].n * kept[q];
   }
-  build_outputs(ctx, scratch, T, ldims, secs, kept, sv, mode, V, iso_off, iso_ld, Mbuf, res);
+  double *Z = scratch.get<double>(std::max<int64_t>(ztot, 1));
+  sym_eig_vectors(ctx, scratch, jobs, G, lam, hlam, kept, iso_off, iso_ld, Z, wk);
+  build_outputs(ctx, scratch, T, ldims, secs, kept, sv, mode, Z, iso_off, iso_ld, Mbuf, res);
   res.sector_sketch.assign(nsec, 0);
   return res;
 }
@@ -560,7 +564,17 @@ SvdResult svd_trunc_sketch(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv
       gemm_finalize(g);
       run_gemm(ctx, g, kF64, Z, Z, Sg, 1.0, 0.0);
     }
-    check_eig_status(run_jacobi_eig(ctx, jobs, Sg, Vv, Wk, lam));
+    {  // Rayleigh-Ritz: all s eigenpairs of G (Vv: row-major s x s eigenvectors)
+      SymEigWork wk;
+      check_eig_status(sym_eig_values(ctx, rs, jobs, Sg, lam, wk));
+      const std::vector<double> hlr = download_vec(ctx, lam, ltot);
+      std::vector<int64_t> kk(na), zo(na), zl(na);
+      for (int a = 0; a < na; ++a) {
+        kk[a] = zl[a] = s[act[a]];
+        zo[a] = soff[a];
+      }
+      sym_eig_vectors(ctx, rs, jobs, Sg, lam, hlr, kk, zo, zl, Vv, wk);
+    }
     mult_small(Y, Vv, Y2, yoff, true);   // U = Q W (xr x s)
     mult_small(Z, Vv, Z2, zoff, false);  // P = X^T U = Z W (xc x s)
     // residuals: Y := X P - U Theta (Q in Y is no longer needed), column norms

@@ -19,6 +19,18 @@ struct EigJob {
   int32_t smem;     // set by run_jacobi_eig
 };
 
+// Batched symmetric eigen-solver (Householder tridiagonalisation, bisection,
+// inverse iteration, Newton-Schulz orthonormalisation, back-transformation).
+struct EigCluster {  // eigenvalues close enough to share a Gram-Schmidt sweep
+  int64_t z_off, ld;
+  uint64_t seed;
+  int32_t job, first, count, pad;
+};
+struct SymEigWork {
+  EigJob *jobs = nullptr;  // device copy of the jobs
+  double *d = nullptr, *e = nullptr, *tau = nullptr, *scale = nullptr;
+};
+
 struct ScaleJob {
   int64_t x_off, f_off;
   int32_t rows, cols;
@@ -38,6 +50,20 @@ void run_scale(Ctx &ctx, const std::vector<ScaleJob> &jobs, double *X, const dou
 // singular values ordered by descending size, ties within rtol*s_max ordered by
 // (sector, position); keep the smallest D in [min(Dmin,n), min(Dmax,n)] whose
 // discarded weight sum_{discarded} s^2 / sum s^2 <= trunc_err.
+// Phase 1: reduce every job's symmetric n x n matrix in G to tridiagonal form
+// (G keeps the reflectors) and put all its eigenvalues, descending, at
+// lam[lam_off ...].  Returns 0, or 2 for non-finite input.  jobs[].smem is set.
+int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, double *G,
+                   double *lam, SymEigWork &wk);
+// Phase 2: the leading k[q] eigenvectors of job q (hlam: host copy of lam) as
+// the columns of Z (row-major n x k[q], leading dimension z_ld[q], at z_off[q]),
+// orthonormal to FP64 accuracy.
+void sym_eig_vectors(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJob> &jobs,
+                     const double *G, const double *lam, const std::vector<double> &hlam,
+                     const std::vector<int64_t> &k, const std::vector<int64_t> &z_off,
+                     const std::vector<int64_t> &z_ld, double *Z, const SymEigWork &wk,
+                     uint64_t seed = 0x5EED5EEDull);
+
 void select_kept(const std::vector<std::vector<double>> &svals, double trunc_err, int64_t Dmin,
                  int64_t Dmax, std::vector<int64_t> &kept, int64_t &D, double &err,
                  double rtol = 1e-12, double extra_mass = 0.0);
