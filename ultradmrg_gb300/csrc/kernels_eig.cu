@@ -24,7 +24,7 @@ namespace udmrg {
 namespace {
 
 constexpr int kTriThreads = 512;
-constexpr int kBisectThreads = 128;
+constexpr int kBisectThreads = 32;
 constexpr int kBackThreads = 256;
 
 __device__ double block_sum(double v, double *red) {
@@ -189,11 +189,15 @@ __device__ __forceinline__ int sturm_count(const double *d, const double *e, int
 }
 
 // All eigenvalues by bisection; lam[lam_off + i] (descending) = scale * value.
-__global__ void bisect_kernel(const EigJob *__restrict__ jobs, const double *__restrict__ d_all,
-                              const double *__restrict__ e_all,
+// Block b handles the eigenvalues i0 .. i0 + blockDim.x - 1 (ascending index)
+// of job chunk[b].x, i0 = chunk[b].y, one per thread, so a large matrix is
+// spread over many SMs.
+__global__ void bisect_kernel(const EigJob *__restrict__ jobs, const int2 *__restrict__ chunk,
+                              const double *__restrict__ d_all, const double *__restrict__ e_all,
                               const double *__restrict__ scale_all, double *__restrict__ lam_all) {
   extern __shared__ double sm[];
-  const EigJob job = jobs[blockIdx.x];
+  const int jb = chunk[blockIdx.x].x, i0 = chunk[blockIdx.x].y;
+  const EigJob job = jobs[jb];
   const int n = job.n;
   if (n == 0) return;
   double *d = sm, *e = sm + n;
@@ -218,10 +222,12 @@ __global__ void bisect_kernel(const EigJob *__restrict__ jobs, const double *__r
   }
   __syncthreads();
   const double pivmin = 1e-290 * fmax(1.0, emax * emax);
-  const double scale = scale_all[blockIdx.x];
+  const double scale = scale_all[jb];
   // absolute accuracy far below the eps * |T| the reduction itself achieves
   const double atol = 1e-18 * fmax(fabs(lo0), fabs(hi0));
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {  // i-th smallest
+  {
+    const int i = i0 + threadIdx.x;  // i-th smallest
+    if (i >= n) return;
     double lo = lo0, hi = hi0;
     for (int it = 0; it < 128; ++it) {
       const double mid = 0.5 * (lo + hi);
@@ -346,20 +352,27 @@ __global__ void invit_kernel(const EigCluster *__restrict__ cl, int ncl,
 
 // Z (row-major n x k, leading dimension ld, at z_off) <- Q Z with
 // Q = H_0 H_1 ... H_{n-3}, H_j = I - tau_j v_j v_j^T acting on rows j+1 ...
+// Block b transforms columns c0 .. c0 + 31 of job bt[b].job (columns are
+// independent), threads as 32 columns x 8 row groups.
+struct BackChunk {
+  int64_t z_off, ld;
+  int32_t job, c0, cw, pad;
+};
 __global__ void backtransform_kernel(const EigJob *__restrict__ jobs,
-                                     const int64_t *__restrict__ zoff,
-                                     const int32_t *__restrict__ kcols,
-                                     const int64_t *__restrict__ zld,
+                                     const BackChunk *__restrict__ bt,
                                      const double *__restrict__ G_all,
                                      const double *__restrict__ tau_all, double *__restrict__ Z) {
   extern __shared__ double sm[];
-  const EigJob job = jobs[blockIdx.x];
-  const int n = job.n, k = kcols[blockIdx.x];
-  if (n < 3 || k == 0) return;
-  const int64_t ld = zld[blockIdx.x];
-  double *z = Z + zoff[blockIdx.x];
-  double *v = sm, *w = sm + n;  // v (n), w (k)
+  __shared__ double part[8][33];
+  const BackChunk ch = bt[blockIdx.x];
+  const EigJob job = jobs[ch.job];
+  const int n = job.n;
+  if (n < 3 || ch.cw == 0) return;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // blockDim.x == 256
+  double *z = Z + ch.z_off + ch.c0;
+  double *v = sm;  // n
   const double *A = G_all + job.g_off;
+  const bool col = tx < ch.cw;
   for (int j = n - 3; j >= 0; --j) {
     const double t = tau_all[job.lam_off + j];
     if (t == 0.0) continue;  // uniform across the block
@@ -367,16 +380,16 @@ __global__ void backtransform_kernel(const EigJob *__restrict__ jobs,
     for (int r = threadIdx.x; r < m; r += blockDim.x)
       v[r] = r == 0 ? 1.0 : A[(int64_t)j * n + j + 1 + r];
     __syncthreads();
-    for (int cc = threadIdx.x; cc < k; cc += blockDim.x) {
-      double s = 0.0;
-      for (int r = 0; r < m; ++r) s += v[r] * z[(int64_t)(j + 1 + r) * ld + cc];
-      w[cc] = t * s;
-    }
+    double s = 0.0;
+    if (col)
+      for (int r = ty; r < m; r += 8) s += v[r] * z[(int64_t)(j + 1 + r) * ch.ld + tx];
+    part[ty][tx] = s;
     __syncthreads();
-    for (int64_t x = threadIdx.x; x < (int64_t)m * k; x += blockDim.x) {
-      const int r = (int)(x / k), cc = (int)(x - (int64_t)r * k);
-      z[(int64_t)(j + 1 + r) * ld + cc] -= v[r] * w[cc];
-    }
+    double w = 0.0;
+    for (int g = 0; g < 8; ++g) w += part[g][tx];
+    w *= t;
+    if (col)
+      for (int r = ty; r < m; r += 8) z[(int64_t)(j + 1 + r) * ch.ld + tx] -= v[r] * w;
     __syncthreads();
   }
 }
@@ -422,8 +435,15 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
   if (bsmem > 48 * 1024)
     UDMRG_CHECK_CUDA(cudaFuncSetAttribute(bisect_kernel,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem));
-  bisect_kernel<<<nj, kBisectThreads, bsmem, ctx.stream>>>(
-      wk.jobs, wk.d, wk.e, wk.scale, lam);
+  std::vector<int2> chunks;
+  for (int q = 0; q < nj; ++q)
+    for (int i0 = 0; i0 < jobs[q].n; i0 += kBisectThreads) chunks.push_back(make_int2(q, i0));
+  int2 *dch = scratch.get<int2>(chunks.size());
+  UDMRG_CHECK_CUDA(cudaMemcpyAsync(dch, chunks.data(), chunks.size() * sizeof(int2),
+                                   cudaMemcpyHostToDevice, ctx.stream));
+  if (!chunks.empty())
+    bisect_kernel<<<(int)chunks.size(), kBisectThreads, bsmem, ctx.stream>>>(
+        wk.jobs, dch, wk.d, wk.e, wk.scale, lam);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches += 2;
   int hstat = 0;
@@ -508,34 +528,27 @@ void sym_eig_vectors(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJob>
       }
     }
   }
-  // back-transformation by the reflectors
+  // back-transformation by the reflectors, 32 columns per block
   {
-    std::vector<int64_t> zo(nj), zl(nj);
-    std::vector<int32_t> kc(nj);
-    int kmax = 0;
-    for (int q = 0; q < nj; ++q) {
-      zo[q] = z_off[q];
-      zl[q] = z_ld[q];
-      kc[q] = (int32_t)k[q];
-      kmax = std::max<int>(kmax, (int)k[q]);
+    std::vector<BackChunk> bt;
+    for (int q = 0; q < nj; ++q)
+      for (int64_t c0 = 0; c0 < k[q]; c0 += 32)
+        bt.push_back(BackChunk{z_off[q], z_ld[q], q, (int32_t)c0,
+                               (int32_t)std::min<int64_t>(32, k[q] - c0), 0});
+    if (!bt.empty()) {
+      BackChunk *dbt = scratch.get<BackChunk>(bt.size());
+      UDMRG_CHECK_CUDA(cudaMemcpyAsync(dbt, bt.data(), bt.size() * sizeof(BackChunk),
+                                       cudaMemcpyHostToDevice, ctx.stream));
+      const size_t smem = (size_t)nmax * sizeof(double);
+      if (smem > 48 * 1024)
+        UDMRG_CHECK_CUDA(cudaFuncSetAttribute(backtransform_kernel,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem));
+      backtransform_kernel<<<(int)bt.size(), kBackThreads, smem, ctx.stream>>>(wk.jobs, dbt, G,
+                                                                              wk.tau, Z);
+      UDMRG_CHECK_CUDA(cudaGetLastError());
+      ctx.launches++;
     }
-    int64_t *dzo = scratch.get<int64_t>(nj), *dzl = scratch.get<int64_t>(nj);
-    int32_t *dkc = scratch.get<int32_t>(nj);
-    UDMRG_CHECK_CUDA(
-        cudaMemcpyAsync(dzo, zo.data(), nj * sizeof(int64_t), cudaMemcpyHostToDevice, ctx.stream));
-    UDMRG_CHECK_CUDA(
-        cudaMemcpyAsync(dzl, zl.data(), nj * sizeof(int64_t), cudaMemcpyHostToDevice, ctx.stream));
-    UDMRG_CHECK_CUDA(
-        cudaMemcpyAsync(dkc, kc.data(), nj * sizeof(int32_t), cudaMemcpyHostToDevice, ctx.stream));
-    const size_t smem = ((size_t)nmax + kmax) * sizeof(double);
-    if (smem > 48 * 1024)
-      UDMRG_CHECK_CUDA(cudaFuncSetAttribute(backtransform_kernel,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)smem));
-    backtransform_kernel<<<nj, kBackThreads, smem, ctx.stream>>>(wk.jobs, dzo, dkc, dzl, G, wk.tau,
-                                                                 Z);
-    UDMRG_CHECK_CUDA(cudaGetLastError());
-    ctx.launches++;
   }
   ctx.sync();  // host vectors above must outlive the uploads
 }

@@ -26,10 +26,14 @@ __global__ void fill_normal_kernel(double *__restrict__ x, int64_t n, uint64_t s
   }
 }
 
-// In place: S (n x n, symmetric PSD, row-major) -> R^{-1} where S = R^T R,
-// R upper triangular.  Pivots below rel_tol * max diag drop their direction
-// (row/column of R^{-1} set to zero), which handles rank-deficient sketches.
-// One CTA per job; the matrix stays in global memory (L1/L2 resident).
+// S (n x n, symmetric PSD, row-major) -> R^{-T} (R^{-1} transposed, into
+// work) where S = R^T R,
+// R upper triangular (kept in S's upper triangle).  Pivots below
+// rel_tol * max diag drop their direction (row/column of R^{-1} set to zero),
+// which handles rank-deficient sketches.  One CTA per job; the matrix stays in
+// global memory (L1/L2 resident).  The trailing update runs one warp per row
+// over the upper triangle; R^{-1} is built row by row from the bottom, all
+// columns of a row in parallel.
 __global__ void chol_inv_kernel(const EigJob *__restrict__ jobs, double *__restrict__ S_all,
                                 double *__restrict__ work_all, double rel_tol) {
   const EigJob job = jobs[blockIdx.x];
@@ -38,6 +42,7 @@ __global__ void chol_inv_kernel(const EigJob *__restrict__ jobs, double *__restr
   double *S = S_all + job.g_off;
   double *Ri = work_all + job.g_off;  // R^{-1}
   const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
   __shared__ double dmax;
   __shared__ double piv;
   if (tid == 0) {
@@ -55,31 +60,40 @@ __global__ void chol_inv_kernel(const EigJob *__restrict__ jobs, double *__restr
     }
     __syncthreads();
     const double p = piv;
-    for (int j = k + 1 + tid; j < n; j += nt) S[(int64_t)k * n + j] = p > 0 ? S[(int64_t)k * n + j] / p : 0.0;
+    const double ip = p > 0 ? 1.0 / p : 0.0;
+    for (int j = k + 1 + tid; j < n; j += nt) S[(int64_t)k * n + j] *= ip;
     __syncthreads();
     // trailing update S[i][j] -= R[k][i] R[k][j] for k < i <= j
-    const int m = n - k - 1;
-    for (int64_t e = tid; e < (int64_t)m * m; e += nt) {
-      const int i = k + 1 + (int)(e / m), j = k + 1 + (int)(e % m);
-      if (j >= i) S[(int64_t)i * n + j] -= S[(int64_t)k * n + i] * S[(int64_t)k * n + j];
-    }
+    if (p > 0)
+      for (int i = k + 1 + warp; i < n; i += nwarp) {
+        const double rki = S[(int64_t)k * n + i];
+        double *si = S + (int64_t)i * n;
+        const double *rk = S + (int64_t)k * n;
+        for (int j = i + lane; j < n; j += 32) si[j] -= rki * rk[j];
+      }
     __syncthreads();
   }
-  // R^{-1} by back substitution, column by column (upper triangular)
-  for (int64_t e = tid; e < (int64_t)n * n; e += nt) Ri[e] = 0.0;
+  // R^{-1}, stored transposed (RiT[j][k] = R^{-1}[k][j]): row i from the rows
+  // below, R^{-1}[i][j] = -(sum_{i<k<=j} R[i][k] R^{-1}[k][j]) / R[i][i];
+  // one warp per column j, lanes over k (contiguous in both R and RiT)
+  double *RiT = Ri;
+  for (int64_t e = tid; e < (int64_t)n * n; e += nt) RiT[e] = 0.0;
   __syncthreads();
-  for (int j = tid; j < n; j += nt) {
-    // solve R x = e_j for column j of R^{-1}
-    const double djj = S[(int64_t)j * n + j];
-    if (djj == 0.0) continue;
-    Ri[(int64_t)j * n + j] = 1.0 / djj;
-    for (int i = j - 1; i >= 0; --i) {
-      const double dii = S[(int64_t)i * n + i];
-      if (dii == 0.0) continue;
-      double s = 0.0;
-      for (int k = i + 1; k <= j; ++k) s += S[(int64_t)i * n + k] * Ri[(int64_t)k * n + j];
-      Ri[(int64_t)i * n + j] = -s / dii;
+  for (int i = n - 1; i >= 0; --i) {
+    const double dii = S[(int64_t)i * n + i];
+    if (dii != 0.0) {
+      const double inv = 1.0 / dii;
+      const double *ri = S + (int64_t)i * n;
+      if (tid == 0) RiT[(int64_t)i * n + i] = inv;
+      for (int j = i + 1 + warp; j < n; j += nwarp) {
+        const double *xj = RiT + (int64_t)j * n;
+        double acc = 0.0;
+        for (int k = i + 1 + lane; k <= j; k += 32) acc += ri[k] * xj[k];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) RiT[(int64_t)j * n + i] = -acc * inv;
+      }
     }
+    __syncthreads();
   }
 }
 

@@ -515,14 +515,16 @@ SvdResult svd_trunc_sketch(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv
       run_gemm(ctx, g, kF64, Mbuf, yin, zout, 1.0, 0.0);
     };
     // small per-sector products: out(rows x s) = in(rows x s) * S(s x s)
+    // (S^T when trans: S stored row-major as its transpose)
     auto mult_small = [&](const double *in, const double *S, double *out,
-                          const std::vector<int64_t> &off, bool on_y) {
+                          const std::vector<int64_t> &off, bool on_y, bool trans = false) {
       GemmPlan h;
       h.ctx = &ctx;
       for (int a = 0; a < na; ++a) {
         const XView x = xview(secs[act[a]], left);
         const int64_t rows = on_y ? x.xr : x.xc, sq = s[act[a]];
-        gemm_add_simple(h, off[a], rows, sq, sq, off[a], sq, 1, soff[a], sq, 1, false);
+        gemm_add_simple(h, off[a], rows, sq, sq, off[a], sq, 1, soff[a], trans ? 1 : sq,
+                        trans ? sq : 1, false);
       }
       gemm_finalize(h);
       run_gemm(ctx, h, kF64, in, S, out, 1.0, 0.0);
@@ -540,7 +542,7 @@ SvdResult svd_trunc_sketch(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv
       gemm_finalize(g);
       run_gemm(ctx, g, kF64, bin, bin, Sg, 1.0, 0.0);
       run_chol_inv(ctx, jobs, Sg, Ri, 1e-28);
-      mult_small(bin, Ri, bout, boff, on_y);
+      mult_small(bin, Ri, bout, boff, on_y, true);
     };
     mult_xz(Z, Y, 0.0);
     for (int it = 0; it < sp.power_iters; ++it) {

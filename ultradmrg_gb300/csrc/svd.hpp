@@ -71,7 +71,8 @@ void select_kept(const std::vector<std::vector<double>> &svals, double trunc_err
 void fill_normal(Ctx &ctx, double *x, int64_t n, uint64_t seed);
 // out[f_off + j] = sum_i X[x_off + i * cols + j]^2 for every job (by_row unused)
 void run_col_sumsq(Ctx &ctx, const std::vector<ScaleJob> &jobs, const double *X, double *out);
-// S (per job, n x n PSD) -> R^{-1} with S = R^T R (pivots below rel_tol drop)
+// S (per job, n x n PSD) -> R^{-T} (row-major, i.e. R^{-1} column-major) with
+// S = R^T R (pivots below rel_tol drop)
 void run_chol_inv(Ctx &ctx, const std::vector<EigJob> &jobs, double *S, double *Rinv,
                   double rel_tol);
 
