@@ -75,6 +75,9 @@ typedef struct {
   /* nonzero: the exact block SVD also runs on every randomized SVD's input
    * and judges it (svd_audit_* of the site log; its time is not counted) */
   int64_t svd_audit;
+  /* cost rule: when a randomized SVD's total sketch exceeds this fraction of
+   * the total sector dimension, the exact SVD runs instead (<= 0 or >= 1: off) */
+  double svd_sketch_max_fraction;
 } udmrg_sweep_params;
 
 /* One line of the per-site log printed by TwoSiteFiniteVMPSUpdate
@@ -138,13 +141,19 @@ int udmrg_dag(udmrg_ctx *ctx, const udmrg_tensor *a, udmrg_tensor **out);
  * eff_ham = {L, W_l, W_r, R}; returns a new tensor H_eff * state. */
 int udmrg_eff_ham_mul_two_site_state(udmrg_ctx *ctx, udmrg_tensor *const *eff_ham,
                                      const udmrg_tensor *state, udmrg_tensor **out);
+/* eff_ham_mul_single_site_state (lanczos_vmps_solver_impl.h:291-304):
+ * eff_ham = {L, W, R}; returns a new tensor H_eff * state (rank-3 state). */
+int udmrg_eff_ham_mul_single_site_state(udmrg_ctx *ctx, udmrg_tensor *const *eff_ham,
+                                        const udmrg_tensor *state, udmrg_tensor **out);
 /* LanczosSolver with eff_ham_mul_two_site_state
  * (lanczos_vmps_solver_impl.h:114-248). init_state is not modified. */
 int udmrg_lanczos_solver(udmrg_ctx *ctx, udmrg_tensor *const *eff_ham,
                          const udmrg_tensor *init_state, const udmrg_lanczos_params *params,
                          udmrg_lanczos_res *res);
 /* LanczosExpmvSolver (algorithm/tdvp/lanczos_expmv_solver_impl.h:70-184):
- * exp(-i step H_eff) state for complex tensors; iters returned. */
+ * exp(-i step H_eff) state for complex tensors; iters returned.  A rank-4
+ * state uses eff_ham_mul_two_site_state (eff_ham = {L, W_l, W_r, R}), a
+ * rank-3 state eff_ham_mul_single_site_state (eff_ham = {L, W, R}). */
 int udmrg_lanczos_expmv_solver(udmrg_ctx *ctx, udmrg_tensor *const *eff_ham,
                                const udmrg_tensor *init_state, double step,
                                const udmrg_lanczos_params *params, int64_t *iters,
@@ -191,6 +200,50 @@ int udmrg_two_site_finite_vmps(udmrg_ctx *ctx, int64_t N, udmrg_tensor **mps,
                                double *e0, udmrg_site_log *log, int64_t log_cap,
                                int64_t *log_len);
 
+/* ---- FiniteDMRG over a matrix-representation MPO ------------------------ */
+/* One site of MatReprMPO (one_dim_tn/mpo/mat_repr_mpo.h:21, a SparMat of
+ * one-site operators): rows x cols, nnz non-null elements at (x[n], y[n])
+ * holding the operator tensors {pb_in, pb_out} ops[n]. */
+typedef struct {
+  int64_t rows, cols, nnz;
+  const int64_t *x, *y;
+  udmrg_tensor *const *ops;
+} udmrg_mat_repr_site;
+/* FiniteDMRG(mps, mat_repr_mpo, sweep_params) (algorithm/dmrg/dmrg_impl.h:504-511):
+ * the super-block matvec sum_j sum_k (W_r(j,k) x R_k)[sum_i (L_i x W_l(i,j)) psi]
+ * is the two-site matvec with the MPO bond split into channels, so the matrix
+ * representation becomes MPO tensors (channels of equal quantum number in one
+ * bond sector) and the two-site sweep runs on them; returns the last energy. */
+int udmrg_finite_dmrg(udmrg_ctx *ctx, int64_t N, udmrg_tensor **mps,
+                      const udmrg_mat_repr_site *mro, const udmrg_sweep_params *params,
+                      double *e0, udmrg_site_log *log, int64_t log_cap, int64_t *log_len);
+
+/* ---- two-site TDVP ----------------------------------------------------- */
+/* TDVPEvolveParams (algorithm/tdvp/tdvp_evolve_params.h:20-85), the part the
+ * time evolution itself uses: time step tau, number of steps (sweeps), bond
+ * dimension bounds, truncation error and Krylov parameters.  The operator
+ * insertion and the measurements of TwoSiteFiniteTDVP are the caller's. */
+typedef struct {
+  double tau;
+  int64_t steps;
+  int64_t Dmin, Dmax;
+  double trunc_err;
+  udmrg_lanczos_params lancz_params;
+} udmrg_tdvp_params;
+typedef struct {
+  int64_t step, site, kind; /* kind 2: two-site forward, 1: single-site backward */
+  double trunc_err;
+  int64_t D, iters;
+  double ee, lancz_sec, tot_sec;
+} udmrg_tdvp_log;
+/* TwoSiteFiniteTDVP time stepping (two_site_update_finite_tdvp_impl.h:123-531):
+ * brings the MPS to right-canonical form (centre at site 0), then `steps`
+ * TwoSiteFiniteTDVPSweep sweeps; tensors become complex and are replaced in
+ * place. */
+int udmrg_two_site_finite_tdvp(udmrg_ctx *ctx, int64_t N, udmrg_tensor **mps,
+                               udmrg_tensor *const *mpo, const udmrg_tdvp_params *params,
+                               udmrg_tdvp_log *log, int64_t log_cap, int64_t *log_len);
+
 /* ---- learned rank predictor (no counterpart in the reference) --------------- */
 /* Two-layer MLP (n_in = 70 features -> 128 ReLU -> 1) predicting, for one
  * bond sector, y = log2(1 + kept states) from the sector's spectrum at the
@@ -207,6 +260,8 @@ int udmrg_rank_model_sizes(int *n_in, int *n_hidden, int *n_params);
 int udmrg_rank_model_create(udmrg_ctx *ctx, uint64_t seed, udmrg_rank_model **out);
 int udmrg_rank_model_destroy(udmrg_rank_model *m);
 int udmrg_rank_model_forget(udmrg_rank_model *m);
+/* dst takes a copy of src's bond history (to run several sweeps from one state). */
+int udmrg_rank_model_copy_history(udmrg_rank_model *dst, const udmrg_rank_model *src);
 /* Parameters: W1 (hidden x in, row-major) | b1 | w2 | b2, n_params floats. */
 int udmrg_rank_model_get_params(udmrg_rank_model *m, float *params);
 int udmrg_rank_model_set_params(udmrg_rank_model *m, const float *params);

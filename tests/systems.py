@@ -72,3 +72,52 @@ def max_block_diff(gpu, ref):
             diff = max(diff, float(np.max(np.abs(g))))
     scale = max(1e-300, max(float(np.max(np.abs(v))) for v in ref.blocks.values()))
     return diff, scale
+
+
+# ---- free fermions (TDVP pins, tests/test_algorithm/test_two_site_finite_tdvp.cc:82-150) ----
+
+def op_tensor(op, pb, dtype=np.complex128):
+    """Operator tensor {pb_in, pb_out} of an ``models.Operator``."""
+    from ultradmrg_gb300.tensor_data import BlockTensorData
+    t = BlockTensorData([pb.inverse(), pb], {}, dtype)
+    for (i, o) in np.argwhere(op.mat != 0):
+        t.set_elem((int(i), int(o)), op.mat[i, o])
+    return t
+
+
+def act_operator(mps, op_t, inst_t, site):
+    """``ActOperatorOnMps``: op on ``site``, the string operator on every site
+    left of it (two_site_update_finite_tdvp_impl.h:25-54)."""
+    out = list(mps)
+    for i, o in [(site, op_t)] + [(j, inst_t) for j in range(site - 1, -1, -1)]:
+        t = bs.contract(o, out[i], [0], [1])  # (s_out, l, r)
+        out[i] = bs.transpose(t, [1, 0, 2])
+    return out
+
+
+def mps_dense(mps):
+    """The state vector (shape (d,)*N) of a short MPS."""
+    v = mps[0].to_dense()[0]  # (s, r)
+    for A in mps[1:]:
+        v = np.tensordot(v, A.to_dense(), axes=([v.ndim - 1], [0]))
+    return v[..., 0]
+
+
+def apply_dense(v, mat, site, string=None):
+    """(op ket)_out = sum_in mat[in, out] ket_in on ``site`` (and the string left of it)."""
+    ops = [(site, mat)] + ([(j, string) for j in range(site)] if string is not None else [])
+    for j, m in ops:
+        v = np.moveaxis(np.tensordot(m, v, axes=([0], [j])), 0, j)
+    return v
+
+
+def free_fermion_green(time, L, x1, x2):
+    """<GS| c_{x2}(t) c^dag_{x1}(0) |GS> of the open chain (H = -sum c^dag c + h.c.),
+    half filling (test_two_site_finite_tdvp.cc:82-101)."""
+    res = 0j
+    for k in range(1, L + 1):
+        eps = -2 * np.cos(k * np.pi / (L + 1))
+        if eps > 0:
+            res += (np.exp(-1j * eps * time) * np.sin(k * np.pi / (L + 1) * (x1 + 1)) *
+                    np.sin(k * np.pi / (L + 1) * (x2 + 1)))
+    return res * 2.0 / (L + 1)

@@ -33,7 +33,7 @@ class SweepParams(C.Structure):
     _fields_ = [("sweeps", C.c_int64), ("Dmin", C.c_int64), ("Dmax", C.c_int64),
                 ("trunc_err", C.c_double), ("lancz_params", LanczosParams),
                 ("svd_mode", C.c_int64), ("svd_oversample", C.c_int64),
-                ("svd_audit", C.c_int64)]
+                ("svd_audit", C.c_int64), ("svd_sketch_max_fraction", C.c_double)]
 
 
 class SiteLog(C.Structure):
@@ -43,6 +43,22 @@ class SiteLog(C.Structure):
                 ("tot_sec", C.c_double), ("matvec_flops", C.c_double),
                 ("svd_sketch_total", C.c_int64), ("svd_grow_rounds", C.c_int64),
                 ("svd_audit_err", C.c_double), ("svd_audit_kept_diff", C.c_int64)]
+
+
+class TdvpParams(C.Structure):
+    _fields_ = [("tau", C.c_double), ("steps", C.c_int64), ("Dmin", C.c_int64),
+                ("Dmax", C.c_int64), ("trunc_err", C.c_double), ("lancz_params", LanczosParams)]
+
+
+class TdvpLog(C.Structure):
+    _fields_ = [("step", C.c_int64), ("site", C.c_int64), ("kind", C.c_int64),
+                ("trunc_err", C.c_double), ("D", C.c_int64), ("iters", C.c_int64),
+                ("ee", C.c_double), ("lancz_sec", C.c_double), ("tot_sec", C.c_double)]
+
+
+class MatReprSite(C.Structure):
+    _fields_ = [("rows", C.c_int64), ("cols", C.c_int64), ("nnz", C.c_int64),
+                ("x", c_int64_p), ("y", c_int64_p), ("ops", c_void_pp)]
 
 
 # name -> argtypes (all return int status)
@@ -69,6 +85,13 @@ SIGNATURES = {
                               c_void_pp],
     "udmrg_dag": [C.c_void_p, C.c_void_p, c_void_pp],
     "udmrg_eff_ham_mul_two_site_state": [C.c_void_p, c_void_pp, C.c_void_p, c_void_pp],
+    "udmrg_eff_ham_mul_single_site_state": [C.c_void_p, c_void_pp, C.c_void_p, c_void_pp],
+    "udmrg_finite_dmrg": [C.c_void_p, C.c_int64, c_void_pp, C.POINTER(MatReprSite),
+                          C.POINTER(SweepParams), c_double_p, C.POINTER(SiteLog), C.c_int64,
+                          c_int64_p],
+    "udmrg_two_site_finite_tdvp": [C.c_void_p, C.c_int64, c_void_pp, c_void_pp,
+                                   C.POINTER(TdvpParams), C.POINTER(TdvpLog), C.c_int64,
+                                   c_int64_p],
     "udmrg_lanczos_solver": [C.c_void_p, c_void_pp, C.c_void_p, C.POINTER(LanczosParams),
                              C.POINTER(LanczosRes)],
     "udmrg_lanczos_expmv_solver": [C.c_void_p, c_void_pp, C.c_void_p, C.c_double,
@@ -96,6 +119,7 @@ SIGNATURES = {
     "udmrg_rank_model_create": [C.c_void_p, C.c_uint64, c_void_pp],
     "udmrg_rank_model_destroy": [C.c_void_p],
     "udmrg_rank_model_forget": [C.c_void_p],
+    "udmrg_rank_model_copy_history": [C.c_void_p, C.c_void_p],
     "udmrg_rank_model_get_params": [C.c_void_p, c_float_p],
     "udmrg_rank_model_set_params": [C.c_void_p, c_float_p],
     "udmrg_rank_model_predict": [C.c_void_p, C.c_int64, c_float_p, c_float_p],

@@ -253,6 +253,13 @@ def lanczos_solver(ctx, eff_ham, init_state, error=1e-7, max_iterations=200,
                          int(r.fp64_matvecs))
 
 
+def eff_ham_mul_single_site_state(ctx, eff_ham: Sequence[DeviceTensor], state: DeviceTensor):
+    """``eff_ham_mul_single_site_state`` (eff_ham = [L, W, R]) on the device."""
+    h = C.c_void_p()
+    call("udmrg_eff_ham_mul_single_site_state", ctx.h, _handles(eff_ham), state.h, C.byref(h))
+    return _new(ctx, h)
+
+
 def lanczos_expmv_solver(ctx, eff_ham, init_state, step, error=1e-10, max_iterations=20):
     p = _lib.LanczosParams(error, max_iterations, PREC_FP64)
     it = C.c_int64()
@@ -316,13 +323,15 @@ class FiniteVMPSSweepParams:
     svd_mode: int = 0  # 0 exact, 1 randomized (previous sector dims), 2 randomized (learned)
     svd_oversample: int = 8
     svd_audit: bool = False  # exact SVD judges every randomized one (untimed)
+    svd_sketch_max_fraction: float = 1.0  # randomized SVD only below this sketch fraction
 
 
 def _sweep_params(params: FiniteVMPSSweepParams):
     return _lib.SweepParams(params.sweeps, params.Dmin, params.Dmax, params.trunc_err,
                             _lib.LanczosParams(params.lanczos_error,
                                                params.lanczos_max_iterations, params.precision),
-                            params.svd_mode, params.svd_oversample, int(params.svd_audit))
+                            params.svd_mode, params.svd_oversample, int(params.svd_audit),
+                            params.svd_sketch_max_fraction)
 
 
 def _log_rows(log, n):
@@ -410,6 +419,10 @@ class RankModel:
         """Drop the bond history of the last chain swept with this model."""
         call("udmrg_rank_model_forget", self.h)
 
+    def copy_history_from(self, other: "RankModel"):
+        """Take a copy of another model's bond history."""
+        call("udmrg_rank_model_copy_history", self.h, other.h)
+
     def close(self):
         if self.h:
             call("udmrg_rank_model_destroy", self.h)
@@ -452,6 +465,65 @@ def two_site_finite_vmps_learned(ctx, mps: List[DeviceTensor], mpo: List[DeviceT
          C.byref(ns), C.byref(e0), log, lcap, C.byref(nlog))
     n = min(ns.value, xs.shape[0])
     return float(e0.value), _log_rows(log, min(lcap, nlog.value)), xs[:n], ys[:n]
+
+
+def finite_dmrg(ctx, mps: List[DeviceTensor], mat_repr, params: FiniteVMPSSweepParams):
+    """``FiniteDMRG(mps, mat_repr_mpo, sweep_params)``: ``mat_repr`` is a
+    MatReprMPO as returned by ``models.mat_repr_mpo`` (per site rows, cols and
+    the (x, y, operator tensor) elements).  Updates ``mps`` in place; returns
+    (e0, per-site log)."""
+    N = len(mps)
+    keep, sites = [], (_lib.MatReprSite * N)()
+    for i, (rows, cols, elems) in enumerate(mat_repr):
+        ops = [DeviceTensor.from_data(ctx, t) for _, _, t in elems]
+        xs = np.array([x for x, _, _ in elems], np.int64)
+        ys = np.array([y for _, y, _ in elems], np.int64)
+        hs = _handles(ops)
+        keep += [ops, xs, ys, hs]
+        sites[i] = _lib.MatReprSite(rows, cols, len(elems), xs.ctypes.data_as(_lib.c_int64_p),
+                                    ys.ctypes.data_as(_lib.c_int64_p), hs)
+    sp = _sweep_params(params)
+    cap = 2 * N * max(params.sweeps, 1)
+    log = (_lib.SiteLog * cap)()
+    e0, nlog = C.c_double(), C.c_int64()
+    call("udmrg_finite_dmrg", ctx.h, N, _handles(mps), sites, C.byref(sp), C.byref(e0), log, cap,
+         C.byref(nlog))
+    return float(e0.value), _log_rows(log, min(cap, nlog.value))
+
+
+@dataclass
+class TDVPEvolveParams:
+    """The time-stepping part of ``TDVPEvolveParams`` (tdvp_evolve_params.h:20-85)."""
+
+    tau: float
+    steps: int
+    Dmin: int
+    Dmax: int
+    trunc_err: float
+    lanczos_error: float = 1e-10
+    lanczos_max_iterations: int = 20
+
+
+def two_site_finite_tdvp(ctx, mps: List[DeviceTensor], mpo: List[DeviceTensor],
+                         params: TDVPEvolveParams):
+    """``TwoSiteFiniteTDVP`` time stepping: right-canonicalises ``mps`` (centre
+    at site 0), then ``params.steps`` sweeps; ``mps`` is updated in place
+    (complex).  Returns the per-update log."""
+    N = len(mps)
+    tp = _lib.TdvpParams(params.tau, params.steps, params.Dmin, params.Dmax, params.trunc_err,
+                         _lib.LanczosParams(params.lanczos_error, params.lanczos_max_iterations,
+                                            0))
+    cap = max(1, params.steps) * (4 * N)
+    log = (_lib.TdvpLog * cap)()
+    nlog = C.c_int64()
+    call("udmrg_two_site_finite_tdvp", ctx.h, N, _handles(mps), _handles(mpo), C.byref(tp), log,
+         cap, C.byref(nlog))
+    rows = []
+    for i in range(min(cap, nlog.value)):
+        L = log[i]
+        rows.append(dict(step=L.step, site=L.site, kind=L.kind, trunc_err=L.trunc_err, D=L.D,
+                         iters=L.iters, ee=L.ee, lancz_sec=L.lancz_sec, tot_sec=L.tot_sec))
+    return rows
 
 
 def trivial_env_data(mps_ten: BlockTensorData, mpo_ten: BlockTensorData, side: str):

@@ -6,6 +6,7 @@
 
 #include "../../include/ultradmrg_gb300.h"
 #include "dmrg.hpp"
+#include "matrepr.hpp"
 #include "svd.hpp"
 #include "tc_gemm.hpp"
 
@@ -265,8 +266,8 @@ struct EffHam {
   TensorPtr keep[4];
 };
 
-void prepare_eff_ham(Ctx &ctx, udmrg_tensor *const *eff_ham, DType dt, EffHam &e) {
-  for (int i = 0; i < 4; ++i) {
+void prepare_eff_ham(Ctx &ctx, udmrg_tensor *const *eff_ham, DType dt, EffHam &e, int nops = 4) {
+  for (int i = 0; i < nops; ++i) {
     const BTensor &t = T(eff_ham[i]);
     if (t.dtype == dt) {
       e.op[i] = &t;
@@ -288,6 +289,23 @@ int udmrg_eff_ham_mul_two_site_state(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
     EffHam e;
     prepare_eff_ham(ctx, eff_ham, psi.dtype, e);
     auto mv = plan_matvec2(ctx, *e.op[0], *e.op[1], *e.op[2], *e.op[3], psi);
+    auto in = embed(ctx, psi, *mv->sstruct);
+    auto res = mv->sstruct->clone_struct();
+    res->alloc_data();
+    mv->apply(in->data, res->data);
+    ctx.sync();
+    *out = wrap(std::move(res));
+  });
+}
+
+int udmrg_eff_ham_mul_single_site_state(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
+                                        const udmrg_tensor *state, udmrg_tensor **out) {
+  return guarded([&] {
+    Ctx &ctx = c->ctx;
+    const BTensor &psi = T(state);
+    EffHam e;
+    prepare_eff_ham(ctx, eff_ham, psi.dtype, e, 3);
+    auto mv = plan_matvec1(ctx, *e.op[0], *e.op[1], *e.op[2], psi);
     auto in = embed(ctx, psi, *mv->sstruct);
     auto res = mv->sstruct->clone_struct();
     res->alloc_data();
@@ -331,8 +349,10 @@ int udmrg_lanczos_expmv_solver(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
       psi = promoted.get();
     }
     EffHam e;
-    prepare_eff_ham(ctx, eff_ham, kC128, e);
-    auto mv = plan_matvec2(ctx, *e.op[0], *e.op[1], *e.op[2], *e.op[3], *psi);
+    const bool one = psi->rank() == 3;  // single-site form: eff_ham = {L, W, R}
+    prepare_eff_ham(ctx, eff_ham, kC128, e, one ? 3 : 4);
+    auto mv = one ? plan_matvec1(ctx, *e.op[0], *e.op[1], *e.op[2], *psi)
+                  : plan_matvec2(ctx, *e.op[0], *e.op[1], *e.op[2], *e.op[3], *psi);
     LanczosParams p{params->error, params->max_iterations};
     auto r = lanczos_expmv(ctx, *mv, *psi, step, p);
     if (iters) *iters = r.iters;
@@ -424,6 +444,10 @@ int udmrg_two_site_update(udmrg_ctx *c, const udmrg_tensor *lenv, const udmrg_te
     p.svd_mode = (int)params->svd_mode;
     p.svd_oversample = params->svd_oversample;
     p.svd_audit = params->svd_audit != 0;
+    p.svd_sketch_max_fraction = params->svd_sketch_max_fraction > 0.0 &&
+                                        params->svd_sketch_max_fraction < 1.0
+                                    ? params->svd_sketch_max_fraction
+                                    : 1.0;
     SiteLog s{};
     auto r = two_site_update_local(c->ctx, T(lenv), T(renv), T(mps_l), T(mps_r), T(mpo_l),
                                    T(mpo_r), p, dir, &s);
@@ -471,6 +495,13 @@ int udmrg_rank_model_forget(udmrg_rank_model *m) {
   return guarded([&] {
     m->hist.prev.clear();
     m->hist.prev_kept.clear();
+  });
+}
+
+int udmrg_rank_model_copy_history(udmrg_rank_model *dst, const udmrg_rank_model *src) {
+  return guarded([&] {
+    dst->hist.prev = src->hist.prev;
+    dst->hist.prev_kept = src->hist.prev_kept;
   });
 }
 
@@ -599,6 +630,10 @@ int udmrg_two_site_finite_vmps_learned(udmrg_ctx *c, int64_t N, udmrg_tensor **m
     p.svd_mode = (int)params->svd_mode;
     p.svd_oversample = params->svd_oversample;
     p.svd_audit = params->svd_audit != 0;
+    p.svd_sketch_max_fraction = params->svd_sketch_max_fraction > 0.0 &&
+                                        params->svd_sketch_max_fraction < 1.0
+                                    ? params->svd_sketch_max_fraction
+                                    : 1.0;
     std::vector<SiteLog> lg;
     const double e = two_site_finite_vmps(c->ctx, m, w, p, &lg, use_learn ? &learn : nullptr);
     c->ctx.sync();
@@ -614,6 +649,79 @@ int udmrg_two_site_finite_vmps_learned(udmrg_ctx *c, int64_t N, udmrg_tensor **m
     if (log)
       for (int64_t i = 0; i < std::min<int64_t>(log_cap, (int64_t)lg.size()); ++i) {
         log[i] = site_log(lg[i]);
+      }
+  });
+}
+
+int udmrg_finite_dmrg(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
+                      const udmrg_mat_repr_site *mro, const udmrg_sweep_params *params,
+                      double *e0, udmrg_site_log *log, int64_t log_cap, int64_t *log_len) {
+  return guarded([&] {
+    std::vector<MatReprSite> sites(N);
+    for (int64_t i = 0; i < N; ++i) {
+      sites[i].rows = mro[i].rows;
+      sites[i].cols = mro[i].cols;
+      for (int64_t n = 0; n < mro[i].nnz; ++n) {
+        sites[i].x.push_back(mro[i].x[n]);
+        sites[i].y.push_back(mro[i].y[n]);
+        sites[i].ops.push_back(&T(mro[i].ops[n]));
+      }
+    }
+    auto W = mat_repr_to_mpo(c->ctx, sites);
+    std::vector<const BTensor *> w(N);
+    for (int64_t i = 0; i < N; ++i) w[i] = W[i].get();
+    std::vector<TensorPtr> m(N);
+    for (int64_t i = 0; i < N; ++i) m[i] = T(mps[i]).clone();
+    SweepParams p;
+    p.sweeps = params->sweeps;
+    p.Dmin = params->Dmin;
+    p.Dmax = params->Dmax;
+    p.trunc_err = params->trunc_err;
+    p.lancz = {params->lancz_params.error, params->lancz_params.max_iterations,
+               (int)params->lancz_params.matvec_precision};
+    p.svd_mode = (int)params->svd_mode;
+    p.svd_oversample = params->svd_oversample;
+    p.svd_audit = params->svd_audit != 0;
+    p.svd_sketch_max_fraction = params->svd_sketch_max_fraction > 0.0 &&
+                                        params->svd_sketch_max_fraction < 1.0
+                                    ? params->svd_sketch_max_fraction
+                                    : 1.0;
+    std::vector<SiteLog> lg;
+    const double e = two_site_finite_vmps(c->ctx, m, w, p, &lg, nullptr);
+    c->ctx.sync();
+    for (int64_t i = 0; i < N; ++i) mps[i]->t = std::move(m[i]);
+    if (e0) *e0 = e;
+    if (log_len) *log_len = (int64_t)lg.size();
+    if (log)
+      for (int64_t i = 0; i < std::min<int64_t>(log_cap, (int64_t)lg.size()); ++i)
+        log[i] = site_log(lg[i]);
+  });
+}
+
+int udmrg_two_site_finite_tdvp(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
+                               udmrg_tensor *const *mpo, const udmrg_tdvp_params *params,
+                               udmrg_tdvp_log *log, int64_t log_cap, int64_t *log_len) {
+  return guarded([&] {
+    UDMRG_REQUIRE(params->steps >= 0, "tdvp: negative step count");
+    std::vector<TensorPtr> m(N);
+    for (int64_t i = 0; i < N; ++i) m[i] = T(mps[i]).clone();
+    std::vector<const BTensor *> w(N);
+    for (int64_t i = 0; i < N; ++i) w[i] = &T(mpo[i]);
+    TdvpParams p;
+    p.tau = params->tau;
+    p.Dmin = params->Dmin;
+    p.Dmax = params->Dmax;
+    p.trunc_err = params->trunc_err;
+    p.lancz = {params->lancz_params.error, params->lancz_params.max_iterations, kPrecFP64};
+    std::vector<TdvpLog> lg;
+    two_site_finite_tdvp(c->ctx, m, w, p, params->steps, &lg);
+    c->ctx.sync();
+    for (int64_t i = 0; i < N; ++i) mps[i]->t = std::move(m[i]);
+    if (log_len) *log_len = (int64_t)lg.size();
+    if (log)
+      for (int64_t i = 0; i < std::min<int64_t>(log_cap, (int64_t)lg.size()); ++i) {
+        const TdvpLog &t = lg[i];
+        log[i] = {t.step, t.site, t.kind, t.trunc_err, t.D, t.iters, t.ee, t.lancz_sec, t.tot_sec};
       }
   });
 }

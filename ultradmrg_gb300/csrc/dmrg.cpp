@@ -120,6 +120,38 @@ std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTens
   return mv;
 }
 
+std::unique_ptr<MatvecPlan> plan_matvec1(Ctx &ctx, const BTensor &L, const BTensor &W,
+                                         const BTensor &R, const BTensor &psi0) {
+  UDMRG_REQUIRE(psi0.rank() == 3 && L.rank() == 3 && R.rank() == 3 && W.rank() == 4,
+                "single-site matvec: expects L(3), W(4), R(3), psi(3)");
+  auto mv = std::make_unique<MatvecPlan>();
+  mv->ctx = &ctx;
+  mv->sites = 1;
+  mv->L = &L;
+  mv->W1 = &W;
+  mv->R = &R;
+  TensorPtr S = psi0.clone_struct();
+  std::vector<int> ca, cb, fa, fb;
+  cyclic_axes(4, 3, 3, 1, 2, ca, cb, fa, fb);
+  for (int it = 0; it < 16; ++it) {
+    mv->p1 = plan_contract_axes(L, *S, {2}, {0});
+    mv->p2 = plan_contract_cyclic(*mv->p1->out, W, 1, 0, 2);
+    auto p4 = plan_contract(*mv->p2->out, R, ca, cb, fa, fb);
+    auto U = struct_union(*S, *p4->out);
+    const bool closed = U->keys == S->keys;
+    S = std::move(U);
+    if (closed) break;
+    UDMRG_REQUIRE(it < 15, "matvec: Krylov block structure did not close");
+  }
+  mv->p4 = plan_contract_into(*mv->p2->out, R, ca, cb, fa, fb, *S, &mv->missing);
+  mv->sstruct = std::move(S);
+  mv->flops = mv->p1->gemm.flops + mv->p2->gemm.flops + mv->p4->gemm.flops;
+  const int es = elem_doubles(psi0.dtype);
+  mv->t1 = (double *)ctx.alloc(std::max<int64_t>(mv->p1->out->size(), 1) * es * sizeof(double));
+  mv->t2 = (double *)ctx.alloc(std::max<int64_t>(mv->p2->out->size(), 1) * es * sizeof(double));
+  return mv;
+}
+
 void MatvecPlan::apply(const double *in, double *out) {
   if (sg) {
     sg->apply(in, out);
@@ -133,11 +165,11 @@ void MatvecPlan::apply_fp64(const double *in, double *out) {
   const int es = elem_doubles(dt);
   run_gemm(*ctx, p1->gemm, dt, L->data, in, t1, 1.0, 0.0);
   run_gemm(*ctx, p2->gemm, dt, t1, W1->data, t2, 1.0, 0.0);
-  run_gemm(*ctx, p3->gemm, dt, t2, W2->data, t3, 1.0, 0.0);
+  if (sites == 2) run_gemm(*ctx, p3->gemm, dt, t2, W2->data, t3, 1.0, 0.0);
   for (int64_t b : missing)
     UDMRG_CHECK_CUDA(cudaMemsetAsync(out + sstruct->offs[b] * es, 0,
                                      sstruct->block_elems(b) * es * sizeof(double), ctx->stream));
-  run_gemm(*ctx, p4->gemm, dt, t3, R->data, out, 1.0, 0.0);
+  run_gemm(*ctx, p4->gemm, dt, sites == 2 ? t3 : t2, R->data, out, 1.0, 0.0);
 }
 
 // ---------------------------------------------------------------------------
@@ -686,6 +718,7 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
   } else {
     SketchParams sp;
     sp.oversample = p.svd_oversample;
+    sp.max_fraction = p.svd_sketch_max_fraction;
     sp.seed = 0x5EEDull + (uint64_t)mps_l.nblocks();
     if (hint) {
       sp.sketch = *hint;
@@ -775,6 +808,117 @@ double two_site_finite_vmps(Ctx &ctx, std::vector<TensorPtr> &mps,
       e0 = two_site_update(ctx, mps, lenvs, renvs, W, p, 'l', i, log, learn);
   }
   return e0;
+}
+
+namespace {
+
+// Two-site forward evolution exp(-i step H_eff) of the pair (l, l+1), truncated
+// SVD, MPS split by direction and one environment update
+// (TwoSiteFiniteTDVPEvolution, two_site_update_finite_tdvp_impl.h:261-417).
+void tdvp_two_site(Ctx &ctx, std::vector<TensorPtr> &mps, std::vector<TensorPtr> &lenvs,
+                   std::vector<TensorPtr> &renvs, const std::vector<const BTensor *> &W,
+                   const TdvpParams &p, char dir, int64_t target, double step, TdvpLog &lg) {
+  const int64_t N = (int64_t)mps.size();
+  int64_t l, r, lenv_len, renv_len;
+  if (dir == 'r') {
+    l = target;
+    r = target + 1;
+    lenv_len = target;
+    renv_len = N - (target + 2);
+  } else {
+    l = target - 1;
+    r = target;
+    lenv_len = target - 1;
+    renv_len = N - target - 1;
+  }
+  const double t0 = now();
+  auto init = contract_axes(ctx, *mps[l], *mps[r], {2}, {0});
+  auto mv = plan_matvec2(ctx, *lenvs[lenv_len], *W[l], *W[r], *renvs[renv_len], *init);
+  auto ex = lanczos_expmv(ctx, *mv, *init, step, p.lancz);
+  mv.reset();
+  init.reset();
+  const double t1 = now();
+  SvdResult sres = svd_trunc(ctx, *ex.expmv, 2, mps[l]->div(), p.trunc_err, p.Dmin, p.Dmax,
+                             dir == 'r' ? kSvdSplitLeft : kSvdSplitRight);
+  ex.expmv.reset();
+  mps[l] = std::move(sres.u);
+  mps[r] = std::move(sres.vt);
+  if (dir == 'r')
+    lenvs[lenv_len + 1] = update_site_lenv(ctx, *lenvs[lenv_len], *mps[target], *W[target]);
+  else
+    renvs[renv_len + 1] = update_site_renv(ctx, *renvs[renv_len], *mps[target], *W[target]);
+  ctx.sync();
+  lg = TdvpLog{0, target, 2, sres.trunc_err, sres.D, ex.iters, sres.ee, t1 - t0, now() - t0};
+}
+
+// Single-site backward evolution exp(+i tau/2 H_eff) of the centre tensor at
+// `site`, without a split (SingleSiteFiniteTDVPBackwardEvolution with
+// dir 'n', two_site_update_finite_tdvp_impl.h:419-531).
+void tdvp_one_site(Ctx &ctx, std::vector<TensorPtr> &mps, std::vector<TensorPtr> &lenvs,
+                   std::vector<TensorPtr> &renvs, const std::vector<const BTensor *> &W,
+                   const TdvpParams &p, int64_t site, double step, TdvpLog &lg) {
+  const int64_t N = (int64_t)mps.size();
+  const double t0 = now();
+  auto mv = plan_matvec1(ctx, *lenvs[site], *W[site], *renvs[N - site - 1], *mps[site]);
+  auto ex = lanczos_expmv(ctx, *mv, *mps[site], step, p.lancz);
+  mv.reset();
+  mps[site] = std::move(ex.expmv);
+  ctx.sync();
+  const double t1 = now();
+  lg = TdvpLog{0, site, 1, 0.0, 0, ex.iters, 0.0, t1 - t0, t1 - t0};
+}
+
+}  // namespace
+
+void two_site_finite_tdvp(Ctx &ctx, std::vector<TensorPtr> &mps,
+                          const std::vector<const BTensor *> &mpo, const TdvpParams &p,
+                          int64_t steps, std::vector<TdvpLog> *log) {
+  const int64_t N = (int64_t)mps.size();
+  UDMRG_REQUIRE(N >= 3 && (int64_t)mpo.size() == N, "tdvp: MPS and MPO sizes differ or N < 3");
+  std::vector<TensorPtr> mpo_c;
+  std::vector<const BTensor *> W = mpo;
+  for (auto &t : mps)
+    if (t->dtype != kC128) t = to_complex(ctx, *t);
+  for (int64_t i = 0; i < N; ++i)
+    if (mpo[i]->dtype != kC128) {
+      mpo_c.push_back(to_complex(ctx, *mpo[i]));
+      W[i] = mpo_c.back().get();
+    }
+  // right-canonical form from the last site down to site 1 (centre at site 0):
+  // mps[i] = (U S) V^T, V^T right-isometric, U S absorbed into mps[i - 1]
+  for (int64_t i = N - 1; i > 0; --i) {
+    SvdResult sr = svd_trunc(ctx, *mps[i], 1, mps[i]->div(), 0.0, 1, INT64_MAX / 4,
+                             kSvdSplitRight);
+    mps[i] = std::move(sr.vt);
+    mps[i - 1] = contract_axes(ctx, *mps[i - 1], *sr.u, {2}, {0});
+  }
+  std::vector<TensorPtr> lenvs(N), renvs(N);
+  renvs[0] = trivial_renv(ctx, *mps[N - 1], *W[N - 1]);
+  for (int64_t i = 1; i <= N - 2; ++i)
+    renvs[i] = update_site_renv(ctx, *renvs[i - 1], *mps[N - i], *W[N - i]);
+  lenvs[0] = trivial_lenv(ctx, *mps[0], *W[0]);
+  const double half = p.tau / 2;
+  TdvpLog lg{};
+  auto put = [&](int64_t st) {
+    lg.step = st;
+    if (log) log->push_back(lg);
+  };
+  for (int64_t st = 0; st < steps; ++st) {
+    for (int64_t i = 0; i < N - 2; ++i) {
+      tdvp_two_site(ctx, mps, lenvs, renvs, W, p, 'r', i, half, lg);
+      put(st);
+      tdvp_one_site(ctx, mps, lenvs, renvs, W, p, i + 1, -half, lg);
+      put(st);
+    }
+    for (int64_t i = N - 1; i > 1; --i) {
+      tdvp_two_site(ctx, mps, lenvs, renvs, W, p, 'l', i, i == N - 1 ? p.tau : half, lg);
+      put(st);
+      tdvp_one_site(ctx, mps, lenvs, renvs, W, p, i - 1, -half, lg);
+      put(st);
+    }
+    tdvp_two_site(ctx, mps, lenvs, renvs, W, p, 'r', 0, half, lg);
+    put(st);
+  }
 }
 
 }  // namespace udmrg

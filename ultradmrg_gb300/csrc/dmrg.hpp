@@ -36,6 +36,7 @@ struct MatvecPlan {
   double *t1 = nullptr, *t2 = nullptr, *t3 = nullptr;
   double flops = 0;  // algorithmic flops of one matvec
   int precision = kPrecFP64;
+  int sites = 2;  // 1: single-site form (L, W1, R; p3 unused)
   std::unique_ptr<SgMatvecPlan> sg;  // the mixed-precision form
   ~MatvecPlan();
   void apply(const double *in, double *out);       // device buffers in sstruct layout
@@ -45,6 +46,12 @@ struct MatvecPlan {
 std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTensor &W1,
                                          const BTensor &W2, const BTensor &R,
                                          const BTensor &psi0, int precision = kPrecFP64);
+
+// H_eff * psi of one site (eff_ham_mul_single_site_state,
+// lanczos_vmps_solver_impl.h:291-304): L * psi, * W (cyclic 1,0,2), * R
+// (cyclic 3,1,2).  FP64 form only.
+std::unique_ptr<MatvecPlan> plan_matvec1(Ctx &ctx, const BTensor &L, const BTensor &W,
+                                         const BTensor &R, const BTensor &psi0);
 
 struct LanczosParams {
   double error = 1e-7;
@@ -103,6 +110,7 @@ struct SweepParams {
   int svd_mode = kSvdExact;
   int64_t svd_oversample = 8;
   bool svd_audit = false;  // judge every randomized SVD by the exact one
+  double svd_sketch_max_fraction = 1.0;  // cost rule of the randomized SVD (1: off)
 };
 
 struct SiteLog {
@@ -156,5 +164,27 @@ struct LearnState {
 double two_site_finite_vmps(Ctx &ctx, std::vector<TensorPtr> &mps,
                             const std::vector<const BTensor *> &mpo, const SweepParams &p,
                             std::vector<SiteLog> *log, LearnState *learn = nullptr);
+
+// Two-site TDVP (two_site_update_finite_tdvp_impl.h:123-531), device
+// resident.  One step is one sweep: two-site forward evolution by tau/2 and
+// single-site backward evolution by -tau/2 from left to right, the pair at the
+// right end by tau, the same from right to left, and the first pair by tau/2.
+struct TdvpParams {
+  double tau = 0.01;
+  int64_t Dmin = 1, Dmax = 1;
+  double trunc_err = 0;
+  LanczosParams lancz;
+};
+struct TdvpLog {
+  int64_t step, site, kind;  // kind 2: two-site forward, 1: single-site backward
+  double trunc_err;
+  int64_t D, iters;
+  double ee, lancz_sec, tot_sec;
+};
+// The MPS is brought to right-canonical form (centre at site 0) first;
+// tensors are complex (real ones are promoted) and replaced in place.
+void two_site_finite_tdvp(Ctx &ctx, std::vector<TensorPtr> &mps,
+                          const std::vector<const BTensor *> &mpo, const TdvpParams &p,
+                          int64_t steps, std::vector<TdvpLog> *log);
 
 }  // namespace udmrg

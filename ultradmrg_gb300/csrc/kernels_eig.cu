@@ -18,6 +18,7 @@
 #include <cmath>
 
 #include "svd.hpp"
+#include "vecops.hpp"
 
 namespace udmrg {
 
@@ -394,12 +395,214 @@ __global__ void backtransform_kernel(const EigJob *__restrict__ jobs,
   }
 }
 
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cmulc(double2 a, double2 b) {  // conj(a) * b
+  return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) {
+  return make_double2(a.x + b.x, a.y + b.y);
+}
+
+// Complex Hermitian version of tridiag_kernel.  Step j (0 <= j <= n-2)
+// reflects the column x = A[j+1.., j] (read as conj of row j) with
+// H = I - tau v v^H, v_0 = 1, beta real, so that H^H x = beta e_0 and the
+// tridiagonal matrix is real; v (r >= 1) is stored in row j at column j+1+r,
+// tau (complex) in tau[lam_off + j].
+__global__ void tridiag_c_kernel(const EigJob *__restrict__ jobs, double2 *__restrict__ G_all,
+                                 double *__restrict__ d_all, double *__restrict__ e_all,
+                                 double2 *__restrict__ tau_all, double *__restrict__ scale_all,
+                                 int *__restrict__ status) {
+  extern __shared__ double2 smc[];
+  __shared__ double red[33];
+  __shared__ double redi[33];
+  __shared__ int bad;
+  const EigJob job = jobs[blockIdx.x];
+  const int n = job.n;
+  if (n == 0) return;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  double2 *A = job.smem ? smc : G_all + job.g_off;
+  double2 *v = smc + (job.smem ? (int64_t)n * n : 0);
+  double2 *w = v + n;
+  double *d = d_all + job.lam_off, *e = e_all + job.lam_off;
+  double2 *tau = tau_all + job.lam_off;
+
+  if (job.smem)
+    for (int64_t x = tid; x < (int64_t)n * n; x += nt) A[x] = G_all[job.g_off + x];
+  double mx = 0.0;
+  int nf = 0;
+  if (tid == 0) bad = 0;
+  for (int64_t x = tid; x < (int64_t)n * n; x += nt) {
+    const double2 g = A[x];
+    nf |= !isfinite(g.x) || !isfinite(g.y);
+    mx = fmax(mx, fmax(fabs(g.x), fabs(g.y)));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    nf |= __shfl_down_sync(0xffffffffu, nf, o);
+  }
+  __syncthreads();
+  if (lane == 0) {
+    red[warp] = mx;
+    if (nf) atomicOr(&bad, 1);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double m = 0.0;
+    for (int i = 0; i < nwarp; ++i) m = fmax(m, red[i]);
+    red[32] = m;
+  }
+  __syncthreads();
+  if (bad) {
+    if (tid == 0) atomicExch(status, 2);
+    return;
+  }
+  const double scale = red[32];
+  if (tid == 0) scale_all[blockIdx.x] = scale;
+  // scale and make exactly Hermitian
+  const double inv = scale > 0.0 ? 1.0 / scale : 0.0;
+  for (int64_t x = tid; x < (int64_t)n * n; x += nt) {
+    const int r = (int)(x / n), c = (int)(x - (int64_t)r * n);
+    if (r < c) {
+      const double2 a = A[x], b = A[(int64_t)c * n + r];
+      const double2 g = make_double2(0.5 * inv * (a.x + b.x), 0.5 * inv * (a.y - b.y));
+      A[x] = g;
+      A[(int64_t)c * n + r] = make_double2(g.x, -g.y);
+    } else if (r == c) {
+      A[x] = make_double2(A[x].x * inv, 0.0);
+    }
+  }
+  __syncthreads();
+
+  for (int j = 0; j + 1 < n; ++j) {
+    const int m = n - j - 1;
+    double2 *rowj = A + (int64_t)j * n;
+    const double2 alpha = make_double2(rowj[j + 1].x, -rowj[j + 1].y);  // x_0
+    double x2 = 0.0;
+    for (int c = j + 2 + tid; c < n; c += nt) x2 += rowj[c].x * rowj[c].x + rowj[c].y * rowj[c].y;
+    x2 = block_sum(x2, red);
+    double2 t = make_double2(0.0, 0.0), sc = make_double2(0.0, 0.0);
+    double beta = alpha.x;
+    if (x2 > 0.0 || alpha.y != 0.0) {
+      beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + x2), alpha.x);
+      t = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
+      const double2 den = make_double2(alpha.x - beta, alpha.y);  // 1 / (alpha - beta)
+      const double dd = den.x * den.x + den.y * den.y;
+      sc = make_double2(den.x / dd, -den.y / dd);
+    }
+    const bool refl = t.x != 0.0 || t.y != 0.0;
+    for (int r = tid; r < m; r += nt) {
+      double2 vr;
+      if (r == 0)
+        vr = make_double2(1.0, 0.0);
+      else if (!refl)
+        vr = make_double2(0.0, 0.0);
+      else
+        vr = cmul(make_double2(rowj[j + 1 + r].x, -rowj[j + 1 + r].y), sc);
+      v[r] = vr;
+      if (r > 0) rowj[j + 1 + r] = vr;
+    }
+    if (tid == 0) {
+      d[j] = rowj[j].x;
+      e[j] = beta;
+      tau[j] = t;
+    }
+    __syncthreads();
+    if (!refl) continue;
+    // w = t * A_t v (one warp per row)
+    for (int r = warp; r < m; r += nwarp) {
+      const double2 *ar = A + (int64_t)(j + 1 + r) * n + (j + 1);
+      double2 acc = make_double2(0.0, 0.0);
+      for (int c = lane; c < m; c += 32) acc = cadd(acc, cmul(ar[c], v[c]));
+      for (int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+      }
+      if (lane == 0) w[r] = cmul(t, acc);
+    }
+    __syncthreads();
+    // K = -1/2 t (w^H v); w += K v
+    double kr = 0.0, ki = 0.0;
+    for (int r = tid; r < m; r += nt) {
+      const double2 q = cmulc(w[r], v[r]);
+      kr += q.x;
+      ki += q.y;
+    }
+    kr = block_sum(kr, red);
+    ki = block_sum(ki, redi);
+    const double2 K = cmul(make_double2(-0.5 * t.x, -0.5 * t.y), make_double2(kr, ki));
+    for (int r = tid; r < m; r += nt) w[r] = cadd(w[r], cmul(K, v[r]));
+    __syncthreads();
+    // A_t -= v w^H + w v^H
+    for (int64_t x = tid; x < (int64_t)m * m; x += nt) {
+      const int r = (int)(x / m), c = (int)(x - (int64_t)r * m);
+      const double2 a = cmul(v[r], make_double2(w[c].x, -w[c].y));
+      const double2 b = cmul(w[r], make_double2(v[c].x, -v[c].y));
+      double2 &g = A[(int64_t)(j + 1 + r) * n + (j + 1 + c)];
+      g = make_double2(g.x - a.x - b.x, g.y - a.y - b.y);
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    d[n - 1] = A[(int64_t)(n - 1) * n + (n - 1)].x;
+    e[n - 1] = 0.0;
+    tau[n - 1] = make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  if (job.smem)
+    for (int64_t x = tid; x < (int64_t)n * n; x += nt) G_all[job.g_off + x] = A[x];
+}
+
+// Complex back-transformation: Z <- H_0 H_1 ... H_{n-2} Z, H_j = I - tau_j v_j v_j^H.
+__global__ void backtransform_c_kernel(const EigJob *__restrict__ jobs,
+                                       const BackChunk *__restrict__ bt,
+                                       const double2 *__restrict__ G_all,
+                                       const double2 *__restrict__ tau_all,
+                                       double2 *__restrict__ Z) {
+  extern __shared__ double2 smc[];
+  __shared__ double2 part[8][33];
+  const BackChunk ch = bt[blockIdx.x];
+  const EigJob job = jobs[ch.job];
+  const int n = job.n;
+  if (n < 2 || ch.cw == 0) return;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  double2 *z = Z + ch.z_off + ch.c0;
+  double2 *v = smc;
+  const double2 *A = G_all + job.g_off;
+  const bool col = tx < ch.cw;
+  for (int j = n - 2; j >= 0; --j) {
+    const double2 t = tau_all[job.lam_off + j];
+    if (t.x == 0.0 && t.y == 0.0) continue;
+    const int m = n - j - 1;
+    for (int r = threadIdx.x; r < m; r += blockDim.x)
+      v[r] = r == 0 ? make_double2(1.0, 0.0) : A[(int64_t)j * n + j + 1 + r];
+    __syncthreads();
+    double2 s = make_double2(0.0, 0.0);
+    if (col)
+      for (int r = ty; r < m; r += 8) s = cadd(s, cmulc(v[r], z[(int64_t)(j + 1 + r) * ch.ld + tx]));
+    part[ty][tx] = s;
+    __syncthreads();
+    double2 w = make_double2(0.0, 0.0);
+    for (int g = 0; g < 8; ++g) w = cadd(w, part[g][tx]);
+    w = cmul(t, w);
+    if (col)
+      for (int r = ty; r < m; r += 8) {
+        double2 &zz = z[(int64_t)(j + 1 + r) * ch.ld + tx];
+        const double2 q = cmul(v[r], w);
+        zz = make_double2(zz.x - q.x, zz.y - q.y);
+      }
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 constexpr size_t kTriSmemBytes = 200 * 1024;
 
 int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, double *G,
-                   double *lam, SymEigWork &wk) {
+                   double *lam, SymEigWork &wk, bool cplx) {
   const int nj = (int)jobs.size();
   if (nj == 0) return 0;
   int64_t ltot = 0;
@@ -411,16 +614,21 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
   UDMRG_REQUIRE(nmax <= 4096, "eigensolver: matrix larger than 4096 is not supported");
   wk.d = scratch.get<double>(std::max<int64_t>(ltot, 1));
   wk.e = scratch.get<double>(std::max<int64_t>(ltot, 1));
-  wk.tau = scratch.get<double>(std::max<int64_t>(ltot, 1));
+  wk.tau = scratch.get<double>((cplx ? 2 : 1) * std::max<int64_t>(ltot, 1));
   wk.scale = scratch.get<double>(nj);
+  wk.cplx = cplx;
+  const size_t es = (cplx ? 2 : 1) * sizeof(double);
   size_t smem = 0;
   for (auto &j : jobs) {
-    const size_t base = 2 * (size_t)j.n * sizeof(double);
-    const size_t full = base + (size_t)j.n * j.n * sizeof(double);
+    const size_t base = 2 * (size_t)j.n * es;
+    const size_t full = base + (size_t)j.n * j.n * es;
     j.smem = full <= kTriSmemBytes ? 1 : 0;
     smem = std::max(smem, j.smem ? full : base);
   }
   UDMRG_CHECK_CUDA(cudaFuncSetAttribute(tridiag_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)kTriSmemBytes));
+  UDMRG_CHECK_CUDA(cudaFuncSetAttribute(tridiag_c_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)kTriSmemBytes));
   wk.jobs = scratch.get<EigJob>(nj);
@@ -428,8 +636,12 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
   UDMRG_CHECK_CUDA(cudaMemsetAsync(dstat, 0, sizeof(int), ctx.stream));
   UDMRG_CHECK_CUDA(cudaMemcpyAsync(wk.jobs, jobs.data(), nj * sizeof(EigJob),
                                    cudaMemcpyHostToDevice, ctx.stream));
-  tridiag_kernel<<<nj, kTriThreads, smem, ctx.stream>>>(wk.jobs, G, wk.d, wk.e, wk.tau, wk.scale,
-                                                        dstat);
+  if (cplx)
+    tridiag_c_kernel<<<nj, kTriThreads, smem, ctx.stream>>>(
+        wk.jobs, (double2 *)G, wk.d, wk.e, (double2 *)wk.tau, wk.scale, dstat);
+  else
+    tridiag_kernel<<<nj, kTriThreads, smem, ctx.stream>>>(wk.jobs, G, wk.d, wk.e, wk.tau,
+                                                          wk.scale, dstat);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   const size_t bsmem = 2 * (size_t)nmax * sizeof(double);
   if (bsmem > 48 * 1024)
@@ -454,10 +666,23 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
 
 void sym_eig_vectors(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJob> &jobs,
                      const double *G, const double *lam, const std::vector<double> &hlam,
-                     const std::vector<int64_t> &k, const std::vector<int64_t> &z_off,
-                     const std::vector<int64_t> &z_ld, double *Z, const SymEigWork &wk,
+                     const std::vector<int64_t> &k, const std::vector<int64_t> &z_off_out,
+                     const std::vector<int64_t> &z_ld_out, double *Zout, const SymEigWork &wk,
                      uint64_t seed) {
   const int nj = (int)jobs.size();
+  // the eigenvectors of the (real) tridiagonal matrix: in place for real
+  // matrices, in a packed real buffer for complex ones
+  double *Z = Zout;
+  std::vector<int64_t> z_off = z_off_out, z_ld = z_ld_out;
+  int64_t zr_tot = 0;
+  if (wk.cplx) {
+    for (int q = 0; q < nj; ++q) {
+      z_off[q] = zr_tot;
+      z_ld[q] = std::max<int64_t>(k[q], 1);
+      zr_tot += (int64_t)jobs[q].n * k[q];
+    }
+    Z = scratch.get<double>(std::max<int64_t>(zr_tot, 1));
+  }
   // clusters: descending neighbours closer than 1e-9 of the matrix's largest |eigenvalue|
   std::vector<EigCluster> cl;
   int nmax = 0;
@@ -528,24 +753,42 @@ void sym_eig_vectors(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJob>
       }
     }
   }
+  if (wk.cplx && zr_tot > 0) {  // real eigenvectors of T -> complex, into the caller's layout
+    double *Zc = scratch.get<double>(2 * zr_tot);
+    real_to_complex(ctx, Z, Zc, zr_tot);
+    std::vector<Copy2D> ops;
+    for (int q = 0; q < nj; ++q)
+      if (k[q] > 0)
+        ops.push_back(Copy2D{z_off[q], z_off_out[q], jobs[q].n, (int32_t)k[q], k[q], 1,
+                             z_ld_out[q], 1});
+    run_copy2d(ctx, ops, Zc, Zout, true);
+  }
   // back-transformation by the reflectors, 32 columns per block
   {
     std::vector<BackChunk> bt;
     for (int q = 0; q < nj; ++q)
       for (int64_t c0 = 0; c0 < k[q]; c0 += 32)
-        bt.push_back(BackChunk{z_off[q], z_ld[q], q, (int32_t)c0,
+        bt.push_back(BackChunk{z_off_out[q], z_ld_out[q], q, (int32_t)c0,
                                (int32_t)std::min<int64_t>(32, k[q] - c0), 0});
     if (!bt.empty()) {
       BackChunk *dbt = scratch.get<BackChunk>(bt.size());
       UDMRG_CHECK_CUDA(cudaMemcpyAsync(dbt, bt.data(), bt.size() * sizeof(BackChunk),
                                        cudaMemcpyHostToDevice, ctx.stream));
-      const size_t smem = (size_t)nmax * sizeof(double);
-      if (smem > 48 * 1024)
+      const size_t smem = (size_t)nmax * (wk.cplx ? 2 : 1) * sizeof(double);
+      if (smem > 48 * 1024) {
         UDMRG_CHECK_CUDA(cudaFuncSetAttribute(backtransform_kernel,
                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)smem));
-      backtransform_kernel<<<(int)bt.size(), kBackThreads, smem, ctx.stream>>>(wk.jobs, dbt, G,
-                                                                              wk.tau, Z);
+        UDMRG_CHECK_CUDA(cudaFuncSetAttribute(backtransform_c_kernel,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem));
+      }
+      if (wk.cplx)
+        backtransform_c_kernel<<<(int)bt.size(), kBackThreads, smem, ctx.stream>>>(
+            wk.jobs, dbt, (const double2 *)G, (const double2 *)wk.tau, (double2 *)Zout);
+      else
+        backtransform_kernel<<<(int)bt.size(), kBackThreads, smem, ctx.stream>>>(
+            wk.jobs, dbt, G, wk.tau, Zout);
       UDMRG_CHECK_CUDA(cudaGetLastError());
       ctx.launches++;
     }

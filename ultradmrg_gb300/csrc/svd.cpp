@@ -131,7 +131,9 @@ std::vector<Sector> group_sectors(const BTensor &T, int ldims, const QN &ldiv, i
 void gather(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, std::vector<Sector> &secs,
             double *Mbuf, int64_t mtot) {
   const int r = T.rank();
-  UDMRG_CHECK_CUDA(cudaMemsetAsync(Mbuf, 0, std::max<int64_t>(mtot, 1) * sizeof(double), ctx.stream));
+  const bool cplx = T.dtype == kC128;
+  UDMRG_CHECK_CUDA(cudaMemsetAsync(Mbuf, 0, std::max<int64_t>(mtot, 1) * (cplx ? 2 : 1) *
+                                                sizeof(double), ctx.stream));
   std::vector<Copy2D> ops;
   std::map<QN, int> qidx;
   for (int q = 0; q < (int)secs.size(); ++q) qidx[secs[q].qn] = q;
@@ -151,7 +153,7 @@ void gather(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, std::vector<S
     c.dst_cs = 1;
     ops.push_back(c);
   }
-  run_copy2d(ctx, ops, T.data, Mbuf, false);
+  run_copy2d(ctx, ops, T.data, Mbuf, cplx);
 }
 
 // View of M_q (left side) or M_q^T (right side) as an (xr x xc) matrix.
@@ -166,13 +168,20 @@ XView xview(const Sector &s, bool left) {
 // Build u, s, vt from the isometric factor of every sector: iso(i, j) =
 // iso_buf[iso_off[q] + i*iso_ld[q] + j], i over rows (left) or columns (right)
 // of M_q, j over the kept states.
+// Complex tensors (interleaved storage, offsets in complex elements): the
+// isometric factor holds eigenvectors of X X^H; the centre product uses its
+// conjugate (U^H M on the left, M conj(W) on the right, W the eigenvectors of
+// the transposed view's Gram matrix, whose transpose is V^H).
 void build_outputs(Ctx &ctx, DeviceScratch &scratch, const BTensor &T, int ldims,
                    const std::vector<Sector> &secs, const std::vector<int64_t> &kept,
                    const std::vector<std::vector<double>> &sv, int mode, const double *iso_buf,
                    const std::vector<int64_t> &iso_off, const std::vector<int64_t> &iso_ld,
-                   const double *Mbuf, SvdResult &res) {
+                   const double *Mbuf, SvdResult &res, int64_t iso_total = 0) {
   const int nsec = (int)secs.size();
   const bool left = (mode != kSvdSplitRight);
+  const bool cplx = T.dtype == kC128;
+  const DType dt = cplx ? kC128 : kF64;
+  const int es = cplx ? 2 : 1;
   Index bond;
   bond.dir = 1;
   std::vector<int> bid(nsec, -1);
@@ -190,6 +199,7 @@ void build_outputs(Ctx &ctx, DeviceScratch &scratch, const BTensor &T, int ldims
     t->dtype = kF64;
     t->nq = T.nq;
   }
+  u->dtype = vt->dtype = dt;  // singular values stay real
   u->idx.assign(T.idx.begin(), T.idx.begin() + ldims);
   u->idx.push_back(bond);
   vt->idx.push_back(bond.inverse());
@@ -240,7 +250,15 @@ void build_outputs(Ctx &ctx, DeviceScratch &scratch, const BTensor &T, int ldims
     coffs[q] = ctot;
     ctot += kept[q] * (left ? secs[q].cols : secs[q].rows);
   }
-  double *Cbuf = scratch.get<double>(std::max<int64_t>(ctot, 1));
+  double *Cbuf = scratch.get<double>(es * std::max<int64_t>(ctot, 1));
+  const double *iso_c = iso_buf;  // the operand of the centre product (conjugated if complex)
+  if (cplx && iso_total > 0) {
+    double *t = scratch.get<double>(2 * iso_total);
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(t, iso_buf, 2 * iso_total * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, ctx.stream));
+    conj_inplace(ctx, t, iso_total);
+    iso_c = t;
+  }
   {
     GemmPlan g;
     g.ctx = &ctx;
@@ -249,16 +267,16 @@ void build_outputs(Ctx &ctx, DeviceScratch &scratch, const BTensor &T, int ldims
       const Sector &sc = secs[q];
       if (left)  // C(i, col) = sum_row U[row, i] M[row, col]
         gemm_add_simple(g, coffs[q], kept[q], sc.cols, sc.rows, iso_off[q], 1, iso_ld[q], sc.m_off,
-                        sc.cols, 1, false);
+                        sc.cols, 1, cplx);
       else  // C(row, i) = sum_col M[row, col] V[col, i]
         gemm_add_simple(g, coffs[q], sc.rows, kept[q], sc.cols, sc.m_off, sc.cols, 1,
-                        iso_off[q], iso_ld[q], 1, false);
+                        iso_off[q], iso_ld[q], 1, cplx);
     }
     gemm_finalize(g);
     if (left)
-      run_gemm(ctx, g, kF64, iso_buf, Mbuf, Cbuf, 1.0, 0.0);
+      run_gemm(ctx, g, dt, iso_c, Mbuf, Cbuf, 1.0, 0.0);
     else
-      run_gemm(ctx, g, kF64, Mbuf, iso_buf, Cbuf, 1.0, 0.0);
+      run_gemm(ctx, g, dt, Mbuf, iso_c, Cbuf, 1.0, 0.0);
   }
   if (mode == kSvdFull) {
     // vt = S^{-1} (U^T M): scale row i of each centre block by 1/s_i (0 for s_i == 0)
@@ -278,7 +296,7 @@ void build_outputs(Ctx &ctx, DeviceScratch &scratch, const BTensor &T, int ldims
     double *dinv = scratch.get<double>(std::max<size_t>(inv.size(), 1));
     UDMRG_CHECK_CUDA(cudaMemcpyAsync(dinv, inv.data(), inv.size() * sizeof(double),
                                      cudaMemcpyHostToDevice, ctx.stream));
-    run_scale(ctx, sj, Cbuf, dinv, false);
+    run_scale(ctx, sj, Cbuf, dinv, cplx);
   }
   std::vector<Copy2D> uops, vops;
   for (int q = 0; q < nsec; ++q) {
@@ -327,8 +345,8 @@ void build_outputs(Ctx &ctx, DeviceScratch &scratch, const BTensor &T, int ldims
       vops.push_back(c);
     }
   }
-  run_copy2d(ctx, uops, left ? iso_buf : Cbuf, u->data, false);
-  run_copy2d(ctx, vops, left ? Cbuf : iso_buf, vt->data, false);
+  run_copy2d(ctx, uops, left ? iso_buf : Cbuf, u->data, cplx);
+  run_copy2d(ctx, vops, left ? Cbuf : iso_buf, vt->data, cplx);
   res.u = std::move(u);
   res.s = std::move(s);
   res.vt = std::move(vt);
@@ -361,13 +379,23 @@ std::vector<double> download_vec(Ctx &ctx, const double *d, int64_t n) {
 SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, double trunc_err,
                     int64_t Dmin, int64_t Dmax, int mode) {
   UDMRG_REQUIRE(ldims > 0 && ldims < T.rank(), "svd: bad ldims");
-  UDMRG_REQUIRE(T.dtype == kF64, "svd: complex tensors are not supported by this SVD yet");
+  const bool cplx = T.dtype == kC128;
+  const int es = cplx ? 2 : 1;
   int64_t mtot = 0;
   auto secs = group_sectors(T, ldims, ldiv, mtot);
   const int nsec = (int)secs.size();
   DeviceScratch scratch(ctx);
-  double *Mbuf = scratch.get<double>(std::max<int64_t>(mtot, 1));
+  double *Mbuf = scratch.get<double>(es * std::max<int64_t>(mtot, 1));
   gather(ctx, T, ldims, ldiv, secs, Mbuf, mtot);
+  // conjugate copy for the Hermitian Gram matrices X X^H
+  const double *Mc = Mbuf;
+  if (cplx && mtot > 0) {
+    double *t = scratch.get<double>(2 * mtot);
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(t, Mbuf, 2 * mtot * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     ctx.stream));
+    conj_inplace(ctx, t, mtot);
+    Mc = t;
+  }
   // Gram matrices on the isometry side
   const bool left = (mode != kSvdSplitRight);
   std::vector<EigJob> jobs(nsec);
@@ -380,21 +408,21 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
     gtot += n * n;
     ltot += n;
   }
-  double *G = scratch.get<double>(std::max<int64_t>(gtot, 1));
+  double *G = scratch.get<double>(es * std::max<int64_t>(gtot, 1));
   double *lam = scratch.get<double>(std::max<int64_t>(ltot, 1));
   {
     GemmPlan g;
     g.ctx = &ctx;
     for (int q = 0; q < nsec; ++q) {
-      const XView x = xview(secs[q], left);  // G = X X^T
+      const XView x = xview(secs[q], left);  // G = X X^T (X X^H)
       gemm_add_simple(g, jobs[q].g_off, x.xr, x.xr, x.xc, x.off, x.sr, x.sc, x.off, x.sc, x.sr,
-                      false);
+                      cplx);
     }
     gemm_finalize(g);
-    run_gemm(ctx, g, kF64, Mbuf, Mbuf, G, 1.0, 0.0);
+    run_gemm(ctx, g, cplx ? kC128 : kF64, Mbuf, Mc, G, 1.0, 0.0);
   }
   SymEigWork wk;
-  check_eig_status(sym_eig_values(ctx, scratch, jobs, G, lam, wk));
+  check_eig_status(sym_eig_values(ctx, scratch, jobs, G, lam, wk, cplx));
   const std::vector<double> hlam = download_vec(ctx, lam, ltot);
   std::vector<std::vector<double>> sv(nsec);
   for (int q = 0; q < nsec; ++q) {
@@ -414,9 +442,10 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
     iso_ld[q] = std::max<int64_t>(kept[q], 1);
     ztot += (int64_t)jobs[q].n * kept[q];
   }
-  double *Z = scratch.get<double>(std::max<int64_t>(ztot, 1));
+  double *Z = scratch.get<double>(es * std::max<int64_t>(ztot, 1));
   sym_eig_vectors(ctx, scratch, jobs, G, lam, hlam, kept, iso_off, iso_ld, Z, wk);
-  build_outputs(ctx, scratch, T, ldims, secs, kept, sv, mode, Z, iso_off, iso_ld, Mbuf, res);
+  build_outputs(ctx, scratch, T, ldims, secs, kept, sv, mode, Z, iso_off, iso_ld, Mbuf, res,
+                ztot);
   res.sector_sketch.assign(nsec, 0);
   return res;
 }
@@ -448,6 +477,15 @@ SvdResult svd_trunc_sketch(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv
     auto it = req.find(secs[q].qn);
     const int64_t want = it == req.end() ? full[q] : it->second + sp.oversample;
     s[q] = std::max<int64_t>(1, std::min(full[q], want));
+  }
+  {
+    int64_t ssum = 0, fsum = 0;
+    for (int q = 0; q < nsec; ++q) {
+      ssum += s[q];
+      fsum += full[q];
+    }
+    if (sp.max_fraction < 1.0 && (double)ssum > sp.max_fraction * (double)fsum)
+      return svd_trunc(ctx, T, ldims, ldiv, trunc_err, Dmin, Dmax, mode);
   }
   // isometric factor of sector q (xr x s_q, row-major) kept at uoff[q] across
   // rounds; a round recomputes only the sectors that missed

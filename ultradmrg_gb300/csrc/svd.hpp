@@ -16,7 +16,7 @@ struct EigJob {
   int64_t g_off;    // offset of the n x n matrix in the G / V / W buffers
   int64_t lam_off;  // offset of the n eigenvalues
   int32_t n;
-  int32_t smem;     // set by run_jacobi_eig
+  int32_t smem;     // set by sym_eig_values (matrix held in shared memory)
 };
 
 // Batched symmetric eigen-solver (Householder tridiagonalisation, bisection,
@@ -29,6 +29,7 @@ struct EigCluster {  // eigenvalues close enough to share a Gram-Schmidt sweep
 struct SymEigWork {
   EigJob *jobs = nullptr;  // device copy of the jobs
   double *d = nullptr, *e = nullptr, *tau = nullptr, *scale = nullptr;
+  bool cplx = false;  // complex Hermitian matrices (interleaved re, im; tau complex)
 };
 
 struct ScaleJob {
@@ -37,13 +38,9 @@ struct ScaleJob {
   int32_t by_row, pad;
 };
 
-constexpr size_t kJacobiSmemBytes = 200 * 1024;
 
 void run_copy2d(Ctx &ctx, const std::vector<Copy2D> &ops, const double *src, double *dst,
                 bool cplx);
-// Returns 0, or 1 when some sector did not converge within the sweep limit.
-int run_jacobi_eig(Ctx &ctx, const std::vector<EigJob> &jobs, double *G, double *V, double *W,
-                   double *lam);
 void run_scale(Ctx &ctx, const std::vector<ScaleJob> &jobs, double *X, const double *f, bool cplx);
 
 // Kept-state selection over all bond sectors (the rule of the oracle):
@@ -53,8 +50,10 @@ void run_scale(Ctx &ctx, const std::vector<ScaleJob> &jobs, double *X, const dou
 // Phase 1: reduce every job's symmetric n x n matrix in G to tridiagonal form
 // (G keeps the reflectors) and put all its eigenvalues, descending, at
 // lam[lam_off ...].  Returns 0, or 2 for non-finite input.  jobs[].smem is set.
+// With cplx, G holds complex Hermitian matrices (offsets in complex elements)
+// and phase 2 returns complex eigenvectors.
 int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, double *G,
-                   double *lam, SymEigWork &wk);
+                   double *lam, SymEigWork &wk, bool cplx = false);
 // Phase 2: the leading k[q] eigenvectors of job q (hlam: host copy of lam) as
 // the columns of Z (row-major n x k[q], leading dimension z_ld[q], at z_off[q]),
 // orthonormal to FP64 accuracy.
@@ -112,6 +111,9 @@ struct SketchParams {
   int64_t oversample = 8;
   int power_iters = 4;
   uint64_t seed = 1;
+  // cost rule: if the total sketch exceeds this fraction of the total sector
+  // dimension, the exact SVD is cheaper and runs instead (1: never)
+  double max_fraction = 1.0;
 };
 SvdResult svd_trunc_sketch(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv,
                            double trunc_err, int64_t Dmin, int64_t Dmax, int mode,

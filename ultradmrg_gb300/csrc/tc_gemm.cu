@@ -8,15 +8,17 @@ namespace udmrg {
 
 namespace {
 
-constexpr int kStages = 2;
-constexpr int kThreads = 128;
+constexpr int kStages = 3;
+constexpr int kThreads = 192;  // warp 0: loads, warp 1: MMA issue, warps 2-5: epilogue
+constexpr int kAcc = 2;        // TMEM accumulators (epilogue of tile i overlaps tile i+1)
 constexpr int kStageBytes = (int)(kTcUnitA + kTcUnitB);  // 72 KB
 // Headroom after the stage buffers: no descriptor read can leave the
 // allocation even if a stride field were misread.
-constexpr int kPadBytes = 32 * 1024;
+constexpr int kPadBytes = 8 * 1024;
 constexpr int kBarOffset = kStages * kStageBytes + kPadBytes;
 constexpr int kSmemBytes = kBarOffset + 1024;
-constexpr uint32_t kTmemCols = kTcBN;  // FP32 accumulator: BN columns x 128 lanes
+static_assert(kSmemBytes <= 227 * 1024, "tc_gemm: shared memory budget");
+constexpr uint32_t kTmemCols = kAcc * kTcBN;  // FP32 accumulators: 2 x BN columns x 128 lanes
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s: a wait this long means a fault
 
 __device__ __forceinline__ uint64_t global_ns() {
@@ -88,6 +90,11 @@ __global__ void pack_kernel(const PackOp *__restrict__ ops, int nops, const T *_
 __device__ __constant__ int kProdA[6] = {0, 0, 1, 0, 1, 2};
 __device__ __constant__ int kProdB[6] = {0, 1, 0, 2, 1, 0};
 
+// Warp-specialised persistent kernel over the tile list (static schedule
+// t = blockIdx.x + i * gridDim.x).  Barriers: full/empty per shared-memory
+// stage (bulk copies -> MMA -> copies), tfull/tempty per TMEM accumulator
+// (MMA -> epilogue -> MMA).  Every wait is bounded; a timeout sets *err and the
+// abort flag, and every role leaves its loop.
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_kernel(const TcTile *__restrict__ tiles, int ntiles, const TcGroup *__restrict__ groups,
                    const uint8_t *__restrict__ aimg, const uint8_t *__restrict__ bimg,
@@ -96,8 +103,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   extern __shared__ __align__(1024) uint8_t smem[];
   uint64_t *full = (uint64_t *)(smem + kBarOffset);
   uint64_t *empty = full + kStages;
-  uint64_t *done = empty + kStages;
-  uint64_t *fin = done + 1;
+  uint64_t *tfull = empty + kStages;
+  uint64_t *tempty = tfull + kAcc;
+  uint64_t *fin = tempty + kAcc;
   uint32_t *tmem_slot = (uint32_t *)(fin + 1);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -107,7 +115,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
-    tc::mbar_init(done, 1);
+    for (int a = 0; a < kAcc; ++a) {
+      tc::mbar_init(&tfull[a], 1);
+      tc::mbar_init(&tempty[a], 4);  // one arrival per epilogue warp
+    }
     tc::mbar_init(fin, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -121,103 +132,123 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
   constexpr uint32_t idesc = tc::idesc_bf16_f32(kTcBM, kTcBN);
+  auto fail = [&](int code) {
+    atomicExch(err, code);
+    *abort_flag = 1;
+  };
 
-  uint32_t gchunk = 0;  // chunks issued so far by this CTA (thread 0's view)
-  uint32_t tile_iter = 0;
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const TcTile tile = tiles[t];
-    const TcGroup g = groups[tile.group];
-    const int nk = g.kc;
-    if (tid == 0 && !*abort_flag) {
-      const uint8_t *abase = aimg + g.a_img + (int64_t)tile.mtile * g.kc * kTcUnitA;
-      const uint8_t *bbase = bimg + g.b_img + (int64_t)tile.ntile * g.kc * kTcUnitB;
-      auto issue = [&](int c) -> bool {
-        const uint32_t G = gchunk + c, s = G % kStages;
-        if (G >= kStages && !wait_phase(&empty[s], ((G / kStages) - 1) & 1)) return false;
-        uint8_t *st = smem + s * kStageBytes;
-        tc::mbar_expect_tx(&full[s], (uint32_t)(kTcUnitA + kTcUnitB));
-        tc::bulk_g2s(st, abase + (int64_t)c * kTcUnitA, (uint32_t)kTcUnitA, &full[s]);
-        tc::bulk_g2s(st + kTcUnitA, bbase + (int64_t)c * kTcUnitB, (uint32_t)kTcUnitB, &full[s]);
-        return true;
-      };
-      bool ok = true;
-      for (int c = 0; c < min(kStages, nk) && ok; ++c) ok = issue(c);
-      for (int c = 0; c < nk && ok; ++c) {
-        const uint32_t G = gchunk + c, s = G % kStages;
-        if (!wait_phase(&full[s], (G / kStages) & 1)) {
-          ok = false;
+  if (warp == 0) {
+    if (lane == 0) {  // producer: one bulk copy per operand unit and chunk
+      uint32_t G = 0;
+      for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+        const TcTile tile = tiles[t];
+        const TcGroup g = groups[tile.group];
+        const uint8_t *abase = aimg + g.a_img + (int64_t)tile.mtile * g.kc * kTcUnitA;
+        const uint8_t *bbase = bimg + g.b_img + (int64_t)tile.ntile * g.kc * kTcUnitB;
+        for (int c = 0; c < g.kc; ++c, ++G) {
+          const uint32_t s = G % kStages;
+          if (G >= kStages && !wait_phase(&empty[s], ((G / kStages) - 1) & 1)) {
+            fail(1);
+            break;
+          }
+          uint8_t *st = smem + s * kStageBytes;
+          tc::mbar_expect_tx(&full[s], (uint32_t)(kTcUnitA + kTcUnitB));
+          tc::bulk_g2s(st, abase + (int64_t)c * kTcUnitA, (uint32_t)kTcUnitA, &full[s]);
+          tc::bulk_g2s(st + kTcUnitA, bbase + (int64_t)c * kTcUnitB, (uint32_t)kTcUnitB, &full[s]);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issue: six split products per 16-deep K step
+      uint32_t G = 0, i = 0;
+      for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x, ++i) {
+        const TcGroup g = groups[tiles[t].group];
+        const uint32_t acc = i & 1;
+        if (i >= kAcc && !wait_phase(&tempty[acc], ((i >> 1) - 1) & 1)) {
+          fail(4);
           break;
         }
         tc::fence_after_sync();
-        const uint32_t sa = tc::smem_u32(smem + s * kStageBytes);
-        const uint32_t sb = sa + (uint32_t)kTcUnitA;
-        constexpr uint32_t planeA = kTcBM * kTcBK * 2, planeB = kTcBN * kTcBK * 2;
+        const uint32_t dcol = tmem + acc * kTcBN;
+        bool ok = true;
+        for (int c = 0; c < g.kc; ++c, ++G) {
+          const uint32_t s = G % kStages;
+          if (!wait_phase(&full[s], (G / kStages) & 1)) {
+            ok = false;
+            break;
+          }
+          tc::fence_after_sync();
+          const uint32_t sa = tc::smem_u32(smem + s * kStageBytes);
+          const uint32_t sb = sa + (uint32_t)kTcUnitA;
+          constexpr uint32_t planeA = kTcBM * kTcBK * 2, planeB = kTcBN * kTcBK * 2;
 #pragma unroll
-        for (int ks = 0; ks < kTcBK / 16; ++ks) {
+          for (int ks = 0; ks < kTcBK / 16; ++ks) {
 #pragma unroll
-          for (int p = 0; p < 6; ++p) {
-            // K step ks covers core-matrix columns 2ks, 2ks+1
-            const uint64_t ad = tc::make_desc(sa + kProdA[p] * planeA + ks * 2 * (kTcBM / 8) * 128,
-                                              (kTcBM / 8) * 128, 128);
-            const uint64_t bd = tc::make_desc(sb + kProdB[p] * planeB + ks * 2 * (kTcBN / 8) * 128,
-                                              (kTcBN / 8) * 128, 128);
-            tc::mma_bf16(tmem, ad, bd, idesc, (c > 0 || ks > 0 || p > 0) ? 1u : 0u);
+            for (int p = 0; p < 6; ++p) {
+              // K step ks covers core-matrix columns 2ks, 2ks+1
+              const uint64_t ad = tc::make_desc(
+                  sa + kProdA[p] * planeA + ks * 2 * (kTcBM / 8) * 128, (kTcBM / 8) * 128, 128);
+              const uint64_t bd = tc::make_desc(
+                  sb + kProdB[p] * planeB + ks * 2 * (kTcBN / 8) * 128, (kTcBN / 8) * 128, 128);
+              tc::mma_bf16(dcol, ad, bd, idesc, (c > 0 || ks > 0 || p > 0) ? 1u : 0u);
+            }
+          }
+          tc::mma_commit(&empty[s]);  // the stage is free once these MMAs completed
+        }
+        if (!ok) {
+          fail(1);
+          break;
+        }
+        tc::mma_commit(&tfull[acc]);  // the accumulator is complete
+      }
+      tc::mma_commit(fin);  // every MMA of this CTA has completed
+      if (!wait_phase(fin, 0)) fail(3);
+    }
+  } else {  // epilogue: warp w drains TMEM lanes 32 (w % 4) ...
+    const int q = warp & 3;
+    const int m = q * 32 + lane;
+    uint32_t i = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+      const TcTile tile = tiles[t];
+      const TcGroup g = groups[tile.group];
+      const uint32_t acc = i & 1;
+      if (*abort_flag) break;
+      if (!wait_phase(&tfull[acc], (i >> 1) & 1)) {
+        if (lane == 0) fail(2);
+        break;
+      }
+      tc::fence_after_sync();
+      const int64_t grow = (int64_t)tile.mtile * kTcBM + m;
+      const bool row_ok = grow < g.M;
+      const int64_t base = row_ok ? rowaddr[g.row0 + grow] : 0;
+      const int n0 = tile.ntile * kTcBN;
+#pragma unroll
+      for (int cb = 0; cb < kTcBN / 16; ++cb) {
+        uint32_t r[16];
+        tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + acc * kTcBN + cb * 16, r);
+        tc::tmem_wait_ld();
+        if (row_ok) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = n0 + cb * 16 + j;
+            if (n < g.N) {
+              const float v = g.kc > 0 ? __uint_as_float(r[j]) : 0.0f;
+              if (out_kind == kTcOutF64)
+                ((double *)out)[base + n] = alpha * (double)v;
+              else
+                ((float *)out)[base + n] = (float)(alpha * (double)v);
+            }
           }
         }
-        tc::mma_commit(&empty[s]);
-        if (c + kStages < nk) ok = issue(c + kStages);
       }
-      gchunk += nk;
-      tc::mma_commit(done);  // arrives once every MMA of this tile completed
-      if (!ok) {
-        atomicExch(err, 1);
-        *abort_flag = 1;
-      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&tempty[acc]);
     }
-    // epilogue: all warps drain their 32 TMEM lanes
-    const bool got = wait_phase(done, tile_iter & 1);
-    if (!got) {
-      if (lane == 0) atomicExch(err, 2);
-      *abort_flag = 1;
-    }
-    tc::fence_after_sync();
-    const int m = warp * 32 + lane;
-    const int64_t grow = (int64_t)tile.mtile * kTcBM + m;
-    const bool row_ok = grow < g.M && got && !*abort_flag;
-    const int64_t base = row_ok ? rowaddr[g.row0 + grow] : 0;
-    const int n0 = tile.ntile * kTcBN;
-#pragma unroll
-    for (int cb = 0; cb < kTcBN / 16; ++cb) {
-      uint32_t r[16];
-      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + cb * 16, r);
-      tc::tmem_wait_ld();
-      if (row_ok) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int n = n0 + cb * 16 + j;
-          if (n < g.N) {
-            const float v = nk > 0 ? __uint_as_float(r[j]) : 0.0f;
-            if (out_kind == kTcOutF64)
-              ((double *)out)[base + n] = alpha * (double)v;
-            else
-              ((float *)out)[base + n] = (float)(alpha * (double)v);
-          }
-        }
-      }
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    ++tile_iter;
-    if (*abort_flag) break;
-  }
-  // all MMAs of this CTA have completed before the accumulator is released
-  if (tid == 0) {
-    tc::mma_commit(fin);
-    if (!wait_phase(fin, 0)) atomicExch(err, 3);
   }
   tc::fence_before_sync();
   __syncthreads();
+  tc::fence_after_sync();
   if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 

@@ -344,6 +344,31 @@ def heisenberg_chain_mpo(N, J=1.0, dtype=np.float64, pairs=None):
     return g.gen(), pb
 
 
+def spinless_fermion_site(dtype=np.float64):
+    """Spinless fermion site with a U(1) charge: basis [0 (+1), 1 (-1)];
+    c sets element {0,1}, c^dag element {1,0}, the Jordan-Wigner string
+    f = diag(-1, 1) (``tests/test_algorithm/test_two_site_finite_tdvp.cc:38-80``)."""
+    pb_out = Index.make([((1,), 1), ((-1,), 1)], OUT)
+    ops = {
+        "id": _op("id", 2, {(0, 0): 1, (1, 1): 1}, dtype),
+        "c": _op("c", 2, {(0, 1): 1}, dtype),
+        "cdag": _op("cdag", 2, {(1, 0): 1}, dtype),
+        "f": _op("f", 2, {(0, 0): -1, (1, 1): 1}, dtype),
+    }
+    return pb_out, ops
+
+
+def free_fermion_chain_mpo(N, t=1.0, dtype=np.float64):
+    """H = -t sum_i (c^dag_i c_{i+1} + c_i c^dag_{i+1}) on an open chain
+    (``test_two_site_finite_tdvp.cc:108-113``)."""
+    pb, ops = spinless_fermion_site(dtype)
+    g = MPOGenerator([pb] * N, [ops["id"]] * N, dtype)
+    for i in range(N - 1):
+        g.add_two_site(-t, ops["cdag"], i, ops["c"], i + 1)
+        g.add_two_site(-t, ops["c"], i, ops["cdag"], i + 1)
+    return g.gen(), pb, ops
+
+
 def ising_chain_mpo(N, dtype=np.float64):
     pb, ops = spin_half_site(dtype)
     g = MPOGenerator([pb] * N, [ops["id"]] * N, dtype)
@@ -447,6 +472,34 @@ def hubbard_2x2_test_mpo(dtype=np.float64, t0=1.0, t1=0.5, U=2.0, Nx=2, Ny=2):
 # ---------------------------------------------------------------------------
 # MPS initialisation
 # ---------------------------------------------------------------------------
+
+
+def operator_tensor(mat: np.ndarray, pb_out: Index, dtype=None) -> BlockTensorData:
+    """One-site operator tensor {pb_in, pb_out} from a dense matrix mat[in, out]."""
+    mat = np.asarray(mat)
+    t = BlockTensorData([pb_out.inverse(), pb_out], {}, dtype or mat.dtype)
+    for (i, o) in np.argwhere(mat != 0):
+        t.set_elem((int(i), int(o)), mat[i, o])
+    return t
+
+
+def mat_repr_mpo(mpo: Sequence[BlockTensorData]):
+    """The matrix representation (MatReprMPO, ``one_dim_tn/mpo/mat_repr_mpo.h:21``)
+    of MPO tensors W(lvb, pb_in, pb_out, rvb): per site (rows, cols, [(x, y,
+    operator tensor {pb_in, pb_out})]) for the non-null operators W[x, :, :, y]."""
+    out = []
+    for W in mpo:
+        d = W.to_dense()
+        pb = W.indexes[2]
+        rows, cols = d.shape[0], d.shape[3]
+        elems = []
+        for x in range(rows):
+            for y in range(cols):
+                m = d[x, :, :, y]
+                if np.any(m != 0):
+                    elems.append((x, y, operator_tensor(m, pb, W.dtype)))
+        out.append((rows, cols, elems))
+    return out
 
 
 def direct_product_mps(sites: Sequence[Index], labels: Sequence[int], dtype=np.float64):

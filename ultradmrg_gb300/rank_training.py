@@ -16,6 +16,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import sys
 import time
 from dataclasses import dataclass
 from typing import List, Sequence, Tuple
@@ -90,8 +91,9 @@ def sweep_schedule(ctx, chain: Chain, schedule: Sequence[Stage], *, model=None, 
 # Training chains: 4x8 and 4x16 cylinders, U in {4, 8, 12}, doping 1/8 and 1/16.
 TRAIN_CHAINS = [Chain(8, 4, U, h) for U in (4.0, 8.0, 12.0) for h in (4, 2)] + \
                [Chain(16, 4, U, h) for U in (4.0, 8.0, 12.0) for h in (8, 4)]
-TRAIN_SCHEDULE_4x8 = [Stage(64, 1), Stage(128, 1), Stage(256, 2), Stage(512, 2)]
-TRAIN_SCHEDULE_4x16 = [Stage(64, 1), Stage(128, 1), Stage(256, 1), Stage(400, 2)]
+TRAIN_SCHEDULE_4x8 = [Stage(64, 1), Stage(128, 1), Stage(256, 1), Stage(512, 1), Stage(1000, 2)]
+TRAIN_SCHEDULE_4x16 = [Stage(100, 1), Stage(250, 1), Stage(500, 1), Stage(1000, 1),
+                       Stage(2000, 1)]
 
 
 def collect(ctx, chains: Sequence[Chain], schedule_of, **kw) -> Tuple[np.ndarray, np.ndarray]:
@@ -99,9 +101,12 @@ def collect(ctx, chains: Sequence[Chain], schedule_of, **kw) -> Tuple[np.ndarray
     rec = api.RankModel(ctx, seed=0)
     xs, ys = [], []
     for ch in chains:
+        t0 = time.time()
         _, _, X, Y = sweep_schedule(ctx, ch, schedule_of(ch), model=rec, record=True, **kw)
         xs.append(X)
         ys.append(Y)
+        print(f"collected {len(Y)} samples from {ch} in {time.time() - t0:.1f} s",
+              file=sys.stderr, flush=True)
     rec.close()
     return np.concatenate(xs), np.concatenate(ys)
 
@@ -127,7 +132,9 @@ def load(ctx, path=WEIGHTS):
 def main(argv: List[str] | None = None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=WEIGHTS)
-    ap.add_argument("--epochs", type=int, default=400)
+    ap.add_argument("--epochs", type=int, default=40)
+    ap.add_argument("--batch", type=int, default=2048)
+    ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--small", action="store_true", help="4x8 chains only")
     a = ap.parse_args(argv)
     ctx = api.Context(0)
@@ -135,11 +142,14 @@ def main(argv: List[str] | None = None):
     t0 = time.time()
     X, Y = collect(ctx, chains,
                    lambda c: TRAIN_SCHEDULE_4x8 if c.Lx == 8 else TRAIN_SCHEDULE_4x16,
-                   svd_mode=1)
+                   svd_mode=0)
     t1 = time.time()
-    m, loss = train(ctx, X, Y, epochs=a.epochs)
+    m, loss = train(ctx, X, Y, epochs=a.epochs, batch=a.batch, lr=a.lr)
     t2 = time.time()
+    # the rule without the network (kept count of the previous visit), same samples
+    base = float(np.mean((10.0 * X[:, -3] - Y) ** 2))
     meta = dict(samples=int(len(Y)), chains=[c.__dict__ for c in chains], loss=loss,
+                previous_kept_rule_mse=base, epochs=a.epochs, batch=a.batch, lr=a.lr,
                 collect_seconds=t1 - t0, train_seconds=t2 - t1)
     save(m, a.out, meta)
     print(json.dumps(meta))

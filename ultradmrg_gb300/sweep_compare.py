@@ -1,0 +1,131 @@
+"""Two-site sweep of the Hubbard 4x16 cylinder at D = 2000 in three forms.
+
+The reference benchmark (``benchmark/ultradmrg_hubbard2d.cpp:227-253``) grows
+the bond dimension over calls of the sweep driver (D = 10, 100, 1000, 2000)
+from the product state with one hole every N/8 sites, then times a sweep at
+D = 2000.  Here a shorter schedule prepares the D = 2000 state (mixed
+precision, exact SVD, the rank model recording each bond's spectrum), and one
+full sweep is timed from that same state in each form:
+
+* ``fp64_exact``: plain FP64 block GEMMs in Lanczos, exact block SVD;
+* ``mixed_exact``: split-BF16 tensor-core matvec, exact block SVD;
+* ``mixed_learned``: split-BF16 matvec, randomized SVD sized by the learned
+  rank model (exact SVD on a miss; optional audit by the exact SVD);
+* ``mixed_learned_rule``: the same with the cost rule (the exact SVD when
+  the predicted sketch exceeds a fraction of the sector dimensions).
+
+``python -m ultradmrg_gb300.sweep_compare [--out FILE]`` prints one JSON object.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import api
+from . import models as M
+from . import rank_training as RT
+
+
+def _upload(ctx, tensors):
+    return [api.DeviceTensor.from_data(ctx, t) for t in tensors]
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--Lx", type=int, default=16)
+    ap.add_argument("--Ly", type=int, default=4)
+    ap.add_argument("--D", type=int, default=2000)
+    ap.add_argument("--schedule", default="10:2,100:2,500:2,1000:2,2000:1")
+    ap.add_argument("--weights", default=RT.WEIGHTS)
+    ap.add_argument("--forms", default="fp64_exact,mixed_exact,mixed_learned")
+    ap.add_argument("--audit", action="store_true")
+    ap.add_argument("--lanczos-error", type=float, default=1e-9)
+    ap.add_argument("--max-fraction", type=float, default=0.1,
+                    help="sketch fraction above which the learned form runs the exact SVD "
+                         "(form mixed_learned_rule)")
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args(argv)
+    ctx = api.Context(0)
+    N = a.Lx * a.Ly
+    mpo, pb = M.hubbard_cylinder_mpo(a.Lx, a.Ly, t=1.0, U=8.0)
+    labels = M.hubbard_cylinder_holes(N, 8)
+    dmpo = _upload(ctx, mpo)
+    dmps = _upload(ctx, M.direct_product_mps([pb] * N, labels))
+    model = RT.load(ctx, a.weights)
+    t0 = time.perf_counter()
+    prep = []
+    for item in a.schedule.split(","):
+        D, sw = (int(v) for v in item.split(":"))
+        p = api.FiniteVMPSSweepParams(sw, D, D, 1e-8, a.lanczos_error, 100,
+                                      precision=api.PREC_MIXED)
+        e0, log, _, _ = api.two_site_finite_vmps_learned(ctx, dmps, dmpo, p, model, False)
+        prep.append(dict(D=D, sweeps=sw, e0=e0, max_trunc_err=max(r["trunc_err"] for r in log)))
+    prep_sec = time.perf_counter() - t0
+    state = [t.to_data() for t in dmps]
+    out = dict(workload=f"hubbard{a.Ly}x{a.Lx}", D=a.D, sites=N, preparation=prep,
+               preparation_seconds=prep_sec, forms={})
+    forms = a.forms.split(",")
+    if a.audit and "mixed_learned" in forms:
+        forms.append("mixed_learned_audit")  # untimed: the exact SVD judges every truncation
+    for form in forms:
+        prec = api.PREC_FP64 if form.startswith("fp64") else api.PREC_MIXED
+        mode = 2 if "learned" in form else 0
+        p = api.FiniteVMPSSweepParams(1, a.D, a.D, 1e-8, a.lanczos_error, 100, precision=prec,
+                                      svd_mode=mode, svd_audit=form.endswith("audit"),
+                                      svd_sketch_max_fraction=(a.max_fraction
+                                                               if form.endswith("rule") else 1.0))
+        if mode == 2:  # a model carrying the bond history of the prepared state
+            hist = api.RankModel(ctx, 0)
+            hist.params = model.params
+            hist.copy_history_from(model)
+        mps = _upload(ctx, state)
+        ctx.sync()
+        t1 = time.perf_counter()
+        if mode == 2:
+            e0, log, _, _ = api.two_site_finite_vmps_learned(ctx, mps, dmpo, p, hist, False)
+        else:
+            e0, log = api.two_site_finite_vmps(ctx, mps, dmpo, p)
+        ctx.sync()
+        sec = time.perf_counter() - t1
+        f = dict(sweep_seconds=sec, e0=e0,
+                 lanczos_seconds=sum(r["lancz_sec"] for r in log),
+                 svd_seconds=sum(r["svd_sec"] for r in log),
+                 env_seconds=sum(r["env_sec"] for r in log),
+                 lanczos_iters=int(sum(r["iters"] for r in log)),
+                 max_trunc_err=max(r["trunc_err"] for r in log),
+                 svd_grow_rounds=int(sum(r["svd_grow_rounds"] for r in log)),
+                 energies=[r["e0"] for r in log], trunc_errs=[r["trunc_err"] for r in log])
+        if p.svd_audit:
+            aud = [r for r in log if r["svd_audit_err"] >= 0]
+            f["audit"] = dict(updates=len(aud),
+                              max_trunc_err_diff=max((r["svd_audit_err"] for r in aud),
+                                                     default=0.0),
+                              kept_state_diffs=int(sum(r["svd_audit_kept_diff"] for r in aud)))
+        out["forms"][form] = f
+        for t in mps:
+            t.close()
+    ref = out["forms"].get("fp64_exact")
+    if ref:
+        for k, f in out["forms"].items():
+            f["speedup_vs_fp64_exact"] = ref["sweep_seconds"] / f["sweep_seconds"]
+            f["rel_dE_vs_fp64_exact"] = abs(f["e0"] - ref["e0"]) / abs(ref["e0"])
+            f["max_site_rel_dE_vs_fp64_exact"] = float(np.max(
+                np.abs(np.array(f["energies"]) - np.array(ref["energies"])) /
+                np.abs(np.array(ref["energies"]))))
+            f["max_trunc_err_diff_vs_fp64_exact"] = float(np.max(
+                np.abs(np.array(f["trunc_errs"]) - np.array(ref["trunc_errs"]))))
+    for f in out["forms"].values():
+        f.pop("energies")
+        f.pop("trunc_errs")
+    s = json.dumps(out)
+    print(s)
+    if a.out:
+        with open(a.out, "w") as fh:
+            fh.write(s + "\n")
+
+
+if __name__ == "__main__":
+    main()
