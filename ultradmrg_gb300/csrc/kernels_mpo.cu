@@ -1,11 +1,12 @@
 // MPO step of the mixed-precision matvec: T3 = (W1 W2) T1 on CUDA cores,
-// grouped by (A', B) sector pair.  One CTA takes a pair and a chunk of a'
-// rows; for every 32-wide tile of the contiguous b index it stages all input
-// channels of the pair in shared memory (each T1 entry is read once), then
-// each warp produces output channels (lanes over b) as FP32 dot products with
-// the pair's coefficient matrix, split into three BF16 planes and written into
-// the step-3 tile images.  HBM bound: T1 read once (FP32), T3 written once
-// (3 x BF16).
+// grouped by (A', B) sector pair.  The work unit of one warp is (pair, a',
+// 32-wide tile of the contiguous b index): the warp stages the pair's input
+// channels for its 32 columns in a warp-private slice of shared memory (each
+// T1 entry read once, coalesced), then produces every output channel as an
+// FP32 dot product with the pair's CSR coefficient row (lanes over b), splits
+// it into three BF16 planes and writes them into the step-3 tile images.
+// Units are independent: no block-wide barrier.  HBM bound: T1 read once
+// (FP32), T3 written once (3 x BF16).
 #include <cuda_bf16.h>
 
 #include "sg_matvec.hpp"
@@ -14,83 +15,93 @@ namespace udmrg {
 
 namespace {
 
-constexpr int kAChunk = 8;  // a' rows per work unit (matches the planner)
-constexpr int kThreads = 256;
-
 __device__ __forceinline__ int canon(int r, int k, int tr) {
   return (((k >> 3) * (tr >> 3) + (r >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1);
 }
 
-__global__ void __launch_bounds__(kThreads)
-    mpo_pair_kernel(const int32_t *__restrict__ units, int nunits,
-                    const MpoPair *__restrict__ pairs, const MpoIn *__restrict__ ins,
-                    const MpoOut *__restrict__ outs, const int32_t *__restrict__ rowptr,
-                    const MpoNz *__restrict__ nz, const float *__restrict__ t1,
-                    uint8_t *__restrict__ img) {
+__global__ void mpo_unit_kernel(const int64_t *__restrict__ unit0, int npairs, int64_t nunits,
+                                const MpoPair *__restrict__ pairs, const MpoIn *__restrict__ ins,
+                                const MpoOut *__restrict__ outs,
+                                const int32_t *__restrict__ rowptr, const MpoNz *__restrict__ nz,
+                                const float *__restrict__ t1, uint8_t *__restrict__ img,
+                                int slice) {
   extern __shared__ float sm[];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  constexpr int nwarps = kThreads / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarp = blockDim.x >> 5;
+  float *X = sm + (int64_t)warp * slice;  // slice = max input channels x 32
   const int64_t plane = (int64_t)kTcBM * kTcBK * 2;
-  for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
-    const MpoPair pr = pairs[units[2 * u]];
-    const int a0 = units[2 * u + 1];
-    float *X = sm;
-    const int a1 = min(a0 + kAChunk, pr.da);
-    for (int a = a0; a < a1; ++a) {
-      for (int b0 = 0; b0 < pr.db; b0 += 32) {
-        __syncthreads();  // C loaded / previous tile consumed
-        for (int e = tid; e < pr.nin * 32; e += kThreads) {
-          const int i = e >> 5, b = b0 + (e & 31);
-          const MpoIn in = ins[pr.in0 + i];
-          X[e] = b < pr.db ? t1[in.base + (int64_t)a * in.astride + b] : 0.f;
-        }
-        __syncthreads();
-        const int b = b0 + lane;
-        for (int o = warp; o < pr.nout; o += nwarps) {
-          const int k0 = __ldg(rowptr + pr.row0 + o), k1 = __ldg(rowptr + pr.row0 + o + 1);
-          float acc = 0.f;
-          for (int k = k0; k < k1; ++k) {
-            const MpoNz e = nz[k];
-            acc = fmaf(e.v, X[(e.i << 5) + lane], acc);
-          }
-          if (b < pr.db) {
-            const MpoOut ot = outs[pr.out0 + o];
-            const int row = ot.row0 + a * ot.rstride;
-            const int col = ot.col0 + b;
-            const int64_t off = ot.img_off +
-                                ((int64_t)(row / kTcBM) * ot.kc + col / kTcBK) * 3 * plane +
-                                canon(row % kTcBM, col % kTcBK, kTcBM);
-            const __nv_bfloat16 h = __float2bfloat16_rn(acc);
-            const float r1 = acc - __bfloat162float(h);
-            const __nv_bfloat16 m = __float2bfloat16_rn(r1);
-            const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
-            *(__nv_bfloat16 *)(img + off) = h;
-            *(__nv_bfloat16 *)(img + off + plane) = m;
-            *(__nv_bfloat16 *)(img + off + 2 * plane) = l;
-          }
-        }
+  for (int64_t u = (int64_t)blockIdx.x * nwarp + warp; u < nunits;
+       u += (int64_t)gridDim.x * nwarp) {
+    // pair of this unit: the last p with unit0[p] <= u
+    int lo = 0, hi = npairs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(unit0 + mid) <= u)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const MpoPair pr = pairs[lo];
+    const int nbt = (pr.db + 31) >> 5;
+    const int64_t local = u - __ldg(unit0 + lo);
+    const int a = (int)(local / nbt);
+    const int b = (int)(local - (int64_t)a * nbt) * 32 + lane;
+    const bool col = b < pr.db;
+    for (int i = 0; i < pr.nin; ++i) {
+      const MpoIn in = ins[pr.in0 + i];
+      X[(i << 5) + lane] = col ? __ldg(t1 + in.base + (int64_t)a * in.astride + b) : 0.f;
+    }
+    __syncwarp();
+    for (int o = 0; o < pr.nout; ++o) {
+      const int k0 = __ldg(rowptr + pr.row0 + o), k1 = __ldg(rowptr + pr.row0 + o + 1);
+      float acc = 0.f;
+      for (int k = k0; k < k1; ++k) {
+        const MpoNz e = nz[k];
+        acc = fmaf(e.v, X[(e.i << 5) + lane], acc);
+      }
+      if (col) {
+        const MpoOut ot = outs[pr.out0 + o];
+        const int row = ot.row0 + a * ot.rstride;
+        const int c = ot.col0 + b;
+        const int64_t off = ot.img_off +
+                            ((int64_t)(row / kTcBM) * ot.kc + c / kTcBK) * 3 * plane +
+                            canon(row % kTcBM, c % kTcBK, kTcBM);
+        const __nv_bfloat16 h = __float2bfloat16_rn(acc);
+        const float r1 = acc - __bfloat162float(h);
+        const __nv_bfloat16 m = __float2bfloat16_rn(r1);
+        const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
+        *(__nv_bfloat16 *)(img + off) = h;
+        *(__nv_bfloat16 *)(img + off + plane) = m;
+        *(__nv_bfloat16 *)(img + off + 2 * plane) = l;
       }
     }
+    __syncwarp();  // X is rewritten by the next unit
   }
 }
 
 }  // namespace
 
 void run_mpo_step(Ctx &ctx, const SgMatvecPlan &p) {
-  const int nunits = (int)p.units.size() / 2;
+  const int npairs = (int)p.pairs.size();
+  if (npairs == 0) return;
+  const int64_t nunits = p.unit0.back();
   if (nunits == 0) return;
-  const size_t smem = (size_t)p.max_nin * 32 * sizeof(float);
-  UDMRG_REQUIRE(smem <= 200 * 1024, "mixed matvec: too many MPO input channels in a sector pair");
+  const int slice = std::max(1, p.max_nin) * 32;
+  const size_t per_warp = (size_t)slice * sizeof(float);
+  UDMRG_REQUIRE(per_warp <= 200 * 1024, "mixed matvec: too many MPO input channels in a pair");
+  const int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (96 * 1024) / per_warp));
+  const size_t smem = per_warp * warps;
   static size_t attr = 0;
   if (smem > 48 * 1024 && smem > attr) {
-    UDMRG_CHECK_CUDA(cudaFuncSetAttribute(mpo_pair_kernel,
+    UDMRG_CHECK_CUDA(cudaFuncSetAttribute(mpo_unit_kernel,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = smem;
   }
-  const int grid = std::min(nunits, 16 * ctx.num_sms);
-  mpo_pair_kernel<<<grid, kThreads, smem, ctx.stream>>>(p.d_units, nunits, p.d_pairs, p.d_ins,
-                                                         p.d_outs, p.d_rowptr, p.d_nz, p.t1,
-                                                         p.t3_img);
+  const int64_t blocks = (nunits + warps - 1) / warps;
+  const int grid = (int)std::min<int64_t>(blocks, 16 * (int64_t)ctx.num_sms);
+  mpo_unit_kernel<<<grid, 32 * warps, smem, ctx.stream>>>(p.d_unit0, npairs, nunits, p.d_pairs,
+                                                          p.d_ins, p.d_outs, p.d_rowptr, p.d_nz,
+                                                          p.t1, p.t3_img, slice);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches++;
 }

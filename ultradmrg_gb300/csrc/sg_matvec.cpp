@@ -9,7 +9,7 @@ SgMatvecPlan::~SgMatvecPlan() {
   for (void *p : {(void *)l_img, (void *)psi_img, (void *)t3_img, (void *)r_img, (void *)t1,
                   (void *)d_psi_ops, (void *)d_targets, (void *)d_sources, (void *)d_coefs,
                   (void *)d_pairs, (void *)d_ins, (void *)d_outs, (void *)d_rowptr,
-                  (void *)d_nz, (void *)d_units})
+                  (void *)d_nz, (void *)d_unit0})
     ctx->free(p);
 }
 
@@ -304,7 +304,6 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   {
     std::map<std::pair<int32_t, int32_t>, std::vector<int>> by_pair;
     for (size_t t = 0; t < p->targets.size(); ++t) by_pair[tgt_key[t]].push_back((int)t);
-    constexpr int kAChunk = 8;
     for (auto &kv : by_pair) {
       MpoPair pr{};
       pr.in0 = (int32_t)p->ins.size();
@@ -363,11 +362,9 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       }
       p->max_nin = std::max(p->max_nin, (int)pr.nin);
       p->max_nout = std::max(p->max_nout, (int)pr.nout);
-      const int32_t pid = (int32_t)p->pairs.size();
-      for (int a = 0; a < pr.da; a += kAChunk) {
-        p->units.push_back(pid);
-        p->units.push_back(a);
-      }
+      // work units: one per (a', 32-wide tile of b); prefix over the pairs
+      if (p->unit0.empty()) p->unit0.push_back(0);
+      p->unit0.push_back(p->unit0.back() + (int64_t)pr.da * ((pr.db + 31) / 32));
       p->pairs.push_back(pr);
     }
   }
@@ -376,7 +373,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   p->d_outs = upload_vec(ctx, p->outs);
   p->d_rowptr = upload_vec(ctx, p->rowptr);
   p->d_nz = upload_vec(ctx, p->nz);
-  p->d_units = upload_vec(ctx, p->units);
+  p->d_unit0 = upload_vec(ctx, p->unit0);
   p->mixed_flops = 6.0 * (p->g1.flops + p->g3.flops);
   ctx.sync();
   return p;

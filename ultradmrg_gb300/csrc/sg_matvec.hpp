@@ -89,13 +89,13 @@ struct SgMatvecPlan {
   std::vector<MpoOut> outs;
   std::vector<int32_t> rowptr;  // CSR row pointers over all output channels (+1)
   std::vector<MpoNz> nz;
-  std::vector<int32_t> units;  // (pair, first a') work units, flattened pairs
+  std::vector<int64_t> unit0;  // first work unit of each pair (prefix, pairs + 1 entries)
   MpoPair *d_pairs = nullptr;
   MpoIn *d_ins = nullptr;
   MpoOut *d_outs = nullptr;
   int32_t *d_rowptr = nullptr;
   MpoNz *d_nz = nullptr;
-  int32_t *d_units = nullptr;
+  int64_t *d_unit0 = nullptr;
   int max_nin = 0, max_nout = 0;
   double mixed_flops = 0;  // tensor-core work actually issued (2MNK per group, x6 products)
   ~SgMatvecPlan();

@@ -37,6 +37,24 @@ __device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t parity) {
   }
 }
 
+// FP32 -> FP64 by bit manipulation on the integer pipes (exact for normal
+// numbers; sub-normal FP32 values, below 1.2e-38, become zero): the FP64
+// conversion instruction would run on this GPU's narrow FP64 pipe.
+__device__ __forceinline__ double widen_f32(float v) {
+  const uint32_t u = __float_as_uint(v);
+  const uint64_t sign = (uint64_t)(u >> 31) << 63;
+  const uint32_t e = (u >> 23) & 0xFFu;
+  const uint64_t m = (uint64_t)(u & 0x7FFFFFu) << 29;
+  uint64_t d;
+  if (e == 0)
+    d = sign;
+  else if (e == 0xFFu)
+    d = sign | (0x7FFull << 52) | m;
+  else
+    d = sign | ((uint64_t)(e + 896u) << 52) | m;
+  return __longlong_as_double((long long)d);
+}
+
 // Byte offset of element (r, k) inside one plane of a TR x 64 tile.
 __device__ __forceinline__ int canon_off(int r, int k, int tr) {
   return (((k >> 3) * (tr >> 3) + (r >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1);
@@ -46,15 +64,6 @@ template <typename T>
 __device__ __forceinline__ void split3(T x, __nv_bfloat16 &h, __nv_bfloat16 &m,
                                        __nv_bfloat16 &l);
 template <>
-__device__ __forceinline__ void split3<double>(double x, __nv_bfloat16 &h, __nv_bfloat16 &m,
-                                               __nv_bfloat16 &l) {
-  h = __double2bfloat16(x);
-  const double r1 = x - (double)__bfloat162float(h);
-  m = __double2bfloat16(r1);
-  const double r2 = r1 - (double)__bfloat162float(m);
-  l = __double2bfloat16(r2);
-}
-template <>
 __device__ __forceinline__ void split3<float>(float x, __nv_bfloat16 &h, __nv_bfloat16 &m,
                                               __nv_bfloat16 &l) {
   h = __float2bfloat16_rn(x);
@@ -62,6 +71,37 @@ __device__ __forceinline__ void split3<float>(float x, __nv_bfloat16 &h, __nv_bf
   m = __float2bfloat16_rn(r1);
   const float r2 = r1 - __bfloat162float(m);
   l = __float2bfloat16_rn(r2);
+}
+
+// FP64 -> FP32, round to nearest even, on the integer pipes (the conversion
+// instruction would use this GPU's narrow FP64 pipe).  |x| below the FP32
+// normal range (1.2e-38) becomes zero, overflow becomes infinity.
+__device__ __forceinline__ float narrow_f64(double x) {
+  const uint64_t d = (uint64_t)__double_as_longlong(x);
+  const uint32_t sign = (uint32_t)(d >> 63) << 31;
+  const int e = (int)((d >> 52) & 0x7FF);
+  const uint64_t mant = d & 0xFFFFFFFFFFFFFull;
+  if (e == 0x7FF) return __uint_as_float(sign | 0x7F800000u | (mant ? 0x400000u : 0u));
+  int fe = e - 1023 + 127;
+  if (fe >= 255) return __uint_as_float(sign | 0x7F800000u);
+  if (fe <= 0) return __uint_as_float(sign);
+  uint32_t fm = (uint32_t)(mant >> 29);
+  const uint64_t rest = mant & 0x1FFFFFFFull;
+  if (rest > 0x10000000ull || (rest == 0x10000000ull && (fm & 1u))) {
+    if (++fm == 0x800000u) {
+      fm = 0;
+      if (++fe >= 255) return __uint_as_float(sign | 0x7F800000u);
+    }
+  }
+  return __uint_as_float(sign | ((uint32_t)fe << 23) | fm);
+}
+
+// FP64 operands are narrowed to FP32 first: the three BF16 planes hold ~24
+// significant bits either way, and the split then runs in FP32.
+template <>
+__device__ __forceinline__ void split3<double>(double x, __nv_bfloat16 &h, __nv_bfloat16 &m,
+                                               __nv_bfloat16 &l) {
+  split3<float>(narrow_f64(x), h, m, l);
 }
 
 template <typename T>
@@ -222,6 +262,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       const bool row_ok = grow < g.M;
       const int64_t base = row_ok ? rowaddr[g.row0 + grow] : 0;
       const int n0 = tile.ntile * kTcBN;
+      // epilogue math in FP32 (the accumulator's precision); no FP64 instruction
+      const float af = (float)alpha;
 #pragma unroll
       for (int cb = 0; cb < kTcBN / 16; ++cb) {
         uint32_t r[16];
@@ -232,11 +274,11 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int j = 0; j < 16; ++j) {
             const int n = n0 + cb * 16 + j;
             if (n < g.N) {
-              const float v = g.kc > 0 ? __uint_as_float(r[j]) : 0.0f;
+              const float v = g.kc > 0 ? af * __uint_as_float(r[j]) : 0.0f;
               if (out_kind == kTcOutF64)
-                ((double *)out)[base + n] = alpha * (double)v;
+                ((double *)out)[base + n] = widen_f32(v);
               else
-                ((float *)out)[base + n] = (float)(alpha * (double)v);
+                ((float *)out)[base + n] = v;
             }
           }
         }
