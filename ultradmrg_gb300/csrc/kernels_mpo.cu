@@ -19,7 +19,8 @@ __device__ __forceinline__ int canon(int r, int k, int tr) {
   return (((k >> 3) * (tr >> 3) + (r >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1);
 }
 
-__global__ void mpo_unit_kernel(const int64_t *__restrict__ unit0, int npairs, int64_t nunits,
+__global__ void mpo_unit_kernel(const int64_t *__restrict__ unit0,
+                                const int32_t *__restrict__ unit_pair, int64_t nunits,
                                 const MpoPair *__restrict__ pairs, const MpoIn *__restrict__ ins,
                                 const MpoOut *__restrict__ outs,
                                 const int32_t *__restrict__ rowptr, const MpoNz *__restrict__ nz,
@@ -32,15 +33,7 @@ __global__ void mpo_unit_kernel(const int64_t *__restrict__ unit0, int npairs, i
   const int64_t plane = (int64_t)kTcBM * kTcBK * 2;
   for (int64_t u = (int64_t)blockIdx.x * nwarp + warp; u < nunits;
        u += (int64_t)gridDim.x * nwarp) {
-    // pair of this unit: the last p with unit0[p] <= u
-    int lo = 0, hi = npairs - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (__ldg(unit0 + mid) <= u)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
+    const int lo = __ldg(unit_pair + u);
     const MpoPair pr = pairs[lo];
     const int nbt = (pr.db + 31) >> 5;
     const int64_t local = u - __ldg(unit0 + lo);
@@ -99,7 +92,8 @@ void run_mpo_step(Ctx &ctx, const SgMatvecPlan &p) {
   }
   const int64_t blocks = (nunits + warps - 1) / warps;
   const int grid = (int)std::min<int64_t>(blocks, 16 * (int64_t)ctx.num_sms);
-  mpo_unit_kernel<<<grid, 32 * warps, smem, ctx.stream>>>(p.d_unit0, npairs, nunits, p.d_pairs,
+  mpo_unit_kernel<<<grid, 32 * warps, smem, ctx.stream>>>(p.d_unit0, p.d_unit_pair, nunits,
+                                                          p.d_pairs,
                                                           p.d_ins, p.d_outs, p.d_rowptr, p.d_nz,
                                                           p.t1, p.t3_img, slice);
   UDMRG_CHECK_CUDA(cudaGetLastError());

@@ -9,7 +9,7 @@ SgMatvecPlan::~SgMatvecPlan() {
   for (void *p : {(void *)l_img, (void *)psi_img, (void *)t3_img, (void *)r_img, (void *)t1,
                   (void *)d_psi_ops, (void *)d_targets, (void *)d_sources, (void *)d_coefs,
                   (void *)d_pairs, (void *)d_ins, (void *)d_outs, (void *)d_rowptr,
-                  (void *)d_nz, (void *)d_unit0})
+                  (void *)d_nz, (void *)d_unit0, (void *)d_unit_pair})
     ctx->free(p);
 }
 
@@ -362,9 +362,12 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       }
       p->max_nin = std::max(p->max_nin, (int)pr.nin);
       p->max_nout = std::max(p->max_nout, (int)pr.nout);
-      // work units: one per (a', 32-wide tile of b); prefix over the pairs
+      // work units: one per (a', 32-wide tile of b); prefix over the pairs and
+      // the pair of every unit
       if (p->unit0.empty()) p->unit0.push_back(0);
-      p->unit0.push_back(p->unit0.back() + (int64_t)pr.da * ((pr.db + 31) / 32));
+      const int64_t nu = (int64_t)pr.da * ((pr.db + 31) / 32);
+      p->unit0.push_back(p->unit0.back() + nu);
+      p->unit_pair.insert(p->unit_pair.end(), nu, (int32_t)p->pairs.size());
       p->pairs.push_back(pr);
     }
   }
@@ -374,6 +377,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   p->d_rowptr = upload_vec(ctx, p->rowptr);
   p->d_nz = upload_vec(ctx, p->nz);
   p->d_unit0 = upload_vec(ctx, p->unit0);
+  p->d_unit_pair = upload_vec(ctx, p->unit_pair);
   p->mixed_flops = 6.0 * (p->g1.flops + p->g3.flops);
   ctx.sync();
   return p;

@@ -90,12 +90,14 @@ struct SgMatvecPlan {
   std::vector<int32_t> rowptr;  // CSR row pointers over all output channels (+1)
   std::vector<MpoNz> nz;
   std::vector<int64_t> unit0;  // first work unit of each pair (prefix, pairs + 1 entries)
+  std::vector<int32_t> unit_pair;  // pair of every work unit
   MpoPair *d_pairs = nullptr;
   MpoIn *d_ins = nullptr;
   MpoOut *d_outs = nullptr;
   int32_t *d_rowptr = nullptr;
   MpoNz *d_nz = nullptr;
   int64_t *d_unit0 = nullptr;
+  int32_t *d_unit_pair = nullptr;
   int max_nin = 0, max_nout = 0;
   double mixed_flops = 0;  // tensor-core work actually issued (2MNK per group, x6 products)
   ~SgMatvecPlan();

@@ -96,6 +96,9 @@ __device__ __forceinline__ float narrow_f64(double x) {
   return __uint_as_float(sign | ((uint32_t)fe << 23) | fm);
 }
 
+__device__ __forceinline__ float to_f32(float x) { return x; }
+__device__ __forceinline__ float to_f32(double x) { return narrow_f64(x); }
+
 // FP64 operands are narrowed to FP32 first: the three BF16 planes hold ~24
 // significant bits either way, and the split then runs in FP32.
 template <>
@@ -104,25 +107,62 @@ __device__ __forceinline__ void split3<double>(double x, __nv_bfloat16 &h, __nv_
   split3<float>(narrow_f64(x), h, m, l);
 }
 
+// Pack sub-matrices into split-BF16 images.  A 32 x 64 tile of the source is
+// staged in shared memory (as FP32), loaded along whichever source direction
+// is contiguous, then written row by row with lanes along K (canonical
+// layout: 8 consecutive K values of a row are 16 contiguous bytes).
 template <typename T>
-__global__ void pack_kernel(const PackOp *__restrict__ ops, int nops, const T *__restrict__ src,
-                            uint8_t *__restrict__ img) {
+__global__ void __launch_bounds__(256)
+    pack_kernel(const PackOp *__restrict__ ops, int nops, const T *__restrict__ src,
+                uint8_t *__restrict__ img) {
+  __shared__ float tile[32][65];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int o = blockIdx.x; o < nops; o += gridDim.x) {
     const PackOp op = ops[o];
-    const int64_t tot = (int64_t)op.rows * op.cols;
     const int64_t plane = (int64_t)op.tr * kTcBK * 2;
-    for (int64_t e = threadIdx.x; e < tot; e += blockDim.x) {
-      const int r = (int)(e / op.cols), k = (int)(e - (int64_t)r * op.cols);
-      const T x = src[op.src_off + r * op.src_rs + k * op.src_cs];
-      __nv_bfloat16 h, m, l;
-      split3<T>(x, h, m, l);
-      const int rr = op.r0 + r, kk = op.k0 + k;
-      const int64_t unit = ((int64_t)(rr / op.tr) * op.kc + kk / kTcBK) * 3 * plane;
-      const int64_t off = op.img_off + unit + canon_off(rr % op.tr, kk % kTcBK, op.tr);
-      *(__nv_bfloat16 *)(img + off) = h;
-      *(__nv_bfloat16 *)(img + off + plane) = m;
-      *(__nv_bfloat16 *)(img + off + 2 * plane) = l;
-    }
+    const int ts = op.tr == 128 ? 7 : 6;
+    const bool rows_contig = op.src_rs == 1 && op.src_cs != 1;
+    for (int r0 = 0; r0 < op.rows; r0 += 32)
+      for (int k0 = 0; k0 < op.cols; k0 += 64) {
+        __syncthreads();  // the previous tile has been written out
+        for (int e = tid; e < 32 * 64; e += 256) {
+          int r, k;
+          if (rows_contig) {
+            r = e & 31;
+            k = e >> 5;
+          } else {
+            k = e & 63;
+            r = e >> 6;
+          }
+          const int rr = r0 + r, kk = k0 + k;
+          float v = 0.f;
+          if (rr < op.rows && kk < op.cols) {
+            const T x = src[op.src_off + (int64_t)rr * op.src_rs + (int64_t)kk * op.src_cs];
+            v = to_f32(x);
+          }
+          tile[r][k] = v;
+        }
+        __syncthreads();
+        for (int r = warp; r < 32; r += 8) {
+          const int rs = r0 + r;
+          if (rs >= op.rows) break;
+          const int rr = op.r0 + rs;
+          const int64_t rowbase = op.img_off + (int64_t)(rr >> ts) * op.kc * 3 * plane;
+          const int rin = rr & (op.tr - 1);
+          for (int k = lane; k < 64; k += 32) {
+            const int ks = k0 + k;
+            if (ks >= op.cols) break;
+            __nv_bfloat16 h, m, l;
+            split3<float>(tile[r][k], h, m, l);
+            const int kk = op.k0 + ks;
+            const int64_t off =
+                rowbase + (int64_t)(kk >> 6) * 3 * plane + canon_off(rin, kk & 63, op.tr);
+            *(__nv_bfloat16 *)(img + off) = h;
+            *(__nv_bfloat16 *)(img + off + plane) = m;
+            *(__nv_bfloat16 *)(img + off + 2 * plane) = l;
+          }
+        }
+      }
   }
 }
 
