@@ -54,14 +54,21 @@ struct SubDim {
   int64_t sa, sb;  // strides in operand A / B (unused one = 0)
 };
 
+constexpr int kMaxRank = 8;
+
 // Row-major strides of a block with the given sector ids.
-void block_strides(const BTensor &T, int64_t b, std::vector<int64_t> &st) {
+void block_strides(const BTensor &T, int64_t b, int64_t *st) {
   const int r = T.rank();
-  st.assign(r, 1);
+  st[r - 1] = 1;
   for (int i = r - 2; i >= 0; --i) st[i] = st[i + 1] * T.dim_of(b, i + 1);
 }
 
-struct Pair {
+// Sector-id tuples packed 16 bits per axis, first axis in the highest bits,
+// so integer order is the lexicographic order of the tuples.
+using Key128 = unsigned __int128;
+
+struct Match {
+  Key128 okey;
   int64_t a, b;
 };
 
@@ -110,32 +117,54 @@ static std::unique_ptr<ContractPlan> plan_impl(const BTensor &A, const BTensor &
   const int ro = out->rank();
   UDMRG_REQUIRE(ro > 0, "contract: full contractions to a scalar are not supported here");
 
-  // B blocks grouped by contracted sector ids
-  std::map<std::vector<int32_t>, std::vector<int64_t>> bgroups;
+  UDMRG_REQUIRE(A.rank() <= kMaxRank && B.rank() <= kMaxRank && ro <= kMaxRank,
+                "contract: tensors of rank above 8 are not supported");
+  for (const BTensor *T : {&A, &B})
+    for (const Index &ix : T->idx)
+      UDMRG_REQUIRE(ix.nsec() < 65536, "contract: more than 65535 sectors on one index");
+  // B blocks sorted by their contracted sector ids
+  std::vector<std::pair<uint64_t, int64_t>> bk(B.nblocks());
   for (int64_t b = 0; b < B.nblocks(); ++b) {
-    std::vector<int32_t> k;
-    for (int ax : cb) k.push_back(B.key(b)[ax]);
-    bgroups[k].push_back(b);
+    uint64_t k = 0;
+    for (int ax : cb) k = (k << 16) | (uint64_t)B.key(b)[ax];
+    bk[b] = {k, b};
   }
-  // enumerate matching pairs -> output keys
-  std::map<std::vector<int32_t>, std::vector<Pair>> outmap;
+  std::sort(bk.begin(), bk.end());
+  // matching pairs with their output keys, sorted by (output key, a, b)
+  std::vector<Match> matches;
   for (int64_t a = 0; a < A.nblocks(); ++a) {
-    std::vector<int32_t> k;
-    for (int ax : ca) k.push_back(A.key(a)[ax]);
-    auto it = bgroups.find(k);
-    if (it == bgroups.end()) continue;
-    for (int64_t b : it->second) {
-      std::vector<int32_t> ok;
-      ok.reserve(ro);
-      for (int ax : fa) ok.push_back(A.key(a)[ax]);
-      for (int ax : fb) ok.push_back(B.key(b)[ax]);
-      outmap[ok].push_back({a, b});
+    uint64_t k = 0;
+    for (int ax : ca) k = (k << 16) | (uint64_t)A.key(a)[ax];
+    auto it = std::lower_bound(bk.begin(), bk.end(), std::make_pair(k, (int64_t)-1));
+    Key128 ka = 0;
+    for (int ax : fa) ka = (ka << 16) | (Key128)A.key(a)[ax];
+    for (; it != bk.end() && it->first == k; ++it) {
+      Key128 ok = ka;
+      for (int ax : fb) ok = (ok << 16) | (Key128)B.key(it->second)[ax];
+      matches.push_back({ok, a, it->second});
     }
   }
+  std::sort(matches.begin(), matches.end(), [](const Match &x, const Match &y) {
+    if (x.okey != y.okey) return x.okey < y.okey;
+    if (x.a != y.a) return x.a < y.a;
+    return x.b < y.b;
+  });
+  // output blocks = distinct keys; [mstart[o], mstart[o + 1]) are their matches
   std::vector<int32_t> flat;
-  flat.reserve(outmap.size() * ro);
-  for (auto &kv : outmap) flat.insert(flat.end(), kv.first.begin(), kv.first.end());
-  out->set_blocks(flat);  // std::map iteration is already sorted and unique
+  std::vector<size_t> mstart;
+  for (size_t i = 0; i < matches.size(); ++i) {
+    if (i > 0 && matches[i].okey == matches[i - 1].okey) continue;
+    mstart.push_back(i);
+    flat.resize(flat.size() + ro);
+    Key128 ok = matches[i].okey;
+    for (int j = ro - 1; j >= 0; --j) {
+      flat[flat.size() - ro + j] = (int32_t)(uint32_t)(ok & 0xFFFF);
+      ok >>= 16;
+    }
+  }
+  mstart.push_back(matches.size());
+  const size_t nout = mstart.size() - 1;
+  out->set_blocks(flat);  // sorted and unique by construction
 
   const BTensor *C = out.get();
   if (dst) {
@@ -143,112 +172,134 @@ static std::unique_ptr<ContractPlan> plan_impl(const BTensor &A, const BTensor &
     for (int i = 0; i < ro; ++i)
       UDMRG_REQUIRE(dst->idx[i] == out->idx[i], "contract-into: index mismatch");
     C = dst;
-    if (missing) {
-      missing->clear();
-      std::vector<char> hit(dst->nblocks(), 0);
-      for (auto &kv : outmap) {
-        int64_t id = dst->find(kv.first);
-        UDMRG_REQUIRE(id >= 0, "contract-into: produced block absent from destination");
-        hit[id] = 1;
+  }
+  // destination block of every output block
+  std::vector<int64_t> dest(nout);
+  {
+    std::vector<int32_t> okey(ro);
+    std::vector<char> hit(dst ? dst->nblocks() : 0, 0);
+    for (size_t o = 0; o < nout; ++o) {
+      if (!dst) {
+        dest[o] = (int64_t)o;
+        continue;
       }
+      std::copy(flat.begin() + o * ro, flat.begin() + (o + 1) * ro, okey.begin());
+      const int64_t id = dst->find(okey);
+      UDMRG_REQUIRE(id >= 0, "contract-into: produced block absent from destination");
+      dest[o] = id;
+      hit[id] = 1;
+    }
+    if (dst && missing) {
+      missing->clear();
       for (int64_t i = 0; i < dst->nblocks(); ++i)
         if (!hit[i]) missing->push_back(i);
     }
   }
 
   GemmPlan &g = plan->gemm;
-  std::vector<int64_t> sa, sb;
+  int64_t sa[kMaxRank], sb[kMaxRank];
   const double cplx = A.dtype == kC128 ? 4.0 : 1.0;
-  for (auto &kv : outmap) {
-    const std::vector<int32_t> &okey = kv.first;
-    const std::vector<Pair> &pairs = kv.second;
+  const int nmi = (int)fa.size(), nni = (int)fb.size();
+  // merged groups of free axes: (extent, index of the last original axis),
+  // extent-1 groups dropped
+  auto groups = [](const int64_t *ext, int n, const char *mg, int64_t *gext, int *glast) {
+    int ng = 0;
+    int64_t ce = 1;
+    int cl = -1;
+    for (int i = 0; i < n; ++i) {
+      if (i > 0 && mg[i - 1]) {
+        ce *= ext[i];
+        cl = i;
+      } else {
+        if (cl >= 0 && ce != 1) {
+          gext[ng] = ce;
+          glast[ng++] = cl;
+        }
+        ce = ext[i];
+        cl = i;
+      }
+    }
+    if (cl >= 0 && ce != 1) {
+      gext[ng] = ce;
+      glast[ng++] = cl;
+    }
+    return ng;
+  };
+  for (size_t o = 0; o < nout; ++o) {
+    const int32_t *okey = flat.data() + o * ro;
+    const size_t m0 = mstart[o], m1 = mstart[o + 1];
     GProb p{};
-    p.c_off = C->offs[dst ? dst->find(okey) : (int64_t)g.probs.size()];
+    p.c_off = C->offs[dest[o]];
     // M / N sub-dims (extents are the output block's sector dims)
-    std::vector<int64_t> mext, next;
-    for (size_t i = 0; i < fa.size(); ++i) mext.push_back(A.idx[fa[i]].dims[okey[i]]);
-    for (size_t i = 0; i < fb.size(); ++i) next.push_back(B.idx[fb[i]].dims[okey[fa.size() + i]]);
+    int64_t mext[kMaxRank], next[kMaxRank];
+    for (int i = 0; i < nmi; ++i) mext[i] = A.idx[fa[i]].dims[okey[i]];
+    for (int i = 0; i < nni; ++i) next[i] = B.idx[fb[i]].dims[okey[nmi + i]];
     // merge decisions valid for all segments
-    const int nmi = (int)mext.size(), nni = (int)next.size();
-    std::vector<char> mmerge(std::max(nmi - 1, 0), 1), nmerge(std::max(nni - 1, 0), 1);
-    for (auto &pr : pairs) {
-      block_strides(A, pr.a, sa);
-      block_strides(B, pr.b, sb);
+    char mmerge[kMaxRank], nmerge[kMaxRank];
+    for (int i = 0; i < kMaxRank; ++i) mmerge[i] = nmerge[i] = 1;
+    for (size_t q = m0; q < m1; ++q) {
+      block_strides(A, matches[q].a, sa);
+      block_strides(B, matches[q].b, sb);
       for (int i = 0; i + 1 < nmi; ++i)
         if (sa[fa[i]] != mext[i + 1] * sa[fa[i + 1]]) mmerge[i] = 0;
       for (int i = 0; i + 1 < nni; ++i)
         if (sb[fb[i]] != next[i + 1] * sb[fb[i + 1]]) nmerge[i] = 0;
     }
-    // build merged M groups: list of (ext, index of last original dim)
-    auto groups = [](const std::vector<int64_t> &ext, const std::vector<char> &mg) {
-      std::vector<std::pair<int64_t, int>> gr;
-      for (int i = 0; i < (int)ext.size(); ++i) {
-        if (i > 0 && mg[i - 1]) {
-          gr.back().first *= ext[i];
-          gr.back().second = i;
-        } else {
-          gr.push_back({ext[i], i});
-        }
-      }
-      // drop extent-1 groups
-      std::vector<std::pair<int64_t, int>> r;
-      for (auto &x : gr)
-        if (x.first != 1) r.push_back(x);
-      return r;
-    };
-    auto mg = groups(mext, mmerge);
-    auto ng = groups(next, nmerge);
-    UDMRG_REQUIRE(mg.size() <= (size_t)kMaxSub && ng.size() <= (size_t)kMaxSub,
-                  "contract: too many non-mergeable free axes");
+    int64_t mgx[kMaxRank], ngx[kMaxRank];
+    int mgl[kMaxRank], ngl[kMaxRank];
+    const int nmg = groups(mext, nmi, mmerge, mgx, mgl);
+    const int nng = groups(next, nni, nmerge, ngx, ngl);
+    UDMRG_REQUIRE(nmg <= kMaxSub && nng <= kMaxSub, "contract: too many non-mergeable free axes");
     int64_t M = 1, N = 1;
-    for (auto &x : mext) M *= x;
-    for (auto &x : next) N *= x;
+    for (int i = 0; i < nmi; ++i) M *= mext[i];
+    for (int i = 0; i < nni; ++i) N *= next[i];
     UDMRG_REQUIRE(M < (1ll << 31) && N < (1ll << 31), "contract: block too large");
     p.M = (int32_t)M;
     p.N = (int32_t)N;
-    p.nm = (int32_t)mg.size();
-    p.nn = (int32_t)ng.size();
-    for (size_t j = 0; j < mg.size(); ++j) p.m_ext[j] = (int32_t)mg[j].first;
-    for (size_t j = 0; j < ng.size(); ++j) p.n_ext[j] = (int32_t)ng[j].first;
+    p.nm = nmg;
+    p.nn = nng;
+    for (int j = 0; j < nmg; ++j) p.m_ext[j] = (int32_t)mgx[j];
+    for (int j = 0; j < nng; ++j) p.n_ext[j] = (int32_t)ngx[j];
     p.seg0 = (int32_t)g.segs.size();
-    p.nseg = (int32_t)pairs.size();
+    p.nseg = (int32_t)(m1 - m0);
     double kflops = 0;
-    for (auto &pr : pairs) {
-      block_strides(A, pr.a, sa);
-      block_strides(B, pr.b, sb);
-      GSeg s{};
-      s.a_off = A.offs[pr.a];
-      s.b_off = B.offs[pr.b];
-      for (size_t j = 0; j < mg.size(); ++j) s.a_ms[j] = sa[fa[mg[j].second]];
-      for (size_t j = 0; j < ng.size(); ++j) s.b_ns[j] = sb[fb[ng[j].second]];
-      // K sub-dims with merging where both operands allow it
-      std::vector<SubDim> kd;
+    for (size_t q = m0; q < m1; ++q) {
+      const int64_t pa = matches[q].a, pb = matches[q].b;
+      block_strides(A, pa, sa);
+      block_strides(B, pb, sb);
+      GSeg sg{};
+      sg.a_off = A.offs[pa];
+      sg.b_off = B.offs[pb];
+      for (int j = 0; j < nmg; ++j) sg.a_ms[j] = sa[fa[mgl[j]]];
+      for (int j = 0; j < nng; ++j) sg.b_ns[j] = sb[fb[ngl[j]]];
+      // K sub-dims merged where both operands allow it; unit dims dropped
+      SubDim kd[kMaxRank];
+      int nk = 0;
       for (size_t i = 0; i < ca.size(); ++i) {
-        SubDim d{A.dim_of(pr.a, ca[i]), sa[ca[i]], sb[cb[i]]};
-        if (!kd.empty() && kd.back().sa == d.ext * d.sa && kd.back().sb == d.ext * d.sb) {
-          kd.back().ext *= d.ext;
-          kd.back().sa = d.sa;
-          kd.back().sb = d.sb;
+        SubDim d{A.dim_of(pa, ca[i]), sa[ca[i]], sb[cb[i]]};
+        if (nk > 0 && kd[nk - 1].sa == d.ext * d.sa && kd[nk - 1].sb == d.ext * d.sb) {
+          kd[nk - 1].ext *= d.ext;
+          kd[nk - 1].sa = d.sa;
+          kd[nk - 1].sb = d.sb;
         } else if (d.ext != 1) {
-          kd.push_back(d);
+          kd[nk++] = d;
         }
       }
-      // drop unit dims that slipped in through the first slot
-      std::vector<SubDim> kd2;
-      for (auto &d : kd)
-        if (d.ext != 1) kd2.push_back(d);
-      UDMRG_REQUIRE(kd2.size() <= (size_t)kMaxSub, "contract: too many contracted sub-dims");
+      int nk2 = 0;
+      for (int i = 0; i < nk; ++i)
+        if (kd[i].ext != 1) kd[nk2++] = kd[i];
+      UDMRG_REQUIRE(nk2 <= kMaxSub, "contract: too many contracted sub-dims");
       int64_t K = 1;
-      for (auto &d : kd2) K *= d.ext;
-      s.nk = (int32_t)kd2.size();
-      s.K = (int32_t)K;
-      for (size_t j = 0; j < kd2.size(); ++j) {
-        s.k_ext[j] = (int32_t)kd2[j].ext;
-        s.a_ks[j] = kd2[j].sa;
-        s.b_ks[j] = kd2[j].sb;
+      for (int i = 0; i < nk2; ++i) K *= kd[i].ext;
+      sg.nk = nk2;
+      sg.K = (int32_t)K;
+      for (int j = 0; j < nk2; ++j) {
+        sg.k_ext[j] = (int32_t)kd[j].ext;
+        sg.a_ks[j] = kd[j].sa;
+        sg.b_ks[j] = kd[j].sb;
       }
       kflops += (double)K;
-      g.segs.push_back(s);
+      g.segs.push_back(sg);
     }
     g.flops += 2.0 * cplx * (double)M * (double)N * kflops;
     add_tiles(g, (int32_t)g.probs.size(), M, N);
