@@ -1,5 +1,6 @@
 #include "sg_matvec.hpp"
 
+#include <array>
 #include <map>
 
 namespace udmrg {
@@ -150,7 +151,13 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   std::map<int32_t, std::vector<int64_t>> w1_by_s1o;
   for (int64_t b = 0; b < W1.nblocks(); ++b) w1_by_s1o[W1.key(b)[2]].push_back(b);
   std::vector<std::pair<int32_t, int32_t>> tgt_key;  // (A', B) of every target
-  std::map<Key, std::vector<int64_t>> w2_by;  // (wr, s2out, w2)
+  std::map<std::array<int32_t, 3>, std::vector<int64_t>> w2_by;  // (wr, s2out, w2)
+  // fused W1 W2 coefficients per (s1', s2', w2): the contributing (W, S1, S2)
+  struct CoefEntry {
+    std::array<int32_t, 3> src;  // (W, S1, S2)
+    std::vector<double> coef;    // nin x nout
+  };
+  std::map<std::array<int32_t, 3>, std::vector<CoefEntry>> coef_cache;
   for (int64_t b = 0; b < W2.nblocks(); ++b)
     w2_by[{W2.key(b)[0], W2.key(b)[2], W2.key(b)[3]}].push_back(b);
   for (int Bp = 0; Bp < nB; ++Bp) {
@@ -211,19 +218,20 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
         tg.dw2 = dw2;
         tg.nout = tg.ds12p * dw2;
         tg.src0 = (int32_t)p->sources.size();
-        // sources: T1 blocks (A', W, S1, S2, B) through W1 (W,S1,S1p,Wr) W2 (Wr,S2,S2p,W2s)
-        std::map<Key, std::vector<double>> acc;  // (W, S1, S2) -> coef
-        auto it1 = w1_by_s1o.find(S1p);
-        if (it1 != w1_by_s1o.end()) {
-          for (int64_t b1 : it1->second) {
-            const int32_t Ws = W1.key(b1)[0], S1 = W1.key(b1)[1], Wr = W1.key(b1)[3];
-            for (int32_t S2 = 0; S2 < W2.idx[1].nsec(); ++S2) {
+        // sources: T1 blocks (A', W, S1, S2, B) through W1 (W,S1,S1p,Wr) W2 (Wr,S2,S2p,W2s);
+        // the fused coefficients depend on the MPO sectors only and are cached
+        const std::array<int32_t, 3> ck = {S1p, S2p, W2s};
+        auto cit = coef_cache.find(ck);
+        if (cit == coef_cache.end()) {
+          std::map<std::array<int32_t, 3>, std::vector<double>> acc;  // (W, S1, S2) -> coef
+          auto it1 = w1_by_s1o.find(S1p);
+          if (it1 != w1_by_s1o.end()) {
+            for (int64_t b1 : it1->second) {
+              const int32_t Ws = W1.key(b1)[0], S1 = W1.key(b1)[1], Wr = W1.key(b1)[3];
               auto it2 = w2_by.find({Wr, S2p, W2s});
-              if (it2 == w2_by.end()) break;
+              if (it2 == w2_by.end()) continue;
               for (int64_t b2 : it2->second) {
-                if (W2.key(b2)[1] != S2) continue;
-                Key src = {Ap, Ws, S1, S2, Bs};
-                if (!t1map.count(src)) continue;
+                const int32_t S2 = W2.key(b2)[1];
                 const int64_t dw = W1.idx[0].dims[Ws], ds1 = W1.idx[1].dims[S1];
                 const int64_t dwr = W1.idx[3].dims[Wr], ds2 = W2.idx[1].dims[S2];
                 const int64_t nin = dw * ds1 * ds2;
@@ -249,20 +257,24 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
               }
             }
           }
+          std::vector<CoefEntry> entries;
+          for (auto &kv : acc) {
+            bool nz = false;
+            for (double v : kv.second) nz |= (v != 0.0);
+            if (nz) entries.push_back({kv.first, std::move(kv.second)});
+          }
+          cit = coef_cache.emplace(ck, std::move(entries)).first;
         }
-        for (auto &kv : acc) {
-          bool nz = false;
-          for (double v : kv.second) nz |= (v != 0.0);
-          if (!nz) continue;
-          const Key src = {Ap, kv.first[0], kv.first[1], kv.first[2], Bs};
-          const T1Block &tb = t1map.at(src);
+        for (const CoefEntry &ce : cit->second) {
+          auto tb = t1map.find(Key{Ap, ce.src[0], ce.src[1], ce.src[2], Bs});
+          if (tb == t1map.end()) continue;
           MpoSource s{};
-          s.t1_off = tb.origin;
-          s.row_pitch = tb.pitch;
-          s.dw = tb.dw;
-          s.ds12 = tb.ds12;
+          s.t1_off = tb->second.origin;
+          s.row_pitch = tb->second.pitch;
+          s.dw = tb->second.dw;
+          s.ds12 = tb->second.ds12;
           s.coef_off = (int32_t)p->coefs.size();
-          for (double v : kv.second) p->coefs.push_back((float)v);
+          for (double v : ce.coef) p->coefs.push_back((float)v);
           p->sources.push_back(s);
         }
         tg.nsrc = (int32_t)p->sources.size() - tg.src0;
