@@ -102,3 +102,48 @@ def test_sym_eig_batch(ctx, kfrac):
         for i in range(k):
             if gaps[i] > 1e-3 * nrm:
                 assert abs(abs(z[:, i] @ v_ref[:, i]) - 1) <= 1e-10, (name, i)
+
+
+def _graded_block(rows, cols, decades, rng, dtype):
+    k = min(rows, cols)
+    s = 10.0 ** (-np.linspace(0, decades, k))
+
+    def orth(n):
+        a = rng.normal(size=(n, k))
+        if dtype == np.complex128:
+            a = a + 1j * rng.normal(size=(n, k))
+        q, _ = np.linalg.qr(a)
+        return q
+    return (orth(rows) * s) @ orth(cols).conj().T
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.complex128])
+def test_svd_large_sectors(ctx, dtype):
+    """Truncated SVD whose Gram sectors (n = 150 .. 300) exceed shared memory,
+    so the reduction runs on several cooperating CTAs per sector."""
+    from oracle import blocksparse as bs
+    from ultradmrg_gb300.tensor_data import BlockTensorData, Index
+    rng = np.random.default_rng(23)
+    li = Index.make([((0,), 260), ((1,), 150), ((2,), 40)], -1)
+    ri = Index.make([((0,), 300), ((1,), 180), ((2,), 60)], +1)
+    blocks = {(0, 0): _graded_block(260, 300, 7, rng, dtype),
+              (1, 1): 0.3 * _graded_block(150, 180, 9, rng, dtype),
+              (2, 2): 0.1 * _graded_block(40, 60, 5, rng, dtype)}
+    t = BlockTensorData([li, ri], blocks, dtype)
+    bs.normalize(t)
+    ldiv = (0,)
+    u, s, vt, err, Dk = bs.svd(t, 1, ldiv, 1e-10, 1, 400)
+    gu, gs, gvt, gerr, gD = api.svd(ctx, api.DeviceTensor.from_data(ctx, t), 1, ldiv, 1e-10, 1,
+                                    400)
+    gu, gs, gvt = gu.to_data(), gs.to_data(), gvt.to_data()
+    assert gD == Dk and abs(gerr - err) <= 1e-12
+    w = np.concatenate([np.diag(b) for _, b in sorted(s.blocks.items())])
+    gw = np.concatenate([np.diag(b) for _, b in sorted(gs.blocks.items())])
+    assert np.allclose(gw ** 2, w ** 2, atol=1e-14)
+    rec = bs.contract(bs.contract(u, s, [1], [0]), vt, [1], [0])
+    grec = bs.contract(bs.contract(gu, gs, [1], [0]), gvt, [1], [0])
+    for k, b in rec.blocks.items():
+        assert np.max(np.abs(grec.blocks[k] - b)) <= 1e-11
+    uu = bs.contract(bs.dag(gu), gu, [0], [0])
+    for k, b in uu.blocks.items():
+        assert np.allclose(b, np.eye(b.shape[0]), atol=1e-12)

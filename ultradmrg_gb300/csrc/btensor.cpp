@@ -9,6 +9,7 @@ namespace udmrg {
 Ctx::Ctx(int dev) : device(dev) {
   UDMRG_CHECK_CUDA(cudaSetDevice(dev));
   UDMRG_CHECK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  UDMRG_CHECK_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
   UDMRG_CHECK_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
   // keep freed blocks in the pool instead of returning them to the driver
   cudaMemPool_t pool;
@@ -22,6 +23,10 @@ Ctx::~Ctx() {
   if (stream) {
     cudaStreamSynchronize(stream);
     cudaStreamDestroy(stream);
+  }
+  if (side) {
+    cudaStreamSynchronize(side);
+    cudaStreamDestroy(side);
   }
   if (pinned) cudaFreeHost(pinned);
 }

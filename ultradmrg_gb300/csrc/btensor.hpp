@@ -44,6 +44,7 @@ struct Index {
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // second stream for work that overlaps the main one
   int num_sms = 0;
   // pinned host scratch for small device->host reads
   double *pinned = nullptr;

@@ -300,7 +300,7 @@ struct Bases {
 }  // namespace
 
 LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
-                         const LanczosParams &p) {
+                         const LanczosParams &p, bool defer_rayleigh) {
   const BTensor &S = *mv.sstruct;
   const bool cplx = S.dtype == kC128;
   const int es = elem_doubles(S.dtype);
@@ -315,18 +315,21 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
   std::vector<double> a(maxit, 0.0), b(maxit, 0.0), N(maxit, 0.0);
   LanczosResult res;
   const bool mixed = mv.sg != nullptr;
+  KrylovWork kw(ctx, n, cplx);
   EventTimer ev;
-  float ms = 0;
+  // the matvec is timed by events, read after the step's one synchronisation
   auto matvec = [&](const double *in) {
     double *out = (double *)ctx.alloc(vbytes);
     cudaEventRecord(ev.a, ctx.stream);
     mv.apply(in, out);
     cudaEventRecord(ev.b, ctx.stream);
-    UDMRG_CHECK_CUDA(cudaEventSynchronize(ev.b));
-    cudaEventElapsedTime(&ms, ev.a, ev.b);
-    res.matvec_seconds += ms * 1e-3;
     res.matvecs++;
     return out;
+  };
+  auto matvec_time = [&]() {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev.a, ev.b);
+    res.matvec_seconds += ms * 1e-3;
   };
   auto finish = [&](int64_t m, const std::vector<double> &vec) {
     if (mv.sg && (tc_check(ctx, mv.sg->g1) | tc_check(ctx, mv.sg->g3)))
@@ -339,46 +342,19 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
       coef.push_back(vec[i]);
       if (cplx) coef.push_back(0.0);
     }
-    if (cplx) {
-      lincomb(w, gs->data, vs, coef, n, true);
-    } else {
-      lincomb(w, gs->data, vs, coef, n, false);
-    }
-    if (mixed) {
+    lincomb(w, gs->data, vs, coef, n, cplx);
+    res.ritz_eng = res.gs_eng;
+    if (mixed && !defer_rayleigh) {
       // reported energy: FP64 Rayleigh quotient of the mixed-precision eigenvector
       double *y = (double *)ctx.alloc(vbytes);
       mv.apply_fp64(gs->data, y);
       const double num = dot(w, gs->data, y, n, cplx).real();
       const double den = dot(w, gs->data, gs->data, n, cplx).real();
       ctx.free(y);
-      res.ritz_eng = res.gs_eng;
       res.gs_eng = num / den;
       res.fp64_matvecs = 1;
     }
     return gs;
-  };
-  // Mixed precision: FP64 Gram-Schmidt (twice) of every new Lanczos vector
-  // against all previous ones, so rounding in the matvec cannot build up
-  // ghost Ritz values; returns |gamma|.
-  auto reorthogonalize = [&](double *gamma, int64_t m) {
-    for (int pass = 0; pass < 2; ++pass) {
-      for (int64_t j = 0; j < m; ++j) dot_async(w, bases.v[j], gamma, n, cplx, w.result + 2 * j);
-      double *h = ctx.host_scratch(2 * m + 2);
-      UDMRG_CHECK_CUDA(cudaMemcpyAsync(h, w.result, 2 * m * sizeof(double),
-                                       cudaMemcpyDeviceToHost, ctx.stream));
-      ctx.sync();
-      std::vector<double> c(h, h + 2 * m);
-      std::vector<const double *> vs = {gamma};
-      std::vector<double> coef = {1.0};
-      if (cplx) coef.push_back(0.0);
-      for (int64_t j = 0; j < m; ++j) {
-        vs.push_back(bases.v[j]);
-        coef.push_back(-c[2 * j]);
-        if (cplx) coef.push_back(-c[2 * j + 1]);
-      }
-      lincomb(w, gamma, vs, coef, n, cplx);
-    }
-    return std::sqrt(norm2(w, gamma, nd));
   };
   // bases[0] = init / |init| (QuasiNormalize)
   {
@@ -389,59 +365,118 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
     const double nrm = std::sqrt(norm2(w, d0, nd));
     if (nrm != 0.0) scale(ctx, d0, nd, 1.0 / nrm);
     bases.v.push_back(d0);
+    kw.push(0, d0);
   }
+  // Step m: gamma = H v_m - a_m v_m - b_{m-1} v_{m-1}; with mixed precision
+  // gamma is then projected against every basis vector (FP64 classical
+  // Gram-Schmidt, a second pass where the first removed more than half of
+  // |gamma|^2), so rounding in the matvec cannot build up ghost Ritz values.
+  // alpha and |gamma| reach the host once per step; the convergence test on
+  // the (m+1)-dimensional tridiagonal matrix follows.
   double *last = matvec(bases.v[0]);
-  a[0] = dot(w, bases.v[0], last, n, cplx).real();
-  N[0] = 0.0;
+  krylov_alpha(kw, 0, last);
   int64_t m = 0;
-  double energy0 = a[0];
-  double *hres = ctx.host_scratch(4);
+  double energy0 = 0.0;
   while (true) {
-    m += 1;
     double *gamma = last;
-    lanczos_update_async(w, gamma, bases.v[m - 1], m == 1 ? nullptr : bases.v[m - 2], a[m - 1],
-                         m == 1 ? 0.0 : std::sqrt(N[m - 1]), nd, w.result);
-    UDMRG_CHECK_CUDA(
-        cudaMemcpyAsync(hres, w.result, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
-    ctx.sync();
-    double norm_gamma = std::sqrt(hres[0]);
-    if (mixed && norm_gamma != 0.0) norm_gamma = reorthogonalize(gamma, m);
-    if (norm_gamma == 0.0) {
-      ctx.free(gamma);
-      if (m == 1) {
-        res.iters = m;
-        res.gs_eng = energy0;
-        res.gs_vec = finish(1, {1.0});
+    krylov_update(kw, (int)m, gamma);
+    if (mixed) {
+      krylov_project(kw, (int)m, gamma, false);
+      krylov_project(kw, (int)m, gamma, true);
+    }
+    krylov_fetch(kw, (int)m);
+    matvec_time();
+    a[m] = kw.hres[0];
+    const double n2 = kw.hres[1];
+    if (m == 0) {
+      energy0 = a[0];
+    } else {
+      const double e_new = tridiag_lowest(a, b, m + 1, nullptr);
+      // mixed precision also stops once the Ritz value no longer moves above
+      // the rounding level of the split-BF16 products
+      const bool noise_floor = mixed && std::fabs(energy0 - e_new) <= 1e-12 * std::fabs(e_new);
+      if ((energy0 - e_new) < p.error || noise_floor || m == eff_dim || m == maxit - 1) {
+        std::vector<double> vec;
+        tridiag_lowest(a, b, m + 1, &vec);
+        ctx.free(gamma);
+        res.iters = m + 1;
+        res.gs_eng = e_new;
+        res.gs_vec = finish(m + 1, vec);
         return res;
       }
-      std::vector<double> vec;
-      tridiag_lowest(a, b, m, &vec);
-      res.iters = m;
-      res.gs_eng = energy0;
-      res.gs_vec = finish(m, vec);
-      return res;
+      energy0 = e_new;
     }
-    scale(ctx, gamma, nd, 1.0 / norm_gamma);
-    N[m] = norm_gamma * norm_gamma;
-    b[m - 1] = norm_gamma;
-    bases.v.push_back(gamma);
-    last = matvec(bases.v[m]);
-    a[m] = dot(w, bases.v[m], last, n, cplx).real();
-    const double e_new = tridiag_lowest(a, b, m + 1, nullptr);
-    // mixed precision also stops once the Ritz value no longer moves above the
-    // rounding level of the split-BF16 products
-    const bool noise_floor = mixed && std::fabs(energy0 - e_new) <= 1e-12 * std::fabs(e_new);
-    if ((energy0 - e_new) < p.error || noise_floor || m == eff_dim || m == maxit - 1) {
-      std::vector<double> vec;
-      tridiag_lowest(a, b, m + 1, &vec);
-      ctx.free(last);
+    const double norm_gamma = std::sqrt(n2);
+    if (norm_gamma == 0.0) {  // invariant subspace
+      ctx.free(gamma);
+      std::vector<double> vec = {1.0};
+      if (m > 0) tridiag_lowest(a, b, m + 1, &vec);
       res.iters = m + 1;
-      res.gs_eng = e_new;
+      res.gs_eng = energy0;
       res.gs_vec = finish(m + 1, vec);
       return res;
     }
-    energy0 = e_new;
+    krylov_normalise(kw, (int)m, gamma);
+    N[m + 1] = n2;
+    b[m] = norm_gamma;
+    bases.v.push_back(gamma);
+    kw.push((int)m + 1, gamma);
+    last = matvec(gamma);
+    m += 1;
+    krylov_alpha(kw, (int)m, last);
   }
+}
+
+namespace {
+// Makes the context's side stream its current one for the guard's lifetime
+// (every launch and stream-ordered allocation in between goes there).
+struct SideStream {
+  Ctx &ctx;
+  explicit SideStream(Ctx &c) : ctx(c) { std::swap(ctx.stream, ctx.side); }
+  ~SideStream() { std::swap(ctx.stream, ctx.side); }
+};
+}  // namespace
+
+void PendingEnergy::launch(Ctx &c, std::unique_ptr<MatvecPlan> plan, TensorPtr state) {
+  ctx = &c;
+  mv = std::move(plan);
+  psi = std::move(state);
+  UDMRG_CHECK_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  UDMRG_CHECK_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+  UDMRG_CHECK_CUDA(cudaEventRecord(ready, c.stream));  // psi is complete
+  UDMRG_CHECK_CUDA(cudaStreamWaitEvent(c.side, ready, 0));
+  {
+    SideStream guard(c);
+    const bool cplx = psi->dtype == kC128;
+    const int64_t n = psi->size();
+    y = (double *)c.alloc(std::max<int64_t>(n, 1) * elem_doubles(psi->dtype) * sizeof(double));
+    res = (double *)c.alloc(4 * sizeof(double));
+    mv->apply_fp64(psi->data, y);
+    VecWork w(c);  // its buffers are freed on the side stream too
+    dot_async(w, psi->data, y, n, cplx, res);
+    dot_async(w, psi->data, psi->data, n, cplx, res + 2);
+  }
+  UDMRG_CHECK_CUDA(cudaEventRecord(done, c.side));
+}
+
+double PendingEnergy::value() {
+  if (resolved) return energy;
+  UDMRG_CHECK_CUDA(cudaEventSynchronize(done));
+  double h[4];
+  UDMRG_CHECK_CUDA(cudaMemcpy(h, res, sizeof(h), cudaMemcpyDeviceToHost));
+  energy = h[0] / h[2];
+  resolved = true;
+  return energy;
+}
+
+PendingEnergy::~PendingEnergy() {
+  if (!ctx) return;
+  if (done) cudaEventSynchronize(done);
+  // buffers used on the side stream go back to the pool in its order
+  if (y) cudaFreeAsync(y, ctx->side);
+  if (res) cudaFreeAsync(res, ctx->side);
+  if (ready) cudaEventDestroy(ready);
+  if (done) cudaEventDestroy(done);
 }
 
 ExpmvResult lanczos_expmv(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state, double step,
@@ -479,54 +514,59 @@ ExpmvResult lanczos_expmv(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state, d
     mv.apply(in, out);
     return out;
   };
+  KrylovWork kw(ctx, n, true);
+  kw.push(0, bases.v[0]);
   double *last = matvec(bases.v[0]);
-  a[0] = dot(w, bases.v[0], last, n, true).real();
+  krylov_alpha(kw, 0, last);
   int64_t m = 0;
   std::vector<double> last_coef(2 * maxit, 0.0);
-  double *hres = ctx.host_scratch(4);
+  // step m as in lanczos_gs: one host synchronisation per step
   while (true) {
-    m += 1;
     double *gamma = last;
-    lanczos_update_async(w, gamma, bases.v[m - 1], m == 1 ? nullptr : bases.v[m - 2], a[m - 1],
-                         m == 1 ? 0.0 : b[m - 2], nd, w.result);
-    UDMRG_CHECK_CUDA(
-        cudaMemcpyAsync(hres, w.result, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
-    ctx.sync();
-    const double norm_gamma = std::sqrt(hres[0]);
-    if (norm_gamma == 0.0) {
+    krylov_update(kw, (int)m, gamma);
+    krylov_fetch(kw, (int)m);
+    a[m] = kw.hres[0];
+    const double n2 = kw.hres[1];
+    if (m > 0) {
+      auto coef = tridiag_expme1(a, b, m + 1, step);
+      double dist = 0;
+      for (int64_t i = 0; i < m + 1; ++i) {
+        const double dr = coef[2 * i] - last_coef[2 * i];
+        const double di = coef[2 * i + 1] - last_coef[2 * i + 1];
+        dist += dr * dr + di * di;
+      }
+      dist = std::sqrt(dist);
+      if (dist < p.error || m == eff_dim || m == maxit - 1) {
+        ctx.free(gamma);
+        for (auto &x : coef) x *= initial_norm;
+        res.iters = m + 1;
+        res.expmv = combine(m + 1, coef);
+        return res;
+      }
+      std::fill(last_coef.begin(), last_coef.end(), 0.0);
+      std::copy(coef.begin(), coef.end(), last_coef.begin());
+    }
+    const double norm_gamma = std::sqrt(n2);
+    if (norm_gamma == 0.0) {  // invariant subspace
       ctx.free(gamma);
-      res.iters = m;
-      if (m == 1) {
+      res.iters = m + 1;
+      if (m == 0) {
         const double ph = -step * a[0];
         res.expmv = combine(1, {initial_norm * std::cos(ph), initial_norm * std::sin(ph)});
       } else {
-        auto c = tridiag_expme1(a, b, m, step);
+        auto c = tridiag_expme1(a, b, m + 1, step);
         for (auto &x : c) x *= initial_norm;
-        res.expmv = combine(m, c);
+        res.expmv = combine(m + 1, c);
       }
       return res;
     }
-    scale(ctx, gamma, nd, 1.0 / norm_gamma);
-    b[m - 1] = norm_gamma;
+    krylov_normalise(kw, (int)m, gamma);
+    b[m] = norm_gamma;
     bases.v.push_back(gamma);
-    last = matvec(bases.v[m]);
-    a[m] = dot(w, bases.v[m], last, n, true).real();
-    auto coef = tridiag_expme1(a, b, m + 1, step);
-    double dist = 0;
-    for (int64_t i = 0; i < m + 1; ++i) {
-      const double dr = coef[2 * i] - last_coef[2 * i], di = coef[2 * i + 1] - last_coef[2 * i + 1];
-      dist += dr * dr + di * di;
-    }
-    dist = std::sqrt(dist);
-    if (dist < p.error || m == eff_dim || m == maxit - 1) {
-      ctx.free(last);
-      for (auto &x : coef) x *= initial_norm;
-      res.iters = m + 1;
-      res.expmv = combine(m + 1, coef);
-      return res;
-    }
-    std::fill(last_coef.begin(), last_coef.end(), 0.0);
-    std::copy(coef.begin(), coef.end(), last_coef.begin());
+    kw.push((int)m + 1, gamma);
+    last = matvec(gamma);
+    m += 1;
+    krylov_alpha(kw, (int)m, last);
   }
 }
 
@@ -703,18 +743,26 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
   const double t0 = now();
   auto init_state = contract_axes(ctx, mps_l, mps_r, {2}, {0});
   auto mv = plan_matvec2(ctx, lenv, mpo_l, mpo_r, renv, *init_state, p.lancz.precision);
-  auto lres = lanczos_gs(ctx, *mv, *init_state, p.lancz);
+  const bool mixed = mv->sg != nullptr;
+  auto lres = lanczos_gs(ctx, *mv, *init_state, p.lancz, /*defer_rayleigh=*/mixed);
   const double t1 = now();
   const double mvflops = mv->flops;
-  mv.reset();
   init_state.reset();
+  // mixed precision: the FP64 Rayleigh quotient runs beside the SVD and the
+  // environment update
+  PendingEnergy pe;
+  if (mixed)
+    pe.launch(ctx, std::move(mv), std::move(lres.gs_vec));
+  else
+    mv.reset();
+  const BTensor &psi = mixed ? *pe.psi : *lres.gs_vec;
   const QN ldiv = mps_l.div();
   const int split = dir == 'r' ? kSvdSplitLeft : kSvdSplitRight;
   SvdResult sres;
   double audit_err = -1.0, audit_sec = 0.0;
   int64_t audit_diff = 0;
   if (p.svd_mode == kSvdExact || (p.svd_mode == kSvdSketchLearned && !hint)) {
-    sres = svd_trunc(ctx, *lres.gs_vec, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split);
+    sres = svd_trunc(ctx, psi, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split);
   } else {
     SketchParams sp;
     sp.oversample = p.svd_oversample;
@@ -726,10 +774,10 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
       const Index &bond = mps_l.idx[2];
       for (int q = 0; q < bond.nsec(); ++q) sp.sketch.push_back({bond.qns[q], bond.dims[q]});
     }
-    sres = svd_trunc_sketch(ctx, *lres.gs_vec, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split, sp);
+    sres = svd_trunc_sketch(ctx, psi, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split, sp);
     if (p.svd_audit) {  // the exact block SVD judges the randomized one
       const double ta = now();
-      SvdResult ex = svd_trunc(ctx, *lres.gs_vec, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split);
+      SvdResult ex = svd_trunc(ctx, psi, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split);
       audit_err = std::fabs(ex.trunc_err - sres.trunc_err);
       std::map<QN, int64_t> kx;
       for (size_t q = 0; q < ex.sector_qn.size(); ++q) kx[ex.sector_qn[q]] = ex.sector_kept[q];
@@ -759,12 +807,13 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
   else
     out.env = update_site_renv(ctx, renv, *out.mps_r, mpo_r);
   ctx.sync();
+  const double e0 = mixed ? pe.value() : lres.gs_eng;
   const double t3 = now();
   {
     int64_t sk = 0;
     for (int64_t v : sres.sector_sketch) sk += v;
     if (log)
-      *log = {0, lres.gs_eng, sres.trunc_err, sres.D, lres.iters, sres.ee, t1 - t0,
+      *log = {0, e0, sres.trunc_err, sres.D, lres.iters, sres.ee, t1 - t0,
               t2 - t1 - audit_sec, t3 - t2, t3 - t0 - audit_sec, mvflops, sk, sres.grow_rounds,
               audit_err, audit_diff};
   }

@@ -70,10 +70,30 @@ struct LanczosResult {
 };
 
 // Ground state by Lanczos (lanczos_vmps_solver_impl.h:114-248): three-term
-// recurrence without reorthogonalisation, all bases kept on the device,
-// FP64 tridiagonal eigenproblem on the host.
+// recurrence (FP64 form: without reorthogonalisation, as the reference),
+// all bases kept on the device, FP64 tridiagonal eigenproblem on the host.
+// With the mixed-precision matvec the reported energy is the FP64 Rayleigh
+// quotient of the eigenvector; defer_rayleigh leaves it to the caller
+// (gs_eng is then the Ritz value; see PendingEnergy).
 LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
-                         const LanczosParams &p);
+                         const LanczosParams &p, bool defer_rayleigh = false);
+
+// FP64 Rayleigh quotient <psi|H|psi> / <psi|psi> computed on the context's
+// side stream while the main stream goes on (the truncated SVD and the
+// environment update read psi and the environments too, but write neither).
+// The plan and psi are owned here until value() has waited for the result.
+struct PendingEnergy {
+  Ctx *ctx = nullptr;
+  std::unique_ptr<MatvecPlan> mv;
+  TensorPtr psi;
+  double *y = nullptr, *res = nullptr;
+  cudaEvent_t ready = nullptr, done = nullptr;
+  bool resolved = false;
+  double energy = 0.0;
+  void launch(Ctx &c, std::unique_ptr<MatvecPlan> plan, TensorPtr state);
+  double value();
+  ~PendingEnergy();
+};
 
 // exp(-i dt H_eff) psi (lanczos_expmv_solver_impl.h:70-184).
 struct ExpmvResult {

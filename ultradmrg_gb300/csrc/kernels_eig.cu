@@ -3,8 +3,9 @@
 //
 // FP64 throughput per SM is low on this GPU, so the solver does as little
 // FP64 work as the problem allows:
-//   1. Householder reduction to tridiagonal form (about 2 n^3 flops, one CTA
-//      per matrix; the reflectors stay in the matrix's upper triangle);
+//   1. Householder reduction to tridiagonal form (about 2 n^3 flops; one CTA
+//      per matrix held in shared memory, several co-resident CTAs per larger
+//      matrix; the reflectors stay in the matrix's upper triangle);
 //   2. every eigenvalue by Sturm-sequence bisection (O(n) per step and
 //      eigenvalue, all eigenvalues of all matrices in parallel);
 //   3. only the eigenvectors the caller needs, by inverse iteration on the
@@ -15,6 +16,7 @@
 // These are the textbook methods (Golub & Van Loan ch. 8; Wilkinson's
 // inverse iteration; the Sturm count of Barth, Martin & Wilkinson), written
 // for this batch layout.
+#include <algorithm>
 #include <cmath>
 
 #include "svd.hpp"
@@ -44,10 +46,11 @@ __device__ double block_sum(double v, double *red) {
 }
 
 // Householder tridiagonalisation of the symmetric n x n matrix of each job
-// (row-major at G + g_off; the matrix is first scaled to unit max-abs, the
-// scale goes to scale[job]).  Step j reflects row/column j: v (v_0 = 1) is
-// stored in row j right of the first superdiagonal, tau in tau[lam_off + j],
-// the diagonal in d[lam_off + i] and the off-diagonal in e[lam_off + i].
+// that fits in shared memory (row-major at G + g_off; the matrix is first
+// scaled to unit max-abs, the scale goes to scale[job]).  Step j reflects
+// row/column j: v (v_0 = 1) is stored in row j right of the first
+// superdiagonal, tau in tau[lam_off + j], the diagonal in d[lam_off + i] and
+// the off-diagonal in e[lam_off + i].
 __global__ void tridiag_kernel(const EigJob *__restrict__ jobs, double *__restrict__ G_all,
                                double *__restrict__ d_all, double *__restrict__ e_all,
                                double *__restrict__ tau_all, double *__restrict__ scale_all,
@@ -57,16 +60,15 @@ __global__ void tridiag_kernel(const EigJob *__restrict__ jobs, double *__restri
   __shared__ int bad;
   const EigJob job = jobs[blockIdx.x];
   const int n = job.n;
-  if (n == 0) return;
+  if (n == 0 || !job.smem) return;  // larger matrices: tridiag_mc_kernel
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
-  double *A = job.smem ? sm : G_all + job.g_off;
-  double *v = sm + (job.smem ? (int64_t)n * n : 0);
+  double *A = sm;
+  double *v = sm + (int64_t)n * n;
   double *w = v + n;
   double *d = d_all + job.lam_off, *e = e_all + job.lam_off, *tau = tau_all + job.lam_off;
 
-  if (job.smem)
-    for (int64_t x = tid; x < (int64_t)n * n; x += nt) A[x] = G_all[job.g_off + x];
+  for (int64_t x = tid; x < (int64_t)n * n; x += nt) A[x] = G_all[job.g_off + x];
   // scale to unit max-abs; non-finite input is reported
   double mx = 0.0;
   int nf = 0;
@@ -170,8 +172,8 @@ __global__ void tridiag_kernel(const EigJob *__restrict__ jobs, double *__restri
     tau[n - 1] = 0.0;
   }
   __syncthreads();
-  if (job.smem)  // the reflectors live in the rows' upper parts
-    for (int64_t x = tid; x < (int64_t)n * n; x += nt) G_all[job.g_off + x] = A[x];
+  // the reflectors live in the rows' upper parts
+  for (int64_t x = tid; x < (int64_t)n * n; x += nt) G_all[job.g_off + x] = A[x];
 }
 
 // Number of eigenvalues of the tridiagonal (d, e) below x (Sturm count).
@@ -405,6 +407,330 @@ __device__ __forceinline__ double2 cadd(double2 a, double2 b) {
   return make_double2(a.x + b.x, a.y + b.y);
 }
 
+// ---- Householder tridiagonalisation of one large matrix by several CTAs ----
+//
+// A matrix too large for shared memory is reduced by P co-resident CTAs (a
+// cooperative launch): CTA p owns the rows i with i % P == p.  Step j uses
+// the reflector v_j of row j and w_j = t_j A v_j - K v_j; one fused pass over
+// each CTA's own rows applies the rank-2 update of step j and forms the
+// matrix-vector product of step j + 1, so the trailing block is read and
+// written once per step.  Per step the CTAs meet twice: a counter barrier
+// (every w_j entry and partial sum is written) and a flag that the owner of
+// row j + 1 raises once it has updated that row (every CTA forms the next
+// reflector from it).  Each wait gives up after kTriTimeoutNs and sets
+// status 3.  Partial sums are added in CTA order, so the result does not
+// depend on timing.
+struct TriPart {
+  int32_t job, p, P, slot;
+  int64_t wb_off;  // 2 n scalars of w buffers (double-buffered by step parity)
+};
+struct TriSlot {  // one per matrix, zeroed before the launch
+  unsigned int arrive;
+  int flag;
+  int pad[2];
+};
+constexpr int kTriMaxParts = 64;
+constexpr unsigned long long kTriTimeoutNs = 2000000000ull;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ double cj(double a) { return a; }
+__device__ __forceinline__ double2 cj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double smul(double a, double b) { return a * b; }
+__device__ __forceinline__ double2 smul(double2 a, double2 b) { return cmul(a, b); }
+__device__ __forceinline__ double sadd(double a, double b) { return a + b; }
+__device__ __forceinline__ double2 sadd(double2 a, double2 b) { return cadd(a, b); }
+__device__ __forceinline__ double ssub(double a, double b) { return a - b; }
+__device__ __forceinline__ double2 ssub(double2 a, double2 b) {
+  return make_double2(a.x - b.x, a.y - b.y);
+}
+__device__ __forceinline__ double sre(double a) { return a; }
+__device__ __forceinline__ double sre(double2 a) { return a.x; }
+__device__ __forceinline__ double sim(double) { return 0.0; }
+__device__ __forceinline__ double sim(double2 a) { return a.y; }
+__device__ __forceinline__ double sabs2(double a) { return a * a; }
+__device__ __forceinline__ double sabs2(double2 a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ double samax(double a) { return fabs(a); }
+__device__ __forceinline__ double samax(double2 a) { return fmax(fabs(a.x), fabs(a.y)); }
+__device__ __forceinline__ bool sfinite(double a) { return isfinite(a); }
+__device__ __forceinline__ bool sfinite(double2 a) { return isfinite(a.x) && isfinite(a.y); }
+template <typename T> __device__ __forceinline__ T smake(double re, double im);
+template <> __device__ __forceinline__ double smake<double>(double re, double) { return re; }
+template <> __device__ __forceinline__ double2 smake<double2>(double re, double im) {
+  return make_double2(re, im);
+}
+__device__ __forceinline__ double sscale(double s, double a) { return s * a; }
+__device__ __forceinline__ double2 sscale(double s, double2 a) {
+  return make_double2(s * a.x, s * a.y);
+}
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double2 warp_sum(double2 v) {
+  return make_double2(warp_sum(v.x), warp_sum(v.y));
+}
+
+// All CTAs of the matrix arrive; false (status 3) if the others do not
+// arrive within the time limit.
+__device__ bool tri_barrier(TriSlot *sl, unsigned target, int *status) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(&sl->arrive, 1u);
+    const unsigned long long t0 = global_ns();
+    int good = 1;
+    while (*(volatile unsigned *)&sl->arrive < target) {
+      if (global_ns() - t0 > kTriTimeoutNs) {
+        good = 0;
+        atomicExch(status, 3);
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Waits until the owner of row `row` has published it.
+__device__ bool tri_wait_row(TriSlot *sl, int row, int *status) {
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    const unsigned long long t0 = global_ns();
+    int good = 1;
+    while (*(volatile int *)&sl->flag < row) {
+      if (global_ns() - t0 > kTriTimeoutNs) {
+        good = 0;
+        atomicExch(status, 3);
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Reflector of step j from row j (columns j+1 ..): v (v_0 = 1) into v[0 .. m),
+// returns tau; the CTA with p == 0 writes d[j], e[j], tau[j].  Same formulas
+// as the single-CTA kernels.
+template <typename T>
+__device__ T tri_reflector(const T *A, int n, int j, T *v, double *red, bool writer, double *d,
+                           double *e, T *tau) {
+  const T *rowj = A + (int64_t)j * n;
+  const int m = n - j - 1;
+  const T alpha = cj(__ldcg(&rowj[j + 1]));
+  double x2 = 0.0;
+  for (int c = j + 2 + threadIdx.x; c < n; c += blockDim.x) x2 += sabs2(__ldcg(&rowj[c]));
+  x2 = block_sum(x2, red);
+  T t = smake<T>(0.0, 0.0), sc = smake<T>(0.0, 0.0);
+  double beta = sre(alpha);
+  const bool refl = x2 > 0.0 || sim(alpha) != 0.0;
+  if (refl) {
+    beta = -copysign(sqrt(sabs2(alpha) + x2), sre(alpha));
+    t = smake<T>((beta - sre(alpha)) / beta, -sim(alpha) / beta);
+    const double dr = sre(alpha) - beta, di = sim(alpha), dd = dr * dr + di * di;
+    sc = smake<T>(dr / dd, -di / dd);  // 1 / (alpha - beta)
+  }
+  for (int r = threadIdx.x; r < m; r += blockDim.x)
+    v[r] = r == 0 ? smake<T>(1.0, 0.0)
+                  : (refl ? smul(cj(__ldcg(&rowj[j + 1 + r])), sc) : smake<T>(0.0, 0.0));
+  if (writer && threadIdx.x == 0) {
+    d[j] = sre(__ldcg(&rowj[j]));
+    e[j] = beta;
+    tau[j] = t;
+  }
+  __syncthreads();
+  return t;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTriThreads)
+    tridiag_mc_kernel(const EigJob *__restrict__ jobs, const TriPart *__restrict__ parts,
+                      T *__restrict__ G_all, double *__restrict__ d_all,
+                      double *__restrict__ e_all, T *__restrict__ tau_all,
+                      double *__restrict__ scale_all, TriSlot *__restrict__ slots,
+                      T *__restrict__ wbuf_all, T *__restrict__ red_all,
+                      int *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned char tri_sm[];
+  __shared__ double red[33];
+  __shared__ T ksum;
+  const TriPart pt = parts[blockIdx.x];
+  const EigJob job = jobs[pt.job];
+  const int n = job.n, p = pt.p, P = pt.P;
+  TriSlot *sl = slots + pt.slot;
+  T *A = G_all + job.g_off;
+  T *wb = wbuf_all + pt.wb_off;
+  T *rd = red_all + (int64_t)pt.slot * 2 * kTriMaxParts;
+  double *d = d_all + job.lam_off, *e = e_all + job.lam_off;
+  T *tau = tau_all + job.lam_off;
+  T *vA = (T *)tri_sm, *vB = vA + n, *wA = vB + n;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarp = nt >> 5;
+  unsigned nbar = 0;
+  // first row >= lo owned by this CTA
+  auto first_own = [&](int lo) { return lo + ((p - lo % P) + P) % P; };
+
+  // 1. max-abs and finiteness of the own rows; partials in the w buffer
+  double mx = 0.0;
+  int nf = 0;
+  for (int i = first_own(0) + P * warp; i < n; i += P * nwarp)
+    for (int c = lane; c < n; c += 32) {
+      const T g = A[(int64_t)i * n + c];
+      nf |= !sfinite(g);
+      mx = fmax(mx, samax(g));
+    }
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    nf |= __shfl_down_sync(0xffffffffu, nf, o);
+  }
+  __syncthreads();
+  if (lane == 0) red[warp] = nf ? -1.0 : mx;
+  __syncthreads();
+  double *pw = (double *)wb;  // 2 P doubles (P <= n / 4)
+  if (tid == 0) {
+    double m = 0.0;
+    int bad = 0;
+    for (int i = 0; i < nwarp; ++i) {
+      bad |= red[i] < 0.0;
+      m = fmax(m, red[i]);
+    }
+    pw[p] = m;
+    pw[P + p] = bad;
+  }
+  if (!tri_barrier(sl, ++nbar * P, status)) return;
+  if (tid == 0) {
+    double m = 0.0;
+    int bad = 0;
+    for (int q = 0; q < P; ++q) {
+      m = fmax(m, __ldcg(&pw[q]));
+      bad |= __ldcg(&pw[P + q]) != 0.0;
+    }
+    red[32] = bad ? -1.0 : m;
+  }
+  __syncthreads();
+  const double scale = red[32];
+  if (scale < 0.0) {  // every CTA sees the same flag and leaves
+    if (tid == 0 && p == 0) atomicExch(status, 2);
+    return;
+  }
+  if (tid == 0 && p == 0) scale_all[pt.job] = scale;
+  const double inv = scale > 0.0 ? 1.0 / scale : 0.0;
+  // 2. lower triangle of the own rows <- scaled conjugate of the upper triangle
+  //    (exactly Hermitian; the upper triangle is not written in this phase)
+  for (int i = first_own(0) + P * warp; i < n; i += P * nwarp) {
+    T *ar = A + (int64_t)i * n;
+    for (int c = lane; c < i; c += 32) ar[c] = sscale(inv, cj(__ldcg(&A[(int64_t)c * n + i])));
+    if (lane == 0) ar[i] = smake<T>(inv * sre(ar[i]), 0.0);
+  }
+  if (!tri_barrier(sl, ++nbar * P, status)) return;
+  // 3. upper triangle of the own rows scaled
+  for (int i = first_own(0) + P * warp; i < n; i += P * nwarp) {
+    T *ar = A + (int64_t)i * n;
+    for (int c = i + 1 + lane; c < n; c += 32) ar[c] = sscale(inv, ar[c]);
+  }
+  if (!tri_barrier(sl, ++nbar * P, status)) return;
+
+  // Own rows i >= lo: optional rank-2 update with (vA, wA) of step j = lo - 2,
+  // then w[i - lo] = t * (row i, columns lo ..) . vn into wbuf, and the CTA's
+  // partial sum of conj(w_i) vn_i into rd.
+  auto rows_pass = [&](int lo, bool upd, const T *vn, T t, T *wout, T *rout) {
+    const int j = lo - 2;
+    T acc = smake<T>(0.0, 0.0);
+    for (int i = first_own(lo) + P * warp; i < n; i += P * nwarp) {
+      T *ar = A + (int64_t)i * n;
+      T s = smake<T>(0.0, 0.0);
+      if (upd) {
+        const T vi = vA[i - j - 1], wi = wA[i - j - 1];
+        for (int c = lo + lane; c < n; c += 32) {
+          const T a = ssub(ar[c], sadd(smul(vi, cj(wA[c - j - 1])), smul(wi, cj(vA[c - j - 1]))));
+          ar[c] = a;
+          s = sadd(s, smul(a, vn[c - lo]));
+        }
+      } else {
+        for (int c = lo + lane; c < n; c += 32) s = sadd(s, smul(ar[c], vn[c - lo]));
+      }
+      s = warp_sum(s);
+      if (lane == 0) {
+        const T wi = smul(t, s);
+        wout[i - lo] = wi;
+        acc = sadd(acc, smul(cj(wi), vn[i - lo]));
+      }
+    }
+    // CTA partial, summed over warps in order
+    __syncthreads();
+    T *wp = (T *)(tri_sm + 3 * (size_t)n * sizeof(T));  // nwarp scalars
+    if (lane == 0) wp[warp] = acc;
+    __syncthreads();
+    if (tid == 0) {
+      T s = smake<T>(0.0, 0.0);
+      for (int q = 0; q < nwarp; ++q) s = sadd(s, wp[q]);
+      rout[p] = s;
+    }
+  };
+
+  // step 0: reflector and products of the own rows
+  T t = tri_reflector(A, n, 0, vA, red, p == 0, d, e, tau);
+  rows_pass(1, false, vA, t, wb, rd);
+  for (int j = 0; j + 1 < n; ++j) {
+    const int m = n - j - 1, par = j & 1;
+    if (!tri_barrier(sl, ++nbar * P, status)) return;
+    if (j % P == p)  // reflector storage; every CTA has read row j by now
+      for (int c = j + 2 + tid; c < n; c += nt) A[(int64_t)j * n + c] = vA[c - j - 1];
+    if (tid == 0) {
+      T s = smake<T>(0.0, 0.0);
+      for (int q = 0; q < P; ++q) s = sadd(s, __ldcg(&rd[par * kTriMaxParts + q]));
+      ksum = smul(sscale(-0.5, t), s);  // K = -t (w^H v) / 2
+    }
+    __syncthreads();
+    const T K = ksum;
+    for (int r = tid; r < m; r += nt) wA[r] = sadd(__ldcg(&wb[par * n + r]), smul(K, vA[r]));
+    __syncthreads();
+    if (j + 2 == n) {  // the trailing block is the last diagonal entry
+      if ((n - 1) % P == p && tid == 0) {
+        T *a = A + (int64_t)(n - 1) * n + (n - 1);
+        const T v0 = vA[0], w0 = wA[0];
+        const T an = ssub(*a, sadd(smul(v0, cj(w0)), smul(w0, cj(v0))));
+        *a = an;
+        d[n - 1] = sre(an);
+        e[n - 1] = 0.0;
+        tau[n - 1] = smake<T>(0.0, 0.0);
+      }
+      break;
+    }
+    // row j + 1 first, then published
+    if ((j + 1) % P == p) {
+      T *ar = A + (int64_t)(j + 1) * n;
+      const T v0 = vA[0], w0 = wA[0];
+      for (int c = j + 1 + tid; c < n; c += nt)
+        ar[c] = ssub(ar[c], sadd(smul(v0, cj(wA[c - j - 1])), smul(w0, cj(vA[c - j - 1]))));
+      __syncthreads();
+      if (tid == 0) {
+        __threadfence();
+        atomicExch(&sl->flag, j + 1);
+      }
+      __syncthreads();
+    } else if (!tri_wait_row(sl, j + 1, status)) {
+      return;
+    }
+    const T tn = tri_reflector(A, n, j + 1, vB, red, p == 0, d, e, tau);
+    rows_pass(j + 2, true, vB, tn, wb + (par ^ 1) * n, rd + (par ^ 1) * kTriMaxParts);
+    T *x = vA;
+    vA = vB;
+    vB = x;
+    t = tn;
+  }
+}
+
 // Complex Hermitian version of tridiag_kernel.  Step j (0 <= j <= n-2)
 // reflects the column x = A[j+1.., j] (read as conj of row j) with
 // H = I - tau v v^H, v_0 = 1, beta real, so that H^H x = beta e_0 and the
@@ -420,17 +746,16 @@ __global__ void tridiag_c_kernel(const EigJob *__restrict__ jobs, double2 *__res
   __shared__ int bad;
   const EigJob job = jobs[blockIdx.x];
   const int n = job.n;
-  if (n == 0) return;
+  if (n == 0 || !job.smem) return;  // larger matrices: tridiag_mc_kernel
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
-  double2 *A = job.smem ? smc : G_all + job.g_off;
-  double2 *v = smc + (job.smem ? (int64_t)n * n : 0);
+  double2 *A = smc;
+  double2 *v = smc + (int64_t)n * n;
   double2 *w = v + n;
   double *d = d_all + job.lam_off, *e = e_all + job.lam_off;
   double2 *tau = tau_all + job.lam_off;
 
-  if (job.smem)
-    for (int64_t x = tid; x < (int64_t)n * n; x += nt) A[x] = G_all[job.g_off + x];
+  for (int64_t x = tid; x < (int64_t)n * n; x += nt) A[x] = G_all[job.g_off + x];
   double mx = 0.0;
   int nf = 0;
   if (tid == 0) bad = 0;
@@ -551,8 +876,7 @@ __global__ void tridiag_c_kernel(const EigJob *__restrict__ jobs, double2 *__res
     tau[n - 1] = make_double2(0.0, 0.0);
   }
   __syncthreads();
-  if (job.smem)
-    for (int64_t x = tid; x < (int64_t)n * n; x += nt) G_all[job.g_off + x] = A[x];
+  for (int64_t x = tid; x < (int64_t)n * n; x += nt) G_all[job.g_off + x] = A[x];
 }
 
 // Complex back-transformation: Z <- H_0 H_1 ... H_{n-2} Z, H_j = I - tau_j v_j v_j^H.
@@ -601,6 +925,67 @@ __global__ void backtransform_c_kernel(const EigJob *__restrict__ jobs,
 
 constexpr size_t kTriSmemBytes = 200 * 1024;
 
+// Reduces the jobs without shared-memory residence with tridiag_mc_kernel.
+// The SMs are shared out in proportion to n^3 (the flop count), at most
+// kTriMaxParts and n / 8 CTAs per matrix; jobs that do not fit one
+// cooperative launch go to the next.
+template <typename T>
+void tridiag_multi_cta(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJob> &jobs,
+                       const SymEigWork &wk, double *G, int *dstat) {
+  std::vector<int> big;
+  double work = 0.0;
+  int nmax = 0;
+  for (int q = 0; q < (int)jobs.size(); ++q)
+    if (!jobs[q].smem && jobs[q].n > 0) {
+      big.push_back(q);
+      work += std::pow((double)jobs[q].n, 3);
+      nmax = std::max(nmax, jobs[q].n);
+    }
+  if (big.empty()) return;
+  std::sort(big.begin(), big.end(), [&](int a, int b) { return jobs[a].n > jobs[b].n; });
+  const void *kern = (const void *)tridiag_mc_kernel<T>;
+  const size_t msmem = (3 * (size_t)nmax + kTriThreads / 32) * sizeof(T);
+  UDMRG_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)msmem));
+  int per_sm = 0;
+  UDMRG_CHECK_CUDA(
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTriThreads, msmem));
+  const int budget = std::min(ctx.num_sms, per_sm * ctx.num_sms);
+  UDMRG_REQUIRE(budget >= 1, "eigensolver: the reduction kernel does not fit an SM");
+  size_t at = 0;
+  while (at < big.size()) {
+    std::vector<TriPart> parts;
+    int64_t wb_tot = 0;
+    int slot = 0;
+    for (; at < big.size(); ++at) {
+      const int q = big[at], n = jobs[q].n;
+      const double share = std::pow((double)n, 3) / work;
+      int P = std::max(1, (int)(budget * share));
+      P = std::min({P, kTriMaxParts, std::max(1, n / 8)});
+      if (!parts.empty() && (int)parts.size() + P > budget) break;
+      P = std::min(P, budget);
+      for (int p = 0; p < P; ++p) parts.push_back(TriPart{q, p, P, slot, wb_tot});
+      wb_tot += 2 * (int64_t)n;
+      ++slot;
+    }
+    TriPart *dparts = scratch.get<TriPart>(parts.size());
+    TriSlot *dslots = scratch.get<TriSlot>(slot);
+    T *dwb = scratch.get<T>(wb_tot);
+    T *dred = scratch.get<T>((int64_t)slot * 2 * kTriMaxParts);
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(dparts, parts.data(), parts.size() * sizeof(TriPart),
+                                     cudaMemcpyHostToDevice, ctx.stream));
+    UDMRG_CHECK_CUDA(cudaMemsetAsync(dslots, 0, slot * sizeof(TriSlot), ctx.stream));
+    const EigJob *djobs = wk.jobs;
+    T *g = (T *)G, *tau = (T *)wk.tau;
+    double *d = wk.d, *e = wk.e, *sc = wk.scale;
+    void *args[] = {&djobs, &dparts, &g, &d, &e, &tau, &sc, &dslots, &dwb, &dred, &dstat};
+    UDMRG_CHECK_CUDA(cudaLaunchCooperativeKernel(kern, dim3((unsigned)parts.size()),
+                                                 dim3(kTriThreads), args, msmem, ctx.stream));
+    ctx.launches++;
+    ctx.sync();  // `parts` must outlive the upload
+  }
+}
+
 int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, double *G,
                    double *lam, SymEigWork &wk, bool cplx) {
   const int nj = (int)jobs.size();
@@ -623,7 +1008,7 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
     const size_t base = 2 * (size_t)j.n * es;
     const size_t full = base + (size_t)j.n * j.n * es;
     j.smem = full <= kTriSmemBytes ? 1 : 0;
-    smem = std::max(smem, j.smem ? full : base);
+    if (j.smem) smem = std::max(smem, full);
   }
   UDMRG_CHECK_CUDA(cudaFuncSetAttribute(tridiag_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -643,6 +1028,10 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
     tridiag_kernel<<<nj, kTriThreads, smem, ctx.stream>>>(wk.jobs, G, wk.d, wk.e, wk.tau,
                                                           wk.scale, dstat);
   UDMRG_CHECK_CUDA(cudaGetLastError());
+  if (cplx)
+    tridiag_multi_cta<double2>(ctx, scratch, jobs, wk, G, dstat);
+  else
+    tridiag_multi_cta<double>(ctx, scratch, jobs, wk, G, dstat);
   const size_t bsmem = 2 * (size_t)nmax * sizeof(double);
   if (bsmem > 48 * 1024)
     UDMRG_CHECK_CUDA(cudaFuncSetAttribute(bisect_kernel,

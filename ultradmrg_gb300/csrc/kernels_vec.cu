@@ -1,6 +1,8 @@
 // Krylov vector kernels (HBM-bound): dot products, the fused three-term
 // Lanczos update with its norm, scaling, multi-vector combinations, conjugation.
 // Reductions are two-stage with a fixed grid, so results are deterministic.
+#include <type_traits>
+
 #include "vecops.hpp"
 
 namespace udmrg {
@@ -136,6 +138,221 @@ __global__ void real_to_complex_kernel(const double *__restrict__ x, double2 *__
     y[i] = make_double2(x[i], 0.0);
 }
 
+// ---- device-resident Krylov step ----
+
+constexpr int kMdThreads = 256;
+constexpr int kMdWarps = kMdThreads / 32;
+constexpr int kMdPer = 4;  // elements of g per lane and chunk, held in registers
+
+// Second Gram-Schmidt pass only where the first one removed a large part of
+// the vector: |g|^2 after the pass < 1/2 |g|^2 before it (the classical
+// "twice is enough" test, eta = 1/sqrt(2)).  gate == nullptr: always run.
+__device__ __forceinline__ bool gate_open(const double *gate) {
+  return gate == nullptr || gate[1] < 0.5 * gate[0];
+}
+
+// partial[(j * gridDim.x + b) * 2 + {0,1}] = block b's share of <v_j | g>,
+// j < m.  Chunks of 32 * kMdPer elements per warp, grid-strided; each warp
+// keeps its running sums per vector in shared memory (warp-private slots,
+// 2 * m * kMdWarps doubles), summed over the block's warps at the end.  The
+// loads of a group of vectors are issued before their products.
+template <bool CPLX>
+__global__ void __launch_bounds__(kMdThreads)
+    multidot_kernel(const double *const *__restrict__ vecs, int m, const double *__restrict__ g,
+                    int64_t n, double *__restrict__ partial, const double *__restrict__ gate) {
+  if (!gate_open(gate)) return;
+  constexpr int G = CPLX ? 4 : 8;  // vectors per group
+  using E = typename std::conditional<CPLX, double2, double>::type;
+  extern __shared__ double md_sm[];  // [m][kMdWarps][2]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int x = threadIdx.x; x < 2 * m * kMdWarps; x += kMdThreads) md_sm[x] = 0.0;
+  __syncthreads();
+  const E *ge = (const E *)g;
+  const int64_t chunk = 32 * kMdPer;
+  const int64_t nchunks = (n + chunk - 1) / chunk;
+  for (int64_t c = (int64_t)blockIdx.x * kMdWarps + warp; c < nchunks;
+       c += (int64_t)gridDim.x * kMdWarps) {
+    const int64_t base = c * chunk + lane;
+    E gv[kMdPer];
+#pragma unroll
+    for (int k = 0; k < kMdPer; ++k) {
+      const int64_t i = base + 32 * k;
+      if constexpr (CPLX)
+        gv[k] = i < n ? ge[i] : make_double2(0.0, 0.0);
+      else
+        gv[k] = i < n ? ge[i] : 0.0;
+    }
+    for (int j0 = 0; j0 < m; j0 += G) {
+      E vv[G][kMdPer];
+#pragma unroll
+      for (int q = 0; q < G; ++q) {
+        const bool ok = j0 + q < m;
+        const E *v = (const E *)vecs[ok ? j0 + q : j0];
+#pragma unroll
+        for (int k = 0; k < kMdPer; ++k) {
+          const int64_t i = base + 32 * k;
+          if constexpr (CPLX)
+            vv[q][k] = ok && i < n ? v[i] : make_double2(0.0, 0.0);
+          else
+            vv[q][k] = ok && i < n ? v[i] : 0.0;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < G; ++q) {
+        double sr = 0.0, si = 0.0;
+#pragma unroll
+        for (int k = 0; k < kMdPer; ++k) {
+          if constexpr (CPLX) {  // conj(v) g
+            sr = fma(vv[q][k].x, gv[k].x, fma(vv[q][k].y, gv[k].y, sr));
+            si = fma(vv[q][k].x, gv[k].y, fma(-vv[q][k].y, gv[k].x, si));
+          } else {
+            sr = fma(vv[q][k], gv[k], sr);
+          }
+        }
+        sr = warp_sum(sr);
+        if constexpr (CPLX) si = warp_sum(si);
+        if (lane == 0 && j0 + q < m) {
+          md_sm[(2 * (j0 + q)) * kMdWarps + 2 * warp] += sr;
+          md_sm[(2 * (j0 + q)) * kMdWarps + 2 * warp + 1] += si;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < m; j += kMdThreads) {
+    double sr = 0.0, si = 0.0;
+    for (int w = 0; w < kMdWarps; ++w) {
+      sr += md_sm[(2 * j) * kMdWarps + 2 * w];
+      si += md_sm[(2 * j) * kMdWarps + 2 * w + 1];
+    }
+    partial[((int64_t)j * gridDim.x + blockIdx.x) * 2] = sr;
+    partial[((int64_t)j * gridDim.x + blockIdx.x) * 2 + 1] = si;
+  }
+}
+
+// res[2 j .. 2 j + 1] = sum over the nb partial pairs of row j (block j, fixed order)
+__global__ void multidot_finish_kernel(const double *__restrict__ partial, int nb,
+                                       double *__restrict__ res, const double *__restrict__ gate) {
+  if (!gate_open(gate)) return;
+  const double *p = partial + (int64_t)blockIdx.x * nb * 2;
+  double v[2] = {0.0, 0.0};
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    v[0] += p[2 * i];
+    v[1] += p[2 * i + 1];
+  }
+  double out[2];
+  block_sum<2>(v, out);
+  if (threadIdx.x == 0) {
+    res[2 * blockIdx.x] = out[0];
+    res[2 * blockIdx.x + 1] = out[1];
+  }
+}
+
+// g -= sum_j c_j v_j (complex c_j when CPLX), partial[b] = |g|^2 slice.  The
+// vector loop is unrolled by 8 with two accumulators, so eight loads are in
+// flight per element.
+template <bool CPLX>
+__global__ void project_kernel(double *__restrict__ g, const double *const *__restrict__ vecs,
+                               const double *__restrict__ c, int m, int64_t n,
+                               double *__restrict__ partial, const double *__restrict__ gate) {
+  if (!gate_open(gate)) return;
+  __shared__ double cs[2 * kMaxVecs];
+  __shared__ const double *vs[kMaxVecs];
+  for (int j = threadIdx.x; j < m; j += blockDim.x) {
+    cs[2 * j] = c[2 * j];
+    cs[2 * j + 1] = c[2 * j + 1];
+    vs[j] = vecs[j];
+  }
+  __syncthreads();
+  double v[1] = {0.0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    if constexpr (CPLX) {
+      double2 x = ((double2 *)g)[i], y = make_double2(0.0, 0.0);
+#pragma unroll 8
+      for (int j = 0; j < m; ++j) {
+        const double2 a = ((const double2 *)vs[j])[i];
+        const double cr = cs[2 * j], ci = cs[2 * j + 1];
+        if (j & 1) {
+          y.x = fma(cr, a.x, fma(-ci, a.y, y.x));
+          y.y = fma(cr, a.y, fma(ci, a.x, y.y));
+        } else {
+          x.x = fma(-cr, a.x, fma(ci, a.y, x.x));
+          x.y = fma(-cr, a.y, fma(-ci, a.x, x.y));
+        }
+      }
+      x.x -= y.x;
+      x.y -= y.y;
+      ((double2 *)g)[i] = x;
+      v[0] = fma(x.x, x.x, fma(x.y, x.y, v[0]));
+    } else {
+      double x = g[i], y = 0.0;
+#pragma unroll 8
+      for (int j = 0; j < m; ++j) {
+        if (j & 1)
+          y = fma(cs[2 * j], vs[j][i], y);
+        else
+          x = fma(-cs[2 * j], vs[j][i], x);
+      }
+      x -= y;
+      g[i] = x;
+      v[0] = fma(x, x, v[0]);
+    }
+  }
+  double out[1];
+  block_sum<1>(v, out);
+  if (threadIdx.x == 0) partial[blockIdx.x] = out[0];
+}
+
+// res[0] = sum of the nb partials (fixed order); with keep, keep[0] = the
+// previous res[0] (|g|^2 before a Gram-Schmidt pass) and keep[1] = the sum
+__global__ void norm_finish_kernel(const double *__restrict__ partial, int nb,
+                                   double *__restrict__ res, double *__restrict__ keep,
+                                   const double *__restrict__ gate) {
+  if (!gate_open(gate)) return;
+  double v[1] = {0.0};
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) v[0] += partial[i];
+  double out[1];
+  block_sum<1>(v, out);
+  if (threadIdx.x == 0) {
+    if (keep) {
+      keep[0] = res[0];
+      keep[1] = out[0];
+    }
+    res[0] = out[0];
+  }
+}
+
+// g = g - Re(alpha) v1 - sqrt(nrm2_prev) v2 (v2 may be null), partial = |g|^2 slices
+__global__ void krylov_update_kernel(double *__restrict__ g, const double *__restrict__ v1,
+                                     const double *__restrict__ v2,
+                                     const double *__restrict__ alpha,
+                                     const double *__restrict__ nrm2_prev, int64_t n,
+                                     double *__restrict__ partial) {
+  const double c1 = alpha[0], c2 = v2 ? sqrt(nrm2_prev[0]) : 0.0;
+  double v[1] = {0.0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    double x = g[i];
+    x = fma(-c1, v1[i], x);
+    if (v2) x = fma(-c2, v2[i], x);
+    g[i] = x;
+    v[0] = fma(x, x, v[0]);
+  }
+  double out[1];
+  block_sum<1>(v, out);
+  if (threadIdx.x == 0) partial[blockIdx.x] = out[0];
+}
+
+__global__ void normalise_kernel(double *__restrict__ x, int64_t n,
+                                 const double *__restrict__ nrm2) {
+  const double nr = sqrt(nrm2[0]);
+  if (nr == 0.0) return;
+  const double s = 1.0 / nr;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) x[i] *= s;
+}
+
 int red_grid(const Ctx &ctx, int64_t n) {
   int64_t g = (n + kRedThreads - 1) / kRedThreads;
   return (int)std::max<int64_t>(1, std::min<int64_t>(g, 4 * ctx.num_sms));
@@ -221,6 +438,113 @@ void lincomb(VecWork &w, double *out, const std::vector<const double *> &vecs,
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches++;
   ctx.sync();  // pinned staging buffer is reused by the next call
+}
+
+KrylovWork::KrylovWork(Ctx &c, int64_t n_elems, bool complex_data)
+    : ctx(c), n(n_elems), cplx(complex_data) {
+  const int64_t blocks = (n + kMdThreads * kMdPer - 1) / (kMdThreads * kMdPer);
+  nb = (int)std::max<int64_t>(1, std::min<int64_t>(blocks, 2 * ctx.num_sms));
+  partial = (double *)ctx.alloc(sizeof(double) * 2 * (size_t)kMaxVecs * nb);
+  gate = (double *)ctx.alloc(sizeof(double) * 2);
+  const int msm = (int)(sizeof(double) * 2 * kMaxVecs * kMdWarps);
+  UDMRG_CHECK_CUDA(cudaFuncSetAttribute(multidot_kernel<true>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, msm));
+  UDMRG_CHECK_CUDA(cudaFuncSetAttribute(multidot_kernel<false>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, msm));
+  red = (double *)ctx.alloc(sizeof(double) * 8 * 1024);
+  coef = (double *)ctx.alloc(sizeof(double) * 2 * kMaxVecs);
+  alpha = (double *)ctx.alloc(sizeof(double) * 2 * kMaxVecs);
+  nrm2 = (double *)ctx.alloc(sizeof(double) * kMaxVecs);
+  ptrs = (const double **)ctx.alloc(sizeof(double *) * kMaxVecs);
+  UDMRG_CHECK_CUDA(cudaMallocHost((void **)&hptrs, sizeof(double *) * kMaxVecs));
+  UDMRG_CHECK_CUDA(cudaMallocHost((void **)&hres, sizeof(double) * 4));
+}
+
+KrylovWork::~KrylovWork() {
+  cudaStreamSynchronize(ctx.stream);  // pinned sources of queued copies
+  cudaFreeHost((void *)hptrs);
+  cudaFreeHost(hres);
+  ctx.free(partial);
+  ctx.free(gate);
+  ctx.free(red);
+  ctx.free(coef);
+  ctx.free(alpha);
+  ctx.free(nrm2);
+  ctx.free((void *)ptrs);
+}
+
+void KrylovWork::push(int j, const double *v) {
+  UDMRG_REQUIRE(j < kMaxVecs, "Krylov basis: too many vectors");
+  hptrs[j] = v;
+  UDMRG_CHECK_CUDA(cudaMemcpyAsync((void *)(ptrs + j), (const void *)(hptrs + j),
+                                   sizeof(double *), cudaMemcpyHostToDevice, ctx.stream));
+}
+
+void krylov_alpha(KrylovWork &k, int j, const double *y) {
+  Ctx &ctx = k.ctx;
+  const int g = red_grid(ctx, k.n);
+  dot_partial_kernel<<<g, kRedThreads, 0, ctx.stream>>>(k.hptrs[j], y, k.n, k.cplx ? 1 : 0,
+                                                         k.red);
+  finish_sum_kernel<<<1, kRedThreads, 0, ctx.stream>>>(k.red, g, 2, k.alpha + 2 * j);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  ctx.launches += 2;
+}
+
+void krylov_update(KrylovWork &k, int j, double *g) {
+  Ctx &ctx = k.ctx;
+  const int64_t nd = k.n * (k.cplx ? 2 : 1);
+  const int gr = red_grid(ctx, nd);
+  krylov_update_kernel<<<gr, kRedThreads, 0, ctx.stream>>>(
+      g, k.hptrs[j], j > 0 ? k.hptrs[j - 1] : nullptr, k.alpha + 2 * j, k.nrm2 + j, nd, k.red);
+  finish_sum_kernel<<<1, kRedThreads, 0, ctx.stream>>>(k.red, gr, 1, k.nrm2 + j + 1);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  ctx.launches += 2;
+}
+
+void krylov_project(KrylovWork &k, int j, double *g, bool second) {
+  Ctx &ctx = k.ctx;
+  const int m = j + 1;
+  // gate[0] = |g|^2 before the first pass, gate[1] = after it (k.gate has
+  // the two slots for the current step)
+  const double *gate = second ? k.gate : nullptr;
+  const size_t msm = sizeof(double) * 2 * (size_t)m * kMdWarps;
+  if (k.cplx)
+    multidot_kernel<true><<<k.nb, kMdThreads, msm, ctx.stream>>>(k.ptrs, m, g, k.n, k.partial,
+                                                                 gate);
+  else
+    multidot_kernel<false><<<k.nb, kMdThreads, msm, ctx.stream>>>(k.ptrs, m, g, k.n, k.partial,
+                                                                  gate);
+  multidot_finish_kernel<<<m, kRedThreads, 0, ctx.stream>>>(k.partial, k.nb, k.coef, gate);
+  const int gr = red_grid(ctx, k.n);
+  if (k.cplx)
+    project_kernel<true><<<gr, kRedThreads, 0, ctx.stream>>>(g, k.ptrs, k.coef, m, k.n, k.red,
+                                                             gate);
+  else
+    project_kernel<false><<<gr, kRedThreads, 0, ctx.stream>>>(g, k.ptrs, k.coef, m, k.n, k.red,
+                                                              gate);
+  // both passes end in nrm2[j+1]; the first also sets gate = {before, after}
+  norm_finish_kernel<<<1, kRedThreads, 0, ctx.stream>>>(k.red, gr, k.nrm2 + j + 1,
+                                                        second ? nullptr : k.gate, gate);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  ctx.launches += 4;
+}
+
+void krylov_normalise(KrylovWork &k, int j, double *g) {
+  Ctx &ctx = k.ctx;
+  const int64_t nd = k.n * (k.cplx ? 2 : 1);
+  if (nd == 0) return;
+  normalise_kernel<<<ew_grid(ctx, nd), 256, 0, ctx.stream>>>(g, nd, k.nrm2 + j + 1);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  ctx.launches++;
+}
+
+void krylov_fetch(KrylovWork &k, int j) {
+  Ctx &ctx = k.ctx;
+  UDMRG_CHECK_CUDA(cudaMemcpyAsync(k.hres, k.alpha + 2 * j, sizeof(double),
+                                   cudaMemcpyDeviceToHost, ctx.stream));
+  UDMRG_CHECK_CUDA(cudaMemcpyAsync(k.hres + 1, k.nrm2 + j + 1, sizeof(double),
+                                   cudaMemcpyDeviceToHost, ctx.stream));
+  ctx.sync();
 }
 
 void conj_inplace(Ctx &ctx, double *x, int64_t n_cplx) {

@@ -362,7 +362,8 @@ void build_outputs(Ctx &ctx, DeviceScratch &scratch, const BTensor &T, int ldims
 // throws on a failed eigensolve (1: no convergence, 2: non-finite input)
 void check_eig_status(int st) {
   if (st == 2) throw Error(kErrNumerics, "svd: non-finite values in the matrix to decompose");
-  if (st != 0) throw Error(kErrNumerics, "svd: Jacobi eigensolver did not converge");
+  if (st == 3) throw Error(kErrNumerics, "svd: the multi-CTA reduction timed out");
+  if (st != 0) throw Error(kErrNumerics, "svd: eigensolver failed");
 }
 
 std::vector<double> download_vec(Ctx &ctx, const double *d, int64_t n) {
