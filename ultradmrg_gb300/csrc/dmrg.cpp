@@ -3,9 +3,12 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <limits>
 #include <map>
 
 namespace udmrg {
+
+static_assert(kSpectrumFloor == kRankSv, "the SVD keeps the spectrum the rank model reads");
 
 TensorPtr contract_axes(Ctx &ctx, const BTensor &A, const BTensor &B, const std::vector<int> &ca,
                         const std::vector<int> &cb) {
@@ -627,11 +630,19 @@ static double now() {
       .count();
 }
 
-static double two_site_update(Ctx &ctx, std::vector<TensorPtr> &mps,
-                              std::vector<TensorPtr> &lenvs, std::vector<TensorPtr> &renvs,
-                              const std::vector<const BTensor *> &mpo, const SweepParams &p,
-                              char dir, int64_t target, std::vector<SiteLog> *log,
-                              LearnState *learn) {
+void PendingSlot::resolve() {
+  if (!pe) return;
+  e0 = pe->value();
+  if (log && idx >= 0) (*log)[idx].e0 = e0;
+  pe.reset();
+  idx = -1;
+}
+
+static void two_site_update(Ctx &ctx, std::vector<TensorPtr> &mps,
+                            std::vector<TensorPtr> &lenvs, std::vector<TensorPtr> &renvs,
+                            const std::vector<const BTensor *> &mpo, const SweepParams &p,
+                            char dir, int64_t target, std::vector<SiteLog> *log,
+                            LearnState *learn, PendingSlot &slot) {
   const int64_t N = (int64_t)mps.size();
   int64_t l, r, lenv_len, renv_len;
   if (dir == 'r') {
@@ -704,7 +715,8 @@ static double two_site_update(Ctx &ctx, std::vector<TensorPtr> &mps,
     }
   }
   auto res = two_site_update_local(ctx, *lenvs[lenv_len], *renvs[renv_len], *mps[l], *mps[r],
-                                   *mpo[l], *mpo[r], p, dir, &lg, hp, learn ? &now : nullptr);
+                                   *mpo[l], *mpo[r], p, dir, &lg, hp, learn ? &now : nullptr,
+                                   &slot);
   lg.site = target;
   if (learn) {
     // kept counts of this update per bond QN = the new bond index of mps[l]
@@ -730,39 +742,41 @@ static double two_site_update(Ctx &ctx, std::vector<TensorPtr> &mps,
     lenvs[lenv_len + 1] = std::move(res.env);
   else
     renvs[renv_len + 1] = std::move(res.env);
+  if (slot.pe) {  // energy still on its way: the slot fills the entry
+    slot.log = log;
+    slot.idx = log ? (int64_t)log->size() : -1;
+  } else {
+    slot.e0 = lg.e0;
+  }
   if (log) log->push_back(lg);
-  return lg.e0;
 }
 
 LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &renv,
                                   const BTensor &mps_l, const BTensor &mps_r,
                                   const BTensor &mpo_l, const BTensor &mpo_r,
                                   const SweepParams &p, char dir, SiteLog *log,
-                                  const SketchHint *hint, BondSpectra *spectra) {
+                                  const SketchHint *hint, BondSpectra *spectra,
+                                  PendingSlot *slot) {
   UDMRG_REQUIRE(dir == 'r' || dir == 'l', "dir must be 'r' or 'l'");
   const double t0 = now();
   auto init_state = contract_axes(ctx, mps_l, mps_r, {2}, {0});
   auto mv = plan_matvec2(ctx, lenv, mpo_l, mpo_r, renv, *init_state, p.lancz.precision);
   const bool mixed = mv->sg != nullptr;
+  if (slot) slot->resolve();  // the previous update's energy
   auto lres = lanczos_gs(ctx, *mv, *init_state, p.lancz, /*defer_rayleigh=*/mixed);
   const double t1 = now();
   const double mvflops = mv->flops;
   init_state.reset();
-  // mixed precision: the FP64 Rayleigh quotient runs beside the SVD and the
-  // environment update
-  PendingEnergy pe;
-  if (mixed)
-    pe.launch(ctx, std::move(mv), std::move(lres.gs_vec));
-  else
-    mv.reset();
-  const BTensor &psi = mixed ? *pe.psi : *lres.gs_vec;
+  if (!mixed) mv.reset();
+  const BTensor &psi = *lres.gs_vec;
   const QN ldiv = mps_l.div();
   const int split = dir == 'r' ? kSvdSplitLeft : kSvdSplitRight;
   SvdResult sres;
   double audit_err = -1.0, audit_sec = 0.0;
   int64_t audit_diff = 0;
   if (p.svd_mode == kSvdExact || (p.svd_mode == kSvdSketchLearned && !hint)) {
-    sres = svd_trunc(ctx, psi, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split);
+    sres = svd_trunc(ctx, psi, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split,
+                     spectra ? kSpectrumFloor : 0);
   } else {
     SketchParams sp;
     sp.oversample = p.svd_oversample;
@@ -791,6 +805,14 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
       audit_sec = now() - ta;
     }
   }
+  // mixed precision: the FP64 Rayleigh quotient of psi runs on the side
+  // stream beside the environment update (and, in a sweep, the next
+  // update's planning); it owns the plan and psi from here
+  std::unique_ptr<PendingEnergy> pe;
+  if (mixed) {
+    pe = std::make_unique<PendingEnergy>();
+    pe->launch(ctx, std::move(mv), std::move(lres.gs_vec));
+  }
   lres.gs_vec.reset();
   if (spectra) {
     spectra->clear();
@@ -807,7 +829,15 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
   else
     out.env = update_site_renv(ctx, renv, *out.mps_r, mpo_r);
   ctx.sync();
-  const double e0 = mixed ? pe.value() : lres.gs_eng;
+  double e0 = lres.gs_eng;
+  if (mixed) {
+    if (slot) {
+      e0 = std::numeric_limits<double>::quiet_NaN();  // filled in by the slot
+      slot->pe = std::move(pe);
+    } else {
+      e0 = pe->value();
+    }
+  }
   const double t3 = now();
   {
     int64_t sk = 0;
@@ -845,18 +875,19 @@ double two_site_finite_vmps(Ctx &ctx, std::vector<TensorPtr> &mps,
   for (int64_t i = 1; i <= N - 2; ++i)
     renvs[i] = update_site_renv(ctx, *renvs[i - 1], *mps[N - i], *W[N - i]);
   lenvs[0] = trivial_lenv(ctx, *mps[0], *W[0]);
-  double e0 = 0;
   if (learn && (int64_t)learn->prev.size() != N) {  // history is kept across calls
     learn->prev.assign(N, {});
     learn->prev_kept.assign(N, {});
   }
+  PendingSlot slot;  // destroyed before the environments it reads
   for (int64_t s = 0; s < p.sweeps; ++s) {
     for (int64_t i = 0; i < N - 2; ++i)
-      e0 = two_site_update(ctx, mps, lenvs, renvs, W, p, 'r', i, log, learn);
+      two_site_update(ctx, mps, lenvs, renvs, W, p, 'r', i, log, learn, slot);
     for (int64_t i = N - 1; i > 1; --i)
-      e0 = two_site_update(ctx, mps, lenvs, renvs, W, p, 'l', i, log, learn);
+      two_site_update(ctx, mps, lenvs, renvs, W, p, 'l', i, log, learn, slot);
   }
-  return e0;
+  slot.resolve();
+  return slot.e0;
 }
 
 namespace {

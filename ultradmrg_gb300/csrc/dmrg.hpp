@@ -156,14 +156,29 @@ using BondSpectra = std::vector<std::pair<QN, std::vector<double>>>;
 struct LocalUpdate {
   TensorPtr mps_l, mps_r, env;
 };
+// A mixed-precision update's FP64 energy still being computed on the side
+// stream, carried to the next update of a sweep (which collects it after its
+// matvec plan is built, so the Rayleigh quotient overlaps the environment
+// update and the host-side planning).  resolve() writes it into the log.
+struct PendingSlot {
+  std::unique_ptr<PendingEnergy> pe;
+  std::vector<SiteLog> *log = nullptr;
+  int64_t idx = -1;  // log entry waiting for the energy
+  double e0 = 0.0;   // the last resolved energy
+  void resolve();
+};
+
 // hint: sketch sizes for the randomized SVD (learned mode); spectra: receives
-// the leading singular values of every bond sector of this update.
+// the leading singular values of every bond sector of this update.  With a
+// slot, the previous update's pending energy is resolved before this
+// update's Lanczos and this update's (mixed precision) is left pending there;
+// log->e0 is then filled in by the slot.
 LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &renv,
                                   const BTensor &mps_l, const BTensor &mps_r,
                                   const BTensor &mpo_l, const BTensor &mpo_r,
                                   const SweepParams &p, char dir, SiteLog *log,
                                   const SketchHint *hint = nullptr,
-                                  BondSpectra *spectra = nullptr);
+                                  BondSpectra *spectra = nullptr, PendingSlot *slot = nullptr);
 
 // Learned truncation state: the rank model (used when svd_mode ==
 // kSvdSketchLearned), the spectra and kept counts of every bond at its last

@@ -245,6 +245,96 @@ __global__ void bisect_kernel(const EigJob *__restrict__ jobs, const int2 *__res
   }
 }
 
+// ---- leading eigenvalues only (positive semi-definite jobs) ----
+//
+// A truncated SVD keeps at most Dmax states of all bond sectors together, and
+// the weight of the discarded ones follows from each Gram matrix's trace, so
+// only the leading eigenvalues of every sector need bisection.  A common
+// threshold is read off Sturm counts at a logarithmic grid of points below
+// the largest Gershgorin bound of all jobs.
+constexpr int kGrid = 256;             // grid points
+constexpr double kGridDecades = 32.0;  // the grid spans top .. top * 1e-32
+
+// top[0] = max over jobs of scale * (Gershgorin upper bound of its tridiagonal)
+__global__ void grid_top_kernel(const EigJob *__restrict__ jobs, int nj,
+                                const double *__restrict__ d_all, const double *__restrict__ e_all,
+                                const double *__restrict__ scale_all, double *__restrict__ top) {
+  __shared__ double red[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  double m = 0.0;
+  for (int q = warp; q < nj; q += nwarp) {
+    const EigJob job = jobs[q];
+    const int n = job.n;
+    const double *d = d_all + job.lam_off, *e = e_all + job.lam_off;
+    double h = 0.0;
+    for (int i = lane; i < n; i += 32)
+      h = fmax(h, d[i] + (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0));
+    for (int o = 16; o > 0; o >>= 1) h = fmax(h, __shfl_down_sync(0xffffffffu, h, o));
+    if (lane == 0) m = fmax(m, scale_all[q] * h);
+  }
+  if (lane == 0) red[warp] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < nwarp; ++w) t = fmax(t, red[w]);
+    top[0] = t;
+  }
+}
+
+// cnt[q * (kGrid + 1) + k] = number of eigenvalues of job q not below
+// x_k = top * 10^(-k * kGridDecades / (kGrid - 1)) for k < kGrid, and n for
+// k = kGrid; tr[q] = scale * sum of the diagonal (the trace).  One block per
+// job, one grid point per thread.
+__global__ void grid_count_kernel(const EigJob *__restrict__ jobs,
+                                  const double *__restrict__ d_all,
+                                  const double *__restrict__ e_all,
+                                  const double *__restrict__ scale_all,
+                                  const double *__restrict__ top, int *__restrict__ cnt,
+                                  double *__restrict__ tr) {
+  extern __shared__ double sm[];
+  __shared__ double pm[2];
+  const int q = blockIdx.x;
+  const EigJob job = jobs[q];
+  const int n = job.n;
+  double *d = sm, *e = sm + n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    d[i] = d_all[job.lam_off + i];
+    e[i] = i + 1 < n ? e_all[job.lam_off + i] : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = 0.0, em = 0.0;
+    for (int i = threadIdx.x; i < n; i += 32) {
+      t += d[i];
+      em = fmax(em, fabs(e[i]));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      t += __shfl_down_sync(0xffffffffu, t, o);
+      em = fmax(em, __shfl_down_sync(0xffffffffu, em, o));
+    }
+    if (threadIdx.x == 0) {
+      pm[0] = t;
+      pm[1] = em;
+    }
+  }
+  __syncthreads();
+  const double sc = scale_all[q];
+  if (threadIdx.x == 0) tr[q] = sc * pm[0];
+  const double pivmin = 1e-290 * fmax(1.0, pm[1] * pm[1]);  // as in bisect_kernel
+  for (int k = threadIdx.x; k <= kGrid; k += blockDim.x) {
+    int c;
+    if (k == kGrid || n == 0) {
+      c = n;
+    } else if (sc <= 0.0 || top[0] <= 0.0) {
+      c = 0;  // a zero matrix: no eigenvalue reaches x_k > 0
+    } else {
+      const double x = top[0] * exp10(-(double)k * kGridDecades / (kGrid - 1));
+      c = n - sturm_count(d, e, n, x / sc, pivmin);
+    }
+    cnt[(int64_t)q * (kGrid + 1) + k] = c;
+  }
+}
+
 __device__ __forceinline__ double start_entry(uint64_t seed, int i) {
   uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(i + 1);
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -414,20 +504,19 @@ __device__ __forceinline__ double2 cadd(double2 a, double2 b) {
 // the reflector v_j of row j and w_j = t_j A v_j - K v_j; one fused pass over
 // each CTA's own rows applies the rank-2 update of step j and forms the
 // matrix-vector product of step j + 1, so the trailing block is read and
-// written once per step.  Per step the CTAs meet twice: a counter barrier
-// (every w_j entry and partial sum is written) and a flag that the owner of
-// row j + 1 raises once it has updated that row (every CTA forms the next
-// reflector from it).  Each wait gives up after kTriTimeoutNs and sets
-// status 3.  Partial sums are added in CTA order, so the result does not
-// depend on timing.
+// written once per step.  Per step the CTAs meet once, at a counter barrier
+// (every w_j entry and partial sum is written); then every CTA applies step
+// j's update to row j + 1 in its own shared memory (the same arithmetic in
+// every CTA) and forms the next reflector from it.  The barrier gives up
+// after kTriTimeoutNs and sets status 3.  Partial sums are added in CTA
+// order, so the result does not depend on timing.
 struct TriPart {
   int32_t job, p, P, slot;
   int64_t wb_off;  // 2 n scalars of w buffers (double-buffered by step parity)
 };
 struct TriSlot {  // one per matrix, zeroed before the launch
   unsigned int arrive;
-  int flag;
-  int pad[2];
+  int pad[3];
 };
 constexpr int kTriMaxParts = 64;
 constexpr unsigned long long kTriTimeoutNs = 2000000000ull;
@@ -499,38 +588,18 @@ __device__ bool tri_barrier(TriSlot *sl, unsigned target, int *status) {
   return ok != 0;
 }
 
-// Waits until the owner of row `row` has published it.
-__device__ bool tri_wait_row(TriSlot *sl, int row, int *status) {
-  __shared__ int ok;
-  if (threadIdx.x == 0) {
-    const unsigned long long t0 = global_ns();
-    int good = 1;
-    while (*(volatile int *)&sl->flag < row) {
-      if (global_ns() - t0 > kTriTimeoutNs) {
-        good = 0;
-        atomicExch(status, 3);
-        break;
-      }
-      __nanosleep(32);
-    }
-    __threadfence();
-    ok = good;
-  }
-  __syncthreads();
-  return ok != 0;
-}
-
-// Reflector of step j from row j (columns j+1 ..): v (v_0 = 1) into v[0 .. m),
-// returns tau; the CTA with p == 0 writes d[j], e[j], tau[j].  Same formulas
-// as the single-CTA kernels.
+// Reflector of step j from row j, held in shared memory from its diagonal
+// on (row[c - j] = A[j][c]): v (v_0 = 1) into v[0 .. m), returns tau; the CTA
+// with writer set writes d[j], e[j], tau[j].  Same formulas as the
+// single-CTA kernels.
 template <typename T>
-__device__ T tri_reflector(const T *A, int n, int j, T *v, double *red, bool writer, double *d,
+__device__ T tri_reflector(const T *row, int n, int j, T *v, double *red, bool writer, double *d,
                            double *e, T *tau) {
-  const T *rowj = A + (int64_t)j * n;
+  const T *rowj = row - j;  // rowj[c] = A[j][c], c >= j
   const int m = n - j - 1;
-  const T alpha = cj(__ldcg(&rowj[j + 1]));
+  const T alpha = cj(rowj[j + 1]);
   double x2 = 0.0;
-  for (int c = j + 2 + threadIdx.x; c < n; c += blockDim.x) x2 += sabs2(__ldcg(&rowj[c]));
+  for (int c = j + 2 + threadIdx.x; c < n; c += blockDim.x) x2 += sabs2(rowj[c]);
   x2 = block_sum(x2, red);
   T t = smake<T>(0.0, 0.0), sc = smake<T>(0.0, 0.0);
   double beta = sre(alpha);
@@ -543,9 +612,9 @@ __device__ T tri_reflector(const T *A, int n, int j, T *v, double *red, bool wri
   }
   for (int r = threadIdx.x; r < m; r += blockDim.x)
     v[r] = r == 0 ? smake<T>(1.0, 0.0)
-                  : (refl ? smul(cj(__ldcg(&rowj[j + 1 + r])), sc) : smake<T>(0.0, 0.0));
+                  : (refl ? smul(cj(rowj[j + 1 + r]), sc) : smake<T>(0.0, 0.0));
   if (writer && threadIdx.x == 0) {
-    d[j] = sre(__ldcg(&rowj[j]));
+    d[j] = sre(rowj[j]);
     e[j] = beta;
     tau[j] = t;
   }
@@ -573,7 +642,7 @@ __global__ void __launch_bounds__(kTriThreads)
   T *rd = red_all + (int64_t)pt.slot * 2 * kTriMaxParts;
   double *d = d_all + job.lam_off, *e = e_all + job.lam_off;
   T *tau = tau_all + job.lam_off;
-  T *vA = (T *)tri_sm, *vB = vA + n, *wA = vB + n;
+  T *vA = (T *)tri_sm, *vB = vA + n, *wA = vB + n, *rb = wA + n;  // rb: the next pivot row
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
   const int nwarp = nt >> 5;
   unsigned nbar = 0;
@@ -608,14 +677,18 @@ __global__ void __launch_bounds__(kTriThreads)
     pw[P + p] = bad;
   }
   if (!tri_barrier(sl, ++nbar * P, status)) return;
-  if (tid == 0) {
+  if (warp == 0) {
     double m = 0.0;
     int bad = 0;
-    for (int q = 0; q < P; ++q) {
+    for (int q = lane; q < P; q += 32) {
       m = fmax(m, __ldcg(&pw[q]));
       bad |= __ldcg(&pw[P + q]) != 0.0;
     }
-    red[32] = bad ? -1.0 : m;
+    for (int o = 16; o > 0; o >>= 1) {
+      m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+      bad |= __shfl_down_sync(0xffffffffu, bad, o);
+    }
+    if (lane == 0) red[32] = bad ? -1.0 : m;
   }
   __syncthreads();
   const double scale = red[32];
@@ -668,7 +741,7 @@ __global__ void __launch_bounds__(kTriThreads)
     }
     // CTA partial, summed over warps in order
     __syncthreads();
-    T *wp = (T *)(tri_sm + 3 * (size_t)n * sizeof(T));  // nwarp scalars
+    T *wp = (T *)(tri_sm + 4 * (size_t)n * sizeof(T));  // nwarp scalars
     if (lane == 0) wp[warp] = acc;
     __syncthreads();
     if (tid == 0) {
@@ -679,17 +752,21 @@ __global__ void __launch_bounds__(kTriThreads)
   };
 
   // step 0: reflector and products of the own rows
-  T t = tri_reflector(A, n, 0, vA, red, p == 0, d, e, tau);
+  for (int c = tid; c < n; c += nt) rb[c] = __ldcg(&A[c]);
+  __syncthreads();
+  T t = tri_reflector(rb, n, 0, vA, red, p == 0, d, e, tau);
   rows_pass(1, false, vA, t, wb, rd);
   for (int j = 0; j + 1 < n; ++j) {
     const int m = n - j - 1, par = j & 1;
     if (!tri_barrier(sl, ++nbar * P, status)) return;
     if (j % P == p)  // reflector storage; every CTA has read row j by now
       for (int c = j + 2 + tid; c < n; c += nt) A[(int64_t)j * n + c] = vA[c - j - 1];
-    if (tid == 0) {
+    if (warp == 0) {  // the P partials: lane q holds q and q + 32, tree sum in lane order
       T s = smake<T>(0.0, 0.0);
-      for (int q = 0; q < P; ++q) s = sadd(s, __ldcg(&rd[par * kTriMaxParts + q]));
-      ksum = smul(sscale(-0.5, t), s);  // K = -t (w^H v) / 2
+      if (lane < P) s = __ldcg(&rd[par * kTriMaxParts + lane]);
+      if (lane + 32 < P) s = sadd(s, __ldcg(&rd[par * kTriMaxParts + lane + 32]));
+      s = warp_sum(s);
+      if (lane == 0) ksum = smul(sscale(-0.5, t), s);  // K = -t (w^H v) / 2
     }
     __syncthreads();
     const T K = ksum;
@@ -707,22 +784,16 @@ __global__ void __launch_bounds__(kTriThreads)
       }
       break;
     }
-    // row j + 1 first, then published
-    if ((j + 1) % P == p) {
-      T *ar = A + (int64_t)(j + 1) * n;
+    // row j + 1 (updated through step j - 1 by its owner) with step j's update
+    {
+      const T *ar = A + (int64_t)(j + 1) * n;
       const T v0 = vA[0], w0 = wA[0];
       for (int c = j + 1 + tid; c < n; c += nt)
-        ar[c] = ssub(ar[c], sadd(smul(v0, cj(wA[c - j - 1])), smul(w0, cj(vA[c - j - 1]))));
+        rb[c - j - 1] =
+            ssub(__ldcg(&ar[c]), sadd(smul(v0, cj(wA[c - j - 1])), smul(w0, cj(vA[c - j - 1]))));
       __syncthreads();
-      if (tid == 0) {
-        __threadfence();
-        atomicExch(&sl->flag, j + 1);
-      }
-      __syncthreads();
-    } else if (!tri_wait_row(sl, j + 1, status)) {
-      return;
     }
-    const T tn = tri_reflector(A, n, j + 1, vB, red, p == 0, d, e, tau);
+    const T tn = tri_reflector(rb, n, j + 1, vB, red, p == 0, d, e, tau);
     rows_pass(j + 2, true, vB, tn, wb + (par ^ 1) * n, rd + (par ^ 1) * kTriMaxParts);
     T *x = vA;
     vA = vB;
@@ -944,7 +1015,7 @@ void tridiag_multi_cta(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJo
   if (big.empty()) return;
   std::sort(big.begin(), big.end(), [&](int a, int b) { return jobs[a].n > jobs[b].n; });
   const void *kern = (const void *)tridiag_mc_kernel<T>;
-  const size_t msmem = (3 * (size_t)nmax + kTriThreads / 32) * sizeof(T);
+  const size_t msmem = (4 * (size_t)nmax + kTriThreads / 32) * sizeof(T);
   UDMRG_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)msmem));
   int per_sm = 0;
@@ -987,7 +1058,7 @@ void tridiag_multi_cta(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJo
 }
 
 int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, double *G,
-                   double *lam, SymEigWork &wk, bool cplx) {
+                   double *lam, SymEigWork &wk, bool cplx, int64_t need, int64_t floor) {
   const int nj = (int)jobs.size();
   if (nj == 0) return 0;
   int64_t ltot = 0;
@@ -1033,12 +1104,57 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
   else
     tridiag_multi_cta<double>(ctx, scratch, jobs, wk, G, dstat);
   const size_t bsmem = 2 * (size_t)nmax * sizeof(double);
-  if (bsmem > 48 * 1024)
+  if (bsmem > 48 * 1024) {
     UDMRG_CHECK_CUDA(cudaFuncSetAttribute(bisect_kernel,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem));
+    UDMRG_CHECK_CUDA(cudaFuncSetAttribute(grid_count_kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem));
+  }
+  // how many leading eigenvalues of each job to compute
+  wk.computed.assign(nj, 0);
+  wk.trace.clear();
+  int64_t ntot = 0;
+  for (int q = 0; q < nj; ++q) {
+    wk.computed[q] = jobs[q].n;
+    ntot += jobs[q].n;
+  }
+  if (need > 0 && need < ntot) {
+    double *dtop = scratch.get<double>(1), *dtr = scratch.get<double>(nj);
+    int *dcnt = scratch.get<int>((size_t)nj * (kGrid + 1));
+    grid_top_kernel<<<1, 1024, 0, ctx.stream>>>(wk.jobs, nj, wk.d, wk.e, wk.scale, dtop);
+    grid_count_kernel<<<nj, kGrid, bsmem, ctx.stream>>>(wk.jobs, wk.d, wk.e, wk.scale, dtop, dcnt,
+                                                        dtr);
+    UDMRG_CHECK_CUDA(cudaGetLastError());
+    ctx.launches += 2;
+    std::vector<int> cnt((size_t)nj * (kGrid + 1));
+    wk.trace.assign(nj, 0.0);
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(cnt.data(), dcnt, cnt.size() * sizeof(int),
+                                     cudaMemcpyDeviceToHost, ctx.stream));
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(wk.trace.data(), dtr, nj * sizeof(double),
+                                     cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.sync();
+    // the first grid point with `need` eigenvalues above it, then one point
+    // lower (a factor 1.34: near-ties and rounding at the threshold)
+    int ks = kGrid;
+    for (int k = 0; k <= kGrid; ++k) {
+      int64_t t = 0;
+      for (int q = 0; q < nj; ++q) t += cnt[(size_t)q * (kGrid + 1) + k];
+      if (t >= need) {
+        ks = k;
+        break;
+      }
+    }
+    ks = std::min(ks + 1, kGrid);
+    for (int q = 0; q < nj; ++q) {
+      const int64_t n = jobs[q].n;
+      const int64_t c = std::max<int64_t>(cnt[(size_t)q * (kGrid + 1) + ks], std::min(n, floor));
+      wk.computed[q] = std::min(c, n);
+    }
+  }
   std::vector<int2> chunks;
   for (int q = 0; q < nj; ++q)
-    for (int i0 = 0; i0 < jobs[q].n; i0 += kBisectThreads) chunks.push_back(make_int2(q, i0));
+    for (int i0 = jobs[q].n - (int)wk.computed[q]; i0 < jobs[q].n; i0 += kBisectThreads)
+      chunks.push_back(make_int2(q, i0));
   int2 *dch = scratch.get<int2>(chunks.size());
   UDMRG_CHECK_CUDA(cudaMemcpyAsync(dch, chunks.data(), chunks.size() * sizeof(int2),
                                    cudaMemcpyHostToDevice, ctx.stream));
@@ -1080,7 +1196,8 @@ void sym_eig_vectors(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJob>
     nmax = std::max(nmax, n);
     if (k[q] == 0) continue;
     const double *h = hlam.data() + jobs[q].lam_off;
-    const double big = std::max(std::fabs(h[0]), std::fabs(h[n - 1]));
+    const int64_t nc = q < (int)wk.computed.size() ? wk.computed[q] : n;  // computed values
+    const double big = std::max(std::fabs(h[0]), std::fabs(h[std::max<int64_t>(nc, 1) - 1]));
     const double tol = 1e-9 * big;
     int first = 0;
     for (int p = 1; p <= k[q]; ++p) {

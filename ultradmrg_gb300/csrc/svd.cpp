@@ -378,7 +378,7 @@ std::vector<double> download_vec(Ctx &ctx, const double *d, int64_t n) {
 }  // namespace
 
 SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, double trunc_err,
-                    int64_t Dmin, int64_t Dmax, int mode) {
+                    int64_t Dmin, int64_t Dmax, int mode, int64_t spectrum_floor) {
   UDMRG_REQUIRE(ldims > 0 && ldims < T.rank(), "svd: bad ldims");
   const bool cplx = T.dtype == kC128;
   const int es = cplx ? 2 : 1;
@@ -422,19 +422,29 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
     gemm_finalize(g);
     run_gemm(ctx, g, cplx ? kC128 : kF64, Mbuf, Mc, G, 1.0, 0.0);
   }
+  // at most Dmax states are kept: only the leading eigenvalues of the sectors
+  // (a margin of 64 below the Dmax-th largest) are computed; the weight of
+  // the rest is each Gram matrix's trace minus the computed ones
   SymEigWork wk;
-  check_eig_status(sym_eig_values(ctx, scratch, jobs, G, lam, wk, cplx));
+  check_eig_status(sym_eig_values(ctx, scratch, jobs, G, lam, wk, cplx,
+                                  Dmax > 0 ? Dmax + 64 : 0, spectrum_floor));
   const std::vector<double> hlam = download_vec(ctx, lam, ltot);
   std::vector<std::vector<double>> sv(nsec);
+  double rest = 0.0;
   for (int q = 0; q < nsec; ++q) {
-    const int64_t n = jobs[q].n;
+    const int64_t nc = wk.computed[q];
     const int64_t rank_max = std::min(secs[q].rows, secs[q].cols);
-    for (int64_t i = 0; i < std::min(n, rank_max); ++i)
-      sv[q].push_back(std::sqrt(std::max(hlam[jobs[q].lam_off + i], 0.0)));
+    double listed = 0.0;
+    for (int64_t i = 0; i < std::min(nc, rank_max); ++i) {
+      const double l = std::max(hlam[jobs[q].lam_off + i], 0.0);
+      sv[q].push_back(std::sqrt(l));
+      listed += l;
+    }
+    if (!wk.trace.empty()) rest += std::max(wk.trace[q] - listed, 0.0);
   }
   SvdResult res;
   std::vector<int64_t> kept;
-  select_kept(sv, trunc_err, Dmin, Dmax, kept, res.D, res.trunc_err);
+  select_kept(sv, trunc_err, Dmin, Dmax, kept, res.D, res.trunc_err, 1e-12, rest);
   // eigenvectors of the kept states only: the isometric factor (n x kept)
   std::vector<int64_t> iso_off(nsec), iso_ld(nsec);
   int64_t ztot = 0;
@@ -486,7 +496,7 @@ SvdResult svd_trunc_sketch(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv
       fsum += full[q];
     }
     if (sp.max_fraction < 1.0 && (double)ssum > sp.max_fraction * (double)fsum)
-      return svd_trunc(ctx, T, ldims, ldiv, trunc_err, Dmin, Dmax, mode);
+      return svd_trunc(ctx, T, ldims, ldiv, trunc_err, Dmin, Dmax, mode, kSpectrumFloor);
   }
   // isometric factor of sector q (xr x s_q, row-major) kept at uoff[q] across
   // rounds; a round recomputes only the sectors that missed

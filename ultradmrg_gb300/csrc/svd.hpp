@@ -30,6 +30,10 @@ struct SymEigWork {
   EigJob *jobs = nullptr;  // device copy of the jobs
   double *d = nullptr, *e = nullptr, *tau = nullptr, *scale = nullptr;
   bool cplx = false;  // complex Hermitian matrices (interleaved re, im; tau complex)
+  // host: eigenvalues computed per job (the leading ones; all by default) and
+  // each job's trace (the sum of all its eigenvalues)
+  std::vector<int64_t> computed;
+  std::vector<double> trace;
 };
 
 struct ScaleJob {
@@ -48,12 +52,19 @@ void run_scale(Ctx &ctx, const std::vector<ScaleJob> &jobs, double *X, const dou
 // (sector, position); keep the smallest D in [min(Dmin,n), min(Dmax,n)] whose
 // discarded weight sum_{discarded} s^2 / sum s^2 <= trunc_err.
 // Phase 1: reduce every job's symmetric n x n matrix in G to tridiagonal form
-// (G keeps the reflectors) and put all its eigenvalues, descending, at
-// lam[lam_off ...].  Returns 0, or 2 for non-finite input.  jobs[].smem is set.
-// With cplx, G holds complex Hermitian matrices (offsets in complex elements)
-// and phase 2 returns complex eigenvectors.
+// (G keeps the reflectors) and put its eigenvalues, descending, at
+// lam[lam_off ...].  Returns 0, 2 for non-finite input, 3 if the multi-CTA
+// reduction timed out.  jobs[].smem is set.  With cplx, G holds complex
+// Hermitian matrices (offsets in complex elements) and phase 2 returns
+// complex eigenvectors.
+// need > 0 (positive semi-definite matrices, e.g. Gram matrices): only the
+// leading eigenvalues of every job down to a common threshold below which
+// fewer than `need` eigenvalues of all jobs together lie above, at least
+// min(n, floor) per job, are computed (wk.computed); wk.trace holds each job's
+// trace, so the weight of the rest is known exactly.
 int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, double *G,
-                   double *lam, SymEigWork &wk, bool cplx = false);
+                   double *lam, SymEigWork &wk, bool cplx = false, int64_t need = 0,
+                   int64_t floor = 0);
 // Phase 2: the leading k[q] eigenvectors of job q (hlam: host copy of lam) as
 // the columns of Z (row-major n x k[q], leading dimension z_ld[q], at z_off[q]),
 // orthonormal to FP64 accuracy.
@@ -95,8 +106,14 @@ struct SvdResult {
   int64_t grow_rounds = 0;  // randomized path: sketch enlargements after a miss
 };
 
+// Leading singular values per sector that the rank model reads.
+constexpr int64_t kSpectrumFloor = 64;
+
+// Exact truncated SVD.  Only the leading singular values of the sectors are
+// computed (all of them when Dmax does not truncate); spectrum_floor: at
+// least that many per sector (the leading values the rank model reads).
 SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, double trunc_err,
-                    int64_t Dmin, int64_t Dmax, int mode);
+                    int64_t Dmin, int64_t Dmax, int mode, int64_t spectrum_floor = 0);
 
 // Sector-wise randomized truncated SVD.  For every bond sector a Gaussian
 // sketch of `sketch[q]` columns (default: full rank, i.e. exact) spans the

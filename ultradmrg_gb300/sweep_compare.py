@@ -14,6 +14,11 @@ full sweep is timed from that same state in each form:
 * ``mixed_learned_rule``: the same with the cost rule (the exact SVD when
   the predicted sketch exceeds a fraction of the sector dimensions).
 
+A form name may end in ``@<tol>`` (e.g. ``mixed_exact@1e-11``): that form's
+Lanczos runs to that tolerance instead of ``--lanczos-error``.  Each form is
+compared with the FP64 form of the same tolerance (``fp64_exact`` with the
+same suffix) when it is in the list.
+
 ``python -m ultradmrg_gb300.sweep_compare [--out FILE]`` prints one JSON object.
 """
 from __future__ import annotations
@@ -33,6 +38,33 @@ def _upload(ctx, tensors):
     return [api.DeviceTensor.from_data(ctx, t) for t in tensors]
 
 
+def prepare(ctx, Lx=16, Ly=4, schedule="10:2,100:2,500:2,1000:2,2000:1", lanczos_error=1e-9,
+            weights=RT.WEIGHTS):
+    """The Hubbard cylinder (t=1, U=8, one hole every N/8 sites) grown over the
+    schedule ``D:sweeps,...`` (mixed precision, exact SVD, the rank model
+    recording each bond's spectrum).  Returns (host MPO, device MPO, host
+    state, rank model, per-stage log, seconds)."""
+    N = Lx * Ly
+    mpo, pb = M.hubbard_cylinder_mpo(Lx, Ly, t=1.0, U=8.0)
+    labels = M.hubbard_cylinder_holes(N, 8)
+    dmpo = _upload(ctx, mpo)
+    dmps = _upload(ctx, M.direct_product_mps([pb] * N, labels))
+    model = RT.load(ctx, weights)
+    t0 = time.perf_counter()
+    prep = []
+    for item in schedule.split(","):
+        D, sw = (int(v) for v in item.split(":"))
+        p = api.FiniteVMPSSweepParams(sw, D, D, 1e-8, lanczos_error, 100,
+                                      precision=api.PREC_MIXED)
+        e0, log, _, _ = api.two_site_finite_vmps_learned(ctx, dmps, dmpo, p, model, False)
+        prep.append(dict(D=D, sweeps=sw, e0=e0, max_trunc_err=max(r["trunc_err"] for r in log)))
+    sec = time.perf_counter() - t0
+    state = [t.to_data() for t in dmps]
+    for t in dmps:
+        t.close()
+    return mpo, dmpo, state, model, prep, sec
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--Lx", type=int, default=16)
@@ -50,33 +82,22 @@ def main(argv=None):
     a = ap.parse_args(argv)
     ctx = api.Context(0)
     N = a.Lx * a.Ly
-    mpo, pb = M.hubbard_cylinder_mpo(a.Lx, a.Ly, t=1.0, U=8.0)
-    labels = M.hubbard_cylinder_holes(N, 8)
-    dmpo = _upload(ctx, mpo)
-    dmps = _upload(ctx, M.direct_product_mps([pb] * N, labels))
-    model = RT.load(ctx, a.weights)
-    t0 = time.perf_counter()
-    prep = []
-    for item in a.schedule.split(","):
-        D, sw = (int(v) for v in item.split(":"))
-        p = api.FiniteVMPSSweepParams(sw, D, D, 1e-8, a.lanczos_error, 100,
-                                      precision=api.PREC_MIXED)
-        e0, log, _, _ = api.two_site_finite_vmps_learned(ctx, dmps, dmpo, p, model, False)
-        prep.append(dict(D=D, sweeps=sw, e0=e0, max_trunc_err=max(r["trunc_err"] for r in log)))
-    prep_sec = time.perf_counter() - t0
-    state = [t.to_data() for t in dmps]
+    _, dmpo, state, model, prep, prep_sec = prepare(ctx, a.Lx, a.Ly, a.schedule,
+                                                    a.lanczos_error, a.weights)
     out = dict(workload=f"hubbard{a.Ly}x{a.Lx}", D=a.D, sites=N, preparation=prep,
                preparation_seconds=prep_sec, forms={})
     forms = a.forms.split(",")
     if a.audit and "mixed_learned" in forms:
         forms.append("mixed_learned_audit")  # untimed: the exact SVD judges every truncation
     for form in forms:
-        prec = api.PREC_FP64 if form.startswith("fp64") else api.PREC_MIXED
-        mode = 2 if "learned" in form else 0
-        p = api.FiniteVMPSSweepParams(1, a.D, a.D, 1e-8, a.lanczos_error, 100, precision=prec,
-                                      svd_mode=mode, svd_audit=form.endswith("audit"),
+        base, _, tol = form.partition("@")
+        lerr = float(tol) if tol else a.lanczos_error
+        prec = api.PREC_FP64 if base.startswith("fp64") else api.PREC_MIXED
+        mode = 2 if "learned" in base else 0
+        p = api.FiniteVMPSSweepParams(1, a.D, a.D, 1e-8, lerr, 100, precision=prec,
+                                      svd_mode=mode, svd_audit=base.endswith("audit"),
                                       svd_sketch_max_fraction=(a.max_fraction
-                                                               if form.endswith("rule") else 1.0))
+                                                               if base.endswith("rule") else 1.0))
         if mode == 2:  # a model carrying the bond history of the prepared state
             hist = api.RankModel(ctx, 0)
             hist.params = model.params
@@ -97,6 +118,8 @@ def main(argv=None):
                  lanczos_iters=int(sum(r["iters"] for r in log)),
                  max_trunc_err=max(r["trunc_err"] for r in log),
                  svd_grow_rounds=int(sum(r["svd_grow_rounds"] for r in log)),
+                 svd_slowest=[(r["site"], round(r["svd_sec"], 4)) for r in
+                              sorted(log, key=lambda r: -r["svd_sec"])[:5]],
                  energies=[r["e0"] for r in log], trunc_errs=[r["trunc_err"] for r in log])
         if p.svd_audit:
             aud = [r for r in log if r["svd_audit_err"] >= 0]
@@ -107,16 +130,28 @@ def main(argv=None):
         out["forms"][form] = f
         for t in mps:
             t.close()
-    ref = out["forms"].get("fp64_exact")
-    if ref:
-        for k, f in out["forms"].items():
-            f["speedup_vs_fp64_exact"] = ref["sweep_seconds"] / f["sweep_seconds"]
-            f["rel_dE_vs_fp64_exact"] = abs(f["e0"] - ref["e0"]) / abs(ref["e0"])
-            f["max_site_rel_dE_vs_fp64_exact"] = float(np.max(
-                np.abs(np.array(f["energies"]) - np.array(ref["energies"])) /
-                np.abs(np.array(ref["energies"]))))
-            f["max_trunc_err_diff_vs_fp64_exact"] = float(np.max(
-                np.abs(np.array(f["trunc_errs"]) - np.array(ref["trunc_errs"]))))
+    for k, f in out["forms"].items():
+        _, at, tol = k.partition("@")
+        ref = out["forms"].get("fp64_exact" + at + tol)
+        if ref is None:
+            continue
+        f["speedup_vs_fp64_exact"] = ref["sweep_seconds"] / f["sweep_seconds"]
+        f["rel_dE_vs_fp64_exact"] = abs(f["e0"] - ref["e0"]) / abs(ref["e0"])
+        f["max_site_rel_dE_vs_fp64_exact"] = float(np.max(
+            np.abs(np.array(f["energies"]) - np.array(ref["energies"])) /
+            np.abs(np.array(ref["energies"]))))
+        f["max_trunc_err_diff_vs_fp64_exact"] = float(np.max(
+            np.abs(np.array(f["trunc_errs"]) - np.array(ref["trunc_errs"]))))
+    # FP64 against itself at two tolerances: the sweep's own sensitivity
+    tight = [k for k in out["forms"] if k.startswith("fp64_exact@")]
+    if "fp64_exact" in out["forms"] and tight:
+        r0, r1 = out["forms"]["fp64_exact"], out["forms"][tight[0]]
+        out["fp64_tolerance_sensitivity"] = dict(
+            forms=["fp64_exact", tight[0]],
+            rel_dE=abs(r0["e0"] - r1["e0"]) / abs(r1["e0"]),
+            max_site_rel_dE=float(np.max(np.abs(np.array(r0["energies"]) -
+                                                np.array(r1["energies"])) /
+                                         np.abs(np.array(r1["energies"])))))
     for f in out["forms"].values():
         f.pop("energies")
         f.pop("trunc_errs")
