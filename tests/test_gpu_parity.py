@@ -62,7 +62,9 @@ def test_lanczos_parity(ctx, name, l):
     ref = krylov.lanczos_solver(eff, psi.copy(), krylov.eff_ham_mul_two_site_state, params)
     dev = [up(ctx, t) for t in eff]
     res = api.lanczos_solver(ctx, dev, up(ctx, psi), 1e-12, 100)
-    assert abs(res.gs_eng - ref.gs_eng) <= 1e-10 * abs(ref.gs_eng)
+    # 1e-10 relative; absolute below |E| = 1 (both solvers stop at an energy
+    # change of 1e-12, so a near-zero energy agrees only to that level)
+    assert abs(res.gs_eng - ref.gs_eng) <= 1e-10 * max(abs(ref.gs_eng), 1.0)
     g = res.gs_vec.to_data()
     ov = abs(bs.inner(ref.gs_vec, g)) / (bs.norm(ref.gs_vec) * bs.norm(g))
     assert abs(ov - 1.0) < 1e-8
@@ -162,16 +164,19 @@ def test_vmps_golden_hubbard2x2(ctx):
 
 def test_vmps_heisenberg16_vs_oracle(ctx):
     """A truncating sweep (L=16, D=24): per-site energies, truncation errors and
-    bond dimensions against the oracle run with the same parameters."""
+    bond dimensions against the oracle run with the same parameters.  Lanczos
+    runs to 1e-12 on both sides: a truncating sweep carries each local
+    solve's residual into the next environments, so a looser tolerance lets
+    summation order alone move the final energy by about that tolerance."""
     N = 16
     mpo, pb = M.heisenberg_chain_mpo(N)
     labels = M.random_sz0_labels(N, 0)
-    params = api.FiniteVMPSSweepParams(2, 24, 24, 1e-8, 1e-9, 100)
+    params = api.FiniteVMPSSweepParams(2, 24, 24, 1e-8, 1e-12, 100)
     e0, log, _ = _gpu_vmps(ctx, mpo, pb, labels, params)
     mps = M.direct_product_mps([pb] * N, labels)
     olog = []
     oe = ovmps.two_site_finite_vmps(
-        mps, mpo, ovmps.FiniteVMPSSweepParams(2, 24, 24, 1e-8, krylov.LanczosParams(1e-9, 100)),
+        mps, mpo, ovmps.FiniteVMPSSweepParams(2, 24, 24, 1e-8, krylov.LanczosParams(1e-12, 100)),
         olog)
     assert abs(e0 - oe) <= 1e-9 * abs(oe)
     assert len(log) == len(olog)

@@ -902,9 +902,14 @@ int udmrg_matvec_plan_stage_times(udmrg_matvec_plan *p, const double *d_in, doub
       cudaEventRecord(ev[0], ctx.stream);
       run_gemm(ctx, m.p1->gemm, dt, m.L->data, d_in, m.t1, 1.0, 0.0);
       cudaEventRecord(ev[1], ctx.stream);
-      run_gemm(ctx, m.p2->gemm, dt, m.t1, m.W1->data, m.t2, 1.0, 0.0);
-      cudaEventRecord(ev[2], ctx.stream);
-      run_gemm(ctx, m.p3->gemm, dt, m.t2, m.W2->data, m.t3, 1.0, 0.0);
+      if (m.m64) {  // both MPO steps in one channel map (stage 2; stage 3 empty)
+        run_mpo_step64(ctx, *m.m64, m.t1, m.t3);
+        cudaEventRecord(ev[2], ctx.stream);
+      } else {
+        run_gemm(ctx, m.p2->gemm, dt, m.t1, m.W1->data, m.t2, 1.0, 0.0);
+        cudaEventRecord(ev[2], ctx.stream);
+        run_gemm(ctx, m.p3->gemm, dt, m.t2, m.W2->data, m.t3, 1.0, 0.0);
+      }
       cudaEventRecord(ev[3], ctx.stream);
       for (int64_t b : m.missing)
         UDMRG_CHECK_CUDA(cudaMemsetAsync(d_out + m.sstruct->offs[b] * es, 0,

@@ -111,14 +111,24 @@ std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTens
   mv->flops = mv->p1->gemm.flops + mv->p2->gemm.flops + mv->p3->gemm.flops + mv->p4->gemm.flops;
   mv->precision = precision;
   UDMRG_REQUIRE(precision == kPrecFP64 || precision == kPrecMixed, "matvec: unknown precision");
+  // real tensors: the two MPO steps as one sparse channel map (FP64 form) and
+  // the same fused coefficients for the mixed form
+  const bool real = L.dtype == kF64 && W1.dtype == kF64 && W2.dtype == kF64 &&
+                    R.dtype == kF64 && psi0.dtype == kF64;
+  std::unique_ptr<FusedMpo> fm;
+  if (real) {
+    fm = std::make_unique<FusedMpo>(ctx, W1, W2);
+    mv->m64 = plan_mpo_step64(ctx, *fm, *mv->p1->out, *mv->p3->out);
+  }
   if (precision == kPrecMixed) {
-    UDMRG_REQUIRE(psi0.dtype == kF64, "mixed-precision matvec: real tensors only");
-    mv->sg = plan_sg_matvec(ctx, L, W1, W2, R, *mv->sstruct);
+    UDMRG_REQUIRE(real, "mixed-precision matvec: real tensors only");
+    mv->sg = plan_sg_matvec(ctx, L, W1, W2, R, *mv->sstruct, *fm);
   }
   // the FP64 form is kept in both modes (the mixed solver's final Rayleigh quotient)
   const int es = elem_doubles(psi0.dtype);
   mv->t1 = (double *)ctx.alloc(std::max<int64_t>(mv->p1->out->size(), 1) * es * sizeof(double));
-  mv->t2 = (double *)ctx.alloc(std::max<int64_t>(mv->p2->out->size(), 1) * es * sizeof(double));
+  if (!mv->m64)
+    mv->t2 = (double *)ctx.alloc(std::max<int64_t>(mv->p2->out->size(), 1) * es * sizeof(double));
   mv->t3 = (double *)ctx.alloc(std::max<int64_t>(mv->p3->out->size(), 1) * es * sizeof(double));
   return mv;
 }
@@ -167,8 +177,12 @@ void MatvecPlan::apply_fp64(const double *in, double *out) {
   const DType dt = sstruct->dtype;
   const int es = elem_doubles(dt);
   run_gemm(*ctx, p1->gemm, dt, L->data, in, t1, 1.0, 0.0);
-  run_gemm(*ctx, p2->gemm, dt, t1, W1->data, t2, 1.0, 0.0);
-  if (sites == 2) run_gemm(*ctx, p3->gemm, dt, t2, W2->data, t3, 1.0, 0.0);
+  if (m64) {
+    run_mpo_step64(*ctx, *m64, t1, t3);
+  } else {
+    run_gemm(*ctx, p2->gemm, dt, t1, W1->data, t2, 1.0, 0.0);
+    if (sites == 2) run_gemm(*ctx, p3->gemm, dt, t2, W2->data, t3, 1.0, 0.0);
+  }
   for (int64_t b : missing)
     UDMRG_CHECK_CUDA(cudaMemsetAsync(out + sstruct->offs[b] * es, 0,
                                      sstruct->block_elems(b) * es * sizeof(double), ctx->stream));

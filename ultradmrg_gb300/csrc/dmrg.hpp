@@ -1,6 +1,7 @@
 // Two-site update: matvec plan, Lanczos solvers, environment updates, sweeps.
 #pragma once
 
+#include "mpo_step.hpp"
 #include "rank_mlp.hpp"
 #include "sg_matvec.hpp"
 #include "svd.hpp"
@@ -38,6 +39,9 @@ struct MatvecPlan {
   int precision = kPrecFP64;
   int sites = 2;  // 1: single-site form (L, W1, R; p3 unused)
   std::unique_ptr<SgMatvecPlan> sg;  // the mixed-precision form
+  // real two-site FP64 form: the two MPO steps as one sparse channel map
+  // (p2, p3 then only describe the intermediate structures)
+  std::unique_ptr<MpoStep64> m64;
   ~MatvecPlan();
   void apply(const double *in, double *out);       // device buffers in sstruct layout
   void apply_fp64(const double *in, double *out);  // always the plain FP64 form

@@ -9,6 +9,7 @@
 // (FP32), T3 written once (3 x BF16).
 #include <cuda_bf16.h>
 
+#include "mpo_step.hpp"
 #include "sg_matvec.hpp"
 
 namespace udmrg {
@@ -72,7 +73,76 @@ __global__ void mpo_unit_kernel(const int64_t *__restrict__ unit0,
   }
 }
 
+// FP64 form: the same work units; inputs from T1 and outputs to T3 in their
+// block layouts (b contiguous in T1, strided in T3), FP64 accumulation.
+__global__ void mpo_unit64_kernel(const int64_t *__restrict__ unit0,
+                                  const int32_t *__restrict__ unit_pair, int64_t nunits,
+                                  const MpoPair64 *__restrict__ pairs,
+                                  const MpoIn64 *__restrict__ ins,
+                                  const MpoOut64 *__restrict__ outs,
+                                  const int32_t *__restrict__ rowptr,
+                                  const MpoNz64 *__restrict__ nz,
+                                  const double *__restrict__ t1, double *__restrict__ t3,
+                                  int slice) {
+  extern __shared__ double sm64[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarp = blockDim.x >> 5;
+  double *X = sm64 + (int64_t)warp * slice;  // slice = max input channels x 32
+  for (int64_t u = (int64_t)blockIdx.x * nwarp + warp; u < nunits;
+       u += (int64_t)gridDim.x * nwarp) {
+    const int lo = __ldg(unit_pair + u);
+    const MpoPair64 pr = pairs[lo];
+    const int nbt = (pr.db + 31) >> 5;
+    const int64_t local = u - __ldg(unit0 + lo);
+    const int a = (int)(local / nbt);
+    const int b = (int)(local - (int64_t)a * nbt) * 32 + lane;
+    const bool col = b < pr.db;
+    for (int i = 0; i < pr.nin; ++i) {
+      const MpoIn64 in = ins[pr.in0 + i];
+      X[(i << 5) + lane] = col ? __ldg(t1 + in.base + (int64_t)a * in.astride + b) : 0.0;
+    }
+    __syncwarp();
+    for (int o = 0; o < pr.nout; ++o) {
+      const int k0 = __ldg(rowptr + pr.row0 + o), k1 = __ldg(rowptr + pr.row0 + o + 1);
+      double acc = 0.0;
+      for (int k = k0; k < k1; ++k) {
+        const MpoNz64 e = nz[k];
+        acc = fma(e.v, X[(e.i << 5) + lane], acc);
+      }
+      if (col) {
+        const MpoOut64 ot = outs[pr.out0 + o];
+        t3[ot.base + (int64_t)a * ot.astride + (int64_t)b * ot.bstride] = acc;
+      }
+    }
+    __syncwarp();  // X is rewritten by the next unit
+  }
+}
+
 }  // namespace
+
+void run_mpo_step64(Ctx &ctx, const MpoStep64 &p, const double *t1, double *t3) {
+  if (p.pairs.empty()) return;
+  const int64_t nunits = p.unit0.back();
+  if (nunits == 0) return;
+  const int slice = std::max(1, p.max_nin) * 32;
+  const size_t per_warp = (size_t)slice * sizeof(double);
+  UDMRG_REQUIRE(per_warp <= 200 * 1024, "MPO step: too many input channels in a pair");
+  const int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (96 * 1024) / per_warp));
+  const size_t smem = per_warp * warps;
+  static size_t attr = 0;
+  if (smem > 48 * 1024 && smem > attr) {
+    UDMRG_CHECK_CUDA(cudaFuncSetAttribute(mpo_unit64_kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = smem;
+  }
+  const int64_t blocks = (nunits + warps - 1) / warps;
+  const int grid = (int)std::min<int64_t>(blocks, 16 * (int64_t)ctx.num_sms);
+  mpo_unit64_kernel<<<grid, 32 * warps, smem, ctx.stream>>>(
+      p.d_unit0, p.d_unit_pair, nunits, p.d_pairs, p.d_ins, p.d_outs, p.d_rowptr, p.d_nz, t1, t3,
+      slice);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  ctx.launches++;
+}
 
 void run_mpo_step(Ctx &ctx, const SgMatvecPlan &p) {
   const int npairs = (int)p.pairs.size();

@@ -25,15 +25,6 @@ V *upload_vec(Ctx &ctx, const std::vector<V> &v) {
   return d;
 }
 
-std::vector<double> download(Ctx &ctx, const BTensor &t) {
-  std::vector<double> h(t.size());
-  if (t.size())
-    UDMRG_CHECK_CUDA(cudaMemcpyAsync(h.data(), t.data, t.size() * sizeof(double),
-                                     cudaMemcpyDeviceToHost, ctx.stream));
-  ctx.sync();
-  return h;
-}
-
 using Key = std::vector<int32_t>;
 
 struct T1Block {
@@ -46,7 +37,7 @@ struct T1Block {
 
 std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const BTensor &W1,
                                              const BTensor &W2, const BTensor &R,
-                                             const BTensor &S) {
+                                             const BTensor &S, FusedMpo &fm) {
   UDMRG_REQUIRE(L.dtype == kF64 && W1.dtype == kF64 && W2.dtype == kF64 && R.dtype == kF64 &&
                     S.dtype == kF64,
                 "mixed matvec: real FP64 tensors required");
@@ -145,21 +136,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   for (int64_t b = 0; b < S.nblocks(); ++b) orows[S.key(b)[3]].push_back(b);
   std::vector<PackOp> rops;
   int64_t t3bytes = 0, rbytes = 0;
-  // host copies of the MPO tensors for the fused coefficients
-  const std::vector<double> w1h = download(ctx, W1), w2h = download(ctx, W2);
-  // W1 blocks by (s1_out); W2 blocks by (wr, s2_out, w2)
-  std::map<int32_t, std::vector<int64_t>> w1_by_s1o;
-  for (int64_t b = 0; b < W1.nblocks(); ++b) w1_by_s1o[W1.key(b)[2]].push_back(b);
   std::vector<std::pair<int32_t, int32_t>> tgt_key;  // (A', B) of every target
-  std::map<std::array<int32_t, 3>, std::vector<int64_t>> w2_by;  // (wr, s2out, w2)
-  // fused W1 W2 coefficients per (s1', s2', w2): the contributing (W, S1, S2)
-  struct CoefEntry {
-    std::array<int32_t, 3> src;  // (W, S1, S2)
-    std::vector<double> coef;    // nin x nout
-  };
-  std::map<std::array<int32_t, 3>, std::vector<CoefEntry>> coef_cache;
-  for (int64_t b = 0; b < W2.nblocks(); ++b)
-    w2_by[{W2.key(b)[0], W2.key(b)[2], W2.key(b)[3]}].push_back(b);
   for (int Bp = 0; Bp < nB; ++Bp) {
     if (orows[Bp].empty()) continue;
     const int64_t dBp = R.idx[0].dims[Bp];
@@ -219,53 +196,8 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
         tg.nout = tg.ds12p * dw2;
         tg.src0 = (int32_t)p->sources.size();
         // sources: T1 blocks (A', W, S1, S2, B) through W1 (W,S1,S1p,Wr) W2 (Wr,S2,S2p,W2s);
-        // the fused coefficients depend on the MPO sectors only and are cached
-        const std::array<int32_t, 3> ck = {S1p, S2p, W2s};
-        auto cit = coef_cache.find(ck);
-        if (cit == coef_cache.end()) {
-          std::map<std::array<int32_t, 3>, std::vector<double>> acc;  // (W, S1, S2) -> coef
-          auto it1 = w1_by_s1o.find(S1p);
-          if (it1 != w1_by_s1o.end()) {
-            for (int64_t b1 : it1->second) {
-              const int32_t Ws = W1.key(b1)[0], S1 = W1.key(b1)[1], Wr = W1.key(b1)[3];
-              auto it2 = w2_by.find({Wr, S2p, W2s});
-              if (it2 == w2_by.end()) continue;
-              for (int64_t b2 : it2->second) {
-                const int32_t S2 = W2.key(b2)[1];
-                const int64_t dw = W1.idx[0].dims[Ws], ds1 = W1.idx[1].dims[S1];
-                const int64_t dwr = W1.idx[3].dims[Wr], ds2 = W2.idx[1].dims[S2];
-                const int64_t nin = dw * ds1 * ds2;
-                auto &c = acc[{Ws, S1, S2}];
-                if (c.empty()) c.assign(nin * tg.nout, 0.0);
-                // W1(w, s1, s1', wr) W2(wr, s2, s2', w2), blocks row-major
-                const double *w1 = w1h.data() + W1.offs[b1];
-                const double *w2 = w2h.data() + W2.offs[b2];
-                for (int64_t w = 0; w < dw; ++w)
-                  for (int64_t s1 = 0; s1 < ds1; ++s1)
-                    for (int64_t s2 = 0; s2 < ds2; ++s2)
-                      for (int64_t s1o = 0; s1o < ds1p; ++s1o)
-                        for (int64_t s2o = 0; s2o < ds2p; ++s2o)
-                          for (int64_t w2i = 0; w2i < dw2; ++w2i) {
-                            double v = 0;
-                            for (int64_t wr = 0; wr < dwr; ++wr)
-                              v += w1[((w * ds1 + s1) * ds1p + s1o) * dwr + wr] *
-                                   w2[((wr * ds2 + s2) * ds2p + s2o) * dw2 + w2i];
-                            const int64_t ic = (w * ds1 + s1) * ds2 + s2;
-                            const int64_t oc = (s1o * ds2p + s2o) * dw2 + w2i;
-                            c[ic * tg.nout + oc] += v;
-                          }
-              }
-            }
-          }
-          std::vector<CoefEntry> entries;
-          for (auto &kv : acc) {
-            bool nz = false;
-            for (double v : kv.second) nz |= (v != 0.0);
-            if (nz) entries.push_back({kv.first, std::move(kv.second)});
-          }
-          cit = coef_cache.emplace(ck, std::move(entries)).first;
-        }
-        for (const CoefEntry &ce : cit->second) {
+        // the fused coefficients depend on the MPO sectors only (cached in fm)
+        for (const FusedMpo::Entry &ce : fm.get(S1p, S2p, W2s)) {
           auto tb = t1map.find(Key{Ap, ce.src[0], ce.src[1], ce.src[2], Bs});
           if (tb == t1map.end()) continue;
           MpoSource s{};
