@@ -27,7 +27,6 @@ namespace udmrg {
 namespace {
 
 constexpr int kTriThreads = 512;
-constexpr int kBisectThreads = 32;
 constexpr int kBackThreads = 256;
 
 __device__ double block_sum(double v, double *red) {
@@ -191,58 +190,75 @@ __device__ __forceinline__ int sturm_count(const double *d, const double *e, int
   return cnt;
 }
 
-// All eigenvalues by bisection; lam[lam_off + i] (descending) = scale * value.
-// Block b handles the eigenvalues i0 .. i0 + blockDim.x - 1 (ascending index)
-// of job chunk[b].x, i0 = chunk[b].y, one per thread, so a large matrix is
-// spread over many SMs.
-__global__ void bisect_kernel(const EigJob *__restrict__ jobs, const int2 *__restrict__ chunk,
-                              const double *__restrict__ d_all, const double *__restrict__ e_all,
-                              const double *__restrict__ scale_all, double *__restrict__ lam_all) {
+// Eigenvalues by multisection; lam[lam_off + i] (descending) = scale * value.
+// A warp handles kBisectEigs eigenvalues of one job, kBisectLanes lanes each:
+// per step the lanes of an eigenvalue take Sturm counts at the kBisectLanes
+// interior points that cut its interval into kBisectLanes + 1 equal parts,
+// and the part holding the eigenvalue is kept (the division chain of a Sturm
+// count is serial, so points side by side shorten the chain of steps).
+// Block b handles eigenvalues i0 .. i0 + kBisectEigs - 1 (ascending index) of
+// job chunk[b].x, i0 = chunk[b].y.
+constexpr int kBisectLanes = 8;
+constexpr int kBisectEigs = 32 / kBisectLanes;
+__global__ void __launch_bounds__(32)
+    bisect_kernel(const EigJob *__restrict__ jobs, const int2 *__restrict__ chunk,
+                  const double *__restrict__ d_all, const double *__restrict__ e_all,
+                  const double *__restrict__ scale_all, double *__restrict__ lam_all) {
   extern __shared__ double sm[];
   const int jb = chunk[blockIdx.x].x, i0 = chunk[blockIdx.x].y;
   const EigJob job = jobs[jb];
   const int n = job.n;
   if (n == 0) return;
+  const int lane = threadIdx.x, grp = lane / kBisectLanes, k = lane % kBisectLanes;
   double *d = sm, *e = sm + n;
-  __shared__ double lo0, hi0, emax;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int i = lane; i < n; i += 32) {
     d[i] = d_all[job.lam_off + i];
     e[i] = i + 1 < n ? e_all[job.lam_off + i] : 0.0;
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {  // Gershgorin interval
-    double lo = d[0], hi = d[0], em = 0.0;
-    for (int i = 0; i < n; ++i) {
-      const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
-      lo = fmin(lo, d[i] - r);
-      hi = fmax(hi, d[i] + r);
-      if (i + 1 < n) em = fmax(em, fabs(e[i]));
-    }
-    const double pad = 2.2e-16 * fmax(fabs(lo), fabs(hi)) * n + 1e-300;
-    lo0 = lo - pad;
-    hi0 = hi + pad;
-    emax = em;
+  __syncwarp();
+  // Gershgorin interval and the largest off-diagonal (warp reduction)
+  double glo = 1e308, ghi = -1e308, em = 0.0;
+  for (int i = lane; i < n; i += 32) {
+    const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
+    glo = fmin(glo, d[i] - r);
+    ghi = fmax(ghi, d[i] + r);
+    if (i + 1 < n) em = fmax(em, fabs(e[i]));
   }
-  __syncthreads();
-  const double pivmin = 1e-290 * fmax(1.0, emax * emax);
+  for (int o = 16; o > 0; o >>= 1) {
+    glo = fmin(glo, __shfl_xor_sync(0xffffffffu, glo, o));
+    ghi = fmax(ghi, __shfl_xor_sync(0xffffffffu, ghi, o));
+    em = fmax(em, __shfl_xor_sync(0xffffffffu, em, o));
+  }
+  const double pad = 2.2e-16 * fmax(fabs(glo), fabs(ghi)) * n + 1e-300;
+  const double lo0 = glo - pad, hi0 = ghi + pad;
+  const double pivmin = 1e-290 * fmax(1.0, em * em);
   const double scale = scale_all[jb];
   // absolute accuracy far below the eps * |T| the reduction itself achieves
   const double atol = 1e-18 * fmax(fabs(lo0), fabs(hi0));
-  {
-    const int i = i0 + threadIdx.x;  // i-th smallest
-    if (i >= n) return;
-    double lo = lo0, hi = hi0;
-    for (int it = 0; it < 128; ++it) {
-      const double mid = 0.5 * (lo + hi);
-      if (hi - lo <= 4.4e-16 * fmax(fabs(lo), fabs(hi)) + atol || mid <= lo || mid >= hi)
-        break;
-      if (sturm_count(d, e, n, mid, pivmin) > i)
-        hi = mid;
-      else
-        lo = mid;
+  const int i = i0 + grp;  // i-th smallest
+  double lo = lo0, hi = hi0;
+  bool done = i >= n;
+  for (int it = 0; it < 64; ++it) {
+    if (!done && hi - lo <= 4.4e-16 * fmax(fabs(lo), fabs(hi)) + atol) done = true;
+    if (__all_sync(0xffffffffu, done)) break;
+    const double w = (hi - lo) / (kBisectLanes + 1);
+    const double x = lo + w * (k + 1);
+    const bool above = !done && x > lo && x < hi && sturm_count(d, e, n, x, pivmin) > i;
+    const unsigned m = (__ballot_sync(0xffffffffu, above) >> (grp * kBisectLanes)) &
+                       ((1u << kBisectLanes) - 1);
+    if (!done) {
+      // first point with more than i eigenvalues below it bounds eigenvalue i
+      const int f = m ? __ffs(m) - 1 : kBisectLanes;
+      const double nlo = f == 0 ? lo : lo + w * f, nhi = f == kBisectLanes ? hi : lo + w * (f + 1);
+      if (nlo <= lo && nhi >= hi) {
+        done = true;  // no representable point inside the interval
+      } else {
+        lo = nlo;
+        hi = nhi;
+      }
     }
-    lam_all[job.lam_off + (n - 1 - i)] = scale * 0.5 * (lo + hi);
   }
+  if (i < n && k == 0) lam_all[job.lam_off + (n - 1 - i)] = scale * 0.5 * (lo + hi);
 }
 
 // ---- leading eigenvalues only (positive semi-definite jobs) ----
@@ -380,15 +396,19 @@ __global__ void invit_kernel(const EigCluster *__restrict__ cl, int ncl,
       zc[p] = 1.0;
       continue;
     }
-    // LU of T - lam I with row interchanges: row i of U holds u0 (diagonal),
-    // u1, u2 (the two superdiagonals); l the multipliers; pv the interchanges
+    // LU of T - lam I with row interchanges: row i of U holds u0 (the
+    // reciprocal of the diagonal, kept away from zero), u1, u2 (the two
+    // superdiagonals); l the multipliers; pv the interchanges
+    auto rinv = [&](double v) {
+      return 1.0 / (fabs(v) > tiny ? v : (v < 0 ? -tiny : tiny));
+    };
     double a = d[0] - lam, b = e[0];
     for (int i = 0; i + 1 < n; ++i) {
       const double sub = e[i], dn = d[i + 1] - lam, sup = i + 2 < n ? e[i + 1] : 0.0;
       if (fabs(a) >= fabs(sub)) {
         const double piv = a != 0.0 ? a : tiny;
         const double f = sub / piv;
-        at(u0, i) = piv;
+        at(u0, i) = rinv(piv);
         at(u1, i) = b;
         at(u2, i) = 0.0;
         at(l, i) = f;
@@ -397,7 +417,7 @@ __global__ void invit_kernel(const EigCluster *__restrict__ cl, int ncl,
         b = sup;
       } else {
         const double f = a / sub;
-        at(u0, i) = sub;
+        at(u0, i) = rinv(sub);
         at(u1, i) = dn;
         at(u2, i) = sup;
         at(l, i) = f;
@@ -406,7 +426,7 @@ __global__ void invit_kernel(const EigCluster *__restrict__ cl, int ncl,
         b = -f * sup;
       }
     }
-    at(u0, n - 1) = fabs(a) > tiny ? a : (a < 0 ? -tiny : tiny);
+    at(u0, n - 1) = rinv(a);
     for (int i = 0; i < n; ++i) at(y, i) = start_entry(c.seed + 7919ull * (uint64_t)p, i);
     for (int it = 0; it < 3; ++it) {
       // forward: apply the interchanges and multipliers
@@ -424,8 +444,7 @@ __global__ void invit_kernel(const EigCluster *__restrict__ cl, int ncl,
         double s = at(y, i);
         if (i + 1 < n) s -= at(u1, i) * at(y, i + 1);
         if (i + 2 < n) s -= at(u2, i) * at(y, i + 2);
-        const double piv = fabs(at(u0, i)) > tiny ? at(u0, i) : (at(u0, i) < 0 ? -tiny : tiny);
-        at(y, i) = s / piv;
+        at(y, i) = s * at(u0, i);
       }
       // orthogonalise against the cluster's earlier vectors, normalise
       for (int q = c.first; q < p; ++q) {
@@ -1153,13 +1172,13 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
   }
   std::vector<int2> chunks;
   for (int q = 0; q < nj; ++q)
-    for (int i0 = jobs[q].n - (int)wk.computed[q]; i0 < jobs[q].n; i0 += kBisectThreads)
+    for (int i0 = jobs[q].n - (int)wk.computed[q]; i0 < jobs[q].n; i0 += kBisectEigs)
       chunks.push_back(make_int2(q, i0));
   int2 *dch = scratch.get<int2>(chunks.size());
   UDMRG_CHECK_CUDA(cudaMemcpyAsync(dch, chunks.data(), chunks.size() * sizeof(int2),
                                    cudaMemcpyHostToDevice, ctx.stream));
   if (!chunks.empty())
-    bisect_kernel<<<(int)chunks.size(), kBisectThreads, bsmem, ctx.stream>>>(
+    bisect_kernel<<<(int)chunks.size(), 32, bsmem, ctx.stream>>>(
         wk.jobs, dch, wk.d, wk.e, wk.scale, lam);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches += 2;
