@@ -311,6 +311,12 @@ int udmrg_matvec_plan_destroy(udmrg_matvec_plan *p);
  * FP64 stages: the four block contractions. */
 int udmrg_matvec_plan_stage_times(udmrg_matvec_plan *p, const double *d_in, double *d_out,
                                   double *ms, double *flops);
+/* Algorithmic HBM bytes of the mixed form's memory-bound stages (bytes[4],
+ * same order as the stage times): psi pack (FP64 read, three BF16 planes
+ * written per element) and the MPO step (FP32 T1 entries read, three BF16
+ * planes written per T3 entry); 0 for the two tensor-core stages and for
+ * the FP64 form. */
+int udmrg_matvec_plan_stage_bytes(udmrg_matvec_plan *p, double *bytes);
 
 /* ---- measurement ---------------------------------------------------- */
 /* FP64 FMA throughput of the device (TFLOP/s), measured by a DFMA-bound

@@ -611,6 +611,12 @@ class MatvecPlan:
              C.cast(C.c_void_p(d_out), _lib.c_double_p), ms, fl)
         return list(ms), list(fl)
 
+    def stage_bytes(self):
+        """Algorithmic HBM bytes of the mixed form's memory-bound stages."""
+        b = (C.c_double * 4)()
+        call("udmrg_matvec_plan_stage_bytes", self.h, b)
+        return list(b)
+
     def close(self):
         if self.h:
             call("udmrg_matvec_plan_destroy", self.h)

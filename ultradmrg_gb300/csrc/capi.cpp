@@ -882,6 +882,17 @@ int udmrg_ctx_flush_l2(udmrg_ctx *c, int64_t bytes) {
   });
 }
 
+int udmrg_matvec_plan_stage_bytes(udmrg_matvec_plan *p, double *bytes) {
+  return guarded([&] {
+    MatvecPlan &m = *p->plan;
+    for (int i = 0; i < 4; ++i) bytes[i] = 0.0;
+    if (m.sg) {
+      bytes[0] = 14.0 * (double)m.sg->psi_size;  // 8 B read, 3 x 2 B written
+      bytes[2] = m.sg->mpo_bytes;
+    }
+  });
+}
+
 int udmrg_matvec_plan_stage_times(udmrg_matvec_plan *p, const double *d_in, double *d_out,
                                   double *ms, double *flops) {
   return guarded([&] {

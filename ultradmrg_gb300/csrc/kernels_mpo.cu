@@ -46,27 +46,47 @@ __global__ void mpo_unit_kernel(const int64_t *__restrict__ unit0,
       X[(i << 5) + lane] = col ? __ldg(t1 + in.base + (int64_t)a * in.astride + b) : 0.f;
     }
     __syncwarp();
-    for (int o = 0; o < pr.nout; ++o) {
-      const int k0 = __ldg(rowptr + pr.row0 + o), k1 = __ldg(rowptr + pr.row0 + o + 1);
-      float acc = 0.f;
-      for (int k = k0; k < k1; ++k) {
-        const MpoNz e = nz[k];
-        acc = fmaf(e.v, X[(e.i << 5) + lane], acc);
-      }
-      if (col) {
-        const MpoOut ot = outs[pr.out0 + o];
-        const int row = ot.row0 + a * ot.rstride;
-        const int c = ot.col0 + b;
-        const int64_t off = ot.img_off +
-                            ((int64_t)(row / kTcBM) * ot.kc + c / kTcBK) * 3 * plane +
-                            canon(row % kTcBM, c % kTcBK, kTcBM);
-        const __nv_bfloat16 h = __float2bfloat16_rn(acc);
-        const float r1 = acc - __bfloat162float(h);
-        const __nv_bfloat16 m = __float2bfloat16_rn(r1);
-        const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
-        *(__nv_bfloat16 *)(img + off) = h;
-        *(__nv_bfloat16 *)(img + off + plane) = m;
-        *(__nv_bfloat16 *)(img + off + 2 * plane) = l;
+    for (int ob = 0; ob < pr.nout; ob += 32) {
+      // row pointers of outputs ob .. ob + 31 (lane oc holds the end of the last)
+      const int oc = min(32, pr.nout - ob);
+      const int rp = __ldg(rowptr + pr.row0 + ob + min(lane, oc));
+      for (int oo = 0; oo < oc; ++oo) {
+        const int o = ob + oo;
+        const int k0 = __shfl_sync(0xffffffffu, rp, oo), k1 = __shfl_sync(0xffffffffu, rp, oo + 1);
+        float acc = 0.f;
+        // 32 nonzeros per coalesced load, broadcast lane by lane
+        for (int kb = k0; kb < k1; kb += 32) {
+          const int k = kb + lane;
+          int ei = 0;
+          float ev = 0.f;
+          if (k < k1) {
+            const MpoNz e = nz[k];
+            ei = e.i;
+            ev = e.v;
+          }
+          const int cnt = min(32, k1 - kb);
+#pragma unroll 4
+          for (int t = 0; t < cnt; ++t) {
+            const int i = __shfl_sync(0xffffffffu, ei, t);
+            const float v = __shfl_sync(0xffffffffu, ev, t);
+            acc = fmaf(v, X[(i << 5) + lane], acc);
+          }
+        }
+        if (col) {
+          const MpoOut ot = outs[pr.out0 + o];
+          const int row = ot.row0 + a * ot.rstride;
+          const int c = ot.col0 + b;
+          const int64_t off = ot.img_off +
+                              ((int64_t)(row / kTcBM) * ot.kc + c / kTcBK) * 3 * plane +
+                              canon(row % kTcBM, c % kTcBK, kTcBM);
+          const __nv_bfloat16 h = __float2bfloat16_rn(acc);
+          const float r1 = acc - __bfloat162float(h);
+          const __nv_bfloat16 m = __float2bfloat16_rn(r1);
+          const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
+          *(__nv_bfloat16 *)(img + off) = h;
+          *(__nv_bfloat16 *)(img + off + plane) = m;
+          *(__nv_bfloat16 *)(img + off + 2 * plane) = l;
+        }
       }
     }
     __syncwarp();  // X is rewritten by the next unit

@@ -59,11 +59,12 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   struct G1 {
     int A;
     int64_t M, N, K, t1_off, l_off, p_off;
+    int64_t Np;  // T1 row pitch: N rounded up to 4 (16-byte aligned rows)
   };
   std::vector<G1> g1s;
   for (int A = 0; A < nA; ++A) {
     if (lrows[A].empty() || pcols[A].empty()) continue;
-    G1 g{A, 0, 0, L.idx[2].dims[A], t1tot, lbytes, pbytes};
+    G1 g{A, 0, 0, L.idx[2].dims[A], t1tot, lbytes, pbytes, 0};
     std::vector<int64_t> rof, cof;
     for (int64_t b : lrows[A]) {
       rof.push_back(g.M);
@@ -74,6 +75,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       g.N += dim(S, b, 1) * dim(S, b, 2) * dim(S, b, 3);
     }
     UDMRG_REQUIRE(g.M < (1 << 30) && g.N < (1 << 30) && g.K < (1 << 30), "mixed matvec: group too large");
+    g.Np = (g.N + 3) & ~(int64_t)3;
     const int32_t kc = (int32_t)((g.K + kTcBK - 1) / kTcBK);
     for (size_t i = 0; i < lrows[A].size(); ++i) {
       const int64_t b = lrows[A][i];
@@ -113,14 +115,14 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
         const int64_t pb = pcols[A][j];
         Key k = {L.key(lb)[0], L.key(lb)[1], S.key(pb)[1], S.key(pb)[2], S.key(pb)[3]};
         T1Block t;
-        t.origin = g.t1_off + rof[i] * g.N + cof[j];
-        t.pitch = g.N;
+        t.origin = g.t1_off + rof[i] * g.Np + cof[j];
+        t.pitch = g.Np;
         t.dw = (int32_t)dim(L, lb, 1);
         t.ds12 = (int32_t)(dim(S, pb, 1) * dim(S, pb, 2));
         t1map[k] = t;
       }
     }
-    t1tot += g.M * g.N;
+    t1tot += g.M * g.Np;
     lbytes += tc_image_bytes(g.M, g.K, kTcBM);
     pbytes += tc_image_bytes(g.N, g.K, kTcBN);
     g1s.push_back(g);
@@ -239,7 +241,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   p->d_psi_ops = upload_pack_ops(ctx, p->psi_ops);
   for (auto &g : g1s) {
     std::vector<int64_t> rows(g.M);
-    for (int64_t m = 0; m < g.M; ++m) rows[m] = g.t1_off + m * g.N;
+    for (int64_t m = 0; m < g.M; ++m) rows[m] = g.t1_off + m * g.Np;
     p->g1.add_group(g.l_off, g.p_off, (int32_t)g.M, (int32_t)g.N, (int32_t)g.K, rows);
   }
   p->g1.finalize();
@@ -306,6 +308,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       }
       p->max_nin = std::max(p->max_nin, (int)pr.nin);
       p->max_nout = std::max(p->max_nout, (int)pr.nout);
+      p->mpo_bytes += (double)pr.da * pr.db * (4.0 * pr.nin + 6.0 * pr.nout);
       // work units: one per (a', 32-wide tile of b); prefix over the pairs and
       // the pair of every unit
       if (p->unit0.empty()) p->unit0.push_back(0);

@@ -11,7 +11,8 @@
 //   step 3 (tcgen05): for every bra sector B' of R, one dense GEMM
 //          res_B'[(a',s1',s2') x b'] = T3_B'[(a',s1',s2') x (w2,b)] . R_B'[b' x (w2,b)]^T.
 // L_A and R_B' images are packed once per plan (the environments are fixed
-// during a Lanczos solve); psi is packed every matvec.  T1 is FP32.
+// during a Lanczos solve); psi is packed every matvec.  T1 is FP32, its rows
+// padded to a multiple of four entries (16-byte aligned epilogue stores).
 #pragma once
 
 #include "gemm.hpp"
@@ -101,6 +102,7 @@ struct SgMatvecPlan {
   int32_t *d_unit_pair = nullptr;
   int max_nin = 0, max_nout = 0;
   double mixed_flops = 0;  // tensor-core work actually issued (2MNK per group, x6 products)
+  double mpo_bytes = 0;    // MPO step: 4 B per T1 entry read, 3 x 2 B per T3 entry written
   ~SgMatvecPlan();
   void apply(const double *psi_in, double *out);
   // apply with CUDA events between the stages: ms[0] psi pack, ms[1] GEMM

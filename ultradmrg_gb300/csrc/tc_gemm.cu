@@ -310,15 +310,36 @@ __global__ void __launch_bounds__(kThreads, 1)
         tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + acc * kTcBN + cb * 16, r);
         tc::tmem_wait_ld();
         if (row_ok) {
+          // 16-byte stores where the row position allows (four FP32 or two
+          // FP64 values per store; a lane writes one row)
+          const int nc = n0 + cb * 16;
+          float v[16];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int n = n0 + cb * 16 + j;
-            if (n < g.N) {
-              const float v = g.kc > 0 ? af * __uint_as_float(r[j]) : 0.0f;
-              if (out_kind == kTcOutF64)
-                ((double *)out)[base + n] = widen_f32(v);
-              else
-                ((float *)out)[base + n] = v;
+          for (int j = 0; j < 16; ++j) v[j] = g.kc > 0 ? af * __uint_as_float(r[j]) : 0.0f;
+          if (out_kind == kTcOutF64) {
+            double *o = (double *)out + base + nc;
+            const bool vec = (((base + nc) & 1) == 0);
+#pragma unroll
+            for (int j = 0; j < 16; j += 2) {
+              if (vec && nc + j + 1 < g.N) {
+                *(double2 *)(o + j) = make_double2(widen_f32(v[j]), widen_f32(v[j + 1]));
+              } else {
+                if (nc + j < g.N) o[j] = widen_f32(v[j]);
+                if (nc + j + 1 < g.N) o[j + 1] = widen_f32(v[j + 1]);
+              }
+            }
+          } else {
+            float *o = (float *)out + base + nc;
+            const bool vec = (((base + nc) & 3) == 0);
+#pragma unroll
+            for (int j = 0; j < 16; j += 4) {
+              if (vec && nc + j + 3 < g.N) {
+                *(float4 *)(o + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+              } else {
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                  if (nc + j + t < g.N) o[j + t] = v[j + t];
+              }
             }
           }
         }
