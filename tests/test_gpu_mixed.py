@@ -116,3 +116,26 @@ def test_mixed_vmps_heisenberg16_vs_fp64(ctx):
     rel = abs(e_mixed - e_fp64) / abs(e_fp64)
     print(f"L=16 D=32 sweep: |dE/E| mixed vs FP64 = {rel:.2e}")
     assert rel <= 1e-9
+
+
+@pytest.mark.parametrize("workload", ["hubbard4x8_D256"])
+def test_mixed_matvec_workload(ctx, workload):
+    """The benchmark's synthetic Hubbard workload, whose sector pairs carry
+    more than 32 MPO output channels (several channel chunks per warp):
+    mixed against the device FP64 form, element-wise 2e-5 of the largest
+    element."""
+    from ultradmrg_gb300.workloads import WORKLOADS, build_host
+    w = WORKLOADS[workload]
+    mpo, mps = build_host(w)
+    l = w.centre
+    L, R = api.build_envs(ctx, mpo, mps, l, normalize=False)
+    psi = api.contract(ctx, up(ctx, mps[l]), up(ctx, mps[l + 1]), [2], [0])
+    eh = [L, up(ctx, mpo[l]), up(ctx, mpo[l + 1]), R]
+    pm = api.MatvecPlan(ctx, eh, psi, precision=MIXED)
+    p64 = api.MatvecPlan(ctx, eh, psi, precision=api.PREC_FP64)
+    x, ym, yd = pm.embed(psi), pm.embed(psi), pm.embed(psi)
+    pm.apply(x, ym)
+    p64.apply(x, yd)
+    a, b = ym.download_packed(), yd.download_packed()
+    assert np.max(np.abs(a - b)) <= 2e-5 * np.max(np.abs(b))
+    assert np.linalg.norm(a - b) <= 2e-5 * np.linalg.norm(b)

@@ -47,12 +47,16 @@ __global__ void mpo_unit_kernel(const int64_t *__restrict__ unit0,
     }
     __syncwarp();
     for (int ob = 0; ob < pr.nout; ob += 32) {
-      // row pointers of outputs ob .. ob + 31 (lane oc holds the end of the last)
+      // row pointers of outputs ob .. ob + oc - 1 (lane oo holds output oo's
+      // start) and the end pointer of the last one
       const int oc = min(32, pr.nout - ob);
       const int rp = __ldg(rowptr + pr.row0 + ob + min(lane, oc));
+      const int rend = __ldg(rowptr + pr.row0 + ob + oc);
       for (int oo = 0; oo < oc; ++oo) {
         const int o = ob + oo;
-        const int k0 = __shfl_sync(0xffffffffu, rp, oo), k1 = __shfl_sync(0xffffffffu, rp, oo + 1);
+        const int k0 = __shfl_sync(0xffffffffu, rp, oo);
+        const int k1n = __shfl_sync(0xffffffffu, rp, (oo + 1) & 31);
+        const int k1 = oo + 1 < oc ? k1n : rend;
         float acc = 0.f;
         // 32 nonzeros per coalesced load, broadcast lane by lane
         for (int kb = k0; kb < k1; kb += 32) {
