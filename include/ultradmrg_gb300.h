@@ -222,7 +222,10 @@ int udmrg_finite_dmrg(udmrg_ctx *ctx, int64_t N, udmrg_tensor **mps,
 /* TDVPEvolveParams (algorithm/tdvp/tdvp_evolve_params.h:20-85), the part the
  * time evolution itself uses: time step tau, number of steps (sweeps), bond
  * dimension bounds, truncation error and Krylov parameters.  The operator
- * insertion and the measurements of TwoSiteFiniteTDVP are the caller's. */
+ * insertion and the measurements of TwoSiteFiniteTDVP are the caller's.
+ * lancz_params.matvec_precision selects the two-site Krylov matvec (mixed:
+ * the split-BF16 form through its real embedding of the complex data; the
+ * MPO's coefficients must be real); the single-site backward steps are FP64. */
 typedef struct {
   double tau;
   int64_t steps;

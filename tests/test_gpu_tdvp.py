@@ -19,7 +19,7 @@ from oracle import tdvp as otdvp
 from oracle.krylov import LanczosParams
 from systems import (act_operator, apply_dense, canonical_system, free_fermion_green,
                      max_block_diff, mps_dense, op_tensor, two_site_problem)
-from ultradmrg_gb300 import api, models as M
+from ultradmrg_gb300 import _lib, api, models as M
 
 pytestmark = pytest.mark.gpu
 
@@ -159,3 +159,67 @@ def test_tdvp_free_fermion_dynamics(ctx):
             worst = max(worst, d)
             assert d <= 1e-10, (step, x2, d)
     print(f"max |G - G_exact| over {steps} steps: {worst:.2e}")
+
+
+# ---- complex mixed precision (real embedding of the split-BF16 pipeline) ----
+
+@pytest.mark.parametrize("kind,l", [("heis", 4), ("hub", 2)])
+def test_complex_mixed_matvec_parity(ctx, kind, l):
+    """Complex L, R, psi with a (promoted) real MPO: element-wise 2e-5 of the
+    largest element against the oracle, as the real mixed form."""
+    mpo, mps = _complex_system(kind, l, 3)
+    eff, psi = two_site_problem(mpo, mps, l)
+    ref = krylov.eff_ham_mul_two_site_state(eff, psi)
+    dev = [up(ctx, t) for t in eff]
+    dpsi = up(ctx, psi)
+    plan = api.MatvecPlan(ctx, dev, dpsi, precision=api.PREC_MIXED)
+    x, y = plan.embed(dpsi), plan.embed(dpsi)
+    plan.apply(x, y)
+    d, s = max_block_diff(y.to_data(), ref)
+    assert d <= 2e-5 * s, (d, s)
+
+
+def test_complex_mixed_rejects_complex_mpo(ctx):
+    """MPO tensors with nonzero imaginary parts are refused by the mixed form
+    (its fused coefficients are real); the FP64 form takes them."""
+    mpo, mps = _complex_system("heis", 4, 3)
+    mpo = [bs.scale(w, 1.0 + 0.5j) for w in mpo]
+    eff, psi = two_site_problem(mpo, mps, 4)
+    dev = [up(ctx, t) for t in eff]
+    with pytest.raises(_lib.UdmrgError):
+        api.MatvecPlan(ctx, dev, up(ctx, psi), precision=api.PREC_MIXED)
+    api.MatvecPlan(ctx, dev, up(ctx, psi), precision=api.PREC_FP64).close()
+
+
+def test_mixed_expmv(ctx):
+    """exp(-i dt H) psi with the mixed two-site matvec against the oracle."""
+    mpo, mps = _complex_system("heis", 4, 7)
+    eff, psi = two_site_problem(mpo, mps, 4)
+    step = 0.05
+    ref = krylov.lanczos_expmv_solver(eff, psi.copy(), krylov.eff_ham_mul_two_site_state, step,
+                                      LanczosParams(1e-12, 30))
+    it, out = api.lanczos_expmv_solver(ctx, [up(ctx, t) for t in eff], up(ctx, psi), step,
+                                       1e-12, 30, precision=api.PREC_MIXED)
+    d, scale = max_block_diff(out.to_data(), ref.expmv)
+    print(f"mixed expmv: iters {it}, max diff {d / scale:.2e} of the largest element")
+    assert d <= 1e-5 * scale
+
+
+def test_mixed_tdvp_vs_fp64(ctx):
+    """Two TDVP sweeps of a complex Heisenberg chain with the mixed two-site
+    matvec against the FP64 form on the device: state and energy."""
+    N = 8
+    mpo, pb = M.heisenberg_chain_mpo(N, dtype=np.complex128)
+    mps = M.random_mps([pb] * N, (0,), 12, seed=4, dtype=np.complex128)
+    dmpo = [up(ctx, t) for t in mpo]
+    out = {}
+    for prec in (api.PREC_FP64, api.PREC_MIXED):
+        dmps = [up(ctx, t) for t in mps]
+        api.two_site_finite_tdvp(ctx, dmps, dmpo,
+                                 api.TDVPEvolveParams(0.05, 2, 4, 12, 1e-9, 1e-12, 30,
+                                                      precision=prec))
+        out[prec] = mps_dense([t.to_data() for t in dmps])
+    a, b = out[api.PREC_MIXED], out[api.PREC_FP64]
+    err = np.linalg.norm(a - b) / np.linalg.norm(b)
+    print(f"mixed TDVP vs FP64: relative state difference {err:.2e}")
+    assert err <= 1e-5

@@ -260,8 +260,9 @@ def eff_ham_mul_single_site_state(ctx, eff_ham: Sequence[DeviceTensor], state: D
     return _new(ctx, h)
 
 
-def lanczos_expmv_solver(ctx, eff_ham, init_state, step, error=1e-10, max_iterations=20):
-    p = _lib.LanczosParams(error, max_iterations, PREC_FP64)
+def lanczos_expmv_solver(ctx, eff_ham, init_state, step, error=1e-10, max_iterations=20,
+                         precision=PREC_FP64):
+    p = _lib.LanczosParams(error, max_iterations, precision)
     it = C.c_int64()
     h = C.c_void_p()
     call("udmrg_lanczos_expmv_solver", ctx.h, _handles(eff_ham), init_state.h, step, C.byref(p),
@@ -502,6 +503,7 @@ class TDVPEvolveParams:
     trunc_err: float
     lanczos_error: float = 1e-10
     lanczos_max_iterations: int = 20
+    precision: int = 0  # two-site Krylov matvec: 0 FP64, 1 mixed (split-BF16 tensor cores)
 
 
 def two_site_finite_tdvp(ctx, mps: List[DeviceTensor], mpo: List[DeviceTensor],
@@ -512,7 +514,7 @@ def two_site_finite_tdvp(ctx, mps: List[DeviceTensor], mpo: List[DeviceTensor],
     N = len(mps)
     tp = _lib.TdvpParams(params.tau, params.steps, params.Dmin, params.Dmax, params.trunc_err,
                          _lib.LanczosParams(params.lanczos_error, params.lanczos_max_iterations,
-                                            0))
+                                            params.precision))
     cap = max(1, params.steps) * (4 * N)
     log = (_lib.TdvpLog * cap)()
     nlog = C.c_int64()

@@ -351,9 +351,12 @@ int udmrg_lanczos_expmv_solver(udmrg_ctx *c, udmrg_tensor *const *eff_ham,
     EffHam e;
     const bool one = psi->rank() == 3;  // single-site form: eff_ham = {L, W, R}
     prepare_eff_ham(ctx, eff_ham, kC128, e, one ? 3 : 4);
+    UDMRG_REQUIRE(!one || params->matvec_precision == kPrecFP64,
+                  "expmv: the single-site form is FP64 only");
     auto mv = one ? plan_matvec1(ctx, *e.op[0], *e.op[1], *e.op[2], *psi)
-                  : plan_matvec2(ctx, *e.op[0], *e.op[1], *e.op[2], *e.op[3], *psi);
-    LanczosParams p{params->error, params->max_iterations};
+                  : plan_matvec2(ctx, *e.op[0], *e.op[1], *e.op[2], *e.op[3], *psi,
+                                 (int)params->matvec_precision);
+    LanczosParams p{params->error, params->max_iterations, (int)params->matvec_precision};
     auto r = lanczos_expmv(ctx, *mv, *psi, step, p);
     if (iters) *iters = r.iters;
     *out = wrap(std::move(r.expmv));
@@ -712,7 +715,8 @@ int udmrg_two_site_finite_tdvp(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
     p.Dmin = params->Dmin;
     p.Dmax = params->Dmax;
     p.trunc_err = params->trunc_err;
-    p.lancz = {params->lancz_params.error, params->lancz_params.max_iterations, kPrecFP64};
+    p.lancz = {params->lancz_params.error, params->lancz_params.max_iterations,
+               (int)params->lancz_params.matvec_precision};
     std::vector<TdvpLog> lg;
     two_site_finite_tdvp(c->ctx, m, w, p, params->steps, &lg);
     c->ctx.sync();
@@ -887,7 +891,8 @@ int udmrg_matvec_plan_stage_bytes(udmrg_matvec_plan *p, double *bytes) {
     MatvecPlan &m = *p->plan;
     for (int i = 0; i < 4; ++i) bytes[i] = 0.0;
     if (m.sg) {
-      bytes[0] = 14.0 * (double)m.sg->psi_size;  // 8 B read, 3 x 2 B written
+      // 8 B read, 3 x 2 B written per real number
+      bytes[0] = 14.0 * (double)m.sg->psi_size * (m.sg->cplx ? 2 : 1);
       bytes[2] = m.sg->mpo_bytes;
     }
   });

@@ -120,8 +120,8 @@ std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTens
     fm = std::make_unique<FusedMpo>(ctx, W1, W2);
     mv->m64 = plan_mpo_step64(ctx, *fm, *mv->p1->out, *mv->p3->out);
   }
-  if (precision == kPrecMixed) {
-    UDMRG_REQUIRE(real, "mixed-precision matvec: real tensors only");
+  if (precision == kPrecMixed) {  // complex data through the real embedding
+    if (!fm) fm = std::make_unique<FusedMpo>(ctx, W1, W2);
     mv->sg = plan_sg_matvec(ctx, L, W1, W2, R, *mv->sstruct, *fm);
   }
   // the FP64 form is kept in both modes (the mixed solver's final Rayleigh quotient)
@@ -531,6 +531,7 @@ ExpmvResult lanczos_expmv(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state, d
     mv.apply(in, out);
     return out;
   };
+  const bool mixed = mv.sg != nullptr;
   KrylovWork kw(ctx, n, true);
   kw.push(0, bases.v[0]);
   double *last = matvec(bases.v[0]);
@@ -541,6 +542,10 @@ ExpmvResult lanczos_expmv(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state, d
   while (true) {
     double *gamma = last;
     krylov_update(kw, (int)m, gamma);
+    if (mixed) {  // as in lanczos_gs: FP64 Gram-Schmidt against the basis
+      krylov_project(kw, (int)m, gamma, false);
+      krylov_project(kw, (int)m, gamma, true);
+    }
     krylov_fetch(kw, (int)m);
     a[m] = kw.hres[0];
     const double n2 = kw.hres[1];
@@ -927,7 +932,8 @@ void tdvp_two_site(Ctx &ctx, std::vector<TensorPtr> &mps, std::vector<TensorPtr>
   }
   const double t0 = now();
   auto init = contract_axes(ctx, *mps[l], *mps[r], {2}, {0});
-  auto mv = plan_matvec2(ctx, *lenvs[lenv_len], *W[l], *W[r], *renvs[renv_len], *init);
+  auto mv = plan_matvec2(ctx, *lenvs[lenv_len], *W[l], *W[r], *renvs[renv_len], *init,
+                         p.lancz.precision);
   auto ex = lanczos_expmv(ctx, *mv, *init, step, p.lancz);
   mv.reset();
   init.reset();

@@ -6,13 +6,24 @@ namespace udmrg {
 
 namespace {
 
+// Host copy of a real tensor, or the real parts of a complex one whose
+// imaginary parts are all zero (an MPO made complex by promotion).
 std::vector<double> download_data(Ctx &ctx, const BTensor &t) {
-  std::vector<double> h(t.size());
+  const int es = elem_doubles(t.dtype);
+  std::vector<double> h(t.size() * es);
   if (t.size())
-    UDMRG_CHECK_CUDA(cudaMemcpyAsync(h.data(), t.data, t.size() * sizeof(double),
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(h.data(), t.data, h.size() * sizeof(double),
                                      cudaMemcpyDeviceToHost, ctx.stream));
   ctx.sync();
-  return h;
+  if (es == 1) return h;
+  std::vector<double> r(t.size());
+  for (int64_t i = 0; i < t.size(); ++i) {
+    if (h[2 * i + 1] != 0.0)
+      throw Error(kErrInvalid,
+                  "mixed-precision matvec: MPO with complex coefficients (use the FP64 form)");
+    r[i] = h[2 * i];
+  }
+  return r;
 }
 
 template <typename V>
@@ -27,7 +38,6 @@ V *upload(Ctx &ctx, const std::vector<V> &v) {
 }  // namespace
 
 FusedMpo::FusedMpo(Ctx &ctx, const BTensor &w1, const BTensor &w2) : W1(w1), W2(w2) {
-  UDMRG_REQUIRE(W1.dtype == kF64 && W2.dtype == kF64, "fused MPO: real tensors required");
   w1h = download_data(ctx, W1);
   w2h = download_data(ctx, W2);
   for (int64_t b = 0; b < W1.nblocks(); ++b) w1_by_s1o[W1.key(b)[2]].push_back(b);

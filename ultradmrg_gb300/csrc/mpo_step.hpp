@@ -22,7 +22,8 @@ namespace udmrg {
 // output sector triple (S1', S2', W2): the contributing input sectors
 // (W, S1, S2) with their dense coefficient matrices coef[ic * nout + oc],
 // ic = (w ds1 + s1) ds2 + s2, oc = (s1' ds2' + s2') dw2 + w2.  Host side;
-// zero matrices are dropped.
+// zero matrices are dropped.  Complex MPO tensors are accepted when every
+// imaginary part is zero (an MPO promoted to complex with its state).
 struct FusedMpo {
   struct Entry {
     std::array<int32_t, 3> src;  // (W, S1, S2)

@@ -29,6 +29,7 @@ using Key = std::vector<int32_t>;
 
 struct T1Block {
   int64_t origin;  // element offset of (a'=0, w=0, s1=s2=0, b=0)
+  int64_t im;      // offset of the imaginary half (complex data)
   int64_t pitch;
   int32_t dw, ds12;
 };
@@ -38,14 +39,37 @@ struct T1Block {
 std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const BTensor &W1,
                                              const BTensor &W2, const BTensor &R,
                                              const BTensor &S, FusedMpo &fm) {
-  UDMRG_REQUIRE(L.dtype == kF64 && W1.dtype == kF64 && W2.dtype == kF64 && R.dtype == kF64 &&
-                    S.dtype == kF64,
-                "mixed matvec: real FP64 tensors required");
+  // complex L, R, psi: the real embedding [[Re, -Im], [Im, Re]] (the MPO
+  // coefficients are real, see FusedMpo)
+  const bool cplx = S.dtype == kC128;
+  UDMRG_REQUIRE(L.dtype == S.dtype && R.dtype == S.dtype,
+                "mixed matvec: L, R and psi must share the element type");
+  const int64_t es = cplx ? 2 : 1;  // doubles per element
   auto p = std::make_unique<SgMatvecPlan>();
   p->ctx = &ctx;
   p->g1.ctx = &ctx;
   p->g3.ctx = &ctx;
   p->psi_size = S.size();
+  p->cplx = cplx;
+  // pack a block (or its real / imaginary part) of a tensor with element
+  // offset `off`, row and column strides in elements
+  auto add_pack = [&](std::vector<PackOp> &ops, int64_t off, int64_t rs, int64_t cs,
+                      int64_t img_off, int64_t rows, int64_t cols, int64_t r0, int64_t k0,
+                      int32_t kc, int32_t tr, int part, bool neg) {
+    PackOp op{};
+    op.src_off = off * es + (part == 1 ? 1 : 0);
+    op.src_rs = rs * es;
+    op.src_cs = cs * es;
+    op.img_off = img_off;
+    op.rows = (int32_t)rows;
+    op.cols = (int32_t)cols;
+    op.r0 = (int32_t)r0;
+    op.k0 = (int32_t)k0;
+    op.kc = kc;
+    op.tr = tr;
+    op.neg = neg ? 1 : 0;
+    ops.push_back(op);
+  };
   auto dim = [](const BTensor &t, int64_t b, int ax) { return t.idx[ax].dims[t.key(b)[ax]]; };
 
   // ---------------- step 1 groups: one per ket sector A ----------------------
@@ -60,11 +84,12 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
     int A;
     int64_t M, N, K, t1_off, l_off, p_off;
     int64_t Np;  // T1 row pitch: N rounded up to 4 (16-byte aligned rows)
+    int64_t Me, Ke;  // embedded GEMM shape (2M x 2K for complex data)
   };
   std::vector<G1> g1s;
   for (int A = 0; A < nA; ++A) {
     if (lrows[A].empty() || pcols[A].empty()) continue;
-    G1 g{A, 0, 0, L.idx[2].dims[A], t1tot, lbytes, pbytes, 0};
+    G1 g{A, 0, 0, L.idx[2].dims[A], t1tot, lbytes, pbytes, 0, 0, 0};
     std::vector<int64_t> rof, cof;
     for (int64_t b : lrows[A]) {
       rof.push_back(g.M);
@@ -76,37 +101,30 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
     }
     UDMRG_REQUIRE(g.M < (1 << 30) && g.N < (1 << 30) && g.K < (1 << 30), "mixed matvec: group too large");
     g.Np = (g.N + 3) & ~(int64_t)3;
-    const int32_t kc = (int32_t)((g.K + kTcBK - 1) / kTcBK);
+    g.Me = es * g.M;
+    g.Ke = es * g.K;
+    const int32_t kc = (int32_t)((g.Ke + kTcBK - 1) / kTcBK);
     for (size_t i = 0; i < lrows[A].size(); ++i) {
-      const int64_t b = lrows[A][i];
-      PackOp op{};
-      op.src_off = L.offs[b];
-      op.src_rs = g.K;
-      op.src_cs = 1;
-      op.img_off = g.l_off;
-      op.rows = (int32_t)(dim(L, b, 0) * dim(L, b, 1));
-      op.cols = (int32_t)g.K;
-      op.r0 = (int32_t)rof[i];
-      op.k0 = 0;
-      op.kc = kc;
-      op.tr = kTcBM;
-      lops.push_back(op);
+      const int64_t b = lrows[A][i], nr = dim(L, b, 0) * dim(L, b, 1);
+      // real rows [Lr | -Li], imaginary rows [Li | Lr]
+      add_pack(lops, L.offs[b], g.K, 1, g.l_off, nr, g.K, rof[i], 0, kc, kTcBM, 0, false);
+      if (cplx) {
+        add_pack(lops, L.offs[b], g.K, 1, g.l_off, nr, g.K, rof[i], g.K, kc, kTcBM, 1, true);
+        add_pack(lops, L.offs[b], g.K, 1, g.l_off, nr, g.K, g.M + rof[i], 0, kc, kTcBM, 1,
+                 false);
+        add_pack(lops, L.offs[b], g.K, 1, g.l_off, nr, g.K, g.M + rof[i], g.K, kc, kTcBM, 0,
+                 false);
+      }
     }
     for (size_t j = 0; j < pcols[A].size(); ++j) {
       const int64_t b = pcols[A][j];
       const int64_t ncol = dim(S, b, 1) * dim(S, b, 2) * dim(S, b, 3);
-      PackOp op{};
-      op.src_off = S.offs[b];
-      op.src_rs = 1;
-      op.src_cs = ncol;
-      op.img_off = g.p_off;
-      op.rows = (int32_t)ncol;
-      op.cols = (int32_t)g.K;
-      op.r0 = (int32_t)cof[j];
-      op.k0 = 0;
-      op.kc = kc;
-      op.tr = kTcBN;
-      p->psi_ops.push_back(op);
+      // K range [psi_r; psi_i]
+      add_pack(p->psi_ops, S.offs[b], 1, ncol, g.p_off, ncol, g.K, cof[j], 0, kc, kTcBN, 0,
+               false);
+      if (cplx)
+        add_pack(p->psi_ops, S.offs[b], 1, ncol, g.p_off, ncol, g.K, cof[j], g.K, kc, kTcBN, 1,
+                 false);
     }
     // T1 block locations
     for (size_t i = 0; i < lrows[A].size(); ++i) {
@@ -116,15 +134,16 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
         Key k = {L.key(lb)[0], L.key(lb)[1], S.key(pb)[1], S.key(pb)[2], S.key(pb)[3]};
         T1Block t;
         t.origin = g.t1_off + rof[i] * g.Np + cof[j];
+        t.im = cplx ? g.M * g.Np : 0;  // the imaginary half of the group's rows
         t.pitch = g.Np;
         t.dw = (int32_t)dim(L, lb, 1);
         t.ds12 = (int32_t)(dim(S, pb, 1) * dim(S, pb, 2));
         t1map[k] = t;
       }
     }
-    t1tot += g.M * g.Np;
-    lbytes += tc_image_bytes(g.M, g.K, kTcBM);
-    pbytes += tc_image_bytes(g.N, g.K, kTcBN);
+    t1tot += g.Me * g.Np;
+    lbytes += tc_image_bytes(g.Me, g.Ke, kTcBM);
+    pbytes += tc_image_bytes(g.N, g.Ke, kTcBN);
     g1s.push_back(g);
   }
   p->t1_size = t1tot;
@@ -153,28 +172,24 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       K += dim(R, b, 1) * dim(R, b, 2);
     }
     UDMRG_REQUIRE(M < (1 << 30) && K < (1 << 30), "mixed matvec: group too large");
-    const int32_t kc = (int32_t)((K + kTcBK - 1) / kTcBK);
+    const int64_t Ke = es * K, Ne = es * dBp;  // embedded shape: M x 2K times (2 dB') x 2K
+    const int32_t kc = (int32_t)((Ke + kTcBK - 1) / kTcBK);
     const int64_t t3_off = t3bytes, r_off = rbytes;
-    std::vector<int64_t> rows(M);
+    std::vector<int64_t> rows(M);  // output row addresses in doubles
     for (size_t i = 0; i < orows[Bp].size(); ++i) {
       const int64_t b = orows[Bp][i];
       const int64_t nr = dim(S, b, 0) * dim(S, b, 1) * dim(S, b, 2);
-      for (int64_t m = 0; m < nr; ++m) rows[rof[i] + m] = S.offs[b] + m * dBp;
+      for (int64_t m = 0; m < nr; ++m) rows[rof[i] + m] = (S.offs[b] + m * dBp) * es;
     }
     for (size_t j = 0; j < rks[Bp].size(); ++j) {
-      const int64_t b = rks[Bp][j];
-      PackOp op{};
-      op.src_off = R.offs[b];
-      op.src_rs = dim(R, b, 1) * dim(R, b, 2);
-      op.src_cs = 1;
-      op.img_off = r_off;
-      op.rows = (int32_t)dBp;
-      op.cols = (int32_t)(dim(R, b, 1) * dim(R, b, 2));
-      op.r0 = 0;
-      op.k0 = (int32_t)kof[j];
-      op.kc = kc;
-      op.tr = kTcBN;
-      rops.push_back(op);
+      const int64_t b = rks[Bp][j], nc = dim(R, b, 1) * dim(R, b, 2);
+      // B rows: [Rr | -Ri] (real output columns), [Ri | Rr] (imaginary)
+      add_pack(rops, R.offs[b], nc, 1, r_off, dBp, nc, 0, kof[j], kc, kTcBN, 0, false);
+      if (cplx) {
+        add_pack(rops, R.offs[b], nc, 1, r_off, dBp, nc, 0, K + kof[j], kc, kTcBN, 1, true);
+        add_pack(rops, R.offs[b], nc, 1, r_off, dBp, nc, dBp, kof[j], kc, kTcBN, 1, false);
+        add_pack(rops, R.offs[b], nc, 1, r_off, dBp, nc, dBp, K + kof[j], kc, kTcBN, 0, false);
+      }
     }
     // MPO-step targets of this group
     for (size_t i = 0; i < orows[Bp].size(); ++i) {
@@ -196,6 +211,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
         tg.ds12p = ds1p * ds2p;
         tg.dw2 = dw2;
         tg.nout = tg.ds12p * dw2;
+        tg.kim = (int32_t)K;  // imaginary half of the image columns
         tg.src0 = (int32_t)p->sources.size();
         // sources: T1 blocks (A', W, S1, S2, B) through W1 (W,S1,S1p,Wr) W2 (Wr,S2,S2p,W2s);
         // the fused coefficients depend on the MPO sectors only (cached in fm)
@@ -204,6 +220,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
           if (tb == t1map.end()) continue;
           MpoSource s{};
           s.t1_off = tb->second.origin;
+          s.t1_im = tb->second.im;
           s.row_pitch = tb->second.pitch;
           s.dw = tb->second.dw;
           s.ds12 = tb->second.ds12;
@@ -218,9 +235,9 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
         }
       }
     }
-    p->g3.add_group(t3_off, r_off, (int32_t)M, (int32_t)dBp, (int32_t)K, rows);
-    t3bytes += tc_image_bytes(M, K, kTcBM);
-    rbytes += tc_image_bytes(dBp, K, kTcBN);
+    p->g3.add_group(t3_off, r_off, (int32_t)M, (int32_t)Ne, (int32_t)Ke, rows);
+    t3bytes += tc_image_bytes(M, Ke, kTcBM);
+    rbytes += tc_image_bytes(Ne, Ke, kTcBN);
   }
   p->t3_bytes = t3bytes;
   p->r_bytes = rbytes;
@@ -240,9 +257,9 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   run_pack(ctx, rops, nullptr, (int)rops.size(), R.data, true, p->r_img);
   p->d_psi_ops = upload_pack_ops(ctx, p->psi_ops);
   for (auto &g : g1s) {
-    std::vector<int64_t> rows(g.M);
-    for (int64_t m = 0; m < g.M; ++m) rows[m] = g.t1_off + m * g.Np;
-    p->g1.add_group(g.l_off, g.p_off, (int32_t)g.M, (int32_t)g.N, (int32_t)g.K, rows);
+    std::vector<int64_t> rows(g.Me);
+    for (int64_t m = 0; m < g.Me; ++m) rows[m] = g.t1_off + m * g.Np;
+    p->g1.add_group(g.l_off, g.p_off, (int32_t)g.Me, (int32_t)g.N, (int32_t)g.Ke, rows);
   }
   p->g1.finalize();
   p->g3.finalize();
@@ -250,6 +267,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   {
     std::map<std::pair<int32_t, int32_t>, std::vector<int>> by_pair;
     for (size_t t = 0; t < p->targets.size(); ++t) by_pair[tgt_key[t]].push_back((int)t);
+    const size_t nreal = by_pair.size();
     for (auto &kv : by_pair) {
       MpoPair pr{};
       pr.in0 = (int32_t)p->ins.size();
@@ -267,9 +285,11 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
           if (in_first.count(sr.t1_off)) continue;
           in_first[sr.t1_off] = (int32_t)(p->ins.size() - pr.in0);
           for (int w = 0; w < sr.dw; ++w)
-            for (int s12 = 0; s12 < sr.ds12; ++s12)
+            for (int s12 = 0; s12 < sr.ds12; ++s12) {
               p->ins.push_back({sr.t1_off + (int64_t)w * sr.row_pitch + (int64_t)s12 * tg.db,
                                 (int64_t)sr.dw * sr.row_pitch});
+              p->in_im.push_back(sr.t1_im);
+            }
         }
       }
       pr.nin = (int32_t)p->ins.size() - pr.in0;
@@ -278,9 +298,11 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       for (int t : kv.second) {
         const MpoTarget &tg = p->targets[t];
         out_first.push_back((int32_t)(p->outs.size() - pr.out0));
-        for (int oc = 0; oc < tg.nout; ++oc)
+        for (int oc = 0; oc < tg.nout; ++oc) {
           p->outs.push_back({tg.img_off, tg.row0 + oc / tg.dw2, tg.ds12p,
                              tg.k0 + (oc % tg.dw2) * tg.db, tg.kc});
+          p->out_im.push_back(tg.kim);
+        }
       }
       pr.nout = (int32_t)p->outs.size() - pr.out0;
       UDMRG_REQUIRE(pr.nin <= 256 && pr.nout <= 256,
@@ -317,6 +339,34 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       p->unit_pair.insert(p->unit_pair.end(), nu, (int32_t)p->pairs.size());
       p->pairs.push_back(pr);
     }
+    // complex data: every pair again on the imaginary halves (the same
+    // coefficients: T1 rows shifted by the group's real row count, T3
+    // image columns by the group's real K)
+    if (cplx) {
+      for (size_t q = 0; q < nreal; ++q) {
+        MpoPair tw = p->pairs[q];
+        const int32_t in0 = (int32_t)p->ins.size(), out0 = (int32_t)p->outs.size();
+        for (int i = 0; i < tw.nin; ++i) {
+          MpoIn in = p->ins[tw.in0 + i];
+          in.base += p->in_im[tw.in0 + i];
+          p->ins.push_back(in);
+          p->in_im.push_back(0);
+        }
+        for (int o = 0; o < tw.nout; ++o) {
+          MpoOut ot = p->outs[tw.out0 + o];
+          ot.col0 += p->out_im[tw.out0 + o];
+          p->outs.push_back(ot);
+          p->out_im.push_back(0);
+        }
+        tw.in0 = in0;
+        tw.out0 = out0;
+        p->mpo_bytes += (double)tw.da * tw.db * (4.0 * tw.nin + 6.0 * tw.nout);
+        const int64_t nu = (int64_t)tw.da * ((tw.db + 31) / 32);
+        p->unit0.push_back(p->unit0.back() + nu);
+        p->unit_pair.insert(p->unit_pair.end(), nu, (int32_t)p->pairs.size());
+        p->pairs.push_back(tw);
+      }
+    }
   }
   p->d_pairs = upload_vec(ctx, p->pairs);
   p->d_ins = upload_vec(ctx, p->ins);
@@ -334,7 +384,7 @@ void SgMatvecPlan::apply(const double *psi_in, double *out) {
   run_pack(*ctx, psi_ops, d_psi_ops, (int)psi_ops.size(), psi_in, true, psi_img);
   run_tc_gemm(*ctx, g1, l_img, psi_img, t1, kTcOutF32, 1.0);
   run_mpo_step(*ctx, *this);
-  run_tc_gemm(*ctx, g3, t3_img, r_img, out, kTcOutF64, 1.0);
+  run_tc_gemm(*ctx, g3, t3_img, r_img, out, cplx ? kTcOutC128 : kTcOutF64, 1.0);
 }
 
 void SgMatvecPlan::apply_timed(const double *psi_in, double *out, float ms[4]) {
@@ -347,7 +397,7 @@ void SgMatvecPlan::apply_timed(const double *psi_in, double *out, float ms[4]) {
   cudaEventRecord(ev[2], ctx->stream);
   run_mpo_step(*ctx, *this);
   cudaEventRecord(ev[3], ctx->stream);
-  run_tc_gemm(*ctx, g3, t3_img, r_img, out, kTcOutF64, 1.0);
+  run_tc_gemm(*ctx, g3, t3_img, r_img, out, cplx ? kTcOutC128 : kTcOutF64, 1.0);
   cudaEventRecord(ev[4], ctx->stream);
   UDMRG_CHECK_CUDA(cudaEventSynchronize(ev[4]));
   for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);

@@ -11,7 +11,11 @@
 //   step 3 (tcgen05): for every bra sector B' of R, one dense GEMM
 //          res_B'[(a',s1',s2') x b'] = T3_B'[(a',s1',s2') x (w2,b)] . R_B'[b' x (w2,b)]^T.
 // L_A and R_B' images are packed once per plan (the environments are fixed
-// during a Lanczos solve); psi is packed every matvec.  T1 is FP32, its rows
+// during a Lanczos solve); psi is packed every matvec.  Complex L, R and psi
+// (real MPO coefficients) run through the real embedding: step 1 is
+// [T1r; T1i] = [[Lr, -Li], [Li, Lr]] [psi_r; psi_i] (2M x 2K GEMMs), the MPO
+// step maps both halves, step 3 is res = [T3r | T3i] [[Rr | -Ri]; [Ri | Rr]]^T
+// whose 2 dB' columns the epilogue interleaves into complex values.  T1 is FP32, its rows
 // padded to a multiple of four entries (16-byte aligned epilogue stores).
 #pragma once
 
@@ -32,12 +36,14 @@ struct MpoTarget {
   int32_t ds12p;       // ds1' * ds2'
   int32_t dw2;
   int32_t src0, nsrc;  // source list
+  int32_t kim;         // complex data: first image column of the imaginary half
 };
 
 // One MPO-step source: a T1 block (a', w, s1, s2, b) in T1_A and its
 // coefficient matrix coef[(w s1 s2) x (s1' s2' w2)].
 struct MpoSource {
   int64_t t1_off;      // element offset of entry (a'=0, w=0, s1=s2=0, b=0) in T1
+  int64_t t1_im;       // complex data: offset of the imaginary half
   int64_t row_pitch;   // T1 elements between consecutive (a', w) rows (N_A)
   int32_t dw, ds12;    // w dim, ds1 * ds2
   int32_t coef_off;    // offset into the coefficient array
@@ -68,6 +74,7 @@ struct MpoOut {
 struct SgMatvecPlan {
   Ctx *ctx = nullptr;
   int64_t psi_size = 0;
+  bool cplx = false;  // complex data through the real embedding
   // images
   uint8_t *l_img = nullptr, *psi_img = nullptr, *t3_img = nullptr, *r_img = nullptr;
   int64_t l_bytes = 0, psi_bytes = 0, t3_bytes = 0, r_bytes = 0;
@@ -89,6 +96,8 @@ struct SgMatvecPlan {
   std::vector<MpoPair> pairs;
   std::vector<MpoIn> ins;
   std::vector<MpoOut> outs;
+  std::vector<int64_t> in_im;   // planning only: imaginary-half shift of each input
+  std::vector<int32_t> out_im;  // and image-column shift of each output
   std::vector<int32_t> rowptr;  // CSR row pointers over all output channels (+1)
   std::vector<MpoNz> nz;
   std::vector<int64_t> unit0;  // first work unit of each pair (prefix, pairs + 1 entries)

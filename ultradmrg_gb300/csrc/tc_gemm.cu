@@ -139,6 +139,7 @@ __global__ void __launch_bounds__(256)
           if (rr < op.rows && kk < op.cols) {
             const T x = src[op.src_off + (int64_t)rr * op.src_rs + (int64_t)kk * op.src_cs];
             v = to_f32(x);
+            if (op.neg) v = -v;
           }
           tile[r][k] = v;
         }
@@ -316,7 +317,17 @@ __global__ void __launch_bounds__(kThreads, 1)
           float v[16];
 #pragma unroll
           for (int j = 0; j < 16; ++j) v[j] = g.kc > 0 ? af * __uint_as_float(r[j]) : 0.0f;
-          if (out_kind == kTcOutF64) {
+          if (out_kind == kTcOutC128) {
+            // columns [0, N/2): real parts, [N/2, N): imaginary parts of the
+            // interleaved complex row at base
+            const int half = g.N >> 1;
+            double *o = (double *)out + base;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const int n = nc + j;
+              if (n < g.N) o[n < half ? 2 * n : 2 * (n - half) + 1] = widen_f32(v[j]);
+            }
+          } else if (out_kind == kTcOutF64) {
             double *o = (double *)out + base + nc;
             const bool vec = (((base + nc) & 1) == 0);
 #pragma unroll

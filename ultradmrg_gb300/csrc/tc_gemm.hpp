@@ -34,6 +34,7 @@ struct PackOp {
   int32_t r0, k0;
   int32_t kc;  // K chunks of the image
   int32_t tr;  // rows per tile of the image (kTcBM or kTcBN)
+  int32_t neg, pad;  // neg: pack the negated values
 };
 
 // One dense GEMM C(MxN) = alpha * A(MxK) * B(NxK)^T between two images.
@@ -48,7 +49,9 @@ struct TcTile {
   int32_t group, mtile, ntile, pad;
 };
 
-enum TcOut : int { kTcOutF32 = 0, kTcOutF64 = 1 };
+// kTcOutC128: the N columns are the real parts (first half) and imaginary
+// parts (second half) of N/2 interleaved complex values per output row.
+enum TcOut : int { kTcOutF32 = 0, kTcOutF64 = 1, kTcOutC128 = 2 };
 
 struct TcPlan {
   Ctx *ctx = nullptr;
