@@ -78,24 +78,6 @@ __global__ void finish_sum_kernel(const double *__restrict__ partial, int nb, in
   }
 }
 
-// g = g - c1 * v1 - c2 * v2 (real coefficients), partial[b] = |g|^2 slice
-__global__ void lanczos_update_kernel(double *__restrict__ g, const double *__restrict__ v1,
-                                      const double *__restrict__ v2, double c1, double c2,
-                                      int64_t n, double *__restrict__ partial) {
-  double v[1] = {0.0};
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
-    double x = g[i];
-    x = fma(-c1, v1[i], x);
-    if (v2) x = fma(-c2, v2[i], x);
-    g[i] = x;
-    v[0] = fma(x, x, v[0]);
-  }
-  double out[1];
-  block_sum<1>(v, out);
-  if (threadIdx.x == 0) partial[blockIdx.x] = out[0];
-}
-
 __global__ void scale_kernel(double *__restrict__ x, int64_t n, double s) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) x[i] *= s;
@@ -395,17 +377,6 @@ std::complex<double> dot(VecWork &w, const double *x, const double *y, int64_t n
                                    w.ctx.stream));
   w.ctx.sync();
   return {h[0], h[1]};
-}
-
-void lanczos_update_async(VecWork &w, double *g, const double *v1, const double *v2, double c1,
-                          double c2, int64_t n_doubles, double *dnorm2) {
-  Ctx &ctx = w.ctx;
-  const int gr = red_grid(ctx, n_doubles);
-  lanczos_update_kernel<<<gr, kRedThreads, 0, ctx.stream>>>(g, v1, v2, c1, c2, n_doubles,
-                                                             w.partial);
-  finish_sum_kernel<<<1, kRedThreads, 0, ctx.stream>>>(w.partial, gr, 1, dnorm2);
-  UDMRG_CHECK_CUDA(cudaGetLastError());
-  ctx.launches += 2;
 }
 
 double norm2(VecWork &w, const double *x, int64_t n_doubles) {

@@ -8,7 +8,7 @@ namespace udmrg {
 SgMatvecPlan::~SgMatvecPlan() {
   if (!ctx) return;
   for (void *p : {(void *)l_img, (void *)psi_img, (void *)t3_img, (void *)r_img, (void *)t1,
-                  (void *)d_psi_ops, (void *)d_targets, (void *)d_sources, (void *)d_coefs,
+                  (void *)d_psi_ops,
                   (void *)d_pairs, (void *)d_ins, (void *)d_outs, (void *)d_rowptr,
                   (void *)d_nz, (void *)d_unit0, (void *)d_unit_pair})
     ctx->free(p);

@@ -89,9 +89,6 @@ struct SgMatvecPlan {
   std::vector<MpoTarget> targets;
   std::vector<MpoSource> sources;
   std::vector<float> coefs;
-  MpoTarget *d_targets = nullptr;
-  MpoSource *d_sources = nullptr;
-  float *d_coefs = nullptr;
   // pair-grouped form (the one the kernel runs)
   std::vector<MpoPair> pairs;
   std::vector<MpoIn> ins;

@@ -22,9 +22,6 @@ struct VecWork {
 // <x|y> = sum conj(x_i) y_i over n elements (complex when cplx).
 std::complex<double> dot(VecWork &w, const double *x, const double *y, int64_t n, bool cplx);
 void dot_async(VecWork &w, const double *x, const double *y, int64_t n, bool cplx, double *dres);
-// g -= c1*v1 + c2*v2 over n doubles (v2 may be null); writes |g|^2 to dnorm2.
-void lanczos_update_async(VecWork &w, double *g, const double *v1, const double *v2, double c1,
-                          double c2, int64_t n_doubles, double *dnorm2);
 double norm2(VecWork &w, const double *x, int64_t n_doubles);
 void scale(Ctx &ctx, double *x, int64_t n_doubles, double s);
 // out = sum_j coef_j vecs_j; coef interleaved (re, im) pairs when cplx, else plain reals.
