@@ -134,69 +134,68 @@ __device__ __forceinline__ bool gate_open(const double *gate) {
 }
 
 // partial[(j * gridDim.x + b) * 2 + {0,1}] = block b's share of <v_j | g>,
-// j < m.  Chunks of 32 * kMdPer elements per warp, grid-strided; each warp
-// keeps its running sums per vector in shared memory (warp-private slots,
-// 2 * m * kMdWarps doubles), summed over the block's warps at the end.  The
-// loads of a group of vectors are issued before their products.
+// j < m.  For each group of G vectors a lane streams its grid-strided
+// elements of g and of the group's vectors, keeping G running sums in
+// registers (no reduction inside the stream); at the end of the group the
+// sums are reduced over the warp and over the block's warps (shared memory,
+// 2 * m * kMdWarps doubles).  g is read once per group.
 template <bool CPLX>
 __global__ void __launch_bounds__(kMdThreads)
     multidot_kernel(const double *const *__restrict__ vecs, int m, const double *__restrict__ g,
                     int64_t n, double *__restrict__ partial, const double *__restrict__ gate) {
   if (!gate_open(gate)) return;
   constexpr int G = CPLX ? 4 : 8;  // vectors per group
+  constexpr int U = 2;             // elements per lane per step (independent loads)
   using E = typename std::conditional<CPLX, double2, double>::type;
   extern __shared__ double md_sm[];  // [m][kMdWarps][2]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int x = threadIdx.x; x < 2 * m * kMdWarps; x += kMdThreads) md_sm[x] = 0.0;
-  __syncthreads();
   const E *ge = (const E *)g;
-  const int64_t chunk = 32 * kMdPer;
-  const int64_t nchunks = (n + chunk - 1) / chunk;
-  for (int64_t c = (int64_t)blockIdx.x * kMdWarps + warp; c < nchunks;
-       c += (int64_t)gridDim.x * kMdWarps) {
-    const int64_t base = c * chunk + lane;
-    E gv[kMdPer];
+  const int64_t stride = (int64_t)gridDim.x * kMdThreads;
+  const int64_t i0 = (int64_t)blockIdx.x * kMdThreads + threadIdx.x;
+  for (int j0 = 0; j0 < m; j0 += G) {
+    const E *v[G];
 #pragma unroll
-    for (int k = 0; k < kMdPer; ++k) {
-      const int64_t i = base + 32 * k;
-      if constexpr (CPLX)
-        gv[k] = i < n ? ge[i] : make_double2(0.0, 0.0);
-      else
-        gv[k] = i < n ? ge[i] : 0.0;
-    }
-    for (int j0 = 0; j0 < m; j0 += G) {
-      E vv[G][kMdPer];
+    for (int q = 0; q < G; ++q) v[q] = (const E *)vecs[j0 + q < m ? j0 + q : j0];
+    double sr[G], si[G];
 #pragma unroll
-      for (int q = 0; q < G; ++q) {
-        const bool ok = j0 + q < m;
-        const E *v = (const E *)vecs[ok ? j0 + q : j0];
+    for (int q = 0; q < G; ++q) sr[q] = si[q] = 0.0;
+    for (int64_t i = i0; i < n; i += U * stride) {
+      E gv[U], vv[U][G];
 #pragma unroll
-        for (int k = 0; k < kMdPer; ++k) {
-          const int64_t i = base + 32 * k;
+      for (int u = 0; u < U; ++u) {
+        const int64_t ii = i + u * stride;
+        const bool ok = ii < n;
+        if constexpr (CPLX)
+          gv[u] = ok ? ge[ii] : make_double2(0.0, 0.0);
+        else
+          gv[u] = ok ? ge[ii] : 0.0;
+#pragma unroll
+        for (int q = 0; q < G; ++q) {
           if constexpr (CPLX)
-            vv[q][k] = ok && i < n ? v[i] : make_double2(0.0, 0.0);
+            vv[u][q] = ok ? v[q][ii] : make_double2(0.0, 0.0);
           else
-            vv[q][k] = ok && i < n ? v[i] : 0.0;
+            vv[u][q] = ok ? v[q][ii] : 0.0;
         }
       }
 #pragma unroll
-      for (int q = 0; q < G; ++q) {
-        double sr = 0.0, si = 0.0;
+      for (int u = 0; u < U; ++u)
 #pragma unroll
-        for (int k = 0; k < kMdPer; ++k) {
+        for (int q = 0; q < G; ++q) {
           if constexpr (CPLX) {  // conj(v) g
-            sr = fma(vv[q][k].x, gv[k].x, fma(vv[q][k].y, gv[k].y, sr));
-            si = fma(vv[q][k].x, gv[k].y, fma(-vv[q][k].y, gv[k].x, si));
+            sr[q] = fma(vv[u][q].x, gv[u].x, fma(vv[u][q].y, gv[u].y, sr[q]));
+            si[q] = fma(vv[u][q].x, gv[u].y, fma(-vv[u][q].y, gv[u].x, si[q]));
           } else {
-            sr = fma(vv[q][k], gv[k], sr);
+            sr[q] = fma(vv[u][q], gv[u], sr[q]);
           }
         }
-        sr = warp_sum(sr);
-        if constexpr (CPLX) si = warp_sum(si);
-        if (lane == 0 && j0 + q < m) {
-          md_sm[(2 * (j0 + q)) * kMdWarps + 2 * warp] += sr;
-          md_sm[(2 * (j0 + q)) * kMdWarps + 2 * warp + 1] += si;
-        }
+    }
+#pragma unroll
+    for (int q = 0; q < G; ++q) {
+      const double a = warp_sum(sr[q]);
+      const double b = CPLX ? warp_sum(si[q]) : 0.0;
+      if (lane == 0 && j0 + q < m) {
+        md_sm[(2 * (j0 + q)) * kMdWarps + 2 * warp] = a;
+        md_sm[(2 * (j0 + q)) * kMdWarps + 2 * warp + 1] = b;
       }
     }
   }
