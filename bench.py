@@ -193,7 +193,7 @@ def run_reference(args):
     w = WORKLOADS[args.workload]
     eff, psi = cpu_problem(w)
     # size each step so that warm-up + steps stay within about two minutes
-    per_step = max(2.0, min(args.cpu_budget, 120.0 / max(1, args.steps + args.warmup)))
+    per_step = max(0.05, min(args.cpu_budget, 120.0 / max(1, args.steps + args.warmup)))
     flops, dt, kept, nbra = cpu_matvec_sample(eff, psi, per_step)
     L = eff[0]
     bra = sorted({k[0] for k in L.blocks})
@@ -273,14 +273,19 @@ def run_ours(args):
     def step():
         plan.apply_ptr(xp, yp)
 
-    def timed(fn, steps, slot0):
-        for i in range(steps):
-            ctx.flush_l2()
-            ctx.event(slot0 + 2 * i)
-            fn()
-            ctx.event(slot0 + 2 * i + 1)
-        ctx.sync()
-        return sum(ctx.elapsed_ms(slot0 + 2 * i, slot0 + 2 * i + 1) for i in range(steps)) / steps / 1e3
+    def timed(fn, steps, slot0, ring=100):
+        # event pairs in a ring of `ring` slots, read back every `ring` steps
+        total = 0.0
+        for c0 in range(0, steps, ring):
+            cn = min(ring, steps - c0)
+            for i in range(cn):
+                ctx.flush_l2()
+                ctx.event(slot0 + 2 * i)
+                fn()
+                ctx.event(slot0 + 2 * i + 1)
+            ctx.sync()
+            total += sum(ctx.elapsed_ms(slot0 + 2 * i, slot0 + 2 * i + 1) for i in range(cn))
+        return total / steps / 1e3
 
     for _ in range(args.warmup):
         ctx.flush_l2()
