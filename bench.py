@@ -175,6 +175,30 @@ def cpu_matvec_sample(eff, psi, budget_s):
     return bs.FLOPS[0], dt, len(keep), len(bra)
 
 
+def krylov_graph_probe(api, ctx, ops, psi, prec, reps=2):
+    """Wall seconds of one Lanczos solve (1e-10, at most 120 steps; matvec plan
+    included) with each Krylov step replayed as a CUDA graph and with its
+    kernels launched directly, the faster of `reps` runs each."""
+    out = {}
+    for graph in (False, True):
+        ctx.set_krylov_graph(graph)
+        best, res = None, None
+        for _ in range(reps):
+            ctx.sync()
+            t0 = time.perf_counter()
+            r = api.lanczos_solver(ctx, ops, psi, 1e-10, 120, precision=prec)
+            dt = time.perf_counter() - t0
+            res = (r.iters, r.gs_eng)
+            r.gs_vec.close()
+            best = dt if best is None else min(best, dt)
+        out[graph] = (best, res)
+    ctx.set_krylov_graph(True)
+    (tg, rg), (td, rd) = out[True], out[False]
+    return {"graph_sec": tg, "direct_sec": td, "iters": rg[0],
+            "us_per_step_graph": tg / rg[0] * 1e6, "us_per_step_direct": td / rd[0] * 1e6,
+            "identical": rg == rd}
+
+
 def cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -332,6 +356,21 @@ def run_ours(args):
         r = api.lanczos_solver(ctx, ops, psi, 1e-10, 120, precision=prec)
         lz[name] = (r.gs_eng, r.iters, r.matvec_seconds / max(r.matvecs, 1))
         r.gs_vec.close()
+    # Krylov steps as CUDA graph replays against direct launches: this
+    # workload (mixed) and the L = 32 Heisenberg chain at D = 256 (short steps)
+    kg = {f"{w.name}_mixed": krylov_graph_probe(api, ctx, ops, psi, api.PREC_MIXED)}
+    sw = WORKLOADS["heisenberg32_D256"]
+    smpo, smps = build_host(sw)
+    sL, sR = api.build_envs(ctx, smpo, smps, sw.centre, normalize=False)
+    sA1 = api.DeviceTensor.from_data(ctx, smps[sw.centre])
+    sA2 = api.DeviceTensor.from_data(ctx, smps[sw.centre + 1])
+    spsi = api.contract(ctx, sA1, sA2, [2], [0])
+    sW1 = api.DeviceTensor.from_data(ctx, smpo[sw.centre])
+    sW2 = api.DeviceTensor.from_data(ctx, smpo[sw.centre + 1])
+    for prec, tag in ((api.PREC_FP64, "fp64"), (api.PREC_MIXED, "mixed")):
+        kg[f"{sw.name}_{tag}"] = krylov_graph_probe(api, ctx, [sL, sW1, sW2, sR], spsi, prec)
+    for t in (sL, sR, sA1, sA2, spsi, sW1, sW2):
+        t.close()
     # one full local update at the centre bond (Lanczos to 1e-9 as the reference
     # benchmark, truncated SVD to D, environment update) in three forms: plain
     # FP64 + exact SVD, mixed + exact SVD, mixed + randomized SVD sized from the
@@ -434,6 +473,7 @@ def run_ours(args):
                      "lanczos_E_mixed": lz["mixed"][0], "lanczos_E_fp64": lz["fp64"][0],
                      "lanczos_iters": [lz["mixed"][1], lz["fp64"][1]],
                      "lanczos_rel_dE": abs(lz["mixed"][0] - lz["fp64"][0]) / abs(lz["fp64"][0])},
+        "krylov_graph": kg,
         "centre_site_update": {
             k: {kk: v[kk] for kk in ("wall_sec", "lancz_sec", "svd_sec", "env_sec", "iters", "D",
                                      "trunc_err", "e0", "svd_grow_rounds")}

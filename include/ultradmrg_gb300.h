@@ -103,6 +103,13 @@ int udmrg_ctx_destroy(udmrg_ctx *ctx);
 int udmrg_ctx_sync(udmrg_ctx *ctx);
 /* Number of device kernels this library launched through ctx so far. */
 int udmrg_ctx_launches(udmrg_ctx *ctx, uint64_t *out);
+/* Krylov steps (Lanczos ground state, Lanczos exponential) as CUDA graphs:
+ * enable != 0 (the default) captures each solve's step launch sequence once
+ * and replays it per step; 0 launches the kernels directly.  Both run the
+ * same kernels on the same data (identical results).  Replaces nothing in
+ * qlmps: the reference loop calls the matvec function pointer per step
+ * (lanczos_vmps_solver_impl.h:148, 213). */
+int udmrg_ctx_set_krylov_graph(udmrg_ctx *ctx, int enable);
 
 /* ---- tensors (QLTensor storage model) -------------------------------- */
 /* nsec[rank]: sectors per index; qns[sum(nsec)*nq]; dims[sum(nsec)];

@@ -67,6 +67,7 @@ SIGNATURES = {
     "udmrg_ctx_destroy": [C.c_void_p],
     "udmrg_ctx_sync": [C.c_void_p],
     "udmrg_ctx_launches": [C.c_void_p, C.POINTER(C.c_uint64)],
+    "udmrg_ctx_set_krylov_graph": [C.c_void_p, C.c_int],
     "udmrg_tensor_create": [C.c_void_p, C.c_int, C.c_int, C.c_int, c_int32_p, c_int32_p,
                             c_int64_p, c_int32_p, C.c_int64, c_int32_p, c_void_pp],
     "udmrg_tensor_destroy": [C.c_void_p],

@@ -37,6 +37,10 @@ class Context:
         call("udmrg_ctx_launches", self.h, C.byref(v))
         return int(v.value)
 
+    def set_krylov_graph(self, enable: bool):
+        """Krylov steps as one CUDA graph replay each (default) or direct launches."""
+        call("udmrg_ctx_set_krylov_graph", self.h, 1 if enable else 0)
+
     def event(self, slot: int):
         call("udmrg_ctx_event_record", self.h, slot)
 

@@ -51,6 +51,8 @@ struct Ctx {
   size_t pinned_cap = 0;
   // counts of kernels launched by this library through this context
   uint64_t launches = 0;
+  // Krylov solvers replay each step as one CUDA graph (captured once per solve)
+  bool krylov_graph = true;
   // C-ABI lifetime: live tensor / plan handles on this context; a context
   // whose destroy was requested is deleted when the last handle goes
   int64_t live_handles = 0;

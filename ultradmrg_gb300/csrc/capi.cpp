@@ -117,6 +117,13 @@ int udmrg_ctx_launches(udmrg_ctx *c, uint64_t *out) {
   return guarded([&] { *out = c->ctx.launches; });
 }
 
+int udmrg_ctx_set_krylov_graph(udmrg_ctx *c, int enable) {
+  return guarded([&] {
+    UDMRG_REQUIRE(c, "null argument");
+    c->ctx.krylov_graph = enable != 0;
+  });
+}
+
 int udmrg_tensor_create(udmrg_ctx *c, int dtype, int nq, int rank, const int32_t *nsec,
                         const int32_t *qns, const int64_t *dims, const int32_t *dirs,
                         int64_t nblocks, const int32_t *keys, udmrg_tensor **out) {

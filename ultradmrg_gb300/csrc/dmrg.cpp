@@ -314,6 +314,78 @@ struct Bases {
   }
 };
 
+// Runs the Krylov steps of one solve.  A step is the fixed launch sequence
+// normalise (Y -> v_s, X), matvec (X -> Y), alpha, three-term update, the
+// optional Gram-Schmidt passes and publish; every kernel reads the step
+// index from the device, so with ctx.krylov_graph the sequence is captured
+// once as a CUDA graph and each step is one graph launch.  Direct launches
+// and graph replays run the same kernels on the same data (identical
+// results).  run() returns after the step's one host synchronisation.
+struct KrylovSteps {
+  Ctx &ctx;
+  KrylovWork &kw;
+  MatvecPlan &mv;
+  bool reorth;
+  bool graph;
+  EventTimer ev;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t graph_kernels = 0;  // kernels one replay launches
+  double seconds = 0;          // matvec device time (graph: whole steps)
+  KrylovSteps(Ctx &c, KrylovWork &k, MatvecPlan &m, bool with_reorth)
+      : ctx(c), kw(k), mv(m), reorth(with_reorth), graph(c.krylov_graph) {}
+  ~KrylovSteps() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+  void issue(bool timed) {
+    krylov_normalise(kw);
+    if (timed) cudaEventRecord(ev.a, ctx.stream);
+    mv.apply(kw.X, kw.Y);
+    if (timed) cudaEventRecord(ev.b, ctx.stream);
+    krylov_alpha(kw);
+    krylov_update(kw);
+    if (reorth) {
+      krylov_project(kw, false);
+      krylov_project(kw, true);
+    }
+    krylov_publish(kw);
+  }
+  void capture() {
+    const uint64_t l0 = ctx.launches;
+    UDMRG_CHECK_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeRelaxed));
+    cudaGraph_t g = nullptr;
+    try {
+      issue(false);
+    } catch (...) {
+      cudaStreamEndCapture(ctx.stream, &g);
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      ctx.launches = l0;
+      throw;
+    }
+    UDMRG_CHECK_CUDA(cudaStreamEndCapture(ctx.stream, &g));
+    graph_kernels = ctx.launches - l0;
+    ctx.launches = l0;  // captured, not launched
+    const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    UDMRG_CHECK_CUDA(e);
+  }
+  void run() {
+    if (graph) {
+      if (!exec) capture();
+      cudaEventRecord(ev.a, ctx.stream);
+      UDMRG_CHECK_CUDA(cudaGraphLaunch(exec, ctx.stream));
+      cudaEventRecord(ev.b, ctx.stream);
+      ctx.launches += graph_kernels;
+    } else {
+      issue(true);
+    }
+    ctx.sync();
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev.a, ev.b);
+    seconds += ms * 1e-3;
+  }
+};
+
 }  // namespace
 
 LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
@@ -332,23 +404,10 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
   std::vector<double> a(maxit, 0.0), b(maxit, 0.0), N(maxit, 0.0);
   LanczosResult res;
   const bool mixed = mv.sg != nullptr;
-  KrylovWork kw(ctx, n, cplx);
-  EventTimer ev;
-  // the matvec is timed by events, read after the step's one synchronisation
-  auto matvec = [&](const double *in) {
-    double *out = (double *)ctx.alloc(vbytes);
-    cudaEventRecord(ev.a, ctx.stream);
-    mv.apply(in, out);
-    cudaEventRecord(ev.b, ctx.stream);
-    res.matvecs++;
-    return out;
-  };
-  auto matvec_time = [&]() {
-    float ms = 0;
-    cudaEventElapsedTime(&ms, ev.a, ev.b);
-    res.matvec_seconds += ms * 1e-3;
-  };
+  KrylovWork kw(ctx, n, cplx, maxit);
+  KrylovSteps steps(ctx, kw, mv, mixed);
   auto finish = [&](int64_t m, const std::vector<double> &vec) {
+    res.matvec_seconds = steps.seconds;
     if (mv.sg && (tc_check(ctx, mv.sg->g1) | tc_check(ctx, mv.sg->g3)))
       throw Error(kErrTimeout, "tcgen05 GEMM: a bounded device wait ran out");
     auto gs = S.clone_struct();
@@ -373,36 +432,26 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
     }
     return gs;
   };
-  // bases[0] = init / |init| (QuasiNormalize)
+  // Y = init; step 0 normalises it into bases[0] (QuasiNormalize)
   {
     auto v0 = embed(ctx, init_state, S);
-    double *d0 = (double *)ctx.alloc(vbytes);
-    UDMRG_CHECK_CUDA(cudaMemcpyAsync(d0, v0->data, nd * sizeof(double), cudaMemcpyDeviceToDevice,
-                                     ctx.stream));
-    const double nrm = std::sqrt(norm2(w, d0, nd));
-    if (nrm != 0.0) scale(ctx, d0, nd, 1.0 / nrm);
-    bases.v.push_back(d0);
-    kw.push(0, d0);
+    krylov_begin(kw, v0->data);
   }
-  // Step m: gamma = H v_m - a_m v_m - b_{m-1} v_{m-1}; with mixed precision
-  // gamma is then projected against every basis vector (FP64 classical
-  // Gram-Schmidt, a second pass where the first removed more than half of
-  // |gamma|^2), so rounding in the matvec cannot build up ghost Ritz values.
-  // alpha and |gamma| reach the host once per step; the convergence test on
-  // the (m+1)-dimensional tridiagonal matrix follows.
-  double *last = matvec(bases.v[0]);
-  krylov_alpha(kw, 0, last);
+  // Step m: v_m = gamma_{m-1} / |gamma_{m-1}|, gamma_m = H v_m - a_m v_m -
+  // b_{m-1} v_{m-1}; with mixed precision gamma is then projected against
+  // every basis vector (FP64 classical Gram-Schmidt, a second pass where the
+  // first removed more than half of |gamma|^2), so rounding in the matvec
+  // cannot build up ghost Ritz values.  alpha and |gamma| reach the host once
+  // per step; the convergence test on the (m+1)-dimensional tridiagonal
+  // matrix follows.
   int64_t m = 0;
   double energy0 = 0.0;
   while (true) {
-    double *gamma = last;
-    krylov_update(kw, (int)m, gamma);
-    if (mixed) {
-      krylov_project(kw, (int)m, gamma, false);
-      krylov_project(kw, (int)m, gamma, true);
-    }
-    krylov_fetch(kw, (int)m);
-    matvec_time();
+    double *vm = (double *)ctx.alloc(vbytes);
+    bases.v.push_back(vm);
+    kw.push((int)m, vm);
+    steps.run();
+    res.matvecs++;
     a[m] = kw.hres[0];
     const double n2 = kw.hres[1];
     if (m == 0) {
@@ -415,7 +464,6 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
       if ((energy0 - e_new) < p.error || noise_floor || m == eff_dim || m == maxit - 1) {
         std::vector<double> vec;
         tridiag_lowest(a, b, m + 1, &vec);
-        ctx.free(gamma);
         res.iters = m + 1;
         res.gs_eng = e_new;
         res.gs_vec = finish(m + 1, vec);
@@ -425,7 +473,6 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
     }
     const double norm_gamma = std::sqrt(n2);
     if (norm_gamma == 0.0) {  // invariant subspace
-      ctx.free(gamma);
       std::vector<double> vec = {1.0};
       if (m > 0) tridiag_lowest(a, b, m + 1, &vec);
       res.iters = m + 1;
@@ -433,14 +480,9 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
       res.gs_vec = finish(m + 1, vec);
       return res;
     }
-    krylov_normalise(kw, (int)m, gamma);
     N[m + 1] = n2;
     b[m] = norm_gamma;
-    bases.v.push_back(gamma);
-    kw.push((int)m + 1, gamma);
-    last = matvec(gamma);
     m += 1;
-    krylov_alpha(kw, (int)m, last);
   }
 }
 
@@ -516,37 +558,23 @@ ExpmvResult lanczos_expmv(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state, d
     lincomb(w, out->data, vs, coef_il, n, true);
     return out;
   };
-  double initial_norm;
+  const bool mixed = mv.sg != nullptr;
+  KrylovWork kw(ctx, n, true, maxit);
+  KrylovSteps steps(ctx, kw, mv, mixed);
   {
     auto v0 = embed(ctx, init_state, S);
-    double *d0 = (double *)ctx.alloc(vbytes);
-    UDMRG_CHECK_CUDA(cudaMemcpyAsync(d0, v0->data, nd * sizeof(double), cudaMemcpyDeviceToDevice,
-                                     ctx.stream));
-    initial_norm = std::sqrt(norm2(w, d0, nd));
-    if (initial_norm != 0.0) scale(ctx, d0, nd, 1.0 / initial_norm);
-    bases.v.push_back(d0);
+    krylov_begin(kw, v0->data);
   }
-  auto matvec = [&](const double *in) {
-    double *out = (double *)ctx.alloc(vbytes);
-    mv.apply(in, out);
-    return out;
-  };
-  const bool mixed = mv.sg != nullptr;
-  KrylovWork kw(ctx, n, true);
-  kw.push(0, bases.v[0]);
-  double *last = matvec(bases.v[0]);
-  krylov_alpha(kw, 0, last);
+  double initial_norm = 0.0;
   int64_t m = 0;
   std::vector<double> last_coef(2 * maxit, 0.0);
   // step m as in lanczos_gs: one host synchronisation per step
   while (true) {
-    double *gamma = last;
-    krylov_update(kw, (int)m, gamma);
-    if (mixed) {  // as in lanczos_gs: FP64 Gram-Schmidt against the basis
-      krylov_project(kw, (int)m, gamma, false);
-      krylov_project(kw, (int)m, gamma, true);
-    }
-    krylov_fetch(kw, (int)m);
+    double *vm = (double *)ctx.alloc(vbytes);
+    bases.v.push_back(vm);
+    kw.push((int)m, vm);
+    steps.run();
+    if (m == 0) initial_norm = std::sqrt(kw.hres[2]);
     a[m] = kw.hres[0];
     const double n2 = kw.hres[1];
     if (m > 0) {
@@ -559,7 +587,6 @@ ExpmvResult lanczos_expmv(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state, d
       }
       dist = std::sqrt(dist);
       if (dist < p.error || m == eff_dim || m == maxit - 1) {
-        ctx.free(gamma);
         for (auto &x : coef) x *= initial_norm;
         res.iters = m + 1;
         res.expmv = combine(m + 1, coef);
@@ -570,7 +597,6 @@ ExpmvResult lanczos_expmv(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state, d
     }
     const double norm_gamma = std::sqrt(n2);
     if (norm_gamma == 0.0) {  // invariant subspace
-      ctx.free(gamma);
       res.iters = m + 1;
       if (m == 0) {
         const double ph = -step * a[0];
@@ -582,13 +608,8 @@ ExpmvResult lanczos_expmv(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state, d
       }
       return res;
     }
-    krylov_normalise(kw, (int)m, gamma);
     b[m] = norm_gamma;
-    bases.v.push_back(gamma);
-    kw.push((int)m + 1, gamma);
-    last = matvec(gamma);
     m += 1;
-    krylov_alpha(kw, (int)m, last);
   }
 }
 

@@ -134,16 +134,18 @@ __device__ __forceinline__ bool gate_open(const double *gate) {
 }
 
 // partial[(j * gridDim.x + b) * 2 + {0,1}] = block b's share of <v_j | g>,
-// j < m.  For each group of G vectors a lane streams its grid-strided
+// j < m = step + 1.  For each group of G vectors a lane streams its grid-strided
 // elements of g and of the group's vectors, keeping G running sums in
 // registers (no reduction inside the stream); at the end of the group the
 // sums are reduced over the warp and over the block's warps (shared memory,
 // 2 * m * kMdWarps doubles).  g is read once per group.
 template <bool CPLX>
 __global__ void __launch_bounds__(kMdThreads)
-    multidot_kernel(const double *const *__restrict__ vecs, int m, const double *__restrict__ g,
-                    int64_t n, double *__restrict__ partial, const double *__restrict__ gate) {
+    multidot_kernel(const double *const *__restrict__ vecs, const int *__restrict__ step,
+                    const double *__restrict__ g, int64_t n, double *__restrict__ partial,
+                    const double *__restrict__ gate) {
   if (!gate_open(gate)) return;
+  const int m = *step + 1;
   constexpr int G = CPLX ? 4 : 8;  // vectors per group
   constexpr int U = 2;             // elements per lane per step (independent loads)
   using E = typename std::conditional<CPLX, double2, double>::type;
@@ -211,10 +213,12 @@ __global__ void __launch_bounds__(kMdThreads)
   }
 }
 
-// res[2 j .. 2 j + 1] = sum over the nb partial pairs of row j (block j, fixed order)
+// res[2 j .. 2 j + 1] = sum over the nb partial pairs of row j (block j, fixed
+// order) for j <= step; the grid covers the largest step, later blocks return
 __global__ void multidot_finish_kernel(const double *__restrict__ partial, int nb,
-                                       double *__restrict__ res, const double *__restrict__ gate) {
-  if (!gate_open(gate)) return;
+                                       double *__restrict__ res, const int *__restrict__ step,
+                                       const double *__restrict__ gate) {
+  if (!gate_open(gate) || (int)blockIdx.x > *step) return;
   const double *p = partial + (int64_t)blockIdx.x * nb * 2;
   double v[2] = {0.0, 0.0};
   for (int i = threadIdx.x; i < nb; i += blockDim.x) {
@@ -229,14 +233,16 @@ __global__ void multidot_finish_kernel(const double *__restrict__ partial, int n
   }
 }
 
-// g -= sum_j c_j v_j (complex c_j when CPLX), partial[b] = |g|^2 slice.  The
-// vector loop is unrolled by 8 with two accumulators, so eight loads are in
+// g -= sum_{j <= step} c_j v_j (complex c_j when CPLX), partial[b] = |g|^2
+// slice.  The vector loop is unrolled by 8 with two accumulators, so eight loads are in
 // flight per element.
 template <bool CPLX>
 __global__ void project_kernel(double *__restrict__ g, const double *const *__restrict__ vecs,
-                               const double *__restrict__ c, int m, int64_t n,
-                               double *__restrict__ partial, const double *__restrict__ gate) {
+                               const double *__restrict__ c, const int *__restrict__ step,
+                               int64_t n, double *__restrict__ partial,
+                               const double *__restrict__ gate) {
   if (!gate_open(gate)) return;
+  const int m = *step + 1;
   __shared__ double cs[2 * kMaxVecs];
   __shared__ const double *vs[kMaxVecs];
   for (int j = threadIdx.x; j < m; j += blockDim.x) {
@@ -285,12 +291,13 @@ __global__ void project_kernel(double *__restrict__ g, const double *const *__re
   if (threadIdx.x == 0) partial[blockIdx.x] = out[0];
 }
 
-// res[0] = sum of the nb partials (fixed order); with keep, keep[0] = the
-// previous res[0] (|g|^2 before a Gram-Schmidt pass) and keep[1] = the sum
+// nrm2[step + 1] = sum of the nb partials (fixed order); with keep, keep[0] =
+// its previous value (|g|^2 before a Gram-Schmidt pass) and keep[1] = the sum
 __global__ void norm_finish_kernel(const double *__restrict__ partial, int nb,
-                                   double *__restrict__ res, double *__restrict__ keep,
-                                   const double *__restrict__ gate) {
+                                   double *__restrict__ nrm2, const int *__restrict__ step,
+                                   double *__restrict__ keep, const double *__restrict__ gate) {
   if (!gate_open(gate)) return;
+  double *res = nrm2 + *step + 1;
   double v[1] = {0.0};
   for (int i = threadIdx.x; i < nb; i += blockDim.x) v[0] += partial[i];
   double out[1];
@@ -304,13 +311,17 @@ __global__ void norm_finish_kernel(const double *__restrict__ partial, int nb,
   }
 }
 
-// g = g - Re(alpha) v1 - sqrt(nrm2_prev) v2 (v2 may be null), partial = |g|^2 slices
+// s = step: g = g - Re(alpha[s]) v1 - sqrt(nrm2[s]) v_{s-1} (the second term
+// when s > 0), partial = |g|^2 slices
 __global__ void krylov_update_kernel(double *__restrict__ g, const double *__restrict__ v1,
-                                     const double *__restrict__ v2,
+                                     const double *const *__restrict__ vecs,
+                                     const int *__restrict__ step,
                                      const double *__restrict__ alpha,
-                                     const double *__restrict__ nrm2_prev, int64_t n,
+                                     const double *__restrict__ nrm2, int64_t n,
                                      double *__restrict__ partial) {
-  const double c1 = alpha[0], c2 = v2 ? sqrt(nrm2_prev[0]) : 0.0;
+  const int s = *step;
+  const double *v2 = s > 0 ? vecs[s - 1] : nullptr;
+  const double c1 = alpha[2 * s], c2 = v2 ? sqrt(nrm2[s]) : 0.0;
   double v[1] = {0.0};
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
@@ -325,13 +336,52 @@ __global__ void krylov_update_kernel(double *__restrict__ g, const double *__res
   if (threadIdx.x == 0) partial[blockIdx.x] = out[0];
 }
 
-__global__ void normalise_kernel(double *__restrict__ x, int64_t n,
-                                 const double *__restrict__ nrm2) {
-  const double nr = sqrt(nrm2[0]);
-  if (nr == 0.0) return;
-  const double s = 1.0 / nr;
+// s = step: v_s = y / sqrt(nrm2[s]) (y unchanged when the norm is zero),
+// written to the registered basis vector s and to x
+__global__ void krylov_normalise_kernel(const double *__restrict__ y, double *__restrict__ x,
+                                        const double *const *__restrict__ vecs,
+                                        const int *__restrict__ step,
+                                        const double *__restrict__ nrm2, int64_t n) {
+  const int s = *step;
+  const double nr = sqrt(nrm2[s]);
+  const double sc = nr == 0.0 ? 1.0 : 1.0 / nr;
+  double *v = const_cast<double *>(vecs[s]);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) x[i] *= s;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double t = nr == 0.0 ? y[i] : y[i] * sc;
+    x[i] = t;
+    v[i] = t;
+  }
+}
+
+// res[stride * step + offset + {0, 1}] = the sum of nb partials of `width`
+// values (the second only when width > 1), fixed order
+__global__ void finish_step_kernel(const double *__restrict__ partial, int nb, int width,
+                                   double *__restrict__ res, const int *__restrict__ step,
+                                   int stride, int offset) {
+  double v[2] = {0.0, 0.0};
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    v[0] += partial[width * i];
+    if (width > 1) v[1] += partial[width * i + 1];
+  }
+  double out[2];
+  block_sum<2>(v, out);
+  if (threadIdx.x == 0) {
+    double *r = res + (int64_t)stride * *step + offset;
+    r[0] = out[0];
+    if (width > 1) r[1] = out[1];
+  }
+}
+
+// host-visible results of step s, then the step counter moves on
+__global__ void krylov_publish_kernel(const double *__restrict__ alpha,
+                                      const double *__restrict__ nrm2, int *__restrict__ step,
+                                      double *__restrict__ hres) {
+  const int s = *step;
+  hres[0] = alpha[2 * s];
+  hres[1] = nrm2[s + 1];
+  hres[2] = nrm2[s];
+  *step = s + 1;
 }
 
 int red_grid(const Ctx &ctx, int64_t n) {
@@ -410,11 +460,12 @@ void lincomb(VecWork &w, double *out, const std::vector<const double *> &vecs,
   ctx.sync();  // pinned staging buffer is reused by the next call
 }
 
-KrylovWork::KrylovWork(Ctx &c, int64_t n_elems, bool complex_data)
+KrylovWork::KrylovWork(Ctx &c, int64_t n_elems, bool complex_data, int64_t max_steps)
     : ctx(c), n(n_elems), cplx(complex_data) {
+  mcap = (int)std::max<int64_t>(1, std::min<int64_t>(max_steps + 1, kMaxVecs));
   const int64_t blocks = (n + kMdThreads * kMdPer - 1) / (kMdThreads * kMdPer);
   nb = (int)std::max<int64_t>(1, std::min<int64_t>(blocks, 2 * ctx.num_sms));
-  partial = (double *)ctx.alloc(sizeof(double) * 2 * (size_t)kMaxVecs * nb);
+  partial = (double *)ctx.alloc(sizeof(double) * 2 * (size_t)mcap * nb);
   gate = (double *)ctx.alloc(sizeof(double) * 2);
   const int msm = (int)(sizeof(double) * 2 * kMaxVecs * kMdWarps);
   UDMRG_CHECK_CUDA(cudaFuncSetAttribute(multidot_kernel<true>,
@@ -424,10 +475,15 @@ KrylovWork::KrylovWork(Ctx &c, int64_t n_elems, bool complex_data)
   red = (double *)ctx.alloc(sizeof(double) * 8 * 1024);
   coef = (double *)ctx.alloc(sizeof(double) * 2 * kMaxVecs);
   alpha = (double *)ctx.alloc(sizeof(double) * 2 * kMaxVecs);
-  nrm2 = (double *)ctx.alloc(sizeof(double) * kMaxVecs);
+  nrm2 = (double *)ctx.alloc(sizeof(double) * (kMaxVecs + 2));
   ptrs = (const double **)ctx.alloc(sizeof(double *) * kMaxVecs);
+  step = (int *)ctx.alloc(sizeof(int));
+  const size_t vbytes = sizeof(double) * std::max<int64_t>(1, n * (cplx ? 2 : 1));
+  X = (double *)ctx.alloc(vbytes);
+  Y = (double *)ctx.alloc(vbytes);
   UDMRG_CHECK_CUDA(cudaMallocHost((void **)&hptrs, sizeof(double *) * kMaxVecs));
-  UDMRG_CHECK_CUDA(cudaMallocHost((void **)&hres, sizeof(double) * 4));
+  UDMRG_CHECK_CUDA(cudaHostAlloc((void **)&hres, sizeof(double) * 4, cudaHostAllocMapped));
+  UDMRG_CHECK_CUDA(cudaHostGetDevicePointer((void **)&dres, hres, 0));
 }
 
 KrylovWork::~KrylovWork() {
@@ -441,80 +497,96 @@ KrylovWork::~KrylovWork() {
   ctx.free(alpha);
   ctx.free(nrm2);
   ctx.free((void *)ptrs);
+  ctx.free(step);
+  ctx.free(X);
+  ctx.free(Y);
 }
 
 void KrylovWork::push(int j, const double *v) {
-  UDMRG_REQUIRE(j < kMaxVecs, "Krylov basis: too many vectors");
+  UDMRG_REQUIRE(j < mcap, "Krylov basis: more vectors than the solve's step limit");
   hptrs[j] = v;
   UDMRG_CHECK_CUDA(cudaMemcpyAsync((void *)(ptrs + j), (const void *)(hptrs + j),
                                    sizeof(double *), cudaMemcpyHostToDevice, ctx.stream));
 }
 
-void krylov_alpha(KrylovWork &k, int j, const double *y) {
+void krylov_begin(KrylovWork &k, const double *v0) {
   Ctx &ctx = k.ctx;
-  const int g = red_grid(ctx, k.n);
-  dot_partial_kernel<<<g, kRedThreads, 0, ctx.stream>>>(k.hptrs[j], y, k.n, k.cplx ? 1 : 0,
-                                                         k.red);
-  finish_sum_kernel<<<1, kRedThreads, 0, ctx.stream>>>(k.red, g, 2, k.alpha + 2 * j);
+  const int64_t nd = k.n * (k.cplx ? 2 : 1);
+  if (nd > 0)
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(k.Y, v0, nd * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     ctx.stream));
+  UDMRG_CHECK_CUDA(cudaMemsetAsync(k.step, 0, sizeof(int), ctx.stream));
+  const int g = red_grid(ctx, nd);
+  dot_partial_kernel<<<g, kRedThreads, 0, ctx.stream>>>(k.Y, k.Y, nd, 0, k.red);
+  // the partials are (re, im) pairs: nrm2[0] = |v0|^2, nrm2[1] = 0 (step 0 overwrites it)
+  finish_step_kernel<<<1, kRedThreads, 0, ctx.stream>>>(k.red, g, 2, k.nrm2, k.step, 1, 0);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches += 2;
 }
 
-void krylov_update(KrylovWork &k, int j, double *g) {
+void krylov_normalise(KrylovWork &k) {
+  Ctx &ctx = k.ctx;
+  const int64_t nd = k.n * (k.cplx ? 2 : 1);
+  krylov_normalise_kernel<<<ew_grid(ctx, nd), 256, 0, ctx.stream>>>(k.Y, k.X, k.ptrs, k.step,
+                                                                     k.nrm2, nd);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  ctx.launches++;
+}
+
+void krylov_alpha(KrylovWork &k) {
+  Ctx &ctx = k.ctx;
+  const int g = red_grid(ctx, k.n);
+  dot_partial_kernel<<<g, kRedThreads, 0, ctx.stream>>>(k.X, k.Y, k.n, k.cplx ? 1 : 0, k.red);
+  finish_step_kernel<<<1, kRedThreads, 0, ctx.stream>>>(k.red, g, 2, k.alpha, k.step, 2, 0);
+  UDMRG_CHECK_CUDA(cudaGetLastError());
+  ctx.launches += 2;
+}
+
+void krylov_update(KrylovWork &k) {
   Ctx &ctx = k.ctx;
   const int64_t nd = k.n * (k.cplx ? 2 : 1);
   const int gr = red_grid(ctx, nd);
-  krylov_update_kernel<<<gr, kRedThreads, 0, ctx.stream>>>(
-      g, k.hptrs[j], j > 0 ? k.hptrs[j - 1] : nullptr, k.alpha + 2 * j, k.nrm2 + j, nd, k.red);
-  finish_sum_kernel<<<1, kRedThreads, 0, ctx.stream>>>(k.red, gr, 1, k.nrm2 + j + 1);
+  krylov_update_kernel<<<gr, kRedThreads, 0, ctx.stream>>>(k.Y, k.X, k.ptrs, k.step, k.alpha,
+                                                           k.nrm2, nd, k.red);
+  finish_step_kernel<<<1, kRedThreads, 0, ctx.stream>>>(k.red, gr, 1, k.nrm2, k.step, 1, 1);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches += 2;
 }
 
-void krylov_project(KrylovWork &k, int j, double *g, bool second) {
+void krylov_project(KrylovWork &k, bool second) {
   Ctx &ctx = k.ctx;
-  const int m = j + 1;
   // gate[0] = |g|^2 before the first pass, gate[1] = after it (k.gate has
   // the two slots for the current step)
   const double *gate = second ? k.gate : nullptr;
-  const size_t msm = sizeof(double) * 2 * (size_t)m * kMdWarps;
+  // shared memory for the largest basis of the solve (the step is read on the device)
+  const size_t msm = sizeof(double) * 2 * (size_t)k.mcap * kMdWarps;
   if (k.cplx)
-    multidot_kernel<true><<<k.nb, kMdThreads, msm, ctx.stream>>>(k.ptrs, m, g, k.n, k.partial,
-                                                                 gate);
+    multidot_kernel<true><<<k.nb, kMdThreads, msm, ctx.stream>>>(k.ptrs, k.step, k.Y, k.n,
+                                                                 k.partial, gate);
   else
-    multidot_kernel<false><<<k.nb, kMdThreads, msm, ctx.stream>>>(k.ptrs, m, g, k.n, k.partial,
-                                                                  gate);
-  multidot_finish_kernel<<<m, kRedThreads, 0, ctx.stream>>>(k.partial, k.nb, k.coef, gate);
+    multidot_kernel<false><<<k.nb, kMdThreads, msm, ctx.stream>>>(k.ptrs, k.step, k.Y, k.n,
+                                                                  k.partial, gate);
+  multidot_finish_kernel<<<k.mcap, kRedThreads, 0, ctx.stream>>>(k.partial, k.nb, k.coef,
+                                                                  k.step, gate);
   const int gr = red_grid(ctx, k.n);
   if (k.cplx)
-    project_kernel<true><<<gr, kRedThreads, 0, ctx.stream>>>(g, k.ptrs, k.coef, m, k.n, k.red,
-                                                             gate);
+    project_kernel<true><<<gr, kRedThreads, 0, ctx.stream>>>(k.Y, k.ptrs, k.coef, k.step, k.n,
+                                                             k.red, gate);
   else
-    project_kernel<false><<<gr, kRedThreads, 0, ctx.stream>>>(g, k.ptrs, k.coef, m, k.n, k.red,
-                                                              gate);
-  // both passes end in nrm2[j+1]; the first also sets gate = {before, after}
-  norm_finish_kernel<<<1, kRedThreads, 0, ctx.stream>>>(k.red, gr, k.nrm2 + j + 1,
+    project_kernel<false><<<gr, kRedThreads, 0, ctx.stream>>>(k.Y, k.ptrs, k.coef, k.step, k.n,
+                                                              k.red, gate);
+  // both passes end in nrm2[s+1]; the first also sets gate = {before, after}
+  norm_finish_kernel<<<1, kRedThreads, 0, ctx.stream>>>(k.red, gr, k.nrm2, k.step,
                                                         second ? nullptr : k.gate, gate);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches += 4;
 }
 
-void krylov_normalise(KrylovWork &k, int j, double *g) {
+void krylov_publish(KrylovWork &k) {
   Ctx &ctx = k.ctx;
-  const int64_t nd = k.n * (k.cplx ? 2 : 1);
-  if (nd == 0) return;
-  normalise_kernel<<<ew_grid(ctx, nd), 256, 0, ctx.stream>>>(g, nd, k.nrm2 + j + 1);
+  krylov_publish_kernel<<<1, 1, 0, ctx.stream>>>(k.alpha, k.nrm2, k.step, k.dres);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches++;
-}
-
-void krylov_fetch(KrylovWork &k, int j) {
-  Ctx &ctx = k.ctx;
-  UDMRG_CHECK_CUDA(cudaMemcpyAsync(k.hres, k.alpha + 2 * j, sizeof(double),
-                                   cudaMemcpyDeviceToHost, ctx.stream));
-  UDMRG_CHECK_CUDA(cudaMemcpyAsync(k.hres + 1, k.nrm2 + j + 1, sizeof(double),
-                                   cudaMemcpyDeviceToHost, ctx.stream));
-  ctx.sync();
 }
 
 void conj_inplace(Ctx &ctx, double *x, int64_t n_cplx) {

@@ -30,43 +30,51 @@ void lincomb(VecWork &w, double *out, const std::vector<const double *> &vecs,
 void conj_inplace(Ctx &ctx, double *x, int64_t n_cplx);
 void real_to_complex(Ctx &ctx, const double *x, double *y, int64_t n);
 
-// Krylov basis with device-resident step scalars: the three-term update, the
-// projection against the whole basis and the normalisation read their
-// coefficients from device memory, so a Lanczos step needs one host
-// synchronisation (to read alpha and |gamma|^2 for the tridiagonal matrix).
+// Krylov basis with device-resident step scalars.  Every kernel of a step
+// reads the step index s from device memory (KrylovWork::step) and works on
+// two fixed buffers (X = v_s, the matvec input; Y = H v_s, which becomes
+// gamma_s), so the launch sequence of a step is the same for every s and is
+// captured once as a CUDA graph.  One host synchronisation per step reads
+// alpha_s and |gamma_s|^2 for the tridiagonal matrix.
 struct KrylovWork {
   Ctx &ctx;
   int64_t n = 0;  // elements (complex or real)
   bool cplx = false;
+  int mcap = 0;                     // largest basis a projection sees (steps + 1)
   int nb = 0;                       // blocks of the multi-dot kernel
-  double *partial = nullptr;        // kMaxVecs x nb x 2 multi-dot partials
+  double *partial = nullptr;        // mcap x nb x 2 multi-dot partials
   double *red = nullptr;            // reduction partials of the fused norms
   double *gate = nullptr;           // |gamma|^2 before / after the first projection
   double *coef = nullptr;           // kMaxVecs x 2 projection coefficients
-  double *alpha = nullptr;          // kMaxVecs x 2: <v_j | H v_j>
-  double *nrm2 = nullptr;           // kMaxVecs: |gamma_j|^2
+  double *alpha = nullptr;          // kMaxVecs x 2: <v_s | H v_s>
+  double *nrm2 = nullptr;           // kMaxVecs + 2: nrm2[s] = |gamma_{s-1}|^2 (s = 0: |v0|^2)
   const double **ptrs = nullptr;    // device array of the basis pointers
   const double **hptrs = nullptr;   // pinned mirror (entries written once)
-  double *hres = nullptr;           // pinned host results
-  KrylovWork(Ctx &c, int64_t n_elems, bool complex_data);
+  int *step = nullptr;              // device: the step the next launch sequence runs
+  double *X = nullptr, *Y = nullptr;
+  double *hres = nullptr;  // mapped pinned: {alpha_s, |gamma_s|^2, |gamma_{s-1}|^2}
+  double *dres = nullptr;  // device alias of hres
+  // max_steps: the most steps a solve may run (its Krylov dimension cap)
+  KrylovWork(Ctx &c, int64_t n_elems, bool complex_data, int64_t max_steps);
   ~KrylovWork();
-  // registers basis vector j (j = number of vectors so far)
+  // registers basis vector j; the step j normalisation writes it
   void push(int j, const double *v);
 };
-// Scalars on the device: alpha[j] = <v_j | H v_j>; nrm2[i] = |gamma|^2 of the
-// vector that becomes v_i.
-// alpha[j] = <v_j | y>
-void krylov_alpha(KrylovWork &k, int j, const double *y);
-// g (= H v_j on entry) -= Re(alpha[j]) v_j + sqrt(nrm2[j]) v_{j-1} (the
-// second term when j > 0); nrm2[j+1] = |g|^2
-void krylov_update(KrylovWork &k, int j, double *g);
-// g -= sum_{i <= j} <v_i | g> v_i (one classical Gram-Schmidt pass);
-// nrm2[j+1] = |g|^2.  The second pass runs (decided on the device) only if
-// the first one reduced |g|^2 below half its value.
-void krylov_project(KrylovWork &k, int j, double *g, bool second);
-// g /= sqrt(nrm2[j+1]) (unchanged when that norm is zero)
-void krylov_normalise(KrylovWork &k, int j, double *g);
-// hres[0] = Re alpha[j], hres[1] = nrm2[j+1]; synchronises the stream
-void krylov_fetch(KrylovWork &k, int j);
+// Y = v0 (a copy), nrm2[0] = |v0|^2, step = 0
+void krylov_begin(KrylovWork &k, const double *v0);
+// v_s = Y / sqrt(nrm2[s]) (Y itself when that norm is zero), written to the
+// registered basis vector s and to X
+void krylov_normalise(KrylovWork &k);
+// alpha[s] = <X | Y>
+void krylov_alpha(KrylovWork &k);
+// Y -= Re(alpha[s]) X + sqrt(nrm2[s]) v_{s-1} (the second term when s > 0);
+// nrm2[s+1] = |Y|^2
+void krylov_update(KrylovWork &k);
+// Y -= sum_{i <= s} <v_i | Y> v_i (one classical Gram-Schmidt pass);
+// nrm2[s+1] = |Y|^2.  The second pass runs (decided on the device) only if
+// the first one reduced |Y|^2 below half its value.
+void krylov_project(KrylovWork &k, bool second);
+// hres = {Re alpha[s], nrm2[s+1], nrm2[s]}; step = s + 1
+void krylov_publish(KrylovWork &k);
 
 }  // namespace udmrg
