@@ -23,6 +23,9 @@ reference's MPO conventions:
 The generator in the reference additionally compresses the channel graph; this
 one does prefix sharing only, so its bond dimension can differ from the
 reference's for the same Hamiltonian (the operator it represents is the same).
+The Hamiltonian builders below take ``builder="reference"`` to use
+``mpogen`` instead, the reference's generator restated, whose MPOs have the
+reference's bond layout.
 """
 from __future__ import annotations
 
@@ -326,14 +329,52 @@ class MPOGenerator:
         return mpo
 
 
+class _ReferenceLayoutGenerator:
+    """The builder calls of this module on ``mpogen.MPOGenerator`` (the
+    reference's compressing generator): MPOs with the reference's bond
+    dimensions, sector order and channel order."""
+
+    def __init__(self, sites: Sequence[Index], ops_id: Sequence[Operator], dtype=np.float64):
+        from .mpogen import MPOGenerator as RefGen
+        self.g = RefGen(sites, [o.mat for o in ops_id], dtype=dtype)
+
+    def add_term(self, coef, ops: Sequence[Operator], sites: Sequence[int], insts=None):
+        if insts is not None and not isinstance(insts, (list, tuple)):
+            insts = [insts] * (len(ops) - 1)
+        if insts is None or all(i is None for i in insts):
+            self.g.add_term(coef, [o.mat for o in ops], list(sites))
+        else:
+            self.g.add_term_insert(coef, [o.mat for o in ops], list(sites),
+                                   [o.mat for o in insts])
+
+    def add_two_site(self, coef, op1, s1, op2, s2, inst=None):
+        self.g.add_two_body(coef, op1.mat, s1, op2.mat, s2, None if inst is None else inst.mat)
+
+    def gen(self) -> List[BlockTensorData]:
+        return self.g.gen()
+
+
+BUILDERS = ("prefix", "reference")
+
+
+def _generator(builder: str, sites, ops_id, dtype):
+    """builder "prefix": this module's prefix-sharing generator; "reference":
+    the reference's FSM generator with symbolic compression (``mpogen``)."""
+    if builder == "prefix":
+        return MPOGenerator(sites, ops_id, dtype)
+    if builder == "reference":
+        return _ReferenceLayoutGenerator(sites, ops_id, dtype)
+    raise ValueError(f"unknown MPO builder {builder!r}")
+
+
 # ---------------------------------------------------------------------------
-# Hamiltonians used by the tests and the benchmark
+# Hamiltonians used by the tests and the benchmark (builder: see _generator)
 # ---------------------------------------------------------------------------
 
 
-def heisenberg_chain_mpo(N, J=1.0, dtype=np.float64, pairs=None):
+def heisenberg_chain_mpo(N, J=1.0, dtype=np.float64, pairs=None, builder="prefix"):
     pb, ops = spin_half_site(dtype)
-    g = MPOGenerator([pb] * N, [ops["id"]] * N, dtype)
+    g = _generator(builder, [pb] * N, [ops["id"]] * N, dtype)
     if pairs is None:
         pairs = [(i, i + 1) for i in range(N - 1)]
     for (i, j) in pairs:
@@ -358,20 +399,20 @@ def spinless_fermion_site(dtype=np.float64):
     return pb_out, ops
 
 
-def free_fermion_chain_mpo(N, t=1.0, dtype=np.float64):
+def free_fermion_chain_mpo(N, t=1.0, dtype=np.float64, builder="prefix"):
     """H = -t sum_i (c^dag_i c_{i+1} + c_i c^dag_{i+1}) on an open chain
     (``test_two_site_finite_tdvp.cc:108-113``)."""
     pb, ops = spinless_fermion_site(dtype)
-    g = MPOGenerator([pb] * N, [ops["id"]] * N, dtype)
+    g = _generator(builder, [pb] * N, [ops["id"]] * N, dtype)
     for i in range(N - 1):
         g.add_two_site(-t, ops["cdag"], i, ops["c"], i + 1)
         g.add_two_site(-t, ops["c"], i, ops["cdag"], i + 1)
     return g.gen(), pb, ops
 
 
-def ising_chain_mpo(N, dtype=np.float64):
+def ising_chain_mpo(N, dtype=np.float64, builder="prefix"):
     pb, ops = spin_half_site(dtype)
-    g = MPOGenerator([pb] * N, [ops["id"]] * N, dtype)
+    g = _generator(builder, [pb] * N, [ops["id"]] * N, dtype)
     for i in range(N - 1):
         g.add_two_site(1.0, ops["sz"], i, ops["sz"], i + 1)
     return g.gen(), pb
@@ -390,12 +431,12 @@ def heisenberg_ladder_pairs(Lx, Ly=2):
     return pairs
 
 
-def hubbard_cylinder_mpo(Lx, Ly, t=1.0, U=8.0, t2=0.0, dtype=np.float64):
+def hubbard_cylinder_mpo(Lx, Ly, t=1.0, U=8.0, t2=0.0, dtype=np.float64, builder="prefix"):
     """Hubbard cylinder (open x, periodic y) with the site map and hopping terms
     of ``benchmark/ultradmrg_hubbard2d.cpp:138-202`` (site = x*Ly + y)."""
     pb, o = hubbard_site_nsz(dtype)
     N = Lx * Ly
-    g = MPOGenerator([pb] * N, [o["id"]] * N, dtype)
+    g = _generator(builder, [pb] * N, [o["id"]] * N, dtype)
     f = o["f"]
 
     def hop(tt, s1, s2, inst):
@@ -437,11 +478,11 @@ def hubbard_cylinder_holes(N, n_holes_per=8):
     return labs
 
 
-def hubbard_2x2_test_mpo(dtype=np.float64, t0=1.0, t1=0.5, U=2.0, Nx=2, Ny=2):
+def hubbard_2x2_test_mpo(dtype=np.float64, t0=1.0, t1=0.5, U=2.0, Nx=2, Ny=2, builder="prefix"):
     """Hubbard model of ``test_two_site_update_finite_vmps.cc:848-905``."""
     pb, o = hubbard_site_nupndn(dtype)
     N = Nx * Ny
-    g = MPOGenerator([pb] * N, [o["id"]] * N, dtype)
+    g = _generator(builder, [pb] * N, [o["id"]] * N, dtype)
     f = o["f"]
     idx = lambda i, j: i * Ny + j
 
