@@ -10,7 +10,9 @@ writes ``reference_goldens.json`` next to this script:
 * the MATLAB known answers of ``TridiagExpme1Solver``
   (``tests/test_algorithm/test_lanczos_expmv_solver.cc:70-109``);
 * the TDVP free-fermion ground-state energy
-  (``tests/test_algorithm/test_two_site_finite_tdvp.cc``).
+  (``tests/test_algorithm/test_two_site_finite_tdvp.cc``);
+* the entanglement entropies of the N = 6 Heisenberg ground state, bond by
+  bond (``tests/test_one_dim_tn/test_finite_mps/test_finite_mps.cc:304-333``).
 
 Usage: python tests/golden/extract_reference_goldens.py [reference_root]
 """
@@ -81,6 +83,14 @@ def main():
     gs = re.search(r"(-3\.49395920743493\d*)", tdvp)
     if gs:
         goldens["tdvp_free_fermion_gs"] = float(gs.group(1))
+    fmps = read("tests/test_one_dim_tn/test_finite_mps/test_finite_mps.cc")
+    ee = re.search(r"ee_list_std\s*=\s*\{([^}]*)\}", fmps)
+    ee_tol = re.search(r"EXPECT_NEAR\(ee_list\[i\],\s*ee_list_std\[i\],\s*([0-9.eE-]+)\)", fmps)
+    ee_sweep = re.search(r"Test1DHeisenbergEntanglementEntropy.*?FiniteVMPSSweepParams\((.*?)\);",
+                         fmps, re.S)
+    goldens["ee_heisenberg6"] = {
+        "ee": fl(ee.group(1)), "tol": float(ee_tol.group(1)),
+        "sweep_params": " ".join(ee_sweep.group(1).split())}
     with open(os.path.join(HERE, "reference_goldens.json"), "w") as f:
         json.dump(goldens, f, indent=1)
     print(json.dumps(goldens, indent=1))
