@@ -15,6 +15,10 @@ the device sweeps, never a product code path.
 * ``measure_two_site_op_group`` follows ``MeasureTwoSiteOpGroup``
   (``finite_mps_measu_disk.h``).  One first site is paired with a list of
   second sites, with a uniform insertion operator in between.
+* ``cal_psi1_op_psi2`` follows ``CalPsi1OpPsi2``
+  (``algorithm/tdvp/two_site_update_finite_tdvp_impl.h:540-614``): for every
+  site i, <psi2| inst_0 ... inst_{i-1} O_i |psi1> between two MPS, not
+  normalised.
 * ``entanglement_entropy`` follows ``FiniteMPS::GetEntanglementEntropy``
   (``one_dim_tn/mps/finite_mps/finite_mps.h:277-310``).  It returns the von
   Neumann entropy -sum p ln p (n = 1) or the Renyi entropy
@@ -152,3 +156,22 @@ def _right_gram(dense, start):
         T = np.tensordot(A, G, axes=([2], [0]))                  # (b, s, r')
         G = np.tensordot(T, np.conj(A), axes=([1, 2], [1, 2]))  # (b, b')
     return G
+
+
+def cal_psi1_op_psi2(mps1, mps2, op, inst=None) -> list:
+    """res[i] = <psi2| inst_0 ... inst_{i-1} op_i |psi1> (the string only when
+    inst is given), unnormalised."""
+    d1, d2 = _dense(mps1), _dense(mps2)
+    O = _mat(op)
+    I = None if inst is None else _mat(inst)
+    out = []
+    for i in range(len(d1)):
+        E = np.ones((1, 1), dtype=np.result_type(d1[0], d2[0], O, np.float64))
+        for k, (A, B) in enumerate(zip(d1, d2)):
+            X = O if k == i else (I if (I is not None and k < i) else None)
+            T = np.tensordot(E, A, axes=([1], [0]))              # (a2, s, r1)
+            if X is not None:
+                T = np.transpose(np.tensordot(T, X, axes=([1], [0])), (0, 2, 1))
+            E = np.tensordot(np.conj(B), T, axes=([0, 1], [0, 1]))  # (r2, r1)
+        out.append(E[0, 0])
+    return out

@@ -66,3 +66,27 @@ def test_known_answers():
     sites = [[0, 1], [0, 2], [0, 5], [1, 2], [1, 3], [4, 5]]
     assert [r.avg for r in dm.measure_two_site_op(m, [ntot, ntot], idm, sites)] == \
         [0, 0, 0, 0, 1, 0]
+
+
+ORACLE2 = dm.Backend(ov.update_site_lenvs, ov.update_site_renvs, bs.contract,
+                     lambda t: t, lambda t: t, lambda t: (t.indexes, t.dtype), lambda t: None,
+                     bs.dag)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.complex128])
+def test_cal_psi1_op_psi2(dtype):
+    """<psi2| F...F O_i |psi1> between two random MPS: a neutral operator with
+    and without the string, and c^dag between states whose charges differ by
+    its charge (+2 in units where the basis states carry +1 and -1; six sites
+    reach even totals only)."""
+    pb, o = M.spinless_fermion_site(dtype)
+    f, cd = o["f"].mat, o["cdag"].mat
+    n = np.diag([0.0, 1.0]).astype(dtype)
+    a = M.random_mps([pb] * 6, (0,), 8, seed=1, dtype=dtype)
+    b = M.random_mps([pb] * 6, (0,), 8, seed=2, dtype=dtype)
+    c = M.random_mps([pb] * 6, (2,), 8, seed=3, dtype=dtype)
+    for psi1, psi2, op, inst in ((a, b, n, None), (a, b, n, f), (a, c, cd, f), (a, c, cd, None)):
+        got = dm.cal_psi1_op_psi2(ORACLE2, psi1, psi2, op, inst)
+        want = om.cal_psi1_op_psi2(psi1, psi2, op, inst)
+        assert np.abs(want).max() > 1e-3
+        assert np.allclose(got, want, atol=1e-12 * np.abs(want).max())

@@ -69,3 +69,18 @@ def test_device_measurement_of_a_device_ground_state(ctx):
     sz = dm.measure_one_site_op(m, ops["sz"].mat)
     assert abs(sum(r.avg for r in sz)) < 1e-9  # total Sz = 0 sector
     m.close()
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.complex128])
+def test_device_cal_psi1_op_psi2(ctx, dtype):
+    """CalPsi1OpPsi2 on the device (contract and dag through the C ABI)."""
+    pb, o = M.spinless_fermion_site(dtype)
+    a = M.random_mps([pb] * 6, (0,), 8, seed=1, dtype=dtype)
+    c = M.random_mps([pb] * 6, (2,), 8, seed=3, dtype=dtype)
+    da = [api.DeviceTensor.from_data(ctx, t) for t in a]
+    dc = [api.DeviceTensor.from_data(ctx, t) for t in c]
+    got = dm.cal_psi1_op_psi2(dm.device_backend(ctx), da, dc, o["cdag"].mat, o["f"].mat)
+    want = om.cal_psi1_op_psi2(a, c, o["cdag"].mat, o["f"].mat)
+    assert np.allclose(got, want, atol=1e-12 * np.abs(want).max())
+    for t in da + dc:
+        t.close()

@@ -45,7 +45,8 @@ class Backend:
     """update_left(L, A, W) / update_right(R, A, W): the sweep's environment
     updates; contract(a, b, axes_a, axes_b); upload(BlockTensorData) and
     download(t) -> BlockTensorData; info(t) -> (indexes, dtype);
-    release(t) frees a backend tensor."""
+    release(t) frees a backend tensor; dag(t) flips the index directions and
+    conjugates."""
     update_left: Callable
     update_right: Callable
     contract: Callable
@@ -53,6 +54,7 @@ class Backend:
     download: Callable
     info: Callable
     release: Callable
+    dag: Optional[Callable] = None
 
 
 def device_backend(ctx) -> Backend:
@@ -69,6 +71,7 @@ def device_backend(ctx) -> Backend:
         download=lambda t: t.to_data(),
         info=info,
         release=lambda t: t.close(),
+        dag=lambda t: api.dag(ctx, t),
     )
 
 
@@ -218,3 +221,67 @@ def measure_two_site_op_group(m: MPSMeasurer, op1, op2, site1, site2_set,
                               inst_op) -> List[MeasuResElem]:
     """``MeasureTwoSiteOpGroup``: one first site against a list of second sites."""
     return measure_two_site_op(m, [op1, op2], inst_op, [[site1, s2] for s2 in site2_set])
+
+
+def _op_data(mat, pb_out: Index, dtype) -> BlockTensorData:
+    """O[in, out] as the rank-2 tensor {pb_in, pb_out}."""
+    m = np.asarray(mat.mat if hasattr(mat, "mat") else mat)
+    t = BlockTensorData([pb_out.inverse(), pb_out], {}, dtype)
+    for a, o in np.argwhere(m != 0):
+        t.set_elem((int(a), int(o)), m[a, o])
+    return t
+
+
+def _trace(t: BlockTensorData):
+    """Trace of a matrix whose two indexes are one bond and its inverse."""
+    return np.trace(t.to_dense()) if t.blocks else 0.0
+
+
+def cal_psi1_op_psi2(b: Backend, mps1: Sequence, mps2: Sequence, op, inst=None) -> list:
+    """``CalPsi1OpPsi2`` (algorithm/tdvp/two_site_update_finite_tdvp_impl.h:540-614):
+    res[i] = <psi2| inst_0 ... inst_{i-1} op_i |psi1> for every site i (the
+    string only when inst is given), not normalised.  Right boundaries are
+    built from the right end, the left one is carried site by site; each
+    value closes the left boundary, the operator and the right boundary.
+    The final contraction keeps the ket bond open and the trace is taken on
+    the host (device tensors have rank >= 1)."""
+    N = len(mps1)
+    if len(mps2) != N or N < 1:
+        raise ValueError("two MPS of the same length")
+    i1 = [b.info(t)[0] for t in mps1]
+    i2 = [b.info(t)[0] for t in mps2]
+    dtype = np.result_type(*[b.info(t)[1] for t in list(mps1) + list(mps2)])
+    owned = []
+
+    def keep(t):
+        owned.append(t)
+        return t
+
+    def boundary(a: Index, c: Index):
+        t = BlockTensorData([a, c.inverse()], {}, dtype)
+        t.set_elem((0, 0), 1.0)
+        return keep(b.upload(t))
+
+    # right boundaries: rb[k] covers the sites >= k
+    rb = [None] * (N + 1)
+    rb[N] = boundary(i2[N - 1][2], i1[N - 1][2])
+    for k in range(N - 1, 0, -1):
+        t = keep(b.contract(keep(b.dag(mps2[k])), rb[k + 1], [2], [0]))
+        rb[k] = keep(b.contract(t, mps1[k], [1, 2], [1, 2]))
+    opt = keep(b.upload(_op_data(op, i1[0][1], dtype)))
+    instt = None if inst is None else keep(b.upload(_op_data(inst, i1[0][1], dtype)))
+    L = boundary(i2[0][0], i1[0][0])
+    res = []
+    for i in range(N):
+        t1 = keep(b.contract(keep(b.dag(mps2[i])), L, [0], [0]))
+        t2 = keep(b.contract(opt, t1, [1], [0]))
+        t3 = keep(b.contract(t2, mps1[i], [2, 0], [0, 1]))
+        t4 = b.contract(t3, rb[i + 1], [0], [0])
+        res.append(_trace(b.download(t4)))
+        b.release(t4)
+        if i < N - 1:
+            src = t1 if instt is None else keep(b.contract(instt, t1, [1], [0]))
+            L = keep(b.contract(src, mps1[i], [2, 0], [0, 1]))
+    for t in owned:
+        b.release(t)
+    return res
