@@ -90,3 +90,24 @@ def test_cal_psi1_op_psi2(dtype):
         want = om.cal_psi1_op_psi2(psi1, psi2, op, inst)
         assert np.abs(want).max() > 1e-3
         assert np.allclose(got, want, atol=1e-12 * np.abs(want).max())
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.complex128])
+def test_act_operator_on_mps(dtype):
+    """The host ActOperatorOnMps against the oracle's contraction of the
+    operator tensor (block keys and values) and against the state vector."""
+    from systems import act_operator, apply_dense, mps_dense
+    pb, o = M.spinless_fermion_site(dtype)
+    mps = M.random_mps([pb] * 6, (0,), 8, seed=4, dtype=dtype)
+    cd, f = o["cdag"].mat, o["f"].mat
+    got = M.act_operator_on_mps(mps, cd, f, 3)
+    want = act_operator(mps, M.operator_tensor(cd, pb), M.operator_tensor(f, pb), 3)
+    for g, w in zip(got, want):
+        assert set(g.blocks) == set(w.blocks)
+        for k in w.blocks:
+            assert np.allclose(g.blocks[k], w.blocks[k], rtol=0, atol=1e-14)
+    v = apply_dense(mps_dense(mps), cd, 3, f)
+    assert np.allclose(mps_dense(got), v, atol=1e-12)
+    # without a string only the site's tensor changes
+    only = M.act_operator_on_mps(mps, cd, None, 2)
+    assert all(a is b for i, (a, b) in enumerate(zip(only, mps)) if i != 2)

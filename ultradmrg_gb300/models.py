@@ -510,6 +510,36 @@ def hubbard_2x2_test_mpo(dtype=np.float64, t0=1.0, t1=0.5, U=2.0, Nx=2, Ny=2, bu
     return g.gen(), pb
 
 
+def act_operator_on_mps(mps: Sequence[BlockTensorData], op, inst, site: int
+                        ) -> List[BlockTensorData]:
+    """``ActOperatorOnMps`` (algorithm/tdvp/two_site_update_finite_tdvp_impl.h:23-54):
+    the operator ``op`` on ``site`` and, when ``inst`` is given, the string
+    operator on every site left of it: ``A'[l, o, r] = sum_i O[i, o] A[l, i, r]``.
+    A block (l, o-sector, r) of the result exists where the site has a block
+    (l, i-sector, r) and O has a non-zero element between the two sectors.
+    The MPS keeps its bonds; the operator's divergence moves into ``site``'s
+    tensor.  Host data in, host data out."""
+    out = list(mps)
+    todo = [(site, op)] + ([] if inst is None else [(j, inst) for j in range(site - 1, -1, -1)])
+    for i, o in todo:
+        O = np.asarray(o.mat if hasattr(o, "mat") else o)
+        A = out[i]
+        pb = A.indexes[1]
+        off = pb.offsets()
+        dtype = np.result_type(A.dtype, O.dtype)
+        blocks: Dict[Tuple[int, ...], np.ndarray] = {}
+        for (ls, ps, rs), B in A.blocks.items():
+            for so in range(pb.nsec):
+                sub = O[off[ps]:off[ps + 1], off[so]:off[so + 1]]
+                if not sub.any():
+                    continue
+                C = np.einsum("lir,io->lor", B, sub)
+                key = (ls, so, rs)
+                blocks[key] = blocks[key] + C if key in blocks else C.astype(dtype)
+        out[i] = BlockTensorData(list(A.indexes), blocks, dtype)
+    return out
+
+
 # ---------------------------------------------------------------------------
 # MPS initialisation
 # ---------------------------------------------------------------------------
