@@ -151,7 +151,7 @@ def test_learned_gain(ctx):
           f"sketch columns {s_prev} vs {s_lrn}; svd s {t_prev:.3f} vs {t_lrn:.3f}")
     assert mse_net < mse_base
     assert g_lrn < g_prev
-    # the truncation itself is unchanged: exact SVD is the judge
+    # the truncation itself is unchanged: the exact SVD decides it
     for log in (log_prev, log_lrn):
         audited = [r for r in log if r["svd_audit_err"] >= 0]
         assert len(audited) >= len(log) // 2
