@@ -190,7 +190,7 @@ def cpu_baseline(args, w):
            "--cpu-budget", str(args.cpu_budget)]
     why = ""
     try:
-        r = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=600)
+        r = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=300)
         if r.returncode == 0:
             ref = json.loads(r.stdout.strip().splitlines()[-1])
             cb = ref["cpu_baseline"]
