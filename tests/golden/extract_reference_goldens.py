@@ -12,7 +12,10 @@ writes ``reference_goldens.json`` next to this script:
 * the TDVP free-fermion ground-state energy
   (``tests/test_algorithm/test_two_site_finite_tdvp.cc``);
 * the entanglement entropies of the N = 6 Heisenberg ground state, bond by
-  bond (``tests/test_one_dim_tn/test_finite_mps/test_finite_mps.cc:304-333``).
+  bond (``tests/test_one_dim_tn/test_finite_mps/test_finite_mps.cc:304-333``);
+* the fermionic two-site VMPS energies (free fermions N = 8, t-J 1D and 2D,
+  ``tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc:80-270``)
+  with their sweep parameters and initial product states.
 
 Usage: python tests/golden/extract_reference_goldens.py [reference_root]
 """
@@ -39,6 +42,25 @@ def case_energies(src, case):
         args = [a.strip() for a in mm.group(1).split(",")]
         out.append((args[-2], args[-1]))
     return out
+
+
+def fixture_case(src, fixture, case):
+    """Body of TEST_F(fixture, case)."""
+    m = re.search(r"TEST_F\(\s*%s\s*,\s*%s\s*\)(.*?)(?=\nTEST_F|\nTEST\(|\Z)" % (fixture, case),
+                  src, re.S)
+    return m.group(1)
+
+
+def sweep_case(body):
+    """(energy, tol, sweep-parameter text, initial labels) of the first
+    RunTest*Case in a test body."""
+    e = re.search(r"RunTest\w*Case\((.*?)\);", body, re.S).group(1)
+    args = [a.strip() for a in e.split(",")]
+    p = re.search(r"FiniteVMPSSweepParams\((.*?)\);", body, re.S).group(1)
+    labs = re.search(r"DirectStateInit\w*\(\s*\w+\s*,\s*\{([^}]*)\}", body).group(1)
+    return {"energy": float(args[-2]), "tol": float(args[-1]),
+            "sweep_params": " ".join(p.split()),
+            "labels": [int(x) for x in labs.split(",")]}
 
 
 def num(s):
@@ -91,6 +113,13 @@ def main():
     goldens["ee_heisenberg6"] = {
         "ee": fl(ee.group(1)), "tol": float(ee_tol.group(1)),
         "sweep_params": " ".join(ee_sweep.group(1).split())}
+    ferm = read("tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc")
+    goldens["fermion_vmps"] = {
+        "free_fermion8": sweep_case(fixture_case(ferm, "TestTwoSiteAlgorithmSpinlessFermion",
+                                                 "1DFreeFermion")),
+        "tj1d": sweep_case(fixture_case(ferm, "TestTwoSiteAlgorithmTjSystem2U1Symm", "1DCase")),
+        "tj2d": sweep_case(fixture_case(ferm, "TestTwoSiteAlgorithmTjSystem2U1Symm", "2DCase")),
+    }
     with open(os.path.join(HERE, "reference_goldens.json"), "w") as f:
         json.dump(goldens, f, indent=1)
     print(json.dumps(goldens, indent=1))

@@ -141,3 +141,55 @@ def test_svd_truncation_rule():
     assert abs(err - 0.0025 / tot) < 1e-15
     kept, D, _ = bs.select_kept(sv, 1e-2, 1, 2)
     assert D == 2 and kept == [2, 0]  # tie 0.3/0.3 broken by sector order
+
+
+# ---- fermionic two-site goldens (test_fermion_two_site_update_finite_vmps.cc) ----
+# The reference runs these with fermionic tensors; here the same Hamiltonians
+# carry explicit Jordan-Wigner strings.  A dense exact diagonalisation of each
+# MPO pins the Hamiltonian, the oracle sweep with the reference's parameters
+# and initial product state pins the energy.
+
+FERMION = {
+    "free_fermion8": lambda dt: M.free_fermion_chain_mpo(8, dtype=dt)[:2],
+    "tj1d": lambda dt: M.tj_mpo(4, dtype=dt),
+    "tj2d": lambda dt: M.tj_mpo(4, pairs=[(0, 1), (0, 2), (2, 3), (1, 3)], dtype=dt),
+}
+
+
+def _sweep_params(text):
+    """FiniteVMPSSweepParams(sweeps, Dmin, Dmax, trunc, LanczosParams(err, max_it))."""
+    import re
+    nums = [float(x) for x in re.findall(r"[-0-9.]+(?:[eE][-+]?[0-9]+)?", text)]
+    sweeps, dmin, dmax, trunc, err = nums[:5]
+    it = int(nums[5]) if len(nums) > 5 else 200
+    return vmps.FiniteVMPSSweepParams(int(sweeps), int(dmin), int(dmax), trunc,
+                                      krylov.LanczosParams(err, it))
+
+
+def _sector_ground_energy(mpo, pb, labels):
+    import itertools
+    from test_mpogen import mpo_dense
+    N = len(labels)
+    qs = [pb.qns[pb.sector_of(i)[0]] for i in range(pb.dim)]
+    tgt = tuple(np.sum([qs[x] for x in labels], axis=0))
+    idx = [k for k, c in enumerate(itertools.product(range(pb.dim), repeat=N))
+           if tuple(np.sum([qs[x] for x in c], axis=0)) == tgt]
+    H = mpo_dense(mpo)[np.ix_(idx, idx)]
+    return np.linalg.eigvalsh((H + H.conj().T) / 2)[0]
+
+
+@pytest.mark.parametrize("case", sorted(FERMION))
+def test_fermion_hamiltonians_by_exact_diagonalisation(case):
+    g = GOLD["fermion_vmps"][case]
+    mpo, pb = FERMION[case](np.float64)
+    assert abs(_sector_ground_energy(mpo, pb, g["labels"]) - g["energy"]) < max(g["tol"], 1e-11)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.complex128])
+@pytest.mark.parametrize("case", sorted(FERMION))
+def test_fermion_vmps_goldens(case, dtype):
+    g = GOLD["fermion_vmps"][case]
+    mpo, pb = FERMION[case](dtype)
+    mps = M.direct_product_mps([pb] * len(g["labels"]), g["labels"], dtype=dtype)
+    e = vmps.two_site_finite_vmps(mps, mpo, _sweep_params(g["sweep_params"]))
+    assert abs(e - g["energy"]) < g["tol"]

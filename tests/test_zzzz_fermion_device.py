@@ -1,0 +1,54 @@
+"""The fermionic two-site VMPS goldens through the device sweep
+(``tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc``): free
+fermions N = 8, t-J 1D and 2D with explicit Jordan-Wigner strings, the
+reference's sweep parameters and initial product states, real and complex.
+The host side (the Hamiltonians by exact diagonalisation, the oracle sweeps)
+is pinned in ``test_oracle_golden.py``.  The file name sorts last so that a
+run stopping at the first failure has run every other test before this one.
+"""
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+from ultradmrg_gb300 import api, models as M
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_goldens.json")))
+
+FERMION = {
+    "free_fermion8": lambda dt: M.free_fermion_chain_mpo(8, dtype=dt)[:2],
+    "tj1d": lambda dt: M.tj_mpo(4, dtype=dt),
+    "tj2d": lambda dt: M.tj_mpo(4, pairs=[(0, 1), (0, 2), (2, 3), (1, 3)], dtype=dt),
+}
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from ultradmrg_gb300 import build
+    build.build()
+    c = api.Context(0)
+    yield c
+    c.close()
+
+
+def _params(text):
+    nums = [float(x) for x in re.findall(r"[-0-9.]+(?:[eE][-+]?[0-9]+)?", text)]
+    sweeps, dmin, dmax, trunc, err = nums[:5]
+    it = int(nums[5]) if len(nums) > 5 else 200
+    return api.FiniteVMPSSweepParams(int(sweeps), int(dmin), int(dmax), trunc, err, it)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.complex128])
+@pytest.mark.parametrize("case", sorted(FERMION))
+def test_fermion_vmps_goldens_device(ctx, case, dtype):
+    g = GOLD["fermion_vmps"][case]
+    mpo, pb = FERMION[case](dtype)
+    mps = [api.DeviceTensor.from_data(ctx, t)
+           for t in M.direct_product_mps([pb] * len(g["labels"]), g["labels"], dtype=dtype)]
+    e0, _ = api.two_site_finite_vmps(ctx, mps, [api.DeviceTensor.from_data(ctx, w) for w in mpo],
+                                     _params(g["sweep_params"]))
+    assert abs(e0 - g["energy"]) < g["tol"]

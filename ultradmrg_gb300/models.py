@@ -418,6 +418,53 @@ def ising_chain_mpo(N, dtype=np.float64, builder="prefix"):
     return g.gen(), pb
 
 
+def tj_site(dtype=np.float64):
+    """t-J site with U(1)xU(1) (N, Sz): basis [up (1,1), down (1,-1), empty (0,0)];
+    operator tables of ``tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc:110-160``
+    (``cup`` sets {0,2}: up -> empty; ``sp`` sets {1,0}: down -> up) and the
+    on-site parity ``f = diag(-1, -1, 1)``."""
+    pb_out = Index.make([((1, 1), 1), ((1, -1), 1), ((0, 0), 1)], OUT)
+    e = lambda name, t: _op(name, 3, t, dtype)
+    ops = {
+        "id": e("id", {(0, 0): 1, (1, 1): 1, (2, 2): 1}),
+        "f": e("f", {(0, 0): -1, (1, 1): -1, (2, 2): 1}),
+        "sz": e("sz", {(0, 0): 0.5, (1, 1): -0.5}),
+        "sp": e("sp", {(1, 0): 1}),
+        "sm": e("sm", {(0, 1): 1}),
+        "cup": e("cup", {(0, 2): 1}),
+        "cdagup": e("cdagup", {(2, 0): 1}),
+        "cdn": e("cdn", {(1, 2): 1}),
+        "cdagdn": e("cdagdn", {(2, 1): 1}),
+    }
+    return pb_out, ops
+
+
+def tj_mpo(N, t=3.0, J=1.0, pairs=None, dtype=np.float64, builder="prefix"):
+    """t-J model of ``test_fermion_two_site_update_finite_vmps.cc:162-270``:
+    sum over bonds (i < j) of t (c^dag_i c_j - c_i c^dag_j) per spin plus
+    J (Sz Sz + (S+ S- + S- S+) / 2).  The reference's fermionic tensors carry
+    the signs; here they are explicit Jordan-Wigner strings:
+    c^dag_i c_j = (c^dag f)_i f_{i+1} ... f_{j-1} c_j, where the operator
+    product (c^dag f) applies f first (the matrix f @ c^dag in the [in, out]
+    layout)."""
+    pb, o = tj_site(dtype)
+    g = _generator(builder, [pb] * N, [o["id"]] * N, dtype)
+    f = o["f"]
+    if pairs is None:
+        pairs = [(i, i + 1) for i in range(N - 1)]
+    after_f = lambda op: Operator(op.name + "F", f.mat @ op.mat)
+    for (i, j) in pairs:
+        i, j = min(i, j), max(i, j)
+        inst = f if j - i > 1 else None
+        for s in ("up", "dn"):
+            g.add_term(t, [after_f(o["cdag" + s]), o["c" + s]], [i, j], inst)
+            g.add_term(-t, [after_f(o["c" + s]), o["cdag" + s]], [i, j], inst)
+        g.add_two_site(J, o["sz"], i, o["sz"], j)
+        g.add_two_site(J / 2, o["sp"], i, o["sm"], j)
+        g.add_two_site(J / 2, o["sm"], i, o["sp"], j)
+    return g.gen(), pb
+
+
 def heisenberg_ladder_pairs(Lx, Ly=2):
     """Nearest-neighbour bonds of an Lx x Ly open ladder, site = x*Ly + y."""
     pairs = []
