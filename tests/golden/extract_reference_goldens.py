@@ -15,7 +15,10 @@ writes ``reference_goldens.json`` next to this script:
   bond (``tests/test_one_dim_tn/test_finite_mps/test_finite_mps.cc:304-333``);
 * the fermionic two-site VMPS energies (free fermions N = 8, t-J 1D and 2D,
   ``tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc:80-270``)
-  with their sweep parameters and initial product states.
+  with their sweep parameters and initial product states;
+* the FiniteDMRG energy of the J-K-Gamma model without symmetry
+  (``tests/test_algorithm/test_finite_dmrg.cc:346-444``; its initial state
+  alternates up and down from site 0).
 
 Usage: python tests/golden/extract_reference_goldens.py [reference_root]
 """
@@ -120,6 +123,18 @@ def main():
         "tj1d": sweep_case(fixture_case(ferm, "TestTwoSiteAlgorithmTjSystem2U1Symm", "1DCase")),
         "tj2d": sweep_case(fixture_case(ferm, "TestTwoSiteAlgorithmTjSystem2U1Symm", "2DCase")),
     }
+    kit = re.search(r"TEST\(\s*TestTwoSiteAlgorithmNoSymmetrySpinSystem\s*,\s*"
+                    r"2DKitaevComplexCase\s*\)(.*?)(?=\nTEST_F|\nTEST\(|\nstruct|\Z)", dmrg,
+                    re.S).group(1)
+    e = [a.strip() for a in re.search(r"RunTestDMRGCase\((.*?)\);", kit, re.S).group(1).split(",")]
+    par = lambda name: float(re.search(r"double\s+%s\s*=\s*([-0-9.eE]+);" % name, kit).group(1))
+    size = re.search(r"size_t\s+Nx\s*=\s*(\d+)\s*,\s*Ny\s*=\s*(\d+);", kit)
+    goldens["dmrg_kitaev_gamma"] = {
+        "energy": float(e[-2]), "tol": float(e[-1]),
+        "sweep_params": " ".join(re.search(r"FiniteVMPSSweepParams\((.*?)\);", kit,
+                                           re.S).group(1).split()),
+        "J": par("J"), "K": par("K"), "Gm": par("Gm"), "h": par("h"),
+        "Nx": int(size.group(1)), "Ny": int(size.group(2))}
     with open(os.path.join(HERE, "reference_goldens.json"), "w") as f:
         json.dump(goldens, f, indent=1)
     print(json.dumps(goldens, indent=1))

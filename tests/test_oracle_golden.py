@@ -193,3 +193,29 @@ def test_fermion_vmps_goldens(case, dtype):
     mps = M.direct_product_mps([pb] * len(g["labels"]), g["labels"], dtype=dtype)
     e = vmps.two_site_finite_vmps(mps, mpo, _sweep_params(g["sweep_params"]))
     assert abs(e - g["energy"]) < g["tol"]
+
+
+def _kitaev():
+    g = GOLD["dmrg_kitaev_gamma"]
+    mpo, pb = M.kitaev_gamma_mpo(g["Nx"], g["Ny"], g["J"], g["K"], g["Gm"], g["h"])
+    return g, mpo, pb
+
+
+def test_kitaev_gamma_by_exact_diagonalisation():
+    """test_finite_dmrg.cc:346-444 (no symmetry, complex, 12 sites): the
+    ground energy of the dense Hamiltonian (4096 states)."""
+    from test_mpogen import mpo_dense
+    g, mpo, _ = _kitaev()
+    H = mpo_dense(mpo)
+    assert np.allclose(H, H.conj().T, atol=1e-13)
+    assert abs(np.linalg.eigvalsh(H)[0] - g["energy"]) < g["tol"]
+
+
+def test_kitaev_gamma_oracle_sweep():
+    """The same energy from the oracle's two-site sweep with the test's
+    parameters (D = 60, truncation 1e-4) from the alternating product state."""
+    g, mpo, pb = _kitaev()
+    N = g["Nx"] * g["Ny"]
+    mps = M.direct_product_mps([pb] * N, [i % 2 for i in range(N)], dtype=np.complex128)
+    e = vmps.two_site_finite_vmps(mps, mpo, _sweep_params(g["sweep_params"]))
+    assert abs(e - g["energy"]) < g["tol"]

@@ -1,7 +1,14 @@
-"""The fermionic two-site VMPS goldens through the device sweep
-(``tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc``): free
-fermions N = 8, t-J 1D and 2D with explicit Jordan-Wigner strings, the
-reference's sweep parameters and initial product states, real and complex.
+"""Golden energies through the device drivers:
+
+* the fermionic two-site VMPS goldens
+  (``tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc``): free
+  fermions N = 8, t-J 1D and 2D with explicit Jordan-Wigner strings, real
+  and complex;
+* the FiniteDMRG golden of the J-K-Gamma model without symmetry
+  (``tests/test_algorithm/test_finite_dmrg.cc:346-444``): one sector of
+  dimension 2 per site and an MPO with imaginary entries.
+
+Each runs with the reference's sweep parameters and initial product states.
 The host side (the Hamiltonians by exact diagonalisation, the oracle sweeps)
 is pinned in ``test_oracle_golden.py``.  The file name sorts last so that a
 run stopping at the first failure has run every other test before this one.
@@ -51,4 +58,15 @@ def test_fermion_vmps_goldens_device(ctx, case, dtype):
            for t in M.direct_product_mps([pb] * len(g["labels"]), g["labels"], dtype=dtype)]
     e0, _ = api.two_site_finite_vmps(ctx, mps, [api.DeviceTensor.from_data(ctx, w) for w in mpo],
                                      _params(g["sweep_params"]))
+    assert abs(e0 - g["energy"]) < g["tol"]
+
+
+def test_kitaev_gamma_finite_dmrg_device(ctx):
+    g = GOLD["dmrg_kitaev_gamma"]
+    mpo, pb = M.kitaev_gamma_mpo(g["Nx"], g["Ny"], g["J"], g["K"], g["Gm"], g["h"])
+    N = g["Nx"] * g["Ny"]
+    mps = [api.DeviceTensor.from_data(ctx, t)
+           for t in M.direct_product_mps([pb] * N, [i % 2 for i in range(N)],
+                                         dtype=np.complex128)]
+    e0, _ = api.finite_dmrg(ctx, mps, M.mat_repr_mpo(mpo), _params(g["sweep_params"]))
     assert abs(e0 - g["energy"]) < g["tol"]

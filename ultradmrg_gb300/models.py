@@ -418,6 +418,60 @@ def ising_chain_mpo(N, dtype=np.float64, builder="prefix"):
     return g.gen(), pb
 
 
+def spin_half_site_nosym(dtype=np.complex128):
+    """S=1/2 without symmetry: one sector of dimension 2 (a trivial quantum
+    number), basis [up, down]; the operator tables of
+    ``include/qlmps/model_relevant/operators/spin/spin_one_half_operators.h``
+    (``sp`` sets {down, up}; ``sx``, and ``sy`` with <up|Sy|down> = -i/2)."""
+    pb_out = Index.make([((0,), 2)], OUT)
+    e = lambda name, t: _op(name, 2, t, dtype)
+    ops = {
+        "id": e("id", {(0, 0): 1, (1, 1): 1}),
+        "sz": e("sz", {(0, 0): 0.5, (1, 1): -0.5}),
+        "sp": e("sp", {(1, 0): 1}),
+        "sm": e("sm", {(0, 1): 1}),
+        "sx": e("sx", {(1, 0): 0.5, (0, 1): 0.5}),
+    }
+    if np.issubdtype(np.dtype(dtype), np.complexfloating):
+        ops["sy"] = e("sy", {(1, 0): -0.5j, (0, 1): 0.5j})
+    return pb_out, ops
+
+
+def kitaev_gamma_mpo(Nx=3, Ny=4, J=-1.0, K=1.0, Gm=0.1, h=0.1, dtype=np.complex128,
+                     builder="prefix"):
+    """The J-K-Gamma model with a field of ``tests/test_algorithm/test_finite_dmrg.cc:346-436``
+    (no symmetry, complex): sites x * Ny + y; per site -h (Sz + Sx + Sy); x
+    links (y even, to y + 1) J S.S + K Sx Sx + Gm (Sz Sy + Sy Sz); z links
+    (y odd, to (y + 1) mod Ny) J S.S + K Sz Sz + Gm (Sx Sy + Sy Sx); y links
+    (y odd, x < Nx - 1, to (x + 1, y - 1)) J S.S + K Sy Sy + Gm (Sz Sx + Sx Sz)."""
+    pb, o = spin_half_site_nosym(dtype)
+    N = Nx * Ny
+    g = _generator(builder, [pb] * N, [o["id"]] * N, dtype)
+    idx = lambda x, y: x * Ny + y
+    sx, sy, sz = o["sx"], o["sy"], o["sz"]
+
+    def bond(s0, s1, kit, gam):
+        s0, s1 = min(s0, s1), max(s0, s1)
+        for a in (sz, sx, sy):
+            g.add_two_site(J, a, s0, a, s1)
+        g.add_two_site(K, kit, s0, kit, s1)
+        g.add_two_site(Gm, gam[0], s0, gam[1], s1)
+        g.add_two_site(Gm, gam[1], s0, gam[0], s1)
+
+    for x in range(Nx):
+        for y in range(Ny):
+            s0 = idx(x, y)
+            for a in (sz, sx, sy):
+                g.add_term(-h, [a], [s0])
+            if y % 2 == 0:
+                bond(s0, idx(x, y + 1), sx, (sz, sy))
+            if y % 2 == 1:
+                bond(s0, idx(x, (y + 1) % Ny), sz, (sx, sy))
+            if y % 2 == 1 and x != Nx - 1:
+                bond(s0, idx(x + 1, y - 1), sy, (sz, sx))
+    return g.gen(), pb
+
+
 def tj_site(dtype=np.float64):
     """t-J site with U(1)xU(1) (N, Sz): basis [up (1,1), down (1,-1), empty (0,0)];
     operator tables of ``tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc:110-160``
