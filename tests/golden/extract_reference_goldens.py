@@ -16,6 +16,9 @@ writes ``reference_goldens.json`` next to this script:
 * the fermionic two-site VMPS energies (free fermions N = 8, t-J 1D and 2D,
   ``tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc:80-270``)
   with their sweep parameters and initial product states;
+* the two-site VMPS energy of the Kondo insulator double chain
+  (``tests/test_algorithm/test_two_site_update_finite_vmps.cc:976-1084``;
+  initial state i % 2);
 * the FiniteDMRG energy of the J-K-Gamma model without symmetry
   (``tests/test_algorithm/test_finite_dmrg.cc:346-444``; its initial state
   alternates up and down from site 0).
@@ -60,10 +63,10 @@ def sweep_case(body):
     e = re.search(r"RunTest\w*Case\((.*?)\);", body, re.S).group(1)
     args = [a.strip() for a in e.split(",")]
     p = re.search(r"FiniteVMPSSweepParams\((.*?)\);", body, re.S).group(1)
-    labs = re.search(r"DirectStateInit\w*\(\s*\w+\s*,\s*\{([^}]*)\}", body).group(1)
+    labs = re.search(r"DirectStateInit\w*\(\s*\w+\s*,\s*\{([^}]*)\}", body)
     return {"energy": float(args[-2]), "tol": float(args[-1]),
             "sweep_params": " ".join(p.split()),
-            "labels": [int(x) for x in labs.split(",")]}
+            "labels": [int(x) for x in labs.group(1).split(",")] if labs else None}
 
 
 def num(s):
@@ -117,6 +120,8 @@ def main():
         "ee": fl(ee.group(1)), "tol": float(ee_tol.group(1)),
         "sweep_params": " ".join(ee_sweep.group(1).split())}
     ferm = read("tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc")
+    goldens["vmps"]["KondoDoubleChain"] = sweep_case(
+        fixture_case(vmps, "TestKondoInsulatorSystem", "doublechain"))
     goldens["fermion_vmps"] = {
         "free_fermion8": sweep_case(fixture_case(ferm, "TestTwoSiteAlgorithmSpinlessFermion",
                                                  "1DFreeFermion")),

@@ -219,3 +219,19 @@ def test_kitaev_gamma_oracle_sweep():
     mps = M.direct_product_mps([pb] * N, [i % 2 for i in range(N)], dtype=np.complex128)
     e = vmps.two_site_finite_vmps(mps, mpo, _sweep_params(g["sweep_params"]))
     assert abs(e - g["energy"]) < g["tol"]
+
+
+def test_kondo_double_chain():
+    """test_two_site_update_finite_vmps.cc:976-1084: alternating four-state
+    electron and two-state spin sites; exact diagonalisation (4096 states)
+    and the oracle sweep with the test's parameters, both builders."""
+    from test_mpogen import mpo_dense
+    g = GOLD["vmps"]["KondoDoubleChain"]
+    mpo, sites = M.kondo_chain_mpo()
+    H = mpo_dense(mpo)
+    assert abs(np.linalg.eigvalsh((H + H.T) / 2)[0] - g["energy"]) < g["tol"]
+    for builder in ("prefix", "reference"):
+        mpo, sites = M.kondo_chain_mpo(builder=builder)
+        mps = M.direct_product_mps(sites, [i % 2 for i in range(len(sites))])
+        e = vmps.two_site_finite_vmps(mps, mpo, _sweep_params(g["sweep_params"]))
+        assert abs(e - g["energy"]) < g["tol"]

@@ -70,3 +70,14 @@ def test_kitaev_gamma_finite_dmrg_device(ctx):
                                          dtype=np.complex128)]
     e0, _ = api.finite_dmrg(ctx, mps, M.mat_repr_mpo(mpo), _params(g["sweep_params"]))
     assert abs(e0 - g["energy"]) < g["tol"]
+
+
+def test_kondo_double_chain_device(ctx):
+    """Alternating four-state and two-state sites through the device sweep."""
+    g = GOLD["vmps"]["KondoDoubleChain"]
+    mpo, sites = M.kondo_chain_mpo()
+    mps = [api.DeviceTensor.from_data(ctx, t)
+           for t in M.direct_product_mps(sites, [i % 2 for i in range(len(sites))])]
+    e0, _ = api.two_site_finite_vmps(ctx, mps, [api.DeviceTensor.from_data(ctx, w) for w in mpo],
+                                     _params(g["sweep_params"]))
+    assert abs(e0 - g["energy"]) < g["tol"]

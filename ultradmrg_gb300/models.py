@@ -472,6 +472,46 @@ def kitaev_gamma_mpo(Nx=3, Ny=4, J=-1.0, K=1.0, Gm=0.1, h=0.1, dtype=np.complex1
     return g.gen(), pb
 
 
+def kondo_chain_mpo(Nx=4, t=0.25, Jk=1.0, Jz=0.5, dtype=np.float64, builder="prefix"):
+    """Kondo insulator double chain of
+    ``tests/test_algorithm/test_two_site_update_finite_vmps.cc:976-1084``: even
+    sites conduction electrons (four states in one Sz = 0 sector), odd sites
+    localized spins (two states, one sector); hopping between consecutive
+    electron sites i, i + 2 (the Jordan-Wigner sign is inside the tables, the
+    spin between carries the identity), Jz Sz Sz between consecutive spins
+    and the Kondo coupling Jk S_e . S_l on each rung.  Returns (mpo, sites)."""
+    pbE = Index.make([((0,), 4)], OUT)
+    pbL = Index.make([((0,), 2)], OUT)
+    e4 = lambda name, tb: _op(name, 4, tb, dtype)
+    e2 = lambda name, tb: _op(name, 2, tb, dtype)
+    o = {
+        "sz": e4("sz", {(0, 0): 0.5, (1, 1): -0.5}), "sp": e4("sp", {(0, 1): 1.0}),
+        "sm": e4("sm", {(1, 0): 1.0}),
+        "bupcF": e4("bupcF", {(2, 1): -1, (0, 3): 1}), "Fbdnc": e4("Fbdnc", {(2, 0): 1, (1, 3): -1}),
+        "bupaF": e4("bupaF", {(1, 2): 1, (3, 0): -1}), "Fbdna": e4("Fbdna", {(0, 2): -1, (3, 1): 1}),
+        "bupc": e4("bupc", {(2, 1): 1, (0, 3): 1}), "bdnc": e4("bdnc", {(2, 0): 1, (1, 3): 1}),
+        "bupa": e4("bupa", {(1, 2): 1, (3, 0): 1}), "bdna": e4("bdna", {(0, 2): 1, (3, 1): 1}),
+        "Sz": e2("Sz", {(0, 0): 0.5, (1, 1): -0.5}), "Sp": e2("Sp", {(0, 1): 1.0}),
+        "Sm": e2("Sm", {(1, 0): 1.0}),
+        "idE": e4("idE", {(i, i): 1 for i in range(4)}), "idL": e2("idL", {(0, 0): 1, (1, 1): 1}),
+    }
+    N = 2 * Nx
+    sites = [pbE if i % 2 == 0 else pbL for i in range(N)]
+    ids = [o["idE"] if i % 2 == 0 else o["idL"] for i in range(N)]
+    g = _generator(builder, sites, ids, dtype)
+    for i in range(0, N - 2, 2):
+        g.add_two_site(-t, o["bupcF"], i, o["bupa"], i + 2)
+        g.add_two_site(-t, o["bdnc"], i, o["Fbdna"], i + 2)
+        g.add_two_site(t, o["bupaF"], i, o["bupc"], i + 2)
+        g.add_two_site(t, o["bdna"], i, o["Fbdnc"], i + 2)
+        g.add_two_site(Jz, o["Sz"], i + 1, o["Sz"], i + 3)
+    for i in range(0, N, 2):
+        g.add_two_site(Jk, o["sz"], i, o["Sz"], i + 1)
+        g.add_two_site(Jk / 2, o["sp"], i, o["Sm"], i + 1)
+        g.add_two_site(Jk / 2, o["sm"], i, o["Sp"], i + 1)
+    return g.gen(), sites
+
+
 def tj_site(dtype=np.float64):
     """t-J site with U(1)xU(1) (N, Sz): basis [up (1,1), down (1,-1), empty (0,0)];
     operator tables of ``tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc:110-160``
