@@ -16,6 +16,8 @@ writes ``reference_goldens.json`` next to this script:
 * the fermionic two-site VMPS energies (free fermions N = 8, t-J 1D and 2D,
   ``tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc:80-270``)
   with their sweep parameters and initial product states;
+* the two-site VMPS energy of the t-J model with a Rashba term
+  (``tests/test_algorithm/test_two_site_update_finite_vmps.cc:627-751``);
 * the two-site VMPS energy of the Kondo insulator double chain
   (``tests/test_algorithm/test_two_site_update_finite_vmps.cc:976-1084``;
   initial state i % 2);
@@ -120,6 +122,8 @@ def main():
         "ee": fl(ee.group(1)), "tol": float(ee_tol.group(1)),
         "sweep_params": " ".join(ee_sweep.group(1).split())}
     ferm = read("tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc")
+    goldens["vmps"]["RashbaTJ"] = sweep_case(
+        fixture_case(vmps, "TestTwoSiteAlgorithmTjSystem1U1Symm", "RashbaTermCase"))
     goldens["vmps"]["KondoDoubleChain"] = sweep_case(
         fixture_case(vmps, "TestKondoInsulatorSystem", "doublechain"))
     goldens["fermion_vmps"] = {

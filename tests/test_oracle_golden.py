@@ -235,3 +235,16 @@ def test_kondo_double_chain():
         mps = M.direct_product_mps(sites, [i % 2 for i in range(len(sites))])
         e = vmps.two_site_finite_vmps(mps, mpo, _sweep_params(g["sweep_params"]))
         assert abs(e - g["energy"]) < g["tol"]
+
+
+def test_rashba_tj():
+    """test_two_site_update_finite_vmps.cc:627-751: complex spin-orbit hopping,
+    periodic x; exact diagonalisation in the charge sector of the initial
+    state and the oracle sweep with the test's parameters."""
+    from test_mpogen import mpo_dense
+    g = GOLD["vmps"]["RashbaTJ"]
+    mpo, pb = M.rashba_tj_mpo()
+    assert abs(_sector_ground_energy(mpo, pb, g["labels"]) - g["energy"]) < g["tol"]
+    mps = M.direct_product_mps([pb] * len(g["labels"]), g["labels"], dtype=np.complex128)
+    e = vmps.two_site_finite_vmps(mps, mpo, _sweep_params(g["sweep_params"]))
+    assert abs(e - g["energy"]) < g["tol"]

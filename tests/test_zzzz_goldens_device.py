@@ -81,3 +81,16 @@ def test_kondo_double_chain_device(ctx):
     e0, _ = api.two_site_finite_vmps(ctx, mps, [api.DeviceTensor.from_data(ctx, w) for w in mpo],
                                      _params(g["sweep_params"]))
     assert abs(e0 - g["energy"]) < g["tol"]
+
+
+def test_rashba_tj_device(ctx):
+    """Complex spin-orbit hopping (an MPO with imaginary entries) through the
+    device sweep."""
+    g = GOLD["vmps"]["RashbaTJ"]
+    mpo, pb = M.rashba_tj_mpo()
+    mps = [api.DeviceTensor.from_data(ctx, t)
+           for t in M.direct_product_mps([pb] * len(g["labels"]), g["labels"],
+                                         dtype=np.complex128)]
+    e0, _ = api.two_site_finite_vmps(ctx, mps, [api.DeviceTensor.from_data(ctx, w) for w in mpo],
+                                     _params(g["sweep_params"]))
+    assert abs(e0 - g["energy"]) < g["tol"]

@@ -512,6 +512,64 @@ def kondo_chain_mpo(Nx=4, t=0.25, Jk=1.0, Jz=0.5, dtype=np.float64, builder="pre
     return g.gen(), sites
 
 
+def rashba_tj_mpo(Nx=3, Ny=2, t=3.0, J=1.0, lamb=0.03, builder="prefix"):
+    """t-J model with a Rashba spin-orbit term on an Nx x Ny lattice, periodic
+    in x and open in y, of ``tests/test_algorithm/test_two_site_update_finite_vmps.cc:627-751``:
+    one U(1) (charge; sectors N = 1 of two states [up, down], N = 0 of one),
+    complex.  Operator tables, term list (hard-core operators with the
+    parity string f strictly between the two sites) and the swap of a wrapped
+    bond's site indices while its operators keep their order are the test's,
+    term for term.  Sites x * Ny + y."""
+    dtype = np.complex128
+    pb = Index.make([((1,), 2), ((0,), 1)], OUT)
+    e = lambda name, tb: _op(name, 3, tb, dtype)
+    o = {
+        "id": e("id", {(0, 0): 1, (1, 1): 1, (2, 2): 1}),
+        "f": e("f", {(0, 0): -1, (1, 1): -1, (2, 2): 1}),
+        "sz": e("sz", {(0, 0): 0.5, (1, 1): -0.5}), "sp": e("sp", {(1, 0): 1}),
+        "sm": e("sm", {(0, 1): 1}),
+        "cup": e("cup", {(0, 2): 1}), "cdagup": e("cdagup", {(2, 0): 1}),
+        "cdn": e("cdn", {(1, 2): 1}), "cdagdn": e("cdagdn", {(2, 1): 1}),
+        "ntot": e("ntot", {(0, 0): 1, (1, 1): 1}),
+    }
+    N = Nx * Ny
+    g = _generator(builder, [pb] * N, [o["id"]] * N, dtype)
+    idx = lambda x, y: x * Ny + y
+    f = o["f"]
+    ilamb = 1j * lamb
+
+    def common(s0, s1):
+        for c, a, b_ in ((-t, "cdagup", "cup"), (-t, "cdagdn", "cdn"), (-t, "cup", "cdagup"),
+                         (-t, "cdn", "cdagdn")):
+            g.add_two_site(c, o[a], s0, o[b_], s1, f)
+        g.add_two_site(J, o["sz"], s0, o["sz"], s1)
+        g.add_two_site(J / 2, o["sp"], s0, o["sm"], s1)
+        g.add_two_site(J / 2, o["sm"], s0, o["sp"], s1)
+        g.add_two_site(-J / 4, o["ntot"], s0, o["ntot"], s1)
+
+    for x in range(Nx):
+        for y in range(Ny):
+            # x bonds, periodic
+            s0, s1 = idx(x, y), idx((x + 1) % Nx, y)
+            s0, s1 = min(s0, s1), max(s0, s1)
+            common(s0, s1)
+            so = ((lamb, "cdagup", "cdn"), (lamb, "cup", "cdagdn"), (-lamb, "cdagdn", "cup"),
+                  (-lamb, "cdn", "cdagup")) if x != Nx - 1 else \
+                 ((lamb, "cdn", "cdagup"), (lamb, "cdagdn", "cup"), (-lamb, "cup", "cdagdn"),
+                  (-lamb, "cdagup", "cdn"))
+            for c, a, b_ in so:
+                g.add_two_site(c, o[a], s0, o[b_], s1, f)
+            # y bonds, open
+            if y != Ny - 1:
+                s0, s2 = idx(x, y), idx(x, (y + 1) % Ny)
+                s0, s2 = min(s0, s2), max(s0, s2)
+                common(s0, s2)
+                for c, a, b_ in ((ilamb, "cdagup", "cdn"), (ilamb, "cdagdn", "cup"),
+                                 (-ilamb, "cup", "cdagdn"), (-ilamb, "cdn", "cdagup")):
+                    g.add_two_site(c, o[a], s0, o[b_], s2, f)
+    return g.gen(), pb
+
+
 def tj_site(dtype=np.float64):
     """t-J site with U(1)xU(1) (N, Sz): basis [up (1,1), down (1,-1), empty (0,0)];
     operator tables of ``tests/test_algorithm/test_fermion_two_site_update_finite_vmps.cc:110-160``
