@@ -401,7 +401,7 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
   const int64_t maxit = p.max_iterations;
   VecWork w(ctx);
   Bases bases(ctx);
-  std::vector<double> a(maxit, 0.0), b(maxit, 0.0), N(maxit, 0.0);
+  std::vector<double> a(maxit, 0.0), b(maxit, 0.0);
   LanczosResult res;
   const bool mixed = mv.sg != nullptr;
   KrylovWork kw(ctx, n, cplx, maxit);
@@ -480,7 +480,6 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
       res.gs_vec = finish(m + 1, vec);
       return res;
     }
-    N[m + 1] = n2;
     b[m] = norm_gamma;
     m += 1;
   }
