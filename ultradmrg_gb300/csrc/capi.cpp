@@ -843,8 +843,8 @@ int udmrg_selftest_tc_gemm(udmrg_ctx *c, int64_t M, int64_t N, int64_t K, const 
     UDMRG_CHECK_CUDA(cudaMemsetAsync(ai, 0, abytes, ctx.stream));
     UDMRG_CHECK_CUDA(cudaMemsetAsync(bi, 0, bbytes, ctx.stream));
     const int32_t kc = (int32_t)((K + kTcBK - 1) / kTcBK);
-    PackOp pa{0, K, 1, 0, (int32_t)M, (int32_t)K, 0, 0, kc, kTcBM};
-    PackOp pb{0, 1, N, 0, (int32_t)N, (int32_t)K, 0, 0, kc, kTcBN};
+    PackOp pa{0, K, 1, 0, (int32_t)M, (int32_t)K, 0, 0, kc, kTcBM, 0, 0};
+    PackOp pb{0, 1, N, 0, (int32_t)N, (int32_t)K, 0, 0, kc, kTcBN, 0, 0};
     run_pack(ctx, {pa}, nullptr, 1, dA, true, ai);
     run_pack(ctx, {pb}, nullptr, 1, dB, true, bi);
     TcPlan plan;

@@ -36,8 +36,7 @@ struct T1Block {
 
 }  // namespace
 
-std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const BTensor &W1,
-                                             const BTensor &W2, const BTensor &R,
+std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const BTensor &R,
                                              const BTensor &S, FusedMpo &fm) {
   // complex L, R, psi: the real embedding [[Re, -Im], [Im, Re]] (the MPO
   // coefficients are real, see FusedMpo)

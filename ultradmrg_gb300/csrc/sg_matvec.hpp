@@ -116,10 +116,10 @@ struct SgMatvecPlan {
   void apply_timed(const double *psi_in, double *out, float ms[4]);
 };
 
-// L(a',w,a), W1, W2, R(b',w2,b) real FP64; S the Krylov structure of psi;
-// fm: the fused W1 W2 coefficients (shared with the FP64 form's MPO step).
-std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const BTensor &W1,
-                                             const BTensor &W2, const BTensor &R,
+// L(a',w,a), R(b',w2,b) FP64 (real, or complex through the real embedding);
+// S the Krylov structure of psi; fm: the fused W1 W2 coefficients (shared
+// with the FP64 form's MPO step), which carry all the MPO tensors take part in.
+std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const BTensor &R,
                                              const BTensor &S, FusedMpo &fm);
 
 void run_mpo_step(Ctx &ctx, const SgMatvecPlan &p);

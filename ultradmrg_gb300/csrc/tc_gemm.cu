@@ -99,14 +99,6 @@ __device__ __forceinline__ float narrow_f64(double x) {
 __device__ __forceinline__ float to_f32(float x) { return x; }
 __device__ __forceinline__ float to_f32(double x) { return narrow_f64(x); }
 
-// FP64 operands are narrowed to FP32 first: the three BF16 planes hold ~24
-// significant bits either way, and the split then runs in FP32.
-template <>
-__device__ __forceinline__ void split3<double>(double x, __nv_bfloat16 &h, __nv_bfloat16 &m,
-                                               __nv_bfloat16 &l) {
-  split3<float>(narrow_f64(x), h, m, l);
-}
-
 // Pack sub-matrices into split-BF16 images.  A 32 x 64 tile of the source is
 // staged in shared memory (as FP32), loaded along whichever source direction
 // is contiguous, then written row by row with lanes along K (canonical
