@@ -281,6 +281,9 @@ MODELS = {
     "hubbard_cyl2x2": lambda b: M.hubbard_cylinder_mpo(2, 2, builder=b)[0],
     "hubbard_cyl1x3": lambda b: M.hubbard_cylinder_mpo(1, 3, builder=b)[0],
     "hubbard_cyl1x4": lambda b: M.hubbard_cylinder_mpo(1, 4, builder=b)[0],
+    "tj1d": lambda b: M.tj_mpo(4, builder=b)[0],
+    "tj2d": lambda b: M.tj_mpo(4, pairs=[(0, 1), (0, 2), (2, 3), (1, 3)], builder=b)[0],
+    "rashba_tj": lambda b: M.rashba_tj_mpo(builder=b)[0],
 }
 
 
