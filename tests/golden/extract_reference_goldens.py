@@ -21,6 +21,8 @@ writes ``reference_goldens.json`` next to this script:
 * the two-site VMPS energy of the Kondo insulator double chain
   (``tests/test_algorithm/test_two_site_update_finite_vmps.cc:976-1084``;
   initial state i % 2);
+* the FiniteDMRG energies of the t-J model (1D, 2D) and the 2 x 2 Hubbard
+  model (``tests/test_algorithm/test_finite_dmrg.cc:484-835``);
 * the FiniteDMRG energy of the J-K-Gamma model without symmetry
   (``tests/test_algorithm/test_finite_dmrg.cc:346-444``; its initial state
   alternates up and down from site 0).
@@ -132,6 +134,12 @@ def main():
         "tj1d": sweep_case(fixture_case(ferm, "TestTwoSiteAlgorithmTjSystem2U1Symm", "1DCase")),
         "tj2d": sweep_case(fixture_case(ferm, "TestTwoSiteAlgorithmTjSystem2U1Symm", "2DCase")),
     }
+    goldens["dmrg"]["tj1d"] = sweep_case(fixture_case(dmrg, "TestTwoSiteAlgorithmTjSystem2U1Symm",
+                                                      "1DCase"))
+    goldens["dmrg"]["tj2d"] = sweep_case(fixture_case(dmrg, "TestTwoSiteAlgorithmTjSystem2U1Symm",
+                                                      "2DCase"))
+    goldens["dmrg"]["Hubbard2x2"] = sweep_case(fixture_case(dmrg, "TestTwoSiteAlgorithmHubbardSystem",
+                                                            "2Dcase"))
     kit = re.search(r"TEST\(\s*TestTwoSiteAlgorithmNoSymmetrySpinSystem\s*,\s*"
                     r"2DKitaevComplexCase\s*\)(.*?)(?=\nTEST_F|\nTEST\(|\nstruct|\Z)", dmrg,
                     re.S).group(1)

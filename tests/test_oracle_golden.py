@@ -248,3 +248,18 @@ def test_rashba_tj():
     mps = M.direct_product_mps([pb] * len(g["labels"]), g["labels"], dtype=np.complex128)
     e = vmps.two_site_finite_vmps(mps, mpo, _sweep_params(g["sweep_params"]))
     assert abs(e - g["energy"]) < g["tol"]
+
+
+@pytest.mark.parametrize("case", ["tj1d", "tj2d", "Hubbard2x2"])
+def test_finite_dmrg_golden_hamiltonians(case):
+    """The FiniteDMRG goldens of test_finite_dmrg.cc:484-835 are the ground
+    energies of the Hamiltonians built here (exact diagonalisation in the
+    sector of the test's initial state)."""
+    g = GOLD["dmrg"][case]
+    if case == "Hubbard2x2":
+        mpo, pb = M.hubbard_2x2_test_mpo()
+        labels = [1 if i % 2 == 0 else 2 for i in range(4)]
+    else:
+        mpo, pb = FERMION[case](np.float64)
+        labels = g["labels"]
+    assert abs(_sector_ground_energy(mpo, pb, labels) - g["energy"]) < g["tol"]

@@ -94,3 +94,24 @@ def test_rashba_tj_device(ctx):
     e0, _ = api.two_site_finite_vmps(ctx, mps, [api.DeviceTensor.from_data(ctx, w) for w in mpo],
                                      _params(g["sweep_params"]))
     assert abs(e0 - g["energy"]) < g["tol"]
+
+
+DMRG = {
+    "tj1d": lambda dt: M.tj_mpo(4, dtype=dt),
+    "tj2d": lambda dt: M.tj_mpo(4, pairs=[(0, 1), (0, 2), (2, 3), (1, 3)], dtype=dt),
+    "Hubbard2x2": lambda dt: M.hubbard_2x2_test_mpo(dtype=dt),
+}
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.complex128])
+@pytest.mark.parametrize("case", sorted(DMRG))
+def test_finite_dmrg_goldens_device(ctx, case, dtype):
+    """test_finite_dmrg.cc:484-835 through udmrg_finite_dmrg (MatReprMPO in);
+    the Hubbard case starts from labels 1, 2, 1, 2 (the test's loop)."""
+    g = GOLD["dmrg"][case]
+    mpo, pb = DMRG[case](dtype)
+    labels = g["labels"] or [1 if i % 2 == 0 else 2 for i in range(len(mpo))]
+    mps = [api.DeviceTensor.from_data(ctx, t)
+           for t in M.direct_product_mps([pb] * len(labels), labels, dtype=dtype)]
+    e0, _ = api.finite_dmrg(ctx, mps, M.mat_repr_mpo(mpo), _params(g["sweep_params"]))
+    assert abs(e0 - g["energy"]) < g["tol"]
