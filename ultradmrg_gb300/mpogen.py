@@ -676,6 +676,7 @@ class MPOGenerator:
         self.op_labels = LabelConvertor(eq=lambda a, b: a.shape == b.shape and np.array_equal(a, b))
         ids = [Op.of(self.op_labels.convert(m)) for m in self.id_mats]
         self.fsm = FSM(self.N, ids)
+        self.bond_dims: Optional[List[int]] = None  # right-bond dimensions, set by gen()
 
     def _mat(self, op):
         m = op.mat if hasattr(op, "mat") else op
