@@ -34,7 +34,7 @@ in the element layout of ``QLTensor({pb_in, pb_out})``.
 from __future__ import annotations
 
 from dataclasses import dataclass
-from typing import List, Sequence
+from typing import List
 
 import numpy as np
 

@@ -21,7 +21,7 @@ from __future__ import annotations
 
 import multiprocessing as mp
 import time
-from typing import Dict, List, Optional, Sequence, Tuple
+from typing import Dict, Optional, Sequence, Tuple
 
 _EFF = None
 _PSI = None

@@ -8,7 +8,6 @@ start state) site by site.
 import json
 import os
 
-import numpy as np
 import pytest
 
 from ultradmrg_gb300 import api, models as M

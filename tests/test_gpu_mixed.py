@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from oracle import blocksparse as bs
-from oracle import krylov, vmps as ovmps
+from oracle import krylov
 from systems import (canonical_system, heisenberg_system, hubbard_system, max_block_diff,
                      two_site_problem)
 from ultradmrg_gb300 import api, models as M

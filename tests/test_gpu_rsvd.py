@@ -10,7 +10,7 @@ import pytest
 
 from oracle import blocksparse as bs
 from oracle import krylov
-from systems import canonical_system, max_block_diff, two_site_problem
+from systems import canonical_system, two_site_problem
 from ultradmrg_gb300 import api, models as M
 
 pytestmark = pytest.mark.gpu
