@@ -281,3 +281,31 @@ def test_lanczos_expmv_vs_dense():
                                       0.1, krylov.LanczosParams(1e-14, 100))
     got = res.expmv.to_dense().reshape(-1)
     assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-13
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.complex128])
+def test_single_site_lanczos_vs_dense_ed(dtype):
+    """``tests/test_algorithm/test_lanczos_solver.cc:209-394``: Lanczos with
+    the single-site matvec against the ground energy of the dense operator
+    (built column by column from the same matvec), 1e-8."""
+    eff_ham, _ = _random_single_sector_eff_ham(D=12, dtype=dtype, seed=5)
+    L, W, _, R = eff_ham
+    D, d = 12, 2
+    q0 = (0,)
+    psi = BlockTensorData([Index.make([(q0, D)], IN), Index.make([(q0, d)], OUT),
+                           Index.make([(q0, D)], OUT)],
+                          {(0, 0, 0): np.random.default_rng(6).standard_normal((D, d, D)).astype(dtype)},
+                          dtype)
+    n = D * d * D
+    H = np.zeros((n, n), dtype=dtype)
+    for c in range(n):
+        e = psi.copy()
+        blk = np.zeros(n, dtype=dtype)
+        blk[c] = 1.0
+        e.blocks[(0, 0, 0)] = blk.reshape(D, d, D)
+        H[:, c] = krylov.eff_ham_mul_single_site_state([L, W, R], e).to_dense().reshape(-1)
+    assert np.allclose(H, H.conj().T, atol=1e-10)
+    w0 = np.linalg.eigvalsh((H + H.conj().T) / 2)[0]
+    res = krylov.lanczos_solver([L, W, R], psi, krylov.eff_ham_mul_single_site_state,
+                                krylov.LanczosParams(1e-9, 200))
+    assert abs(res.gs_eng - w0) < 1e-8
