@@ -39,7 +39,10 @@ METRIC = ("two-site matvec TFLOP/s (H_eff*psi, U(1)xU(1) block-sparse; algorithm
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    # default: 2000 mixed matvecs (~1.4 s with the L2 flushes, so the 200 ms
+    # clock sampler takes several readings inside the timed region); 20 for
+    # the reference arm, whose steps are whole CPU matvecs
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hubbard4x16_D2000")
@@ -49,7 +52,10 @@ def parse():
     ap.add_argument("--matvec-only", action="store_true",
                     help="time the mixed matvec only (profiling runs): no FP64 form, "
                          "Lanczos, local updates, e2e or CPU baseline")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 20 if args.impl == "reference" else 2000
+    return args
 
 
 def dist_env():
