@@ -37,7 +37,7 @@ enum { UDMRG_PREC_FP64 = 0, UDMRG_PREC_MIXED = 1 };
  * vectors, dot products and the tridiagonal problem stay FP64). */
 typedef struct {
   double error;           /* absolute energy change that stops the iteration */
-  int64_t max_iterations; /* maximal Krylov dimension */
+  int64_t max_iterations; /* maximal Krylov dimension, at least 2 */
   int64_t matvec_precision;
 } udmrg_lanczos_params;
 

@@ -399,6 +399,8 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
   // eff_ham_eff_dim: element count of the initial state
   const int64_t eff_dim = init_state.size();
   const int64_t maxit = p.max_iterations;
+  // the second step already writes a[1] (the reference's loop writes bases[1])
+  UDMRG_REQUIRE(maxit >= 2, "Lanczos: max_iterations must be at least 2");
   VecWork w(ctx);
   Bases bases(ctx);
   std::vector<double> a(maxit, 0.0), b(maxit, 0.0);
@@ -546,6 +548,7 @@ ExpmvResult lanczos_expmv(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state, d
   const size_t vbytes = std::max<int64_t>(nd, 1) * sizeof(double);
   const int64_t eff_dim = init_state.size();
   const int64_t maxit = p.max_iterations;
+  UDMRG_REQUIRE(maxit >= 2, "Lanczos expmv: max_iterations must be at least 2");
   VecWork w(ctx);
   Bases bases(ctx);
   std::vector<double> a(maxit, 0.0), b(maxit, 0.0);
