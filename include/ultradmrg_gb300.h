@@ -355,14 +355,17 @@ int udmrg_ctx_flush_l2(udmrg_ctx *ctx, int64_t bytes);
 /* No counterpart in the reference.  2-norm of n_doubles device doubles at
  * d_x, written to the device double *d_norm, stream ordered on `stream` (a
  * cudaStream_t; NULL is the legacy default stream) on the current device.
- * For callers that cannot allocate device memory when they need it (inside
- * their own stream capture, under another allocator, in loops that must not
- * touch an allocator): it calls no cudaMalloc/cudaFree or allocating routine;
- * its scratch is a fixed 32 KB device array held by every GPU that loads the
- * library until exit.  At most 16,777,216 doubles per call (status 1 above
- * that).  The first call on a device sets up the scratch address, so make it
- * before any stream capture.  Calls that overlap on the GPU race on the
- * shared scratch. */
+ * For callers that cannot allocate device memory when they need it (their
+ * device memory belongs to another allocator or is fully reserved, or they
+ * run loops that must not touch an allocator): it calls no cudaMalloc/cudaFree
+ * or allocating routine; its scratch is a fixed 32 KB device array held by
+ * every GPU that loads the library until exit.  At most 16,777,216 doubles
+ * per call (status 1 above that); devices 0..63.  The first call on a device
+ * sets up the scratch address, so make it before any stream capture; that
+ * address is cached for the life of the device's primary context (the
+ * process).  A CUDA error pending from the caller's earlier launches is
+ * reported (status 2) and not cleared.  Calls that overlap on the GPU race on
+ * the shared scratch. */
 int udmrg_norm_noalloc(const double *d_x, int64_t n_doubles, double *d_norm, void *stream);
 
 #ifdef __cplusplus

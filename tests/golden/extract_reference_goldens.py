@@ -27,14 +27,14 @@ writes ``reference_goldens.json`` next to this script:
   (``tests/test_algorithm/test_finite_dmrg.cc:346-444``; its initial state
   alternates up and down from site 0).
 
-Usage: python tests/golden/extract_reference_goldens.py [reference_root]
+Usage: python tests/golden/extract_reference_goldens.py <reference_root>
 """
 import json
 import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = None  # the reference checkout, from the command line
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -81,6 +81,10 @@ def num(s):
 
 
 def main():
+    global REF
+    if len(sys.argv) != 2:
+        sys.exit("usage: extract_reference_goldens.py <reference_root>")
+    REF = sys.argv[1]
     vmps = read("tests/test_algorithm/test_two_site_update_finite_vmps.cc")
     dmrg = read("tests/test_algorithm/test_finite_dmrg.cc")
     expmv = read("tests/test_algorithm/test_lanczos_expmv_solver.cc")

@@ -1,12 +1,13 @@
 """The allocation-free norm entry point against the allocating one.
 
 ``udmrg_norm_noalloc`` serves callers that cannot allocate device memory at
-the point of the call (inside their own stream capture, under an allocator
-they do not control, in loops that must not touch an allocator); its scratch
-is a static device array instead of a pool allocation.  Here it must agree
-with ``udmrg_tensor_norm`` (the same reduction with allocated scratch) on two
-calls in a row.  The file name sorts last so that a run stopping at the first
-failure has run every other test before this one.
+the point of the call (device memory owned by an allocator they do not
+control or fully reserved, loops that must not touch an allocator); its
+scratch is a static device array instead of a pool allocation.  Here it must
+agree with ``udmrg_tensor_norm`` (the same reduction with allocated scratch)
+on two calls in a row, also at the largest accepted length.  The file name
+sorts after every other test file (``pytest --collect-only`` lists it last),
+so a run stopping at the first failure has run every other test first.
 """
 import ctypes as C
 
@@ -56,6 +57,24 @@ def test_norm_noalloc_matches_allocating_norm(ctx):
     _lib.call("udmrg_norm_noalloc", yp, 2, op, None)
     torch.cuda.synchronize()
     assert abs(float(out.download_packed()[0]) - 5.0) <= RTOL * 5.0
+
+
+def test_norm_noalloc_at_the_maximum(ctx):
+    """16,777,216 doubles: every slot of the static scratch array is written."""
+    import torch
+
+    from ultradmrg_gb300 import _lib
+    n = 16_777_216
+    rng = np.random.default_rng(11)
+    x = _vector_tensor(ctx, rng.standard_normal(n))
+    out = _vector_tensor(ctx, np.zeros(1))
+    ref = x.norm()
+    xp = C.cast(C.c_void_p(x.device_ptr()), _lib.c_double_p)
+    op = C.cast(C.c_void_p(out.device_ptr()), _lib.c_double_p)
+    for _ in range(2):
+        _lib.call("udmrg_norm_noalloc", xp, n, op, None)
+        torch.cuda.synchronize()
+        assert abs(float(out.download_packed()[0]) - ref) <= RTOL * ref
 
 
 def test_norm_noalloc_rejects_oversize(ctx):

@@ -1,10 +1,8 @@
 // 2-norm of a device vector without any device allocation.
 //
 // Some callers cannot allocate device memory at the moment they need a norm:
-// code running inside its own CUDA stream capture (cudaMalloc is not
-// capturable), hosts whose device memory is owned by another allocator or
-// fully reserved, and latency-critical loops that must not touch the
-// allocator.  For them this file offers udmrg_norm_noalloc, a variant of the
+// hosts whose device memory is owned by another allocator or fully reserved,
+// and latency-critical loops that must not touch the allocator.  For them this file offers udmrg_norm_noalloc, a variant of the
 // library's two-stage reduction (the one behind udmrg_tensor_norm) whose
 // per-block partial sums live in a fixed, file-scope device array instead of
 // a buffer taken from the stream-ordered pool.
@@ -16,7 +14,12 @@
 //    until the process exits;
 //  * the first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current) and caches it, so make
-//    that first call before any stream capture;
+//    that first call before any stream capture; the cache assumes that the
+//    device's primary context lives until the process exits (after
+//    cudaDeviceReset the cached address is stale);
+//  * devices 0..63 only;
+//  * a CUDA error left pending by an earlier call of the caller is reported
+//    (status 2) and left in place, not cleared;
 //  * all calls share the one array: calls whose kernels overlap on the GPU
 //    (different streams without ordering between them) race.
 #include <mutex>
@@ -81,15 +84,25 @@ __global__ void noalloc_finish_kernel(const double *__restrict__ partials, int n
 }
 
 // Device address of the scratch array for the current device (set up once).
-int partials_for_current_device(double **p) {
+// On failure *msg names the cause.
+int partials_for_current_device(double **p, const char **msg) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return udmrg::kErrCuda;
-  if (dev < 0 || dev >= kMaxDevices) return udmrg::kErrInvalid;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    *msg = "udmrg_norm_noalloc: cudaGetDevice failed";
+    return udmrg::kErrCuda;
+  }
+  if (dev < 0 || dev >= kMaxDevices) {
+    *msg = "udmrg_norm_noalloc: device number above 63 (the address table holds 64 devices)";
+    return udmrg::kErrInvalid;
+  }
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   if (!g_partials_addr[dev]) {
     double *addr = nullptr;
     const cudaError_t rc = cudaGetSymbolAddress((void **)&addr, g_noalloc_partials);
-    if (rc != cudaSuccess || addr == nullptr) return udmrg::kErrCuda;
+    if (rc != cudaSuccess || addr == nullptr) {
+      *msg = "udmrg_norm_noalloc: cudaGetSymbolAddress of the scratch array failed";
+      return udmrg::kErrCuda;
+    }
     g_partials_addr[dev] = addr;
   }
   *p = g_partials_addr[dev];
@@ -110,11 +123,18 @@ extern "C" int udmrg_norm_noalloc(const double *d_x, int64_t n_doubles, double *
         "static scratch");
     return udmrg::kErrInvalid;
   }
-  double *partials = nullptr;
-  const int st = partials_for_current_device(&partials);
-  if (st != udmrg::kOk) {
+  // an error of the caller's own earlier launches is theirs to read: report
+  // it without clearing it, so that the launch check below sees only ours
+  if (cudaPeekAtLastError() != cudaSuccess) {
     udmrg::set_last_error_noalloc(
-        "udmrg_norm_noalloc: cudaGetSymbolAddress of the scratch array failed");
+        "udmrg_norm_noalloc: a CUDA error from an earlier call is pending (not cleared)");
+    return udmrg::kErrCuda;
+  }
+  double *partials = nullptr;
+  const char *msg = nullptr;
+  const int st = partials_for_current_device(&partials, &msg);
+  if (st != udmrg::kOk) {
+    udmrg::set_last_error_noalloc(msg);
     return st;
   }
   cudaStream_t s = (cudaStream_t)stream;
