@@ -845,8 +845,8 @@ int udmrg_selftest_tc_gemm(udmrg_ctx *c, int64_t M, int64_t N, int64_t K, const 
     const int32_t kc = (int32_t)((K + kTcBK - 1) / kTcBK);
     PackOp pa{0, K, 1, 0, (int32_t)M, (int32_t)K, 0, 0, kc, kTcBM, 0, 0};
     PackOp pb{0, 1, N, 0, (int32_t)N, (int32_t)K, 0, 0, kc, kTcBN, 0, 0};
-    run_pack(ctx, {pa}, nullptr, 1, dA, true, ai);
-    run_pack(ctx, {pb}, nullptr, 1, dB, true, bi);
+    run_pack(ctx, std::vector<PackOp>{pa}, dA, true, ai);
+    run_pack(ctx, std::vector<PackOp>{pb}, dB, true, bi);
     TcPlan plan;
     plan.ctx = &ctx;
     std::vector<int64_t> rows(M);

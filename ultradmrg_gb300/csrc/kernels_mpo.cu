@@ -1,12 +1,15 @@
 // MPO step of the mixed-precision matvec: T3 = (W1 W2) T1 on CUDA cores,
-// grouped by (A', B) sector pair.  The work unit of one warp is (pair, a',
-// 32-wide tile of the contiguous b index): the warp stages the pair's input
-// channels for its 32 columns in a warp-private slice of shared memory (each
-// T1 entry read once, coalesced), then produces every output channel as an
-// FP32 dot product with the pair's CSR coefficient row (lanes over b), splits
-// it into three BF16 planes and writes them into the step-3 tile images.
-// Units are independent: no block-wide barrier.  HBM bound: T1 read once
-// (FP32), T3 written once (3 x BF16).
+// grouped by (A', B) sector pair.  A thread owns one unit (pair, a', 8-wide
+// chunk of b): for each output channel of the pair it accumulates the
+// coefficient-weighted input chunks (two 16-byte loads of FP32 T1 per
+// nonzero, read straight from global memory: an input channel serves ~1.25
+// outputs, the second use hits L1), splits the eight sums into three BF16
+// planes and writes each plane with one 16-byte store into the step-3 tile
+// image.  A warp takes 32 consecutive units of one pair, so the CSR walk over
+// the pair's nonzeros is warp-uniform (broadcast metadata loads, no
+// divergence).  Nonzeros are processed four at a time: their eight loads are
+// in flight together.  Padded b columns (up to a multiple of 8) read and
+// write zeros.  HBM bound: T1 read once (FP32), T3 written once (3 x BF16).
 #include <cuda_bf16.h>
 
 #include "mpo_step.hpp"
@@ -20,80 +23,108 @@ __device__ __forceinline__ int canon(int r, int k, int tr) {
   return (((k >> 3) * (tr >> 3) + (r >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1);
 }
 
-__global__ void mpo_unit_kernel(const int64_t *__restrict__ unit0,
-                                const int32_t *__restrict__ unit_pair, int64_t nunits,
-                                const MpoPair *__restrict__ pairs, const MpoIn *__restrict__ ins,
-                                const MpoOut *__restrict__ outs,
-                                const int32_t *__restrict__ rowptr, const MpoNz *__restrict__ nz,
-                                const float *__restrict__ t1, uint8_t *__restrict__ img,
-                                int slice) {
-  extern __shared__ float sm[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nwarp = blockDim.x >> 5;
-  float *X = sm + (int64_t)warp * slice;  // slice = max input channels x 32
-  const int64_t plane = (int64_t)kTcBM * kTcBK * 2;
-  for (int64_t u = (int64_t)blockIdx.x * nwarp + warp; u < nunits;
-       u += (int64_t)gridDim.x * nwarp) {
-    const int lo = __ldg(unit_pair + u);
-    const MpoPair pr = pairs[lo];
-    const int nbt = (pr.db + 31) >> 5;
-    const int64_t local = u - __ldg(unit0 + lo);
-    const int a = (int)(local / nbt);
-    const int b = (int)(local - (int64_t)a * nbt) * 32 + lane;
-    const bool col = b < pr.db;
-    for (int i = 0; i < pr.nin; ++i) {
-      const MpoIn in = ins[pr.in0 + i];
-      X[(i << 5) + lane] = col ? __ldg(t1 + in.base + (int64_t)a * in.astride + b) : 0.f;
+__device__ __forceinline__ uint32_t pack_bf16x2(__nv_bfloat16 a, __nv_bfloat16 b) {
+  return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
+
+// x = hi + mid + lo, each the BF16 rounding of the remainder (exact
+// differences in FP32), eight values into three 16-byte plane segments.
+__device__ __forceinline__ void split8(const float (&x)[8], uint4 &h, uint4 &m, uint4 &l) {
+  uint32_t ph[4], pm[4], pl[4];
+#pragma unroll
+  for (int j = 0; j < 8; j += 2) {
+    __nv_bfloat16 hv[2], mv[2], lv[2];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      hv[t] = __float2bfloat16_rn(x[j + t]);
+      const float r1 = x[j + t] - __bfloat162float(hv[t]);
+      mv[t] = __float2bfloat16_rn(r1);
+      lv[t] = __float2bfloat16_rn(r1 - __bfloat162float(mv[t]));
     }
-    __syncwarp();
-    for (int ob = 0; ob < pr.nout; ob += 32) {
-      // row pointers of outputs ob .. ob + oc - 1 (lane oo holds output oo's
-      // start) and the end pointer of the last one
-      const int oc = min(32, pr.nout - ob);
-      const int rp = __ldg(rowptr + pr.row0 + ob + min(lane, oc));
-      const int rend = __ldg(rowptr + pr.row0 + ob + oc);
-      for (int oo = 0; oo < oc; ++oo) {
-        const int o = ob + oo;
-        const int k0 = __shfl_sync(0xffffffffu, rp, oo);
-        const int k1n = __shfl_sync(0xffffffffu, rp, (oo + 1) & 31);
-        const int k1 = oo + 1 < oc ? k1n : rend;
-        float acc = 0.f;
-        // 32 nonzeros per coalesced load, broadcast lane by lane
-        for (int kb = k0; kb < k1; kb += 32) {
-          const int k = kb + lane;
-          int ei = 0;
-          float ev = 0.f;
-          if (k < k1) {
-            const MpoNz e = nz[k];
-            ei = e.i;
-            ev = e.v;
+    ph[j >> 1] = pack_bf16x2(hv[0], hv[1]);
+    pm[j >> 1] = pack_bf16x2(mv[0], mv[1]);
+    pl[j >> 1] = pack_bf16x2(lv[0], lv[1]);
+  }
+  h = make_uint4(ph[0], ph[1], ph[2], ph[3]);
+  m = make_uint4(pm[0], pm[1], pm[2], pm[3]);
+  l = make_uint4(pl[0], pl[1], pl[2], pl[3]);
+}
+
+constexpr int kMpoWarps = 8;
+
+__global__ void __launch_bounds__(32 * kMpoWarps)
+    mpo_chunk_kernel(const MpoTask *__restrict__ tasks, int ntasks,
+                     const MpoPair *__restrict__ pairs, const MpoOut *__restrict__ outs,
+                     const int32_t *__restrict__ rowptr, const MpoNzRec *__restrict__ nzr,
+                     const float *__restrict__ t1, uint8_t *__restrict__ img) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int64_t plane = (int64_t)kTcBM * kTcBK * 2;
+  for (int t = blockIdx.x * kMpoWarps + warp; t < ntasks; t += gridDim.x * kMpoWarps) {
+    const MpoTask tk = tasks[t];
+    const MpoPair pr = pairs[tk.pair];
+    const int nch = pr.dbp >> 3;
+    const int u = tk.u0 + lane;
+    const bool valid = u < pr.da * nch;
+    const int a = valid ? u / nch : 0;
+    const int c8 = valid ? (u - a * nch) * 8 : 0;
+    const int kend = __ldg(rowptr + pr.row0 + pr.nout);
+    int o = 0;
+    int next = __ldg(rowptr + pr.row0 + 1);  // end of output channel o's nonzeros
+    float acc[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] = 0.f;
+    auto store = [&](int oc) {
+      const MpoOut ot = outs[pr.out0 + oc];
+      if (valid) {
+        const int row = ot.row0 + a * ot.rstride;
+        const int col = ot.col0 + c8;
+        const int64_t off = ot.img_off + ((int64_t)(row >> 7) * ot.kc + (col >> 6)) * 3 * plane +
+                            canon(row & 127, col & 63, kTcBM);
+        uint4 h, m, l;
+        split8(acc, h, m, l);
+        *(uint4 *)(img + off) = h;
+        *(uint4 *)(img + off + plane) = m;
+        *(uint4 *)(img + off + 2 * plane) = l;
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[j] = 0.f;
+    };
+    for (int kb = __ldg(rowptr + pr.row0); kb < kend; kb += 4) {
+      float4 x[4][2];
+      float v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        x[q][0] = x[q][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        v[q] = 0.f;
+        if (kb + q < kend) {
+          const MpoNzRec e = nzr[kb + q];
+          v[q] = e.v;
+          if (valid) {
+            const float4 *src = (const float4 *)(t1 + e.base + (int64_t)a * e.astride + c8);
+            x[q][0] = __ldg(src);
+            x[q][1] = __ldg(src + 1);
           }
-          const int cnt = min(32, k1 - kb);
-#pragma unroll 4
-          for (int t = 0; t < cnt; ++t) {
-            const int i = __shfl_sync(0xffffffffu, ei, t);
-            const float v = __shfl_sync(0xffffffffu, ev, t);
-            acc = fmaf(v, X[(i << 5) + lane], acc);
-          }
-        }
-        if (col) {
-          const MpoOut ot = outs[pr.out0 + o];
-          const int row = ot.row0 + a * ot.rstride;
-          const int c = ot.col0 + b;
-          const int64_t off = ot.img_off +
-                              ((int64_t)(row / kTcBM) * ot.kc + c / kTcBK) * 3 * plane +
-                              canon(row % kTcBM, c % kTcBK, kTcBM);
-          const __nv_bfloat16 h = __float2bfloat16_rn(acc);
-          const float r1 = acc - __bfloat162float(h);
-          const __nv_bfloat16 m = __float2bfloat16_rn(r1);
-          const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
-          *(__nv_bfloat16 *)(img + off) = h;
-          *(__nv_bfloat16 *)(img + off + plane) = m;
-          *(__nv_bfloat16 *)(img + off + 2 * plane) = l;
         }
       }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (kb + q >= kend) break;
+        while (kb + q >= next) {  // output channel o is complete (warp-uniform)
+          store(o);
+          ++o;
+          next = __ldg(rowptr + pr.row0 + o + 1);
+        }
+        acc[0] = fmaf(v[q], x[q][0].x, acc[0]);
+        acc[1] = fmaf(v[q], x[q][0].y, acc[1]);
+        acc[2] = fmaf(v[q], x[q][0].z, acc[2]);
+        acc[3] = fmaf(v[q], x[q][0].w, acc[3]);
+        acc[4] = fmaf(v[q], x[q][1].x, acc[4]);
+        acc[5] = fmaf(v[q], x[q][1].y, acc[5]);
+        acc[6] = fmaf(v[q], x[q][1].z, acc[6]);
+        acc[7] = fmaf(v[q], x[q][1].w, acc[7]);
+      }
     }
-    __syncwarp();  // X is rewritten by the next unit
+    for (; o < pr.nout; ++o) store(o);  // the last channel and channels without nonzeros
   }
 }
 
@@ -169,27 +200,12 @@ void run_mpo_step64(Ctx &ctx, const MpoStep64 &p, const double *t1, double *t3) 
 }
 
 void run_mpo_step(Ctx &ctx, const SgMatvecPlan &p) {
-  const int npairs = (int)p.pairs.size();
-  if (npairs == 0) return;
-  const int64_t nunits = p.unit0.back();
-  if (nunits == 0) return;
-  const int slice = std::max(1, p.max_nin) * 32;
-  const size_t per_warp = (size_t)slice * sizeof(float);
-  UDMRG_REQUIRE(per_warp <= 200 * 1024, "mixed matvec: too many MPO input channels in a pair");
-  const int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (96 * 1024) / per_warp));
-  const size_t smem = per_warp * warps;
-  static size_t attr = 0;
-  if (smem > 48 * 1024 && smem > attr) {
-    UDMRG_CHECK_CUDA(cudaFuncSetAttribute(mpo_unit_kernel,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = smem;
-  }
-  const int64_t blocks = (nunits + warps - 1) / warps;
-  const int grid = (int)std::min<int64_t>(blocks, 16 * (int64_t)ctx.num_sms);
-  mpo_unit_kernel<<<grid, 32 * warps, smem, ctx.stream>>>(p.d_unit0, p.d_unit_pair, nunits,
-                                                          p.d_pairs,
-                                                          p.d_ins, p.d_outs, p.d_rowptr, p.d_nz,
-                                                          p.t1, p.t3_img, slice);
+  const int ntasks = (int)p.tasks.size();
+  if (ntasks == 0) return;
+  const int blocks = (ntasks + kMpoWarps - 1) / kMpoWarps;
+  const int grid = std::min(blocks, 16 * ctx.num_sms);
+  mpo_chunk_kernel<<<grid, 32 * kMpoWarps, 0, ctx.stream>>>(
+      p.d_tasks, ntasks, p.d_pairs, p.d_outs, p.d_rowptr, p.d_nz, p.t1, p.t3_img);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches++;
 }

@@ -1,5 +1,6 @@
 #include "sg_matvec.hpp"
 
+#include <algorithm>
 #include <array>
 #include <map>
 
@@ -8,9 +9,8 @@ namespace udmrg {
 SgMatvecPlan::~SgMatvecPlan() {
   if (!ctx) return;
   for (void *p : {(void *)l_img, (void *)psi_img, (void *)t3_img, (void *)r_img, (void *)t1,
-                  (void *)d_psi_ops,
-                  (void *)d_pairs, (void *)d_ins, (void *)d_outs, (void *)d_rowptr,
-                  (void *)d_nz, (void *)d_unit0, (void *)d_unit_pair})
+                  (void *)d_pairs, (void *)d_outs, (void *)d_rowptr, (void *)d_nz,
+                  (void *)d_tasks})
     ctx->free(p);
 }
 
@@ -32,7 +32,10 @@ struct T1Block {
   int64_t im;      // offset of the imaginary half (complex data)
   int64_t pitch;
   int32_t dw, ds12;
+  int32_t bstride;  // columns per (s1, s2): db rounded up to 8
 };
+
+inline int64_t up8(int64_t x) { return (x + 7) & ~(int64_t)7; }
 
 }  // namespace
 
@@ -82,48 +85,54 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   struct G1 {
     int A;
     int64_t M, N, K, t1_off, l_off, p_off;
-    int64_t Np;  // T1 row pitch: N rounded up to 4 (16-byte aligned rows)
-    int64_t Me, Ke;  // embedded GEMM shape (2M x 2K for complex data)
+    int64_t Np;  // T1 row pitch (N, a multiple of 8: 32-byte aligned rows)
+    int64_t Kh;  // K rounded up to 8: first K column of the imaginary half
+    int64_t Me, Ke;  // embedded GEMM shape (2M x 2Kh for complex data)
   };
   std::vector<G1> g1s;
   for (int A = 0; A < nA; ++A) {
     if (lrows[A].empty() || pcols[A].empty()) continue;
-    G1 g{A, 0, 0, L.idx[2].dims[A], t1tot, lbytes, pbytes, 0, 0, 0};
+    G1 g{A, 0, 0, L.idx[2].dims[A], t1tot, lbytes, pbytes, 0, 0, 0, 0};
     std::vector<int64_t> rof, cof;
     for (int64_t b : lrows[A]) {
       rof.push_back(g.M);
       g.M += dim(L, b, 0) * dim(L, b, 1);
     }
-    for (int64_t b : pcols[A]) {
+    for (int64_t b : pcols[A]) {  // columns (s1, s2, b), each b run padded to 8
       cof.push_back(g.N);
-      g.N += dim(S, b, 1) * dim(S, b, 2) * dim(S, b, 3);
+      g.N += dim(S, b, 1) * dim(S, b, 2) * up8(dim(S, b, 3));
     }
     UDMRG_REQUIRE(g.M < (1 << 30) && g.N < (1 << 30) && g.K < (1 << 30), "mixed matvec: group too large");
-    g.Np = (g.N + 3) & ~(int64_t)3;
+    g.Np = g.N;
+    g.Kh = up8(g.K);
     g.Me = es * g.M;
-    g.Ke = es * g.K;
+    g.Ke = cplx ? 2 * g.Kh : g.K;
     const int32_t kc = (int32_t)((g.Ke + kTcBK - 1) / kTcBK);
     for (size_t i = 0; i < lrows[A].size(); ++i) {
       const int64_t b = lrows[A][i], nr = dim(L, b, 0) * dim(L, b, 1);
       // real rows [Lr | -Li], imaginary rows [Li | Lr]
       add_pack(lops, L.offs[b], g.K, 1, g.l_off, nr, g.K, rof[i], 0, kc, kTcBM, 0, false);
       if (cplx) {
-        add_pack(lops, L.offs[b], g.K, 1, g.l_off, nr, g.K, rof[i], g.K, kc, kTcBM, 1, true);
+        add_pack(lops, L.offs[b], g.K, 1, g.l_off, nr, g.K, rof[i], g.Kh, kc, kTcBM, 1, true);
         add_pack(lops, L.offs[b], g.K, 1, g.l_off, nr, g.K, g.M + rof[i], 0, kc, kTcBM, 1,
                  false);
-        add_pack(lops, L.offs[b], g.K, 1, g.l_off, nr, g.K, g.M + rof[i], g.K, kc, kTcBM, 0,
+        add_pack(lops, L.offs[b], g.K, 1, g.l_off, nr, g.K, g.M + rof[i], g.Kh, kc, kTcBM, 0,
                  false);
       }
     }
     for (size_t j = 0; j < pcols[A].size(); ++j) {
       const int64_t b = pcols[A][j];
-      const int64_t ncol = dim(S, b, 1) * dim(S, b, 2) * dim(S, b, 3);
-      // K range [psi_r; psi_i]
-      add_pack(p->psi_ops, S.offs[b], 1, ncol, g.p_off, ncol, g.K, cof[j], 0, kc, kTcBN, 0,
-               false);
-      if (cplx)
-        add_pack(p->psi_ops, S.offs[b], 1, ncol, g.p_off, ncol, g.K, cof[j], g.K, kc, kTcBN, 1,
-                 false);
+      const int64_t ds12 = dim(S, b, 1) * dim(S, b, 2), db = dim(S, b, 3);
+      const int64_t ncol = ds12 * db;
+      // one op per (s1, s2): the b run lands at its padded column; K range
+      // [psi_r; psi_i]
+      for (int64_t q = 0; q < ds12; ++q) {
+        add_pack(p->psi_pack.ops, S.offs[b] + q * db, 1, ncol, g.p_off, db, g.K,
+                 cof[j] + q * up8(db), 0, kc, kTcBN, 0, false);
+        if (cplx)
+          add_pack(p->psi_pack.ops, S.offs[b] + q * db, 1, ncol, g.p_off, db, g.K,
+                   cof[j] + q * up8(db), g.Kh, kc, kTcBN, 1, false);
+      }
     }
     // T1 block locations
     for (size_t i = 0; i < lrows[A].size(); ++i) {
@@ -137,6 +146,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
         t.pitch = g.Np;
         t.dw = (int32_t)dim(L, lb, 1);
         t.ds12 = (int32_t)(dim(S, pb, 1) * dim(S, pb, 2));
+        t.bstride = (int32_t)up8(dim(S, pb, 3));
         t1map[k] = t;
       }
     }
@@ -166,9 +176,9 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       rof.push_back(M);
       M += dim(S, b, 0) * dim(S, b, 1) * dim(S, b, 2);
     }
-    for (int64_t b : rks[Bp]) {
+    for (int64_t b : rks[Bp]) {  // columns (w2, b), each b run padded to 8
       kof.push_back(K);
-      K += dim(R, b, 1) * dim(R, b, 2);
+      K += dim(R, b, 1) * up8(dim(R, b, 2));
     }
     UDMRG_REQUIRE(M < (1 << 30) && K < (1 << 30), "mixed matvec: group too large");
     const int64_t Ke = es * K, Ne = es * dBp;  // embedded shape: M x 2K times (2 dB') x 2K
@@ -181,13 +191,17 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       for (int64_t m = 0; m < nr; ++m) rows[rof[i] + m] = (S.offs[b] + m * dBp) * es;
     }
     for (size_t j = 0; j < rks[Bp].size(); ++j) {
-      const int64_t b = rks[Bp][j], nc = dim(R, b, 1) * dim(R, b, 2);
-      // B rows: [Rr | -Ri] (real output columns), [Ri | Rr] (imaginary)
-      add_pack(rops, R.offs[b], nc, 1, r_off, dBp, nc, 0, kof[j], kc, kTcBN, 0, false);
-      if (cplx) {
-        add_pack(rops, R.offs[b], nc, 1, r_off, dBp, nc, 0, K + kof[j], kc, kTcBN, 1, true);
-        add_pack(rops, R.offs[b], nc, 1, r_off, dBp, nc, dBp, kof[j], kc, kTcBN, 1, false);
-        add_pack(rops, R.offs[b], nc, 1, r_off, dBp, nc, dBp, K + kof[j], kc, kTcBN, 0, false);
+      const int64_t b = rks[Bp][j], dw2 = dim(R, b, 1), db = dim(R, b, 2), nc = dw2 * db;
+      // B rows: [Rr | -Ri] (real output columns), [Ri | Rr] (imaginary); one
+      // op per w2 (the b run at its padded column)
+      for (int64_t w2 = 0; w2 < dw2; ++w2) {
+        const int64_t off = R.offs[b] + w2 * db, k0 = kof[j] + w2 * up8(db);
+        add_pack(rops, off, nc, 1, r_off, dBp, db, 0, k0, kc, kTcBN, 0, false);
+        if (cplx) {
+          add_pack(rops, off, nc, 1, r_off, dBp, db, 0, K + k0, kc, kTcBN, 1, true);
+          add_pack(rops, off, nc, 1, r_off, dBp, db, dBp, k0, kc, kTcBN, 1, false);
+          add_pack(rops, off, nc, 1, r_off, dBp, db, dBp, K + k0, kc, kTcBN, 0, false);
+        }
       }
     }
     // MPO-step targets of this group
@@ -207,6 +221,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
         tg.kc = kc;
         tg.da = da;
         tg.db = db;
+        tg.dbp = (int32_t)up8(db);
         tg.ds12p = ds1p * ds2p;
         tg.dw2 = dw2;
         tg.nout = tg.ds12p * dw2;
@@ -223,6 +238,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
           s.row_pitch = tb->second.pitch;
           s.dw = tb->second.dw;
           s.ds12 = tb->second.ds12;
+          s.bstride = tb->second.bstride;
           s.coef_off = (int32_t)p->coefs.size();
           for (double v : ce.coef) p->coefs.push_back((float)v);
           p->sources.push_back(s);
@@ -252,9 +268,9 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   p->t3_img = zalloc(t3bytes);
   p->r_img = zalloc(rbytes);
   p->t1 = (float *)ctx.alloc(std::max<int64_t>(t1tot, 1) * sizeof(float));
-  run_pack(ctx, lops, nullptr, (int)lops.size(), L.data, true, p->l_img);
-  run_pack(ctx, rops, nullptr, (int)rops.size(), R.data, true, p->r_img);
-  p->d_psi_ops = upload_pack_ops(ctx, p->psi_ops);
+  run_pack(ctx, lops, L.data, true, p->l_img);
+  run_pack(ctx, rops, R.data, true, p->r_img);
+  p->psi_pack.upload(ctx);
   for (auto &g : g1s) {
     std::vector<int64_t> rows(g.Me);
     for (int64_t m = 0; m < g.Me; ++m) rows[m] = g.t1_off + m * g.Np;
@@ -266,15 +282,30 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   {
     std::map<std::pair<int32_t, int32_t>, std::vector<int>> by_pair;
     for (size_t t = 0; t < p->targets.size(); ++t) by_pair[tgt_key[t]].push_back((int)t);
-    const size_t nreal = by_pair.size();
+    // per pair: its input channels' T1 locations (real part), output channels
+    // and coefficient nonzeros (o, i, v); the imaginary twin of a complex pair
+    // shifts the inputs by the group's real row count and the outputs by the
+    // image's real K
+    struct PairNz {
+      int32_t o, i;
+      float v;
+    };
+    struct Built {
+      MpoPair pr;
+      std::vector<int64_t> in_im;
+      std::vector<int32_t> out_im;
+      std::vector<PairNz> nzs;  // sorted by output channel
+    };
+    std::vector<Built> built;
     for (auto &kv : by_pair) {
-      MpoPair pr{};
+      Built bd{};
+      MpoPair &pr = bd.pr;
       pr.in0 = (int32_t)p->ins.size();
       pr.out0 = (int32_t)p->outs.size();
-      pr.row0 = (int32_t)p->outs.size();
       const MpoTarget &t0 = p->targets[kv.second[0]];
       pr.da = t0.da;
       pr.db = t0.db;
+      pr.dbp = t0.dbp;
       // input channels: one per (w, s1 s2) of every distinct source block
       std::map<int64_t, int32_t> in_first;  // T1 origin -> first channel
       for (int t : kv.second) {
@@ -285,9 +316,9 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
           in_first[sr.t1_off] = (int32_t)(p->ins.size() - pr.in0);
           for (int w = 0; w < sr.dw; ++w)
             for (int s12 = 0; s12 < sr.ds12; ++s12) {
-              p->ins.push_back({sr.t1_off + (int64_t)w * sr.row_pitch + (int64_t)s12 * tg.db,
+              p->ins.push_back({sr.t1_off + (int64_t)w * sr.row_pitch + (int64_t)s12 * sr.bstride,
                                 (int64_t)sr.dw * sr.row_pitch});
-              p->in_im.push_back(sr.t1_im);
+              bd.in_im.push_back(sr.t1_im);
             }
         }
       }
@@ -299,8 +330,8 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
         out_first.push_back((int32_t)(p->outs.size() - pr.out0));
         for (int oc = 0; oc < tg.nout; ++oc) {
           p->outs.push_back({tg.img_off, tg.row0 + oc / tg.dw2, tg.ds12p,
-                             tg.k0 + (oc % tg.dw2) * tg.db, tg.kc});
-          p->out_im.push_back(tg.kim);
+                             tg.k0 + (oc % tg.dw2) * tg.dbp, tg.kc});
+          bd.out_im.push_back(tg.kim);
         }
       }
       pr.nout = (int32_t)p->outs.size() - pr.out0;
@@ -319,68 +350,78 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
                   p->coefs[sr.coef_off + ic * tg.nout + oc];
         }
       }
-      if (p->rowptr.empty()) p->rowptr.push_back(0);
-      for (int o = 0; o < pr.nout; ++o) {
+      for (int o = 0; o < pr.nout; ++o)
         for (int i = 0; i < pr.nin; ++i) {
           const float v = C[(size_t)o * pr.nin + i];
-          if (v != 0.f) p->nz.push_back({i, v});
+          if (v != 0.f) bd.nzs.push_back({o, i, v});
+        }
+      p->max_nin = std::max(p->max_nin, (int)pr.nin);
+      p->max_nout = std::max(p->max_nout, (int)pr.nout);
+      built.push_back(std::move(bd));
+    }
+    // emit the pairs (the imaginary twins after all real pairs): CSR rows
+    // and nonzero records with their inputs' T1 locations
+    if (p->rowptr.empty()) p->rowptr.push_back(0);
+    auto emit = [&](const Built &bd, bool imag) {
+      MpoPair pr = bd.pr;
+      if (imag) {
+        const int32_t out0 = (int32_t)p->outs.size();
+        for (int o = 0; o < pr.nout; ++o) {
+          MpoOut ot = p->outs[pr.out0 + o];
+          ot.col0 += bd.out_im[o];
+          p->outs.push_back(ot);
+        }
+        pr.out0 = out0;
+      }
+      pr.row0 = (int32_t)p->rowptr.size() - 1;
+      size_t k = 0;
+      for (int o = 0; o < pr.nout; ++o) {
+        for (; k < bd.nzs.size() && bd.nzs[k].o == o; ++k) {
+          const MpoIn &in = p->ins[pr.in0 + bd.nzs[k].i];
+          const int64_t base = in.base + (imag ? bd.in_im[bd.nzs[k].i] : 0);
+          UDMRG_REQUIRE(in.astride < (1LL << 31) && base % 8 == 0 && in.astride % 8 == 0,
+                        "mixed matvec: MPO-step input not 32-byte aligned");
+          p->nz.push_back({base, (int32_t)in.astride, bd.nzs[k].v});
         }
         p->rowptr.push_back((int32_t)p->nz.size());
       }
-      p->max_nin = std::max(p->max_nin, (int)pr.nin);
-      p->max_nout = std::max(p->max_nout, (int)pr.nout);
+      for (int o = 0; o < pr.nout; ++o)
+        UDMRG_REQUIRE(p->outs[pr.out0 + o].col0 % 8 == 0,
+                      "mixed matvec: MPO-step output not 16-byte aligned");
       p->mpo_bytes += (double)pr.da * pr.db * (4.0 * pr.nin + 6.0 * pr.nout);
-      // work units: one per (a', 32-wide tile of b); prefix over the pairs and
-      // the pair of every unit
-      if (p->unit0.empty()) p->unit0.push_back(0);
-      const int64_t nu = (int64_t)pr.da * ((pr.db + 31) / 32);
-      p->unit0.push_back(p->unit0.back() + nu);
-      p->unit_pair.insert(p->unit_pair.end(), nu, (int32_t)p->pairs.size());
       p->pairs.push_back(pr);
-    }
-    // complex data: every pair again on the imaginary halves (the same
-    // coefficients: T1 rows shifted by the group's real row count, T3
-    // image columns by the group's real K)
-    if (cplx) {
-      for (size_t q = 0; q < nreal; ++q) {
-        MpoPair tw = p->pairs[q];
-        const int32_t in0 = (int32_t)p->ins.size(), out0 = (int32_t)p->outs.size();
-        for (int i = 0; i < tw.nin; ++i) {
-          MpoIn in = p->ins[tw.in0 + i];
-          in.base += p->in_im[tw.in0 + i];
-          p->ins.push_back(in);
-          p->in_im.push_back(0);
-        }
-        for (int o = 0; o < tw.nout; ++o) {
-          MpoOut ot = p->outs[tw.out0 + o];
-          ot.col0 += p->out_im[tw.out0 + o];
-          p->outs.push_back(ot);
-          p->out_im.push_back(0);
-        }
-        tw.in0 = in0;
-        tw.out0 = out0;
-        p->mpo_bytes += (double)tw.da * tw.db * (4.0 * tw.nin + 6.0 * tw.nout);
-        const int64_t nu = (int64_t)tw.da * ((tw.db + 31) / 32);
-        p->unit0.push_back(p->unit0.back() + nu);
-        p->unit_pair.insert(p->unit_pair.end(), nu, (int32_t)p->pairs.size());
-        p->pairs.push_back(tw);
-      }
+    };
+    for (const Built &bd : built) emit(bd, false);
+    if (cplx)
+      for (const Built &bd : built) emit(bd, true);
+    // warp tasks: 32 units (a', 8-wide chunk of b) each, the pairs with the
+    // most work per unit (nonzeros and output channels) first
+    std::vector<int> order(p->pairs.size());
+    for (size_t q = 0; q < order.size(); ++q) order[q] = (int)q;
+    auto cost = [&](int q) {
+      const MpoPair &pr = p->pairs[q];
+      return 2 * (p->rowptr[pr.row0 + pr.nout] - p->rowptr[pr.row0]) + 3 * pr.nout;
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+    for (int q : order) {
+      const MpoPair &pr = p->pairs[q];
+      const int64_t units = (int64_t)pr.da * (pr.dbp / 8);
+      UDMRG_REQUIRE(units < (1LL << 31), "mixed matvec: sector pair too large");
+      for (int64_t u0 = 0; u0 < units; u0 += 32) p->tasks.push_back({q, (int32_t)u0});
     }
   }
   p->d_pairs = upload_vec(ctx, p->pairs);
-  p->d_ins = upload_vec(ctx, p->ins);
   p->d_outs = upload_vec(ctx, p->outs);
   p->d_rowptr = upload_vec(ctx, p->rowptr);
   p->d_nz = upload_vec(ctx, p->nz);
-  p->d_unit0 = upload_vec(ctx, p->unit0);
-  p->d_unit_pair = upload_vec(ctx, p->unit_pair);
+  p->d_tasks = upload_vec(ctx, p->tasks);
   p->mixed_flops = 6.0 * (p->g1.flops + p->g3.flops);
   ctx.sync();
   return p;
 }
 
 void SgMatvecPlan::apply(const double *psi_in, double *out) {
-  run_pack(*ctx, psi_ops, d_psi_ops, (int)psi_ops.size(), psi_in, true, psi_img);
+  run_pack(*ctx, psi_pack, psi_in, true, psi_img);
   run_tc_gemm(*ctx, g1, l_img, psi_img, t1, kTcOutF32, 1.0);
   run_mpo_step(*ctx, *this);
   run_tc_gemm(*ctx, g3, t3_img, r_img, out, cplx ? kTcOutC128 : kTcOutF64, 1.0);
@@ -390,7 +431,7 @@ void SgMatvecPlan::apply_timed(const double *psi_in, double *out, float ms[4]) {
   cudaEvent_t ev[5];
   for (auto &e : ev) UDMRG_CHECK_CUDA(cudaEventCreate(&e));
   cudaEventRecord(ev[0], ctx->stream);
-  run_pack(*ctx, psi_ops, d_psi_ops, (int)psi_ops.size(), psi_in, true, psi_img);
+  run_pack(*ctx, psi_pack, psi_in, true, psi_img);
   cudaEventRecord(ev[1], ctx->stream);
   run_tc_gemm(*ctx, g1, l_img, psi_img, t1, kTcOutF32, 1.0);
   cudaEventRecord(ev[2], ctx->stream);

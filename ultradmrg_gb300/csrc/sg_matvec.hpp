@@ -15,8 +15,15 @@
 // (real MPO coefficients) run through the real embedding: step 1 is
 // [T1r; T1i] = [[Lr, -Li], [Li, Lr]] [psi_r; psi_i] (2M x 2K GEMMs), the MPO
 // step maps both halves, step 3 is res = [T3r | T3i] [[Rr | -Ri]; [Ri | Rr]]^T
-// whose 2 dB' columns the epilogue interleaves into complex values.  T1 is FP32, its rows
-// padded to a multiple of four entries (16-byte aligned epilogue stores).
+// whose 2 dB' columns the epilogue interleaves into complex values.  T1 is FP32.
+//
+// Padding: every run of the b index (a psi block's columns (s1, s2, b) in T1
+// and in the psi image, an R block's K columns (w2, b) in the step-3 images)
+// is padded to a multiple of 8, and complex data put their imaginary K half
+// at a multiple of 8.  So each 8-wide chunk of b is 32-byte aligned in T1 and
+// one 16-byte canonical row segment of the step-3 image: the MPO step moves
+// it with vector loads and stores.  Padded entries are zero (the images are
+// zeroed once; T1 pad columns are products with zero image rows).
 #pragma once
 
 #include "gemm.hpp"
@@ -32,6 +39,7 @@ struct MpoTarget {
   int32_t k0;          // first image column (w2 = 0, b = 0)
   int32_t kc;          // K chunks of the image
   int32_t da, db;      // a' and b sector dims
+  int32_t dbp;         // db rounded up to 8 (image columns per w2)
   int32_t nout;        // output channels per (a', b): ds1' * ds2' * dw2
   int32_t ds12p;       // ds1' * ds2'
   int32_t dw2;
@@ -47,24 +55,33 @@ struct MpoSource {
   int64_t row_pitch;   // T1 elements between consecutive (a', w) rows (N_A)
   int32_t dw, ds12;    // w dim, ds1 * ds2
   int32_t coef_off;    // offset into the coefficient array
-  int32_t pad;
+  int32_t bstride;     // T1 columns between consecutive (s1, s2) (db rounded up to 8)
 };
 
-// The MPO step regrouped by (A', B) sector pair: every T1 entry of the pair
-// is an input channel (a' rows x b columns), every T3 entry an output
-// channel, and out[o] = sum_i coef[o][i] in[i] at each (a', b).
+// The MPO step regrouped by (A', B) sector pair: every T1 block (w, s1, s2)
+// channel of the pair is an input channel (a' rows x b columns), every T3
+// block (s1', s2', w2) channel an output channel, and
+// out[o] = sum_i coef[o][i] in[i] at each (a', b).
 struct MpoPair {
   int32_t in0, nin, out0, nout;
-  int32_t row0, da, db, pad;  // row0: first CSR row (output channel) of the pair
+  int32_t row0, da, db, dbp;  // row0: first CSR row (output channel) of the pair
 };
-// Nonzero of the pair's coefficient matrix (CSR): input channel and value.
-struct MpoNz {
-  int32_t i;
-  float v;
-};
+// Input channel of a pair (planning).
 struct MpoIn {
   int64_t base;     // T1 element offset of (a' = 0, b = 0)
   int64_t astride;  // T1 elements between consecutive a'
+};
+// Nonzero of a pair's coefficient matrix (CSR over the pair's output
+// channels), with its input channel's location: the kernel reads the chunk
+// at t1 + base + a' * astride + b.  base and astride are multiples of 8.
+struct MpoNzRec {
+  int64_t base;
+  int32_t astride;
+  float v;
+};
+// Work of one warp: 32 consecutive units (a', 8-wide b chunk) of one pair.
+struct MpoTask {
+  int32_t pair, u0;
 };
 struct MpoOut {
   int64_t img_off;  // byte offset of the step-3 A image of the target's group
@@ -81,8 +98,7 @@ struct SgMatvecPlan {
   float *t1 = nullptr;
   int64_t t1_size = 0;
   // psi pack ops (device resident)
-  std::vector<PackOp> psi_ops;
-  PackOp *d_psi_ops = nullptr;
+  PackList psi_pack;
   // GEMM plans
   TcPlan g1, g3;
   // MPO step
@@ -91,21 +107,16 @@ struct SgMatvecPlan {
   std::vector<float> coefs;
   // pair-grouped form (the one the kernel runs)
   std::vector<MpoPair> pairs;
-  std::vector<MpoIn> ins;
+  std::vector<MpoIn> ins;       // planning only
   std::vector<MpoOut> outs;
-  std::vector<int64_t> in_im;   // planning only: imaginary-half shift of each input
-  std::vector<int32_t> out_im;  // and image-column shift of each output
   std::vector<int32_t> rowptr;  // CSR row pointers over all output channels (+1)
-  std::vector<MpoNz> nz;
-  std::vector<int64_t> unit0;  // first work unit of each pair (prefix, pairs + 1 entries)
-  std::vector<int32_t> unit_pair;  // pair of every work unit
+  std::vector<MpoNzRec> nz;
+  std::vector<MpoTask> tasks;   // warp tasks, most expensive pair first
   MpoPair *d_pairs = nullptr;
-  MpoIn *d_ins = nullptr;
   MpoOut *d_outs = nullptr;
   int32_t *d_rowptr = nullptr;
-  MpoNz *d_nz = nullptr;
-  int64_t *d_unit0 = nullptr;
-  int32_t *d_unit_pair = nullptr;
+  MpoNzRec *d_nz = nullptr;
+  MpoTask *d_tasks = nullptr;
   int max_nin = 0, max_nout = 0;
   double mixed_flops = 0;  // tensor-core work actually issued (2MNK per group, x6 products)
   double mpo_bytes = 0;    // MPO step: 4 B per T1 entry read, 3 x 2 B per T3 entry written

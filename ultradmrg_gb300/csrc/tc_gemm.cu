@@ -99,63 +99,80 @@ __device__ __forceinline__ float narrow_f64(double x) {
 __device__ __forceinline__ float to_f32(float x) { return x; }
 __device__ __forceinline__ float to_f32(double x) { return narrow_f64(x); }
 
-// Pack sub-matrices into split-BF16 images.  A 32 x 64 tile of the source is
-// staged in shared memory (as FP32), loaded along whichever source direction
-// is contiguous, then written row by row with lanes along K (canonical
-// layout: 8 consecutive K values of a row are 16 contiguous bytes).
+// Pack sub-matrices into split-BF16 images, one 32 x 64 tile of one op per
+// work item (the tiles of all ops are spread over the grid, so one large
+// block does not serialise on one CTA).  The tile is staged in shared memory
+// (as FP32), loaded along whichever source direction is contiguous; then each
+// thread splits one row's 8 consecutive K values into three BF16 planes and
+// writes each plane with one 16-byte store (canonical layout: 8 consecutive
+// K values of a row are 16 contiguous bytes).
 template <typename T>
 __global__ void __launch_bounds__(256)
-    pack_kernel(const PackOp *__restrict__ ops, int nops, const T *__restrict__ src,
-                uint8_t *__restrict__ img) {
-  __shared__ float tile[32][65];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int o = blockIdx.x; o < nops; o += gridDim.x) {
-    const PackOp op = ops[o];
+    pack_kernel(const PackOp *__restrict__ ops, const PackTile *__restrict__ tiles, int ntiles,
+                const T *__restrict__ src, uint8_t *__restrict__ img) {
+  __shared__ float tile[64][33];  // [k][r]
+  const int tid = threadIdx.x;
+  for (int w = blockIdx.x; w < ntiles; w += gridDim.x) {
+    const PackTile pt = tiles[w];
+    const PackOp op = ops[pt.op];
     const int64_t plane = (int64_t)op.tr * kTcBK * 2;
     const int ts = op.tr == 128 ? 7 : 6;
     const bool rows_contig = op.src_rs == 1 && op.src_cs != 1;
-    for (int r0 = 0; r0 < op.rows; r0 += 32)
-      for (int k0 = 0; k0 < op.cols; k0 += 64) {
-        __syncthreads();  // the previous tile has been written out
-        for (int e = tid; e < 32 * 64; e += 256) {
-          int r, k;
-          if (rows_contig) {
-            r = e & 31;
-            k = e >> 5;
-          } else {
-            k = e & 63;
-            r = e >> 6;
-          }
-          const int rr = r0 + r, kk = k0 + k;
-          float v = 0.f;
-          if (rr < op.rows && kk < op.cols) {
-            const T x = src[op.src_off + (int64_t)rr * op.src_rs + (int64_t)kk * op.src_cs];
-            v = to_f32(x);
-            if (op.neg) v = -v;
-          }
-          tile[r][k] = v;
-        }
-        __syncthreads();
-        for (int r = warp; r < 32; r += 8) {
-          const int rs = r0 + r;
-          if (rs >= op.rows) break;
-          const int rr = op.r0 + rs;
-          const int64_t rowbase = op.img_off + (int64_t)(rr >> ts) * op.kc * 3 * plane;
-          const int rin = rr & (op.tr - 1);
-          for (int k = lane; k < 64; k += 32) {
-            const int ks = k0 + k;
-            if (ks >= op.cols) break;
-            __nv_bfloat16 h, m, l;
-            split3<float>(tile[r][k], h, m, l);
-            const int kk = op.k0 + ks;
-            const int64_t off =
-                rowbase + (int64_t)(kk >> 6) * 3 * plane + canon_off(rin, kk & 63, op.tr);
-            *(__nv_bfloat16 *)(img + off) = h;
-            *(__nv_bfloat16 *)(img + off + plane) = m;
-            *(__nv_bfloat16 *)(img + off + 2 * plane) = l;
-          }
-        }
+    __syncthreads();  // the previous tile has been read
+    for (int e = tid; e < 32 * 64; e += 256) {
+      int r, k;
+      if (rows_contig) {
+        r = e & 31;
+        k = e >> 5;
+      } else {
+        k = e & 63;
+        r = e >> 6;
       }
+      const int rr = pt.r0 + r, kk = pt.k0 + k;
+      float v = 0.f;
+      if (rr < op.rows && kk < op.cols) {
+        const T x = src[op.src_off + (int64_t)rr * op.src_rs + (int64_t)kk * op.src_cs];
+        v = to_f32(x);
+        if (op.neg) v = -v;
+      }
+      tile[k][r] = v;
+    }
+    __syncthreads();
+    const int r = tid >> 3, g = tid & 7;
+    const int rs = pt.r0 + r, ks = pt.k0 + g * 8;
+    if (rs >= op.rows || ks >= op.cols) continue;
+    const int rr = op.r0 + rs;
+    const int64_t rowbase = op.img_off + (int64_t)(rr >> ts) * op.kc * 3 * plane;
+    const int rin = rr & (op.tr - 1);
+    const int kk = op.k0 + ks;
+    if ((kk & 7) == 0) {
+      // eight values (zeros past the op's columns: padding) -> 3 x 16 bytes
+      uint32_t ph[4], pm[4], pl[4];
+#pragma unroll
+      for (int j = 0; j < 8; j += 2) {
+        __nv_bfloat16 h0, m0, l0, h1, m1, l1;
+        split3<float>(tile[g * 8 + j][r], h0, m0, l0);
+        split3<float>(tile[g * 8 + j + 1][r], h1, m1, l1);
+        ph[j >> 1] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+        pm[j >> 1] = (uint32_t)__bfloat16_as_ushort(m0) | ((uint32_t)__bfloat16_as_ushort(m1) << 16);
+        pl[j >> 1] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+      }
+      const int64_t off = rowbase + (int64_t)(kk >> 6) * 3 * plane + canon_off(rin, kk & 63, op.tr);
+      *(uint4 *)(img + off) = make_uint4(ph[0], ph[1], ph[2], ph[3]);
+      *(uint4 *)(img + off + plane) = make_uint4(pm[0], pm[1], pm[2], pm[3]);
+      *(uint4 *)(img + off + 2 * plane) = make_uint4(pl[0], pl[1], pl[2], pl[3]);
+    } else {
+      for (int j = 0; j < 8 && ks + j < op.cols; ++j) {
+        __nv_bfloat16 h, m, l;
+        split3<float>(tile[g * 8 + j][r], h, m, l);
+        const int kj = kk + j;
+        const int64_t off =
+            rowbase + (int64_t)(kj >> 6) * 3 * plane + canon_off(rin, kj & 63, op.tr);
+        *(__nv_bfloat16 *)(img + off) = h;
+        *(__nv_bfloat16 *)(img + off + plane) = m;
+        *(__nv_bfloat16 *)(img + off + 2 * plane) = l;
+      }
+    }
   }
 }
 
@@ -416,27 +433,53 @@ void TcPlan::finalize() {
   ctx->sync();
 }
 
-PackOp *upload_pack_ops(Ctx &ctx, const std::vector<PackOp> &ops) { return upload(&ctx, ops); }
+std::vector<PackTile> pack_tiles(const std::vector<PackOp> &ops) {
+  std::vector<PackTile> t;
+  for (size_t o = 0; o < ops.size(); ++o)
+    for (int32_t r0 = 0; r0 < ops[o].rows; r0 += 32)
+      for (int32_t k0 = 0; k0 < ops[o].cols; k0 += 64) t.push_back({(int32_t)o, r0, k0, 0});
+  return t;
+}
 
-void run_pack(Ctx &ctx, const std::vector<PackOp> &ops, const PackOp *d_ops, int nops,
-              const void *src, bool src_f64, uint8_t *img) {
-  if (nops == 0) return;
-  PackOp *tmp = nullptr;
-  if (!d_ops) {
-    tmp = upload(&ctx, ops);
-    d_ops = tmp;
-  }
-  const int grid = std::min(nops, 16 * ctx.num_sms);
+PackList::~PackList() {
+  if (!ctx) return;
+  ctx->free(d_ops);
+  ctx->free(d_tiles);
+}
+
+void PackList::upload(Ctx &c) {
+  ctx = &c;
+  tiles = pack_tiles(ops);
+  d_ops = udmrg::upload(ctx, ops);
+  d_tiles = udmrg::upload(ctx, tiles);
+}
+
+static void launch_pack(Ctx &ctx, const PackOp *d_ops, const PackTile *d_tiles, int ntiles,
+                        const void *src, bool src_f64, uint8_t *img) {
+  if (ntiles == 0) return;
+  const int grid = std::min(ntiles, 16 * ctx.num_sms);
   if (src_f64)
-    pack_kernel<double><<<grid, 256, 0, ctx.stream>>>(d_ops, nops, (const double *)src, img);
+    pack_kernel<double><<<grid, 256, 0, ctx.stream>>>(d_ops, d_tiles, ntiles, (const double *)src,
+                                                      img);
   else
-    pack_kernel<float><<<grid, 256, 0, ctx.stream>>>(d_ops, nops, (const float *)src, img);
+    pack_kernel<float><<<grid, 256, 0, ctx.stream>>>(d_ops, d_tiles, ntiles, (const float *)src,
+                                                     img);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches++;
-  if (tmp) {
-    ctx.sync();
-    ctx.free(tmp);
-  }
+}
+
+void run_pack(Ctx &ctx, const PackList &pl, const void *src, bool src_f64, uint8_t *img) {
+  launch_pack(ctx, pl.d_ops, pl.d_tiles, (int)pl.tiles.size(), src, src_f64, img);
+}
+
+void run_pack(Ctx &ctx, const std::vector<PackOp> &ops, const void *src, bool src_f64,
+              uint8_t *img) {
+  if (ops.empty()) return;
+  PackList pl;
+  pl.ops = ops;
+  pl.upload(ctx);
+  launch_pack(ctx, pl.d_ops, pl.d_tiles, (int)pl.tiles.size(), src, src_f64, img);
+  ctx.sync();  // the lists are freed on return
 }
 
 void run_tc_gemm(Ctx &ctx, const TcPlan &plan, const uint8_t *a_img, const uint8_t *b_img,

@@ -26,7 +26,9 @@ constexpr int64_t kTcUnitB = 3LL * kTcBN * kTcBK * 2;  // 24 KB
 // Pack one strided sub-matrix into an image (element type of the source:
 // FP64 or FP32).  Element (r, k) of the sub-matrix is
 // src[src_off + r*src_rs + k*src_cs] and lands at image row r0 + r, column
-// k0 + k.
+// k0 + k.  When k0 is a multiple of 8, the image columns from k0 + cols up to
+// the next multiple of 8 are written as zeros (16-byte stores): the planners
+// leave those columns as padding.
 struct PackOp {
   int64_t src_off, src_rs, src_cs;
   int64_t img_off;  // byte offset of the image
@@ -74,10 +76,30 @@ struct TcPlan {
 
 int64_t tc_image_bytes(int64_t rows, int64_t K, int tr);
 
-void run_pack(Ctx &ctx, const std::vector<PackOp> &ops, const PackOp *d_ops, int nops,
-              const void *src, bool src_f64, uint8_t *img);
-// Upload pack ops once (returns device copy; caller frees with ctx.free).
-PackOp *upload_pack_ops(Ctx &ctx, const std::vector<PackOp> &ops);
+// One work item of the pack kernel: a 32-row x 64-column tile of one op.
+struct PackTile {
+  int32_t op, r0, k0, pad;
+};
+std::vector<PackTile> pack_tiles(const std::vector<PackOp> &ops);
+
+// A pack list resident on the device (ops and their tiles uploaded once).
+struct PackList {
+  Ctx *ctx = nullptr;
+  std::vector<PackOp> ops;
+  std::vector<PackTile> tiles;
+  PackOp *d_ops = nullptr;
+  PackTile *d_tiles = nullptr;
+  PackList() = default;
+  PackList(const PackList &) = delete;
+  PackList &operator=(const PackList &) = delete;
+  ~PackList();
+  void upload(Ctx &c);  // builds the tiles from ops
+};
+
+void run_pack(Ctx &ctx, const PackList &pl, const void *src, bool src_f64, uint8_t *img);
+// One-shot form: uploads the ops and tiles, packs, frees them.
+void run_pack(Ctx &ctx, const std::vector<PackOp> &ops, const void *src, bool src_f64,
+              uint8_t *img);
 
 void run_tc_gemm(Ctx &ctx, const TcPlan &plan, const uint8_t *a_img, const uint8_t *b_img,
                  void *out, int out_kind, double alpha);
