@@ -49,9 +49,11 @@ typedef struct {
   udmrg_tensor *gs_vec;
   double matvec_seconds; /* device time of the matvecs (CUDA events) */
   int64_t matvecs;
-  /* mixed precision: gs_eng is the FP64 Rayleigh quotient of gs_vec (one FP64
-   * matvec); ritz_eng is the last Ritz value of the mixed-precision Krylov
-   * space.  FP64: ritz_eng = 0, fp64_matvecs = 0. */
+  /* mixed precision: the mixed-precision solve is followed by a refinement
+   * run from its Ritz vector whose first step is one FP64 matvec (an exact
+   * first row of the tridiagonal matrix); gs_eng and gs_vec are that run's
+   * Ritz value and vector, ritz_eng the Ritz value before it, and iters
+   * counts the steps of both runs.  FP64: ritz_eng = 0, fp64_matvecs = 0. */
   double ritz_eng;
   int64_t fp64_matvecs;
 } udmrg_lanczos_res;

@@ -331,15 +331,20 @@ struct KrylovSteps {
   cudaGraphExec_t exec = nullptr;
   uint64_t graph_kernels = 0;  // kernels one replay launches
   double seconds = 0;          // matvec device time (graph: whole steps)
-  KrylovSteps(Ctx &c, KrylovWork &k, MatvecPlan &m, bool with_reorth)
-      : ctx(c), kw(k), mv(m), reorth(with_reorth), graph(c.krylov_graph) {}
+  bool fp64;  // the plain FP64 matvec even for a mixed-precision plan (direct launches)
+  KrylovSteps(Ctx &c, KrylovWork &k, MatvecPlan &m, bool with_reorth, bool fp64_matvec = false)
+      : ctx(c), kw(k), mv(m), reorth(with_reorth), graph(c.krylov_graph && !fp64_matvec),
+        fp64(fp64_matvec) {}
   ~KrylovSteps() {
     if (exec) cudaGraphExecDestroy(exec);
   }
   void issue(bool timed) {
     krylov_normalise(kw);
     if (timed) cudaEventRecord(ev.a, ctx.stream);
-    mv.apply(kw.X, kw.Y);
+    if (fp64)
+      mv.apply_fp64(kw.X, kw.Y);
+    else
+      mv.apply(kw.X, kw.Y);
     if (timed) cudaEventRecord(ev.b, ctx.stream);
     krylov_alpha(kw);
     krylov_update(kw);
@@ -389,7 +394,7 @@ struct KrylovSteps {
 }  // namespace
 
 LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
-                         const LanczosParams &p, bool defer_rayleigh) {
+                         const LanczosParams &p) {
   const BTensor &S = *mv.sstruct;
   const bool cplx = S.dtype == kC128;
   const int es = elem_doubles(S.dtype);
@@ -403,17 +408,14 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
   UDMRG_REQUIRE(maxit >= 2, "Lanczos: max_iterations must be at least 2");
   VecWork w(ctx);
   Bases bases(ctx);
-  std::vector<double> a(maxit, 0.0), b(maxit, 0.0);
   LanczosResult res;
   const bool mixed = mv.sg != nullptr;
   KrylovWork kw(ctx, n, cplx, maxit);
   KrylovSteps steps(ctx, kw, mv, mixed);
-  auto finish = [&](int64_t m, const std::vector<double> &vec) {
-    res.matvec_seconds = steps.seconds;
-    if (mv.sg && (tc_check(ctx, mv.sg->g1) | tc_check(ctx, mv.sg->g3)))
-      throw Error(kErrTimeout, "tcgen05 GEMM: a bounded device wait ran out");
-    auto gs = S.clone_struct();
-    gs->alloc_data();
+  auto gs = S.clone_struct();
+  gs->alloc_data();
+  // gs = sum_i vec_i v_i
+  auto combine = [&](int64_t m, const std::vector<double> &vec) {
     std::vector<const double *> vs(bases.v.begin(), bases.v.begin() + m);
     std::vector<double> coef;
     for (int64_t i = 0; i < m; ++i) {
@@ -421,122 +423,90 @@ LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
       if (cplx) coef.push_back(0.0);
     }
     lincomb(w, gs->data, vs, coef, n, cplx);
-    res.ritz_eng = res.gs_eng;
-    if (mixed && !defer_rayleigh) {
-      // reported energy: FP64 Rayleigh quotient of the mixed-precision eigenvector
-      double *y = (double *)ctx.alloc(vbytes);
-      mv.apply_fp64(gs->data, y);
-      const double num = dot(w, gs->data, y, n, cplx).real();
-      const double den = dot(w, gs->data, gs->data, n, cplx).real();
-      ctx.free(y);
-      res.gs_eng = num / den;
-      res.fp64_matvecs = 1;
+  };
+  // One Lanczos run from the vector in Y (krylov_begin): step m normalises
+  // gamma_{m-1} into v_m, then gamma_m = H v_m - a_m v_m - b_{m-1} v_{m-1};
+  // with mixed precision gamma is then projected against every basis vector
+  // (FP64 classical Gram-Schmidt, a second pass where the first removed more
+  // than half of |gamma|^2), so rounding in the matvec cannot build up ghost
+  // Ritz values.  alpha and |gamma| reach the host once per step; the
+  // convergence test on the (m+1)-dimensional tridiagonal matrix follows
+  // (lanczos_vmps_solver_impl.h:203-235).  first: the steps object of step 0.
+  // Returns the Ritz value and leaves the Ritz vector in gs.
+  auto run = [&](KrylovSteps &first, bool noise_stop, int64_t &iters) {
+    std::vector<double> a(maxit, 0.0), b(maxit, 0.0);
+    int64_t m = 0;
+    double energy0 = 0.0;
+    while (true) {
+      if ((int64_t)bases.v.size() <= m) bases.v.push_back((double *)ctx.alloc(vbytes));
+      kw.push((int)m, bases.v[m]);
+      (m == 0 ? first : steps).run();
+      res.matvecs++;
+      a[m] = kw.hres[0];
+      const double n2 = kw.hres[1];
+      if (m == 0) {
+        energy0 = a[0];
+      } else {
+        const double e_new = tridiag_lowest(a, b, m + 1, nullptr);
+        // mixed precision also stops once the Ritz value no longer moves above
+        // the rounding level of the split-BF16 products
+        const bool noise_floor =
+            noise_stop && std::fabs(energy0 - e_new) <= 1e-12 * std::fabs(e_new);
+        if ((energy0 - e_new) < p.error || noise_floor || m == eff_dim || m == maxit - 1) {
+          std::vector<double> vec;
+          tridiag_lowest(a, b, m + 1, &vec);
+          iters = m + 1;
+          combine(m + 1, vec);
+          return e_new;
+        }
+        energy0 = e_new;
+      }
+      const double norm_gamma = std::sqrt(n2);
+      if (norm_gamma == 0.0) {  // invariant subspace
+        std::vector<double> vec = {1.0};
+        if (m > 0) tridiag_lowest(a, b, m + 1, &vec);
+        iters = m + 1;
+        combine(m + 1, vec);
+        return energy0;
+      }
+      b[m] = norm_gamma;
+      m += 1;
     }
-    return gs;
   };
   // Y = init; step 0 normalises it into bases[0] (QuasiNormalize)
   {
     auto v0 = embed(ctx, init_state, S);
     krylov_begin(kw, v0->data);
   }
-  // Step m: v_m = gamma_{m-1} / |gamma_{m-1}|, gamma_m = H v_m - a_m v_m -
-  // b_{m-1} v_{m-1}; with mixed precision gamma is then projected against
-  // every basis vector (FP64 classical Gram-Schmidt, a second pass where the
-  // first removed more than half of |gamma|^2), so rounding in the matvec
-  // cannot build up ghost Ritz values.  alpha and |gamma| reach the host once
-  // per step; the convergence test on the (m+1)-dimensional tridiagonal
-  // matrix follows.
-  int64_t m = 0;
-  double energy0 = 0.0;
-  while (true) {
-    double *vm = (double *)ctx.alloc(vbytes);
-    bases.v.push_back(vm);
-    kw.push((int)m, vm);
-    steps.run();
-    res.matvecs++;
-    a[m] = kw.hres[0];
-    const double n2 = kw.hres[1];
-    if (m == 0) {
-      energy0 = a[0];
-    } else {
-      const double e_new = tridiag_lowest(a, b, m + 1, nullptr);
-      // mixed precision also stops once the Ritz value no longer moves above
-      // the rounding level of the split-BF16 products
-      const bool noise_floor = mixed && std::fabs(energy0 - e_new) <= 1e-12 * std::fabs(e_new);
-      if ((energy0 - e_new) < p.error || noise_floor || m == eff_dim || m == maxit - 1) {
-        std::vector<double> vec;
-        tridiag_lowest(a, b, m + 1, &vec);
-        res.iters = m + 1;
-        res.gs_eng = e_new;
-        res.gs_vec = finish(m + 1, vec);
-        return res;
-      }
-      energy0 = e_new;
-    }
-    const double norm_gamma = std::sqrt(n2);
-    if (norm_gamma == 0.0) {  // invariant subspace
-      std::vector<double> vec = {1.0};
-      if (m > 0) tridiag_lowest(a, b, m + 1, &vec);
-      res.iters = m + 1;
-      res.gs_eng = energy0;
-      res.gs_vec = finish(m + 1, vec);
-      return res;
-    }
-    b[m] = norm_gamma;
-    m += 1;
+  int64_t it1 = 0;
+  double e = run(steps, mixed, it1);
+  res.iters = it1;
+  if (mixed) {
+    // Refinement.  The mixed-precision Krylov space converges to an
+    // eigenvector of the rounded operator; its error (first order in the
+    // split-BF16 rounding over the spectral gap) would enter the truncation
+    // and the environments.  A second Lanczos run starts from that vector
+    // with one FP64 step: alpha_0 = <psi|H psi> and the residual gamma_0 =
+    // H psi - alpha_0 psi are exact, so the tridiagonal matrix couples psi
+    // to the correction space exactly, and the mixed-precision steps after
+    // it only build the correction space (their rounding enters the Ritz
+    // vector scaled by the correction's size, the energy by its square).
+    // It stops by the same rule; near convergence that is one or two steps.
+    res.ritz_eng = e;
+    krylov_begin(kw, gs->data);
+    KrylovSteps first(ctx, kw, mv, true, /*fp64_matvec=*/true);
+    int64_t it2 = 0;
+    e = run(first, false, it2);
+    steps.seconds += first.seconds;
+    res.iters += it2;
+    res.fp64_matvecs = 1;
   }
-}
-
-namespace {
-// Makes the context's side stream its current one for the guard's lifetime
-// (every launch and stream-ordered allocation in between goes there).
-struct SideStream {
-  Ctx &ctx;
-  explicit SideStream(Ctx &c) : ctx(c) { std::swap(ctx.stream, ctx.side); }
-  ~SideStream() { std::swap(ctx.stream, ctx.side); }
-};
-}  // namespace
-
-void PendingEnergy::launch(Ctx &c, std::unique_ptr<MatvecPlan> plan, TensorPtr state) {
-  ctx = &c;
-  mv = std::move(plan);
-  psi = std::move(state);
-  UDMRG_CHECK_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
-  UDMRG_CHECK_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
-  UDMRG_CHECK_CUDA(cudaEventRecord(ready, c.stream));  // psi is complete
-  UDMRG_CHECK_CUDA(cudaStreamWaitEvent(c.side, ready, 0));
-  {
-    SideStream guard(c);
-    const bool cplx = psi->dtype == kC128;
-    const int64_t n = psi->size();
-    y = (double *)c.alloc(std::max<int64_t>(n, 1) * elem_doubles(psi->dtype) * sizeof(double));
-    res = (double *)c.alloc(4 * sizeof(double));
-    mv->apply_fp64(psi->data, y);
-    VecWork w(c);  // its buffers are freed on the side stream too
-    dot_async(w, psi->data, y, n, cplx, res);
-    dot_async(w, psi->data, psi->data, n, cplx, res + 2);
-  }
-  UDMRG_CHECK_CUDA(cudaEventRecord(done, c.side));
-}
-
-double PendingEnergy::value() {
-  if (resolved) return energy;
-  UDMRG_CHECK_CUDA(cudaEventSynchronize(done));
-  double h[4];
-  UDMRG_CHECK_CUDA(cudaMemcpy(h, res, sizeof(h), cudaMemcpyDeviceToHost));
-  energy = h[0] / h[2];
-  resolved = true;
-  return energy;
-}
-
-PendingEnergy::~PendingEnergy() {
-  if (!ctx) return;
-  if (done) cudaEventSynchronize(done);
-  // buffers used on the side stream go back to the pool in its order
-  if (y) cudaFreeAsync(y, ctx->side);
-  if (res) cudaFreeAsync(res, ctx->side);
-  if (ready) cudaEventDestroy(ready);
-  if (done) cudaEventDestroy(done);
+  res.gs_eng = e;
+  res.matvec_seconds = steps.seconds;
+  if (mv.sg && (tc_check(ctx, mv.sg->g1) | tc_check(ctx, mv.sg->g3)))
+    throw Error(kErrTimeout, "tcgen05 GEMM: a bounded device wait ran out");
+  res.gs_vec = std::move(gs);
+  return res;
 }
 
 ExpmvResult lanczos_expmv(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state, double step,
@@ -672,19 +642,11 @@ static double now() {
       .count();
 }
 
-void PendingSlot::resolve() {
-  if (!pe) return;
-  e0 = pe->value();
-  if (log && idx >= 0) (*log)[idx].e0 = e0;
-  pe.reset();
-  idx = -1;
-}
-
 static void two_site_update(Ctx &ctx, std::vector<TensorPtr> &mps,
                             std::vector<TensorPtr> &lenvs, std::vector<TensorPtr> &renvs,
                             const std::vector<const BTensor *> &mpo, const SweepParams &p,
                             char dir, int64_t target, std::vector<SiteLog> *log,
-                            LearnState *learn, PendingSlot &slot) {
+                            LearnState *learn, double &e0) {
   const int64_t N = (int64_t)mps.size();
   int64_t l, r, lenv_len, renv_len;
   if (dir == 'r') {
@@ -757,8 +719,7 @@ static void two_site_update(Ctx &ctx, std::vector<TensorPtr> &mps,
     }
   }
   auto res = two_site_update_local(ctx, *lenvs[lenv_len], *renvs[renv_len], *mps[l], *mps[r],
-                                   *mpo[l], *mpo[r], p, dir, &lg, hp, learn ? &now : nullptr,
-                                   &slot);
+                                   *mpo[l], *mpo[r], p, dir, &lg, hp, learn ? &now : nullptr);
   lg.site = target;
   if (learn) {
     // kept counts of this update per bond QN = the new bond index of mps[l]
@@ -784,12 +745,7 @@ static void two_site_update(Ctx &ctx, std::vector<TensorPtr> &mps,
     lenvs[lenv_len + 1] = std::move(res.env);
   else
     renvs[renv_len + 1] = std::move(res.env);
-  if (slot.pe) {  // energy still on its way: the slot fills the entry
-    slot.log = log;
-    slot.idx = log ? (int64_t)log->size() : -1;
-  } else {
-    slot.e0 = lg.e0;
-  }
+  e0 = lg.e0;
   if (log) log->push_back(lg);
 }
 
@@ -797,19 +753,16 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
                                   const BTensor &mps_l, const BTensor &mps_r,
                                   const BTensor &mpo_l, const BTensor &mpo_r,
                                   const SweepParams &p, char dir, SiteLog *log,
-                                  const SketchHint *hint, BondSpectra *spectra,
-                                  PendingSlot *slot) {
+                                  const SketchHint *hint, BondSpectra *spectra) {
   UDMRG_REQUIRE(dir == 'r' || dir == 'l', "dir must be 'r' or 'l'");
   const double t0 = now();
   auto init_state = contract_axes(ctx, mps_l, mps_r, {2}, {0});
   auto mv = plan_matvec2(ctx, lenv, mpo_l, mpo_r, renv, *init_state, p.lancz.precision);
-  const bool mixed = mv->sg != nullptr;
-  if (slot) slot->resolve();  // the previous update's energy
-  auto lres = lanczos_gs(ctx, *mv, *init_state, p.lancz, /*defer_rayleigh=*/mixed);
+  auto lres = lanczos_gs(ctx, *mv, *init_state, p.lancz);
   const double t1 = now();
   const double mvflops = mv->flops;
   init_state.reset();
-  if (!mixed) mv.reset();
+  mv.reset();
   const BTensor &psi = *lres.gs_vec;
   const QN ldiv = mps_l.div();
   const int split = dir == 'r' ? kSvdSplitLeft : kSvdSplitRight;
@@ -847,14 +800,6 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
       audit_sec = now() - ta;
     }
   }
-  // mixed precision: the FP64 Rayleigh quotient of psi runs on the side
-  // stream beside the environment update (and, in a sweep, the next
-  // update's planning); it owns the plan and psi from here
-  std::unique_ptr<PendingEnergy> pe;
-  if (mixed) {
-    pe = std::make_unique<PendingEnergy>();
-    pe->launch(ctx, std::move(mv), std::move(lres.gs_vec));
-  }
   lres.gs_vec.reset();
   if (spectra) {
     spectra->clear();
@@ -871,15 +816,7 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
   else
     out.env = update_site_renv(ctx, renv, *out.mps_r, mpo_r);
   ctx.sync();
-  double e0 = lres.gs_eng;
-  if (mixed) {
-    if (slot) {
-      e0 = std::numeric_limits<double>::quiet_NaN();  // filled in by the slot
-      slot->pe = std::move(pe);
-    } else {
-      e0 = pe->value();
-    }
-  }
+  const double e0 = lres.gs_eng;
   const double t3 = now();
   {
     int64_t sk = 0;
@@ -921,15 +858,14 @@ double two_site_finite_vmps(Ctx &ctx, std::vector<TensorPtr> &mps,
     learn->prev.assign(N, {});
     learn->prev_kept.assign(N, {});
   }
-  PendingSlot slot;  // destroyed before the environments it reads
+  double e0 = 0.0;
   for (int64_t s = 0; s < p.sweeps; ++s) {
     for (int64_t i = 0; i < N - 2; ++i)
-      two_site_update(ctx, mps, lenvs, renvs, W, p, 'r', i, log, learn, slot);
+      two_site_update(ctx, mps, lenvs, renvs, W, p, 'r', i, log, learn, e0);
     for (int64_t i = N - 1; i > 1; --i)
-      two_site_update(ctx, mps, lenvs, renvs, W, p, 'l', i, log, learn, slot);
+      two_site_update(ctx, mps, lenvs, renvs, W, p, 'l', i, log, learn, e0);
   }
-  slot.resolve();
-  return slot.e0;
+  return e0;
 }
 
 namespace {

@@ -69,35 +69,18 @@ struct LanczosResult {
   TensorPtr gs_vec;
   double matvec_seconds = 0;  // device time spent in matvecs (CUDA events)
   int64_t matvecs = 0;
-  double ritz_eng = 0;       // mixed precision: the last Ritz value
-  int64_t fp64_matvecs = 0;  // mixed precision: FP64 matvecs (final Rayleigh quotient)
+  double ritz_eng = 0;       // mixed precision: the Ritz value before the refinement
+  int64_t fp64_matvecs = 0;  // mixed precision: FP64 matvecs (the refinement's first step)
 };
 
 // Ground state by Lanczos (lanczos_vmps_solver_impl.h:114-248): three-term
 // recurrence (FP64 form: without reorthogonalisation, as the reference),
 // all bases kept on the device, FP64 tridiagonal eigenproblem on the host.
-// With the mixed-precision matvec the reported energy is the FP64 Rayleigh
-// quotient of the eigenvector; defer_rayleigh leaves it to the caller
-// (gs_eng is then the Ritz value; see PendingEnergy).
+// With the mixed-precision matvec the solve is followed by a refinement run
+// started from its Ritz vector whose first step is an FP64 matvec; gs_eng is
+// that run's Ritz value (ritz_eng: the first run's).
 LanczosResult lanczos_gs(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state,
-                         const LanczosParams &p, bool defer_rayleigh = false);
-
-// FP64 Rayleigh quotient <psi|H|psi> / <psi|psi> computed on the context's
-// side stream while the main stream goes on (the truncated SVD and the
-// environment update read psi and the environments too, but write neither).
-// The plan and psi are owned here until value() has waited for the result.
-struct PendingEnergy {
-  Ctx *ctx = nullptr;
-  std::unique_ptr<MatvecPlan> mv;
-  TensorPtr psi;
-  double *y = nullptr, *res = nullptr;
-  cudaEvent_t ready = nullptr, done = nullptr;
-  bool resolved = false;
-  double energy = 0.0;
-  void launch(Ctx &c, std::unique_ptr<MatvecPlan> plan, TensorPtr state);
-  double value();
-  ~PendingEnergy();
-};
+                         const LanczosParams &p);
 
 // exp(-i dt H_eff) psi (lanczos_expmv_solver_impl.h:70-184).
 struct ExpmvResult {
@@ -160,29 +143,14 @@ using BondSpectra = std::vector<std::pair<QN, std::vector<double>>>;
 struct LocalUpdate {
   TensorPtr mps_l, mps_r, env;
 };
-// A mixed-precision update's FP64 energy still being computed on the side
-// stream, carried to the next update of a sweep (which collects it after its
-// matvec plan is built, so the Rayleigh quotient overlaps the environment
-// update and the host-side planning).  resolve() writes it into the log.
-struct PendingSlot {
-  std::unique_ptr<PendingEnergy> pe;
-  std::vector<SiteLog> *log = nullptr;
-  int64_t idx = -1;  // log entry waiting for the energy
-  double e0 = 0.0;   // the last resolved energy
-  void resolve();
-};
-
 // hint: sketch sizes for the randomized SVD (learned mode); spectra: receives
-// the leading singular values of every bond sector of this update.  With a
-// slot, the previous update's pending energy is resolved before this
-// update's Lanczos and this update's (mixed precision) is left pending there;
-// log->e0 is then filled in by the slot.
+// the leading singular values of every bond sector of this update.
 LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &renv,
                                   const BTensor &mps_l, const BTensor &mps_r,
                                   const BTensor &mpo_l, const BTensor &mpo_r,
                                   const SweepParams &p, char dir, SiteLog *log,
                                   const SketchHint *hint = nullptr,
-                                  BondSpectra *spectra = nullptr, PendingSlot *slot = nullptr);
+                                  BondSpectra *spectra = nullptr);
 
 // Learned truncation state: the rank model (used when svd_mode ==
 // kSvdSketchLearned), the spectra and kept counts of every bond at its last

@@ -15,7 +15,9 @@ full sweep is timed from that same state in each form:
   the predicted sketch exceeds a fraction of the sector dimensions).
 
 A form name may end in ``@<tol>`` (e.g. ``mixed_exact@1e-11``): that form's
-Lanczos runs to that tolerance instead of ``--lanczos-error``.  Each form is
+Lanczos runs to that tolerance instead of ``--lanczos-error``.  With
+``--sweeps k`` each form runs k sweeps (``sweep_seconds`` is per sweep,
+``sweep_energies`` the energy at the end of each).  Each form is
 compared with the FP64 form of the same tolerance (``fp64_exact`` with the
 same suffix) when it is in the list.
 
@@ -75,6 +77,7 @@ def main(argv=None):
     ap.add_argument("--forms", default="fp64_exact,mixed_exact,mixed_learned")
     ap.add_argument("--audit", action="store_true")
     ap.add_argument("--lanczos-error", type=float, default=1e-9)
+    ap.add_argument("--sweeps", type=int, default=1, help="sweeps of each timed form")
     ap.add_argument("--max-fraction", type=float, default=0.1,
                     help="sketch fraction above which the learned form runs the exact SVD "
                          "(form mixed_learned_rule)")
@@ -94,7 +97,7 @@ def main(argv=None):
         lerr = float(tol) if tol else a.lanczos_error
         prec = api.PREC_FP64 if base.startswith("fp64") else api.PREC_MIXED
         mode = 2 if "learned" in base else 0
-        p = api.FiniteVMPSSweepParams(1, a.D, a.D, 1e-8, lerr, 100, precision=prec,
+        p = api.FiniteVMPSSweepParams(a.sweeps, a.D, a.D, 1e-8, lerr, 100, precision=prec,
                                       svd_mode=mode, svd_audit=base.endswith("audit"),
                                       svd_sketch_max_fraction=(a.max_fraction
                                                                if base.endswith("rule") else 1.0))
@@ -111,7 +114,9 @@ def main(argv=None):
             e0, log = api.two_site_finite_vmps(ctx, mps, dmpo, p)
         ctx.sync()
         sec = time.perf_counter() - t1
-        f = dict(sweep_seconds=sec, e0=e0,
+        per = 2 * (N - 2)  # updates per sweep
+        f = dict(sweep_seconds=sec / a.sweeps, e0=e0,
+                 sweep_energies=[log[(k + 1) * per - 1]["e0"] for k in range(a.sweeps)],
                  lanczos_seconds=sum(r["lancz_sec"] for r in log),
                  svd_seconds=sum(r["svd_sec"] for r in log),
                  env_seconds=sum(r["env_sec"] for r in log),
