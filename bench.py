@@ -11,6 +11,12 @@ with host buffers (pinned host -> device copy of psi, matvec, device -> host
 copy of the result, every step).  FLOPs are algorithmic: sum of 2*M*N*K over
 the block-pair GEMMs of the schedule.
 
+The metric's other half, sweep seconds, comes from the sweep leg
+(``sweep_leg``): the same cylinder grown to a near-converged D = 2000 state,
+then one timed two-site sweep in the plain FP64 form, the mixed form and the
+mixed form with learned truncation (keys ``sweep_*`` and ``sweep``, with the
+clocks sampled during each sweep).
+
 ``--impl reference`` times the CPU FP64 oracle on the same workload: one
 forked process per host core, each running the numpy matvec with
 single-threaded OpenBLAS on some of the left environment's bra sectors, the
@@ -22,15 +28,15 @@ subprocess.
 import argparse
 import json
 import os
-import statistics
 import subprocess
 import sys
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
+
+from ultradmrg_gb300.clocks import ClockSampler  # noqa: E402
 
 METRIC = ("two-site matvec TFLOP/s (H_eff*psi, U(1)xU(1) block-sparse; algorithmic FLOPs; "
           "mixed split-BF16 tensor-core form, plain FP64 reported beside)")
@@ -51,7 +57,11 @@ def parse():
                     help="seconds of CPU work for the cpu_baseline sample")
     ap.add_argument("--matvec-only", action="store_true",
                     help="time the mixed matvec only (profiling runs): no FP64 form, "
-                         "Lanczos, local updates, e2e or CPU baseline")
+                         "Lanczos, local updates, sweeps, e2e or CPU baseline")
+    ap.add_argument("--no-sweep", action="store_true",
+                    help="leave out the sweep leg (profiling runs of the matvec and updates)")
+    ap.add_argument("--sweep-schedule", default="10:2,100:2,500:2,1000:2,2000:2",
+                    help="D:sweeps,... that grows the Hubbard 4x16 state before the timed sweeps")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 20 if args.impl == "reference" else 2000
@@ -63,62 +73,6 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
-
-
-class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
-
-    def __init__(self, index):
-        self.index = index
-        self.proc = None
-        self.lines = []
-
-    def __enter__(self):
-        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
-        try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
-        except OSError:
-            self.proc = None
-        return self
-
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
-
-    def __exit__(self, *a):
-        if self.proc:
-            self.proc.terminate()
-            try:
-                self.proc.wait(timeout=5)
-            except subprocess.TimeoutExpired:
-                self.proc.kill()
-
-    def summary(self):
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            p = [x.strip() for x in ln.split(",")]
-            if len(p) < 9:
-                continue
-            try:
-                sm.append(float(p[1]))
-                mx.append(float(p[2]))
-            except ValueError:
-                continue
-            for n, v in zip(names, p[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
-                "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def measured_peaks():
@@ -235,6 +189,79 @@ def krylov_graph_probe(api, ctx, ops, psi, prec, reps=2):
     return {"graph_sec": tg, "direct_sec": td, "iters": rg[0],
             "us_per_step_graph": tg / rg[0] * 1e6, "us_per_step_direct": td / rd[0] * 1e6,
             "identical": rg == rd}
+
+
+def sweep_leg(api, ctx, local, schedule):
+    """The other half of the metric: one full two-site sweep (right then left,
+    as ``TwoSiteFiniteVMPSSweep``) of the Hubbard 4x16 cylinder (t=1, U=8, 56
+    electrons, U(1)xU(1)) at D = 2000, truncation 1e-8, Lanczos (1e-9, 100),
+    timed in each form from one prepared near-converged state: the reference
+    benchmark grows D over calls of the sweep driver and times a sweep at
+    D = 2000 (``benchmark/ultradmrg_hubbard2d.cpp:227-252``).  The state is
+    grown by ``schedule`` in the mixed form (exact SVD; the rank model records
+    each bond's spectra for the learned form).  Forms: plain FP64 block GEMMs +
+    exact SVD; split-BF16 tensor-core matvec + exact SVD; the same with the
+    learned truncation (randomized SVD sized by the rank model where the
+    predicted sketch is below a tenth of the sector, exact SVD elsewhere).
+    nvidia-smi clocks are sampled during each sweep."""
+    import numpy as np
+    from ultradmrg_gb300 import sweep_compare as SC
+    t0 = time.perf_counter()
+    _, dmpo, state, model, prep, _ = SC.prepare(ctx, 16, 4, schedule, 1e-9)
+    prep_s = time.perf_counter() - t0
+    N = len(state)
+    forms, logs = {}, {}
+    for name, prec, mode, frac in (("fp64_exact", api.PREC_FP64, 0, 1.0),
+                                   ("mixed_exact", api.PREC_MIXED, 0, 1.0),
+                                   ("mixed_learned", api.PREC_MIXED, 2, 0.1)):
+        p = api.FiniteVMPSSweepParams(1, 2000, 2000, 1e-8, 1e-9, 100, precision=prec,
+                                      svd_mode=mode, svd_sketch_max_fraction=frac)
+        mps = [api.DeviceTensor.from_data(ctx, t) for t in state]
+        hist = None
+        if mode == 2:  # a model carrying the bond history of the prepared state
+            hist = api.RankModel(ctx, 0)
+            hist.params = model.params
+            hist.copy_history_from(model)
+        ctx.sync()
+        with ClockSampler(local) as clk:
+            t1 = time.perf_counter()
+            if hist is not None:
+                e0, log, _, _ = api.two_site_finite_vmps_learned(ctx, mps, dmpo, p, hist, False)
+            else:
+                e0, log = api.two_site_finite_vmps(ctx, mps, dmpo, p)
+            ctx.sync()
+            sec = time.perf_counter() - t1
+        forms[name] = {
+            "sweep_s": sec, "e0": e0,
+            "lanczos_s": sum(r["lancz_sec"] for r in log),
+            "svd_s": sum(r["svd_sec"] for r in log),
+            "env_s": sum(r["env_sec"] for r in log),
+            "lanczos_iters": int(sum(r["iters"] for r in log)),
+            "updates": len(log), "max_trunc_err": max(r["trunc_err"] for r in log),
+            "svd_grow_rounds": int(sum(r["svd_grow_rounds"] for r in log)),
+            "clocks": clk.summary()}
+        logs[name] = log
+        for t in mps:
+            t.close()
+        if hist is not None:
+            hist.close()
+    ref = forms["fp64_exact"]
+    e_ref = np.array([r["e0"] for r in logs["fp64_exact"]])
+    t_ref = np.array([r["trunc_err"] for r in logs["fp64_exact"]])
+    for name in ("mixed_exact", "mixed_learned"):
+        f = forms[name]
+        f["speedup_vs_fp64"] = ref["sweep_s"] / f["sweep_s"]
+        f["rel_dE_vs_fp64"] = abs(f["e0"] - ref["e0"]) / abs(ref["e0"])
+        e = np.array([r["e0"] for r in logs[name]])
+        t = np.array([r["trunc_err"] for r in logs[name]])
+        f["max_site_rel_dE_vs_fp64"] = float(np.max(np.abs(e - e_ref) / np.abs(e_ref)))
+        f["max_trunc_err_diff_vs_fp64"] = float(np.max(np.abs(t - t_ref)))
+    for t in dmpo:
+        t.close()
+    model.close()
+    return {"workload": "hubbard4x16 cylinder, D=2000, trunc 1e-8, Lanczos (1e-9, 100)",
+            "sites": N, "preparation": prep, "preparation_s": prep_s, "schedule": schedule,
+            "forms": forms}
 
 
 def cpu_threads():
@@ -434,6 +461,12 @@ def run_ours(args):
         for t in (na, nb, ne):
             t.close()
 
+    sweep = None
+    if not args.no_sweep:
+        for t in (A1d, A2d):
+            t.close()
+        sweep = sweep_leg(api, ctx, local, args.sweep_schedule)
+
     # e2e through the C ABI with host buffers
     try:
         import torch
@@ -466,31 +499,30 @@ def run_ours(args):
     fp64_peak = ctx.fp64_peak_tflops()
     peaks = measured_peaks()
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
-    # dominant kernel: the longest of the four stages of one mixed matvec.
-    # Tensor-core stages: algorithmic flops of the matching FP64 contraction
-    # against the bf16 peak; memory-bound stages (psi pack, MPO step):
-    # algorithmic HBM bytes against the measured copy bandwidth
+    # dominant kernel: the longest of the stages of one mixed matvec.  Every
+    # stage moves its operands through HBM (split-BF16 images, FP32 T1, FP64
+    # psi and result): achieved = its algorithmic bytes (plan.stage_bytes)
+    # over its event-timed duration, against the measured copy bandwidth; the
+    # tensor-core work it issued (six split products) is reported beside
     dom = max(range(4), key=lambda i: ms_mx[i])
     stage_names = ["pack_kernel (psi split-BF16 images)", "tc_gemm_kernel (GEMM L.psi)",
-                   "mpo_unit_kernel (MPO step)", "tc_gemm_kernel (GEMM .R)"]
-    if dom in (1, 3):
-        alg_dom = fl_64[0] if dom == 1 else fl_64[3]
-        roof = {"bound": "tensor", "achieved": alg_dom / (ms_mx[dom] / 1e3) / 1e12,
-                "peak": bf16_peak, "unit": "TFLOP/s",
-                "peak_source": "bf16_tflops of MEASURED_PEAKS.json (burst), of measured",
-                "issued_tensor_tflops": fl_mx[dom] / (ms_mx[dom] / 1e3) / 1e12}
-    else:
-        byts = plan.stage_bytes()[dom]
-        hbm = peaks.get("hbm_gbs", 6800.0)
-        roof = {"bound": "hbm", "achieved": byts / (ms_mx[dom] / 1e3) / 1e9, "peak": hbm,
-                "unit": "GB/s", "algorithmic_bytes": byts,
-                "peak_source": ("hbm_gbs of MEASURED_PEAKS.json, of measured" if "hbm_gbs" in peaks
-                                else "fallback 6.8 TB/s")}
+                   "mpo_chunk_kernel (MPO step)",
+                   "tc_mpo_gemm_kernel (MPO step fused into GEMM .R)"]
+    byts = plan.stage_bytes()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    roof = {"bound": "hbm", "achieved": byts[dom] / (ms_mx[dom] / 1e3) / 1e9, "peak": hbm,
+            "unit": "GB/s", "algorithmic_bytes": byts[dom],
+            "peak_source": ("hbm_gbs of MEASURED_PEAKS.json, of measured" if "hbm_gbs" in peaks
+                            else "fallback 6.8 TB/s")}
+    if fl_mx[dom] > 0:
+        roof["issued_tensor_tflops"] = fl_mx[dom] / (ms_mx[dom] / 1e3) / 1e12
+        roof["issued_tensor_frac"] = roof["issued_tensor_tflops"] / bf16_peak
     roof["frac"] = roof["achieved"] / roof["peak"]
     roof["kernel"] = stage_names[dom]
     roof["traffic"] = ncu_traffic(w.name, stage_names[dom].split()[0])
     roof["stage_ms"] = {"psi_pack": ms_mx[0], "gemm_L_psi": ms_mx[1], "mpo_step": ms_mx[2],
-                        "gemm_R": ms_mx[3]}
+                        "gemm_R_with_mpo_step": ms_mx[3]}
+    roof["stage_gbs"] = [b / (t / 1e3) / 1e9 if t > 0 else 0.0 for b, t in zip(byts, ms_mx)]
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
@@ -533,6 +565,17 @@ def run_ours(args):
         "clocks": clk.summary(),
         "wall_seconds_timed": wall,
     }
+    if sweep is not None:
+        fs = sweep["forms"]
+        line["sweep_fp64_s"] = fs["fp64_exact"]["sweep_s"]
+        line["sweep_mixed_s"] = fs["mixed_exact"]["sweep_s"]
+        line["sweep_mixed_learned_s"] = fs["mixed_learned"]["sweep_s"]
+        line["sweep_speedup_mixed_vs_fp64"] = fs["mixed_exact"]["speedup_vs_fp64"]
+        line["sweep_speedup_mixed_learned_vs_fp64"] = fs["mixed_learned"]["speedup_vs_fp64"]
+        line["sweep_rel_dE_mixed_vs_fp64"] = fs["mixed_exact"]["rel_dE_vs_fp64"]
+        line["sweep_max_trunc_err_diff_mixed_vs_fp64"] = fs["mixed_exact"][
+            "max_trunc_err_diff_vs_fp64"]
+        line["sweep"] = sweep
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, w)
     if rank == 0:

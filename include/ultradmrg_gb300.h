@@ -319,16 +319,24 @@ int udmrg_matvec_plan_destroy(udmrg_matvec_plan *p);
 /* One matvec with CUDA events between its four stages (device ms, written to
  * ms[4]) and the work of each stage in FLOP (flops[4]: algorithmic for the
  * FP64 form; tensor-core work issued, six split products included, for the
- * mixed form).  Mixed stages: psi pack, GEMM L.psi, MPO step, GEMM .R;
+ * mixed form).  Mixed stages: psi pack, GEMM L.psi, MPO step, GEMM .R (with
+ * the fused MPO step: stage 2 is empty and stage 3 times the fused kernel);
  * FP64 stages: the four block contractions. */
 int udmrg_matvec_plan_stage_times(udmrg_matvec_plan *p, const double *d_in, double *d_out,
                                   double *ms, double *flops);
-/* Algorithmic HBM bytes of the mixed form's memory-bound stages (bytes[4],
- * same order as the stage times): psi pack (FP64 read, three BF16 planes
- * written per element) and the MPO step (FP32 T1 entries read, three BF16
- * planes written per T3 entry); 0 for the two tensor-core stages and for
- * the FP64 form. */
+/* Algorithmic HBM bytes of the mixed form's stages (bytes[4], same order as
+ * the stage times): psi pack (FP64 read, three BF16 planes written per
+ * element); GEMM L.psi (both split-BF16 images read, FP32 T1 entries
+ * written); unfused: the MPO step (FP32 T1 entries read, three BF16 planes
+ * written per T3 entry) and GEMM .R (T3 and R images read, FP64 result
+ * written); fused: stage 3 reads each FP32 T1 entry and the R image once and
+ * writes the FP64 result.  0 for the FP64 form. */
 int udmrg_matvec_plan_stage_bytes(udmrg_matvec_plan *p, double *bytes);
+/* Mixed form: run the MPO step inside the producers of the .R GEMM (enable =
+ * 1, the default) or as its own kernel writing the split-BF16 T3 image
+ * (enable = 0).  Both give bit-identical results.  No counterpart in the
+ * reference (a kernel check used by the tests). */
+int udmrg_matvec_plan_set_fused(udmrg_matvec_plan *p, int enable);
 
 /* ---- measurement ---------------------------------------------------- */
 /* FP64 FMA throughput of the device (TFLOP/s), measured by a DFMA-bound

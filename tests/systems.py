@@ -121,3 +121,17 @@ def free_fermion_green(time, L, x1, x2):
             res += (np.exp(-1j * eps * time) * np.sin(k * np.pi / (L + 1) * (x1 + 1)) *
                     np.sin(k * np.pi / (L + 1) * (x2 + 1)))
     return res * 2.0 / (L + 1)
+
+
+def config_problem(name):
+    """The two-site problem at the centre bond of a benchmark workload
+    (``ultradmrg_gb300.workloads``: seeded MPS with the configuration's
+    sizes), environments built by the oracle's environment updates without
+    normalisation (their physical scale), as host tensors:
+    ([L, W1, W2, R], psi, left divergence of the bond, workload)."""
+    from ultradmrg_gb300.workloads import WORKLOADS, build_host
+    w = WORKLOADS[name]
+    mpo, mps = build_host(w)
+    l = w.centre
+    eff, psi = two_site_problem(mpo, mps, l, normalize=False)
+    return eff, psi, tuple(mps[l].div()), w

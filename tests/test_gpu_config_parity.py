@@ -1,0 +1,146 @@
+"""GPU against the FP64 oracle at the sizes of the benchmark configurations.
+
+No reference test pins runs of these sizes, so parity here is the device path
+against the oracle on the same seeded inputs (the workloads of
+``ultradmrg_gb300.workloads``: Heisenberg L=32 D=256, Hubbard 4x8 D=1000,
+Hubbard 4x16 D=2000, centre bond, environments from the oracle):
+
+* the two-site matvec, FP64 form to 1e-11 of the largest element, mixed form
+  (split-BF16 tensor cores, FP32 accumulation) to 2e-5 of it, every oracle
+  block present (extra blocks zero) and the oracle's schedule of block pairs
+  inside the device's;
+* one local update: Lanczos energies (FP64 and mixed) within 1e-9 relative of
+  the oracle's Lanczos from the same start vector; the truncated SVD of the
+  device state identical to the oracle's SVD of that state (kept-state set,
+  block lists, bond dimension) with the truncation error within 1e-10;
+* the Heisenberg configuration end to end: six sweeps from the seed-0 product
+  state at D=256, per-site bond dimension, truncation error and energy
+  against the oracle's sweeps.
+
+The oracle's Lanczos runs on a spawned process pool (``SpawnedMatvec``): this
+process already holds a CUDA context, so it must not fork.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import blocksparse as bs
+from oracle import krylov, vmps as ovmps
+from systems import config_problem, max_block_diff
+from ultradmrg_gb300 import api, models as M
+
+pytestmark = pytest.mark.gpu
+
+CONFIGS = ["heisenberg32_D256", "hubbard4x8_D1000", "hubbard4x16_D2000"]
+_CACHE = {}
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from ultradmrg_gb300 import build
+    build.build()
+    c = api.Context(0)
+    yield c
+    c.close()
+
+
+def problem(name):
+    if name not in _CACHE:
+        eff, psi, ldiv, w = config_problem(name)
+        bs.FLOPS[0] = 0.0
+        ref = krylov.eff_ham_mul_two_site_state(eff, psi)
+        _CACHE[name] = (eff, psi, ldiv, w, ref, bs.FLOPS[0])
+    return _CACHE[name]
+
+
+def up(ctx, t):
+    return api.DeviceTensor.from_data(ctx, t)
+
+
+@pytest.mark.parametrize("name", CONFIGS)
+def test_matvec_at_config(ctx, name):
+    eff, psi, _, _, ref, oflops = problem(name)
+    dev = [up(ctx, t) for t in eff]
+    dpsi = up(ctx, psi)
+    for prec, tol in ((api.PREC_FP64, 1e-11), (api.PREC_MIXED, 2e-5)):
+        plan = api.MatvecPlan(ctx, dev, dpsi, precision=prec)
+        # the sector schedule: the oracle counts 2 m n k over its block pairs;
+        # the device's also holds the pairs of the zero blocks the Krylov
+        # structure adds to psi (closure under the matvec)
+        assert oflops <= plan.info()["flops"] <= (1 + 1e-3) * oflops
+        x, y = plan.embed(dpsi), plan.embed(dpsi)
+        plan.apply(x, y)
+        out = y.to_data()
+        assert set(ref.blocks) <= set(out.blocks)
+        extra = set(out.blocks) - set(ref.blocks)
+        assert all(not np.any(out.blocks[k]) for k in extra)
+        d, s = max_block_diff(out, ref)
+        assert d <= tol * s, (prec, d, s)
+
+
+def _workers():
+    return max(1, min(16, os.cpu_count() or 1))
+
+
+@pytest.mark.parametrize("name", ["hubbard4x8_D1000", "hubbard4x16_D2000"])
+def test_local_update_at_config(ctx, name, tmp_path):
+    from oracle.parallel import SpawnedMatvec
+    eff, psi, ldiv, w, _, _ = problem(name)
+    params = krylov.LanczosParams(1e-10, 200)
+    sm = SpawnedMatvec(eff, _workers(), str(tmp_path))
+    try:
+        oref = krylov.lanczos_solver(eff, psi.copy(), sm, params)
+    finally:
+        sm.close()
+    E = oref.gs_eng
+    dev = [up(ctx, t) for t in eff]
+    dpsi = up(ctx, psi)
+    r64 = api.lanczos_solver(ctx, dev, dpsi, 1e-10, 200)
+    rmx = api.lanczos_solver(ctx, dev, dpsi, 1e-10, 200, precision=api.PREC_MIXED)
+    assert abs(r64.gs_eng - E) <= 1e-9 * abs(E), (r64.gs_eng, E)
+    assert abs(rmx.gs_eng - E) <= 1e-9 * abs(E), (rmx.gs_eng, E)
+    # the truncated SVD of the device's state against the oracle's SVD of it
+    D = w.D
+    g64 = r64.gs_vec.to_data()
+    bs.normalize(g64)
+    u, s, vt, err, Dk = bs.svd(g64, 2, ldiv, 1e-8, D, D)
+    gu, gs_, gvt, gerr, gD = api.svd(ctx, up(ctx, g64), 2, ldiv, 1e-8, D, D)
+    assert gD == Dk
+    assert abs(gerr - err) <= 1e-10
+    gu, gs_, gvt = gu.to_data(), gs_.to_data(), gvt.to_data()
+    assert gu.indexes == u.indexes and gvt.indexes == vt.indexes
+    assert set(gu.blocks) == set(u.blocks) and set(gvt.blocks) == set(vt.blocks)
+    sv_ref = np.concatenate([np.diag(b) for _, b in sorted(s.blocks.items())])
+    sv_gpu = np.concatenate([np.diag(b) for _, b in sorted(gs_.blocks.items())])
+    assert np.allclose(sv_gpu ** 2, sv_ref ** 2, rtol=1e-9, atol=1e-13)
+    # the mixed form's state truncates like the FP64 one
+    gmx = rmx.gs_vec.to_data()
+    bs.normalize(gmx)
+    _, _, _, merr, mD = api.svd(ctx, up(ctx, gmx), 2, ldiv, 1e-8, D, D)
+    assert mD == gD
+    assert abs(merr - gerr) <= 1e-10
+
+
+def test_heisenberg32_D256_six_sweeps(ctx):
+    """Config 1: S=1/2 Heisenberg chain L=32, D=256, truncation 1e-8, Lanczos
+    (1e-9, 100), six sweeps from the seed-0 product state (Sz=0), FP64 and
+    mixed forms against the oracle's sweeps."""
+    N, D = 32, 256
+    mpo, pb = M.heisenberg_chain_mpo(N, builder="reference")
+    labels = M.random_sz0_labels(N, 0)
+    olog = []
+    oe = ovmps.two_site_finite_vmps(
+        M.direct_product_mps([pb] * N, labels), mpo,
+        ovmps.FiniteVMPSSweepParams(6, D, D, 1e-8, krylov.LanczosParams(1e-9, 100)), olog)
+    dmpo = [up(ctx, t) for t in mpo]
+    for prec in (api.PREC_FP64, api.PREC_MIXED):
+        dmps = [up(ctx, t) for t in M.direct_product_mps([pb] * N, labels)]
+        e0, log = api.two_site_finite_vmps(
+            ctx, dmps, dmpo, api.FiniteVMPSSweepParams(6, D, D, 1e-8, 1e-9, 100, precision=prec))
+        assert abs(e0 - oe) <= 1e-9 * abs(oe), (prec, e0, oe)
+        assert len(log) == len(olog)
+        for a, b in zip(log, olog):
+            assert a["D"] == b.D
+            assert abs(a["trunc_err"] - b.trunc_err) <= 1e-10
+            assert abs(a["e0"] - b.e0) <= 1e-9 * abs(b.e0)

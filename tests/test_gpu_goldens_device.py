@@ -8,10 +8,12 @@
   (``tests/test_algorithm/test_finite_dmrg.cc:346-444``): one sector of
   dimension 2 per site and an MPO with imaginary entries.
 
-Each runs with the reference's sweep parameters and initial product states.
-The host side (the Hamiltonians by exact diagonalisation, the oracle sweeps)
-is pinned in ``test_oracle_golden.py``.  The file name sorts last so that a
-run stopping at the first failure has run every other test before this one.
+Each runs with the reference's sweep parameters and initial product states,
+and with both MPO builders: the prefix-sharing one and the restated
+reference generator (``mpogen``: the reference's bond dimensions, sector and
+channel order).  The host side (the Hamiltonians by exact diagonalisation,
+the oracle sweeps) is pinned in ``test_oracle_golden.py`` and
+``test_mpogen.py``.
 """
 import json
 import os
@@ -26,10 +28,13 @@ pytestmark = pytest.mark.gpu
 
 GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_goldens.json")))
 
+BUILDERS = ["prefix", "reference"]
+
 FERMION = {
-    "free_fermion8": lambda dt: M.free_fermion_chain_mpo(8, dtype=dt)[:2],
-    "tj1d": lambda dt: M.tj_mpo(4, dtype=dt),
-    "tj2d": lambda dt: M.tj_mpo(4, pairs=[(0, 1), (0, 2), (2, 3), (1, 3)], dtype=dt),
+    "free_fermion8": lambda dt, b: M.free_fermion_chain_mpo(8, dtype=dt, builder=b)[:2],
+    "tj1d": lambda dt, b: M.tj_mpo(4, dtype=dt, builder=b),
+    "tj2d": lambda dt, b: M.tj_mpo(4, pairs=[(0, 1), (0, 2), (2, 3), (1, 3)], dtype=dt,
+                                   builder=b),
 }
 
 
@@ -49,11 +54,12 @@ def _params(text):
     return api.FiniteVMPSSweepParams(int(sweeps), int(dmin), int(dmax), trunc, err, it)
 
 
+@pytest.mark.parametrize("builder", BUILDERS)
 @pytest.mark.parametrize("dtype", [np.float64, np.complex128])
 @pytest.mark.parametrize("case", sorted(FERMION))
-def test_fermion_vmps_goldens_device(ctx, case, dtype):
+def test_fermion_vmps_goldens_device(ctx, case, dtype, builder):
     g = GOLD["fermion_vmps"][case]
-    mpo, pb = FERMION[case](dtype)
+    mpo, pb = FERMION[case](dtype, builder)
     mps = [api.DeviceTensor.from_data(ctx, t)
            for t in M.direct_product_mps([pb] * len(g["labels"]), g["labels"], dtype=dtype)]
     e0, _ = api.two_site_finite_vmps(ctx, mps, [api.DeviceTensor.from_data(ctx, w) for w in mpo],
@@ -72,10 +78,11 @@ def test_kitaev_gamma_finite_dmrg_device(ctx):
     assert abs(e0 - g["energy"]) < g["tol"]
 
 
-def test_kondo_double_chain_device(ctx):
+@pytest.mark.parametrize("builder", BUILDERS)
+def test_kondo_double_chain_device(ctx, builder):
     """Alternating four-state and two-state sites through the device sweep."""
     g = GOLD["vmps"]["KondoDoubleChain"]
-    mpo, sites = M.kondo_chain_mpo()
+    mpo, sites = M.kondo_chain_mpo(builder=builder)
     mps = [api.DeviceTensor.from_data(ctx, t)
            for t in M.direct_product_mps(sites, [i % 2 for i in range(len(sites))])]
     e0, _ = api.two_site_finite_vmps(ctx, mps, [api.DeviceTensor.from_data(ctx, w) for w in mpo],
@@ -83,11 +90,12 @@ def test_kondo_double_chain_device(ctx):
     assert abs(e0 - g["energy"]) < g["tol"]
 
 
-def test_rashba_tj_device(ctx):
+@pytest.mark.parametrize("builder", BUILDERS)
+def test_rashba_tj_device(ctx, builder):
     """Complex spin-orbit hopping (an MPO with imaginary entries) through the
     device sweep."""
     g = GOLD["vmps"]["RashbaTJ"]
-    mpo, pb = M.rashba_tj_mpo()
+    mpo, pb = M.rashba_tj_mpo(builder=builder)
     mps = [api.DeviceTensor.from_data(ctx, t)
            for t in M.direct_product_mps([pb] * len(g["labels"]), g["labels"],
                                          dtype=np.complex128)]
@@ -97,19 +105,21 @@ def test_rashba_tj_device(ctx):
 
 
 DMRG = {
-    "tj1d": lambda dt: M.tj_mpo(4, dtype=dt),
-    "tj2d": lambda dt: M.tj_mpo(4, pairs=[(0, 1), (0, 2), (2, 3), (1, 3)], dtype=dt),
-    "Hubbard2x2": lambda dt: M.hubbard_2x2_test_mpo(dtype=dt),
+    "tj1d": lambda dt, b: M.tj_mpo(4, dtype=dt, builder=b),
+    "tj2d": lambda dt, b: M.tj_mpo(4, pairs=[(0, 1), (0, 2), (2, 3), (1, 3)], dtype=dt,
+                                   builder=b),
+    "Hubbard2x2": lambda dt, b: M.hubbard_2x2_test_mpo(dtype=dt, builder=b),
 }
 
 
+@pytest.mark.parametrize("builder", BUILDERS)
 @pytest.mark.parametrize("dtype", [np.float64, np.complex128])
 @pytest.mark.parametrize("case", sorted(DMRG))
-def test_finite_dmrg_goldens_device(ctx, case, dtype):
+def test_finite_dmrg_goldens_device(ctx, case, dtype, builder):
     """test_finite_dmrg.cc:484-835 through udmrg_finite_dmrg (MatReprMPO in);
     the Hubbard case starts from labels 1, 2, 1, 2 (the test's loop)."""
     g = GOLD["dmrg"][case]
-    mpo, pb = DMRG[case](dtype)
+    mpo, pb = DMRG[case](dtype, builder)
     labels = g["labels"] or [1 if i % 2 == 0 else 2 for i in range(len(mpo))]
     mps = [api.DeviceTensor.from_data(ctx, t)
            for t in M.direct_product_mps([pb] * len(labels), labels, dtype=dtype)]

@@ -139,3 +139,43 @@ def test_mixed_matvec_workload(ctx, workload):
     a, b = ym.download_packed(), yd.download_packed()
     assert np.max(np.abs(a - b)) <= 2e-5 * np.max(np.abs(b))
     assert np.linalg.norm(a - b) <= 2e-5 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("name,l,cplx", [("heis", 4, False), ("hub", 2, False),
+                                         ("hub_big", 3, False), ("heis", 4, True)])
+def test_fused_mpo_gemm_bit_identical(ctx, name, l, cplx):
+    """The MPO step fused into the .R GEMM's producers against the separate MPO
+    kernel + image GEMM: the same FP32 sums in the same order, the same BF16
+    split, the same MMAs, so the results agree bit for bit."""
+    mpo, mps = SYSTEMS[name]()
+    eff, psi = two_site_problem(mpo, mps, l)
+    dt = np.complex128 if cplx else None
+    dev = [api.DeviceTensor.from_data(ctx, t, dt) for t in eff]
+    dpsi = api.DeviceTensor.from_data(ctx, psi, dt)
+    plan = api.MatvecPlan(ctx, dev, dpsi, precision=MIXED)
+    x, yf, yu = plan.embed(dpsi), plan.embed(dpsi), plan.embed(dpsi)
+    plan.apply(x, yf)
+    plan.set_fused(False)
+    plan.apply(x, yu)
+    a, b = yf.download_packed(), yu.download_packed()
+    assert np.array_equal(a, b)
+    if not cplx:
+        ref = krylov.eff_ham_mul_two_site_state(eff, psi)
+        d, s = max_block_diff(yf.to_data(), ref)
+        assert d <= 2e-5 * s, (d, s)
+
+
+def test_fused_mpo_gemm_workload(ctx):
+    """The same on the benchmark's synthetic Hubbard 4x8 D=256 workload."""
+    from ultradmrg_gb300.workloads import WORKLOADS, build_host
+    w = WORKLOADS["hubbard4x8_D256"]
+    mpo, mps = build_host(w)
+    l = w.centre
+    L, R = api.build_envs(ctx, mpo, mps, l, normalize=False)
+    psi = api.contract(ctx, up(ctx, mps[l]), up(ctx, mps[l + 1]), [2], [0])
+    pm = api.MatvecPlan(ctx, [L, up(ctx, mpo[l]), up(ctx, mpo[l + 1]), R], psi, precision=MIXED)
+    x, yf, yu = pm.embed(psi), pm.embed(psi), pm.embed(psi)
+    pm.apply(x, yf)
+    pm.set_fused(False)
+    pm.apply(x, yu)
+    assert np.array_equal(yf.download_packed(), yu.download_packed())

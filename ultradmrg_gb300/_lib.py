@@ -137,6 +137,7 @@ SIGNATURES = {
     "udmrg_matvec_plan_stage_times": [C.c_void_p, c_double_p, c_double_p, c_double_p,
                                       c_double_p],
     "udmrg_matvec_plan_stage_bytes": [C.c_void_p, c_double_p],
+    "udmrg_matvec_plan_set_fused": [C.c_void_p, C.c_int],
     "udmrg_probe_fp64_tflops": [C.c_void_p, c_double_p],
     "udmrg_ctx_event_record": [C.c_void_p, C.c_int],
     "udmrg_ctx_event_elapsed": [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)],

@@ -617,6 +617,11 @@ class MatvecPlan:
              C.cast(C.c_void_p(d_out), _lib.c_double_p), ms, fl)
         return list(ms), list(fl)
 
+    def set_fused(self, enable: bool):
+        """Mixed form: MPO step inside the .R GEMM's producers (default) or as
+        its own kernel (bit-identical results)."""
+        call("udmrg_matvec_plan_set_fused", self.h, 1 if enable else 0)
+
     def stage_bytes(self):
         """Algorithmic HBM bytes of the mixed form's memory-bound stages."""
         b = (C.c_double * 4)()

@@ -898,10 +898,28 @@ int udmrg_matvec_plan_stage_bytes(udmrg_matvec_plan *p, double *bytes) {
     MatvecPlan &m = *p->plan;
     for (int i = 0; i < 4; ++i) bytes[i] = 0.0;
     if (m.sg) {
-      // 8 B read, 3 x 2 B written per real number
-      bytes[0] = 14.0 * (double)m.sg->psi_size * (m.sg->cplx ? 2 : 1);
-      bytes[2] = m.sg->mpo_bytes;
+      const SgMatvecPlan &g = *m.sg;
+      const double es = g.cplx ? 2.0 : 1.0;
+      const double nreal = (double)g.psi_size * es;
+      // psi pack: 8 B read, 3 x 2 B written per real number
+      bytes[0] = 14.0 * nreal;
+      // L.psi: both images read, 4 B per (unpadded) T1 entry written
+      bytes[1] = (double)g.l_bytes + (double)g.psi_bytes + 4.0 * (double)m.p1->out->size() * es;
+      if (g.fused) {  // T1 read once, R image read, FP64 result written
+        bytes[3] = g.t1_read_bytes + (double)g.r_bytes + 8.0 * nreal;
+      } else {
+        bytes[2] = g.mpo_bytes;
+        bytes[3] = (double)g.t3_bytes + (double)g.r_bytes + 8.0 * nreal;
+      }
     }
+  });
+}
+
+int udmrg_matvec_plan_set_fused(udmrg_matvec_plan *p, int enable) {
+  return guarded([&] {
+    MatvecPlan &m = *p->plan;
+    UDMRG_REQUIRE(m.sg != nullptr, "set_fused: not a mixed-precision plan");
+    m.sg->fused = enable != 0;
   });
 }
 

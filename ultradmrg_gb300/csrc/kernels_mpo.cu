@@ -14,6 +14,7 @@
 
 #include "mpo_step.hpp"
 #include "sg_matvec.hpp"
+#include "tc_roles.cuh"
 
 namespace udmrg {
 
@@ -21,33 +22,6 @@ namespace {
 
 __device__ __forceinline__ int canon(int r, int k, int tr) {
   return (((k >> 3) * (tr >> 3) + (r >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1);
-}
-
-__device__ __forceinline__ uint32_t pack_bf16x2(__nv_bfloat16 a, __nv_bfloat16 b) {
-  return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
-}
-
-// x = hi + mid + lo, each the BF16 rounding of the remainder (exact
-// differences in FP32), eight values into three 16-byte plane segments.
-__device__ __forceinline__ void split8(const float (&x)[8], uint4 &h, uint4 &m, uint4 &l) {
-  uint32_t ph[4], pm[4], pl[4];
-#pragma unroll
-  for (int j = 0; j < 8; j += 2) {
-    __nv_bfloat16 hv[2], mv[2], lv[2];
-#pragma unroll
-    for (int t = 0; t < 2; ++t) {
-      hv[t] = __float2bfloat16_rn(x[j + t]);
-      const float r1 = x[j + t] - __bfloat162float(hv[t]);
-      mv[t] = __float2bfloat16_rn(r1);
-      lv[t] = __float2bfloat16_rn(r1 - __bfloat162float(mv[t]));
-    }
-    ph[j >> 1] = pack_bf16x2(hv[0], hv[1]);
-    pm[j >> 1] = pack_bf16x2(mv[0], mv[1]);
-    pl[j >> 1] = pack_bf16x2(lv[0], lv[1]);
-  }
-  h = make_uint4(ph[0], ph[1], ph[2], ph[3]);
-  m = make_uint4(pm[0], pm[1], pm[2], pm[3]);
-  l = make_uint4(pl[0], pl[1], pl[2], pl[3]);
 }
 
 constexpr int kMpoWarps = 8;

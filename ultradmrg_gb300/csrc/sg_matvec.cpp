@@ -10,7 +10,8 @@ SgMatvecPlan::~SgMatvecPlan() {
   if (!ctx) return;
   for (void *p : {(void *)l_img, (void *)psi_img, (void *)t3_img, (void *)r_img, (void *)t1,
                   (void *)d_pairs, (void *)d_outs, (void *)d_rowptr, (void *)d_nz,
-                  (void *)d_tasks})
+                  (void *)d_tasks, (void *)d_gmap, (void *)d_rowinfo, (void *)d_kchunks,
+                  (void *)d_tgtref})
     ctx->free(p);
 }
 
@@ -167,6 +168,11 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   std::vector<PackOp> rops;
   int64_t t3bytes = 0, rbytes = 0;
   std::vector<std::pair<int32_t, int32_t>> tgt_key;  // (A', B) of every target
+  // fused form: the group (its MpoGroupMap), row block and K block of every target
+  struct TgtLoc {
+    int32_t g, i, j;
+  };
+  std::vector<TgtLoc> tgt_loc;
   for (int Bp = 0; Bp < nB; ++Bp) {
     if (orows[Bp].empty()) continue;
     const int64_t dBp = R.idx[0].dims[Bp];
@@ -203,6 +209,34 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
           add_pack(rops, off, nc, 1, r_off, dBp, db, dBp, K + k0, kc, kTcBN, 0, false);
         }
       }
+    }
+    // fused form: per-row (row block, a', s1's2') and per-K-chunk (K block,
+    // w2, b offset, half) tables of the group, in image order
+    {
+      MpoGroupMap gm{};
+      gm.row0 = (int64_t)p->rowinfo.size();
+      gm.kch0 = (int64_t)p->kchunks.size();
+      gm.tgt0 = (int64_t)p->tgtref.size();
+      gm.nrb = (int32_t)orows[Bp].size();
+      gm.nkb = (int32_t)rks[Bp].size();
+      for (size_t i = 0; i < orows[Bp].size(); ++i) {
+        const int64_t b = orows[Bp][i];
+        const int32_t da = (int32_t)dim(S, b, 0);
+        const int32_t ds12p = (int32_t)(dim(S, b, 1) * dim(S, b, 2));
+        for (int32_t a = 0; a < da; ++a)
+          for (int32_t q = 0; q < ds12p; ++q) p->rowinfo.push_back({(int32_t)i, a, q, 0});
+      }
+      for (int32_t half = 0; half < (cplx ? 2 : 1); ++half)
+        for (size_t j = 0; j < rks[Bp].size(); ++j) {
+          const int64_t b = rks[Bp][j];
+          const int32_t dw2 = (int32_t)dim(R, b, 1), dbp = (int32_t)up8(dim(R, b, 2));
+          for (int32_t w2 = 0; w2 < dw2; ++w2)
+            for (int32_t c8 = 0; c8 < dbp; c8 += 8) p->kchunks.push_back({(int32_t)j, w2, c8, half});
+        }
+      gm.nkch = (int32_t)(p->kchunks.size() - gm.kch0);
+      UDMRG_REQUIRE((int64_t)gm.nkch * 8 == Ke, "mixed matvec: K chunk table");
+      p->tgtref.resize(p->tgtref.size() + (size_t)(cplx ? 2 : 1) * gm.nrb * gm.nkb, {-1, 0});
+      p->gmap.push_back(gm);
     }
     // MPO-step targets of this group
     for (size_t i = 0; i < orows[Bp].size(); ++i) {
@@ -247,6 +281,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
         if (tg.nsrc > 0) {
           p->targets.push_back(tg);
           tgt_key.push_back({Ap, Bs});
+          tgt_loc.push_back({(int32_t)p->gmap.size() - 1, (int32_t)i, (int32_t)j});
         }
       }
     }
@@ -297,6 +332,8 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       std::vector<PairNz> nzs;  // sorted by output channel
     };
     std::vector<Built> built;
+    // fused form: the (real) pair of every target and its first output channel there
+    std::vector<int32_t> tgt_pair(p->targets.size(), -1), tgt_out(p->targets.size(), 0);
     for (auto &kv : by_pair) {
       Built bd{};
       MpoPair &pr = bd.pr;
@@ -328,6 +365,8 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       for (int t : kv.second) {
         const MpoTarget &tg = p->targets[t];
         out_first.push_back((int32_t)(p->outs.size() - pr.out0));
+        tgt_pair[t] = (int32_t)built.size();
+        tgt_out[t] = out_first.back();
         for (int oc = 0; oc < tg.nout; ++oc) {
           p->outs.push_back({tg.img_off, tg.row0 + oc / tg.dw2, tg.ds12p,
                              tg.k0 + (oc % tg.dw2) * tg.dbp, tg.kc});
@@ -389,11 +428,25 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
         UDMRG_REQUIRE(p->outs[pr.out0 + o].col0 % 8 == 0,
                       "mixed matvec: MPO-step output not 16-byte aligned");
       p->mpo_bytes += (double)pr.da * pr.db * (4.0 * pr.nin + 6.0 * pr.nout);
+      p->t1_read_bytes += (double)pr.da * pr.db * 4.0 * pr.nin;
       p->pairs.push_back(pr);
     };
     for (const Built &bd : built) emit(bd, false);
     if (cplx)
       for (const Built &bd : built) emit(bd, true);
+    // fused form: the CSR row of output channel 0 of every target (its
+    // imaginary twin's for the imaginary half)
+    const int32_t nreal = (int32_t)built.size();
+    for (size_t t = 0; t < p->targets.size(); ++t) {
+      const TgtLoc &lc = tgt_loc[t];
+      const MpoGroupMap &gm = p->gmap[lc.g];
+      const int32_t q = tgt_pair[t];
+      p->tgtref[gm.tgt0 + (int64_t)lc.i * gm.nkb + lc.j] = {p->pairs[q].row0 + tgt_out[t],
+                                                             p->targets[t].dw2};
+      if (cplx)
+        p->tgtref[gm.tgt0 + ((int64_t)gm.nrb + lc.i) * gm.nkb + lc.j] = {
+            p->pairs[nreal + q].row0 + tgt_out[t], p->targets[t].dw2};
+    }
     // warp tasks: 32 units (a', 8-wide chunk of b) each, the pairs with the
     // most work per unit (nonzeros and output channels) first
     std::vector<int> order(p->pairs.size());
@@ -415,6 +468,10 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   p->d_rowptr = upload_vec(ctx, p->rowptr);
   p->d_nz = upload_vec(ctx, p->nz);
   p->d_tasks = upload_vec(ctx, p->tasks);
+  p->d_gmap = upload_vec(ctx, p->gmap);
+  p->d_rowinfo = upload_vec(ctx, p->rowinfo);
+  p->d_kchunks = upload_vec(ctx, p->kchunks);
+  p->d_tgtref = upload_vec(ctx, p->tgtref);
   p->mixed_flops = 6.0 * (p->g1.flops + p->g3.flops);
   ctx.sync();
   return p;
@@ -423,8 +480,12 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
 void SgMatvecPlan::apply(const double *psi_in, double *out) {
   run_pack(*ctx, psi_pack, psi_in, true, psi_img);
   run_tc_gemm(*ctx, g1, l_img, psi_img, t1, kTcOutF32, 1.0);
-  run_mpo_step(*ctx, *this);
-  run_tc_gemm(*ctx, g3, t3_img, r_img, out, cplx ? kTcOutC128 : kTcOutF64, 1.0);
+  if (fused) {
+    run_tc_mpo_gemm(*ctx, *this, out);
+  } else {
+    run_mpo_step(*ctx, *this);
+    run_tc_gemm(*ctx, g3, t3_img, r_img, out, cplx ? kTcOutC128 : kTcOutF64, 1.0);
+  }
 }
 
 void SgMatvecPlan::apply_timed(const double *psi_in, double *out, float ms[4]) {
@@ -435,9 +496,14 @@ void SgMatvecPlan::apply_timed(const double *psi_in, double *out, float ms[4]) {
   cudaEventRecord(ev[1], ctx->stream);
   run_tc_gemm(*ctx, g1, l_img, psi_img, t1, kTcOutF32, 1.0);
   cudaEventRecord(ev[2], ctx->stream);
-  run_mpo_step(*ctx, *this);
-  cudaEventRecord(ev[3], ctx->stream);
-  run_tc_gemm(*ctx, g3, t3_img, r_img, out, cplx ? kTcOutC128 : kTcOutF64, 1.0);
+  if (fused) {  // one kernel: its time is stage 3, stage 2 is empty
+    cudaEventRecord(ev[3], ctx->stream);
+    run_tc_mpo_gemm(*ctx, *this, out);
+  } else {
+    run_mpo_step(*ctx, *this);
+    cudaEventRecord(ev[3], ctx->stream);
+    run_tc_gemm(*ctx, g3, t3_img, r_img, out, cplx ? kTcOutC128 : kTcOutF64, 1.0);
+  }
   cudaEventRecord(ev[4], ctx->stream);
   UDMRG_CHECK_CUDA(cudaEventSynchronize(ev[4]));
   for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);

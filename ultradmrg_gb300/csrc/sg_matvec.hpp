@@ -88,6 +88,28 @@ struct MpoOut {
   int32_t row0, rstride, col0, kc;  // image row = row0 + a' * rstride, column = col0 + b
 };
 
+// Fused form of the MPO step and the .R GEMM (tc_mpo_gemm.cu): the GEMM's
+// producer warps compute each 128-row x 64-K tile of T3 from T1 into shared
+// memory (the CSR walk of the unfused MPO step), so the T3 image is neither
+// written nor read.  Per step-3 group: where its tables start and their sizes.
+struct MpoGroupMap {
+  int64_t row0;   // first MpoRowInfo of the group (one per GEMM row)
+  int64_t kch0;   // first MpoKChunk (one per 8-wide K chunk)
+  int64_t tgt0;   // first MpoTgtRef ((half, row block, K block) table)
+  int32_t nrb, nkb;  // row blocks (psi blocks (A', S1', S2')) and K blocks (R blocks (W2, B))
+  int32_t nkch, pad;  // K chunks (the real and, for complex data, imaginary halves)
+};
+struct MpoRowInfo {
+  int32_t rb, a, s12p, pad;  // row block, a', (s1', s2') index
+};
+struct MpoKChunk {
+  int32_t kb, w2, c8, half;  // K block, w2, first b of the chunk, imaginary half
+};
+struct MpoTgtRef {
+  int32_t csr0;  // CSR row of output channel (s1's2' = 0, w2 = 0); -1: no coupling
+  int32_t dw2;
+};
+
 struct SgMatvecPlan {
   Ctx *ctx = nullptr;
   int64_t psi_size = 0;
@@ -118,8 +140,20 @@ struct SgMatvecPlan {
   MpoNzRec *d_nz = nullptr;
   MpoTask *d_tasks = nullptr;
   int max_nin = 0, max_nout = 0;
+  // fused MPO step + .R GEMM (the default; the unfused pair of kernels stays
+  // for checks: both give bit-identical results)
+  bool fused = true;
+  std::vector<MpoGroupMap> gmap;
+  std::vector<MpoRowInfo> rowinfo;
+  std::vector<MpoKChunk> kchunks;
+  std::vector<MpoTgtRef> tgtref;
+  MpoGroupMap *d_gmap = nullptr;
+  MpoRowInfo *d_rowinfo = nullptr;
+  MpoKChunk *d_kchunks = nullptr;
+  MpoTgtRef *d_tgtref = nullptr;
   double mixed_flops = 0;  // tensor-core work actually issued (2MNK per group, x6 products)
   double mpo_bytes = 0;    // MPO step: 4 B per T1 entry read, 3 x 2 B per T3 entry written
+  double t1_read_bytes = 0;  // 4 B per T1 entry the MPO step reads
   ~SgMatvecPlan();
   void apply(const double *psi_in, double *out);
   // apply with CUDA events between the stages: ms[0] psi pack, ms[1] GEMM
@@ -134,5 +168,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
                                              const BTensor &S, FusedMpo &fm);
 
 void run_mpo_step(Ctx &ctx, const SgMatvecPlan &p);
+// T3 computed in the producers of the .R GEMM: res = (W1 W2 T1) R^T
+void run_tc_mpo_gemm(Ctx &ctx, const SgMatvecPlan &p, double *out);
 
 }  // namespace udmrg

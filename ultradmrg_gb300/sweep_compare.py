@@ -33,6 +33,7 @@ import numpy as np
 
 from . import api
 from . import models as M
+from .clocks import ClockSampler
 from . import rank_training as RT
 
 
@@ -47,7 +48,7 @@ def prepare(ctx, Lx=16, Ly=4, schedule="10:2,100:2,500:2,1000:2,2000:1", lanczos
     recording each bond's spectrum).  Returns (host MPO, device MPO, host
     state, rank model, per-stage log, seconds)."""
     N = Lx * Ly
-    mpo, pb = M.hubbard_cylinder_mpo(Lx, Ly, t=1.0, U=8.0)
+    mpo, pb = M.hubbard_cylinder_mpo(Lx, Ly, t=1.0, U=8.0, builder="reference")
     labels = M.hubbard_cylinder_holes(N, 8)
     dmpo = _upload(ctx, mpo)
     dmps = _upload(ctx, M.direct_product_mps([pb] * N, labels))
@@ -107,15 +108,16 @@ def main(argv=None):
             hist.copy_history_from(model)
         mps = _upload(ctx, state)
         ctx.sync()
-        t1 = time.perf_counter()
-        if mode == 2:
-            e0, log, _, _ = api.two_site_finite_vmps_learned(ctx, mps, dmpo, p, hist, False)
-        else:
-            e0, log = api.two_site_finite_vmps(ctx, mps, dmpo, p)
-        ctx.sync()
-        sec = time.perf_counter() - t1
+        with ClockSampler(0) as clk:
+            t1 = time.perf_counter()
+            if mode == 2:
+                e0, log, _, _ = api.two_site_finite_vmps_learned(ctx, mps, dmpo, p, hist, False)
+            else:
+                e0, log = api.two_site_finite_vmps(ctx, mps, dmpo, p)
+            ctx.sync()
+            sec = time.perf_counter() - t1
         per = 2 * (N - 2)  # updates per sweep
-        f = dict(sweep_seconds=sec / a.sweeps, e0=e0,
+        f = dict(sweep_seconds=sec / a.sweeps, e0=e0, clocks=clk.summary(),
                  sweep_energies=[log[(k + 1) * per - 1]["e0"] for k in range(a.sweeps)],
                  lanczos_seconds=sum(r["lancz_sec"] for r in log),
                  svd_seconds=sum(r["svd_sec"] for r in log),

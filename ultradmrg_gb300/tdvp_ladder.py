@@ -5,7 +5,7 @@ quench: the mixed-precision Krylov matvec against the FP64 one.
 [--dt 0.05] [--krylov 20] [--every 10] [--forms fp64,mixed] [--out f.json]``
 
 * The lattice is a 2 x Lx ladder with J_leg = J_rung = 1 and U(1) Sz, with
-  sites x*2 + y.  The MPO comes from the prefix-sharing builder.
+  sites x*2 + y.  The MPO comes from the restated reference generator.
 * The ground state comes from device two-site VMPS (FP64).  It starts from
   a seeded random Sz = 0 product state (seed 2) and the bond dimension grows
   to D (``--gs-schedule``).
@@ -19,7 +19,8 @@ quench: the mixed-precision Krylov matvec against the FP64 one.
 * The evolution runs ``--steps`` TDVP steps of dt in each form, from the same
   quenched state: Krylov exp(-i dt H) with at most ``--krylov`` vectors,
   Dmax = D, truncation 1e-10.
-* The report gives the wall seconds of each form (total and per step).
+* The report gives the wall seconds of each form (total and per step) and
+  the nvidia-smi clocks sampled while it ran.
   Every ``--every`` steps it also gives the largest difference of the local
   <Sz_i> between the forms, and 1 - |<psi_fp64|psi_mixed>| / (|psi_fp64|
   |psi_mixed|) (device measurements, ``ultradmrg_gb300.measure``).
@@ -35,11 +36,13 @@ import time
 import numpy as np
 
 from . import api, measure as dm, models as M
+from .clocks import ClockSampler
 
 
 def ladder_problem(Lx: int, dtype=np.complex128):
     N = 2 * Lx
-    mpo, pb = M.heisenberg_chain_mpo(N, dtype=dtype, pairs=M.heisenberg_ladder_pairs(Lx, 2))
+    mpo, pb = M.heisenberg_chain_mpo(N, dtype=dtype, pairs=M.heisenberg_ladder_pairs(Lx, 2),
+                                     builder="reference")
     _, ops = M.spin_half_site(dtype)
     return N, mpo, pb, ops
 
@@ -101,16 +104,19 @@ def main(argv=None):
                       "quench_site": centre, "seed": 2, "gs_schedule": schedule},
            "ground_state": {"energy": e0, "seconds": gs_sec},
            "forms": {f: {"seconds": 0.0, "updates": 0} for f in forms}, "checkpoints": []}
+    clocks = {f: [] for f in forms}
     done = 0
     while done < a.steps:
         n = min(a.every, a.steps - done)
         for f in forms:
             p = api.TDVPEvolveParams(a.dt, n, 1, a.D, 1e-10, 1e-10, a.krylov, precision=prec[f])
             ctx.sync()
-            t1 = time.perf_counter()
-            log = api.two_site_finite_tdvp(ctx, states[f], dmpo, p)
-            ctx.sync()
-            out["forms"][f]["seconds"] += time.perf_counter() - t1
+            with ClockSampler(0) as clk:
+                t1 = time.perf_counter()
+                log = api.two_site_finite_tdvp(ctx, states[f], dmpo, p)
+                ctx.sync()
+                out["forms"][f]["seconds"] += time.perf_counter() - t1
+            clocks[f].append(clk.summary())
             out["forms"][f]["updates"] += len(log)
             out["forms"][f]["D_max"] = max(r["D"] for r in log)
         done += n
@@ -128,6 +134,12 @@ def main(argv=None):
         out["checkpoints"].append(cp)
     for f in forms:
         out["forms"][f]["seconds_per_step"] = out["forms"][f]["seconds"] / a.steps
+        cs = [c for c in clocks[f] if c["samples"]]
+        out["forms"][f]["clocks"] = {
+            "sm_mhz_min_of_medians": min((c["sm_mhz"] for c in cs), default=None),
+            "sm_max_mhz": max((c["sm_max_mhz"] for c in cs), default=None),
+            "reasons": sorted({r for c in cs for r in c["reasons"]}),
+            "samples": sum(c["samples"] for c in cs)}
     if "fp64" in forms and "mixed" in forms:
         out["speedup_mixed_vs_fp64"] = out["forms"]["fp64"]["seconds"] / out["forms"]["mixed"]["seconds"]
     line = json.dumps(out)

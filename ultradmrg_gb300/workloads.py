@@ -6,7 +6,9 @@ workload is: the model's MPO, a seeded random MPS in mixed-canonical form
 around the centre bond whose bond sectors follow a Gaussian Schmidt-weight
 model (``models.bond_sectors``, ``models.random_canonical_mps``), and the
 two-site problem at the centre bond (environments from the MPS by
-environment updates, at the physical scale of a DMRG run).
+environment updates, at the physical scale of a DMRG run).  The MPOs come
+from the restated reference generator (``mpogen``, ``builder="reference"``):
+the reference's bond dimensions, sector order and channel order.
 """
 from __future__ import annotations
 
@@ -27,6 +29,7 @@ class Workload:
     U: float = 8.0
     t: float = 1.0
     electrons: int = 0
+    builder: str = "reference"  # MPO generator (models._generator)
 
     @property
     def N(self):
@@ -54,10 +57,10 @@ WORKLOADS = {
 def build_host(w: Workload):
     """(mpo, mps) as host block tensors."""
     if w.model == "hubbard":
-        mpo, pb = M.hubbard_cylinder_mpo(w.Lx, w.Ly, t=w.t, U=w.U)
+        mpo, pb = M.hubbard_cylinder_mpo(w.Lx, w.Ly, t=w.t, U=w.U, builder=w.builder)
         div = (w.electrons, 0)
     else:
-        mpo, pb = M.heisenberg_chain_mpo(w.N)
+        mpo, pb = M.heisenberg_chain_mpo(w.N, builder=w.builder)
         div = (0,)
     mps = M.random_canonical_mps([pb] * w.N, div, w.D, w.centre, seed=w.seed, sigma=w.sigma)
     return mpo, mps
