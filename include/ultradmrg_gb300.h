@@ -300,6 +300,35 @@ int udmrg_two_site_finite_vmps_learned(udmrg_ctx *ctx, int64_t N, udmrg_tensor *
                                        double *e0, udmrg_site_log *log, int64_t log_cap,
                                        int64_t *log_len);
 
+/* Noise fields of FiniteVMPSSweepParams
+ * (include/qlmps/algorithm/finite_vmps_sweep_params.h:31-107): the starting
+ * noise of each sweep (n_noises values, the last one repeats) and the
+ * adaptation factors. */
+typedef struct {
+  const double *noises;
+  int64_t n_noises;
+  double noise_decrease, noise_increase, max_noise, alpha;
+} udmrg_noise_params;
+
+/* TwoSiteFiniteVMPSWithNoise
+ * (include/qlmps/algorithm/vmps/two_site_update_noise_finite_vmps_impl.h:81-556):
+ * edge tensors whose bond holds the whole block space become index
+ * combiners and the sweeps run between the first sites where Dmax binds
+ * (CheckAndUpdateBoundaryMPSTensors, vmps_init.h:135-246); before each update
+ * the noise adapts from the energy expectation of the current two-site
+ * state; after Lanczos the bond is expanded by noise * (L psi W1 W2) (moving
+ * right) or noise * (psi R W2 W1) (moving left) unless its quantum numbers
+ * are already covered; exact truncated SVD.  The MPS centre must be at site 0
+ * on entry; mps tensors are replaced.  noise_log (log_cap entries, may be
+ * NULL) receives the noise applied at each update, 0 where the bond was not
+ * expanded.  With n_noises = 0: the plain sweep.  Sector order of fused and
+ * expanded indexes: see INTEGRATION.md. */
+int udmrg_two_site_finite_vmps_noise(udmrg_ctx *ctx, int64_t N, udmrg_tensor **mps,
+                                     udmrg_tensor *const *mpo, const udmrg_sweep_params *params,
+                                     const udmrg_noise_params *noise, double *e0,
+                                     udmrg_site_log *log, int64_t log_cap, int64_t *log_len,
+                                     double *noise_log);
+
 /* ---- reusable matvec plan (repeated H_eff * psi on device buffers) -------- */
 /* The plan fixes {L, W_l, W_r, R} and the block structure closed under the
  * matvec that contains psi_struct's blocks (the Krylov structure). */

@@ -156,6 +156,26 @@ def main():
                                            re.S).group(1).split()),
         "J": par("J"), "K": par("K"), "Gm": par("Gm"), "h": par("h"),
         "Nx": int(size.group(1)), "Ny": int(size.group(2))}
+    # the noised two-site VMPS (sweep parameters with their noise fields:
+    # FiniteVMPSSweepParams(sweeps, Dmin, Dmax, trunc, LanczosParams(err),
+    # noises, max_noise, noise_increase, noise_decrease, alpha))
+    noise = read("tests/test_algorithm/test_two_site_noise_update_finite_vmps.cc")
+    goldens["noise_vmps"] = {}
+    for case in ("1DHeisenberg", "2DHeisenberg"):
+        body = fixture_case(noise, "TestNoisedTwoSiteAlgorithmSpinSystem", case)
+        e = [a.strip() for a in re.search(r"RunTest\w*Case\((.*?)\);", body, re.S)
+             .group(1).split(",")]
+        p = re.search(r"FiniteVMPSSweepParams\(\s*(\d+)\s*,\s*(\d+)\s*,\s*(\d+)\s*,\s*"
+                      r"([-0-9.eE]+)\s*,\s*LanczosParams\(\s*([-0-9.eE]+)\s*\)\s*,\s*"
+                      r"std::vector<double>\s*\{([^}]*)\}([^;]*)\);", body, re.S)
+        extra = [float(x) for x in re.findall(r"[-0-9.]+(?:[eE][-+]?[0-9]+)?", p.group(7))]
+        names = ["max_noise", "noise_increase", "noise_decrease", "alpha"]
+        goldens["noise_vmps"][case] = {
+            "energy": float(e[-2]), "tol": float(e[-1]), "sweeps": int(p.group(1)),
+            "Dmin": int(p.group(2)), "Dmax": int(p.group(3)), "trunc_err": float(p.group(4)),
+            "lanczos_error": float(p.group(5)),
+            "noises": [float(x) for x in p.group(6).split(",")],
+            **dict(zip(names, extra))}
     with open(os.path.join(HERE, "reference_goldens.json"), "w") as f:
         json.dump(goldens, f, indent=1)
     print(json.dumps(goldens, indent=1))

@@ -1,0 +1,89 @@
+"""The noised two-site VMPS (subspace expansion) through the device driver
+``udmrg_two_site_finite_vmps_noise``:
+
+* the reference's noise-test goldens (1D and 2D Heisenberg, N = 6, D = 8,
+  ``tests/test_algorithm/test_two_site_noise_update_finite_vmps.cc``), real and
+  complex, with both MPO builders;
+* a truncating case against the oracle's noised sweep (``oracle/noise.py``):
+  per-update energies, bond dimensions, truncation errors and the noise each
+  update applied;
+* the mixed-precision matvec against the FP64 one on the same case.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import krylov, noise as ON
+from ultradmrg_gb300 import api, models as M
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_goldens.json")))
+PAIRS_2D = [(0, 1), (0, 2), (1, 3), (2, 3), (2, 4), (3, 5), (4, 5)]
+KEYS = ("max_noise", "noise_increase", "noise_decrease", "alpha")
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from ultradmrg_gb300 import build
+    build.build()
+    c = api.Context(0)
+    yield c
+    c.close()
+
+
+def _run(ctx, mpo, pb, labels, sweeps, D, trunc, lerr, noises, dtype=np.float64, prec=0, **kw):
+    mps = [api.DeviceTensor.from_data(ctx, t)
+           for t in M.direct_product_mps([pb] * len(labels), labels, dtype=dtype)]
+    dmpo = [api.DeviceTensor.from_data(ctx, w) for w in mpo]
+    p = api.FiniteVMPSSweepParams(sweeps, D, D, trunc, lerr, 200, precision=prec)
+    return api.two_site_finite_vmps_noise(ctx, mps, dmpo, p, noises, **kw)
+
+
+@pytest.mark.parametrize("builder", ["prefix", "reference"])
+@pytest.mark.parametrize("dtype", [np.float64, np.complex128])
+@pytest.mark.parametrize("case", ["1DHeisenberg", "2DHeisenberg"])
+def test_noise_vmps_goldens_device(ctx, case, dtype, builder):
+    g = GOLD["noise_vmps"][case]
+    mpo, pb = M.heisenberg_chain_mpo(6, pairs=PAIRS_2D if case == "2DHeisenberg" else None,
+                                     dtype=dtype, builder=builder)
+    kw = {k: g[k] for k in KEYS if k in g}
+    e0, log, used = _run(ctx, mpo, pb, [i % 2 for i in range(6)], g["sweeps"], g["Dmax"],
+                         g["trunc_err"], g["lanczos_error"], g["noises"], dtype=dtype, **kw)
+    assert abs(e0 - g["energy"]) < g["tol"], (e0, g["energy"])
+    assert any(u > 0 for u in used)
+
+
+def test_noise_vmps_vs_oracle(ctx):
+    """Heisenberg chain N = 12, D = 12 (truncating), noises 0.1, 0.01, 0.001,
+    Lanczos 1e-12: the device sweep against the oracle's, update by update."""
+    N, D = 12, 12
+    mpo, pb = M.heisenberg_chain_mpo(N, builder="reference")
+    labels = M.random_sz0_labels(N, 5)
+    noises = [0.1, 0.01, 0.001]
+    e0, log, used = _run(ctx, mpo, pb, labels, 4, D, 1e-10, 1e-12, noises)
+    olog, oused = [], []
+    oe = ON.two_site_finite_vmps_with_noise(
+        M.direct_product_mps([pb] * N, labels), mpo,
+        ON.NoiseSweepParams(4, D, D, 1e-10, krylov.LanczosParams(1e-12, 200), noises),
+        olog, oused)
+    assert abs(e0 - oe) <= 1e-9 * abs(oe)
+    assert len(log) == len(olog)
+    for a, b, u, ou in zip(log, olog, used, oused):
+        assert a["site"] == b.site and a["D"] == b.D
+        assert abs(a["e0"] - b.e0) <= 1e-9 * abs(b.e0)
+        assert abs(a["trunc_err"] - b.trunc_err) <= 1e-10
+        assert abs(u - ou) <= 1e-12 * max(ou, 1e-300)
+    assert sum(1 for u in used if u > 0) > 0
+
+
+def test_noise_vmps_mixed_vs_fp64(ctx):
+    N, D = 12, 12
+    mpo, pb = M.heisenberg_chain_mpo(N, builder="reference")
+    labels = M.random_sz0_labels(N, 5)
+    noises = [0.1, 0.01, 0.001]
+    e64, _, _ = _run(ctx, mpo, pb, labels, 4, D, 1e-10, 1e-12, noises)
+    emx, _, _ = _run(ctx, mpo, pb, labels, 4, D, 1e-10, 1e-12, noises, prec=api.PREC_MIXED)
+    assert abs(emx - e64) <= 1e-9 * abs(e64)

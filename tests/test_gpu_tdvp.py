@@ -223,3 +223,21 @@ def test_mixed_tdvp_vs_fp64(ctx):
     err = np.linalg.norm(a - b) / np.linalg.norm(b)
     print(f"mixed TDVP vs FP64: relative state difference {err:.2e}")
     assert err <= 1e-5
+
+
+def test_tdvp_ladder_quench_vs_oracle(ctx):
+    """The ladder TDVP benchmark script (``ultradmrg_gb300.tdvp_ladder``) at a
+    reduced size: 2x4 ladder, ground state at D = 16, S+ quench at the centre,
+    four steps of dt = 0.05 with Krylov 20.  The FP64 device evolution against
+    the oracle's TDVP from the same quenched state (amplitudes, 1e-10), the
+    mixed form against the FP64 one (local <Sz> and overlap)."""
+    from ultradmrg_gb300 import tdvp_ladder as TL
+    out, final, quenched, mpo_c = TL.run(ctx, Lx=4, D=16, steps=4, dt=0.05, krylov=20, every=2,
+                                         gs_schedule="2:8,2:16")
+    p = otdvp.TDVPParams(0.05, 1, 16, 1e-10, LanczosParams(1e-10, 20))
+    ref = otdvp.two_site_finite_tdvp([t.copy() for t in quenched], mpo_c, p, 4)
+    v, vr = mps_dense(final["fp64"]), mps_dense(ref)
+    assert np.linalg.norm(v - vr) <= 1e-10 * np.linalg.norm(vr)
+    for cp in out["checkpoints"]:
+        assert cp["max_abs_dSz"] <= 1e-6, cp
+        assert cp["overlap_err"] <= 1e-8, cp

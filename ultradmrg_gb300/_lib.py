@@ -36,6 +36,11 @@ class SweepParams(C.Structure):
                 ("svd_audit", C.c_int64), ("svd_sketch_max_fraction", C.c_double)]
 
 
+class NoiseParams(C.Structure):
+    _fields_ = [("noises", c_double_p), ("n_noises", C.c_int64), ("noise_decrease", C.c_double),
+                ("noise_increase", C.c_double), ("max_noise", C.c_double), ("alpha", C.c_double)]
+
+
 class SiteLog(C.Structure):
     _fields_ = [("site", C.c_int64), ("e0", C.c_double), ("trunc_err", C.c_double),
                 ("D", C.c_int64), ("iters", C.c_int64), ("ee", C.c_double),
@@ -116,6 +121,10 @@ SIGNATURES = {
                                            c_float_p, c_float_p, C.c_int64, c_int64_p,
                                            c_double_p, C.POINTER(SiteLog), C.c_int64,
                                            c_int64_p],
+    "udmrg_two_site_finite_vmps_noise": [C.c_void_p, C.c_int64, c_void_pp, c_void_pp,
+                                         C.POINTER(SweepParams), C.POINTER(NoiseParams),
+                                         c_double_p, C.POINTER(SiteLog), C.c_int64, c_int64_p,
+                                         c_double_p],
     "udmrg_rank_model_sizes": [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)],
     "udmrg_rank_model_create": [C.c_void_p, C.c_uint64, c_void_pp],
     "udmrg_rank_model_destroy": [C.c_void_p],

@@ -352,6 +352,28 @@ def _log_rows(log, n):
     return rows
 
 
+def two_site_finite_vmps_noise(ctx, mps: List[DeviceTensor], mpo: List[DeviceTensor],
+                               params: FiniteVMPSSweepParams, noises: Sequence[float],
+                               noise_decrease=0.95, noise_increase=1.02, max_noise=1.0,
+                               alpha=0.3):
+    """``TwoSiteFiniteVMPSWithNoise``: updates ``mps`` in place (centre at site 0
+    on entry), returns (e0, per-site log, noise applied at each update)."""
+    N = len(mps)
+    sp = _sweep_params(params)
+    arr = (C.c_double * max(1, len(noises)))(*noises)
+    npar = _lib.NoiseParams(C.cast(arr, _lib.c_double_p), len(noises), noise_decrease,
+                            noise_increase, max_noise, alpha)
+    cap = 2 * N * max(params.sweeps, 1)
+    log = (_lib.SiteLog * cap)()
+    nlog_arr = (C.c_double * cap)()
+    e0 = C.c_double()
+    nlog = C.c_int64()
+    call("udmrg_two_site_finite_vmps_noise", ctx.h, N, _handles(mps), _handles(mpo), C.byref(sp),
+         C.byref(npar), C.byref(e0), log, cap, C.byref(nlog), nlog_arr)
+    n = min(cap, nlog.value)
+    return float(e0.value), _log_rows(log, n), [float(nlog_arr[i]) for i in range(n)]
+
+
 def two_site_finite_vmps(ctx, mps: List[DeviceTensor], mpo: List[DeviceTensor],
                          params: FiniteVMPSSweepParams):
     """``TwoSiteFiniteVMPS``: updates ``mps`` in place, returns (e0, per-site log)."""

@@ -663,6 +663,45 @@ int udmrg_two_site_finite_vmps_learned(udmrg_ctx *c, int64_t N, udmrg_tensor **m
   });
 }
 
+int udmrg_two_site_finite_vmps_noise(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
+                                     udmrg_tensor *const *mpo, const udmrg_sweep_params *params,
+                                     const udmrg_noise_params *noise, double *e0,
+                                     udmrg_site_log *log, int64_t log_cap, int64_t *log_len,
+                                     double *noise_log) {
+  return guarded([&] {
+    UDMRG_REQUIRE(noise != nullptr && (noise->n_noises == 0 || noise->noises != nullptr),
+                  "noise vmps: missing noise parameters");
+    std::vector<TensorPtr> m(N);
+    for (int64_t i = 0; i < N; ++i) m[i] = T(mps[i]).clone();
+    std::vector<const BTensor *> w(N);
+    for (int64_t i = 0; i < N; ++i) w[i] = &T(mpo[i]);
+    SweepParams p;
+    p.sweeps = params->sweeps;
+    p.Dmin = params->Dmin;
+    p.Dmax = params->Dmax;
+    p.trunc_err = params->trunc_err;
+    p.lancz = {params->lancz_params.error, params->lancz_params.max_iterations,
+               (int)params->lancz_params.matvec_precision};
+    NoiseParams np;
+    np.noises.assign(noise->noises, noise->noises + noise->n_noises);
+    np.noise_decrease = noise->noise_decrease;
+    np.noise_increase = noise->noise_increase;
+    np.max_noise = noise->max_noise;
+    np.alpha = noise->alpha;
+    std::vector<SiteLog> lg;
+    std::vector<double> nl;
+    const double e = two_site_finite_vmps_noise(c->ctx, m, w, p, np, &lg, &nl);
+    c->ctx.sync();
+    for (int64_t i = 0; i < N; ++i) mps[i]->t = std::move(m[i]);
+    if (e0) *e0 = e;
+    if (log_len) *log_len = (int64_t)lg.size();
+    for (int64_t i = 0; i < std::min<int64_t>(log_cap, (int64_t)lg.size()); ++i) {
+      if (log) log[i] = site_log(lg[i]);
+      if (noise_log) noise_log[i] = i < (int64_t)nl.size() ? nl[i] : 0.0;
+    }
+  });
+}
+
 int udmrg_finite_dmrg(udmrg_ctx *c, int64_t N, udmrg_tensor **mps,
                       const udmrg_mat_repr_site *mro, const udmrg_sweep_params *params,
                       double *e0, udmrg_site_log *log, int64_t log_cap, int64_t *log_len) {

@@ -152,6 +152,25 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
                                   const SketchHint *hint = nullptr,
                                   BondSpectra *spectra = nullptr);
 
+// Noise fields of FiniteVMPSSweepParams (finite_vmps_sweep_params.h:31-107):
+// the starting noise of each sweep (the last one repeats) and its adaptation.
+struct NoiseParams {
+  std::vector<double> noises;
+  // defaults: kVMPSNoiseDecreaseRate, kVMPSNoiseIncreaseRate, kVMPSMaxNoise,
+  // kVMPSNoiseAlpha (finite_vmps_sweep_params.h:25-28)
+  double noise_decrease = 0.95, noise_increase = 1.02, max_noise = 1.0, alpha = 0.3;
+};
+
+// TwoSiteFiniteVMPSWithNoise (two_site_update_noise_finite_vmps_impl.h:81-556):
+// boundaries from the edges, adaptive noise, subspace expansion of every
+// update's bond (noise.cpp).  No noises: the plain sweep.  noise_log: the
+// noise applied at each update (0: no expansion).  The MPS centre must be at
+// site 0 on entry.
+double two_site_finite_vmps_noise(Ctx &ctx, std::vector<TensorPtr> &mps,
+                                  const std::vector<const BTensor *> &mpo, const SweepParams &p,
+                                  const NoiseParams &np, std::vector<SiteLog> *log,
+                                  std::vector<double> *noise_log);
+
 // Learned truncation state: the rank model (used when svd_mode ==
 // kSvdSketchLearned), the spectra and kept counts of every bond at its last
 // visit (kept across sweep calls on the same chain, so a schedule of sweeps

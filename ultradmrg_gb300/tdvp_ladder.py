@@ -71,6 +71,77 @@ def overlap_error(b, ket, bra):
     return float(1.0 - abs(kb) / np.sqrt(abs(kk) * abs(bb)))
 
 
+def run(ctx, Lx=32, D=512, steps=40, dt=0.05, krylov=20, every=10, forms=("fp64", "mixed"),
+        gs_schedule="2:64,2:128,2:256,2:512"):
+    """The benchmark on an open context.  Returns (report, {form: host MPS
+    after the evolution}, the quenched host MPS, the complex host MPO)."""
+    forms = [f for f in forms if f]
+    prec = {"fp64": api.PREC_FP64, "mixed": api.PREC_MIXED}
+    N, mpo, pb, ops = ladder_problem(Lx, np.float64)
+    schedule = [(int(s), min(int(d), D)) for s, d in
+                (x.split(":") for x in gs_schedule.split(","))]
+    t0 = time.perf_counter()
+    e0, gs = ground_state(ctx, mpo, pb, N, schedule)
+    gs_sec = time.perf_counter() - t0
+    centre = N // 2
+    quenched = M.act_operator_on_mps(gs, ops["sp"], None, centre)
+    _, mpo_c, _, _ = ladder_problem(Lx, np.complex128)
+    dmpo = [api.DeviceTensor.from_data(ctx, w) for w in mpo_c]
+    states = {f: [api.DeviceTensor.from_data(ctx, t.copy()) for t in quenched] for f in forms}
+    backend = dm.device_backend(ctx)
+    out = {"config": {"lattice": f"2x{Lx} Heisenberg ladder", "sites": N, "D": D,
+                      "dt": dt, "steps": steps, "krylov": krylov, "quench": "S+",
+                      "quench_site": centre, "seed": 2, "gs_schedule": schedule},
+           "ground_state": {"energy": e0, "seconds": gs_sec},
+           "forms": {f: {"seconds": 0.0, "updates": 0} for f in forms}, "checkpoints": []}
+    clocks = {f: [] for f in forms}
+    done = 0
+    while done < steps:
+        n = min(every, steps - done)
+        for f in forms:
+            p = api.TDVPEvolveParams(dt, n, 1, D, 1e-10, 1e-10, krylov, precision=prec[f])
+            ctx.sync()
+            with ClockSampler(0) as clk:
+                t1 = time.perf_counter()
+                log = api.two_site_finite_tdvp(ctx, states[f], dmpo, p)
+                ctx.sync()
+                out["forms"][f]["seconds"] += time.perf_counter() - t1
+            clocks[f].append(clk.summary())
+            out["forms"][f]["updates"] += len(log)
+            out["forms"][f]["D_max"] = max(r["D"] for r in log)
+        done += n
+        cp = {"step": done, "time": done * dt}
+        sz = {}
+        for f in forms:
+            m = dm.MPSMeasurer(backend, states[f])
+            sz[f] = np.array([r.avg for r in dm.measure_one_site_op(m, ops["sz"].mat.astype(
+                np.complex128))])
+            m.close()
+            cp[f"sz_{f}_centre"] = complex(sz[f][centre]).real
+        if "fp64" in forms and "mixed" in forms:
+            cp["max_abs_dSz"] = float(np.abs(sz["mixed"] - sz["fp64"]).max())
+            cp["overlap_err"] = overlap_error(backend, states["mixed"], states["fp64"])
+        out["checkpoints"].append(cp)
+    for f in forms:
+        out["forms"][f]["seconds_per_step"] = out["forms"][f]["seconds"] / steps
+        cs = [c for c in clocks[f] if c["samples"]]
+        out["forms"][f]["clocks"] = {
+            "sm_mhz_min_of_medians": min((c["sm_mhz"] for c in cs), default=None),
+            "sm_max_mhz": max((c["sm_max_mhz"] for c in cs), default=None),
+            "reasons": sorted({r for c in cs for r in c["reasons"]}),
+            "samples": sum(c["samples"] for c in cs)}
+    if "fp64" in forms and "mixed" in forms:
+        out["speedup_mixed_vs_fp64"] = (out["forms"]["fp64"]["seconds"] /
+                                        out["forms"]["mixed"]["seconds"])
+    final = {f: [t.to_data() for t in states[f]] for f in forms}
+    for f in forms:
+        for t in states[f]:
+            t.close()
+    for t in dmpo:
+        t.close()
+    return out, final, quenched, mpo_c
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--Lx", type=int, default=32)
@@ -84,74 +155,14 @@ def main(argv=None):
                     help="ground-state sweeps:D pairs (D capped at --D)")
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
-    forms = [f for f in a.forms.split(",") if f]
-    prec = {"fp64": api.PREC_FP64, "mixed": api.PREC_MIXED}
     ctx = api.Context(0)
-    N, mpo, pb, ops = ladder_problem(a.Lx, np.float64)
-    schedule = [(int(s), min(int(d), a.D)) for s, d in
-                (x.split(":") for x in a.gs_schedule.split(","))]
-    t0 = time.perf_counter()
-    e0, gs = ground_state(ctx, mpo, pb, N, schedule)
-    gs_sec = time.perf_counter() - t0
-    centre = N // 2
-    quenched = M.act_operator_on_mps(gs, ops["sp"], None, centre)
-    _, mpo_c, _, _ = ladder_problem(a.Lx, np.complex128)
-    dmpo = [api.DeviceTensor.from_data(ctx, w) for w in mpo_c]
-    states = {f: [api.DeviceTensor.from_data(ctx, t.copy()) for t in quenched] for f in forms}
-    backend = dm.device_backend(ctx)
-    out = {"config": {"lattice": f"2x{a.Lx} Heisenberg ladder", "sites": N, "D": a.D,
-                      "dt": a.dt, "steps": a.steps, "krylov": a.krylov, "quench": "S+",
-                      "quench_site": centre, "seed": 2, "gs_schedule": schedule},
-           "ground_state": {"energy": e0, "seconds": gs_sec},
-           "forms": {f: {"seconds": 0.0, "updates": 0} for f in forms}, "checkpoints": []}
-    clocks = {f: [] for f in forms}
-    done = 0
-    while done < a.steps:
-        n = min(a.every, a.steps - done)
-        for f in forms:
-            p = api.TDVPEvolveParams(a.dt, n, 1, a.D, 1e-10, 1e-10, a.krylov, precision=prec[f])
-            ctx.sync()
-            with ClockSampler(0) as clk:
-                t1 = time.perf_counter()
-                log = api.two_site_finite_tdvp(ctx, states[f], dmpo, p)
-                ctx.sync()
-                out["forms"][f]["seconds"] += time.perf_counter() - t1
-            clocks[f].append(clk.summary())
-            out["forms"][f]["updates"] += len(log)
-            out["forms"][f]["D_max"] = max(r["D"] for r in log)
-        done += n
-        cp = {"step": done, "time": done * a.dt}
-        sz = {}
-        for f in forms:
-            m = dm.MPSMeasurer(backend, states[f])
-            sz[f] = np.array([r.avg for r in dm.measure_one_site_op(m, ops["sz"].mat.astype(
-                np.complex128))])
-            m.close()
-            cp[f"sz_{f}_centre"] = complex(sz[f][centre]).real
-        if "fp64" in forms and "mixed" in forms:
-            cp["max_abs_dSz"] = float(np.abs(sz["mixed"] - sz["fp64"]).max())
-            cp["overlap_err"] = overlap_error(backend, states["mixed"], states["fp64"])
-        out["checkpoints"].append(cp)
-    for f in forms:
-        out["forms"][f]["seconds_per_step"] = out["forms"][f]["seconds"] / a.steps
-        cs = [c for c in clocks[f] if c["samples"]]
-        out["forms"][f]["clocks"] = {
-            "sm_mhz_min_of_medians": min((c["sm_mhz"] for c in cs), default=None),
-            "sm_max_mhz": max((c["sm_max_mhz"] for c in cs), default=None),
-            "reasons": sorted({r for c in cs for r in c["reasons"]}),
-            "samples": sum(c["samples"] for c in cs)}
-    if "fp64" in forms and "mixed" in forms:
-        out["speedup_mixed_vs_fp64"] = out["forms"]["fp64"]["seconds"] / out["forms"]["mixed"]["seconds"]
+    out, _, _, _ = run(ctx, a.Lx, a.D, a.steps, a.dt, a.krylov, a.every, a.forms.split(","),
+                       a.gs_schedule)
     line = json.dumps(out)
     print(line)
     if a.out:
         with open(a.out, "w") as fh:
             fh.write(line + "\n")
-    for f in forms:
-        for t in states[f]:
-            t.close()
-    for t in dmpo:
-        t.close()
     ctx.close()
     return 0
 
