@@ -362,9 +362,10 @@ int udmrg_matvec_plan_stage_times(udmrg_matvec_plan *p, const double *d_in, doub
  * writes the FP64 result.  0 for the FP64 form. */
 int udmrg_matvec_plan_stage_bytes(udmrg_matvec_plan *p, double *bytes);
 /* Mixed form: run the MPO step inside the producers of the .R GEMM (enable =
- * 1, the default) or as its own kernel writing the split-BF16 T3 image
- * (enable = 0).  Both give bit-identical results.  No counterpart in the
- * reference (a kernel check used by the tests). */
+ * 1) or as its own kernel writing the split-BF16 T3 image (enable = 0, the
+ * default, faster on the measured workloads).  Both give bit-identical
+ * results.  No counterpart in the reference (a kernel check used by the
+ * tests). */
 int udmrg_matvec_plan_set_fused(udmrg_matvec_plan *p, int enable);
 
 /* ---- measurement ---------------------------------------------------- */

@@ -154,6 +154,7 @@ def test_fused_mpo_gemm_bit_identical(ctx, name, l, cplx):
     dpsi = api.DeviceTensor.from_data(ctx, psi, dt)
     plan = api.MatvecPlan(ctx, dev, dpsi, precision=MIXED)
     x, yf, yu = plan.embed(dpsi), plan.embed(dpsi), plan.embed(dpsi)
+    plan.set_fused(True)
     plan.apply(x, yf)
     plan.set_fused(False)
     plan.apply(x, yu)
@@ -175,6 +176,7 @@ def test_fused_mpo_gemm_workload(ctx):
     psi = api.contract(ctx, up(ctx, mps[l]), up(ctx, mps[l + 1]), [2], [0])
     pm = api.MatvecPlan(ctx, [L, up(ctx, mpo[l]), up(ctx, mpo[l + 1]), R], psi, precision=MIXED)
     x, yf, yu = pm.embed(psi), pm.embed(psi), pm.embed(psi)
+    pm.set_fused(True)
     pm.apply(x, yf)
     pm.set_fused(False)
     pm.apply(x, yu)

@@ -640,8 +640,8 @@ class MatvecPlan:
         return list(ms), list(fl)
 
     def set_fused(self, enable: bool):
-        """Mixed form: MPO step inside the .R GEMM's producers (default) or as
-        its own kernel (bit-identical results)."""
+        """Mixed form: MPO step inside the .R GEMM's producers or as its own
+        kernel (the default; bit-identical results)."""
         call("udmrg_matvec_plan_set_fused", self.h, 1 if enable else 0)
 
     def stage_bytes(self):

@@ -1154,7 +1154,7 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
     ctx.sync();
     // the first grid point with `need` eigenvalues above it, then one point
     // lower (a factor 1.34: near-ties and rounding at the threshold)
-    int ks = kGrid;
+    int ks = -1;
     for (int k = 0; k <= kGrid; ++k) {
       int64_t t = 0;
       for (int q = 0; q < nj; ++q) t += cnt[(size_t)q * (kGrid + 1) + k];
@@ -1163,11 +1163,16 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
         break;
       }
     }
-    ks = std::min(ks + 1, kGrid);
-    for (int q = 0; q < nj; ++q) {
-      const int64_t n = jobs[q].n;
-      const int64_t c = std::max<int64_t>(cnt[(size_t)q * (kGrid + 1) + ks], std::min(n, floor));
-      wk.computed[q] = std::min(c, n);
+    // fewer than `need` eigenvalues above the lowest grid point (a rank-deficient
+    // set, and a Dmin asking for its null states too): every eigenvalue
+    if (ks >= 0) {
+      ks = std::min(ks + 1, kGrid);
+      for (int q = 0; q < nj; ++q) {
+        const int64_t n = jobs[q].n;
+        const int64_t c =
+            std::max<int64_t>(cnt[(size_t)q * (kGrid + 1) + ks], std::min(n, floor));
+        wk.computed[q] = std::min(c, n);
+      }
     }
   }
   std::vector<int2> chunks;

@@ -140,9 +140,11 @@ struct SgMatvecPlan {
   MpoNzRec *d_nz = nullptr;
   MpoTask *d_tasks = nullptr;
   int max_nin = 0, max_nout = 0;
-  // fused MPO step + .R GEMM (the default; the unfused pair of kernels stays
-  // for checks: both give bit-identical results)
-  bool fused = true;
+  // fused MPO step + .R GEMM (off by default: at the Hubbard 4x16 D=2000
+  // centre bond the fused kernel takes 0.43 ms against 0.21 ms for the two
+  // kernels, its producers being latency bound and recomputing a T3 tile for
+  // every N tile; both forms give bit-identical results)
+  bool fused = false;
   std::vector<MpoGroupMap> gmap;
   std::vector<MpoRowInfo> rowinfo;
   std::vector<MpoKChunk> kchunks;

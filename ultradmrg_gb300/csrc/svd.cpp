@@ -427,7 +427,8 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
   // the rest is each Gram matrix's trace minus the computed ones
   SymEigWork wk;
   check_eig_status(sym_eig_values(ctx, scratch, jobs, G, lam, wk, cplx,
-                                  Dmax > 0 ? Dmax + 64 : 0, spectrum_floor));
+                                  Dmax > 0 ? std::max(Dmax, Dmin) + 64 : 0,
+                                  spectrum_floor));
   const std::vector<double> hlam = download_vec(ctx, lam, ltot);
   std::vector<std::vector<double>> sv(nsec);
   double rest = 0.0;
