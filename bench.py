@@ -356,8 +356,9 @@ def run_ours(args):
     W2 = api.DeviceTensor.from_data(ctx, mpo[l + 1])
     ops = [L, W1, W2, R]
     t0 = time.perf_counter()
-    plan = api.MatvecPlan(ctx, ops, psi, precision=api.PREC_MIXED)
+    plan = api.MatvecPlan(ctx, ops, psi, precision=api.PREC_MIXED)  # tile autotuner runs here
     plan_s = time.perf_counter() - t0
+    tiles = plan.tiles()
     plan64 = api.MatvecPlan(ctx, ops, psi, precision=api.PREC_FP64)
     info = plan.info()
     x = plan.embed(psi)
@@ -423,6 +424,28 @@ def run_ours(args):
     # per-stage device times (dominant kernel roofline)
     ms_mx, fl_mx = plan.stage_times(xp, yp)
     ms_64, fl_64 = plan64.stage_times(xp, y64p)
+    # the tile autotuner's choice against the fixed tile shapes (one matvec per
+    # stage, best of three; the plan of each shape built here)
+    tune = {"choice_bn1_bn3": list(tiles[:2]), "tuned": tiles[2],
+            "plan_seconds_with_trials": plan_s}
+    for bn in (64, 128):
+        ctx.set_tc_tiles(bn, bn)
+        pf = api.MatvecPlan(ctx, ops, psi, precision=api.PREC_MIXED)
+        ctx.set_tc_tiles(0, 0)
+        best = None
+        for _ in range(3):
+            ms_f, _ = pf.stage_times(xp, yp)
+            best = ms_f if best is None else [min(u, v) for u, v in zip(best, ms_f)]
+        tune[f"fixed_{bn}_stage_ms"] = best
+        tune[f"fixed_{bn}_ms"] = sum(best)
+        del pf
+    best = None
+    for _ in range(3):
+        ms_t, _ = plan.stage_times(xp, yp)
+        best = ms_t if best is None else [min(u, v) for u, v in zip(best, ms_t)]
+    tune["tuned_stage_ms"] = best
+    tune["tuned_ms"] = sum(best)
+    tune["trials_run"], tune["classes"] = ctx.tc_tuning()
     # Lanczos energies of both forms from the same start vector, to convergence
     lz = {}
     for name, prec in (("mixed", api.PREC_MIXED), ("fp64", api.PREC_FP64)):
@@ -533,6 +556,7 @@ def run_ours(args):
         "config": {"workload": w.name, "D": w.D, "sites": w.N, "bond": l,
                    "psi_elements": info["psi_size"], "mpo_bond_dim": mpo[l].indexes[3].dim,
                    "form": "mixed (tcgen05 split-BF16 block GEMMs)",
+                   "tc_tiles_bn1_bn3": list(tiles[:2]),
                    "parallelism": "replicas only" if ws > 1 else "single GPU",
                    "l2": "flushed (512 MB write) before every timed step",
                    "plan_seconds": plan_s},
@@ -552,6 +576,7 @@ def run_ours(args):
                      "lanczos_iters": [lz["mixed"][1], lz["fp64"][1]],
                      "lanczos_rel_dE": abs(lz["mixed"][0] - lz["fp64"][0]) / abs(lz["fp64"][0])},
         "krylov_graph": kg,
+        "tile_autotuner": tune,
         "centre_site_update": {
             k: {kk: v[kk] for kk in ("wall_sec", "lancz_sec", "svd_sec", "env_sec", "iters", "D",
                                      "trunc_err", "e0", "svd_grow_rounds")}

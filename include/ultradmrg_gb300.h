@@ -112,6 +112,15 @@ int udmrg_ctx_launches(udmrg_ctx *ctx, uint64_t *out);
  * qlmps: the reference loop calls the matvec function pointer per step
  * (lanczos_vmps_solver_impl.h:148, 213). */
 int udmrg_ctx_set_krylov_graph(udmrg_ctx *ctx, int enable);
+/* Mixed matvec: rows of the B tiles of the two tcgen05 GEMMs (L.psi: bn1,
+ * .R: bn3), 64 or 128, or 0 for the tile autotuner (the default): the first
+ * plan of a shape class is built with both tiles, one matvec of each is timed
+ * stage by stage, each GEMM keeps its faster tile and later plans of the class
+ * reuse the choice.  udmrg_ctx_tc_tuning reports the trials run and the shape
+ * classes decided.  No counterpart in the reference (tile tuning of the GB300
+ * kernels). */
+int udmrg_ctx_set_tc_tiles(udmrg_ctx *ctx, int bn1, int bn3);
+int udmrg_ctx_tc_tuning(udmrg_ctx *ctx, int64_t *trials, int64_t *classes);
 
 /* ---- tensors (QLTensor storage model) -------------------------------- */
 /* nsec[rank]: sectors per index; qns[sum(nsec)*nq]; dims[sum(nsec)];
@@ -367,6 +376,9 @@ int udmrg_matvec_plan_stage_bytes(udmrg_matvec_plan *p, double *bytes);
  * results.  No counterpart in the reference (a kernel check used by the
  * tests). */
 int udmrg_matvec_plan_set_fused(udmrg_matvec_plan *p, int enable);
+/* Mixed form: the B-tile rows of its two GEMMs and whether the autotuner
+ * chose them (*tuned = 1).  No counterpart in the reference. */
+int udmrg_matvec_plan_tiles(const udmrg_matvec_plan *p, int *bn1, int *bn3, int *tuned);
 
 /* ---- measurement ---------------------------------------------------- */
 /* FP64 FMA throughput of the device (TFLOP/s), measured by a DFMA-bound

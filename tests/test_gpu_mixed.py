@@ -181,3 +181,50 @@ def test_fused_mpo_gemm_workload(ctx):
     pm.set_fused(False)
     pm.apply(x, yu)
     assert np.array_equal(yf.download_packed(), yu.download_packed())
+
+
+@pytest.mark.parametrize("tiles", [(128, 128), (64, 128), (128, 64)])
+@pytest.mark.parametrize("name,l", [("hub", 2), ("hub_big", 3)])
+def test_tc_tile_shapes(ctx, tiles, name, l):
+    """B tiles of 128 rows (either GEMM) against the oracle and against 64-row
+    tiles; the fused form with the same tiles bit for bit."""
+    mpo, mps = SYSTEMS[name]()
+    eff, psi = two_site_problem(mpo, mps, l)
+    ref = krylov.eff_ham_mul_two_site_state(eff, psi)
+    dev = [up(ctx, t) for t in eff]
+    dpsi = up(ctx, psi)
+    try:
+        ctx.set_tc_tiles(64, 64)
+        p64 = api.MatvecPlan(ctx, dev, dpsi, precision=MIXED)
+        ctx.set_tc_tiles(*tiles)
+        pt = api.MatvecPlan(ctx, dev, dpsi, precision=MIXED)
+    finally:
+        ctx.set_tc_tiles(0, 0)
+    assert pt.tiles()[:2] == tiles
+    x, y64, yt, yf = pt.embed(dpsi), pt.embed(dpsi), pt.embed(dpsi), pt.embed(dpsi)
+    p64.apply(x, y64)
+    pt.apply(x, yt)
+    pt.set_fused(True)
+    pt.apply(x, yf)
+    a, b = yt.download_packed(), y64.download_packed()
+    assert np.array_equal(yf.download_packed(), a)
+    assert np.max(np.abs(a - b)) <= 1e-6 * np.max(np.abs(b))
+    d, s = max_block_diff(yt.to_data(), ref)
+    assert d <= 2e-5 * s, (d, s)
+
+
+def test_tc_tile_autotuner(ctx):
+    """With no tiles set, the first plan of a shape class runs the timed
+    trials and later plans of the class reuse the choice."""
+    mpo, mps = SYSTEMS["hub_big"]()
+    eff, psi = two_site_problem(mpo, mps, 3)
+    dev = [up(ctx, t) for t in eff]
+    dpsi = up(ctx, psi)
+    t0, _ = ctx.tc_tuning()
+    p1 = api.MatvecPlan(ctx, dev, dpsi, precision=MIXED)
+    t1, classes = ctx.tc_tuning()
+    p2 = api.MatvecPlan(ctx, dev, dpsi, precision=MIXED)
+    t2, _ = ctx.tc_tuning()
+    assert p1.tiles()[2] and p2.tiles()[2] and classes >= 1
+    assert p1.tiles() == p2.tiles()
+    assert t2 == t1 and t1 <= t0 + 1

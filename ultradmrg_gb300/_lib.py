@@ -73,6 +73,8 @@ SIGNATURES = {
     "udmrg_ctx_sync": [C.c_void_p],
     "udmrg_ctx_launches": [C.c_void_p, C.POINTER(C.c_uint64)],
     "udmrg_ctx_set_krylov_graph": [C.c_void_p, C.c_int],
+    "udmrg_ctx_set_tc_tiles": [C.c_void_p, C.c_int, C.c_int],
+    "udmrg_ctx_tc_tuning": [C.c_void_p, c_int64_p, c_int64_p],
     "udmrg_tensor_create": [C.c_void_p, C.c_int, C.c_int, C.c_int, c_int32_p, c_int32_p,
                             c_int64_p, c_int32_p, C.c_int64, c_int32_p, c_void_pp],
     "udmrg_tensor_destroy": [C.c_void_p],
@@ -147,6 +149,8 @@ SIGNATURES = {
                                       c_double_p],
     "udmrg_matvec_plan_stage_bytes": [C.c_void_p, c_double_p],
     "udmrg_matvec_plan_set_fused": [C.c_void_p, C.c_int],
+    "udmrg_matvec_plan_tiles": [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                C.POINTER(C.c_int)],
     "udmrg_probe_fp64_tflops": [C.c_void_p, c_double_p],
     "udmrg_ctx_event_record": [C.c_void_p, C.c_int],
     "udmrg_ctx_event_elapsed": [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)],

@@ -37,6 +37,17 @@ class Context:
         call("udmrg_ctx_launches", self.h, C.byref(v))
         return int(v.value)
 
+    def set_tc_tiles(self, bn1: int = 0, bn3: int = 0):
+        """B-tile rows of the mixed matvec's two tcgen05 GEMMs (64 or 128), or
+        0, 0 for the autotuner (the default)."""
+        call("udmrg_ctx_set_tc_tiles", self.h, bn1, bn3)
+
+    def tc_tuning(self):
+        """(timed trials run, shape classes decided) of the tile autotuner."""
+        t, c = C.c_int64(), C.c_int64()
+        call("udmrg_ctx_tc_tuning", self.h, C.byref(t), C.byref(c))
+        return t.value, c.value
+
     def set_krylov_graph(self, enable: bool):
         """Krylov steps as one CUDA graph replay each (default) or direct launches."""
         call("udmrg_ctx_set_krylov_graph", self.h, 1 if enable else 0)
@@ -638,6 +649,12 @@ class MatvecPlan:
         call("udmrg_matvec_plan_stage_times", self.h, C.cast(C.c_void_p(d_in), _lib.c_double_p),
              C.cast(C.c_void_p(d_out), _lib.c_double_p), ms, fl)
         return list(ms), list(fl)
+
+    def tiles(self):
+        """Mixed form: (bn1, bn3, chosen by the autotuner)."""
+        a, b, t = C.c_int(), C.c_int(), C.c_int()
+        call("udmrg_matvec_plan_tiles", self.h, C.byref(a), C.byref(b), C.byref(t))
+        return a.value, b.value, bool(t.value)
 
     def set_fused(self, enable: bool):
         """Mixed form: MPO step inside the .R GEMM's producers or as its own

@@ -9,6 +9,8 @@
 // tensor's axes.
 #pragma once
 
+#include <array>
+#include <map>
 #include <memory>
 #include <unordered_map>
 
@@ -53,6 +55,12 @@ struct Ctx {
   uint64_t launches = 0;
   // Krylov solvers replay each step as one CUDA graph (captured once per solve)
   bool krylov_graph = true;
+  // Mixed matvec: B-tile rows of the tcgen05 GEMMs L.psi (tc_bn1) and .R
+  // (tc_bn3), 64 or 128; 0: chosen per plan by timed trials, cached per
+  // shape class in tc_tuned (class -> {bn1, bn3}); tc_trials counts them
+  int tc_bn1 = 0, tc_bn3 = 0;
+  std::map<std::array<int64_t, 3>, std::array<int, 2>> tc_tuned;
+  int64_t tc_trials = 0;
   // C-ABI lifetime: live tensor / plan handles on this context; a context
   // whose destroy was requested is deleted when the last handle goes
   int64_t live_handles = 0;

@@ -117,6 +117,23 @@ int udmrg_ctx_launches(udmrg_ctx *c, uint64_t *out) {
   return guarded([&] { *out = c->ctx.launches; });
 }
 
+int udmrg_ctx_set_tc_tiles(udmrg_ctx *c, int bn1, int bn3) {
+  return guarded([&] {
+    auto ok = [](int b) { return b == 0 || b == 64 || b == 128; };
+    UDMRG_REQUIRE(ok(bn1) && ok(bn3) && ((bn1 == 0) == (bn3 == 0)),
+                  "tc tiles: 64 or 128 each, or both 0 (autotuner)");
+    c->ctx.tc_bn1 = bn1;
+    c->ctx.tc_bn3 = bn3;
+  });
+}
+
+int udmrg_ctx_tc_tuning(udmrg_ctx *c, int64_t *trials, int64_t *classes) {
+  return guarded([&] {
+    if (trials) *trials = c->ctx.tc_trials;
+    if (classes) *classes = (int64_t)c->ctx.tc_tuned.size();
+  });
+}
+
 int udmrg_ctx_set_krylov_graph(udmrg_ctx *c, int enable) {
   return guarded([&] {
     UDMRG_REQUIRE(c, "null argument");
@@ -951,6 +968,16 @@ int udmrg_matvec_plan_stage_bytes(udmrg_matvec_plan *p, double *bytes) {
         bytes[3] = (double)g.t3_bytes + (double)g.r_bytes + 8.0 * nreal;
       }
     }
+  });
+}
+
+int udmrg_matvec_plan_tiles(const udmrg_matvec_plan *p, int *bn1, int *bn3, int *tuned) {
+  return guarded([&] {
+    const MatvecPlan &m = *p->plan;
+    UDMRG_REQUIRE(m.sg != nullptr, "plan tiles: not a mixed-precision plan");
+    if (bn1) *bn1 = m.sg->bn1;
+    if (bn3) *bn3 = m.sg->bn3;
+    if (tuned) *tuned = m.sg->tuned ? 1 : 0;
   });
 }
 

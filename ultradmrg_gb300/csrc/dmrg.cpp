@@ -122,7 +122,7 @@ std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTens
   }
   if (precision == kPrecMixed) {  // complex data through the real embedding
     if (!fm) fm = std::make_unique<FusedMpo>(ctx, W1, W2);
-    mv->sg = plan_sg_matvec(ctx, L, R, *mv->sstruct, *fm);
+    mv->sg = plan_sg_matvec_tuned(ctx, L, R, *mv->sstruct, *fm);
   }
   // the FP64 form is kept in both modes (the mixed solver's final Rayleigh quotient)
   const int es = elem_doubles(psi0.dtype);

@@ -41,7 +41,9 @@ inline int64_t up8(int64_t x) { return (x + 7) & ~(int64_t)7; }
 }  // namespace
 
 std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const BTensor &R,
-                                             const BTensor &S, FusedMpo &fm) {
+                                             const BTensor &S, FusedMpo &fm, int bn1, int bn3) {
+  UDMRG_REQUIRE((bn1 == 64 || bn1 == 128) && (bn3 == 64 || bn3 == 128),
+                "mixed matvec: B tiles of 64 or 128 rows");
   // complex L, R, psi: the real embedding [[Re, -Im], [Im, Re]] (the MPO
   // coefficients are real, see FusedMpo)
   const bool cplx = S.dtype == kC128;
@@ -54,6 +56,10 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   p->g3.ctx = &ctx;
   p->psi_size = S.size();
   p->cplx = cplx;
+  p->bn1 = bn1;
+  p->bn3 = bn3;
+  p->g1.bn = bn1;
+  p->g3.bn = bn3;
   // pack a block (or its real / imaginary part) of a tensor with element
   // offset `off`, row and column strides in elements
   auto add_pack = [&](std::vector<PackOp> &ops, int64_t off, int64_t rs, int64_t cs,
@@ -129,10 +135,10 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       // [psi_r; psi_i]
       for (int64_t q = 0; q < ds12; ++q) {
         add_pack(p->psi_pack.ops, S.offs[b] + q * db, 1, ncol, g.p_off, db, g.K,
-                 cof[j] + q * up8(db), 0, kc, kTcBN, 0, false);
+                 cof[j] + q * up8(db), 0, kc, bn1, 0, false);
         if (cplx)
           add_pack(p->psi_pack.ops, S.offs[b] + q * db, 1, ncol, g.p_off, db, g.K,
-                   cof[j] + q * up8(db), g.Kh, kc, kTcBN, 1, false);
+                   cof[j] + q * up8(db), g.Kh, kc, bn1, 1, false);
       }
     }
     // T1 block locations
@@ -153,7 +159,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
     }
     t1tot += g.Me * g.Np;
     lbytes += tc_image_bytes(g.Me, g.Ke, kTcBM);
-    pbytes += tc_image_bytes(g.N, g.Ke, kTcBN);
+    pbytes += tc_image_bytes(g.N, g.Ke, bn1);
     g1s.push_back(g);
   }
   p->t1_size = t1tot;
@@ -202,11 +208,11 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       // op per w2 (the b run at its padded column)
       for (int64_t w2 = 0; w2 < dw2; ++w2) {
         const int64_t off = R.offs[b] + w2 * db, k0 = kof[j] + w2 * up8(db);
-        add_pack(rops, off, nc, 1, r_off, dBp, db, 0, k0, kc, kTcBN, 0, false);
+        add_pack(rops, off, nc, 1, r_off, dBp, db, 0, k0, kc, bn3, 0, false);
         if (cplx) {
-          add_pack(rops, off, nc, 1, r_off, dBp, db, 0, K + k0, kc, kTcBN, 1, true);
-          add_pack(rops, off, nc, 1, r_off, dBp, db, dBp, k0, kc, kTcBN, 1, false);
-          add_pack(rops, off, nc, 1, r_off, dBp, db, dBp, K + k0, kc, kTcBN, 0, false);
+          add_pack(rops, off, nc, 1, r_off, dBp, db, 0, K + k0, kc, bn3, 1, true);
+          add_pack(rops, off, nc, 1, r_off, dBp, db, dBp, k0, kc, bn3, 1, false);
+          add_pack(rops, off, nc, 1, r_off, dBp, db, dBp, K + k0, kc, bn3, 0, false);
         }
       }
     }
@@ -287,7 +293,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
     }
     p->g3.add_group(t3_off, r_off, (int32_t)M, (int32_t)Ne, (int32_t)Ke, rows);
     t3bytes += tc_image_bytes(M, Ke, kTcBM);
-    rbytes += tc_image_bytes(Ne, Ke, kTcBN);
+    rbytes += tc_image_bytes(Ne, Ke, bn3);
   }
   p->t3_bytes = t3bytes;
   p->r_bytes = rbytes;
@@ -474,6 +480,53 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   p->d_tgtref = upload_vec(ctx, p->tgtref);
   p->mixed_flops = 6.0 * (p->g1.flops + p->g3.flops);
   ctx.sync();
+  return p;
+}
+
+std::unique_ptr<SgMatvecPlan> plan_sg_matvec_tuned(Ctx &ctx, const BTensor &L, const BTensor &R,
+                                                   const BTensor &S, FusedMpo &fm) {
+  if (ctx.tc_bn1 && ctx.tc_bn3) return plan_sg_matvec(ctx, L, R, S, fm, ctx.tc_bn1, ctx.tc_bn3);
+  auto lg2 = [](int64_t x) {
+    int64_t k = 0;
+    while ((int64_t(1) << k) < x) ++k;
+    return k;
+  };
+  int64_t maxb = 1;
+  for (int64_t d : S.idx[3].dims) maxb = std::max(maxb, d);
+  const std::array<int64_t, 3> key = {S.dtype == kC128 ? 1 : 0, lg2(S.size()), lg2(maxb)};
+  auto it = ctx.tc_tuned.find(key);
+  if (it != ctx.tc_tuned.end()) {
+    auto p = plan_sg_matvec(ctx, L, R, S, fm, it->second[0], it->second[1]);
+    p->tuned = true;
+    return p;
+  }
+  // timed trials: one matvec per tile choice (input zeros: the kernels' work
+  // does not depend on the values), best of two, stage by stage
+  std::unique_ptr<SgMatvecPlan> cand[2];
+  float best[2][4];
+  const int64_t nd = S.size() * (S.dtype == kC128 ? 2 : 1);
+  DeviceScratch sc(ctx);
+  double *x = sc.get<double>(nd), *y = sc.get<double>(nd);
+  UDMRG_CHECK_CUDA(cudaMemsetAsync(x, 0, std::max<int64_t>(nd, 1) * sizeof(double), ctx.stream));
+  for (int c = 0; c < 2; ++c) {
+    const int bn = c == 0 ? 64 : 128;
+    cand[c] = plan_sg_matvec(ctx, L, R, S, fm, bn, bn);
+    for (int rep = 0; rep < 2; ++rep) {
+      float ms[4];
+      cand[c]->apply_timed(x, y, ms);
+      for (int k = 0; k < 4; ++k) best[c][k] = rep == 0 ? ms[k] : std::min(best[c][k], ms[k]);
+    }
+  }
+  ctx.tc_trials++;
+  const int bn1 = best[1][1] < best[0][1] ? 128 : 64;
+  const int bn3 = best[1][3] < best[0][3] ? 128 : 64;
+  ctx.tc_tuned[key] = {bn1, bn3};
+  std::unique_ptr<SgMatvecPlan> p;
+  if (bn1 == bn3)
+    p = std::move(cand[bn1 == 128 ? 1 : 0]);
+  else
+    p = plan_sg_matvec(ctx, L, R, S, fm, bn1, bn3);
+  p->tuned = true;
   return p;
 }
 

@@ -140,6 +140,10 @@ struct SgMatvecPlan {
   MpoNzRec *d_nz = nullptr;
   MpoTask *d_tasks = nullptr;
   int max_nin = 0, max_nout = 0;
+  // B-tile rows of the two tcgen05 GEMMs (their B images are packed with
+  // them); tuned: chosen by timed trials for this plan's shape class
+  int bn1 = kTcBN, bn3 = kTcBN;
+  bool tuned = false;
   // fused MPO step + .R GEMM (off by default: at the Hubbard 4x16 D=2000
   // centre bond the fused kernel takes 0.43 ms against 0.21 ms for the two
   // kernels, its producers being latency bound and recomputing a T3 tile for
@@ -167,7 +171,17 @@ struct SgMatvecPlan {
 // S the Krylov structure of psi; fm: the fused W1 W2 coefficients (shared
 // with the FP64 form's MPO step), which carry all the MPO tensors take part in.
 std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const BTensor &R,
-                                             const BTensor &S, FusedMpo &fm);
+                                             const BTensor &S, FusedMpo &fm, int bn1 = kTcBN,
+                                             int bn3 = kTcBN);
+
+// The plan with the B-tile rows of the context (ctx.tc_bn1 / tc_bn3), or, where
+// those are 0, the tile autotuner's: the first plan of a shape class (element
+// type, log2 of the Krylov structure's size, log2 of its largest right-bond
+// sector) is built with 64- and with 128-row B tiles, one matvec of each is
+// timed per stage (CUDA events, best of two), and each GEMM keeps its faster
+// tile; later plans of the class reuse the choice.
+std::unique_ptr<SgMatvecPlan> plan_sg_matvec_tuned(Ctx &ctx, const BTensor &L, const BTensor &R,
+                                                   const BTensor &S, FusedMpo &fm);
 
 void run_mpo_step(Ctx &ctx, const SgMatvecPlan &p);
 // T3 computed in the producers of the .R GEMM: res = (W1 W2 T1) R^T

@@ -90,15 +90,17 @@ __global__ void __launch_bounds__(256)
 // t = blockIdx.x + i * gridDim.x): warp 0 stages both operands by bulk copies
 // from their images, warp 1 issues the MMAs, warps 2-5 drain the
 // accumulators.
+template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_kernel(const TcTile *__restrict__ tiles, int ntiles, const TcGroup *__restrict__ groups,
                    const uint8_t *__restrict__ aimg, const uint8_t *__restrict__ bimg,
                    const int64_t *__restrict__ rowaddr, void *__restrict__ out, int out_kind,
                    double alpha, int *__restrict__ err) {
+  using S = TcShape<BN>;
   extern __shared__ __align__(1024) uint8_t smem[];
-  const TcBars b = tc_bars(smem);
+  const TcBars b = tc_bars<BN>(smem);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t tmem = tc_setup(b, 1, 0);
+  const uint32_t tmem = tc_setup<BN>(b, 1, 0);
   if (warp == 0) {
     if (lane == 0) {  // producer: one bulk copy per operand unit and chunk
       uint32_t G = 0;
@@ -106,28 +108,28 @@ __global__ void __launch_bounds__(kThreads, 1)
         const TcTile tile = tiles[t];
         const TcGroup g = groups[tile.group];
         const uint8_t *abase = aimg + g.a_img + (int64_t)tile.mtile * g.kc * kTcUnitA;
-        const uint8_t *bbase = bimg + g.b_img + (int64_t)tile.ntile * g.kc * kTcUnitB;
+        const uint8_t *bbase = bimg + g.b_img + (int64_t)tile.ntile * g.kc * S::kUnitB;
         for (int c = 0; c < g.kc; ++c, ++G) {
-          const uint32_t s = G % kStages;
-          if (G >= kStages && !wait_phase(&b.empty[s], ((G / kStages) - 1) & 1)) {
+          const uint32_t s = G % S::kStages;
+          if (G >= S::kStages && !wait_phase(&b.empty[s], ((G / S::kStages) - 1) & 1)) {
             tc_fail(b, err, 1);
             break;
           }
-          uint8_t *st = smem + s * kStageBytes;
-          tc::mbar_expect_tx(&b.full[s], (uint32_t)(kTcUnitA + kTcUnitB));
+          uint8_t *st = smem + s * S::kStageBytes;
+          tc::mbar_expect_tx(&b.full[s], (uint32_t)(kTcUnitA + S::kUnitB));
           tc::bulk_g2s(st, abase + (int64_t)c * kTcUnitA, (uint32_t)kTcUnitA, &b.full[s]);
-          tc::bulk_g2s(st + kTcUnitA, bbase + (int64_t)c * kTcUnitB, (uint32_t)kTcUnitB,
+          tc::bulk_g2s(st + kTcUnitA, bbase + (int64_t)c * S::kUnitB, (uint32_t)S::kUnitB,
                        &b.full[s]);
         }
       }
     }
   } else if (warp == 1) {
-    if (lane == 0) tc_mma_role(tiles, ntiles, groups, smem, b, tmem, err);
+    if (lane == 0) tc_mma_role<BN>(tiles, ntiles, groups, smem, b, tmem, err);
   } else {  // epilogue: warp w drains TMEM lanes 32 (w % 4) ...
-    tc_epilogue_role(warp & 3, lane, tiles, ntiles, groups, rowaddr, out, out_kind, alpha, b,
-                     tmem, err);
+    tc_epilogue_role<BN>(warp & 3, lane, tiles, ntiles, groups, rowaddr, out, out_kind, alpha,
+                         b, tmem, err);
   }
-  tc_teardown(tmem, 0);
+  tc_teardown<BN>(tmem, 0);
 }
 
 }  // namespace
@@ -157,7 +159,7 @@ void TcPlan::add_group(int64_t a_img, int64_t b_img, int32_t M, int32_t N, int32
   g.N = N;
   g.K = K;
   g.mt = (M + kTcBM - 1) / kTcBM;
-  g.nt = (N + kTcBN - 1) / kTcBN;
+  g.nt = (N + bn - 1) / bn;
   g.kc = (K + kTcBK - 1) / kTcBK;
   rowaddr.insert(rowaddr.end(), rows.begin(), rows.end());
   const int32_t gid = (int32_t)groups.size();
@@ -237,23 +239,32 @@ void run_pack(Ctx &ctx, const std::vector<PackOp> &ops, const void *src, bool sr
   ctx.sync();  // the lists are freed on return
 }
 
-void run_tc_gemm(Ctx &ctx, const TcPlan &plan, const uint8_t *a_img, const uint8_t *b_img,
-                 void *out, int out_kind, double alpha) {
+template <int BN>
+static void launch_tc_gemm(Ctx &ctx, const TcPlan &plan, const uint8_t *a_img,
+                           const uint8_t *b_img, void *out, int out_kind, double alpha) {
   const int ntiles = (int)plan.tiles.size();
-  if (ntiles == 0) return;
   static bool attr_set = false;
   if (!attr_set) {
-    UDMRG_CHECK_CUDA(cudaFuncSetAttribute(tc_gemm_kernel,
+    UDMRG_CHECK_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<BN>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          kSmemBytes));
+                                          TcShape<BN>::kSmemBytes));
     attr_set = true;
   }
   const int grid = std::min(ntiles, ctx.num_sms);
-  tc_gemm_kernel<<<grid, kThreads, kSmemBytes, ctx.stream>>>(
+  tc_gemm_kernel<BN><<<grid, kThreads, TcShape<BN>::kSmemBytes, ctx.stream>>>(
       plan.d_tiles, ntiles, plan.d_groups, a_img, b_img, plan.d_rowaddr, out, out_kind, alpha,
       plan.d_err);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches++;
+}
+
+void run_tc_gemm(Ctx &ctx, const TcPlan &plan, const uint8_t *a_img, const uint8_t *b_img,
+                 void *out, int out_kind, double alpha) {
+  if (plan.tiles.empty()) return;
+  if (plan.bn == 128)
+    launch_tc_gemm<128>(ctx, plan, a_img, b_img, out, out_kind, alpha);
+  else
+    launch_tc_gemm<64>(ctx, plan, a_img, b_img, out, out_kind, alpha);
 }
 
 int tc_check(Ctx &ctx, const TcPlan &plan) {

@@ -18,10 +18,9 @@
 namespace udmrg {
 
 constexpr int kTcBM = 128;  // rows of an A tile (UMMA M)
-constexpr int kTcBN = 64;   // rows of a B tile (UMMA N)
+constexpr int kTcBN = 64;   // default rows of a B tile (UMMA N); 64 or 128 per plan
 constexpr int kTcBK = 64;   // K per chunk (four K=16 MMA steps)
 constexpr int64_t kTcUnitA = 3LL * kTcBM * kTcBK * 2;  // 48 KB
-constexpr int64_t kTcUnitB = 3LL * kTcBN * kTcBK * 2;  // 24 KB
 
 // Pack one strided sub-matrix into an image (element type of the source:
 // FP64 or FP32).  Element (r, k) of the sub-matrix is
@@ -57,6 +56,7 @@ enum TcOut : int { kTcOutF32 = 0, kTcOutF64 = 1, kTcOutC128 = 2 };
 
 struct TcPlan {
   Ctx *ctx = nullptr;
+  int bn = kTcBN;  // rows of a B tile (64 or 128; the B images are packed with it)
   std::vector<TcGroup> groups;
   std::vector<TcTile> tiles;
   std::vector<int64_t> rowaddr;  // output element offset of each output row

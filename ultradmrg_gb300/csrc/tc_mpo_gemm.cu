@@ -32,6 +32,7 @@ struct ChunkWork {
   int c8;        // first b of the chunk
 };
 
+template <int BN>
 __global__ void __launch_bounds__(kFusedThreads, 1)
     tc_mpo_gemm_kernel(const TcTile *__restrict__ tiles, int ntiles,
                        const TcGroup *__restrict__ groups, const MpoGroupMap *__restrict__ gmap,
@@ -41,11 +42,12 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
                        const float *__restrict__ t1, const uint8_t *__restrict__ bimg,
                        const int64_t *__restrict__ rowaddr, void *__restrict__ out, int out_kind,
                        double alpha, int *__restrict__ err) {
+  using S = TcShape<BN>;
   extern __shared__ __align__(1024) uint8_t smem[];
-  const TcBars b = tc_bars(smem);
+  const TcBars b = tc_bars<BN>(smem);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // full barrier: every producer thread, plus the expect-tx arrival of thread 0
-  const uint32_t tmem = tc_setup(b, kProducers + 1, kMmaWarp);
+  const uint32_t tmem = tc_setup<BN>(b, kProducers + 1, kMmaWarp);
   if (tid < kProducers) {
     const int r = tid & (kTcBM - 1), h = tid >> 7;
     constexpr int64_t planeA = (int64_t)kTcBM * kTcBK * 2;
@@ -58,18 +60,18 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
       const int64_t grow = (int64_t)tile.mtile * kTcBM + r;
       const bool rv = grow < g.M;
       const MpoRowInfo ri = rv ? rowinfo[gm.row0 + grow] : MpoRowInfo{0, 0, 0, 0};
-      const uint8_t *bbase = bimg + g.b_img + (int64_t)tile.ntile * g.kc * kTcUnitB;
+      const uint8_t *bbase = bimg + g.b_img + (int64_t)tile.ntile * g.kc * S::kUnitB;
       for (int c = 0; c < g.kc; ++c, ++G) {
-        const uint32_t s = G % kStages;
-        if (G >= kStages && !wait_phase(&b.empty[s], ((G / kStages) - 1) & 1)) {
+        const uint32_t s = G % S::kStages;
+        if (G >= S::kStages && !wait_phase(&b.empty[s], ((G / S::kStages) - 1) & 1)) {
           tc_fail(b, err, 1);
           ok = false;
           break;
         }
-        uint8_t *st = smem + s * kStageBytes;
+        uint8_t *st = smem + s * S::kStageBytes;
         if (tid == 0) {
-          tc::mbar_expect_tx(&b.full[s], (uint32_t)kTcUnitB);
-          tc::bulk_g2s(st + kTcUnitA, bbase + (int64_t)c * kTcUnitB, (uint32_t)kTcUnitB,
+          tc::mbar_expect_tx(&b.full[s], (uint32_t)S::kUnitB);
+          tc::bulk_g2s(st + kTcUnitA, bbase + (int64_t)c * S::kUnitB, (uint32_t)S::kUnitB,
                        &b.full[s]);
         }
         // the four chunks' output channels, then their first nonzeros' loads
@@ -142,34 +144,42 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
       }
     }
   } else if (warp == kMmaWarp) {
-    if (lane == 0) tc_mma_role(tiles, ntiles, groups, smem, b, tmem, err);
+    if (lane == 0) tc_mma_role<BN>(tiles, ntiles, groups, smem, b, tmem, err);
   } else {  // epilogue: warps 9-12, TMEM lane quarters 1, 2, 3, 0
-    tc_epilogue_role(warp & 3, lane, tiles, ntiles, groups, rowaddr, out, out_kind, alpha, b,
-                     tmem, err);
+    tc_epilogue_role<BN>(warp & 3, lane, tiles, ntiles, groups, rowaddr, out, out_kind, alpha,
+                         b, tmem, err);
   }
-  tc_teardown(tmem, kMmaWarp);
+  tc_teardown<BN>(tmem, kMmaWarp);
 }
 
 }  // namespace
 
-void run_tc_mpo_gemm(Ctx &ctx, const SgMatvecPlan &p, double *out) {
+template <int BN>
+static void launch_tc_mpo_gemm(Ctx &ctx, const SgMatvecPlan &p, double *out) {
   const TcPlan &plan = p.g3;
   const int ntiles = (int)plan.tiles.size();
-  if (ntiles == 0) return;
   static bool attr_set = false;
   if (!attr_set) {
-    UDMRG_CHECK_CUDA(cudaFuncSetAttribute(tc_mpo_gemm_kernel,
+    UDMRG_CHECK_CUDA(cudaFuncSetAttribute(tc_mpo_gemm_kernel<BN>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          kSmemBytes));
+                                          TcShape<BN>::kSmemBytes));
     attr_set = true;
   }
   const int grid = std::min(ntiles, ctx.num_sms);
-  tc_mpo_gemm_kernel<<<grid, kFusedThreads, kSmemBytes, ctx.stream>>>(
+  tc_mpo_gemm_kernel<BN><<<grid, kFusedThreads, TcShape<BN>::kSmemBytes, ctx.stream>>>(
       plan.d_tiles, ntiles, plan.d_groups, p.d_gmap, p.d_rowinfo, p.d_kchunks, p.d_tgtref,
       p.d_rowptr, p.d_nz, p.t1, p.r_img, plan.d_rowaddr, out,
       p.cplx ? kTcOutC128 : kTcOutF64, 1.0, plan.d_err);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches++;
+}
+
+void run_tc_mpo_gemm(Ctx &ctx, const SgMatvecPlan &p, double *out) {
+  if (p.g3.tiles.empty()) return;
+  if (p.g3.bn == 128)
+    launch_tc_mpo_gemm<128>(ctx, p, out);
+  else
+    launch_tc_mpo_gemm<64>(ctx, p, out);
 }
 
 }  // namespace udmrg

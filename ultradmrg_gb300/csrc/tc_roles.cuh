@@ -15,17 +15,25 @@ namespace udmrg {
 
 namespace {
 
-constexpr int kStages = 3;
-constexpr int kAcc = 2;        // TMEM accumulators (epilogue of tile i overlaps tile i+1)
-constexpr int kStageBytes = (int)(kTcUnitA + kTcUnitB);  // 72 KB
+constexpr int kAcc = 2;  // TMEM accumulators (epilogue of tile i overlaps tile i+1)
 // Headroom after the stage buffers: no descriptor read can leave the
 // allocation even if a stride field were misread.
 constexpr int kPadBytes = 8 * 1024;
-constexpr int kBarOffset = kStages * kStageBytes + kPadBytes;
-constexpr int kSmemBytes = kBarOffset + 1024;
-static_assert(kSmemBytes <= 227 * 1024, "tcgen05 GEMM: shared memory budget");
-constexpr uint32_t kTmemCols = kAcc * kTcBN;  // FP32 accumulators: 2 x BN columns x 128 lanes
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s: a wait this long means a fault
+
+// Shared-memory and TMEM layout for B tiles of BN rows (UMMA N): stages of
+// one A unit (128 x 64, three planes) and one B unit (BN x 64, three planes).
+template <int BN>
+struct TcShape {
+  static_assert(BN == 64 || BN == 128, "tcgen05 GEMM: B tiles of 64 or 128 rows");
+  static constexpr int kStages = BN == 64 ? 3 : 2;
+  static constexpr int64_t kUnitB = 3LL * BN * kTcBK * 2;  // 24 KB / 48 KB
+  static constexpr int kStageBytes = (int)(kTcUnitA + kUnitB);  // 72 KB / 96 KB
+  static constexpr int kBarOffset = kStages * kStageBytes + kPadBytes;
+  static constexpr int kSmemBytes = kBarOffset + 1024;
+  static constexpr uint32_t kTmemCols = kAcc * BN;  // FP32: 2 x BN columns x 128 lanes
+  static_assert(kSmemBytes <= 227 * 1024, "tcgen05 GEMM: shared memory budget");
+};
 
 __device__ __forceinline__ uint64_t global_ns() {
   uint64_t t;
@@ -145,11 +153,13 @@ struct TcBars {
   volatile int *abort_flag;
 };
 
+template <int BN>
 __device__ __forceinline__ TcBars tc_bars(uint8_t *smem) {
+  using S = TcShape<BN>;
   TcBars b;
-  b.full = (uint64_t *)(smem + kBarOffset);
-  b.empty = b.full + kStages;
-  b.tfull = b.empty + kStages;
+  b.full = (uint64_t *)(smem + S::kBarOffset);
+  b.empty = b.full + S::kStages;
+  b.tfull = b.empty + S::kStages;
   b.tempty = b.tfull + kAcc;
   b.fin = b.tempty + kAcc;
   b.tmem_slot = (uint32_t *)(b.fin + 1);
@@ -160,11 +170,13 @@ __device__ __forceinline__ TcBars tc_bars(uint8_t *smem) {
 // Barrier initialisation (thread 0; a full barrier completes after
 // full_count arrivals and its transaction bytes), TMEM allocation (warp
 // alloc_warp) and the block-wide synchronisation; returns the TMEM base.
+template <int BN>
 __device__ __forceinline__ uint32_t tc_setup(const TcBars &b, uint32_t full_count,
                                              int alloc_warp) {
+  using S = TcShape<BN>;
   const int tid = threadIdx.x, warp = tid >> 5;
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < S::kStages; ++s) {
       tc::mbar_init(&b.full[s], full_count);
       tc::mbar_init(&b.empty[s], 1);
     }
@@ -177,7 +189,7 @@ __device__ __forceinline__ uint32_t tc_setup(const TcBars &b, uint32_t full_coun
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == alloc_warp) {
-    tc::tmem_alloc(b.tmem_slot, kTmemCols);
+    tc::tmem_alloc(b.tmem_slot, S::kTmemCols);
     tc::tmem_relinquish();
   }
   tc::fence_before_sync();
@@ -186,11 +198,12 @@ __device__ __forceinline__ uint32_t tc_setup(const TcBars &b, uint32_t full_coun
   return *b.tmem_slot;
 }
 
+template <int BN>
 __device__ __forceinline__ void tc_teardown(uint32_t tmem, int alloc_warp) {
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if ((int)(threadIdx.x >> 5) == alloc_warp) tc::tmem_dealloc(tmem, kTmemCols);
+  if ((int)(threadIdx.x >> 5) == alloc_warp) tc::tmem_dealloc(tmem, TcShape<BN>::kTmemCols);
 }
 
 __device__ __forceinline__ void tc_fail(const TcBars &b, int *err, int code) {
@@ -202,10 +215,12 @@ __device__ __forceinline__ void tc_fail(const TcBars &b, int *err, int code) {
 // t = blockIdx.x + i * gridDim.x): for each K chunk, wait for its stage,
 // issue the six split products per 16-deep K step, release the stage; after
 // the last chunk, hand the accumulator to the epilogue.
+template <int BN>
 __device__ __forceinline__ void tc_mma_role(const TcTile *__restrict__ tiles, int ntiles,
                                             const TcGroup *__restrict__ groups, uint8_t *smem,
                                             const TcBars &b, uint32_t tmem, int *err) {
-  constexpr uint32_t idesc = tc::idesc_bf16_f32(kTcBM, kTcBN);
+  using S = TcShape<BN>;
+  constexpr uint32_t idesc = tc::idesc_bf16_f32(kTcBM, BN);
   uint32_t G = 0, i = 0;
   for (int t = blockIdx.x; t < ntiles && !*b.abort_flag; t += gridDim.x, ++i) {
     const TcGroup g = groups[tiles[t].group];
@@ -215,18 +230,18 @@ __device__ __forceinline__ void tc_mma_role(const TcTile *__restrict__ tiles, in
       break;
     }
     tc::fence_after_sync();
-    const uint32_t dcol = tmem + acc * kTcBN;
+    const uint32_t dcol = tmem + acc * BN;
     bool ok = true;
     for (int c = 0; c < g.kc; ++c, ++G) {
-      const uint32_t s = G % kStages;
-      if (!wait_phase(&b.full[s], (G / kStages) & 1)) {
+      const uint32_t s = G % S::kStages;
+      if (!wait_phase(&b.full[s], (G / S::kStages) & 1)) {
         ok = false;
         break;
       }
       tc::fence_after_sync();
-      const uint32_t sa = tc::smem_u32(smem + s * kStageBytes);
+      const uint32_t sa = tc::smem_u32(smem + s * S::kStageBytes);
       const uint32_t sb = sa + (uint32_t)kTcUnitA;
-      constexpr uint32_t planeA = kTcBM * kTcBK * 2, planeB = kTcBN * kTcBK * 2;
+      constexpr uint32_t planeA = kTcBM * kTcBK * 2, planeB = BN * kTcBK * 2;
 #pragma unroll
       for (int ks = 0; ks < kTcBK / 16; ++ks) {
 #pragma unroll
@@ -235,7 +250,7 @@ __device__ __forceinline__ void tc_mma_role(const TcTile *__restrict__ tiles, in
           const uint64_t ad = tc::make_desc(
               sa + kProdA[p] * planeA + ks * 2 * (kTcBM / 8) * 128, (kTcBM / 8) * 128, 128);
           const uint64_t bd = tc::make_desc(
-              sb + kProdB[p] * planeB + ks * 2 * (kTcBN / 8) * 128, (kTcBN / 8) * 128, 128);
+              sb + kProdB[p] * planeB + ks * 2 * (BN / 8) * 128, (BN / 8) * 128, 128);
           tc::mma_bf16(dcol, ad, bd, idesc, (c > 0 || ks > 0 || p > 0) ? 1u : 0u);
         }
       }
@@ -253,6 +268,7 @@ __device__ __forceinline__ void tc_mma_role(const TcTile *__restrict__ tiles, in
 
 // Epilogue: warp q (0..3, the TMEM lane quarter it may access) drains
 // accumulator rows 32 q .. 32 q + 31 of every tile, one row per lane.
+template <int BN>
 __device__ __forceinline__ void tc_epilogue_role(int q, int lane,
                                                  const TcTile *__restrict__ tiles, int ntiles,
                                                  const TcGroup *__restrict__ groups,
@@ -274,13 +290,13 @@ __device__ __forceinline__ void tc_epilogue_role(int q, int lane,
       const int64_t grow = (int64_t)tile.mtile * kTcBM + m;
       const bool row_ok = grow < g.M;
       const int64_t base = row_ok ? rowaddr[g.row0 + grow] : 0;
-      const int n0 = tile.ntile * kTcBN;
+      const int n0 = tile.ntile * BN;
       // epilogue math in FP32 (the accumulator's precision); no FP64 instruction
       const float af = (float)alpha;
 #pragma unroll
-      for (int cb = 0; cb < kTcBN / 16; ++cb) {
+      for (int cb = 0; cb < BN / 16; ++cb) {
         uint32_t r[16];
-        tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + acc * kTcBN + cb * 16, r);
+        tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + acc * BN + cb * 16, r);
         tc::tmem_wait_ld();
         if (row_ok) {
           // 16-byte stores where the row position allows (four FP32 or two
