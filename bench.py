@@ -484,6 +484,37 @@ def run_ours(args):
         for t in (na, nb, ne):
             t.close()
 
+    # exact truncated SVD against the randomized one with a tight sketch (each
+    # sector sized to the exact SVD's kept count, the best a rank predictor can
+    # do) on the centre ground state, truncated to D and to D/4
+    svd_cmp = {}
+    g = api.lanczos_solver(ctx, ops, psi, 1e-9, 100, precision=api.PREC_MIXED).gs_vec
+    g.scale_(1.0 / g.norm())
+    ldiv = tuple(mps[l].div())
+    for dmax in (w.D, w.D // 4):
+        best = {}
+        for rep in range(2):
+            ctx.sync()
+            t0 = time.perf_counter()
+            u, sv, vt, err, dk = api.svd(ctx, g, 2, ldiv, 1e-8, dmax, dmax, api.SVD_SPLIT_LEFT)
+            ctx.sync()
+            best["exact_sec"] = min(best.get("exact_sec", 1e9), time.perf_counter() - t0)
+            bond = u.to_data().indexes[2]
+            sketch = [(q, d) for q, d in zip(bond.qns, bond.dims)]
+            for t in (u, sv, vt):
+                t.close()
+            ctx.sync()
+            t0 = time.perf_counter()
+            r = api.svd_randomized(ctx, g, 2, ldiv, 1e-8, dmax, dmax, sketch, api.SVD_SPLIT_LEFT)
+            ctx.sync()
+            best["sketch_sec"] = min(best.get("sketch_sec", 1e9), time.perf_counter() - t0)
+            best.update(D=dk, trunc_err_exact=err, trunc_err_sketch=r[3], regrow_rounds=r[5])
+            for t in r[:3]:
+                t.close()
+        best["exact_over_sketch"] = best["exact_sec"] / best["sketch_sec"]
+        svd_cmp[f"Dmax={dmax}"] = best
+    g.close()
+
     sweep = None
     if not args.no_sweep:
         for t in (A1d, A2d):
@@ -584,6 +615,7 @@ def run_ours(args):
         "centre_site_update_speedup": {
             k: site["fp64_exact"]["wall_sec"] / site[k]["wall_sec"]
             for k in ("mixed_exact", "mixed_rsvd")},
+        "svd_exact_vs_tight_sketch": svd_cmp,
         "centre_site_update_rel_dE": {
             k: abs(site[k]["e0"] - site["fp64_exact"]["e0"]) / abs(site["fp64_exact"]["e0"])
             for k in ("mixed_exact", "mixed_rsvd")},
