@@ -34,8 +34,13 @@ def up(ctx, t):
 
 
 def both_modes(ctx, fn):
-    """fn() with direct launches, then with graph replays: [(result, launches)]."""
+    """fn() with direct launches, then with graph replays: [(result, launches)].
+    One untimed call first fills the context's per-shape caches (the tile
+    autotuner's timed trials run once per shape class), so both counted calls
+    launch the same work."""
     out = []
+    fn()
+    ctx.sync()
     try:
         for graph in (False, True):
             ctx.set_krylov_graph(graph)

@@ -462,48 +462,74 @@ __global__ void invit_kernel(const EigCluster *__restrict__ cl, int ncl,
   }
 }
 
-// Z (row-major n x k, leading dimension ld, at z_off) <- Q Z with
-// Q = H_0 H_1 ... H_{n-3}, H_j = I - tau_j v_j v_j^T acting on rows j+1 ...
-// Block b transforms columns c0 .. c0 + 31 of job bt[b].job (columns are
-// independent), threads as 32 columns x 8 row groups.
+// Back transformation: Z (row-major n x k, leading dimension ld, at z_off)
+// <- Q Z with Q = H_0 H_1 ... H_{n-3}, H_j = I - tau_j v_j v_j^T acting on
+// rows j+1 ...  Block b transforms columns c0 .. c0 + cw - 1 of job
+// bt[b].job (columns are independent).
 struct BackChunk {
   int64_t z_off, ld;
   int32_t job, c0, cw, pad;
 };
-__global__ void backtransform_kernel(const EigJob *__restrict__ jobs,
-                                     const BackChunk *__restrict__ bt,
-                                     const double *__restrict__ G_all,
-                                     const double *__restrict__ tau_all, double *__restrict__ Z) {
-  extern __shared__ double sm[];
-  __shared__ double part[8][33];
+// Real data: narrow column chunks (W = 8
+// columns per block, 4 for matrices above 3,400 rows), so that the largest
+// sector's columns spread over many SMs: this GPU issues about two FP64 FMAs
+// per clock per SM, and one sector's 4 n^2 k flops on one SM would bound the
+// whole kernel.  The chunk lives in shared memory (n x W doubles) for all
+// reflectors; thread t owns column t % W and the rows congruent to t / W
+// modulo kBackThreads / W.  Per reflector: partial dot products, a reduction
+// over the row groups (shuffles inside a warp, one shared-memory stage across
+// warps), the rank-1 update; two block barriers.
+template <int W>
+__global__ void __launch_bounds__(kBackThreads)
+    backtransform_narrow_kernel(const EigJob *__restrict__ jobs,
+                                const BackChunk *__restrict__ bt,
+                                const double *__restrict__ G_all,
+                                const double *__restrict__ tau_all, double *__restrict__ Z) {
+  constexpr int RG = kBackThreads / W;  // row groups
+  static_assert(RG * W == kBackThreads && W <= 32 && (32 % W) == 0, "back transformation layout");
+  extern __shared__ double zs[];  // n x W
+  __shared__ double part[kBackThreads / 32][W];
   const BackChunk ch = bt[blockIdx.x];
   const EigJob job = jobs[ch.job];
   const int n = job.n;
   if (n < 3 || ch.cw == 0) return;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // blockDim.x == 256
+  const int c = threadIdx.x % W, g = threadIdx.x / W;
+  const int warp = threadIdx.x >> 5;
   double *z = Z + ch.z_off + ch.c0;
-  double *v = sm;  // n
+  const bool col = c < ch.cw;
+  for (int r = g; r < n; r += RG) zs[r * W + c] = col ? z[(int64_t)r * ch.ld + c] : 0.0;
+  __syncthreads();
   const double *A = G_all + job.g_off;
-  const bool col = tx < ch.cw;
   for (int j = n - 3; j >= 0; --j) {
     const double t = tau_all[job.lam_off + j];
     if (t == 0.0) continue;  // uniform across the block
     const int m = n - j - 1;
-    for (int r = threadIdx.x; r < m; r += blockDim.x)
-      v[r] = r == 0 ? 1.0 : A[(int64_t)j * n + j + 1 + r];
-    __syncthreads();
-    double s = 0.0;
-    if (col)
-      for (int r = ty; r < m; r += 8) s += v[r] * z[(int64_t)(j + 1 + r) * ch.ld + tx];
-    part[ty][tx] = s;
+    const double *vrow = A + (int64_t)j * n + j + 1;  // v[r] for r >= 1; v[0] = 1
+    double *zj = zs + (j + 1) * W + c;
+    double s0 = 0.0, s1 = 0.0;
+    int r = g;
+    for (; r + RG < m; r += 2 * RG) {
+      const double v0 = r == 0 ? 1.0 : __ldg(vrow + r);
+      const double v1 = __ldg(vrow + r + RG);
+      s0 = fma(v0, zj[r * W], s0);
+      s1 = fma(v1, zj[(r + RG) * W], s1);
+    }
+    if (r < m) s0 = fma(r == 0 ? 1.0 : __ldg(vrow + r), zj[r * W], s0);
+    double sum = s0 + s1;
+    // the row groups of this warp, then the warps
+#pragma unroll
+    for (int o = W; o < 32; o <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) < W) part[warp][c] = sum;
     __syncthreads();
     double w = 0.0;
-    for (int g = 0; g < 8; ++g) w += part[g][tx];
+#pragma unroll
+    for (int q = 0; q < kBackThreads / 32; ++q) w += part[q][c];
     w *= t;
-    if (col)
-      for (int r = ty; r < m; r += 8) z[(int64_t)(j + 1 + r) * ch.ld + tx] -= v[r] * w;
+    for (int r2 = g; r2 < m; r2 += RG) zj[r2 * W] -= (r2 == 0 ? 1.0 : __ldg(vrow + r2)) * w;
     __syncthreads();
   }
+  if (col)
+    for (int r = g; r < n; r += RG) z[(int64_t)r * ch.ld + c] = zs[r * W + c];
 }
 
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
@@ -1077,7 +1103,8 @@ void tridiag_multi_cta(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJo
 }
 
 int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, double *G,
-                   double *lam, SymEigWork &wk, bool cplx, int64_t need, int64_t floor) {
+                   double *lam, SymEigWork &wk, bool cplx, int64_t need, int64_t floor,
+                   const std::vector<int64_t> *rank_cap) {
   const int nj = (int)jobs.size();
   if (nj == 0) return 0;
   int64_t ltot = 0;
@@ -1157,14 +1184,18 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
     int ks = -1;
     for (int k = 0; k <= kGrid; ++k) {
       int64_t t = 0;
-      for (int q = 0; q < nj; ++q) t += cnt[(size_t)q * (kGrid + 1) + k];
+      for (int q = 0; q < nj; ++q) {
+        const int64_t c = cnt[(size_t)q * (kGrid + 1) + k];
+        t += rank_cap ? std::min<int64_t>(c, (*rank_cap)[q]) : c;
+      }
       if (t >= need) {
         ks = k;
         break;
       }
     }
-    // fewer than `need` eigenvalues above the lowest grid point (a rank-deficient
-    // set, and a Dmin asking for its null states too): every eigenvalue
+    // fewer than `need` usable eigenvalues above the lowest grid point (a
+    // rank-deficient set, and a Dmin asking for its null states too): every
+    // eigenvalue
     if (ks >= 0) {
       ks = std::min(ks + 1, kGrid);
       for (int q = 0; q < nj; ++q) {
@@ -1293,20 +1324,28 @@ void sym_eig_vectors(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJob>
                              z_ld_out[q], 1});
     run_copy2d(ctx, ops, Zc, Zout, true);
   }
-  // back-transformation by the reflectors, 32 columns per block
+  // back-transformation by the reflectors: complex data 32 columns per block,
+  // real data kBackCols columns per block (the chunk in shared memory)
   {
+    const int narrow = nmax * 8 * (int)sizeof(double) <= 218 * 1024 ? 8 : 4;
+    const int width = wk.cplx ? 32 : narrow;
     std::vector<BackChunk> bt;
     for (int q = 0; q < nj; ++q)
-      for (int64_t c0 = 0; c0 < k[q]; c0 += 32)
+      for (int64_t c0 = 0; c0 < k[q]; c0 += width)
         bt.push_back(BackChunk{z_off_out[q], z_ld_out[q], q, (int32_t)c0,
-                               (int32_t)std::min<int64_t>(32, k[q] - c0), 0});
+                               (int32_t)std::min<int64_t>(width, k[q] - c0), 0});
     if (!bt.empty()) {
       BackChunk *dbt = scratch.get<BackChunk>(bt.size());
       UDMRG_CHECK_CUDA(cudaMemcpyAsync(dbt, bt.data(), bt.size() * sizeof(BackChunk),
                                        cudaMemcpyHostToDevice, ctx.stream));
-      const size_t smem = (size_t)nmax * (wk.cplx ? 2 : 1) * sizeof(double);
+      const size_t smem = wk.cplx ? (size_t)nmax * 2 * sizeof(double)
+                                  : (size_t)nmax * narrow * sizeof(double);
+      UDMRG_REQUIRE(smem <= 227 * 1024, "back transformation: matrix too large");
       if (smem > 48 * 1024) {
-        UDMRG_CHECK_CUDA(cudaFuncSetAttribute(backtransform_kernel,
+        UDMRG_CHECK_CUDA(cudaFuncSetAttribute(backtransform_narrow_kernel<8>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem));
+        UDMRG_CHECK_CUDA(cudaFuncSetAttribute(backtransform_narrow_kernel<4>,
                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)smem));
         UDMRG_CHECK_CUDA(cudaFuncSetAttribute(backtransform_c_kernel,
@@ -1316,8 +1355,11 @@ void sym_eig_vectors(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJob>
       if (wk.cplx)
         backtransform_c_kernel<<<(int)bt.size(), kBackThreads, smem, ctx.stream>>>(
             wk.jobs, dbt, (const double2 *)G, (const double2 *)wk.tau, (double2 *)Zout);
+      else if (narrow == 8)
+        backtransform_narrow_kernel<8><<<(int)bt.size(), kBackThreads, smem, ctx.stream>>>(
+            wk.jobs, dbt, G, wk.tau, Zout);
       else
-        backtransform_kernel<<<(int)bt.size(), kBackThreads, smem, ctx.stream>>>(
+        backtransform_narrow_kernel<4><<<(int)bt.size(), kBackThreads, smem, ctx.stream>>>(
             wk.jobs, dbt, G, wk.tau, Zout);
       UDMRG_CHECK_CUDA(cudaGetLastError());
       ctx.launches++;

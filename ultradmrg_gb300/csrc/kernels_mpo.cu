@@ -7,10 +7,13 @@
 // planes and writes each plane with one 16-byte store into the step-3 tile
 // image.  A warp takes 32 consecutive units of one pair, so the CSR walk over
 // the pair's nonzeros is warp-uniform (broadcast metadata loads, no
-// divergence).  Nonzeros are processed four at a time: their eight loads are
-// in flight together.  Padded b columns (up to a multiple of 8) read and
+// divergence).  The pair's nonzero records, channel ends and image targets
+// are loaded 32 at a time, one per lane, and shuffled out; nonzeros are
+// processed four at a time with their eight loads in flight.  Padded b columns (up to a multiple of 8) read and
 // write zeros.  HBM bound: T1 read once (FP32), T3 written once (3 x BF16).
 #include <cuda_bf16.h>
+
+#include <climits>
 
 #include "mpo_step.hpp"
 #include "sg_matvec.hpp"
@@ -25,8 +28,10 @@ __device__ __forceinline__ int canon(int r, int k, int tr) {
 }
 
 constexpr int kMpoWarps = 8;
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kNzBatch = 4;  // nonzeros whose loads are in flight together
 
-__global__ void __launch_bounds__(32 * kMpoWarps)
+__global__ void __launch_bounds__(32 * kMpoWarps, 2)
     mpo_chunk_kernel(const MpoTask *__restrict__ tasks, int ntasks,
                      const MpoPair *__restrict__ pairs, const MpoOut *__restrict__ outs,
                      const int32_t *__restrict__ rowptr, const MpoNzRec *__restrict__ nzr,
@@ -41,18 +46,30 @@ __global__ void __launch_bounds__(32 * kMpoWarps)
     const bool valid = u < pr.da * nch;
     const int a = valid ? u / nch : 0;
     const int c8 = valid ? (u - a * nch) * 8 : 0;
-    const int kend = __ldg(rowptr + pr.row0 + pr.nout);
+    const int kbeg = __ldg(rowptr + pr.row0), kend = __ldg(rowptr + pr.row0 + pr.nout);
+    // Output channels [ob, ob + 32): lane l holds channel ob + l's end in the
+    // nonzero list and its image target (loaded together, read by shuffles).
+    int ob = 0;
+    const bool has = lane < pr.nout;
+    int endv = has ? __ldg(rowptr + pr.row0 + 1 + lane) : INT_MAX;
+    MpoOut outv = has ? outs[pr.out0 + lane] : MpoOut{0, 0, 0, 0, 0};
     int o = 0;
-    int next = __ldg(rowptr + pr.row0 + 1);  // end of output channel o's nonzeros
+    int next = __shfl_sync(kFull, endv, 0);  // end of output channel o's nonzeros
     float acc[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[j] = 0.f;
-    auto store = [&](int oc) {
-      const MpoOut ot = outs[pr.out0 + oc];
+    // write channel o's sums, then move to channel o + 1 (warp-uniform)
+    auto finish = [&]() {
+      const int sl = o - ob;
+      const long long off0 = __shfl_sync(kFull, (long long)outv.img_off, sl);
+      const int row0 = __shfl_sync(kFull, outv.row0, sl);
+      const int rstride = __shfl_sync(kFull, outv.rstride, sl);
+      const int col0 = __shfl_sync(kFull, outv.col0, sl);
+      const int kc = __shfl_sync(kFull, outv.kc, sl);
       if (valid) {
-        const int row = ot.row0 + a * ot.rstride;
-        const int col = ot.col0 + c8;
-        const int64_t off = ot.img_off + ((int64_t)(row >> 7) * ot.kc + (col >> 6)) * 3 * plane +
+        const int row = row0 + a * rstride;
+        const int col = col0 + c8;
+        const int64_t off = off0 + ((int64_t)(row >> 7) * kc + (col >> 6)) * 3 * plane +
                             canon(row & 127, col & 63, kTcBM);
         uint4 h, m, l;
         split8(acc, h, m, l);
@@ -62,43 +79,52 @@ __global__ void __launch_bounds__(32 * kMpoWarps)
       }
 #pragma unroll
       for (int j = 0; j < 8; ++j) acc[j] = 0.f;
+      if (++o - ob == 32) {
+        ob += 32;
+        const bool h2 = ob + lane < pr.nout;
+        endv = h2 ? __ldg(rowptr + pr.row0 + 1 + ob + lane) : INT_MAX;
+        outv = h2 ? outs[pr.out0 + ob + lane] : MpoOut{0, 0, 0, 0, 0};
+      }
+      next = __shfl_sync(kFull, endv, o - ob);
     };
-    for (int kb = __ldg(rowptr + pr.row0); kb < kend; kb += 4) {
-      float4 x[4][2];
-      float v[4];
+    // Nonzeros 32 at a time, one record per lane (shuffled out), eight
+    // nonzeros' sixteen 16-byte loads in flight together.
+    for (int kb = kbeg; kb < kend; kb += 32) {
+      const int nb = min(32, kend - kb);
+      MpoNzRec mine{0, 0, 0.f};
+      if (lane < nb) mine = nzr[kb + lane];
+      for (int q0 = 0; q0 < nb; q0 += kNzBatch) {
+        float4 x[kNzBatch][2];
+        float v[kNzBatch];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        x[q][0] = x[q][1] = make_float4(0.f, 0.f, 0.f, 0.f);
-        v[q] = 0.f;
-        if (kb + q < kend) {
-          const MpoNzRec e = nzr[kb + q];
-          v[q] = e.v;
-          if (valid) {
-            const float4 *src = (const float4 *)(t1 + e.base + (int64_t)a * e.astride + c8);
+        for (int q = 0; q < kNzBatch; ++q) {
+          const int sl = q0 + q;
+          const long long base = __shfl_sync(kFull, (long long)mine.base, sl);
+          const int astride = __shfl_sync(kFull, mine.astride, sl);
+          v[q] = __shfl_sync(kFull, mine.v, sl);
+          x[q][0] = x[q][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (sl < nb && valid) {
+            const float4 *src = (const float4 *)(t1 + base + (int64_t)a * astride + c8);
             x[q][0] = __ldg(src);
             x[q][1] = __ldg(src + 1);
           }
         }
-      }
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        if (kb + q >= kend) break;
-        while (kb + q >= next) {  // output channel o is complete (warp-uniform)
-          store(o);
-          ++o;
-          next = __ldg(rowptr + pr.row0 + o + 1);
+        for (int q = 0; q < kNzBatch; ++q) {
+          if (q0 + q >= nb) break;
+          while (kb + q0 + q >= next) finish();  // output channel o is complete
+          acc[0] = fmaf(v[q], x[q][0].x, acc[0]);
+          acc[1] = fmaf(v[q], x[q][0].y, acc[1]);
+          acc[2] = fmaf(v[q], x[q][0].z, acc[2]);
+          acc[3] = fmaf(v[q], x[q][0].w, acc[3]);
+          acc[4] = fmaf(v[q], x[q][1].x, acc[4]);
+          acc[5] = fmaf(v[q], x[q][1].y, acc[5]);
+          acc[6] = fmaf(v[q], x[q][1].z, acc[6]);
+          acc[7] = fmaf(v[q], x[q][1].w, acc[7]);
         }
-        acc[0] = fmaf(v[q], x[q][0].x, acc[0]);
-        acc[1] = fmaf(v[q], x[q][0].y, acc[1]);
-        acc[2] = fmaf(v[q], x[q][0].z, acc[2]);
-        acc[3] = fmaf(v[q], x[q][0].w, acc[3]);
-        acc[4] = fmaf(v[q], x[q][1].x, acc[4]);
-        acc[5] = fmaf(v[q], x[q][1].y, acc[5]);
-        acc[6] = fmaf(v[q], x[q][1].z, acc[6]);
-        acc[7] = fmaf(v[q], x[q][1].w, acc[7]);
       }
     }
-    for (; o < pr.nout; ++o) store(o);  // the last channel and channels without nonzeros
+    while (o < pr.nout) finish();  // the last channel and channels without nonzeros
   }
 }
 

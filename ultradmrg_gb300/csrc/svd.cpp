@@ -426,9 +426,11 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
   // (a margin of 64 below the Dmax-th largest) are computed; the weight of
   // the rest is each Gram matrix's trace minus the computed ones
   SymEigWork wk;
+  std::vector<int64_t> rank_cap(nsec);
+  for (int q = 0; q < nsec; ++q) rank_cap[q] = std::min(secs[q].rows, secs[q].cols);
   check_eig_status(sym_eig_values(ctx, scratch, jobs, G, lam, wk, cplx,
                                   Dmax > 0 ? std::max(Dmax, Dmin) + 64 : 0,
-                                  spectrum_floor));
+                                  spectrum_floor, &rank_cap));
   const std::vector<double> hlam = download_vec(ctx, lam, ltot);
   std::vector<std::vector<double>> sv(nsec);
   double rest = 0.0;

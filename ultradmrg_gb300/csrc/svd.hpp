@@ -61,10 +61,12 @@ void run_scale(Ctx &ctx, const std::vector<ScaleJob> &jobs, double *X, const dou
 // leading eigenvalues of every job down to a common threshold below which
 // fewer than `need` eigenvalues of all jobs together lie above, at least
 // min(n, floor) per job, are computed (wk.computed); wk.trace holds each job's
-// trace, so the weight of the rest is known exactly.
+// trace, so the weight of the rest is known exactly.  rank_cap (optional, one
+// per job): the caller uses at most that many of the job's eigenvalues (a Gram
+// matrix of rank min(rows, cols)), so no more of them count towards `need`.
 int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, double *G,
                    double *lam, SymEigWork &wk, bool cplx = false, int64_t need = 0,
-                   int64_t floor = 0);
+                   int64_t floor = 0, const std::vector<int64_t> *rank_cap = nullptr);
 // Phase 2: the leading k[q] eigenvectors of job q (hlam: host copy of lam) as
 // the columns of Z (row-major n x k[q], leading dimension z_ld[q], at z_off[q]),
 // orthonormal to FP64 accuracy.

@@ -132,6 +132,43 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc_teardown<BN>(tmem, 0);
 }
 
+// The same images for sources whose rows are (nearly) contiguous (psi: b
+// runs), when every op starts at a K column that is a multiple of 8: no
+// shared memory.  Warp w of a 32 x 64 work item takes the item's 8-wide
+// column group w, lane l its row l: each of the eight loads is coalesced
+// across the warp (consecutive rows), and the three 16-byte plane stores of
+// 32 consecutive rows fill 512 contiguous bytes of the canonical layout.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    pack_rows_kernel(const PackOp *__restrict__ ops, const PackTile *__restrict__ tiles,
+                     int ntiles, const T *__restrict__ src, uint8_t *__restrict__ img) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int w = blockIdx.x; w < ntiles; w += gridDim.x) {
+    const PackTile pt = tiles[w];
+    const PackOp op = ops[pt.op];
+    const int rs = pt.r0 + lane, ks = pt.k0 + warp * 8;
+    if (rs >= op.rows || ks >= op.cols) continue;
+    float x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float v = 0.f;
+      if (ks + j < op.cols)
+        v = to_f32(src[op.src_off + (int64_t)rs * op.src_rs + (int64_t)(ks + j) * op.src_cs]);
+      x[j] = op.neg ? -v : v;
+    }
+    uint4 hi, mi, lo;
+    split8(x, hi, mi, lo);
+    const int64_t plane = (int64_t)op.tr * kTcBK * 2;
+    const int ts = op.tr == 128 ? 7 : 6;
+    const int rr = op.r0 + rs, kk = op.k0 + ks;
+    const int64_t off = op.img_off + ((int64_t)(rr >> ts) * op.kc + (kk >> 6)) * 3 * plane +
+                        canon_off(rr & (op.tr - 1), kk & 63, op.tr);
+    *(uint4 *)(img + off) = hi;
+    *(uint4 *)(img + off + plane) = mi;
+    *(uint4 *)(img + off + 2 * plane) = lo;
+  }
+}
+
 }  // namespace
 
 int64_t tc_image_bytes(int64_t rows, int64_t K, int tr) {
@@ -207,15 +244,20 @@ PackList::~PackList() {
 void PackList::upload(Ctx &c) {
   ctx = &c;
   tiles = pack_tiles(ops);
+  rows_src = !ops.empty();
+  for (const PackOp &op : ops) rows_src = rows_src && op.src_rs <= 2 && op.k0 % 8 == 0;
   d_ops = udmrg::upload(ctx, ops);
   d_tiles = udmrg::upload(ctx, tiles);
 }
 
 static void launch_pack(Ctx &ctx, const PackOp *d_ops, const PackTile *d_tiles, int ntiles,
-                        const void *src, bool src_f64, uint8_t *img) {
+                        const void *src, bool src_f64, uint8_t *img, bool rows_src = false) {
   if (ntiles == 0) return;
   const int grid = std::min(ntiles, 16 * ctx.num_sms);
-  if (src_f64)
+  if (rows_src && src_f64)
+    pack_rows_kernel<double><<<grid, 256, 0, ctx.stream>>>(d_ops, d_tiles, ntiles,
+                                                           (const double *)src, img);
+  else if (src_f64)
     pack_kernel<double><<<grid, 256, 0, ctx.stream>>>(d_ops, d_tiles, ntiles, (const double *)src,
                                                       img);
   else
@@ -226,7 +268,7 @@ static void launch_pack(Ctx &ctx, const PackOp *d_ops, const PackTile *d_tiles, 
 }
 
 void run_pack(Ctx &ctx, const PackList &pl, const void *src, bool src_f64, uint8_t *img) {
-  launch_pack(ctx, pl.d_ops, pl.d_tiles, (int)pl.tiles.size(), src, src_f64, img);
+  launch_pack(ctx, pl.d_ops, pl.d_tiles, (int)pl.tiles.size(), src, src_f64, img, pl.rows_src);
 }
 
 void run_pack(Ctx &ctx, const std::vector<PackOp> &ops, const void *src, bool src_f64,

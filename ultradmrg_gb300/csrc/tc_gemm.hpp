@@ -89,6 +89,7 @@ struct PackList {
   std::vector<PackTile> tiles;
   PackOp *d_ops = nullptr;
   PackTile *d_tiles = nullptr;
+  bool rows_src = false;  // every op reads rows with stride <= 2 from a K column % 8 == 0
   PackList() = default;
   PackList(const PackList &) = delete;
   PackList &operator=(const PackList &) = delete;
