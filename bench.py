@@ -236,6 +236,7 @@ def sweep_leg(api, ctx, local, schedule):
             "lanczos_s": sum(r["lancz_sec"] for r in log),
             "svd_s": sum(r["svd_sec"] for r in log),
             "env_s": sum(r["env_sec"] for r in log),
+            "plan_s": sum(r["plan_sec"] for r in log),
             "lanczos_iters": int(sum(r["iters"] for r in log)),
             "updates": len(log), "max_trunc_err": max(r["trunc_err"] for r in log),
             "svd_grow_rounds": int(sum(r["svd_grow_rounds"] for r in log)),
@@ -421,8 +422,14 @@ def run_ours(args):
     t64 = timed(lambda: plan64.apply_ptr(xp, y64p), max(2, min(args.steps, 5)), 200)
     ym, yd = y.download_packed(), y64.download_packed()
     mixed_err = float(np.linalg.norm(ym - yd) / max(np.linalg.norm(yd), 1e-300))
-    # per-stage device times (dominant kernel roofline)
-    ms_mx, fl_mx = plan.stage_times(xp, yp)
+    # per-stage device times (dominant kernel roofline): the median of five
+    # matvecs, each after an L2 flush like the timed steps
+    samples = []
+    for _ in range(5):
+        ctx.flush_l2()
+        ms_s, fl_mx = plan.stage_times(xp, yp)
+        samples.append(ms_s)
+    ms_mx = [float(np.median([s_[i] for s_ in samples])) for i in range(4)]
     ms_64, fl_64 = plan64.stage_times(xp, y64p)
     # the tile autotuner's choice against the fixed tile shapes (one matvec per
     # stage, best of three; the plan of each shape built here)

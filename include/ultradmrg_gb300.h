@@ -95,6 +95,7 @@ typedef struct {
    * and the number of kept states that differ from the exact SVD's */
   double svd_audit_err;
   int64_t svd_audit_kept_diff;
+  double plan_sec; /* host seconds building the matvec plan (part of lancz_sec) */
 } udmrg_site_log;
 
 const char *udmrg_last_error(void);
@@ -121,6 +122,11 @@ int udmrg_ctx_set_krylov_graph(udmrg_ctx *ctx, int enable);
  * kernels). */
 int udmrg_ctx_set_tc_tiles(udmrg_ctx *ctx, int bn1, int bn3);
 int udmrg_ctx_tc_tuning(udmrg_ctx *ctx, int64_t *trials, int64_t *classes);
+/* Profiler range: waits for ctx's stream, then starts (start != 0) or stops
+ * the CUDA profiler's collection (cudaProfilerStart / cudaProfilerStop), so
+ * a profiler run with collection off at start records only the bracketed
+ * work.  No counterpart in the reference (measurement). */
+int udmrg_ctx_profiler_range(udmrg_ctx *ctx, int start);
 
 /* ---- tensors (QLTensor storage model) -------------------------------- */
 /* nsec[rank]: sectors per index; qns[sum(nsec)*nq]; dims[sum(nsec)];

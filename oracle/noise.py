@@ -325,11 +325,17 @@ def energy_expectation(mps, lenvs, renvs, mpo, l, r):
     return float(np.real(bs.inner(psi, eff_ham_mul_two_site_state(eff, psi))))
 
 
-def noise_sweep(mps, mpo, p, lenvs, renvs, left, right, noise, log=None, noises_used=None):
+def noise_sweep(mps, mpo, p, lenvs, renvs, left, right, noise, log=None, noises_used=None,
+                margins=None):
+    """``margins`` (optional list) receives, per update, the energy expectation
+    minus the previous update's energy, relative to the latter: the quantity
+    whose sign and size decide the noise adaptation."""
     e0 = 0.0
     last = 0.0
 
     def adapt(actual, noise):
+        if margins is not None:
+            margins.append((actual - e0) / abs(e0) if e0 != 0.0 else np.inf)
         if actual - e0 <= 0.0:
             return noise
         if actual - e0 >= p.alpha * abs(last - e0):
@@ -353,7 +359,8 @@ def noise_sweep(mps, mpo, p, lenvs, renvs, left, right, noise, log=None, noises_
     return e0, noise
 
 
-def two_site_finite_vmps_with_noise(mps, mpo, p: NoiseSweepParams, log=None, noises_used=None):
+def two_site_finite_vmps_with_noise(mps, mpo, p: NoiseSweepParams, log=None, noises_used=None,
+                                    margins=None):
     """Returns the last update's energy; ``mps`` (centre at site 0 on entry) is
     updated in place."""
     from .vmps import FiniteVMPSSweepParams, two_site_finite_vmps
@@ -375,5 +382,5 @@ def two_site_finite_vmps_with_noise(mps, mpo, p: NoiseSweepParams, log=None, noi
         if s < len(p.noises):
             noise = p.noises[s]
         e0, noise = noise_sweep(mps, mpo, p, lenvs, renvs, left, right, noise, log,
-                                noises_used)
+                                noises_used, margins)
     return e0

@@ -94,6 +94,10 @@ class SiteLog:
     D: int
     iters: int
     ee: float
+    # smallest kept singular value over the largest (test bookkeeping: where
+    # Dmin keeps states far below the largest, which ones are kept is decided
+    # by rounding-level differences)
+    s_min_kept: float = float("nan")
 
 
 def two_site_update(mps, lenvs, renvs, mpo, params: FiniteVMPSSweepParams, dir, target,
@@ -124,7 +128,9 @@ def two_site_update(mps, lenvs, renvs, mpo, params: FiniteVMPSSweepParams, dir, 
         mps[r] = vt
         renvs[renv_len + 1] = update_site_renvs(renvs[renv_len], mps[target], mpo[target])
     if log is not None:
-        log.append(SiteLog(target, res.gs_eng, err, D, res.iters, ee))
+        sv = [float(x) for blk in s.blocks.values() for x in np.diag(blk)]
+        smin = min(sv) / max(sv) if sv and max(sv) > 0 else float("nan")
+        log.append(SiteLog(target, res.gs_eng, err, D, res.iters, ee, smin))
     return res.gs_eng
 
 

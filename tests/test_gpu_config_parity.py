@@ -125,7 +125,23 @@ def test_local_update_at_config(ctx, name, tmp_path):
 def test_heisenberg32_D256_six_sweeps(ctx):
     """Config 1: S=1/2 Heisenberg chain L=32, D=256, truncation 1e-8, Lanczos
     (1e-9, 100), six sweeps from the seed-0 product state (Sz=0), FP64 and
-    mixed forms against the oracle's sweeps."""
+    mixed forms against the oracle's sweeps: the final energy (1e-9 relative),
+    every update's truncation error (1e-10) and energy (1e-9 relative plus
+    1e-8: Lanczos stops once an iteration lowers the energy by less than 1e-9,
+    so two forms that stop one iteration apart differ by about that much in
+    the unconverged first sweep).
+
+    Dmin = Dmax = 256 keeps about 180 states whose singular values lie below
+    3e-7 of the largest, some of them null (the chain needs about 70 at
+    truncation 1e-8).  The device reads singular values from Gram matrices,
+    whose eigenvalues carry an absolute error of about n eps lambda_max, so
+    below ~1e-7 s_max its values, and with them which of those states Dmin
+    keeps, are set by rounding; the oracle's LAPACK SVD orders them by values
+    accurate to eps s_max.  Either choice keeps the state's weight to 1e-13,
+    but the bond sectors it leaves differ, and with them the full rank of a
+    later bond near the chain's end.  So bond dimensions are compared up to
+    the first update where the oracle keeps a state below 1e-6 of the
+    largest."""
     N, D = 32, 256
     mpo, pb = M.heisenberg_chain_mpo(N, builder="reference")
     labels = M.random_sz0_labels(N, 0)
@@ -140,7 +156,12 @@ def test_heisenberg32_D256_six_sweeps(ctx):
             ctx, dmps, dmpo, api.FiniteVMPSSweepParams(6, D, D, 1e-8, 1e-9, 100, precision=prec))
         assert abs(e0 - oe) <= 1e-9 * abs(oe), (prec, e0, oe)
         assert len(log) == len(olog)
+        resolvable, compared = True, 0
         for a, b in zip(log, olog):
-            assert a["D"] == b.D
+            if resolvable:
+                assert a["D"] == b.D
+                compared += 1
             assert abs(a["trunc_err"] - b.trunc_err) <= 1e-10
-            assert abs(a["e0"] - b.e0) <= 1e-9 * abs(b.e0)
+            assert abs(a["e0"] - b.e0) <= 1e-9 * abs(b.e0) + 1e-8, (prec, a["site"])
+            resolvable = resolvable and b.s_min_kept >= 1e-6
+        assert compared >= 40

@@ -79,18 +79,31 @@ def test_noise_vmps_vs_oracle(ctx):
     labels = M.random_sz0_labels(N, 5)
     noises = [0.1, 0.01, 0.001]
     e0, log, used = _run(ctx, mpo, pb, labels, 4, D, 1e-10, 1e-12, noises, dmin=1)
-    olog, oused = [], []
+    olog, oused, margins = [], [], []
     oe = ON.two_site_finite_vmps_with_noise(
         M.direct_product_mps([pb] * N, labels), mpo,
         ON.NoiseSweepParams(4, 1, D, 1e-10, krylov.LanczosParams(1e-12, 200), noises),
-        olog, oused)
+        olog, oused, margins)
     assert abs(e0 - oe) <= 1e-9 * abs(oe)
     assert len(log) == len(olog)
-    for a, b, u, ou in zip(log, olog, used, oused):
-        assert a["site"] == b.site and a["D"] == b.D
+    # Update by update until the applied noises part.  Where an update neither
+    # truncates nor changes the state, the next energy expectation equals the
+    # last energy up to rounding, and the sign that raises or keeps the noise
+    # (the reference's sharp rule) is a coin toss on either side: the two
+    # noise sequences may part there, and only there.  Up to the update that
+    # first applies a different noise the states are the same.
+    compared, coin_toss = 0, False
+    for a, b, u, ou, mg in zip(log, olog, used, oused, margins):
+        assert a["site"] == b.site
         assert abs(a["e0"] - b.e0) <= 1e-7 * abs(b.e0)
+        coin_toss = coin_toss or abs(mg) < 1e-10
+        if abs(u - ou) > 1e-12 * max(ou, 1e-300):
+            assert coin_toss, (compared, u, ou)
+            break
+        assert a["D"] == b.D
         assert abs(a["trunc_err"] - b.trunc_err) <= 1e-10
-        assert abs(u - ou) <= 1e-12 * max(ou, 1e-300)
+        compared += 1
+    assert compared >= 5
     assert sum(1 for u in used if u > 0) > 0
 
 

@@ -47,7 +47,8 @@ class SiteLog(C.Structure):
                 ("lancz_sec", C.c_double), ("svd_sec", C.c_double), ("env_sec", C.c_double),
                 ("tot_sec", C.c_double), ("matvec_flops", C.c_double),
                 ("svd_sketch_total", C.c_int64), ("svd_grow_rounds", C.c_int64),
-                ("svd_audit_err", C.c_double), ("svd_audit_kept_diff", C.c_int64)]
+                ("svd_audit_err", C.c_double), ("svd_audit_kept_diff", C.c_int64),
+                ("plan_sec", C.c_double)]
 
 
 class TdvpParams(C.Structure):
@@ -75,6 +76,7 @@ SIGNATURES = {
     "udmrg_ctx_set_krylov_graph": [C.c_void_p, C.c_int],
     "udmrg_ctx_set_tc_tiles": [C.c_void_p, C.c_int, C.c_int],
     "udmrg_ctx_tc_tuning": [C.c_void_p, c_int64_p, c_int64_p],
+    "udmrg_ctx_profiler_range": [C.c_void_p, C.c_int],
     "udmrg_tensor_create": [C.c_void_p, C.c_int, C.c_int, C.c_int, c_int32_p, c_int32_p,
                             c_int64_p, c_int32_p, C.c_int64, c_int32_p, c_void_pp],
     "udmrg_tensor_destroy": [C.c_void_p],

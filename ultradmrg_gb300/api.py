@@ -48,6 +48,11 @@ class Context:
         call("udmrg_ctx_tc_tuning", self.h, C.byref(t), C.byref(c))
         return t.value, c.value
 
+    def profiler_range(self, start: bool):
+        """Start or stop the CUDA profiler's collection after this context's
+        work so far (for a profiler run with collection off at start)."""
+        call("udmrg_ctx_profiler_range", self.h, 1 if start else 0)
+
     def set_krylov_graph(self, enable: bool):
         """Krylov steps as one CUDA graph replay each (default) or direct launches."""
         call("udmrg_ctx_set_krylov_graph", self.h, 1 if enable else 0)
@@ -359,7 +364,7 @@ def _log_rows(log, n):
                          tot_sec=L.tot_sec, matvec_flops=L.matvec_flops,
                          svd_sketch_total=L.svd_sketch_total,
                          svd_grow_rounds=L.svd_grow_rounds, svd_audit_err=L.svd_audit_err,
-                         svd_audit_kept_diff=L.svd_audit_kept_diff))
+                         svd_audit_kept_diff=L.svd_audit_kept_diff, plan_sec=L.plan_sec))
     return rows
 
 

@@ -35,7 +35,7 @@ def sources():
 
 def _compile(src: str, extra) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".hpp")]
+    hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".hpp", ".cuh"))]
     hdrs.append(os.path.join(HERE, "..", "include", "ultradmrg_gb300.h"))
     if os.path.exists(obj):
         t = os.path.getmtime(obj)

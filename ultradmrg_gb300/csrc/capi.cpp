@@ -4,6 +4,8 @@
 #include <cstring>
 #include <memory>
 
+#include <cuda_profiler_api.h>
+
 #include "../../include/ultradmrg_gb300.h"
 #include "dmrg.hpp"
 #include "matrepr.hpp"
@@ -131,6 +133,14 @@ int udmrg_ctx_tc_tuning(udmrg_ctx *c, int64_t *trials, int64_t *classes) {
   return guarded([&] {
     if (trials) *trials = c->ctx.tc_trials;
     if (classes) *classes = (int64_t)c->ctx.tc_tuned.size();
+  });
+}
+
+int udmrg_ctx_profiler_range(udmrg_ctx *c, int start) {
+  return guarded([&] {
+    UDMRG_REQUIRE(c, "null argument");
+    c->ctx.sync();
+    UDMRG_CHECK_CUDA(start ? cudaProfilerStart() : cudaProfilerStop());
   });
 }
 
@@ -452,7 +462,7 @@ static udmrg_site_log site_log(const SiteLog &s) {
   return {s.site,    s.e0,      s.trunc_err, s.D,           s.iters,
           s.ee,      s.lancz_sec, s.svd_sec, s.env_sec,     s.tot_sec,
           s.matvec_flops, s.svd_sketch_total, s.svd_grow_rounds, s.svd_audit_err,
-          s.svd_audit_kept_diff};
+          s.svd_audit_kept_diff, s.plan_sec};
 }
 
 int udmrg_two_site_update(udmrg_ctx *c, const udmrg_tensor *lenv, const udmrg_tensor *renv,

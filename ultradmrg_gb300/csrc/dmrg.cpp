@@ -758,6 +758,7 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
   const double t0 = now();
   auto init_state = contract_axes(ctx, mps_l, mps_r, {2}, {0});
   auto mv = plan_matvec2(ctx, lenv, mpo_l, mpo_r, renv, *init_state, p.lancz.precision);
+  const double tplan = now() - t0;
   auto lres = lanczos_gs(ctx, *mv, *init_state, p.lancz);
   const double t1 = now();
   const double mvflops = mv->flops;
@@ -824,7 +825,7 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
     if (log)
       *log = {0, e0, sres.trunc_err, sres.D, lres.iters, sres.ee, t1 - t0,
               t2 - t1 - audit_sec, t3 - t2, t3 - t0 - audit_sec, mvflops, sk, sres.grow_rounds,
-              audit_err, audit_diff};
+              audit_err, audit_diff, tplan};
   }
   return out;
 }

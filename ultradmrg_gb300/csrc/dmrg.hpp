@@ -130,6 +130,7 @@ struct SiteLog {
   int64_t svd_grow_rounds;   // sketch enlargements after a miss
   double svd_audit_err;      // |trunc_err - exact SVD's| (-1: not audited)
   int64_t svd_audit_kept_diff;  // kept states differing from the exact SVD's
+  double plan_sec = 0.0;     // host time building the matvec plan (part of lancz_sec)
 };
 
 // Sketch sizes of the randomized SVD per bond QN.

@@ -134,20 +134,22 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 // The same images for sources whose rows are (nearly) contiguous (psi: b
 // runs), when every op starts at a K column that is a multiple of 8: no
-// shared memory.  Warp w of a 32 x 64 work item takes the item's 8-wide
-// column group w, lane l its row l: each of the eight loads is coalesced
-// across the warp (consecutive rows), and the three 16-byte plane stores of
-// 32 consecutive rows fill 512 contiguous bytes of the canonical layout.
+// shared memory.  One work item per warp, 32 rows x 8 K columns of one op
+// (psi's ops are small, about 20 x 20, so items of a whole block would leave
+// most warps idle); lane l takes row l: each of the eight loads is coalesced
+// across the warp (consecutive rows), and the three 16-byte plane stores of 32
+// consecutive rows fill 512 contiguous bytes of the canonical layout.
 template <typename T>
 __global__ void __launch_bounds__(256)
-    pack_rows_kernel(const PackOp *__restrict__ ops, const PackTile *__restrict__ tiles,
-                     int ntiles, const T *__restrict__ src, uint8_t *__restrict__ img) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int w = blockIdx.x; w < ntiles; w += gridDim.x) {
-    const PackTile pt = tiles[w];
+    pack_rows_kernel(const PackOp *__restrict__ ops, const PackTile *__restrict__ items,
+                     int nitems, const T *__restrict__ src, uint8_t *__restrict__ img) {
+  const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  for (int w = blockIdx.x * wpb + (threadIdx.x >> 5); w < nitems; w += gridDim.x * wpb) {
+    const PackTile pt = items[w];
     const PackOp op = ops[pt.op];
-    const int rs = pt.r0 + lane, ks = pt.k0 + warp * 8;
-    if (rs >= op.rows || ks >= op.cols) continue;
+    const int rs = pt.r0 + lane, ks = pt.k0;
+    if (rs >= op.rows) continue;
     float x[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
@@ -227,11 +229,11 @@ void TcPlan::finalize() {
   ctx->sync();
 }
 
-std::vector<PackTile> pack_tiles(const std::vector<PackOp> &ops) {
+std::vector<PackTile> pack_tiles(const std::vector<PackOp> &ops, int kstep) {
   std::vector<PackTile> t;
   for (size_t o = 0; o < ops.size(); ++o)
     for (int32_t r0 = 0; r0 < ops[o].rows; r0 += 32)
-      for (int32_t k0 = 0; k0 < ops[o].cols; k0 += 64) t.push_back({(int32_t)o, r0, k0, 0});
+      for (int32_t k0 = 0; k0 < ops[o].cols; k0 += kstep) t.push_back({(int32_t)o, r0, k0, 0});
   return t;
 }
 
@@ -243,9 +245,9 @@ PackList::~PackList() {
 
 void PackList::upload(Ctx &c) {
   ctx = &c;
-  tiles = pack_tiles(ops);
   rows_src = !ops.empty();
   for (const PackOp &op : ops) rows_src = rows_src && op.src_rs <= 2 && op.k0 % 8 == 0;
+  tiles = pack_tiles(ops, rows_src ? 8 : 64);
   d_ops = udmrg::upload(ctx, ops);
   d_tiles = udmrg::upload(ctx, tiles);
 }
@@ -253,10 +255,14 @@ void PackList::upload(Ctx &c) {
 static void launch_pack(Ctx &ctx, const PackOp *d_ops, const PackTile *d_tiles, int ntiles,
                         const void *src, bool src_f64, uint8_t *img, bool rows_src = false) {
   if (ntiles == 0) return;
-  const int grid = std::min(ntiles, 16 * ctx.num_sms);
+  const int grid = rows_src ? std::min((ntiles + 7) / 8, 32 * ctx.num_sms)
+                            : std::min(ntiles, 16 * ctx.num_sms);
   if (rows_src && src_f64)
     pack_rows_kernel<double><<<grid, 256, 0, ctx.stream>>>(d_ops, d_tiles, ntiles,
                                                            (const double *)src, img);
+  else if (rows_src)
+    pack_rows_kernel<float><<<grid, 256, 0, ctx.stream>>>(d_ops, d_tiles, ntiles,
+                                                          (const float *)src, img);
   else if (src_f64)
     pack_kernel<double><<<grid, 256, 0, ctx.stream>>>(d_ops, d_tiles, ntiles, (const double *)src,
                                                       img);
@@ -277,7 +283,7 @@ void run_pack(Ctx &ctx, const std::vector<PackOp> &ops, const void *src, bool sr
   PackList pl;
   pl.ops = ops;
   pl.upload(ctx);
-  launch_pack(ctx, pl.d_ops, pl.d_tiles, (int)pl.tiles.size(), src, src_f64, img);
+  launch_pack(ctx, pl.d_ops, pl.d_tiles, (int)pl.tiles.size(), src, src_f64, img, pl.rows_src);
   ctx.sync();  // the lists are freed on return
 }
 

@@ -80,7 +80,9 @@ int64_t tc_image_bytes(int64_t rows, int64_t K, int tr);
 struct PackTile {
   int32_t op, r0, k0, pad;
 };
-std::vector<PackTile> pack_tiles(const std::vector<PackOp> &ops);
+// Work items: 32 rows x kstep K columns of one op each (64 for the staged
+// kernel, 8 for the one-warp items of rows-contiguous sources).
+std::vector<PackTile> pack_tiles(const std::vector<PackOp> &ops, int kstep = 64);
 
 // A pack list resident on the device (ops and their tiles uploaded once).
 struct PackList {
@@ -90,6 +92,7 @@ struct PackList {
   PackOp *d_ops = nullptr;
   PackTile *d_tiles = nullptr;
   bool rows_src = false;  // every op reads rows with stride <= 2 from a K column % 8 == 0
+                          // (tiles are then one-warp items of 32 x 8)
   PackList() = default;
   PackList(const PackList &) = delete;
   PackList &operator=(const PackList &) = delete;

@@ -14,6 +14,13 @@ full sweep is timed from that same state in each form:
 * ``mixed_learned_rule``: the same with the cost rule (the exact SVD when
   the predicted sketch exceeds a fraction of the sector dimensions).
 
+``--centre-update`` instead runs, from the prepared state, a right sweep of
+mixed-precision two-site updates (exact SVD) up to the centre bond and
+reports the centre update (seconds: total, Lanczos, matvec plan, SVD,
+environment); that update alone is bracketed as the CUDA profiler's
+collection range, so ``ncu --profile-from-start off`` records just its
+kernels.
+
 A form name may end in ``@<tol>`` (e.g. ``mixed_exact@1e-11``): that form's
 Lanczos runs to that tolerance instead of ``--lanczos-error``.  With
 ``--sweeps k`` each form runs k sweeps (``sweep_seconds`` is per sweep,
@@ -68,6 +75,42 @@ def prepare(ctx, Lx=16, Ly=4, schedule="10:2,100:2,500:2,1000:2,2000:1", lanczos
     return mpo, dmpo, state, model, prep, sec
 
 
+def centre_update(ctx, mpo, dmpo, state, D=2000):
+    """The right sweep of mixed two-site updates from the prepared state up to
+    the centre bond; returns the centre update's timings and log."""
+    N = len(state)
+    centre = N // 2 - 1
+    p = api.FiniteVMPSSweepParams(1, D, D, 1e-8, 1e-9, 100, precision=api.PREC_MIXED)
+    mps = _upload(ctx, state)
+    # right environments of the (right-canonical) prepared state: renvs[k]
+    # covers the last k sites
+    renvs = [api.DeviceTensor.from_data(ctx, api.trivial_env_data(state[N - 1], mpo[N - 1], "r"))]
+    for i in range(N - 1, 1, -1):
+        renvs.append(api.update_site_renvs(ctx, renvs[-1], mps[i], dmpo[i]))
+    L = api.DeviceTensor.from_data(ctx, api.trivial_env_data(state[0], mpo[0], "l"))
+    out = {}
+    for l in range(centre + 1):
+        if l == centre:
+            ctx.profiler_range(True)
+        t0 = time.perf_counter()
+        a, b, e, log = api.two_site_update(ctx, L, renvs[N - l - 2], mps[l], mps[l + 1],
+                                           dmpo[l], dmpo[l + 1], p, "r")
+        ctx.sync()
+        sec = time.perf_counter() - t0
+        if l == centre:
+            ctx.profiler_range(False)
+            out = dict(bond=l, seconds=sec, **{k: log[k] for k in (
+                "lancz_sec", "plan_sec", "svd_sec", "env_sec", "iters", "D", "trunc_err", "e0")})
+        mps[l].close()
+        mps[l + 1].close()
+        mps[l], mps[l + 1] = a, b
+        L.close()
+        L = e
+    for t in mps + renvs + [L]:
+        t.close()
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--Lx", type=int, default=16)
@@ -82,14 +125,24 @@ def main(argv=None):
     ap.add_argument("--max-fraction", type=float, default=0.1,
                     help="sketch fraction above which the learned form runs the exact SVD "
                          "(form mixed_learned_rule)")
+    ap.add_argument("--centre-update", action="store_true",
+                    help="time (and mark for the profiler) the centre bond's update instead")
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
     ctx = api.Context(0)
     N = a.Lx * a.Ly
-    _, dmpo, state, model, prep, prep_sec = prepare(ctx, a.Lx, a.Ly, a.schedule,
-                                                    a.lanczos_error, a.weights)
+    mpo, dmpo, state, model, prep, prep_sec = prepare(ctx, a.Lx, a.Ly, a.schedule,
+                                                      a.lanczos_error, a.weights)
     out = dict(workload=f"hubbard{a.Ly}x{a.Lx}", D=a.D, sites=N, preparation=prep,
                preparation_seconds=prep_sec, forms={})
+    if a.centre_update:
+        out.pop("forms")
+        out["centre_update"] = centre_update(ctx, mpo, dmpo, state, a.D)
+        print(json.dumps(out), flush=True)
+        if a.out:
+            with open(a.out, "w") as fh:
+                json.dump(out, fh, indent=1)
+        return
     forms = a.forms.split(",")
     if a.audit and "mixed_learned" in forms:
         forms.append("mixed_learned_audit")  # untimed: the exact SVD judges every truncation
