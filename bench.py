@@ -422,6 +422,15 @@ def run_ours(args):
     t64 = timed(lambda: plan64.apply_ptr(xp, y64p), max(2, min(args.steps, 5)), 200)
     ym, yd = y.download_packed(), y64.download_packed()
     mixed_err = float(np.linalg.norm(ym - yd) / max(np.linalg.norm(yd), 1e-300))
+    # the mixed solver's FP64-accurate anchor matvec (one per local solve):
+    # double-word FP32 block GEMMs against the FP64 pipe's
+    plan.apply_anchor_ptr(xp, yp)
+    t_anchor = timed(lambda: plan.apply_anchor_ptr(xp, yp), max(2, min(args.steps, 5)), 200)
+    ya = y.download_packed()
+    anchor = {"double_word_ms": t_anchor * 1e3, "fp64_pipe_ms": t64 * 1e3,
+              "speedup": t64 / t_anchor,
+              "rel_err_vs_fp64_pipe": float(np.linalg.norm(ya - yd) /
+                                            max(np.linalg.norm(yd), 1e-300))}
     # per-stage device times (dominant kernel roofline): the median of five
     # matvecs, each after an L2 flush like the timed steps
     samples = []
@@ -609,6 +618,7 @@ def run_ours(args):
                                                    "MEASURED_PEAKS.json)"},
                        "stage_ms": ms_64},
         "speedup_mixed_vs_fp64": t64 / t_step,
+        "anchor_matvec": anchor,
         "accuracy": {"matvec_rel_err_mixed_vs_fp64": mixed_err,
                      "lanczos_E_mixed": lz["mixed"][0], "lanczos_E_fp64": lz["fp64"][0],
                      "lanczos_iters": [lz["mixed"][1], lz["fp64"][1]],

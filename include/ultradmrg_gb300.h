@@ -113,6 +113,14 @@ int udmrg_ctx_launches(udmrg_ctx *ctx, uint64_t *out);
  * qlmps: the reference loop calls the matvec function pointer per step
  * (lanczos_vmps_solver_impl.h:148, 213). */
 int udmrg_ctx_set_krylov_graph(udmrg_ctx *ctx, int enable);
+/* The mixed-precision Lanczos ends with a refinement run whose first step is
+ * one FP64-accurate matvec (the anchor).  dw != 0 (the default): its two
+ * block-GEMM stages in double-word FP32 arithmetic (each FP64 operand split
+ * into two floats, 48 significant bits, error-free products and sums; about
+ * 2^-48 relative per product, on this GPU's FP32 pipe instead of its narrow
+ * FP64 pipe) for real data; 0: on the FP64 pipe.  Complex data always uses
+ * the FP64 pipe.  Replaces nothing in qlmps (its matvec is FP64 throughout). */
+int udmrg_ctx_set_anchor_dw(udmrg_ctx *ctx, int dw);
 /* Mixed matvec: rows of the B tiles of the two tcgen05 GEMMs (L.psi: bn1,
  * .R: bn3), 64 or 128, or 0 for the tile autotuner (the default): the first
  * plan of a shape class is built with both tiles, one matvec of each is timed
@@ -359,6 +367,10 @@ int udmrg_matvec_plan_info(const udmrg_matvec_plan *p, double *flops, int64_t *p
 int udmrg_matvec_plan_embed(udmrg_matvec_plan *p, const udmrg_tensor *src, udmrg_tensor **out);
 /* out = H_eff * in on device buffers laid out in the Krylov structure. */
 int udmrg_matvec_plan_apply(udmrg_matvec_plan *p, const double *d_in, double *d_out);
+/* The same product in the mixed solver's anchor form (FP64 pipe or
+ * double-word FP32, per udmrg_ctx_set_anchor_dw), whatever the plan's
+ * precision. */
+int udmrg_matvec_plan_apply_anchor(udmrg_matvec_plan *p, const double *d_in, double *d_out);
 int udmrg_matvec_plan_destroy(udmrg_matvec_plan *p);
 /* One matvec with CUDA events between its four stages (device ms, written to
  * ms[4]) and the work of each stage in FLOP (flops[4]: algorithmic for the

@@ -77,6 +77,68 @@ def test_mixed_lanczos_energy(ctx, name, l):
     assert rel <= 1e-9
 
 
+@pytest.mark.parametrize("name,l", [("heis", 4), ("hub", 2), ("hub_big", 3)])
+def test_anchor_dw_matvec_vs_oracle(ctx, name, l):
+    """The mixed solver's anchor matvec in double-word FP32 arithmetic against
+    the oracle's FP64 matvec: 1e-13 of the largest element (48-bit operands,
+    error-free products and sums)."""
+    mpo, mps = SYSTEMS[name]()
+    eff, psi = two_site_problem(mpo, mps, l)
+    ref = krylov.eff_ham_mul_two_site_state(eff, psi)
+    dev = [up(ctx, t) for t in eff]
+    dpsi = up(ctx, psi)
+    plan = api.MatvecPlan(ctx, dev, dpsi, precision=MIXED)
+    x, y = plan.embed(dpsi), plan.embed(dpsi)
+    plan.apply_anchor(x, y)
+    d, s = max_block_diff(y.to_data(), ref)
+    assert d <= 1e-13 * s, (d, s)
+
+
+def test_anchor_dw_workload(ctx):
+    """The anchor at the 4x8 D=256 workload: double-word against the FP64
+    pipe, 1e-13 of the largest element and in norm."""
+    from ultradmrg_gb300.workloads import WORKLOADS, build_host
+    w = WORKLOADS["hubbard4x8_D256"]
+    mpo, mps = build_host(w)
+    l = w.centre
+    L, R = api.build_envs(ctx, mpo, mps, l, normalize=False)
+    psi = api.contract(ctx, up(ctx, mps[l]), up(ctx, mps[l + 1]), [2], [0])
+    plan = api.MatvecPlan(ctx, [L, up(ctx, mpo[l]), up(ctx, mpo[l + 1]), R], psi,
+                          precision=MIXED)
+    x, ya, yb = plan.embed(psi), plan.embed(psi), plan.embed(psi)
+    try:
+        plan.apply_anchor(x, ya)
+        ctx.set_anchor_dw(False)
+        plan.apply_anchor(x, yb)
+    finally:
+        ctx.set_anchor_dw(True)
+    a, b = ya.download_packed(), yb.download_packed()
+    assert np.max(np.abs(a - b)) <= 1e-13 * np.max(np.abs(b))
+    assert np.linalg.norm(a - b) <= 1e-13 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("name,l", [("hub", 2), ("hub_big", 3)])
+def test_mixed_lanczos_anchor_forms(ctx, name, l):
+    """Mixed Lanczos with the double-word anchor and with the FP64-pipe
+    anchor: energies within 1e-12 relative of each other and of the oracle's
+    FP64 Lanczos to 1e-10."""
+    mpo, mps = canonical_system(name, l, seed=5)
+    eff, psi = two_site_problem(mpo, mps, l, normalize=False)
+    ref = krylov.lanczos_solver(eff, psi.copy(), krylov.eff_ham_mul_two_site_state,
+                                krylov.LanczosParams(1e-12, 100))
+    dev = [up(ctx, t) for t in eff]
+    e = {}
+    try:
+        for dw in (True, False):
+            ctx.set_anchor_dw(dw)
+            e[dw] = api.lanczos_solver(ctx, dev, up(ctx, psi), 1e-12, 100,
+                                       precision=MIXED).gs_eng
+    finally:
+        ctx.set_anchor_dw(True)
+    assert abs(e[True] - e[False]) <= 1e-12 * abs(e[False])
+    assert abs(e[True] - ref.gs_eng) <= 1e-10 * abs(ref.gs_eng)
+
+
 def _gpu_vmps(ctx, mpo, pb, labels, params):
     mps0 = M.direct_product_mps([pb] * len(labels), labels)
     dmps = [up(ctx, t) for t in mps0]

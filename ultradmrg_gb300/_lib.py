@@ -77,6 +77,7 @@ SIGNATURES = {
     "udmrg_ctx_set_tc_tiles": [C.c_void_p, C.c_int, C.c_int],
     "udmrg_ctx_tc_tuning": [C.c_void_p, c_int64_p, c_int64_p],
     "udmrg_ctx_profiler_range": [C.c_void_p, C.c_int],
+    "udmrg_ctx_set_anchor_dw": [C.c_void_p, C.c_int],
     "udmrg_tensor_create": [C.c_void_p, C.c_int, C.c_int, C.c_int, c_int32_p, c_int32_p,
                             c_int64_p, c_int32_p, C.c_int64, c_int32_p, c_void_pp],
     "udmrg_tensor_destroy": [C.c_void_p],
@@ -146,6 +147,7 @@ SIGNATURES = {
     "udmrg_matvec_plan_info": [C.c_void_p, c_double_p, c_int64_p, c_int64_p],
     "udmrg_matvec_plan_embed": [C.c_void_p, C.c_void_p, c_void_pp],
     "udmrg_matvec_plan_apply": [C.c_void_p, c_double_p, c_double_p],
+    "udmrg_matvec_plan_apply_anchor": [C.c_void_p, c_double_p, c_double_p],
     "udmrg_matvec_plan_destroy": [C.c_void_p],
     "udmrg_matvec_plan_stage_times": [C.c_void_p, c_double_p, c_double_p, c_double_p,
                                       c_double_p],

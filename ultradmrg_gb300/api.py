@@ -48,6 +48,11 @@ class Context:
         call("udmrg_ctx_tc_tuning", self.h, C.byref(t), C.byref(c))
         return t.value, c.value
 
+    def set_anchor_dw(self, dw: bool):
+        """The mixed solver's FP64-accurate anchor matvec in double-word FP32
+        arithmetic (default) or on the FP64 pipe."""
+        call("udmrg_ctx_set_anchor_dw", self.h, 1 if dw else 0)
+
     def profiler_range(self, start: bool):
         """Start or stop the CUDA profiler's collection after this context's
         work so far (for a profiler run with collection off at start)."""
@@ -646,6 +651,15 @@ class MatvecPlan:
 
     def apply(self, x: DeviceTensor, y: DeviceTensor):
         self.apply_ptr(x.device_ptr(), y.device_ptr())
+
+    def apply_anchor_ptr(self, d_in: int, d_out: int):
+        call("udmrg_matvec_plan_apply_anchor", self.h,
+             C.cast(C.c_void_p(d_in), _lib.c_double_p), C.cast(C.c_void_p(d_out), _lib.c_double_p))
+
+    def apply_anchor(self, x: DeviceTensor, y: DeviceTensor):
+        """The mixed solver's FP64-accurate anchor product (FP64 pipe or
+        double-word FP32, per ``Context.set_anchor_dw``)."""
+        self.apply_anchor_ptr(x.device_ptr(), y.device_ptr())
 
     def stage_times(self, d_in: int, d_out: int):
         """(ms[4], flops[4]) of one matvec, CUDA events between the stages."""

@@ -55,6 +55,9 @@ struct Ctx {
   uint64_t launches = 0;
   // Krylov solvers replay each step as one CUDA graph (captured once per solve)
   bool krylov_graph = true;
+  // The mixed solver's FP64-accurate anchor matvec: its two block-GEMM stages
+  // in double-word FP32 arithmetic (true) or on the FP64 pipe (false)
+  bool anchor_dw = true;
   // Mixed matvec: B-tile rows of the tcgen05 GEMMs L.psi (tc_bn1) and .R
   // (tc_bn3), 64 or 128; 0: chosen per plan by timed trials, cached per
   // shape class in tc_tuned (class -> {bn1, bn3}); tc_trials counts them

@@ -144,6 +144,13 @@ int udmrg_ctx_profiler_range(udmrg_ctx *c, int start) {
   });
 }
 
+int udmrg_ctx_set_anchor_dw(udmrg_ctx *c, int dw) {
+  return guarded([&] {
+    UDMRG_REQUIRE(c, "null argument");
+    c->ctx.anchor_dw = dw != 0;
+  });
+}
+
 int udmrg_ctx_set_krylov_graph(udmrg_ctx *c, int enable) {
   return guarded([&] {
     UDMRG_REQUIRE(c, "null argument");
@@ -850,6 +857,10 @@ int udmrg_matvec_plan_embed(udmrg_matvec_plan *p, const udmrg_tensor *src, udmrg
 
 int udmrg_matvec_plan_apply(udmrg_matvec_plan *p, const double *d_in, double *d_out) {
   return guarded([&] { p->plan->apply(d_in, d_out); });
+}
+
+int udmrg_matvec_plan_apply_anchor(udmrg_matvec_plan *p, const double *d_in, double *d_out) {
+  return guarded([&] { p->plan->apply_anchor(d_in, d_out); });
 }
 
 int udmrg_probe_fp64_tflops(udmrg_ctx *c, double *tflops) {

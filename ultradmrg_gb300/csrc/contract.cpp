@@ -353,6 +353,59 @@ void gemm_finalize(GemmPlan &g) {
   g.upload();
 }
 
+TensorPtr contract_struct(const BTensor &A, const BTensor &B, const std::vector<int> &ca,
+                          const std::vector<int> &cb, const std::vector<int> &fa,
+                          const std::vector<int> &fb) {
+  UDMRG_REQUIRE(ca.size() == cb.size(), "contract: axis lists differ in length");
+  UDMRG_REQUIRE(fa.size() + ca.size() == (size_t)A.rank(), "contract: bad A axes");
+  UDMRG_REQUIRE(fb.size() + cb.size() == (size_t)B.rank(), "contract: bad B axes");
+  auto out = std::make_unique<BTensor>();
+  out->ctx = A.ctx;
+  out->dtype = A.dtype;
+  out->nq = A.nq;
+  for (int i : fa) out->idx.push_back(A.idx[i]);
+  for (int i : fb) out->idx.push_back(B.idx[i]);
+  const int ro = out->rank();
+  UDMRG_REQUIRE(ro > 0 && ro <= kMaxRank, "contract: output rank");
+  for (const BTensor *T : {&A, &B})
+    for (const Index &ix : T->idx)
+      UDMRG_REQUIRE(ix.nsec() < 65536, "contract: more than 65535 sectors on one index");
+  // B's distinct (contracted key, free key) pairs, grouped by contracted key
+  std::vector<std::pair<uint64_t, Key128>> bk;
+  bk.reserve(B.nblocks());
+  for (int64_t b = 0; b < B.nblocks(); ++b) {
+    uint64_t k = 0;
+    for (int ax : cb) k = (k << 16) | (uint64_t)B.key(b)[ax];
+    Key128 f = 0;
+    for (int ax : fb) f = (f << 16) | (Key128)B.key(b)[ax];
+    bk.push_back({k, f});
+  }
+  std::sort(bk.begin(), bk.end());
+  bk.erase(std::unique(bk.begin(), bk.end()), bk.end());
+  std::vector<Key128> keys;
+  for (int64_t a = 0; a < A.nblocks(); ++a) {
+    uint64_t k = 0;
+    for (int ax : ca) k = (k << 16) | (uint64_t)A.key(a)[ax];
+    Key128 ka = 0;
+    for (int ax : fa) ka = (ka << 16) | (Key128)A.key(a)[ax];
+    if (!fb.empty()) ka = fa.empty() ? 0 : ka << (16 * fb.size());
+    auto it = std::lower_bound(bk.begin(), bk.end(), std::make_pair(k, (Key128)0));
+    for (; it != bk.end() && it->first == k; ++it) keys.push_back(ka | it->second);
+  }
+  std::sort(keys.begin(), keys.end());
+  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+  std::vector<int32_t> flat(keys.size() * ro);
+  for (size_t o = 0; o < keys.size(); ++o) {
+    Key128 ok = keys[o];
+    for (int j = ro - 1; j >= 0; --j) {
+      flat[o * ro + j] = (int32_t)(uint32_t)(ok & 0xFFFF);
+      ok >>= 16;
+    }
+  }
+  out->set_blocks(flat);
+  return out;
+}
+
 std::unique_ptr<ContractPlan> plan_contract(const BTensor &A, const BTensor &B,
                                             const std::vector<int> &ca, const std::vector<int> &cb,
                                             const std::vector<int> &fa,

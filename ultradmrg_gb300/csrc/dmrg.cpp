@@ -92,20 +92,28 @@ std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTens
   mv->W1 = &W1;
   mv->W2 = &W2;
   mv->R = &R;
+  // the Krylov structure: block structures only until it closes, then the
+  // four contraction plans once
   TensorPtr S = psi0.clone_struct();
-  std::vector<int> ca, cb, fa, fb;
+  std::vector<int> ca1, cb1, fa1, fb1, ca2, cb2, fa2, fb2, ca3, cb3, fa3, fb3, ca, cb, fa, fb;
+  cyclic_axes(3, 4, 2, 0, 1, ca1, cb1, fa1, fb1);  // L(a', w, a) . psi(a, s1, s2, b)
+  cyclic_axes(5, 4, 1, 0, 2, ca2, cb2, fa2, fb2);
+  cyclic_axes(5, 4, 4, 0, 2, ca3, cb3, fa3, fb3);
+  cyclic_axes(5, 3, 4, 1, 2, ca, cb, fa, fb);
   for (int it = 0; it < 16; ++it) {
-    mv->p1 = plan_contract_axes(L, *S, {2}, {0});
-    mv->p2 = plan_contract_cyclic(*mv->p1->out, W1, 1, 0, 2);
-    mv->p3 = plan_contract_cyclic(*mv->p2->out, W2, 4, 0, 2);
-    cyclic_axes(5, 3, 4, 1, 2, ca, cb, fa, fb);
-    auto p4 = plan_contract(*mv->p3->out, R, ca, cb, fa, fb);
-    auto U = struct_union(*S, *p4->out);
+    auto s1 = contract_struct(L, *S, ca1, cb1, fa1, fb1);
+    auto s2 = contract_struct(*s1, W1, ca2, cb2, fa2, fb2);
+    auto s3 = contract_struct(*s2, W2, ca3, cb3, fa3, fb3);
+    auto s4 = contract_struct(*s3, R, ca, cb, fa, fb);
+    auto U = struct_union(*S, *s4);
     const bool closed = U->keys == S->keys;
     S = std::move(U);
     if (closed) break;
     UDMRG_REQUIRE(it < 15, "matvec: Krylov block structure did not close");
   }
+  mv->p1 = plan_contract_axes(L, *S, {2}, {0});
+  mv->p2 = plan_contract_cyclic(*mv->p1->out, W1, 1, 0, 2);
+  mv->p3 = plan_contract_cyclic(*mv->p2->out, W2, 4, 0, 2);
   mv->p4 = plan_contract_into(*mv->p3->out, R, ca, cb, fa, fb, *S, &mv->missing);
   mv->sstruct = std::move(S);
   mv->flops = mv->p1->gemm.flops + mv->p2->gemm.flops + mv->p3->gemm.flops + mv->p4->gemm.flops;
@@ -144,18 +152,22 @@ std::unique_ptr<MatvecPlan> plan_matvec1(Ctx &ctx, const BTensor &L, const BTens
   mv->W1 = &W;
   mv->R = &R;
   TensorPtr S = psi0.clone_struct();
-  std::vector<int> ca, cb, fa, fb;
+  std::vector<int> ca1, cb1, fa1, fb1, ca2, cb2, fa2, fb2, ca, cb, fa, fb;
+  cyclic_axes(3, 3, 2, 0, 1, ca1, cb1, fa1, fb1);  // L(a', w, a) . psi(a, s, b)
+  cyclic_axes(4, 4, 1, 0, 2, ca2, cb2, fa2, fb2);
   cyclic_axes(4, 3, 3, 1, 2, ca, cb, fa, fb);
   for (int it = 0; it < 16; ++it) {
-    mv->p1 = plan_contract_axes(L, *S, {2}, {0});
-    mv->p2 = plan_contract_cyclic(*mv->p1->out, W, 1, 0, 2);
-    auto p4 = plan_contract(*mv->p2->out, R, ca, cb, fa, fb);
-    auto U = struct_union(*S, *p4->out);
+    auto s1 = contract_struct(L, *S, ca1, cb1, fa1, fb1);
+    auto s2 = contract_struct(*s1, W, ca2, cb2, fa2, fb2);
+    auto s4 = contract_struct(*s2, R, ca, cb, fa, fb);
+    auto U = struct_union(*S, *s4);
     const bool closed = U->keys == S->keys;
     S = std::move(U);
     if (closed) break;
     UDMRG_REQUIRE(it < 15, "matvec: Krylov block structure did not close");
   }
+  mv->p1 = plan_contract_axes(L, *S, {2}, {0});
+  mv->p2 = plan_contract_cyclic(*mv->p1->out, W, 1, 0, 2);
   mv->p4 = plan_contract_into(*mv->p2->out, R, ca, cb, fa, fb, *S, &mv->missing);
   mv->sstruct = std::move(S);
   mv->flops = mv->p1->gemm.flops + mv->p2->gemm.flops + mv->p4->gemm.flops;
@@ -173,20 +185,21 @@ void MatvecPlan::apply(const double *in, double *out) {
   apply_fp64(in, out);
 }
 
-void MatvecPlan::apply_fp64(const double *in, double *out) {
+void MatvecPlan::apply_fp64(const double *in, double *out, bool dw) {
   const DType dt = sstruct->dtype;
   const int es = elem_doubles(dt);
-  run_gemm(*ctx, p1->gemm, dt, L->data, in, t1, 1.0, 0.0);
+  auto gemm = dw ? run_gemm_dw : run_gemm;
+  gemm(*ctx, p1->gemm, dt, L->data, in, t1, 1.0, 0.0);
   if (m64) {
     run_mpo_step64(*ctx, *m64, t1, t3);
   } else {
-    run_gemm(*ctx, p2->gemm, dt, t1, W1->data, t2, 1.0, 0.0);
-    if (sites == 2) run_gemm(*ctx, p3->gemm, dt, t2, W2->data, t3, 1.0, 0.0);
+    gemm(*ctx, p2->gemm, dt, t1, W1->data, t2, 1.0, 0.0);
+    if (sites == 2) gemm(*ctx, p3->gemm, dt, t2, W2->data, t3, 1.0, 0.0);
   }
   for (int64_t b : missing)
     UDMRG_CHECK_CUDA(cudaMemsetAsync(out + sstruct->offs[b] * es, 0,
                                      sstruct->block_elems(b) * es * sizeof(double), ctx->stream));
-  run_gemm(*ctx, p4->gemm, dt, sites == 2 ? t3 : t2, R->data, out, 1.0, 0.0);
+  gemm(*ctx, p4->gemm, dt, sites == 2 ? t3 : t2, R->data, out, 1.0, 0.0);
 }
 
 // ---------------------------------------------------------------------------
@@ -342,7 +355,7 @@ struct KrylovSteps {
     krylov_normalise(kw);
     if (timed) cudaEventRecord(ev.a, ctx.stream);
     if (fp64)
-      mv.apply_fp64(kw.X, kw.Y);
+      mv.apply_anchor(kw.X, kw.Y);
     else
       mv.apply(kw.X, kw.Y);
     if (timed) cudaEventRecord(ev.b, ctx.stream);

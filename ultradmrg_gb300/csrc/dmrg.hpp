@@ -44,7 +44,11 @@ struct MatvecPlan {
   std::unique_ptr<MpoStep64> m64;
   ~MatvecPlan();
   void apply(const double *in, double *out);       // device buffers in sstruct layout
-  void apply_fp64(const double *in, double *out);  // always the plain FP64 form
+  // always an FP64-accurate form: the plain FP64 GEMMs, or (dw) the
+  // double-word FP32 ones for real data
+  void apply_fp64(const double *in, double *out, bool dw = false);
+  // the mixed solver's anchor: apply_fp64 with the context's anchor_dw
+  void apply_anchor(const double *in, double *out) { apply_fp64(in, out, ctx->anchor_dw); }
 };
 
 std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTensor &W1,

@@ -76,6 +76,11 @@ void gemm_finalize(GemmPlan &g);
 // Run C = alpha * A*B (+ beta * C) for every problem of the plan.
 void run_gemm(Ctx &ctx, const GemmPlan &plan, DType dt, const double *a, const double *b,
               double *c, double alpha, double beta);
+// The same GEMMs of real data in double-word FP32 arithmetic (48-bit
+// operands, FP64 in and out; about 2^-48 relative per product); complex data
+// on the FP64 pipe.
+void run_gemm_dw(Ctx &ctx, const GemmPlan &plan, DType dt, const double *a, const double *b,
+                 double *c, double alpha, double beta);
 
 // Contraction of two block tensors.  Output axes: A's free axes in
 // a_free_order, then B's free axes in b_free_order.
@@ -110,6 +115,13 @@ std::unique_ptr<ContractPlan> plan_contract_cyclic(const BTensor &A, const BTens
                                                    int b_start, int n);
 void cyclic_axes(int ra, int rb, int a_start, int b_start, int n, std::vector<int> &ca,
                  std::vector<int> &cb, std::vector<int> &fa, std::vector<int> &fb);
+
+// Block structure (indexes and blocks, no data, no GEMM plan) of a
+// contraction's output: the same as the plan's `out`, at a fraction of the
+// cost (no segments, tiles or uploads).
+TensorPtr contract_struct(const BTensor &A, const BTensor &B, const std::vector<int> &ca,
+                          const std::vector<int> &cb, const std::vector<int> &fa,
+                          const std::vector<int> &fb);
 
 // Execute a plan: allocates the output data.
 TensorPtr run_contract(Ctx &ctx, const ContractPlan &plan, const BTensor &A, const BTensor &B);
