@@ -115,11 +115,13 @@ int udmrg_ctx_launches(udmrg_ctx *ctx, uint64_t *out);
 int udmrg_ctx_set_krylov_graph(udmrg_ctx *ctx, int enable);
 /* The mixed-precision Lanczos ends with a refinement run whose first step is
  * one FP64-accurate matvec (the anchor).  dw != 0 (the default): its two
- * block-GEMM stages in double-word FP32 arithmetic (each FP64 operand split
- * into two floats, 48 significant bits, error-free products and sums; about
- * 2^-48 relative per product, on this GPU's FP32 pipe instead of its narrow
- * FP64 pipe) for real data; 0: on the FP64 pipe.  Complex data always uses
- * the FP64 pipe.  Replaces nothing in qlmps (its matvec is FP64 throughout). */
+ * block-GEMM stages, and the mixed-precision sweep's environment updates, in
+ * double-word FP32 arithmetic (each FP64 operand split into two floats, 48
+ * significant bits, error-free products and sums; about 2^-48 relative per
+ * product, on this GPU's FP32 pipe instead of its narrow FP64 pipe) for real
+ * data; 0: on the FP64 pipe.  Complex data always uses the FP64 pipe.  The
+ * plain FP64 form is not affected.  Replaces nothing in qlmps (its matvec
+ * is FP64 throughout). */
 int udmrg_ctx_set_anchor_dw(udmrg_ctx *ctx, int dw);
 /* Mixed matvec: rows of the B tiles of the two tcgen05 GEMMs (L.psi: bn1,
  * .R: bn3), 64 or 128, or 0 for the tile autotuner (the default): the first

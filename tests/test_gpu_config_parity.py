@@ -127,12 +127,14 @@ def test_heisenberg32_D256_six_sweeps(ctx):
     (1e-9, 100), six sweeps from the seed-0 product state (Sz=0), FP64 and
     mixed forms against the oracle's sweeps: the final energy (1e-9 relative),
     every update's truncation error (1e-10) and energy.  Lanczos stops once
-    an iteration lowers the energy by less than 1e-9, which in the slowly
-    converging updates of the first sweep can leave a few times that above
-    the eigenvalue: per-update energies agree to 1e-9 relative plus 1e-8 for
-    the FP64 form, and to 2e-8 relative for the mixed form, whose mixed run
-    and FP64-anchored refinement run each stop by that rule at their own
-    point.
+    an iteration lowers the energy by less than 1e-9, and in the first sweeps
+    that leaves a solve-dependent distance to the eigenvalue: the oracle's
+    own per-update energies move by up to 3.9e-7 relative in sweeps 2 and 3
+    when only its Lanczos tolerance goes from 1e-9 to 1e-12 (4.6e-10 in
+    sweep 4, 2e-12 in sweep 5).  The FP64 form follows the oracle to 1e-9
+    relative plus 1e-8 at every update; the mixed form, whose mixed run and
+    FP64-anchored refinement run each stop by that rule at their own point,
+    to 1e-6 relative in sweeps 1-4 and 1e-9 relative in sweeps 5 and 6.
 
     Dmin = Dmax = 256 keeps about 180 states whose singular values lie below
     3e-7 of the largest, some of them null (the chain needs about 70 at
@@ -160,12 +162,16 @@ def test_heisenberg32_D256_six_sweeps(ctx):
         assert abs(e0 - oe) <= 1e-9 * abs(oe), (prec, e0, oe)
         assert len(log) == len(olog)
         resolvable, compared = True, 0
-        for a, b in zip(log, olog):
+        per = 2 * (N - 2)  # updates per sweep
+        for i, (a, b) in enumerate(zip(log, olog)):
             if resolvable:
                 assert a["D"] == b.D
                 compared += 1
             assert abs(a["trunc_err"] - b.trunc_err) <= 1e-10
-            tol = 1e-9 * abs(b.e0) + 1e-8 if prec == api.PREC_FP64 else 2e-8 * abs(b.e0)
+            if prec == api.PREC_FP64:
+                tol = 1e-9 * abs(b.e0) + 1e-8
+            else:
+                tol = (1e-6 if i < 4 * per else 1e-9) * abs(b.e0)
             assert abs(a["e0"] - b.e0) <= tol, (prec, a["site"])
             resolvable = resolvable and b.s_min_kept >= 1e-6
         assert compared >= 40

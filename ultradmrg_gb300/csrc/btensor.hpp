@@ -58,6 +58,10 @@ struct Ctx {
   // The mixed solver's FP64-accurate anchor matvec: its two block-GEMM stages
   // in double-word FP32 arithmetic (true) or on the FP64 pipe (false)
   bool anchor_dw = true;
+  // Set while a mixed-precision update runs its SVD with anchor_dw: the SVD's
+  // Newton-Schulz and factor products in double-word arithmetic (its Gram
+  // products stay on the FP64 pipe)
+  bool svd_dw = false;
   // Mixed matvec: B-tile rows of the tcgen05 GEMMs L.psi (tc_bn1) and .R
   // (tc_bn3), 64 or 128; 0: chosen per plan by timed trials, cached per
   // shape class in tc_tuned (class -> {bn1, bn3}); tc_trials counts them

@@ -440,10 +440,11 @@ std::unique_ptr<ContractPlan> plan_contract_cyclic(const BTensor &A, const BTens
   return plan_contract(A, B, ca, cb, fa, fb);
 }
 
-TensorPtr run_contract(Ctx &ctx, const ContractPlan &plan, const BTensor &A, const BTensor &B) {
+TensorPtr run_contract(Ctx &ctx, const ContractPlan &plan, const BTensor &A, const BTensor &B,
+                       bool dw) {
   auto out = plan.out->clone_struct();
   out->alloc_data();
-  run_gemm(ctx, plan.gemm, A.dtype, A.data, B.data, out->data, 1.0, 0.0);
+  (dw ? run_gemm_dw : run_gemm)(ctx, plan.gemm, A.dtype, A.data, B.data, out->data, 1.0, 0.0);
   return out;
 }
 

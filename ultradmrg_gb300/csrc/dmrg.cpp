@@ -17,9 +17,9 @@ TensorPtr contract_axes(Ctx &ctx, const BTensor &A, const BTensor &B, const std:
 }
 
 TensorPtr contract_cyclic(Ctx &ctx, const BTensor &A, const BTensor &B, int a_start, int b_start,
-                          int n) {
+                          int n, bool dw) {
   auto p = plan_contract_cyclic(A, B, a_start, b_start, n);
-  return run_contract(ctx, *p, A, B);
+  return run_contract(ctx, *p, A, B, dw);
 }
 
 TensorPtr dag(Ctx &ctx, const BTensor &A) {
@@ -602,20 +602,22 @@ ExpmvResult lanczos_expmv(Ctx &ctx, MatvecPlan &mv, const BTensor &init_state, d
 // Environments
 // ---------------------------------------------------------------------------
 
-TensorPtr update_site_lenv(Ctx &ctx, const BTensor &lenv, const BTensor &A, const BTensor &W) {
+TensorPtr update_site_lenv(Ctx &ctx, const BTensor &lenv, const BTensor &A, const BTensor &W,
+                           bool dw) {
   auto Ad = dag(ctx, A);
-  auto t = contract_cyclic(ctx, lenv, A, 2, 0, 1);
-  auto t2 = contract_cyclic(ctx, *t, W, 1, 0, 2);
+  auto t = contract_cyclic(ctx, lenv, A, 2, 0, 1, dw);
+  auto t2 = contract_cyclic(ctx, *t, W, 1, 0, 2, dw);
   t.reset();
-  return contract_cyclic(ctx, *Ad, *t2, 0, 1, 2);
+  return contract_cyclic(ctx, *Ad, *t2, 0, 1, 2, dw);
 }
 
-TensorPtr update_site_renv(Ctx &ctx, const BTensor &renv, const BTensor &A, const BTensor &W) {
+TensorPtr update_site_renv(Ctx &ctx, const BTensor &renv, const BTensor &A, const BTensor &W,
+                           bool dw) {
   auto Ad = dag(ctx, A);
-  auto t = contract_cyclic(ctx, *Ad, renv, 2, 0, 1);
-  auto t2 = contract_cyclic(ctx, *t, W, 1, 2, 2);
+  auto t = contract_cyclic(ctx, *Ad, renv, 2, 0, 1, dw);
+  auto t2 = contract_cyclic(ctx, *t, W, 1, 2, 2, dw);
   t.reset();
-  return contract_cyclic(ctx, *t2, A, 3, 1, 2);
+  return contract_cyclic(ctx, *t2, A, 3, 1, 2, dw);
 }
 
 static TensorPtr trivial_env(Ctx &ctx, const Index &i0, const Index &iw, DType dt) {
@@ -783,6 +785,13 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
   SvdResult sres;
   double audit_err = -1.0, audit_sec = 0.0;
   int64_t audit_diff = 0;
+  // the mixed form's SVD: Newton-Schulz and factor products in double-word
+  // arithmetic (reset on every exit from this scope)
+  struct SvdDw {
+    Ctx &c;
+    SvdDw(Ctx &x, bool on) : c(x) { c.svd_dw = on; }
+    ~SvdDw() { c.svd_dw = false; }
+  } svd_dw(ctx, p.lancz.precision == kPrecMixed && ctx.anchor_dw);
   if (p.svd_mode == kSvdExact || (p.svd_mode == kSvdSketchLearned && !hint)) {
     sres = svd_trunc(ctx, psi, 2, ldiv, p.trunc_err, p.Dmin, p.Dmax, split,
                      spectra ? kSpectrumFloor : 0);
@@ -814,6 +823,7 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
       audit_sec = now() - ta;
     }
   }
+  ctx.svd_dw = false;
   lres.gs_vec.reset();
   if (spectra) {
     spectra->clear();
@@ -825,10 +835,12 @@ LocalUpdate two_site_update_local(Ctx &ctx, const BTensor &lenv, const BTensor &
   out.mps_r = std::move(sres.vt);
   ctx.sync();
   const double t2 = now();
+  // the mixed form's environments in double-word arithmetic with its anchor
+  const bool env_dw = p.lancz.precision == kPrecMixed && ctx.anchor_dw;
   if (dir == 'r')
-    out.env = update_site_lenv(ctx, lenv, *out.mps_l, mpo_l);
+    out.env = update_site_lenv(ctx, lenv, *out.mps_l, mpo_l, env_dw);
   else
-    out.env = update_site_renv(ctx, renv, *out.mps_r, mpo_r);
+    out.env = update_site_renv(ctx, renv, *out.mps_r, mpo_r, env_dw);
   ctx.sync();
   const double e0 = lres.gs_eng;
   const double t3 = now();

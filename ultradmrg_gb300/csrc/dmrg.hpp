@@ -16,7 +16,7 @@ enum Precision : int { kPrecFP64 = 0, kPrecMixed = 1 };
 TensorPtr contract_axes(Ctx &ctx, const BTensor &A, const BTensor &B, const std::vector<int> &ca,
                         const std::vector<int> &cb);
 TensorPtr contract_cyclic(Ctx &ctx, const BTensor &A, const BTensor &B, int a_start, int b_start,
-                          int n);
+                          int n, bool dw = false);
 TensorPtr dag(Ctx &ctx, const BTensor &A);
 TensorPtr to_complex(Ctx &ctx, const BTensor &A);
 // Same data laid out in the (superset) structure `dst` (missing blocks zero).
@@ -106,8 +106,12 @@ std::vector<double> tridiag_expme1(const std::vector<double> &a, const std::vect
                                    int64_t n, double dt);
 
 // Environment updates (algorithm/vmps/vmps_init.h:343-373).
-TensorPtr update_site_lenv(Ctx &ctx, const BTensor &lenv, const BTensor &A, const BTensor &W);
-TensorPtr update_site_renv(Ctx &ctx, const BTensor &renv, const BTensor &A, const BTensor &W);
+// dw: the contractions of real data in double-word FP32 arithmetic (the
+// mixed-precision sweep's environments, 2^-48 relative per product).
+TensorPtr update_site_lenv(Ctx &ctx, const BTensor &lenv, const BTensor &A, const BTensor &W,
+                           bool dw = false);
+TensorPtr update_site_renv(Ctx &ctx, const BTensor &renv, const BTensor &A, const BTensor &W,
+                           bool dw = false);
 TensorPtr trivial_renv(Ctx &ctx, const BTensor &mps_last, const BTensor &mpo_last);
 TensorPtr trivial_lenv(Ctx &ctx, const BTensor &mps_first, const BTensor &mpo_first);
 

@@ -124,6 +124,8 @@ TensorPtr contract_struct(const BTensor &A, const BTensor &B, const std::vector<
                           const std::vector<int> &fb);
 
 // Execute a plan: allocates the output data.
-TensorPtr run_contract(Ctx &ctx, const ContractPlan &plan, const BTensor &A, const BTensor &B);
+// dw: the GEMMs of real data in double-word FP32 arithmetic (run_gemm_dw).
+TensorPtr run_contract(Ctx &ctx, const ContractPlan &plan, const BTensor &A, const BTensor &B,
+                       bool dw = false);
 
 }  // namespace udmrg

@@ -198,12 +198,22 @@ __device__ __forceinline__ int sturm_count(const double *d, const double *e, int
 // count is serial, so points side by side shorten the chain of steps).
 // Block b handles eigenvalues i0 .. i0 + kBisectEigs - 1 (ascending index) of
 // job chunk[b].x, i0 = chunk[b].y.
+// With the threshold grid of the leading-eigenvalue path (top, cnt; see
+// grid_count_kernel) each eigenvalue starts from its grid cell, a factor 1.34
+// wide, instead of the Gershgorin interval: up to ~40% fewer steps for the
+// small eigenvalues of a Gram matrix.
 constexpr int kBisectLanes = 8;
 constexpr int kBisectEigs = 32 / kBisectLanes;
+constexpr int kGrid = 256;             // grid points
+constexpr double kGridDecades = 32.0;  // the grid spans top .. top * 1e-32
+__device__ __forceinline__ double grid_point(double top, int k) {
+  return top * exp10(-(double)k * kGridDecades / (kGrid - 1));
+}
 __global__ void __launch_bounds__(32)
     bisect_kernel(const EigJob *__restrict__ jobs, const int2 *__restrict__ chunk,
                   const double *__restrict__ d_all, const double *__restrict__ e_all,
-                  const double *__restrict__ scale_all, double *__restrict__ lam_all) {
+                  const double *__restrict__ scale_all, double *__restrict__ lam_all,
+                  const double *__restrict__ grid_top, const int *__restrict__ grid_cnt) {
   extern __shared__ double sm[];
   const int jb = chunk[blockIdx.x].x, i0 = chunk[blockIdx.x].y;
   const EigJob job = jobs[jb];
@@ -238,6 +248,20 @@ __global__ void __launch_bounds__(32)
   const int i = i0 + grp;  // i-th smallest
   double lo = lo0, hi = hi0;
   bool done = i >= n;
+  if (grid_cnt && !done && scale > 0.0 && grid_top[0] > 0.0) {
+    // cnt[k] = eigenvalues not below x_k (decreasing x_k); the first k with
+    // cnt[k] >= n - i bounds eigenvalue i from below by x_k, and x_{k-1}
+    // from above (the counts come from the same Sturm sequence)
+    const int *cnt = grid_cnt + (int64_t)jb * (kGrid + 1);
+    int k = 0;
+    while (k < kGrid && cnt[k] < n - i) ++k;
+    if (k < kGrid) lo = fmax(lo, grid_point(grid_top[0], k) / scale);
+    if (k > 0) hi = fmin(hi, grid_point(grid_top[0], k - 1) / scale);
+    if (!(lo < hi)) {  // inconsistent rounding at a cell edge: the full interval
+      lo = lo0;
+      hi = hi0;
+    }
+  }
   for (int it = 0; it < 64; ++it) {
     if (!done && hi - lo <= 4.4e-16 * fmax(fabs(lo), fabs(hi)) + atol) done = true;
     if (__all_sync(0xffffffffu, done)) break;
@@ -268,9 +292,6 @@ __global__ void __launch_bounds__(32)
 // only the leading eigenvalues of every sector need bisection.  A common
 // threshold is read off Sturm counts at a logarithmic grid of points below
 // the largest Gershgorin bound of all jobs.
-constexpr int kGrid = 256;             // grid points
-constexpr double kGridDecades = 32.0;  // the grid spans top .. top * 1e-32
-
 // top[0] = max over jobs of scale * (Gershgorin upper bound of its tridiagonal)
 __global__ void grid_top_kernel(const EigJob *__restrict__ jobs, int nj,
                                 const double *__restrict__ d_all, const double *__restrict__ e_all,
@@ -344,8 +365,7 @@ __global__ void grid_count_kernel(const EigJob *__restrict__ jobs,
     } else if (sc <= 0.0 || top[0] <= 0.0) {
       c = 0;  // a zero matrix: no eigenvalue reaches x_k > 0
     } else {
-      const double x = top[0] * exp10(-(double)k * kGridDecades / (kGrid - 1));
-      c = n - sturm_count(d, e, n, x / sc, pivmin);
+      c = n - sturm_count(d, e, n, grid_point(top[0], k) / sc, pivmin);
     }
     cnt[(int64_t)q * (kGrid + 1) + k] = c;
   }
@@ -1164,9 +1184,12 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
     wk.computed[q] = jobs[q].n;
     ntot += jobs[q].n;
   }
+  double *dtop = nullptr;
+  int *dcnt = nullptr;
   if (need > 0 && need < ntot) {
-    double *dtop = scratch.get<double>(1), *dtr = scratch.get<double>(nj);
-    int *dcnt = scratch.get<int>((size_t)nj * (kGrid + 1));
+    dtop = scratch.get<double>(1);
+    double *dtr = scratch.get<double>(nj);
+    dcnt = scratch.get<int>((size_t)nj * (kGrid + 1));
     grid_top_kernel<<<1, 1024, 0, ctx.stream>>>(wk.jobs, nj, wk.d, wk.e, wk.scale, dtop);
     grid_count_kernel<<<nj, kGrid, bsmem, ctx.stream>>>(wk.jobs, wk.d, wk.e, wk.scale, dtop, dcnt,
                                                         dtr);
@@ -1215,7 +1238,7 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
                                    cudaMemcpyHostToDevice, ctx.stream));
   if (!chunks.empty())
     bisect_kernel<<<(int)chunks.size(), 32, bsmem, ctx.stream>>>(
-        wk.jobs, dch, wk.d, wk.e, wk.scale, lam);
+        wk.jobs, dch, wk.d, wk.e, wk.scale, lam, dtop, dcnt);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches += 2;
   int hstat = 0;
@@ -1307,9 +1330,9 @@ void sym_eig_vectors(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJob>
             Copy2D{zc_off[q], z_off[q], jobs[q].n, (int32_t)k[q], k[q], 1, z_ld[q], 1});
       }
       for (int it = 0; it < 2; ++it) {
-        run_gemm(ctx, gs, kF64, Z, Z, S, 1.0, 0.0);
+        (ctx.svd_dw ? run_gemm_dw : run_gemm)(ctx, gs, kF64, Z, Z, S, 1.0, 0.0);
         run_copy2d(ctx, to_c, Z, Zc, false);
-        run_gemm(ctx, gz, kF64, Z, S, Zc, -0.5, 1.5);
+        (ctx.svd_dw ? run_gemm_dw : run_gemm)(ctx, gz, kF64, Z, S, Zc, -0.5, 1.5);
         run_copy2d(ctx, from_c, Zc, Z, false);
       }
     }

@@ -274,9 +274,9 @@ void build_outputs(Ctx &ctx, DeviceScratch &scratch, const BTensor &T, int ldims
     }
     gemm_finalize(g);
     if (left)
-      run_gemm(ctx, g, dt, iso_c, Mbuf, Cbuf, 1.0, 0.0);
+      (ctx.svd_dw ? run_gemm_dw : run_gemm)(ctx, g, dt, iso_c, Mbuf, Cbuf, 1.0, 0.0);
     else
-      run_gemm(ctx, g, dt, Mbuf, iso_c, Cbuf, 1.0, 0.0);
+      (ctx.svd_dw ? run_gemm_dw : run_gemm)(ctx, g, dt, Mbuf, iso_c, Cbuf, 1.0, 0.0);
   }
   if (mode == kSvdFull) {
     // vt = S^{-1} (U^T M): scale row i of each centre block by 1/s_i (0 for s_i == 0)
