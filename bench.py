@@ -462,6 +462,20 @@ def run_ours(args):
     tune["tuned_stage_ms"] = best
     tune["tuned_ms"] = sum(best)
     tune["trials_run"], tune["classes"] = ctx.tc_tuning()
+    # the grouped FP64 / double-word GEMMs' tile policy: the tuned plans'
+    # choice against both fixed policies (FP64 matvec, double-word anchor)
+    gemm = {"choice_fp64_plan": plan64.gemm_policy(), "choice_mixed_plan": plan.gemm_policy()}
+    for pol in (0, 1):
+        ctx.set_gemm_tiles(pol)
+        pf64 = api.MatvecPlan(ctx, ops, psi, precision=api.PREC_FP64)
+        pfmx = api.MatvecPlan(ctx, ops, psi, precision=api.PREC_MIXED)
+        ctx.set_gemm_tiles(-1)
+        gemm[f"policy{pol}_fp64_matvec_ms"] = timed(
+            lambda: pf64.apply_ptr(xp, y64p), 3, 200) * 1e3
+        gemm[f"policy{pol}_anchor_ms"] = timed(lambda: pfmx.apply_anchor_ptr(xp, yp), 3, 200) * 1e3
+        del pf64, pfmx
+    gemm["trials_run"], gemm["classes"] = ctx.gemm_tuning()
+    tune["fp64_gemm_tiles"] = gemm
     # Lanczos energies of both forms from the same start vector, to convergence
     lz = {}
     for name, prec in (("mixed", api.PREC_MIXED), ("fp64", api.PREC_FP64)):

@@ -132,6 +132,16 @@ int udmrg_ctx_set_anchor_dw(udmrg_ctx *ctx, int dw);
  * kernels). */
 int udmrg_ctx_set_tc_tiles(udmrg_ctx *ctx, int bn1, int bn3);
 int udmrg_ctx_tc_tuning(udmrg_ctx *ctx, int64_t *trials, int64_t *classes);
+/* Tile policy of the grouped FP64 (and double-word) block GEMMs of a
+ * two-site matvec plan's FP64-accurate product: 0 least padded work per
+ * output block, 1 fewer 32 x 32 tiles (taken only where larger tiles would
+ * pad more than twice as much), or -1 (the default) for the autotuner: the
+ * first plan of a shape class times one product under each policy and later
+ * plans of the class reuse the faster.  Results do not depend on the policy
+ * (the same summation order).  udmrg_ctx_gemm_tuning reports the trials run
+ * and the classes decided.  No counterpart in the reference. */
+int udmrg_ctx_set_gemm_tiles(udmrg_ctx *ctx, int policy);
+int udmrg_ctx_gemm_tuning(udmrg_ctx *ctx, int64_t *trials, int64_t *classes);
 /* Profiler range: waits for ctx's stream, then starts (start != 0) or stops
  * the CUDA profiler's collection (cudaProfilerStart / cudaProfilerStop), so
  * a profiler run with collection off at start records only the bracketed
@@ -399,6 +409,9 @@ int udmrg_matvec_plan_set_fused(udmrg_matvec_plan *p, int enable);
 /* Mixed form: the B-tile rows of its two GEMMs and whether the autotuner
  * chose them (*tuned = 1).  No counterpart in the reference. */
 int udmrg_matvec_plan_tiles(const udmrg_matvec_plan *p, int *bn1, int *bn3, int *tuned);
+/* The tile policy of the plan's FP64-accurate grouped GEMMs (0 or 1, see
+ * udmrg_ctx_set_gemm_tiles).  No counterpart in the reference. */
+int udmrg_matvec_plan_gemm_policy(const udmrg_matvec_plan *p, int *policy);
 
 /* ---- measurement ---------------------------------------------------- */
 /* FP64 FMA throughput of the device (TFLOP/s), measured by a DFMA-bound

@@ -139,6 +139,47 @@ def test_mixed_lanczos_anchor_forms(ctx, name, l):
     assert abs(e[True] - ref.gs_eng) <= 1e-10 * abs(ref.gs_eng)
 
 
+@pytest.mark.parametrize("name,l", [("hub", 2), ("hub_big", 3)])
+def test_gemm_tile_policies_bit_identical(ctx, name, l):
+    """The FP64 matvec and the double-word anchor under both tile policies of
+    the grouped GEMMs: bit-identical (every output sums in the same order)."""
+    mpo, mps = SYSTEMS[name]()
+    eff, psi = two_site_problem(mpo, mps, l)
+    dev = [up(ctx, t) for t in eff]
+    dpsi = up(ctx, psi)
+    out = {}
+    try:
+        for pol in (0, 1):
+            ctx.set_gemm_tiles(pol)
+            p64 = api.MatvecPlan(ctx, dev, dpsi, precision=api.PREC_FP64)
+            pmx = api.MatvecPlan(ctx, dev, dpsi, precision=MIXED)
+            assert p64.gemm_policy() == pol and pmx.gemm_policy() == pol
+            x, y, z = p64.embed(dpsi), p64.embed(dpsi), p64.embed(dpsi)
+            p64.apply(x, y)
+            pmx.apply_anchor(x, z)
+            out[pol] = (y.download_packed(), z.download_packed())
+    finally:
+        ctx.set_gemm_tiles(-1)
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_gemm_tile_autotuner(ctx):
+    """With the autotuner on, the first plan of a shape class runs the timed
+    trials; a second plan of the class reuses the decision."""
+    mpo, mps = SYSTEMS["hub_big"]()
+    eff, psi = two_site_problem(mpo, mps, 3)
+    dev = [up(ctx, t) for t in eff]
+    dpsi = up(ctx, psi)
+    ctx.set_gemm_tiles(-1)
+    api.MatvecPlan(ctx, dev, dpsi, precision=api.PREC_FP64)
+    t0, c0 = ctx.gemm_tuning()
+    p = api.MatvecPlan(ctx, dev, dpsi, precision=api.PREC_FP64)
+    t1, c1 = ctx.gemm_tuning()
+    assert c0 >= 1 and t1 == t0 and c1 == c0
+    assert p.gemm_policy() in (0, 1)
+
+
 def _gpu_vmps(ctx, mpo, pb, labels, params):
     mps0 = M.direct_product_mps([pb] * len(labels), labels)
     dmps = [up(ctx, t) for t in mps0]

@@ -77,6 +77,8 @@ SIGNATURES = {
     "udmrg_ctx_set_tc_tiles": [C.c_void_p, C.c_int, C.c_int],
     "udmrg_ctx_tc_tuning": [C.c_void_p, c_int64_p, c_int64_p],
     "udmrg_ctx_profiler_range": [C.c_void_p, C.c_int],
+    "udmrg_ctx_set_gemm_tiles": [C.c_void_p, C.c_int],
+    "udmrg_ctx_gemm_tuning": [C.c_void_p, c_int64_p, c_int64_p],
     "udmrg_ctx_set_anchor_dw": [C.c_void_p, C.c_int],
     "udmrg_tensor_create": [C.c_void_p, C.c_int, C.c_int, C.c_int, c_int32_p, c_int32_p,
                             c_int64_p, c_int32_p, C.c_int64, c_int32_p, c_void_pp],
@@ -155,6 +157,7 @@ SIGNATURES = {
     "udmrg_matvec_plan_set_fused": [C.c_void_p, C.c_int],
     "udmrg_matvec_plan_tiles": [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                 C.POINTER(C.c_int)],
+    "udmrg_matvec_plan_gemm_policy": [C.c_void_p, C.POINTER(C.c_int)],
     "udmrg_probe_fp64_tflops": [C.c_void_p, c_double_p],
     "udmrg_ctx_event_record": [C.c_void_p, C.c_int],
     "udmrg_ctx_event_elapsed": [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)],

@@ -48,6 +48,17 @@ class Context:
         call("udmrg_ctx_tc_tuning", self.h, C.byref(t), C.byref(c))
         return t.value, c.value
 
+    def set_gemm_tiles(self, policy: int = -1):
+        """Tile policy of a matvec plan's FP64-accurate grouped GEMMs: 0 least
+        padding, 1 fewer 32 x 32 tiles, -1 the autotuner (default)."""
+        call("udmrg_ctx_set_gemm_tiles", self.h, int(policy))
+
+    def gemm_tuning(self):
+        """(timed trials run, shape classes decided) of the GEMM tile tuner."""
+        t, c = C.c_int64(), C.c_int64()
+        call("udmrg_ctx_gemm_tuning", self.h, C.byref(t), C.byref(c))
+        return t.value, c.value
+
     def set_anchor_dw(self, dw: bool):
         """The mixed solver's FP64-accurate anchor matvec in double-word FP32
         arithmetic (default) or on the FP64 pipe."""
@@ -674,6 +685,12 @@ class MatvecPlan:
         a, b, t = C.c_int(), C.c_int(), C.c_int()
         call("udmrg_matvec_plan_tiles", self.h, C.byref(a), C.byref(b), C.byref(t))
         return a.value, b.value, bool(t.value)
+
+    def gemm_policy(self) -> int:
+        """Tile policy of the plan's FP64-accurate grouped GEMMs (0 or 1)."""
+        v = C.c_int()
+        call("udmrg_matvec_plan_gemm_policy", self.h, C.byref(v))
+        return v.value
 
     def set_fused(self, enable: bool):
         """Mixed form: MPO step inside the .R GEMM's producers or as its own

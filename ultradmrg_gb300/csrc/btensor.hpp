@@ -68,6 +68,12 @@ struct Ctx {
   int tc_bn1 = 0, tc_bn3 = 0;
   std::map<std::array<int64_t, 3>, std::array<int, 2>> tc_tuned;
   int64_t tc_trials = 0;
+  // Grouped FP64 / double-word GEMMs of a two-site matvec's FP64-accurate
+  // product: tile policy 0 or 1 (gemm.hpp), or -1: chosen per plan by timed
+  // trials, cached per shape class in gemm_tuned; gemm_trials counts them
+  int gemm_policy = -1;
+  std::map<std::array<int64_t, 4>, int> gemm_tuned;
+  int64_t gemm_trials = 0;
   // C-ABI lifetime: live tensor / plan handles on this context; a context
   // whose destroy was requested is deleted when the last handle goes
   int64_t live_handles = 0;

@@ -136,6 +136,20 @@ int udmrg_ctx_tc_tuning(udmrg_ctx *c, int64_t *trials, int64_t *classes) {
   });
 }
 
+int udmrg_ctx_set_gemm_tiles(udmrg_ctx *c, int policy) {
+  return guarded([&] {
+    UDMRG_REQUIRE(c && policy >= -1 && policy <= 1, "gemm tile policy: -1, 0 or 1");
+    c->ctx.gemm_policy = policy;
+  });
+}
+
+int udmrg_ctx_gemm_tuning(udmrg_ctx *c, int64_t *trials, int64_t *classes) {
+  return guarded([&] {
+    if (trials) *trials = c->ctx.gemm_trials;
+    if (classes) *classes = (int64_t)c->ctx.gemm_tuned.size();
+  });
+}
+
 int udmrg_ctx_profiler_range(udmrg_ctx *c, int start) {
   return guarded([&] {
     UDMRG_REQUIRE(c, "null argument");
@@ -1000,6 +1014,10 @@ int udmrg_matvec_plan_tiles(const udmrg_matvec_plan *p, int *bn1, int *bn3, int 
     if (bn3) *bn3 = m.sg->bn3;
     if (tuned) *tuned = m.sg->tuned ? 1 : 0;
   });
+}
+
+int udmrg_matvec_plan_gemm_policy(const udmrg_matvec_plan *p, int *policy) {
+  return guarded([&] { *policy = p->plan->p1->gemm.policy; });
 }
 
 int udmrg_matvec_plan_set_fused(udmrg_matvec_plan *p, int enable) {

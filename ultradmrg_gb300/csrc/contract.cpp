@@ -73,12 +73,16 @@ struct Match {
 };
 
 // Choose the tile configuration with the least padded work and emit the tiles.
-void add_tiles(GemmPlan &g, int32_t pid, int64_t M, int64_t N) {
+// Policy 1 charges 32 x 32 tiles (four outputs per thread) twice their padded
+// work, so they are taken only where the larger tiles would pad more than
+// twice as much.
+void add_tiles(GemmPlan &g, int32_t pid, int64_t M, int64_t N, int policy) {
   int best = 0;
   double bestw = 1e300;
   for (int c = 0; c < kNumCfg; ++c) {
     double w = (double)((M + kCfgBM[c] - 1) / kCfgBM[c] * kCfgBM[c]) *
                (double)((N + kCfgBN[c] - 1) / kCfgBN[c] * kCfgBN[c]);
+    if (policy == 1 && c == kCfg32x32) w *= 2.0;
     if (w < bestw * 0.999) {
       bestw = w;
       best = c;
@@ -302,7 +306,7 @@ static std::unique_ptr<ContractPlan> plan_impl(const BTensor &A, const BTensor &
       g.segs.push_back(sg);
     }
     g.flops += 2.0 * cplx * (double)M * (double)N * kflops;
-    add_tiles(g, (int32_t)g.probs.size(), M, N);
+    add_tiles(g, (int32_t)g.probs.size(), M, N, g.policy);
     g.probs.push_back(p);
   }
   gemm_finalize(g);
@@ -337,11 +341,11 @@ void gemm_add_simple(GemmPlan &g, int64_t c_off, int64_t M, int64_t N, int64_t K
   s.b_ks[0] = b_ks;
   g.segs.push_back(s);
   g.flops += 2.0 * (cplx ? 4.0 : 1.0) * (double)M * (double)N * (double)K;
-  add_tiles(g, (int32_t)g.probs.size(), M, N);
+  add_tiles(g, (int32_t)g.probs.size(), M, N, g.policy);
   g.probs.push_back(p);
 }
 
-void gemm_finalize(GemmPlan &g) {
+static void sort_tiles(GemmPlan &g) {
   // largest K first for load balance
   std::vector<int64_t> ktot(g.probs.size(), 0);
   for (size_t i = 0; i < g.probs.size(); ++i)
@@ -350,7 +354,25 @@ void gemm_finalize(GemmPlan &g) {
     std::stable_sort(g.tiles[c].begin(), g.tiles[c].end(), [&](const GTile &x, const GTile &y) {
       return ktot[x.prob] > ktot[y.prob];
     });
+}
+
+void gemm_finalize(GemmPlan &g) {
+  sort_tiles(g);
   g.upload();
+}
+
+void gemm_retile(GemmPlan &g, int policy) {
+  if (policy == g.policy) return;
+  g.policy = policy;
+  for (auto &t : g.tiles) t.clear();
+  for (size_t p = 0; p < g.probs.size(); ++p)
+    add_tiles(g, (int32_t)p, g.probs[p].M, g.probs[p].N, policy);
+  sort_tiles(g);
+  for (int c = 0; c < kNumCfg; ++c) {
+    g.ctx->free(g.d_tiles[c]);
+    g.d_tiles[c] = upload_vec(g.ctx, g.tiles[c]);
+  }
+  g.ctx->sync();
 }
 
 TensorPtr contract_struct(const BTensor &A, const BTensor &B, const std::vector<int> &ca,

@@ -80,6 +80,69 @@ MatvecPlan::~MatvecPlan() {
   ctx->free(t3);
 }
 
+// Tile policy of the FP64-accurate product's grouped GEMMs (the plain FP64
+// matvec, or the mixed plan's anchor): fixed by ctx.gemm_policy, else the
+// faster of the two policies in timed trials (zero input, best of two; the
+// kernels' work does not depend on the values), cached per shape class
+// (element type, anchor form, log2 of the Krylov structure's size, log2 of
+// its largest right-bond sector).
+static void tune_gemm_tiles(Ctx &ctx, MatvecPlan &mv) {
+  std::vector<GemmPlan *> gp = {&mv.p1->gemm, &mv.p4->gemm};
+  if (!mv.m64) {
+    gp.push_back(&mv.p2->gemm);
+    if (mv.p3) gp.push_back(&mv.p3->gemm);
+  }
+  auto retile = [&](int pol) {
+    for (GemmPlan *g : gp) gemm_retile(*g, pol);
+  };
+  if (ctx.gemm_policy >= 0) {
+    retile(ctx.gemm_policy);
+    return;
+  }
+  const BTensor &S = *mv.sstruct;
+  auto lg2 = [](int64_t x) {
+    int64_t k = 0;
+    while ((int64_t(1) << k) < x) ++k;
+    return k;
+  };
+  int64_t maxb = 1;
+  for (int64_t d : S.idx[S.rank() - 1].dims) maxb = std::max(maxb, d);
+  const bool dw = mv.precision == kPrecMixed && ctx.anchor_dw;
+  const std::array<int64_t, 4> key = {S.dtype == kC128 ? 1 : 0, dw ? 1 : 0, lg2(S.size()),
+                                      lg2(maxb)};
+  auto it = ctx.gemm_tuned.find(key);
+  if (it != ctx.gemm_tuned.end()) {
+    retile(it->second);
+    return;
+  }
+  const int64_t nd = S.size() * elem_doubles(S.dtype);
+  DeviceScratch sc(ctx);
+  double *x = sc.get<double>(std::max<int64_t>(nd, 1)), *y = sc.get<double>(std::max<int64_t>(nd, 1));
+  UDMRG_CHECK_CUDA(cudaMemsetAsync(x, 0, std::max<int64_t>(nd, 1) * sizeof(double), ctx.stream));
+  cudaEvent_t e0, e1;
+  UDMRG_CHECK_CUDA(cudaEventCreate(&e0));
+  UDMRG_CHECK_CUDA(cudaEventCreate(&e1));
+  float best[2] = {0, 0};
+  for (int pol = 0; pol < 2; ++pol) {
+    retile(pol);
+    for (int rep = 0; rep < 2; ++rep) {
+      cudaEventRecord(e0, ctx.stream);
+      mv.apply_fp64(x, y, dw);
+      cudaEventRecord(e1, ctx.stream);
+      UDMRG_CHECK_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best[pol] = rep == 0 ? ms : std::min(best[pol], ms);
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const int choice = best[1] < best[0] ? 1 : 0;
+  retile(choice);
+  ctx.gemm_tuned[key] = choice;
+  ctx.gemm_trials++;
+}
+
 std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTensor &W1,
                                          const BTensor &W2, const BTensor &R,
                                          const BTensor &psi0, int precision) {
@@ -138,6 +201,7 @@ std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTens
   if (!mv->m64)
     mv->t2 = (double *)ctx.alloc(std::max<int64_t>(mv->p2->out->size(), 1) * es * sizeof(double));
   mv->t3 = (double *)ctx.alloc(std::max<int64_t>(mv->p3->out->size(), 1) * es * sizeof(double));
+  tune_gemm_tiles(ctx, *mv);
   return mv;
 }
 

@@ -48,6 +48,7 @@ struct GemmPlan {
   std::vector<GProb> probs;
   std::vector<GTile> tiles[kNumCfg];
   double flops = 0;  // algorithmic: sum 2*M*N*K (x4 for complex data)
+  int policy = 0;    // tile policy (add_tiles): 0 least padded work, 1 fewer 32 x 32 tiles
   // device copies
   GSeg *d_segs = nullptr;
   GProb *d_probs = nullptr;
@@ -72,6 +73,9 @@ void gemm_add_simple(GemmPlan &g, int64_t c_off, int64_t M, int64_t N, int64_t K
                      bool cplx);
 // Sort tiles (largest K first) and upload the descriptors.
 void gemm_finalize(GemmPlan &g);
+// The same problems tiled under another policy (results are bit-identical:
+// every output element sums its segments and K in the same order).
+void gemm_retile(GemmPlan &g, int policy);
 
 // Run C = alpha * A*B (+ beta * C) for every problem of the plan.
 void run_gemm(Ctx &ctx, const GemmPlan &plan, DType dt, const double *a, const double *b,
