@@ -379,6 +379,12 @@ int udmrg_matvec_plan_info(const udmrg_matvec_plan *p, double *flops, int64_t *p
 int udmrg_matvec_plan_embed(udmrg_matvec_plan *p, const udmrg_tensor *src, udmrg_tensor **out);
 /* out = H_eff * in on device buffers laid out in the Krylov structure. */
 int udmrg_matvec_plan_apply(udmrg_matvec_plan *p, const double *d_in, double *d_out);
+/* out = H_eff * in with host buffers (packed Krylov-structure layout): one
+ * call copies in, applies and copies out on the context's stream, then
+ * waits (pinned host memory gives full copy bandwidth).  The plan keeps two
+ * device buffers for it.  The host-facing form of eff_ham_mul_two_site_state
+ * (lanczos_vmps_solver_impl.h:250-289). */
+int udmrg_matvec_plan_apply_host(udmrg_matvec_plan *p, const double *h_in, double *h_out);
 /* The same product in the mixed solver's anchor form (FP64 pipe or
  * double-word FP32, per udmrg_ctx_set_anchor_dw), whatever the plan's
  * precision. */

@@ -150,6 +150,7 @@ SIGNATURES = {
     "udmrg_matvec_plan_embed": [C.c_void_p, C.c_void_p, c_void_pp],
     "udmrg_matvec_plan_apply": [C.c_void_p, c_double_p, c_double_p],
     "udmrg_matvec_plan_apply_anchor": [C.c_void_p, c_double_p, c_double_p],
+    "udmrg_matvec_plan_apply_host": [C.c_void_p, c_double_p, c_double_p],
     "udmrg_matvec_plan_destroy": [C.c_void_p],
     "udmrg_matvec_plan_stage_times": [C.c_void_p, c_double_p, c_double_p, c_double_p,
                                       c_double_p],

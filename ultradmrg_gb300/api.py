@@ -663,6 +663,11 @@ class MatvecPlan:
     def apply(self, x: DeviceTensor, y: DeviceTensor):
         self.apply_ptr(x.device_ptr(), y.device_ptr())
 
+    def apply_host_ptr(self, h_in: int, h_out: int):
+        """H_eff * psi with host buffers (addresses of packed FP64 arrays)."""
+        call("udmrg_matvec_plan_apply_host", self.h, C.cast(C.c_void_p(h_in), _lib.c_double_p),
+             C.cast(C.c_void_p(h_out), _lib.c_double_p))
+
     def apply_anchor_ptr(self, d_in: int, d_out: int):
         call("udmrg_matvec_plan_apply_anchor", self.h,
              C.cast(C.c_void_p(d_in), _lib.c_double_p), C.cast(C.c_void_p(d_out), _lib.c_double_p))

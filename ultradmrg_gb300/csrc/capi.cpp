@@ -37,6 +37,11 @@ struct udmrg_matvec_plan {
   Ctx *ctx;
   std::unique_ptr<MatvecPlan> plan;
   TensorPtr promoted[4];  // complex copies of real operators, when needed
+  double *host_in = nullptr, *host_out = nullptr;  // device buffers of apply_host
+  ~udmrg_matvec_plan() {
+    if (host_in) ctx->free(host_in);
+    if (host_out) ctx->free(host_out);
+  }
 };
 
 namespace {
@@ -871,6 +876,25 @@ int udmrg_matvec_plan_embed(udmrg_matvec_plan *p, const udmrg_tensor *src, udmrg
 
 int udmrg_matvec_plan_apply(udmrg_matvec_plan *p, const double *d_in, double *d_out) {
   return guarded([&] { p->plan->apply(d_in, d_out); });
+}
+
+int udmrg_matvec_plan_apply_host(udmrg_matvec_plan *p, const double *h_in, double *h_out) {
+  return guarded([&] {
+    MatvecPlan &m = *p->plan;
+    Ctx &ctx = *p->ctx;
+    const size_t bytes = (size_t)m.sstruct->size() * elem_doubles(m.sstruct->dtype) * sizeof(double);
+    if (!p->host_in) {
+      p->host_in = (double *)ctx.alloc(std::max<size_t>(bytes, 8));
+      p->host_out = (double *)ctx.alloc(std::max<size_t>(bytes, 8));
+    }
+    if (bytes)
+      UDMRG_CHECK_CUDA(cudaMemcpyAsync(p->host_in, h_in, bytes, cudaMemcpyHostToDevice, ctx.stream));
+    m.apply(p->host_in, p->host_out);
+    if (bytes)
+      UDMRG_CHECK_CUDA(
+          cudaMemcpyAsync(h_out, p->host_out, bytes, cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.sync();
+  });
 }
 
 int udmrg_matvec_plan_apply_anchor(udmrg_matvec_plan *p, const double *d_in, double *d_out) {

@@ -361,6 +361,18 @@ void gemm_finalize(GemmPlan &g) {
   g.upload();
 }
 
+void gemm_keep_upper(GemmPlan &g) {
+  for (int c = 0; c < kNumCfg; ++c) {
+    auto &t = g.tiles[c];
+    t.erase(std::remove_if(t.begin(), t.end(),
+                           [&](const GTile &x) { return x.m0 > x.n0 + kCfgBN[c] - 1; }),
+            t.end());
+    g.ctx->free(g.d_tiles[c]);
+    g.d_tiles[c] = upload_vec(g.ctx, t);
+  }
+  g.ctx->sync();
+}
+
 void gemm_retile(GemmPlan &g, int policy) {
   if (policy == g.policy) return;
   g.policy = policy;

@@ -76,6 +76,9 @@ void gemm_finalize(GemmPlan &g);
 // The same problems tiled under another policy (results are bit-identical:
 // every output element sums its segments and K in the same order).
 void gemm_retile(GemmPlan &g, int policy);
+// Square problems whose result is symmetric (Hermitian): drop the tiles
+// entirely below the diagonal (the caller mirrors the upper triangle).
+void gemm_keep_upper(GemmPlan &g);
 
 // Run C = alpha * A*B (+ beta * C) for every problem of the plan.
 void run_gemm(Ctx &ctx, const GemmPlan &plan, DType dt, const double *a, const double *b,

@@ -1122,9 +1122,41 @@ void tridiag_multi_cta(Ctx &ctx, DeviceScratch &scratch, const std::vector<EigJo
   }
 }
 
+// Lower triangle of each job's matrix from its upper one: G[i][j] = conj(G[j][i]).
+// One block per job walks the 32 x 32 tiles on and below the diagonal; each
+// tile is read transposed from the upper triangle through shared memory, so
+// both the reads and the writes are coalesced rows.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    sym_mirror_kernel(const EigJob *__restrict__ jobs, T *__restrict__ G) {
+  __shared__ T tile[32][33];
+  const EigJob job = jobs[blockIdx.x];
+  const int n = job.n;
+  const int nt = (n + 31) / 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  T *A = G + job.g_off;
+  for (int t = 0; t < nt * (nt + 1) / 2; ++t) {
+    // tile (bi, bj) with bi >= bj: row block bi of the lower triangle
+    int bi = 0;
+    while ((bi + 1) * (bi + 2) / 2 <= t) ++bi;
+    const int bj = t - bi * (bi + 1) / 2;
+    // source: rows bj*32.., columns bi*32.. (upper triangle)
+    for (int r = ty; r < 32; r += 8) {
+      const int i = bj * 32 + r, j = bi * 32 + tx;
+      if (i < n && j < n) tile[r][tx] = A[(int64_t)i * n + j];
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+      const int i = bi * 32 + r, j = bj * 32 + tx;  // destination (i, j), i > j
+      if (i < n && j < n && i > j) A[(int64_t)i * n + j] = cj(tile[tx][r]);
+    }
+    __syncthreads();
+  }
+}
+
 int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, double *G,
                    double *lam, SymEigWork &wk, bool cplx, int64_t need, int64_t floor,
-                   const std::vector<int64_t> *rank_cap) {
+                   const std::vector<int64_t> *rank_cap, bool mirror) {
   const int nj = (int)jobs.size();
   if (nj == 0) return 0;
   int64_t ltot = 0;
@@ -1158,6 +1190,14 @@ int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, 
   UDMRG_CHECK_CUDA(cudaMemsetAsync(dstat, 0, sizeof(int), ctx.stream));
   UDMRG_CHECK_CUDA(cudaMemcpyAsync(wk.jobs, jobs.data(), nj * sizeof(EigJob),
                                    cudaMemcpyHostToDevice, ctx.stream));
+  if (mirror) {
+    if (cplx)
+      sym_mirror_kernel<double2><<<nj, 256, 0, ctx.stream>>>(wk.jobs, (double2 *)G);
+    else
+      sym_mirror_kernel<double><<<nj, 256, 0, ctx.stream>>>(wk.jobs, G);
+    UDMRG_CHECK_CUDA(cudaGetLastError());
+    ctx.launches++;
+  }
   if (cplx)
     tridiag_c_kernel<<<nj, kTriThreads, smem, ctx.stream>>>(
         wk.jobs, (double2 *)G, wk.d, wk.e, (double2 *)wk.tau, wk.scale, dstat);

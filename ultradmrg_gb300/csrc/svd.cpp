@@ -420,6 +420,7 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
                       cplx);
     }
     gemm_finalize(g);
+    gemm_keep_upper(g);  // the eigensolver mirrors the upper triangle
     run_gemm(ctx, g, cplx ? kC128 : kF64, Mbuf, Mc, G, 1.0, 0.0);
   }
   // at most Dmax states are kept: only the leading eigenvalues of the sectors
@@ -430,7 +431,7 @@ SvdResult svd_trunc(Ctx &ctx, const BTensor &T, int ldims, const QN &ldiv, doubl
   for (int q = 0; q < nsec; ++q) rank_cap[q] = std::min(secs[q].rows, secs[q].cols);
   check_eig_status(sym_eig_values(ctx, scratch, jobs, G, lam, wk, cplx,
                                   Dmax > 0 ? std::max(Dmax, Dmin) + 64 : 0,
-                                  spectrum_floor, &rank_cap));
+                                  spectrum_floor, &rank_cap, true));
   const std::vector<double> hlam = download_vec(ctx, lam, ltot);
   std::vector<std::vector<double>> sv(nsec);
   double rest = 0.0;

@@ -64,9 +64,12 @@ void run_scale(Ctx &ctx, const std::vector<ScaleJob> &jobs, double *X, const dou
 // trace, so the weight of the rest is known exactly.  rank_cap (optional, one
 // per job): the caller uses at most that many of the job's eigenvalues (a Gram
 // matrix of rank min(rows, cols)), so no more of them count towards `need`.
+// mirror: only the upper triangles of the matrices hold data; the lower ones
+// are filled from them first (conjugated for complex data).
 int sym_eig_values(Ctx &ctx, DeviceScratch &scratch, std::vector<EigJob> &jobs, double *G,
                    double *lam, SymEigWork &wk, bool cplx = false, int64_t need = 0,
-                   int64_t floor = 0, const std::vector<int64_t> *rank_cap = nullptr);
+                   int64_t floor = 0, const std::vector<int64_t> *rank_cap = nullptr,
+                   bool mirror = false);
 // Phase 2: the leading k[q] eigenvectors of job q (hlam: host copy of lam) as
 // the columns of Z (row-major n x k[q], leading dimension z_ld[q], at z_off[q]),
 // orthonormal to FP64 accuracy.
