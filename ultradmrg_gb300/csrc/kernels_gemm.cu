@@ -149,8 +149,11 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
                         const In *__restrict__ A, const In *__restrict__ B, In *__restrict__ C,
                         double alpha, double beta) {
   constexpr int NT = (BM / TM) * (BN / TN);
-  __shared__ T As[BK][BM];
-  __shared__ T Bs[BK][BN];
+  // rows padded by one element: the staging stores of a warp walk K (the
+  // rows) when K is the operand's contiguous direction, and unpadded rows of
+  // 8-byte elements would all start in the same shared-memory bank
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Bs[BK][BN + 1];
   const int tid = threadIdx.x;
   const int tx = tid % (BN / TN);  // column group
   const int ty = tid / (BN / TN);  // row group
