@@ -38,6 +38,7 @@ __global__ void __launch_bounds__(32 * kMpoWarps, 2)
                      const float *__restrict__ t1, uint8_t *__restrict__ img) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int64_t plane = (int64_t)kTcBM * kTcBK * 2;
+  tc::pdl_wait();  // T1 from the L.psi GEMM
   for (int t = blockIdx.x * kMpoWarps + warp; t < ntasks; t += gridDim.x * kMpoWarps) {
     const MpoTask tk = tasks[t];
     const MpoPair pr = pairs[tk.pair];
@@ -126,6 +127,7 @@ __global__ void __launch_bounds__(32 * kMpoWarps, 2)
     }
     while (o < pr.nout) finish();  // the last channel and channels without nonzeros
   }
+  tc::pdl_launch_dependents();
 }
 
 // FP64 form: the same work units; inputs from T1 and outputs to T3 in their
@@ -204,9 +206,9 @@ void run_mpo_step(Ctx &ctx, const SgMatvecPlan &p) {
   if (ntasks == 0) return;
   const int blocks = (ntasks + kMpoWarps - 1) / kMpoWarps;
   const int grid = std::min(blocks, 16 * ctx.num_sms);
-  mpo_chunk_kernel<<<grid, 32 * kMpoWarps, 0, ctx.stream>>>(
-      p.d_tasks, ntasks, p.d_pairs, p.d_outs, p.d_rowptr, p.d_nz, p.t1, p.t3_img);
-  UDMRG_CHECK_CUDA(cudaGetLastError());
+  UDMRG_CHECK_CUDA(tc::launch_pdl(mpo_chunk_kernel, dim3(grid), dim3(32 * kMpoWarps), 0,
+                                  ctx.stream, p.d_tasks, ntasks, p.d_pairs, p.d_outs, p.d_rowptr,
+                                  p.d_nz, p.t1, p.t3_img));
   ctx.launches++;
 }
 

@@ -500,23 +500,24 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec_tuned(Ctx &ctx, const BTensor &L, c
     p->tuned = true;
     return p;
   }
-  // timed trials: one matvec per tile choice (input zeros: the kernels' work
-  // does not depend on the values), best of two, stage by stage
+  // timed trials: matvecs with each tile choice (input zeros: the kernels'
+  // work does not depend on the values), stage by stage
   std::unique_ptr<SgMatvecPlan> cand[2];
   float best[2][4];
   const int64_t nd = S.size() * (S.dtype == kC128 ? 2 : 1);
   DeviceScratch sc(ctx);
   double *x = sc.get<double>(nd), *y = sc.get<double>(nd);
   UDMRG_CHECK_CUDA(cudaMemsetAsync(x, 0, std::max<int64_t>(nd, 1) * sizeof(double), ctx.stream));
-  for (int c = 0; c < 2; ++c) {
-    const int bn = c == 0 ? 64 : 128;
-    cand[c] = plan_sg_matvec(ctx, L, R, S, fm, bn, bn);
-    for (int rep = 0; rep < 2; ++rep) {
+  for (int c = 0; c < 2; ++c) cand[c] = plan_sg_matvec(ctx, L, R, S, fm, c == 0 ? 64 : 128,
+                                                      c == 0 ? 64 : 128);
+  // the two candidates alternate, the best of four per stage (a stage differs
+  // between the tiles by a few microseconds, about the spread of one timing)
+  for (int rep = 0; rep < 4; ++rep)
+    for (int c = 0; c < 2; ++c) {
       float ms[4];
       cand[c]->apply_timed(x, y, ms);
       for (int k = 0; k < 4; ++k) best[c][k] = rep == 0 ? ms[k] : std::min(best[c][k], ms[k]);
     }
-  }
   ctx.tc_trials++;
   const int bn1 = best[1][1] < best[0][1] ? 128 : 64;
   const int bn3 = best[1][3] < best[0][3] ? 128 : 64;

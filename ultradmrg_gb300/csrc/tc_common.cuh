@@ -4,6 +4,7 @@
 
 #include <cuda_bf16.h>
 #include <cstdint>
+#include <utility>
 
 namespace udmrg {
 namespace tc {
@@ -124,6 +125,33 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
          | (1u << 10)                // B format: BF16
          | ((uint32_t)(N >> 3) << 17)  // N / 8
          | ((uint32_t)(M >> 4) << 24); // M / 16
+}
+
+// Programmatic dependent launch.  A kernel launched with launch_pdl may
+// start while its predecessor on the stream is still running: it calls
+// pdl_wait() before it touches anything the predecessor writes (a no-op when
+// nothing is pending), and pdl_launch_dependents() once its own main loop
+// is done, so that its successor's blocks can be scheduled as the last
+// blocks drain.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t stream, Args &&...args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 
 }  // namespace tc

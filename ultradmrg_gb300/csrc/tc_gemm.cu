@@ -101,6 +101,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const TcBars b = tc_bars<BN>(smem);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t tmem = tc_setup<BN>(b, 1, 0);
+  tc::pdl_wait();  // the images (and outputs) of the previous kernel
   if (warp == 0) {
     if (lane == 0) {  // producer: one bulk copy per operand unit and chunk
       uint32_t G = 0;
@@ -129,6 +130,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_epilogue_role<BN>(warp & 3, lane, tiles, ntiles, groups, rowaddr, out, out_kind, alpha,
                          b, tmem, err);
   }
+  tc::pdl_launch_dependents();
   tc_teardown<BN>(tmem, 0);
 }
 
@@ -169,6 +171,7 @@ __global__ void __launch_bounds__(256)
     *(uint4 *)(img + off + plane) = mi;
     *(uint4 *)(img + off + 2 * plane) = lo;
   }
+  tc::pdl_launch_dependents();
 }
 
 }  // namespace
@@ -299,10 +302,10 @@ static void launch_tc_gemm(Ctx &ctx, const TcPlan &plan, const uint8_t *a_img,
     attr_set = true;
   }
   const int grid = std::min(ntiles, ctx.num_sms);
-  tc_gemm_kernel<BN><<<grid, kThreads, TcShape<BN>::kSmemBytes, ctx.stream>>>(
-      plan.d_tiles, ntiles, plan.d_groups, a_img, b_img, plan.d_rowaddr, out, out_kind, alpha,
-      plan.d_err);
-  UDMRG_CHECK_CUDA(cudaGetLastError());
+  UDMRG_CHECK_CUDA(tc::launch_pdl(tc_gemm_kernel<BN>, dim3(grid), dim3(kThreads),
+                                  (size_t)TcShape<BN>::kSmemBytes, ctx.stream, plan.d_tiles,
+                                  ntiles, plan.d_groups, a_img, b_img, plan.d_rowaddr, out,
+                                  out_kind, alpha, plan.d_err));
   ctx.launches++;
 }
 
