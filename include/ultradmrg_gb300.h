@@ -418,6 +418,16 @@ int udmrg_matvec_plan_tiles(const udmrg_matvec_plan *p, int *bn1, int *bn3, int 
 /* The tile policy of the plan's FP64-accurate grouped GEMMs (0 or 1, see
  * udmrg_ctx_set_gemm_tiles).  No counterpart in the reference. */
 int udmrg_matvec_plan_gemm_policy(const udmrg_matvec_plan *p, int *policy);
+/* Host seconds spent building the plan, by phase: sec[0] the Krylov block
+ * structure's closure, sec[1] the host tables, built on host threads (the
+ * four contraction plans, the FP64 form's MPO step, the mixed form's tables
+ * when its tile shapes are known), sec[2] their uploads, sec[3] the mixed
+ * form's tables alone (a part of sec[1], or of sec[4]), sec[4] the mixed
+ * form's device part (allocations, operand packing, uploads; the tile
+ * trials of a new shape class), sec[5] FP64 workspaces and the GEMM tile
+ * tuning.  Profiling aid with no qlmps counterpart (planning is implicit in
+ * lanczos_vmps_solver_impl.h:114-248). */
+int udmrg_matvec_plan_build_times(const udmrg_matvec_plan *p, double *sec);
 
 /* ---- measurement ---------------------------------------------------- */
 /* FP64 FMA throughput of the device (TFLOP/s), measured by a DFMA-bound

@@ -180,6 +180,33 @@ def test_gemm_tile_autotuner(ctx):
     assert p.gemm_policy() in (0, 1)
 
 
+def test_plan_host_threads_bit_identical(ctx):
+    """The first mixed plan of a fresh context builds its tables on this
+    thread (tile trials); later plans build them on host threads beside the
+    contraction plans.  Both give bit-identical matvecs, and the plan reports
+    its build phases."""
+    mpo, mps = SYSTEMS["hub_big"]()
+    eff, psi = two_site_problem(mpo, mps, 3)
+    c2 = api.Context(0)
+    dev = [up(c2, t) for t in eff]
+    dpsi = up(c2, psi)
+    out = []
+    for rep in range(3):
+        pmx = api.MatvecPlan(c2, dev, dpsi, precision=MIXED)
+        p64 = api.MatvecPlan(c2, dev, dpsi, precision=api.PREC_FP64)
+        bt = pmx.build_times()
+        assert set(bt) == set(api.MatvecPlan.PLAN_PHASES)
+        assert all(v >= 0.0 for v in bt.values())
+        x, y, z, w = (pmx.embed(dpsi) for _ in range(4))
+        pmx.apply(x, y)
+        pmx.apply_anchor(x, z)
+        p64.apply(x, w)
+        out.append([t.download_packed() for t in (y, z, w)])
+    for rep in (1, 2):
+        for k in range(3):
+            assert np.array_equal(out[0][k], out[rep][k])
+
+
 def _gpu_vmps(ctx, mpo, pb, labels, params):
     mps0 = M.direct_product_mps([pb] * len(labels), labels)
     dmps = [up(ctx, t) for t in mps0]

@@ -159,6 +159,7 @@ SIGNATURES = {
     "udmrg_matvec_plan_tiles": [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                 C.POINTER(C.c_int)],
     "udmrg_matvec_plan_gemm_policy": [C.c_void_p, C.POINTER(C.c_int)],
+    "udmrg_matvec_plan_build_times": [C.c_void_p, c_double_p],
     "udmrg_probe_fp64_tflops": [C.c_void_p, c_double_p],
     "udmrg_ctx_event_record": [C.c_void_p, C.c_int],
     "udmrg_ctx_event_elapsed": [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)],

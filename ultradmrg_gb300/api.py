@@ -697,6 +697,15 @@ class MatvecPlan:
         call("udmrg_matvec_plan_gemm_policy", self.h, C.byref(v))
         return v.value
 
+    PLAN_PHASES = ("closure", "host_tables", "uploads", "mixed_tables",
+                   "mixed_device", "tile_tuning")
+
+    def build_times(self) -> dict:
+        """Host seconds of the plan's construction, by phase."""
+        v = (C.c_double * 6)()
+        call("udmrg_matvec_plan_build_times", self.h, v)
+        return dict(zip(self.PLAN_PHASES, list(v)))
+
     def set_fused(self, enable: bool):
         """Mixed form: MPO step inside the .R GEMM's producers or as its own
         kernel (the default; bit-identical results)."""

@@ -125,6 +125,11 @@ struct BTensor {
 
   // block lookup by sector-id tuple (built on demand)
   int64_t find(const std::vector<int32_t> &k) const;
+  // builds find's lookup now (find from several host threads at once is safe
+  // after this)
+  void prepare_lookup() const {
+    if (!lookup_built_) build_lookup();
+  }
   void build_lookup() const;
 
   // Set the block list (must be sorted and unique), compute offsets.

@@ -1044,6 +1044,12 @@ int udmrg_matvec_plan_gemm_policy(const udmrg_matvec_plan *p, int *policy) {
   return guarded([&] { *policy = p->plan->p1->gemm.policy; });
 }
 
+int udmrg_matvec_plan_build_times(const udmrg_matvec_plan *p, double *sec) {
+  return guarded([&] {
+    for (int k = 0; k < 6; ++k) sec[k] = p->plan->build_sec[k];
+  });
+}
+
 int udmrg_matvec_plan_set_fused(udmrg_matvec_plan *p, int enable) {
   return guarded([&] {
     MatvecPlan &m = *p->plan;

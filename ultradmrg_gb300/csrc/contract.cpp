@@ -95,12 +95,14 @@ void add_tiles(GemmPlan &g, int32_t pid, int64_t M, int64_t N, int policy) {
 
 }  // namespace
 
+static void sort_tiles(GemmPlan &g);
+
 static std::unique_ptr<ContractPlan> plan_impl(const BTensor &A, const BTensor &B,
                                                const std::vector<int> &ca,
                                                const std::vector<int> &cb,
                                                const std::vector<int> &fa,
                                                const std::vector<int> &fb, const BTensor *dst,
-                                               std::vector<int64_t> *missing) {
+                                               std::vector<int64_t> *missing, bool upload) {
   UDMRG_REQUIRE(ca.size() == cb.size(), "contract: axis lists differ in length");
   UDMRG_REQUIRE(A.dtype == B.dtype, "contract: operands must have the same element type");
   UDMRG_REQUIRE(fa.size() + ca.size() == (size_t)A.rank(), "contract: bad A axes");
@@ -309,7 +311,10 @@ static std::unique_ptr<ContractPlan> plan_impl(const BTensor &A, const BTensor &
     add_tiles(g, (int32_t)g.probs.size(), M, N, g.policy);
     g.probs.push_back(p);
   }
-  gemm_finalize(g);
+  if (upload)
+    gemm_finalize(g);
+  else
+    sort_tiles(g);
   plan->out = std::move(out);
   return plan;
 }
@@ -360,6 +365,8 @@ void gemm_finalize(GemmPlan &g) {
   sort_tiles(g);
   g.upload();
 }
+
+void gemm_upload(GemmPlan &g) { g.upload(); }
 
 void gemm_keep_upper(GemmPlan &g) {
   for (int c = 0; c < kNumCfg; ++c) {
@@ -443,8 +450,8 @@ TensorPtr contract_struct(const BTensor &A, const BTensor &B, const std::vector<
 std::unique_ptr<ContractPlan> plan_contract(const BTensor &A, const BTensor &B,
                                             const std::vector<int> &ca, const std::vector<int> &cb,
                                             const std::vector<int> &fa,
-                                            const std::vector<int> &fb) {
-  return plan_impl(A, B, ca, cb, fa, fb, nullptr, nullptr);
+                                            const std::vector<int> &fb, bool upload) {
+  return plan_impl(A, B, ca, cb, fa, fb, nullptr, nullptr, upload);
 }
 
 std::unique_ptr<ContractPlan> plan_contract_into(const BTensor &A, const BTensor &B,
@@ -452,26 +459,26 @@ std::unique_ptr<ContractPlan> plan_contract_into(const BTensor &A, const BTensor
                                                  const std::vector<int> &cb,
                                                  const std::vector<int> &fa,
                                                  const std::vector<int> &fb, const BTensor &dst,
-                                                 std::vector<int64_t> *missing) {
-  return plan_impl(A, B, ca, cb, fa, fb, &dst, missing);
+                                                 std::vector<int64_t> *missing, bool upload) {
+  return plan_impl(A, B, ca, cb, fa, fb, &dst, missing, upload);
 }
 
 std::unique_ptr<ContractPlan> plan_contract_axes(const BTensor &A, const BTensor &B,
                                                  const std::vector<int> &ca,
-                                                 const std::vector<int> &cb) {
+                                                 const std::vector<int> &cb, bool upload) {
   std::vector<int> fa, fb;
   for (int i = 0; i < A.rank(); ++i)
     if (std::find(ca.begin(), ca.end(), i) == ca.end()) fa.push_back(i);
   for (int i = 0; i < B.rank(); ++i)
     if (std::find(cb.begin(), cb.end(), i) == cb.end()) fb.push_back(i);
-  return plan_contract(A, B, ca, cb, fa, fb);
+  return plan_contract(A, B, ca, cb, fa, fb, upload);
 }
 
 std::unique_ptr<ContractPlan> plan_contract_cyclic(const BTensor &A, const BTensor &B, int a_start,
-                                                   int b_start, int n) {
+                                                   int b_start, int n, bool upload) {
   std::vector<int> ca, cb, fa, fb;
   cyclic_axes(A.rank(), B.rank(), a_start, b_start, n, ca, cb, fa, fb);
-  return plan_contract(A, B, ca, cb, fa, fb);
+  return plan_contract(A, B, ca, cb, fa, fb, upload);
 }
 
 TensorPtr run_contract(Ctx &ctx, const ContractPlan &plan, const BTensor &A, const BTensor &B,

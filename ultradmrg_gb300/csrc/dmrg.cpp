@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <future>
 #include <limits>
 #include <map>
 
@@ -155,18 +156,26 @@ std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTens
   mv->W1 = &W1;
   mv->W2 = &W2;
   mv->R = &R;
-  // the Krylov structure: block structures only until it closes, then the
-  // four contraction plans once
+  using clk = std::chrono::steady_clock;
+  auto tmark = clk::now();
+  auto lap = [&] {
+    const auto t = clk::now();
+    const double s = std::chrono::duration<double>(t - tmark).count();
+    tmark = t;
+    return s;
+  };
+  // the Krylov structure: block structures only until it closes
   TensorPtr S = psi0.clone_struct();
+  TensorPtr s1, s2, s3;  // the three intermediates' structures for the closed S
   std::vector<int> ca1, cb1, fa1, fb1, ca2, cb2, fa2, fb2, ca3, cb3, fa3, fb3, ca, cb, fa, fb;
   cyclic_axes(3, 4, 2, 0, 1, ca1, cb1, fa1, fb1);  // L(a', w, a) . psi(a, s1, s2, b)
   cyclic_axes(5, 4, 1, 0, 2, ca2, cb2, fa2, fb2);
   cyclic_axes(5, 4, 4, 0, 2, ca3, cb3, fa3, fb3);
   cyclic_axes(5, 3, 4, 1, 2, ca, cb, fa, fb);
   for (int it = 0; it < 16; ++it) {
-    auto s1 = contract_struct(L, *S, ca1, cb1, fa1, fb1);
-    auto s2 = contract_struct(*s1, W1, ca2, cb2, fa2, fb2);
-    auto s3 = contract_struct(*s2, W2, ca3, cb3, fa3, fb3);
+    s1 = contract_struct(L, *S, ca1, cb1, fa1, fb1);
+    s2 = contract_struct(*s1, W1, ca2, cb2, fa2, fb2);
+    s3 = contract_struct(*s2, W2, ca3, cb3, fa3, fb3);
     auto s4 = contract_struct(*s3, R, ca, cb, fa, fb);
     auto U = struct_union(*S, *s4);
     const bool closed = U->keys == S->keys;
@@ -174,26 +183,63 @@ std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTens
     if (closed) break;
     UDMRG_REQUIRE(it < 15, "matvec: Krylov block structure did not close");
   }
-  mv->p1 = plan_contract_axes(L, *S, {2}, {0});
-  mv->p2 = plan_contract_cyclic(*mv->p1->out, W1, 1, 0, 2);
-  mv->p3 = plan_contract_cyclic(*mv->p2->out, W2, 4, 0, 2);
-  mv->p4 = plan_contract_into(*mv->p3->out, R, ca, cb, fa, fb, *S, &mv->missing);
-  mv->sstruct = std::move(S);
-  mv->flops = mv->p1->gemm.flops + mv->p2->gemm.flops + mv->p3->gemm.flops + mv->p4->gemm.flops;
+  mv->build_sec[0] = lap();
   mv->precision = precision;
   UDMRG_REQUIRE(precision == kPrecFP64 || precision == kPrecMixed, "matvec: unknown precision");
   // real tensors: the two MPO steps as one sparse channel map (FP64 form) and
   // the same fused coefficients for the mixed form
   const bool real = L.dtype == kF64 && W1.dtype == kF64 && W2.dtype == kF64 &&
                     R.dtype == kF64 && psi0.dtype == kF64;
-  std::unique_ptr<FusedMpo> fm;
-  if (real) {
+  const bool mixed = precision == kPrecMixed;
+  std::unique_ptr<FusedMpo> fm, fm_sg;  // host copies of W1 W2 (one per thread)
+  if (real || mixed) {
     fm = std::make_unique<FusedMpo>(ctx, W1, W2);
-    mv->m64 = plan_mpo_step64(ctx, *fm, *mv->p1->out, *mv->p3->out);
+    if (real && mixed) fm_sg = std::make_unique<FusedMpo>(*fm);
   }
-  if (precision == kPrecMixed) {  // complex data through the real embedding
-    if (!fm) fm = std::make_unique<FusedMpo>(ctx, W1, W2);
-    mv->sg = plan_sg_matvec_tuned(ctx, L, R, *mv->sstruct, *fm);
+  FusedMpo *fmx = fm_sg ? fm_sg.get() : fm.get();
+  int bn1 = 0, bn3 = 0;
+  const bool sg_known = mixed && sg_tiles_known(ctx, *S, &bn1, &bn3);
+  // The host halves of the plans are independent given the closed structure
+  // and its intermediates, so they are built on host threads: the four
+  // contraction plans, the FP64 MPO step's tables and the mixed form's
+  // tables.  Device work (uploads, packing) follows on this thread.
+  S->prepare_lookup();
+  {
+    using Fut = std::future<void>;
+    std::vector<Fut> jobs;
+    auto run = [&](auto fn) { jobs.push_back(std::async(std::launch::async, fn)); };
+    run([&] { mv->p1 = plan_contract_axes(L, *S, {2}, {0}, false); });
+    run([&] { mv->p2 = plan_contract_cyclic(*s1, W1, 1, 0, 2, false); });
+    run([&] { mv->p3 = plan_contract_cyclic(*s2, W2, 4, 0, 2, false); });
+    run([&] {
+      mv->p4 = plan_contract_into(*s3, R, ca, cb, fa, fb, *S, &mv->missing, false);
+    });
+    if (real) run([&] { mv->m64 = build_mpo_step64(*fm, *s1, *s3); });
+    if (sg_known) run([&] { mv->sg = plan_sg_tables(L, R, *S, *fmx, bn1, bn3); });
+    for (Fut &f : jobs) f.wait();
+    for (Fut &f : jobs) f.get();  // the first failure, after every job ended
+  }
+  // the plans chained on the closure's intermediates: the same structures
+  UDMRG_REQUIRE(mv->p1->out->keys == s1->keys && mv->p2->out->keys == s2->keys &&
+                    mv->p3->out->keys == s3->keys,
+                "matvec: intermediate block structures differ from the closure's");
+  mv->build_sec[1] = lap();
+  for (ContractPlan *cp : {mv->p1.get(), mv->p2.get(), mv->p3.get(), mv->p4.get()})
+    gemm_upload(cp->gemm);
+  if (mv->m64) upload_mpo_step64(ctx, *mv->m64);
+  mv->build_sec[2] = lap();
+  mv->sstruct = std::move(S);
+  mv->flops = mv->p1->gemm.flops + mv->p2->gemm.flops + mv->p3->gemm.flops + mv->p4->gemm.flops;
+  if (mixed) {  // complex data through the real embedding
+    if (mv->sg) {
+      plan_sg_device(ctx, *mv->sg, L, R);
+      mv->sg->tuned = !(ctx.tc_bn1 && ctx.tc_bn3);
+    } else {
+      mv->sg = plan_sg_matvec_tuned(ctx, L, R, *mv->sstruct, *fmx);
+    }
+    const double t = lap();
+    mv->build_sec[3] = mv->sg->host_sec;
+    mv->build_sec[4] = t;
   }
   // the FP64 form is kept in both modes (the mixed solver's final Rayleigh quotient)
   const int es = elem_doubles(psi0.dtype);
@@ -202,6 +248,7 @@ std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTens
     mv->t2 = (double *)ctx.alloc(std::max<int64_t>(mv->p2->out->size(), 1) * es * sizeof(double));
   mv->t3 = (double *)ctx.alloc(std::max<int64_t>(mv->p3->out->size(), 1) * es * sizeof(double));
   tune_gemm_tiles(ctx, *mv);
+  mv->build_sec[5] = lap();
   return mv;
 }
 

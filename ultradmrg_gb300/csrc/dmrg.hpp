@@ -42,6 +42,13 @@ struct MatvecPlan {
   // real two-site FP64 form: the two MPO steps as one sparse channel map
   // (p2, p3 then only describe the intermediate structures)
   std::unique_ptr<MpoStep64> m64;
+  // host seconds of the plan's construction: 0 Krylov closure (and the W1 W2
+  // download), 1 the host tables built on host threads (contraction plans,
+  // FP64 MPO step, mixed form when its tiles are known), 2 their uploads,
+  // 3 the mixed form's tables alone (a part of 1, or of 4), 4 the mixed
+  // form's device part (with the tile trials of a new shape class), 5 FP64
+  // workspaces and GEMM tile tuning
+  double build_sec[6] = {0, 0, 0, 0, 0, 0};
   ~MatvecPlan();
   void apply(const double *in, double *out);       // device buffers in sstruct layout
   // always an FP64-accurate form: the plain FP64 GEMMs, or (dw) the

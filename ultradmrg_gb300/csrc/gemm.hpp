@@ -73,6 +73,8 @@ void gemm_add_simple(GemmPlan &g, int64_t c_off, int64_t M, int64_t N, int64_t K
                      bool cplx);
 // Sort tiles (largest K first) and upload the descriptors.
 void gemm_finalize(GemmPlan &g);
+// the descriptors of a plan made with upload = false onto the device
+void gemm_upload(GemmPlan &g);
 // The same problems tiled under another policy (results are bit-identical:
 // every output element sums its segments and K in the same order).
 void gemm_retile(GemmPlan &g, int policy);
@@ -96,10 +98,13 @@ struct ContractPlan {
   GemmPlan gemm;
 };
 
+// upload = false: the GEMM descriptors stay on the host (no device call;
+// safe on a host thread) until gemm_upload.
 std::unique_ptr<ContractPlan> plan_contract(const BTensor &A, const BTensor &B,
                                             const std::vector<int> &ca, const std::vector<int> &cb,
                                             const std::vector<int> &a_free_order,
-                                            const std::vector<int> &b_free_order);
+                                            const std::vector<int> &b_free_order,
+                                            bool upload = true);
 
 // Plan whose output is written into an existing structure `dst` (every block
 // the contraction produces must exist in dst).  Blocks of dst that receive no
@@ -111,15 +116,16 @@ std::unique_ptr<ContractPlan> plan_contract_into(const BTensor &A, const BTensor
                                                  const std::vector<int> &a_free_order,
                                                  const std::vector<int> &b_free_order,
                                                  const BTensor &dst,
-                                                 std::vector<int64_t> *missing);
+                                                 std::vector<int64_t> *missing,
+                                                 bool upload = true);
 
 // Plain-axes contraction (qlten's Contract(A, B, {axes_a, axes_b}, C)).
 std::unique_ptr<ContractPlan> plan_contract_axes(const BTensor &A, const BTensor &B,
                                                  const std::vector<int> &ca,
-                                                 const std::vector<int> &cb);
+                                                 const std::vector<int> &cb, bool upload = true);
 // Cyclic contraction (qlten's Contract<T, Q, a_tail, b_head>(A, B, a_start, b_start, n, C)).
 std::unique_ptr<ContractPlan> plan_contract_cyclic(const BTensor &A, const BTensor &B, int a_start,
-                                                   int b_start, int n);
+                                                   int b_start, int n, bool upload = true);
 void cyclic_axes(int ra, int rb, int a_start, int b_start, int n, std::vector<int> &ca,
                  std::vector<int> &cb, std::vector<int> &fa, std::vector<int> &fb);
 

@@ -102,11 +102,9 @@ MpoStep64::~MpoStep64() {
     ctx->free(p);
 }
 
-std::unique_ptr<MpoStep64> plan_mpo_step64(Ctx &ctx, FusedMpo &fm, const BTensor &T1,
-                                           const BTensor &T3) {
+std::unique_ptr<MpoStep64> build_mpo_step64(FusedMpo &fm, const BTensor &T1, const BTensor &T3) {
   UDMRG_REQUIRE(T1.rank() == 5 && T3.rank() == 5, "MPO step: rank-5 intermediates expected");
   auto p = std::make_unique<MpoStep64>();
-  p->ctx = &ctx;
   // T1 blocks by key (A', W, S1, S2, B)
   std::map<std::array<int32_t, 5>, int64_t> t1blk;
   for (int64_t b = 0; b < T1.nblocks(); ++b) {
@@ -182,6 +180,12 @@ std::unique_ptr<MpoStep64> plan_mpo_step64(Ctx &ctx, FusedMpo &fm, const BTensor
     p->unit_pair.insert(p->unit_pair.end(), nu, (int32_t)p->pairs.size());
     p->pairs.push_back(pr);
   }
+  return p;
+}
+
+void upload_mpo_step64(Ctx &ctx, MpoStep64 &m) {
+  MpoStep64 *p = &m;
+  p->ctx = &ctx;
   p->d_pairs = upload(ctx, p->pairs);
   p->d_ins = upload(ctx, p->ins);
   p->d_outs = upload(ctx, p->outs);
@@ -190,6 +194,12 @@ std::unique_ptr<MpoStep64> plan_mpo_step64(Ctx &ctx, FusedMpo &fm, const BTensor
   p->d_unit0 = upload(ctx, p->unit0);
   p->d_unit_pair = upload(ctx, p->unit_pair);
   ctx.sync();  // host vectors stay, but the uploads finish before they could move
+}
+
+std::unique_ptr<MpoStep64> plan_mpo_step64(Ctx &ctx, FusedMpo &fm, const BTensor &T1,
+                                           const BTensor &T3) {
+  auto p = build_mpo_step64(fm, T1, T3);
+  upload_mpo_step64(ctx, *p);
   return p;
 }
 

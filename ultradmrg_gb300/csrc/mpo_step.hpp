@@ -83,6 +83,10 @@ struct MpoStep64 {
 // Every T3 entry is written (zero where no coupling reaches it).
 std::unique_ptr<MpoStep64> plan_mpo_step64(Ctx &ctx, FusedMpo &fm, const BTensor &T1,
                                            const BTensor &T3);
+// The same in two parts: the host tables (no device call; safe on a host
+// thread with its own FusedMpo), then their upload.
+std::unique_ptr<MpoStep64> build_mpo_step64(FusedMpo &fm, const BTensor &T1, const BTensor &T3);
+void upload_mpo_step64(Ctx &ctx, MpoStep64 &p);
 void run_mpo_step64(Ctx &ctx, const MpoStep64 &p, const double *t1, double *t3);
 
 }  // namespace udmrg

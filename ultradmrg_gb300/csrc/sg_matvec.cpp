@@ -2,6 +2,7 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <map>
 
 namespace udmrg {
@@ -26,7 +27,7 @@ V *upload_vec(Ctx &ctx, const std::vector<V> &v) {
   return d;
 }
 
-using Key = std::vector<int32_t>;
+using Key = std::array<int32_t, 5>;  // (A', W, S1, S2, B)
 
 struct T1Block {
   int64_t origin;  // element offset of (a'=0, w=0, s1=s2=0, b=0)
@@ -40,10 +41,11 @@ inline int64_t up8(int64_t x) { return (x + 7) & ~(int64_t)7; }
 
 }  // namespace
 
-std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const BTensor &R,
-                                             const BTensor &S, FusedMpo &fm, int bn1, int bn3) {
+std::unique_ptr<SgMatvecPlan> plan_sg_tables(const BTensor &L, const BTensor &R, const BTensor &S,
+                                             FusedMpo &fm, int bn1, int bn3) {
   UDMRG_REQUIRE((bn1 == 64 || bn1 == 128) && (bn3 == 64 || bn3 == 128),
                 "mixed matvec: B tiles of 64 or 128 rows");
+  const auto tstart = std::chrono::steady_clock::now();
   // complex L, R, psi: the real embedding [[Re, -Im], [Im, Re]] (the MPO
   // coefficients are real, see FusedMpo)
   const bool cplx = S.dtype == kC128;
@@ -51,9 +53,6 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
                 "mixed matvec: L, R and psi must share the element type");
   const int64_t es = cplx ? 2 : 1;  // doubles per element
   auto p = std::make_unique<SgMatvecPlan>();
-  p->ctx = &ctx;
-  p->g1.ctx = &ctx;
-  p->g3.ctx = &ctx;
   p->psi_size = S.size();
   p->cplx = cplx;
   p->bn1 = bn1;
@@ -87,7 +86,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   for (int64_t b = 0; b < L.nblocks(); ++b) lrows[L.key(b)[2]].push_back(b);
   for (int64_t b = 0; b < S.nblocks(); ++b) pcols[S.key(b)[0]].push_back(b);
   std::map<Key, T1Block> t1map;  // (A', W, S1, S2, B) -> location in T1
-  std::vector<PackOp> lops;
+  std::vector<PackOp> &lops = p->l_ops;
   int64_t t1tot = 0, lbytes = 0, pbytes = 0;
   struct G1 {
     int A;
@@ -171,7 +170,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   std::vector<std::vector<int64_t>> rks(nB), orows(nB);
   for (int64_t b = 0; b < R.nblocks(); ++b) rks[R.key(b)[0]].push_back(b);
   for (int64_t b = 0; b < S.nblocks(); ++b) orows[S.key(b)[3]].push_back(b);
-  std::vector<PackOp> rops;
+  std::vector<PackOp> &rops = p->r_ops;
   int64_t t3bytes = 0, rbytes = 0;
   std::vector<std::pair<int32_t, int32_t>> tgt_key;  // (A', B) of every target
   // fused form: the group (its MpoGroupMap), row block and K block of every target
@@ -298,27 +297,11 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   p->t3_bytes = t3bytes;
   p->r_bytes = rbytes;
 
-  // ---------------- allocate, pack the fixed operands -------------------------
-  auto zalloc = [&](int64_t bytes) {
-    uint8_t *d = (uint8_t *)ctx.alloc(std::max<int64_t>(bytes, 256));
-    UDMRG_CHECK_CUDA(cudaMemsetAsync(d, 0, std::max<int64_t>(bytes, 256), ctx.stream));
-    return d;
-  };
-  p->l_img = zalloc(lbytes);
-  p->psi_img = zalloc(pbytes);
-  p->t3_img = zalloc(t3bytes);
-  p->r_img = zalloc(rbytes);
-  p->t1 = (float *)ctx.alloc(std::max<int64_t>(t1tot, 1) * sizeof(float));
-  run_pack(ctx, lops, L.data, true, p->l_img);
-  run_pack(ctx, rops, R.data, true, p->r_img);
-  p->psi_pack.upload(ctx);
   for (auto &g : g1s) {
     std::vector<int64_t> rows(g.Me);
     for (int64_t m = 0; m < g.Me; ++m) rows[m] = g.t1_off + m * g.Np;
     p->g1.add_group(g.l_off, g.p_off, (int32_t)g.Me, (int32_t)g.N, (int32_t)g.Ke, rows);
   }
-  p->g1.finalize();
-  p->g3.finalize();
   // ---------------- MPO step regrouped by (A', B) pair ------------------------
   {
     std::map<std::pair<int32_t, int32_t>, std::vector<int>> by_pair;
@@ -469,6 +452,31 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
       for (int64_t u0 = 0; u0 < units; u0 += 32) p->tasks.push_back({q, (int32_t)u0});
     }
   }
+  p->host_sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - tstart).count();
+  return p;
+}
+
+void plan_sg_device(Ctx &ctx, SgMatvecPlan &plan, const BTensor &L, const BTensor &R) {
+  const auto tstart = std::chrono::steady_clock::now();
+  SgMatvecPlan *p = &plan;
+  p->ctx = &ctx;
+  p->g1.ctx = &ctx;
+  p->g3.ctx = &ctx;
+  auto zalloc = [&](int64_t bytes) {
+    uint8_t *d = (uint8_t *)ctx.alloc(std::max<int64_t>(bytes, 256));
+    UDMRG_CHECK_CUDA(cudaMemsetAsync(d, 0, std::max<int64_t>(bytes, 256), ctx.stream));
+    return d;
+  };
+  p->l_img = zalloc(p->l_bytes);
+  p->psi_img = zalloc(p->psi_bytes);
+  p->t3_img = zalloc(p->t3_bytes);
+  p->r_img = zalloc(p->r_bytes);
+  p->t1 = (float *)ctx.alloc(std::max<int64_t>(p->t1_size, 1) * sizeof(float));
+  run_pack(ctx, p->l_ops, L.data, true, p->l_img);
+  run_pack(ctx, p->r_ops, R.data, true, p->r_img);
+  p->psi_pack.upload(ctx);
+  p->g1.finalize();
+  p->g3.finalize();
   p->d_pairs = upload_vec(ctx, p->pairs);
   p->d_outs = upload_vec(ctx, p->outs);
   p->d_rowptr = upload_vec(ctx, p->rowptr);
@@ -480,12 +488,19 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const B
   p->d_tgtref = upload_vec(ctx, p->tgtref);
   p->mixed_flops = 6.0 * (p->g1.flops + p->g3.flops);
   ctx.sync();
+  std::vector<PackOp>().swap(p->l_ops);  // packed; the host copies go
+  std::vector<PackOp>().swap(p->r_ops);
+  p->dev_sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - tstart).count();
+}
+
+std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const BTensor &R,
+                                             const BTensor &S, FusedMpo &fm, int bn1, int bn3) {
+  auto p = plan_sg_tables(L, R, S, fm, bn1, bn3);
+  plan_sg_device(ctx, *p, L, R);
   return p;
 }
 
-std::unique_ptr<SgMatvecPlan> plan_sg_matvec_tuned(Ctx &ctx, const BTensor &L, const BTensor &R,
-                                                   const BTensor &S, FusedMpo &fm) {
-  if (ctx.tc_bn1 && ctx.tc_bn3) return plan_sg_matvec(ctx, L, R, S, fm, ctx.tc_bn1, ctx.tc_bn3);
+std::array<int64_t, 3> sg_shape_class(const BTensor &S) {
   auto lg2 = [](int64_t x) {
     int64_t k = 0;
     while ((int64_t(1) << k) < x) ++k;
@@ -493,7 +508,26 @@ std::unique_ptr<SgMatvecPlan> plan_sg_matvec_tuned(Ctx &ctx, const BTensor &L, c
   };
   int64_t maxb = 1;
   for (int64_t d : S.idx[3].dims) maxb = std::max(maxb, d);
-  const std::array<int64_t, 3> key = {S.dtype == kC128 ? 1 : 0, lg2(S.size()), lg2(maxb)};
+  return {S.dtype == kC128 ? 1 : 0, lg2(S.size()), lg2(maxb)};
+}
+
+bool sg_tiles_known(const Ctx &ctx, const BTensor &S, int *bn1, int *bn3) {
+  if (ctx.tc_bn1 && ctx.tc_bn3) {
+    *bn1 = ctx.tc_bn1;
+    *bn3 = ctx.tc_bn3;
+    return true;
+  }
+  auto it = ctx.tc_tuned.find(sg_shape_class(S));
+  if (it == ctx.tc_tuned.end()) return false;
+  *bn1 = it->second[0];
+  *bn3 = it->second[1];
+  return true;
+}
+
+std::unique_ptr<SgMatvecPlan> plan_sg_matvec_tuned(Ctx &ctx, const BTensor &L, const BTensor &R,
+                                                   const BTensor &S, FusedMpo &fm) {
+  if (ctx.tc_bn1 && ctx.tc_bn3) return plan_sg_matvec(ctx, L, R, S, fm, ctx.tc_bn1, ctx.tc_bn3);
+  const std::array<int64_t, 3> key = sg_shape_class(S);
   auto it = ctx.tc_tuned.find(key);
   if (it != ctx.tc_tuned.end()) {
     auto p = plan_sg_matvec(ctx, L, R, S, fm, it->second[0], it->second[1]);

@@ -160,6 +160,11 @@ struct SgMatvecPlan {
   double mixed_flops = 0;  // tensor-core work actually issued (2MNK per group, x6 products)
   double mpo_bytes = 0;    // MPO step: 4 B per T1 entry read, 3 x 2 B per T3 entry written
   double t1_read_bytes = 0;  // 4 B per T1 entry the MPO step reads
+  // host seconds spent building this plan: its tables (host_sec) and its
+  // device part (allocations, operand packing, uploads; dev_sec)
+  double host_sec = 0, dev_sec = 0;
+  // planning only: the pack ops of L's and R's images (dropped once packed)
+  std::vector<PackOp> l_ops, r_ops;
   ~SgMatvecPlan();
   void apply(const double *psi_in, double *out);
   // apply with CUDA events between the stages: ms[0] psi pack, ms[1] GEMM
@@ -173,13 +178,23 @@ struct SgMatvecPlan {
 std::unique_ptr<SgMatvecPlan> plan_sg_matvec(Ctx &ctx, const BTensor &L, const BTensor &R,
                                              const BTensor &S, FusedMpo &fm, int bn1 = kTcBN,
                                              int bn3 = kTcBN);
+// The same in two parts: the host tables (no device call, so it may run on a
+// host thread, with a FusedMpo of its own), then the device part (images
+// allocated and packed from L's and R's data, tables uploaded).
+std::unique_ptr<SgMatvecPlan> plan_sg_tables(const BTensor &L, const BTensor &R, const BTensor &S,
+                                             FusedMpo &fm, int bn1, int bn3);
+void plan_sg_device(Ctx &ctx, SgMatvecPlan &p, const BTensor &L, const BTensor &R);
+// Shape class of the tile autotuner: element type, log2 of the Krylov
+// structure's size, log2 of its largest right-bond sector.
+std::array<int64_t, 3> sg_shape_class(const BTensor &S);
+// B-tile rows fixed by the context or already chosen for S's shape class.
+bool sg_tiles_known(const Ctx &ctx, const BTensor &S, int *bn1, int *bn3);
 
 // The plan with the B-tile rows of the context (ctx.tc_bn1 / tc_bn3), or, where
-// those are 0, the tile autotuner's: the first plan of a shape class (element
-// type, log2 of the Krylov structure's size, log2 of its largest right-bond
-// sector) is built with 64- and with 128-row B tiles, one matvec of each is
-// timed per stage (CUDA events, best of two), and each GEMM keeps its faster
-// tile; later plans of the class reuse the choice.
+// those are 0, the tile autotuner's: the first plan of a shape class is built
+// with 64- and with 128-row B tiles, matvecs of the two alternate over four
+// trials timed per stage (CUDA events, best of four), and each GEMM keeps its
+// faster tile; later plans of the class reuse the choice.
 std::unique_ptr<SgMatvecPlan> plan_sg_matvec_tuned(Ctx &ctx, const BTensor &L, const BTensor &R,
                                                    const BTensor &S, FusedMpo &fm);
 
