@@ -476,6 +476,19 @@ def run_ours(args):
         del pf64, pfmx
     gemm["trials_run"], gemm["classes"] = ctx.gemm_tuning()
     tune["fp64_gemm_tiles"] = gemm
+    # host planning of a warm plan (tile choices cached): wall time and the
+    # plan's own build phases (host tables on host threads), median of three
+    builds = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        pw = api.MatvecPlan(ctx, ops, psi, precision=api.PREC_MIXED)
+        builds.append((time.perf_counter() - t0, pw.build_times()))
+        del pw
+    builds.sort(key=lambda b_: b_[0])
+    plan_build = {"first_plan_ms_with_trials": plan_s * 1e3,
+                  "warm_plan_ms": builds[1][0] * 1e3,
+                  "warm_phases_ms": {k: v * 1e3 for k, v in builds[1][1].items()},
+                  "first_phases_ms": {k: v * 1e3 for k, v in plan.build_times().items()}}
     # Lanczos energies of both forms from the same start vector, to convergence
     lz = {}
     for name, prec in (("mixed", api.PREC_MIXED), ("fp64", api.PREC_FP64)):
@@ -639,6 +652,7 @@ def run_ours(args):
                      "lanczos_rel_dE": abs(lz["mixed"][0] - lz["fp64"][0]) / abs(lz["fp64"][0])},
         "krylov_graph": kg,
         "tile_autotuner": tune,
+        "plan_build": plan_build,
         "centre_site_update": {
             k: {kk: v[kk] for kk in ("wall_sec", "lancz_sec", "svd_sec", "env_sec", "iters", "D",
                                      "trunc_err", "e0", "svd_grow_rounds")}

@@ -44,14 +44,42 @@ TensorPtr to_complex(Ctx &ctx, const BTensor &A) {
   return t;
 }
 
+// Block lists are sorted and unique, so union and difference are merges.
+static int key_cmp(const int32_t *x, const int32_t *y, int r) {
+  for (int i = 0; i < r; ++i)
+    if (x[i] != y[i]) return x[i] < y[i] ? -1 : 1;
+  return 0;
+}
+
 TensorPtr struct_union(const BTensor &a, const BTensor &b) {
   UDMRG_REQUIRE(a.rank() == b.rank(), "union: rank mismatch");
   for (int i = 0; i < a.rank(); ++i) UDMRG_REQUIRE(a.idx[i] == b.idx[i], "union: index mismatch");
-  std::vector<int32_t> flat = a.keys;
-  flat.insert(flat.end(), b.keys.begin(), b.keys.end());
+  const int r = a.rank();
+  const int64_t na = a.nblocks(), nb = b.nblocks();
+  std::vector<int32_t> flat;
+  flat.reserve((size_t)(na + nb) * r);
+  for (int64_t i = 0, j = 0; i < na || j < nb;) {
+    const int c = i == na ? 1 : j == nb ? -1 : key_cmp(a.key(i), b.key(j), r);
+    const int32_t *k = c <= 0 ? a.key(i) : b.key(j);
+    flat.insert(flat.end(), k, k + r);
+    if (c <= 0) ++i;
+    if (c >= 0) ++j;
+  }
   auto t = a.clone_struct();
-  t->set_blocks(sort_keys(flat, a.rank()));
+  t->set_blocks(std::move(flat));
   return t;
+}
+
+// keys of b's blocks that a lacks (flat, sorted)
+static std::vector<int32_t> struct_minus(const BTensor &b, const BTensor &a) {
+  const int r = b.rank();
+  std::vector<int32_t> out;
+  for (int64_t i = 0, j = 0; j < b.nblocks(); ++j) {
+    while (i < a.nblocks() && key_cmp(a.key(i), b.key(j), r) < 0) ++i;
+    if (i == a.nblocks() || key_cmp(a.key(i), b.key(j), r) != 0)
+      out.insert(out.end(), b.key(j), b.key(j) + r);
+  }
+  return out;
 }
 
 TensorPtr embed(Ctx &ctx, const BTensor &src, const BTensor &dst_struct) {
@@ -164,24 +192,34 @@ std::unique_ptr<MatvecPlan> plan_matvec2(Ctx &ctx, const BTensor &L, const BTens
     tmark = t;
     return s;
   };
-  // the Krylov structure: block structures only until it closes
-  TensorPtr S = psi0.clone_struct();
+  // the Krylov structure: block structures only until it closes.  A
+  // contraction's block set is the union over its operands' blocks, so each
+  // round propagates only the blocks the previous one added (D) and the
+  // intermediates' structures grow by union.
+  TensorPtr S = psi0.clone_struct(), D = psi0.clone_struct();
   TensorPtr s1, s2, s3;  // the three intermediates' structures for the closed S
   std::vector<int> ca1, cb1, fa1, fb1, ca2, cb2, fa2, fb2, ca3, cb3, fa3, fb3, ca, cb, fa, fb;
   cyclic_axes(3, 4, 2, 0, 1, ca1, cb1, fa1, fb1);  // L(a', w, a) . psi(a, s1, s2, b)
   cyclic_axes(5, 4, 1, 0, 2, ca2, cb2, fa2, fb2);
   cyclic_axes(5, 4, 4, 0, 2, ca3, cb3, fa3, fb3);
   cyclic_axes(5, 3, 4, 1, 2, ca, cb, fa, fb);
-  for (int it = 0; it < 16; ++it) {
-    s1 = contract_struct(L, *S, ca1, cb1, fa1, fb1);
-    s2 = contract_struct(*s1, W1, ca2, cb2, fa2, fb2);
-    s3 = contract_struct(*s2, W2, ca3, cb3, fa3, fb3);
-    auto s4 = contract_struct(*s3, R, ca, cb, fa, fb);
-    auto U = struct_union(*S, *s4);
-    const bool closed = U->keys == S->keys;
-    S = std::move(U);
-    if (closed) break;
-    UDMRG_REQUIRE(it < 15, "matvec: Krylov block structure did not close");
+  auto grow = [](TensorPtr &acc, TensorPtr d) {
+    acc = acc ? struct_union(*acc, *d) : std::move(d);
+  };
+  for (int it = 0;; ++it) {
+    UDMRG_REQUIRE(it < 16, "matvec: Krylov block structure did not close");
+    auto d1 = contract_struct(L, *D, ca1, cb1, fa1, fb1);
+    auto d2 = contract_struct(*d1, W1, ca2, cb2, fa2, fb2);
+    auto d3 = contract_struct(*d2, W2, ca3, cb3, fa3, fb3);
+    auto d4 = contract_struct(*d3, R, ca, cb, fa, fb);
+    grow(s1, std::move(d1));
+    grow(s2, std::move(d2));
+    grow(s3, std::move(d3));
+    std::vector<int32_t> fresh = struct_minus(*d4, *S);  // blocks not in S yet
+    if (fresh.empty()) break;
+    D = S->clone_struct();
+    D->set_blocks(fresh);
+    S = struct_union(*S, *D);
   }
   mv->build_sec[0] = lap();
   mv->precision = precision;

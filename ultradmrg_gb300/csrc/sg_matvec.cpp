@@ -4,6 +4,7 @@
 #include <array>
 #include <chrono>
 #include <map>
+#include <unordered_map>
 
 namespace udmrg {
 
@@ -28,6 +29,13 @@ V *upload_vec(Ctx &ctx, const std::vector<V> &v) {
 }
 
 using Key = std::array<int32_t, 5>;  // (A', W, S1, S2, B)
+struct T1KeyHash {
+  size_t operator()(const Key &k) const {
+    uint64_t h = 0x9e3779b97f4a7c15ull;
+    for (int32_t v : k) h = (h ^ (uint32_t)v) * 0x100000001b3ull + (h >> 29);
+    return (size_t)h;
+  }
+};
 
 struct T1Block {
   int64_t origin;  // element offset of (a'=0, w=0, s1=s2=0, b=0)
@@ -85,7 +93,12 @@ std::unique_ptr<SgMatvecPlan> plan_sg_tables(const BTensor &L, const BTensor &R,
   std::vector<std::vector<int64_t>> lrows(nA), pcols(nA);
   for (int64_t b = 0; b < L.nblocks(); ++b) lrows[L.key(b)[2]].push_back(b);
   for (int64_t b = 0; b < S.nblocks(); ++b) pcols[S.key(b)[0]].push_back(b);
-  std::map<Key, T1Block> t1map;  // (A', W, S1, S2, B) -> location in T1
+  std::unordered_map<Key, T1Block, T1KeyHash> t1map;  // (A', W, S1, S2, B) -> location in T1
+  {
+    size_t n = 0;
+    for (int A = 0; A < nA; ++A) n += lrows[A].size() * pcols[A].size();
+    t1map.reserve(n);
+  }
   std::vector<PackOp> &lops = p->l_ops;
   int64_t t1tot = 0, lbytes = 0, pbytes = 0;
   struct G1 {
@@ -304,8 +317,19 @@ std::unique_ptr<SgMatvecPlan> plan_sg_tables(const BTensor &L, const BTensor &R,
   }
   // ---------------- MPO step regrouped by (A', B) pair ------------------------
   {
-    std::map<std::pair<int32_t, int32_t>, std::vector<int>> by_pair;
-    for (size_t t = 0; t < p->targets.size(); ++t) by_pair[tgt_key[t]].push_back((int)t);
+    // targets by (A', B) pair, pairs ascending, targets in plan order
+    std::vector<std::pair<std::pair<int32_t, int32_t>, std::vector<int>>> by_pair;
+    {
+      std::vector<int> ord(p->targets.size());
+      for (size_t t = 0; t < ord.size(); ++t) ord[t] = (int)t;
+      std::stable_sort(ord.begin(), ord.end(),
+                       [&](int x, int y) { return tgt_key[x] < tgt_key[y]; });
+      for (int t : ord) {
+        if (by_pair.empty() || by_pair.back().first != tgt_key[t])
+          by_pair.push_back({tgt_key[t], {}});
+        by_pair.back().second.push_back(t);
+      }
+    }
     // per pair: its input channels' T1 locations (real part), output channels
     // and coefficient nonzeros (o, i, v); the imaginary twin of a complex pair
     // shifts the inputs by the group's real row count and the outputs by the
@@ -333,13 +357,19 @@ std::unique_ptr<SgMatvecPlan> plan_sg_tables(const BTensor &L, const BTensor &R,
       pr.db = t0.db;
       pr.dbp = t0.dbp;
       // input channels: one per (w, s1 s2) of every distinct source block
-      std::map<int64_t, int32_t> in_first;  // T1 origin -> first channel
+      // T1 origin -> first channel (a pair has few source blocks)
+      std::vector<std::pair<int64_t, int32_t>> in_first;
+      auto first_of = [&](int64_t off) {
+        for (const auto &f : in_first)
+          if (f.first == off) return f.second;
+        return -1;
+      };
       for (int t : kv.second) {
         const MpoTarget &tg = p->targets[t];
         for (int s = 0; s < tg.nsrc; ++s) {
           const MpoSource &sr = p->sources[tg.src0 + s];
-          if (in_first.count(sr.t1_off)) continue;
-          in_first[sr.t1_off] = (int32_t)(p->ins.size() - pr.in0);
+          if (first_of(sr.t1_off) >= 0) continue;
+          in_first.push_back({sr.t1_off, (int32_t)(p->ins.size() - pr.in0)});
           for (int w = 0; w < sr.dw; ++w)
             for (int s12 = 0; s12 < sr.ds12; ++s12) {
               p->ins.push_back({sr.t1_off + (int64_t)w * sr.row_pitch + (int64_t)s12 * sr.bstride,
@@ -370,7 +400,7 @@ std::unique_ptr<SgMatvecPlan> plan_sg_tables(const BTensor &L, const BTensor &R,
         const MpoTarget &tg = p->targets[kv.second[j]];
         for (int s = 0; s < tg.nsrc; ++s) {
           const MpoSource &sr = p->sources[tg.src0 + s];
-          const int i0 = in_first[sr.t1_off];
+          const int i0 = first_of(sr.t1_off);
           const int nin_s = sr.dw * sr.ds12;
           for (int ic = 0; ic < nin_s; ++ic)
             for (int oc = 0; oc < tg.nout; ++oc)
