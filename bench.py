@@ -578,6 +578,7 @@ def run_ours(args):
     from ultradmrg_gb300 import _lib
     x.download_packed()  # warm the path
     _lib.call("udmrg_tensor_download", x.h, ctypes.cast(hxp, _lib.c_double_p))  # psi -> host
+    host_mapped_default = ctx.host_mapped()
     for _ in range(2):
         plan.apply_host_ptr(hxp, hyp)
     e0 = time.perf_counter()
@@ -587,6 +588,22 @@ def run_ours(args):
     step()  # the device-buffer product of the same input: the host result must equal it
     e2e_same = bool(np.array_equal(y.download_packed(),
                                    hy.numpy() if hasattr(hy, "numpy") else hy))
+    # the same call with each host-buffer mode (copies, input read in place,
+    # input and output in place); the line's e2e uses the context's default
+    e2e_modes = {}
+    want = y.download_packed()
+    for mode in (0, 1, 2):
+        ctx.set_host_mapped(mode)
+        for _ in range(2):
+            plan.apply_host_ptr(hxp, hyp)
+        nrep = min(args.steps, 500)
+        e0 = time.perf_counter()
+        for _ in range(nrep):
+            plan.apply_host_ptr(hxp, hyp)
+        tm = (time.perf_counter() - e0) / nrep
+        same = bool(np.array_equal(want, hy.numpy() if hasattr(hy, "numpy") else hy))
+        e2e_modes[str(mode)] = {"tflops": flops / tm / 1e12, "ms": tm * 1e3, "matches": same}
+    ctx.set_host_mapped(host_mapped_default)
     if ws > 1:
         tt = torch.tensor([e2e_t], dtype=torch.float64)
         tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
@@ -636,7 +653,8 @@ def run_ours(args):
                    "plan_seconds": plan_s},
         "gpu_launches": launches,
         "e2e": {"value": e2e_val, "unit": "TFLOP/s", "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": nbytes, "matches_device_result": e2e_same},
+                "d2h_bytes_per_step": nbytes, "matches_device_result": e2e_same,
+                "host_mapped": host_mapped_default, "by_host_mapped": e2e_modes},
         "roofline": roof,
         "plain_fp64": {"value": flops / t64 / 1e12, "unit": "TFLOP/s", "ms_per_step": t64 * 1e3,
                        "roofline": {"bound": "fp64", "peak": fp64_peak,

@@ -123,6 +123,15 @@ int udmrg_ctx_set_krylov_graph(udmrg_ctx *ctx, int enable);
  * plain FP64 form is not affected.  Replaces nothing in qlmps (its matvec
  * is FP64 throughout). */
 int udmrg_ctx_set_anchor_dw(udmrg_ctx *ctx, int dw);
+/* Host buffers of udmrg_matvec_plan_apply_host that are page-locked and
+ * mapped into the device's address space (cudaMallocHost, cudaHostAlloc,
+ * cudaHostRegister with mapping) are used in place by a mixed-precision
+ * plan: mode 0 never (one copy each way through device buffers), 1 the input
+ * (read by the psi pack over the host link), 2 input and output (the result
+ * written by the last GEMM's epilogue).  Pageable memory is always copied.
+ * No counterpart in the reference (its matvec takes host tensors). */
+int udmrg_ctx_set_host_mapped(udmrg_ctx *ctx, int mode);
+int udmrg_ctx_host_mapped(const udmrg_ctx *ctx, int *mode);
 /* Mixed matvec: rows of the B tiles of the two tcgen05 GEMMs (L.psi: bn1,
  * .R: bn3), 64 or 128, or 0 for the tile autotuner (the default): the first
  * plan of a shape class is built with both tiles, one matvec of each is timed
@@ -379,10 +388,12 @@ int udmrg_matvec_plan_info(const udmrg_matvec_plan *p, double *flops, int64_t *p
 int udmrg_matvec_plan_embed(udmrg_matvec_plan *p, const udmrg_tensor *src, udmrg_tensor **out);
 /* out = H_eff * in on device buffers laid out in the Krylov structure. */
 int udmrg_matvec_plan_apply(udmrg_matvec_plan *p, const double *d_in, double *d_out);
-/* out = H_eff * in with host buffers (packed Krylov-structure layout): one
- * call copies in, applies and copies out on the context's stream, then
- * waits (pinned host memory gives full copy bandwidth).  The plan keeps two
- * device buffers for it.  The host-facing form of eff_ham_mul_two_site_state
+/* out = H_eff * in with host buffers of psi_size elements each (packed
+ * Krylov-structure layout): one call copies in, applies and copies out on
+ * the context's stream, then waits (pinned host memory gives full copy
+ * bandwidth; with udmrg_ctx_set_host_mapped a mixed plan uses mapped pinned
+ * buffers in place instead).  The plan keeps two device buffers for the
+ * copies.  The host-facing form of eff_ham_mul_two_site_state
  * (lanczos_vmps_solver_impl.h:250-289). */
 int udmrg_matvec_plan_apply_host(udmrg_matvec_plan *p, const double *h_in, double *h_out);
 /* The same product in the mixed solver's anchor form (FP64 pipe or

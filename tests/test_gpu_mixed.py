@@ -207,6 +207,38 @@ def test_plan_host_threads_bit_identical(ctx):
             assert np.array_equal(out[0][k], out[rep][k])
 
 
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_apply_host_modes(ctx, mode):
+    """apply_host with page-locked buffers (used in place under modes 1 and 2)
+    and with pageable ones (always copied): the device-buffer product, bit for
+    bit, every entry written."""
+    torch = pytest.importorskip("torch")
+    mpo, mps = SYSTEMS["hub_big"]()
+    eff, psi = two_site_problem(mpo, mps, 3)
+    dev = [up(ctx, t) for t in eff]
+    dpsi = up(ctx, psi)
+    plan = api.MatvecPlan(ctx, dev, dpsi, precision=MIXED)
+    x, y = plan.embed(dpsi), plan.embed(dpsi)
+    plan.apply(x, y)
+    want = y.download_packed()
+    xin = x.download_packed()
+    n = xin.size
+    before = ctx.host_mapped()
+    try:
+        ctx.set_host_mapped(mode)
+        assert ctx.host_mapped() == mode
+        hx = torch.from_numpy(xin.copy()).pin_memory()
+        hy = torch.full((n,), float("nan"), dtype=torch.float64).pin_memory()
+        for _ in range(2):
+            plan.apply_host_ptr(hx.data_ptr(), hy.data_ptr())
+            assert np.array_equal(hy.numpy(), want)
+        px, py = xin.copy(), np.full(n, np.nan)
+        plan.apply_host_ptr(px.ctypes.data, py.ctypes.data)
+        assert np.array_equal(py, want)
+    finally:
+        ctx.set_host_mapped(before)
+
+
 def _gpu_vmps(ctx, mpo, pb, labels, params):
     mps0 = M.direct_product_mps([pb] * len(labels), labels)
     dmps = [up(ctx, t) for t in mps0]

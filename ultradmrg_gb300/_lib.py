@@ -80,6 +80,8 @@ SIGNATURES = {
     "udmrg_ctx_set_gemm_tiles": [C.c_void_p, C.c_int],
     "udmrg_ctx_gemm_tuning": [C.c_void_p, c_int64_p, c_int64_p],
     "udmrg_ctx_set_anchor_dw": [C.c_void_p, C.c_int],
+    "udmrg_ctx_set_host_mapped": [C.c_void_p, C.c_int],
+    "udmrg_ctx_host_mapped": [C.c_void_p, C.POINTER(C.c_int)],
     "udmrg_tensor_create": [C.c_void_p, C.c_int, C.c_int, C.c_int, c_int32_p, c_int32_p,
                             c_int64_p, c_int32_p, C.c_int64, c_int32_p, c_void_pp],
     "udmrg_tensor_destroy": [C.c_void_p],

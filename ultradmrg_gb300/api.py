@@ -64,6 +64,18 @@ class Context:
         arithmetic (default) or on the FP64 pipe."""
         call("udmrg_ctx_set_anchor_dw", self.h, 1 if dw else 0)
 
+    def set_host_mapped(self, mode: int):
+        """MatvecPlan.apply_host_ptr with page-locked, device-mapped host
+        buffers (a mixed-precision plan): 0 copies both ways, 1 reads the
+        input in place, 2 also writes the output in place."""
+        call("udmrg_ctx_set_host_mapped", self.h, int(mode))
+
+    def host_mapped(self) -> int:
+        """The host-buffer mode of apply_host_ptr (see set_host_mapped)."""
+        v = C.c_int()
+        call("udmrg_ctx_host_mapped", self.h, C.byref(v))
+        return v.value
+
     def profiler_range(self, start: bool):
         """Start or stop the CUDA profiler's collection after this context's
         work so far (for a profiler run with collection off at start)."""

@@ -58,6 +58,13 @@ struct Ctx {
   // The mixed solver's FP64-accurate anchor matvec: its two block-GEMM stages
   // in double-word FP32 arithmetic (true) or on the FP64 pipe (false)
   bool anchor_dw = true;
+  // Host buffers of udmrg_matvec_plan_apply_host that are page-locked and
+  // mapped into the device's address space (cudaMallocHost / cudaHostAlloc /
+  // cudaHostRegister) are used in place by the mixed matvec: 0 never (one
+  // copy each way through device buffers), 1 the input (the psi pack reads
+  // it over the host link), 2 input and output (the .R GEMM's epilogue also
+  // writes the result there).  Other host memory is always copied.
+  int host_mapped = 0;
   // Set while a mixed-precision update runs its SVD with anchor_dw: the SVD's
   // Newton-Schulz and factor products in double-word arithmetic (its Gram
   // products stay on the FP64 pipe)

@@ -170,6 +170,21 @@ int udmrg_ctx_set_anchor_dw(udmrg_ctx *c, int dw) {
   });
 }
 
+int udmrg_ctx_set_host_mapped(udmrg_ctx *c, int mode) {
+  return guarded([&] {
+    UDMRG_REQUIRE(c, "null argument");
+    UDMRG_REQUIRE(mode >= 0 && mode <= 2, "host_mapped: mode 0, 1 or 2");
+    c->ctx.host_mapped = mode;
+  });
+}
+
+int udmrg_ctx_host_mapped(const udmrg_ctx *c, int *mode) {
+  return guarded([&] {
+    UDMRG_REQUIRE(c && mode, "null argument");
+    *mode = c->ctx.host_mapped;
+  });
+}
+
 int udmrg_ctx_set_krylov_graph(udmrg_ctx *c, int enable) {
   return guarded([&] {
     UDMRG_REQUIRE(c, "null argument");
@@ -878,19 +893,50 @@ int udmrg_matvec_plan_apply(udmrg_matvec_plan *p, const double *d_in, double *d_
   return guarded([&] { p->plan->apply(d_in, d_out); });
 }
 
+// Device address of a page-locked, device-mapped host buffer of `bytes`
+// bytes, or null: its first and last bytes must both be page-locked host
+// memory mapped at the same distance apart in the device's address space.
+static void *mapped_host(const void *h, size_t bytes) {
+  if (!h || !bytes) return nullptr;
+  cudaPointerAttributes a{}, z{};
+  const char *last = (const char *)h + bytes - 1;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess ||
+      cudaPointerGetAttributes(&z, last) != cudaSuccess) {
+    cudaGetLastError();  // not an address the runtime knows: copied
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || z.type != cudaMemoryTypeHost || !a.devicePointer ||
+      !z.devicePointer)
+    return nullptr;
+  if ((const char *)z.devicePointer - (const char *)a.devicePointer != (ptrdiff_t)(bytes - 1))
+    return nullptr;
+  return a.devicePointer;
+}
+
 int udmrg_matvec_plan_apply_host(udmrg_matvec_plan *p, const double *h_in, double *h_out) {
   return guarded([&] {
     MatvecPlan &m = *p->plan;
     Ctx &ctx = *p->ctx;
     const size_t bytes = (size_t)m.sstruct->size() * elem_doubles(m.sstruct->dtype) * sizeof(double);
-    if (!p->host_in) {
+    // the mixed form reads its input once (the psi pack) and writes its
+    // output once (the .R GEMM's epilogue, every entry): both may live in
+    // mapped host memory
+    const bool mixed = m.sg != nullptr;
+    const double *d_in =
+        mixed && ctx.host_mapped >= 1 ? (const double *)mapped_host(h_in, bytes) : nullptr;
+    double *d_out = mixed && ctx.host_mapped >= 2 ? (double *)mapped_host(h_out, bytes) : nullptr;
+    if ((!d_in || !d_out) && !p->host_in) {
       p->host_in = (double *)ctx.alloc(std::max<size_t>(bytes, 8));
       p->host_out = (double *)ctx.alloc(std::max<size_t>(bytes, 8));
     }
-    if (bytes)
-      UDMRG_CHECK_CUDA(cudaMemcpyAsync(p->host_in, h_in, bytes, cudaMemcpyHostToDevice, ctx.stream));
-    m.apply(p->host_in, p->host_out);
-    if (bytes)
+    if (!d_in) {
+      if (bytes)
+        UDMRG_CHECK_CUDA(
+            cudaMemcpyAsync(p->host_in, h_in, bytes, cudaMemcpyHostToDevice, ctx.stream));
+      d_in = p->host_in;
+    }
+    m.apply(d_in, d_out ? d_out : p->host_out);
+    if (!d_out && bytes)
       UDMRG_CHECK_CUDA(
           cudaMemcpyAsync(h_out, p->host_out, bytes, cudaMemcpyDeviceToHost, ctx.stream));
     ctx.sync();
