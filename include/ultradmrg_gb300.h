@@ -134,8 +134,9 @@ int udmrg_ctx_set_host_mapped(udmrg_ctx *ctx, int mode);
 int udmrg_ctx_host_mapped(const udmrg_ctx *ctx, int *mode);
 /* Mixed matvec: rows of the B tiles of the two tcgen05 GEMMs (L.psi: bn1,
  * .R: bn3), 64 or 128, or 0 for the tile autotuner (the default): the first
- * plan of a shape class is built with both tiles, one matvec of each is timed
- * stage by stage, each GEMM keeps its faster tile and later plans of the class
+ * plan of a shape class is built with both tiles, matvecs of the two alternate
+ * over four trials timed stage by stage (best of four), each GEMM keeps its
+ * faster tile and later plans of the class
  * reuse the choice.  udmrg_ctx_tc_tuning reports the trials run and the shape
  * classes decided.  No counterpart in the reference (tile tuning of the GB300
  * kernels). */
