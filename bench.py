@@ -510,6 +510,17 @@ def run_ours(args):
         kg[f"{sw.name}_{tag}"] = krylov_graph_probe(api, ctx, [sL, sW1, sW2, sR], spsi, prec)
     for t in (sL, sR, sA1, sA2, spsi, sW1, sW2):
         t.close()
+    # HBM rates of the Lanczos vector kernels on vectors of this workload's
+    # Krylov structure size, at three step counts (device-timed, best of four)
+    kvec = {"n": info["psi_size"], "hbm_peak_gbs": measured_peaks().get("hbm_gbs", 6800.0)}
+    for s_ in (10, 35, 70):
+        pr = ctx.krylov_step_probe(info["psi_size"], s_)
+        row = {}
+        for k_, t_ in pr["ms"].items():
+            b_ = pr["bytes"][k_]
+            row[k_] = {"ms": t_, "gbs": b_ / (t_ * 1e-3) / 1e9 if b_ > 0 and t_ > 0 else None}
+        row["second_pass_ran"] = pr["second_pass_ran"]
+        kvec[f"step{s_}"] = row
     # one full local update at the centre bond (Lanczos to 1e-9 as the reference
     # benchmark, truncated SVD to D, environment update) in three forms: plain
     # FP64 + exact SVD, mixed + exact SVD, mixed + randomized SVD sized from the
@@ -669,6 +680,7 @@ def run_ours(args):
                      "lanczos_iters": [lz["mixed"][1], lz["fp64"][1]],
                      "lanczos_rel_dE": abs(lz["mixed"][0] - lz["fp64"][0]) / abs(lz["fp64"][0])},
         "krylov_graph": kg,
+        "krylov_vector_ops": kvec,
         "tile_autotuner": tune,
         "plan_build": plan_build,
         "centre_site_update": {

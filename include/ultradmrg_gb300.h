@@ -445,6 +445,15 @@ int udmrg_matvec_plan_build_times(const udmrg_matvec_plan *p, double *sec);
 /* FP64 FMA throughput of the device (TFLOP/s), measured by a DFMA-bound
  * kernel; the roofline denominator of the plain FP64 block GEMMs. */
 int udmrg_probe_fp64_tflops(udmrg_ctx *ctx, double *tflops);
+/* HBM rates of the Lanczos vector kernels: one Krylov step's kernels at step
+ * `step` (1 .. 509) on random vectors of n doubles, device-timed (best of
+ * four): ms[0] normalisation, ms[1] alpha, ms[2] three-term update, ms[3]
+ * the first re-orthogonalisation pass against v_0 .. v_step, ms[4] the
+ * second, gated pass; bytes[i] the bytes each moves (0 where the gate
+ * skipped the second pass, *second_pass_ran = 0).  Measurement aid, no
+ * reference counterpart. */
+int udmrg_probe_krylov_step(udmrg_ctx *ctx, int64_t n, int step, double *ms, double *bytes,
+                            int *second_pass_ran);
 /* CUDA events on the context's stream (slot in [0, 1024)), elapsed ms
  * between two recorded slots, and an L2 flush (a write of `bytes` bytes to
  * a scratch buffer, stream ordered) for cold-cache timing. */

@@ -146,3 +146,19 @@ def test_vmps_graph_identical(ctx):
     (a, l0), (b, l1) = both_modes(ctx, run)
     assert a == b
     assert l0 == l1
+
+
+def test_krylov_step_probe(ctx):
+    """The vector-kernel probe times every kernel of one step and counts the
+    bytes each moves: 3, 2 and 4 vectors for normalise, alpha and update,
+    2 (s + 1) + 3 for a re-orthogonalisation pass against v_0 .. v_s."""
+    n, s = 200_003, 6
+    pr = ctx.krylov_step_probe(n, s)
+    v = 8.0 * n
+    assert pr["bytes"]["normalise"] == 3 * v
+    assert pr["bytes"]["alpha"] == 2 * v
+    assert pr["bytes"]["update"] == 4 * v
+    assert pr["bytes"]["reorth_pass1"] == (2 * (s + 1) + 3) * v
+    assert pr["bytes"]["reorth_pass2"] == (pr["bytes"]["reorth_pass1"] if pr["second_pass_ran"]
+                                           else 0.0)
+    assert all(t > 0.0 for t in pr["ms"].values())

@@ -163,6 +163,8 @@ SIGNATURES = {
     "udmrg_matvec_plan_gemm_policy": [C.c_void_p, C.POINTER(C.c_int)],
     "udmrg_matvec_plan_build_times": [C.c_void_p, c_double_p],
     "udmrg_probe_fp64_tflops": [C.c_void_p, c_double_p],
+    "udmrg_probe_krylov_step": [C.c_void_p, C.c_int64, C.c_int, c_double_p, c_double_p,
+                                C.POINTER(C.c_int)],
     "udmrg_ctx_event_record": [C.c_void_p, C.c_int],
     "udmrg_ctx_event_elapsed": [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)],
     "udmrg_ctx_flush_l2": [C.c_void_p, C.c_int64],

@@ -101,6 +101,15 @@ class Context:
         call("udmrg_probe_fp64_tflops", self.h, C.byref(v))
         return float(v.value)
 
+    def krylov_step_probe(self, n: int, step: int) -> dict:
+        """Device times and HBM bytes of one Krylov step's vector kernels at
+        `step` on random vectors of n doubles."""
+        ms, by, ran = (C.c_double * 5)(), (C.c_double * 5)(), C.c_int()
+        call("udmrg_probe_krylov_step", self.h, int(n), int(step), ms, by, C.byref(ran))
+        names = ("normalise", "alpha", "update", "reorth_pass1", "reorth_pass2")
+        return {"ms": dict(zip(names, list(ms))), "bytes": dict(zip(names, list(by))),
+                "second_pass_ran": bool(ran.value)}
+
     def close(self):
         if self.h:
             call("udmrg_ctx_destroy", self.h)

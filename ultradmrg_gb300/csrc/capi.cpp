@@ -951,6 +951,14 @@ int udmrg_probe_fp64_tflops(udmrg_ctx *c, double *tflops) {
   return guarded([&] { *tflops = probe_fp64_tflops(c->ctx); });
 }
 
+int udmrg_probe_krylov_step(udmrg_ctx *c, int64_t n, int step, double *ms, double *bytes,
+                            int *second_pass_ran) {
+  return guarded([&] {
+    UDMRG_REQUIRE(c && ms && bytes && second_pass_ran, "null argument");
+    krylov_step_probe(c->ctx, n, step, ms, bytes, second_pass_ran);
+  });
+}
+
 int udmrg_selftest_sym_eig(udmrg_ctx *c, int64_t nmat, const int32_t *n, const double *mats,
                            const int32_t *k, double *lam, double *vecs) {
   return guarded([&] {

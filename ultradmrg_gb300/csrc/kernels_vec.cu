@@ -5,6 +5,10 @@
 
 #include "vecops.hpp"
 
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 namespace udmrg {
 
 namespace {
@@ -580,6 +584,78 @@ void krylov_project(KrylovWork &k, bool second) {
                                                         second ? nullptr : k.gate, gate);
   UDMRG_CHECK_CUDA(cudaGetLastError());
   ctx.launches += 4;
+}
+
+namespace {
+// uniform deviates in [-w, w] from a counter hash (probe data only)
+__global__ void probe_fill_kernel(double *__restrict__ x, int64_t n, uint64_t seed, double w) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    uint64_t h = seed ^ (0x9E3779B97F4A7C15ull * (uint64_t)(i + 1));
+    h = (h ^ (h >> 30)) * 0xBF58476D1CE4E5B9ull;
+    h = (h ^ (h >> 27)) * 0x94D049BB133111EBull;
+    h ^= h >> 31;
+    x[i] = w * (2.0 * ((double)(h >> 11) * (1.0 / 9007199254740992.0)) - 1.0);
+  }
+}
+}  // namespace
+
+void krylov_step_probe(Ctx &ctx, int64_t n, int s, double ms[5], double bytes[5],
+                       int *second_ran) {
+  UDMRG_REQUIRE(n > 0 && s >= 1 && s + 2 <= kMaxVecs, "Krylov probe: 1 <= step <= 509, n > 0");
+  KrylovWork kw(ctx, n, false, s + 1);
+  // basis vectors 0 .. s + 1 with unit norm on average (random vectors of this
+  // length are nearly orthogonal), Y likewise; every nrm2 entry 1
+  std::vector<double *> basis(s + 2);
+  const double w = std::sqrt(3.0 / (double)n);
+  const int g = ew_grid(ctx, n);
+  for (int j = 0; j < s + 2; ++j) {
+    basis[j] = (double *)ctx.alloc(sizeof(double) * n);
+    probe_fill_kernel<<<g, 256, 0, ctx.stream>>>(basis[j], n, 1000003ull * (j + 1), w);
+    kw.push(j, basis[j]);
+  }
+  std::vector<double> ones(kMaxVecs + 2, 1.0);
+  UDMRG_CHECK_CUDA(cudaMemcpyAsync(kw.nrm2, ones.data(), ones.size() * sizeof(double),
+                                   cudaMemcpyHostToDevice, ctx.stream));
+  cudaEvent_t ev[6];
+  for (auto &e : ev) UDMRG_CHECK_CUDA(cudaEventCreate(&e));
+  double best[5];
+  for (int rep = 0; rep < 4; ++rep) {
+    probe_fill_kernel<<<g, 256, 0, ctx.stream>>>(kw.Y, n, 7ull + rep, w);
+    UDMRG_CHECK_CUDA(cudaMemcpyAsync(kw.step, &s, sizeof(int), cudaMemcpyHostToDevice, ctx.stream));
+    cudaEventRecord(ev[0], ctx.stream);
+    krylov_normalise(kw);
+    cudaEventRecord(ev[1], ctx.stream);
+    krylov_alpha(kw);
+    cudaEventRecord(ev[2], ctx.stream);
+    krylov_update(kw);
+    cudaEventRecord(ev[3], ctx.stream);
+    krylov_project(kw, false);
+    cudaEventRecord(ev[4], ctx.stream);
+    krylov_project(kw, true);
+    cudaEventRecord(ev[5], ctx.stream);
+    UDMRG_CHECK_CUDA(cudaEventSynchronize(ev[5]));
+    for (int i = 0; i < 5; ++i) {
+      float t = 0;
+      cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+      best[i] = rep == 0 ? t : std::min(best[i], (double)t);
+    }
+  }
+  double gate[2];
+  UDMRG_CHECK_CUDA(cudaMemcpy(gate, kw.gate, sizeof(gate), cudaMemcpyDeviceToHost));
+  for (auto &e : ev) cudaEventDestroy(e);
+  for (double *b : basis) ctx.free(b);
+  ctx.launches += (s + 2) + 4;  // the fills (the step's kernels count themselves)
+  const double v = 8.0 * (double)n;  // bytes of one vector
+  // normalise: Y read, X and v_s written; alpha: X, Y read; update: Y, X,
+  // v_{s-1} read, Y written; a projection pass: the multi-dot reads v_0..v_s
+  // and Y, the projection reads them again and writes Y
+  const double b[5] = {3 * v, 2 * v, 4 * v, (2.0 * (s + 1) + 3) * v, (2.0 * (s + 1) + 3) * v};
+  *second_ran = gate[1] < 0.5 * gate[0] ? 1 : 0;
+  for (int i = 0; i < 5; ++i) {
+    ms[i] = best[i];
+    bytes[i] = (i == 4 && !*second_ran) ? 0.0 : b[i];
+  }
 }
 
 void krylov_publish(KrylovWork &k) {

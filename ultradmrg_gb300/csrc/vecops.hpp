@@ -76,5 +76,12 @@ void krylov_update(KrylovWork &k);
 void krylov_project(KrylovWork &k, bool second);
 // hres = {Re alpha[s], nrm2[s+1], nrm2[s]}; step = s + 1
 void krylov_publish(KrylovWork &k);
+// Device times (best of four, ms) of one Krylov step's vector kernels at
+// step s on vectors of n doubles: ms[0] normalise, ms[1] alpha, ms[2]
+// three-term update, ms[3] the first projection pass (multi-dot and
+// projection against v_0 .. v_s), ms[4] the second (gated) pass; bytes[]
+// the HBM bytes each moves (0 for a second pass the gate skipped).
+void krylov_step_probe(Ctx &ctx, int64_t n, int s, double ms[5], double bytes[5],
+                       int *second_ran);
 
 }  // namespace udmrg
