@@ -241,3 +241,27 @@ def test_tdvp_ladder_quench_vs_oracle(ctx):
     for cp in out["checkpoints"]:
         assert cp["max_abs_dSz"] <= 1e-6, cp
         assert cp["overlap_err"] <= 1e-8, cp
+
+
+def test_tdvp_measured_driver_free_fermion(ctx):
+    """The TwoSiteFiniteTDVP driver with its measurements
+    (``ultradmrg_gb300.tdvp``): c^dag inserted at site 3 with the f string,
+    ten steps of dt = 0.01, c measured with the f string; every record
+    <GS| c_x(t) c^dag_3 |GS> e^{i E0 t} against the closed form (1e-10), the
+    records in the reference's order (step-major, sites (site0, x))."""
+    from ultradmrg_gb300 import tdvp as T
+    N, site0, dt, steps = 6, 3, 0.01, 10
+    e0, gs, mpo, pb, ops = _fermion_gs(ctx, N)
+    dmpo = [up(ctx, t) for t in mpo]
+    params = api.TDVPEvolveParams(dt, steps, 10, 16, 1e-10, 1e-12, 40)
+    res, log = T.two_site_finite_tdvp_measured(ctx, gs, dmpo, params, site0, ops["cdag"],
+                                               ops["c"], e0, ops["f"], ops["f"])
+    assert len(res) == (steps + 1) * N
+    assert len(log) == steps * (4 * N - 7)
+    for k in range(steps + 1):
+        for x in range(N):
+            r = res[k * N + x]
+            assert r.sites == (site0, x) and abs(r.times[1] - k * dt) < 1e-15
+            assert abs(r.avg - free_fermion_green(k * dt, N, site0, x)) <= 1e-10, (k, x)
+    for t in dmpo:
+        t.close()
