@@ -9,7 +9,7 @@
 
 Environments and MPS tensors stay in lists instead of on disk.  Operator
 insertion and the correlation measurements of ``TwoSiteFiniteTDVP`` are left
-to the caller (the tests), as in the device interface.
+to the caller (the tests compose them from ``measure.py``).
 """
 from __future__ import annotations
 
